@@ -1,0 +1,185 @@
+/*
+ * isg.h — C ABI of libisinggb, the GB300 (sm_103a) checkerboard Monte Carlo
+ * parallel-tempering engine for periodic cubic (and square) lattices.
+ *
+ * This is the drop-in boundary for the GPU backend of faulknco/ising-rs
+ * (src/cuda/*.rs + src/parallel_tempering.rs).  Each entry point names the
+ * reference interface it replaces.  Conventions:
+ *
+ *   - Every function returns an int status: ISG_OK (0) or a negative ISG_ERR_*
+ *     code; isg_last_error() returns a thread-local text for the last failure.
+ *     (Reference: anyhow::Result everywhere, e.g. src/cuda/lattice_gpu.rs:22,85.)
+ *   - Host arrays are caller-owned; device memory is owned by the handle and is
+ *     released by the matching *_destroy (reference: RAII CudaSlice,
+ *     src/cuda/lattice_gpu.rs:9-19).
+ *   - A handle is not thread-safe; all of its work is ordered on one CUDA
+ *     stream (its own, or the caller's via *_set_stream).
+ *   - Replica order in every per-replica array is size-major: index
+ *     s*replicas + r for size index s and replica r.
+ *
+ * Random numbers (one definition shared by the kernels and any replay):
+ *   Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), key = {lo32(seed),
+ *   hi32(seed)}, counter = {c0, c1, c2, c3} with
+ *     c1 = stream uid: (L << 16) | replica  for a lattice replica,
+ *                      (L << 16) | 0xFFFF   for the exchange stream of size L,
+ *     c3 = (tag << 24) | (colour << 16) | (hi32(step) & 0xFFFF),
+ *     c2 = lo32(step),
+ *   and tag / c0 / step as listed with the ISG_TAG_* constants below.
+ */
+#ifndef ISG_H
+#define ISG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ISG_VERSION 100
+
+#define ISG_OK               0
+#define ISG_ERR_ARG         -1  /* bad argument (size, count, pointer)             */
+#define ISG_ERR_CUDA        -2  /* a CUDA runtime call failed                       */
+#define ISG_ERR_TIMEOUT     -3  /* a bounded device-side wait gave up               */
+#define ISG_ERR_UNSUPPORTED -4  /* e.g. odd lattice size (no checkerboard under PBC) */
+#define ISG_ERR_STATE       -5  /* call order (temperatures not set, ...)           */
+
+/* Philox stream tags (c3 bits 24..31).
+ *  INIT : hot start.  c0 = natural site index / 4, step = 0; word (site & 3);
+ *         spin = -1 if the word's top bit is set, else +1.
+ *  ISING: Metropolis half-sweep.  c0 = colour index / 4 (colour index of
+ *         site (x,y,z) = (z*L*L + y*L + x) >> 1), step = global sweep number,
+ *         colour = 0 (x+y+z even) or 1; word (colour index & 3) is u, and the
+ *         flip is accepted iff u <= threshold[own_down*8 + n_down_neighbours]
+ *         with threshold = 0xFFFFFFFF for dE <= 0, else
+ *         max(floor(exp(-beta*dE) * 2^32), 1) - 1  (FP64 on the host).
+ *  EXCH : replica exchange.  c0 = lower temperature index of the pair,
+ *         c1 = exchange uid, step = exchange count of that size;
+ *         u = ((w0 << 32 | w1) >> 11) * 2^-53.
+ *  CINIT/CMETRO: continuous spins, c0 = natural site index (CINIT) or colour
+ *         index (CMETRO), one Philox call per site.
+ */
+#define ISG_TAG_INIT   0x01u
+#define ISG_TAG_ISING  0x02u
+#define ISG_TAG_EXCH   0x03u
+#define ISG_TAG_CINIT  0x04u
+#define ISG_TAG_CMETRO 0x05u
+
+const char* isg_last_error(void);
+int isg_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Ising batch: every lattice size of a run x `replicas` replicas, int8 spins */
+/* ------------------------------------------------------------------------ */
+typedef struct isg_ising isg_ising;
+
+/* Replaces LatticeGpu::new(n, seed) (src/cuda/lattice_gpu.rs:22-65) for all
+ * (size, replica) pairs of a run at once, and the replica set built in
+ * run_ising_fss (src/bin/gpu_fss.rs:188-193).  dim = 3 (cubic, the reference
+ * path) or 2 (square).  Sizes must be even and 2..1024.  Spins start hot from
+ * the ISG_TAG_INIT stream (the reference draws them unseeded,
+ * src/cuda/lattice_gpu.rs:38-40). */
+int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replicas,
+                     int dim, uint64_t seed);
+int isg_ising_destroy(isg_ising* h);
+
+/* Work on the caller's CUDA stream (a cudaStream_t passed as void*); NULL
+ * restores the handle's own stream. */
+int isg_ising_set_stream(isg_ising* h, void* cuda_stream);
+
+/* Temperature grid per size (temps[s*replicas + t], slot t), coupling J and
+ * field h.  Replaces the beta/J/h arguments of LatticeGpu::step
+ * (src/cuda/lattice_gpu.rs:85) and linspace_temperatures
+ * (src/parallel_tempering.rs:39-46) output handling in gpu_fss.  Resets the
+ * replica->temperature maps to the identity. */
+int isg_ising_set_temperatures(isg_ising* h, const double* temps, double J, double hfield);
+
+/* n_sweeps full sweeps (colour 0 then colour 1) of every replica at the
+ * temperature its r2t slot names; asynchronous.  Replaces LatticeGpu::step /
+ * warm_up (src/cuda/lattice_gpu.rs:85-107,184-189). */
+int isg_ising_step(isg_ising* h, int64_t n_sweeps);
+
+/* Exact integer observables of every replica, synchronous:
+ * bond_sum = sum over bonds s_i s_j, magnetisation = sum s_i, so that
+ * E = -J*bond_sum - h*magnetisation.  Replaces measure_gpu / energy_gpu
+ * (src/cuda/lattice_gpu.rs:116-181; reduce_kernel.cu:7-66).  The energies
+ * are kept on the device for isg_ising_exchange. */
+int isg_ising_measure(isg_ising* h, int64_t* bond_sum, int64_t* magnetisation);
+
+/* One even (parity 0) or odd (parity 1) replica-exchange pass per size using
+ * the energies of the last measurement; swaps temperature labels only.
+ * parity < 0 uses the size's exchange count.  accepted[s] (may be NULL)
+ * receives the swaps accepted for size s.  Synchronous.  Replaces
+ * replica_exchange (src/parallel_tempering.rs:5-36). */
+int isg_ising_exchange(isg_ising* h, int parity, int64_t* accepted);
+
+/* Replica -> temperature-slot map (size-major, values 0..replicas-1). */
+int isg_ising_get_r2t(isg_ising* h, int32_t* r2t);
+int isg_ising_set_r2t(isg_ising* h, const int32_t* r2t);
+
+/* Natural-layout spins (idx = z*L*L + y*L + x) of one replica.  Replaces
+ * LatticeGpu::get_spins (src/cuda/lattice_gpu.rs:110-112). */
+int isg_ising_get_spins(isg_ising* h, int size_index, int replica, int8_t* out);
+int isg_ising_set_spins(isg_ising* h, int size_index, int replica, const int8_t* in);
+
+/* Parallel-tempering sampling: n_sweeps sweeps continuing the sampling phase;
+ * after sampling sweep k (0-based, counted since the last reset) the
+ * observables are measured if (k+1) % measure_every == 0 and an exchange pass
+ * runs if (k+1) % exchange_every == 0, parity = exchange count % 2; each
+ * measured sweep appends, per replica in replica order, one record
+ * (temperature slot, bond_sum, magnetisation).  Records fill the caller's
+ * arrays (max_records rows of n_sizes*replicas entries each); *n_records
+ * returns the rows written.  The sweep/measure/exchange cycle runs as a CUDA
+ * graph.  With all three record pointers NULL the call is asynchronous and
+ * the records stay in a device ring (the newest ring rows survive) for
+ * isg_ising_read_records.  Replaces the sampling loop of run_ising_fss
+ * (src/bin/gpu_fss.rs:235-286). */
+int isg_ising_pt_run(isg_ising* h, int64_t n_sweeps, int exchange_every, int measure_every,
+                     int32_t* tslot_rec, int64_t* bond_rec, int64_t* mag_rec,
+                     int64_t max_records, int64_t* n_records);
+
+/* Copy the records still held in the device ring (at most max_records, the
+ * newest ones) to the caller's arrays; synchronous. */
+int isg_ising_read_records(isg_ising* h, int32_t* tslot_rec, int64_t* bond_rec, int64_t* mag_rec,
+                           int64_t max_records, int64_t* n_records);
+
+/* Zero the sampling-phase counters (sampling sweep, exchange counts, accepted
+ * counts); called between warmup and sampling. */
+int isg_ising_reset_sampling(isg_ising* h);
+
+/* Accepted swaps so far per size (sum over pairs). */
+int isg_ising_get_accepted(isg_ising* h, int64_t* accepted);
+
+/* Global sweep counter (warmup + sampling), the Philox step of ISG_TAG_ISING. */
+int isg_ising_get_sweep(isg_ising* h, uint64_t* sweep);
+
+int isg_ising_sync(isg_ising* h);
+
+/* Launch shape of the half-sweep kernel: threads per block and blocks per SM
+ * (0 = occupancy maximum).  Results never depend on it. */
+int isg_ising_set_launch(isg_ising* h, int threads, int blocks_per_sm);
+/* Time every supported launch shape on a scratch copy of the lattices and
+ * keep the fastest.  best[0..1] (may be NULL) receives threads, blocks/SM. */
+int isg_ising_autotune(isg_ising* h, int* best);
+
+/* Mean device time (ms, CUDA events on the handle's stream) of one half-sweep
+ * launch over n_launches launches of the current batch (colours alternate). */
+int isg_ising_time_halfsweep(isg_ising* h, int n_launches, float* avg_ms);
+
+/* Sites updated by one half-sweep launch (all sizes and replicas). */
+int isg_ising_sites_per_halfsweep(isg_ising* h, int64_t* sites);
+
+/* ------------------------------------------------------------------------ */
+/* Statistics used by the drop-in driver                                     */
+/* ------------------------------------------------------------------------ */
+
+/* Leave-one-block-out jackknife of a (e, m) series exactly as
+ * jackknife_observables (src/bin/gpu_fss.rs:327-412).  out[12] =
+ * E, E_err, M, M_err, M2, M2_err, M4, M4_err, Cv, Cv_err, chi, chi_err. */
+int isg_jackknife(const double* e, const double* m, int64_t n, double beta, double n_sites,
+                  int n_blocks, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ISG_H */

@@ -1,0 +1,496 @@
+"""ising-rs_gb300 — Python host mirror of the reference's GPU backend interface.
+
+Thin ctypes layer over libisinggb (include/isg.h), the sm_103a engine.  It
+mirrors the names, argument meaning and error behaviour of faulknco/ising-rs's
+backend for the checkerboard PT path:
+
+  LatticeGpu            src/cuda/lattice_gpu.rs:9-189  (new/step/warm_up/
+                        measure_gpu/energy_gpu/get_spins)
+  ContinuousGpuLattice  src/cuda/gpu_lattice_continuous.rs:9-245
+  linspace_temperatures src/parallel_tempering.rs:39-46
+  jackknife_observables src/bin/gpu_fss.rs:327-412
+  IsingBatch / ContinuousBatch: every (size, replica) lattice of a run in one
+  handle (the GB300 replacement of the reference's Vec<LatticeGpu>).
+
+Every failure raises IsingError (the reference returns anyhow::Result and its
+drivers panic).  There is no CPU fallback: if the compiled library is missing
+the import of any class fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+_LIB = None
+
+ISG_OK = 0
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "device timeout", -4: "unsupported",
+          -5: "bad call order"}
+
+
+class IsingError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{ERRORS.get(status, 'error')} ({status}): {message}")
+        self.status = status
+
+
+def library_path() -> Path:
+    return _PKG / "lib" / "libisinggb.so"
+
+
+def lib():
+    """Load libisinggb; raises if it has not been built (no fallback)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not path.exists():
+        raise IsingError(-4, f"{path} not built; run python ising-rs_gb300/build.py")
+    L = C.CDLL(str(path))
+    _declare(L)
+    _LIB = L
+    return L
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _declare(L):
+    vp, i32, i64, u64, dbl = C.c_void_p, C.c_int, C.c_int64, C.c_uint64, C.c_double
+    L.isg_last_error.restype = C.c_char_p
+    L.isg_version.restype = i32
+    sig = {
+        "isg_ising_create": [C.POINTER(vp), vp, i32, i32, i32, u64],
+        "isg_ising_destroy": [vp],
+        "isg_ising_set_stream": [vp, vp],
+        "isg_ising_set_temperatures": [vp, vp, dbl, dbl],
+        "isg_ising_step": [vp, i64],
+        "isg_ising_measure": [vp, vp, vp],
+        "isg_ising_exchange": [vp, i32, vp],
+        "isg_ising_get_r2t": [vp, vp],
+        "isg_ising_set_r2t": [vp, vp],
+        "isg_ising_get_spins": [vp, i32, i32, vp],
+        "isg_ising_set_spins": [vp, i32, i32, vp],
+        "isg_ising_pt_run": [vp, i64, i32, i32, vp, vp, vp, i64, vp],
+        "isg_ising_read_records": [vp, vp, vp, vp, i64, vp],
+        "isg_ising_reset_sampling": [vp],
+        "isg_ising_get_accepted": [vp, vp],
+        "isg_ising_get_sweep": [vp, vp],
+        "isg_ising_sync": [vp],
+        "isg_ising_set_launch": [vp, i32, i32],
+        "isg_ising_autotune": [vp, vp],
+        "isg_ising_time_halfsweep": [vp, i32, vp],
+        "isg_ising_sites_per_halfsweep": [vp, vp],
+        "isg_jackknife": [vp, vp, i64, dbl, dbl, i32, vp],
+        "isg_cont_create": [C.POINTER(vp), vp, i32, i32, i32, u64],
+        "isg_cont_destroy": [vp],
+        "isg_cont_set_stream": [vp, vp],
+        "isg_cont_set_temperatures": [vp, vp, dbl],
+        "isg_cont_sweep": [vp, i64, dbl, i32],
+        "isg_cont_overrelax": [vp, i32],
+        "isg_cont_metropolis": [vp, i32, dbl],
+        "isg_cont_normalize": [vp],
+        "isg_cont_measure": [vp, vp, vp, vp],
+        "isg_cont_exchange": [vp, i32, vp],
+        "isg_cont_pt_run": [vp, i64, i32, i32, dbl, i32, i32, vp, vp, vp, vp, i64, vp],
+        "isg_cont_reset_sampling": [vp],
+        "isg_cont_get_r2t": [vp, vp],
+        "isg_cont_get_spins": [vp, i32, i32, vp],
+        "isg_cont_set_spins": [vp, i32, i32, vp],
+        "isg_cont_get_accepted": [vp, vp],
+        "isg_cont_get_metro_accepted": [vp, vp],
+        "isg_cont_sync": [vp],
+        "isg_cont_time_kernels": [vp, i32, vp],
+        "isg_cont_sites_per_sweep": [vp, vp],
+    }
+    for name, args in sig.items():
+        if hasattr(L, name):
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = i32
+
+
+def _check(status: int) -> None:
+    if status != ISG_OK:
+        raise IsingError(status, lib().isg_last_error().decode(errors="replace"))
+
+
+def linspace_temperatures(t_min: float, t_max: float, n: int) -> list[float]:
+    """src/parallel_tempering.rs:39-46 (same FP64 expression)."""
+    if n == 1:
+        return [t_min]
+    return [t_min + (t_max - t_min) * i / (n - 1) for i in range(n)]
+
+
+def jackknife_observables(e, m, beta: float, n3: float, n_blocks: int) -> np.ndarray:
+    """src/bin/gpu_fss.rs:327-412 via isg_jackknife: [E, E_err, M, M_err, M2, M2_err,
+    M4, M4_err, Cv, Cv_err, chi, chi_err]."""
+    e = np.ascontiguousarray(e, np.float64)
+    m = np.ascontiguousarray(m, np.float64)
+    out = np.zeros(12, np.float64)
+    _check(lib().isg_jackknife(_ptr(e), _ptr(m), len(e), beta, n3, n_blocks, _ptr(out)))
+    return out
+
+
+def binder(m2: float, m4: float) -> float:
+    """U4 = 1 - <m^4> / (3 <m^2>^2) (analysis/scripts/ising_stats.py:66)."""
+    if m2 <= 1e-15:
+        return 0.0
+    return 1.0 - m4 / (3.0 * m2 * m2)
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return int(stream.cuda_stream)
+    return int(stream)
+
+
+class IsingBatch:
+    """Every (size, replica) int8 Ising lattice of a run on one GPU."""
+
+    def __init__(self, sizes, replicas: int, seed: int = 42, dim: int = 3):
+        self.sizes = [int(s) for s in sizes]
+        self.replicas = int(replicas)
+        self.dim = int(dim)
+        self.seed = int(seed)
+        arr = np.ascontiguousarray(self.sizes, np.int32)
+        h = C.c_void_p()
+        _check(lib().isg_ising_create(C.byref(h), _ptr(arr), len(self.sizes), self.replicas,
+                                      self.dim, self.seed))
+        self._h = h
+        self.temps = None
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            lib().isg_ising_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n_total(self) -> int:
+        return len(self.sizes) * self.replicas
+
+    def nsites(self, s: int) -> int:
+        return self.sizes[s] ** self.dim
+
+    def set_stream(self, stream) -> None:
+        h = _stream_handle(stream)
+        _check(lib().isg_ising_set_stream(self._h, C.c_void_p(h) if h else None))
+
+    def set_temperatures(self, temps, J: float = 1.0, h: float = 0.0) -> None:
+        t = np.asarray(temps, np.float64)
+        if t.ndim == 1 and len(t) == self.replicas:
+            t = np.tile(t, len(self.sizes))
+        t = np.ascontiguousarray(t.reshape(-1), np.float64)
+        if len(t) != self.n_total:
+            raise IsingError(-1, "need one temperature per (size, slot)")
+        _check(lib().isg_ising_set_temperatures(self._h, _ptr(t), float(J), float(h)))
+        self.temps = t.reshape(len(self.sizes), self.replicas)
+        self.J, self.h = float(J), float(h)
+
+    def step(self, n_sweeps: int = 1) -> None:
+        _check(lib().isg_ising_step(self._h, int(n_sweeps)))
+
+    def measure(self) -> tuple[np.ndarray, np.ndarray]:
+        b = np.zeros(self.n_total, np.int64)
+        m = np.zeros(self.n_total, np.int64)
+        _check(lib().isg_ising_measure(self._h, _ptr(b), _ptr(m)))
+        return b, m
+
+    def exchange(self, parity: int = -1) -> np.ndarray:
+        acc = np.zeros(len(self.sizes), np.int64)
+        _check(lib().isg_ising_exchange(self._h, int(parity), _ptr(acc)))
+        return acc
+
+    def r2t(self) -> np.ndarray:
+        out = np.zeros(self.n_total, np.int32)
+        _check(lib().isg_ising_get_r2t(self._h, _ptr(out)))
+        return out
+
+    def set_r2t(self, r2t) -> None:
+        a = np.ascontiguousarray(r2t, np.int32)
+        _check(lib().isg_ising_set_r2t(self._h, _ptr(a)))
+
+    def get_spins(self, s: int, r: int) -> np.ndarray:
+        out = np.zeros(self.nsites(s), np.int8)
+        _check(lib().isg_ising_get_spins(self._h, s, r, _ptr(out)))
+        return out
+
+    def set_spins(self, s: int, r: int, spins) -> None:
+        a = np.ascontiguousarray(spins, np.int8).reshape(-1)
+        if len(a) != self.nsites(s):
+            raise IsingError(-1, "wrong number of spins")
+        _check(lib().isg_ising_set_spins(self._h, s, r, _ptr(a)))
+
+    def reset_sampling(self) -> None:
+        _check(lib().isg_ising_reset_sampling(self._h))
+
+    def pt_run(self, n_sweeps: int, exchange_every: int, measure_every: int):
+        """Returns (slot, bond, mag) arrays of shape (records, n_total)."""
+        rows = n_sweeps // measure_every + 1
+        t = np.zeros((rows, self.n_total), np.int32)
+        b = np.zeros((rows, self.n_total), np.int64)
+        m = np.zeros((rows, self.n_total), np.int64)
+        n = C.c_int64()
+        _check(lib().isg_ising_pt_run(self._h, int(n_sweeps), int(exchange_every),
+                                      int(measure_every), _ptr(t), _ptr(b), _ptr(m), rows,
+                                      C.byref(n)))
+        k = n.value
+        return t[:k], b[:k], m[:k]
+
+    def pt_launch(self, n_sweeps: int, exchange_every: int, measure_every: int) -> None:
+        """Asynchronous PT sweeps; records stay on the device (read_records)."""
+        _check(lib().isg_ising_pt_run(self._h, int(n_sweeps), int(exchange_every),
+                                      int(measure_every), None, None, None, 0, None))
+
+    def read_records(self, max_records: int):
+        t = np.zeros((max_records, self.n_total), np.int32)
+        b = np.zeros((max_records, self.n_total), np.int64)
+        m = np.zeros((max_records, self.n_total), np.int64)
+        n = C.c_int64()
+        _check(lib().isg_ising_read_records(self._h, _ptr(t), _ptr(b), _ptr(m), int(max_records),
+                                            C.byref(n)))
+        k = n.value
+        return t[:k], b[:k], m[:k]
+
+    def accepted(self) -> np.ndarray:
+        out = np.zeros(len(self.sizes), np.int64)
+        _check(lib().isg_ising_get_accepted(self._h, _ptr(out)))
+        return out
+
+    def sweep_counter(self) -> int:
+        v = C.c_uint64()
+        _check(lib().isg_ising_get_sweep(self._h, C.byref(v)))
+        return v.value
+
+    def sync(self) -> None:
+        _check(lib().isg_ising_sync(self._h))
+
+    def set_launch(self, threads: int, blocks_per_sm: int = 0) -> None:
+        _check(lib().isg_ising_set_launch(self._h, threads, blocks_per_sm))
+
+    def autotune(self) -> tuple[int, int]:
+        best = np.zeros(2, np.int32)
+        _check(lib().isg_ising_autotune(self._h, _ptr(best)))
+        return int(best[0]), int(best[1])
+
+    def time_halfsweep(self, n_launches: int = 20) -> float:
+        v = C.c_float()
+        _check(lib().isg_ising_time_halfsweep(self._h, n_launches, C.byref(v)))
+        return v.value
+
+    def sites_per_halfsweep(self) -> int:
+        v = C.c_int64()
+        _check(lib().isg_ising_sites_per_halfsweep(self._h, C.byref(v)))
+        return v.value
+
+
+class LatticeGpu:
+    """Mirror of LatticeGpu (src/cuda/lattice_gpu.rs:9-189): one cubic replica.
+
+    `step(beta, j, h)` sweeps once (colour 0 then colour 1); `measure_gpu(j)`
+    returns (E/N^3, |M|/N^3) synchronously; `energy_gpu(j)` the total energy.
+    Spins start hot from the seeded Philox stream (the reference's are
+    unseeded, lattice_gpu.rs:38-40)."""
+
+    def __init__(self, n: int, seed: int):
+        self.n = int(n)
+        self._b = IsingBatch([self.n], 1, seed=seed, dim=3)
+        self._key = None
+
+    def _set(self, beta: float, j: float, h: float) -> None:
+        key = (float(beta), float(j), float(h))
+        if key != self._key:
+            self._b.set_temperatures([1.0 / key[0]], J=key[1], h=key[2])
+            self._key = key
+
+    def step(self, beta: float, j: float, h: float) -> None:
+        self._set(beta, j, h)
+        self._b.step(1)
+
+    def warm_up(self, beta: float, j: float, h: float, sweeps: int) -> None:
+        self._set(beta, j, h)
+        self._b.step(sweeps)
+
+    def measure_gpu(self, j: float) -> tuple[float, float]:
+        # The reference reduction sums -J s_i s_j only (reduce_kernel.cu:52-56):
+        # the field term is not part of the measured energy.
+        b, m = self._b.measure()
+        n3 = float(self.n) ** 3
+        return -float(j) * float(b[0]) / n3, abs(float(m[0])) / n3
+
+    def energy_gpu(self, j: float) -> float:
+        b, _ = self._b.measure()
+        return -float(j) * float(b[0])
+
+    def get_spins(self) -> np.ndarray:
+        return self._b.get_spins(0, 0)
+
+
+class ContinuousBatch:
+    """Every (size, replica) O(n) lattice (n_comp 2 = XY, 3 = Heisenberg)."""
+
+    def __init__(self, sizes, replicas: int, n_comp: int, seed: int = 42):
+        self.sizes = [int(s) for s in sizes]
+        self.replicas = int(replicas)
+        self.n_comp = int(n_comp)
+        self.seed = int(seed)
+        arr = np.ascontiguousarray(self.sizes, np.int32)
+        h = C.c_void_p()
+        _check(lib().isg_cont_create(C.byref(h), _ptr(arr), len(self.sizes), self.replicas,
+                                     self.n_comp, self.seed))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            lib().isg_cont_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n_total(self) -> int:
+        return len(self.sizes) * self.replicas
+
+    def nsites(self, s: int) -> int:
+        return self.sizes[s] ** 3
+
+    def set_stream(self, stream) -> None:
+        h = _stream_handle(stream)
+        _check(lib().isg_cont_set_stream(self._h, C.c_void_p(h) if h else None))
+
+    def set_temperatures(self, temps, J: float = 1.0) -> None:
+        t = np.asarray(temps, np.float64)
+        if t.ndim == 1 and len(t) == self.replicas:
+            t = np.tile(t, len(self.sizes))
+        t = np.ascontiguousarray(t.reshape(-1), np.float64)
+        _check(lib().isg_cont_set_temperatures(self._h, _ptr(t), float(J)))
+        self.temps = t.reshape(len(self.sizes), self.replicas)
+        self.J = float(J)
+
+    def sweep(self, n_sweeps: int = 1, delta: float = 0.5, n_overrelax: int = 5) -> None:
+        _check(lib().isg_cont_sweep(self._h, int(n_sweeps), float(delta), int(n_overrelax)))
+
+    def overrelax(self, colour: int) -> None:
+        _check(lib().isg_cont_overrelax(self._h, int(colour)))
+
+    def metropolis(self, colour: int, delta: float) -> None:
+        _check(lib().isg_cont_metropolis(self._h, int(colour), float(delta)))
+
+    def normalize(self) -> None:
+        _check(lib().isg_cont_normalize(self._h))
+
+    def measure(self):
+        """Returns (E [n_total], M [n_total, 3], bond sums [n_total, 6]):
+        bond sums = sum_i S_i.S_{i+a} (a = x,y,z) then sum_i (S_i x S_{i+a})_z."""
+        e = np.zeros(self.n_total, np.float64)
+        m = np.zeros((self.n_total, 3), np.float64)
+        hb = np.zeros((self.n_total, 6), np.float64)
+        _check(lib().isg_cont_measure(self._h, _ptr(e), _ptr(m), _ptr(hb)))
+        return e, m, hb
+
+    def exchange(self, parity: int = -1) -> np.ndarray:
+        acc = np.zeros(len(self.sizes), np.int64)
+        _check(lib().isg_cont_exchange(self._h, int(parity), _ptr(acc)))
+        return acc
+
+    def reset_sampling(self) -> None:
+        _check(lib().isg_cont_reset_sampling(self._h))
+
+    def pt_run(self, n_sweeps: int, exchange_every: int, measure_every: int, delta: float = 0.5,
+               n_overrelax: int = 5, renorm_every: int = 100):
+        """Returns (slot, E, M[...,3], bond sums[...,6]) per record."""
+        rows = n_sweeps // measure_every + 1
+        nt = self.n_total
+        t = np.zeros((rows, nt), np.int32)
+        e = np.zeros((rows, nt), np.float64)
+        m = np.zeros((rows, nt, 3), np.float64)
+        hb = np.zeros((rows, nt, 6), np.float64)
+        n = C.c_int64()
+        _check(lib().isg_cont_pt_run(self._h, int(n_sweeps), int(exchange_every),
+                                     int(measure_every), float(delta), int(n_overrelax),
+                                     int(renorm_every), _ptr(t), _ptr(e), _ptr(m), _ptr(hb), rows,
+                                     C.byref(n)))
+        k = n.value
+        return t[:k], e[:k], m[:k], hb[:k]
+
+    def r2t(self) -> np.ndarray:
+        out = np.zeros(self.n_total, np.int32)
+        _check(lib().isg_cont_get_r2t(self._h, _ptr(out)))
+        return out
+
+    def get_spins(self, s: int, r: int) -> np.ndarray:
+        out = np.zeros(self.nsites(s) * self.n_comp, np.float32)
+        _check(lib().isg_cont_get_spins(self._h, s, r, _ptr(out)))
+        return out.reshape(-1, self.n_comp)
+
+    def set_spins(self, s: int, r: int, spins) -> None:
+        a = np.ascontiguousarray(spins, np.float32).reshape(-1)
+        _check(lib().isg_cont_set_spins(self._h, s, r, _ptr(a)))
+
+    def accepted(self) -> np.ndarray:
+        out = np.zeros(len(self.sizes), np.int64)
+        _check(lib().isg_cont_get_accepted(self._h, _ptr(out)))
+        return out
+
+    def metropolis_accepted(self) -> np.ndarray:
+        out = np.zeros(self.n_total, np.int64)
+        _check(lib().isg_cont_get_metro_accepted(self._h, _ptr(out)))
+        return out
+
+    def sync(self) -> None:
+        _check(lib().isg_cont_sync(self._h))
+
+    def time_kernels(self, n: int = 10) -> np.ndarray:
+        out = np.zeros(3, np.float32)
+        _check(lib().isg_cont_time_kernels(self._h, int(n), _ptr(out)))
+        return out
+
+    def sites_per_sweep(self) -> int:
+        v = C.c_int64()
+        _check(lib().isg_cont_sites_per_sweep(self._h, C.byref(v)))
+        return v.value
+
+
+class ContinuousGpuLattice:
+    """Mirror of ContinuousGpuLattice (src/cuda/gpu_lattice_continuous.rs:9-245).
+
+    `sweep(beta, j, delta, n_overrelax)` runs n_overrelax overrelaxation sweeps
+    then one Metropolis sweep (the reference GPU order, :112-173);
+    `measure_gpu(j)` returns (E_total, mx, my, mz)."""
+
+    def __init__(self, n: int, n_comp: int, seed: int):
+        self.n, self.n_comp = int(n), int(n_comp)
+        self._b = ContinuousBatch([self.n], 1, self.n_comp, seed=seed)
+        self._key = None
+
+    def sweep(self, beta: float, j: float, delta: float, n_overrelax: int) -> None:
+        key = (float(beta), float(j))
+        if key != self._key:
+            self._b.set_temperatures([1.0 / key[0]], J=key[1])
+            self._key = key
+        self._b.sweep(1, delta, n_overrelax)
+
+    def measure_gpu(self, j: float):
+        e, m, _ = self._b.measure()
+        scale = float(j) / (self._key[1] if self._key else 1.0)
+        return float(e[0]) * scale, float(m[0, 0]), float(m[0, 1]), float(m[0, 2])
+
+    def measure_raw(self):
+        return self.measure_gpu(1.0)

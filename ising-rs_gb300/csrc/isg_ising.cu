@@ -1,0 +1,1205 @@
+// isg_ising.cu — batched checkerboard Metropolis for int8 Ising spins on
+// periodic cubic (dim 3) or square (dim 2) lattices, fused integer E/M
+// reductions, device-side replica exchange and the PT cycle as a CUDA graph.
+//
+// Reference path being replaced (faulknco/ising-rs):
+//   src/cuda/kernels.cu:9-56        metropolis_sweep_kernel (one launch per
+//                                    replica per colour, curandState per site)
+//   src/cuda/reduce_kernel.cu:7-66  reduce_mag_ising / reduce_energy_ising
+//   src/cuda/lattice_gpu.rs:22-189  LatticeGpu (owner of one replica)
+//   src/parallel_tempering.rs:5-36  replica_exchange (host, Xoshiro256++)
+//   src/bin/gpu_fss.rs:186-286      the PT sampling loop
+//
+// Layout in HBM.  Every (size, replica) lattice is stored colour-split: plane
+// c holds the L^dim/2 sites with (x+y+z)&1 == c at colour index
+// (z*L*L + y*L + x) >> 1, so one 32-bit word carries 4 consecutive same-colour
+// sites of a row.  Planes of one size are contiguous ([R][2][L^dim/2] bytes).
+//
+// Half-sweep kernels (one launch covers every size and replica):
+//  * word kernel — for L in {8..256}, a power of two whose row (L/8 words)
+//    divides a warp.  One lane updates one word (4 sites) per warp task of 32
+//    words; the x-neighbour word shifted by one byte comes from the row's
+//    other lanes through __shfl_sync + funnel shift; neighbour counts are
+//    byte-SIMD sums of (word & 0x02020202); the acceptance threshold comes
+//    from a 16-entry table of the replica's temperature in shared memory.
+//    Warps own contiguous task ranges (persistent grid) so a warp changes
+//    replica rarely and flushes its integer E/M partials with one 64-bit
+//    atomic per replica change.
+//  * site kernel — any other even L: one thread per site, same stream and
+//    update rule.
+// Both produce identical bits for the same state (the random stream is
+// defined per site, not per thread).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "isg_common.cuh"
+
+namespace isg {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+    g_last_error = std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e);
+    return ISG_ERR_CUDA;
+}
+
+constexpr int kMaxClasses = 16;
+constexpr int kMaxThreads = 512;
+constexpr int kMaxReplicas = 1024;
+
+struct IsingClass {
+    int L;
+    int R;
+    int word_path;
+    int log2L;          // word path only
+    int log2_row_words; // word path only (row_words = L/8)
+    uint32_t plane_sites;     // L^dim / 2
+    uint32_t tasks_per_plane; // word path: plane_sites / 128 (a power of two)
+    int log2_tpp;             // word path: log2(tasks_per_plane)
+    int rep_base;             // global replica index of replica 0 (also slot base)
+    int64_t spin_off;         // byte offset of replica 0 colour 0
+    int64_t task_base;        // word path: first warp task
+    int64_t task_end;
+    int64_t site_base;        // site path: first site (over colour planes)
+    int64_t site_end;
+};
+
+struct IsingParams {
+    int8_t* spins;
+    const uint32_t* thr;            // [slots][16]
+    const int32_t* r2t;             // [replicas]
+    unsigned long long* acc;        // [replicas][2] bond, mag
+    const unsigned long long* ctrl; // ctrl[0] = global sweep base
+    uint64_t seed;
+    int n_classes;
+    int64_t total_tasks;
+    int64_t total_sites;
+    IsingClass cls[kMaxClasses];
+};
+
+// ---------------------------------------------------------------- kernels
+
+__device__ __forceinline__ void flush_acc(unsigned long long* acc, int rep, int b, int m,
+                                          int lane) {
+    const int sb = __reduce_add_sync(ISG_FULL_MASK, b);
+    const int sm = __reduce_add_sync(ISG_FULL_MASK, m);
+    if (lane == 0) {
+        atomicAdd(&acc[2 * rep], (unsigned long long)(long long)sb);
+        atomicAdd(&acc[2 * rep + 1], (unsigned long long)(long long)sm);
+    }
+}
+
+// MODE 0: update; 1: update then accumulate bond/mag of the new state;
+// 2: accumulate only (no update).
+template <int DIM, int MODE>
+__global__ void __launch_bounds__(kMaxThreads)
+    k_ising_words(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
+    __shared__ uint32_t s_thr[kMaxThreads / 32][16];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    int64_t t = gw * P.total_tasks / nwarps;
+    const int64_t t_end = (gw + 1) * P.total_tasks / nwarps;
+    if (t >= t_end) return;
+
+    const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
+    const uint32_t c2 = (uint32_t)sweep;
+    const uint32_t c3 = counter_word3(ISG_TAG_ISING, (uint32_t)colour, sweep);
+    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    const uint32_t M2 = 0x02020202u;
+
+    int ci = 0;
+    while (P.cls[ci].task_end <= t) ++ci;
+    int cur_rep = -1;
+    int accb = 0, accm = 0;
+    uint32_t* own = nullptr;
+    const uint32_t* oth = nullptr;
+    uint32_t uid = 0;
+    const char* tb = reinterpret_cast<const char*>(s_thr[wib]);
+
+    for (; t < t_end; ++t) {
+        while (P.cls[ci].task_end <= t) ++ci;
+        const IsingClass& C = P.cls[ci];
+        const int64_t lt = t - C.task_base;
+        const int r = (int)(lt >> C.log2_tpp);
+        const uint32_t tw = (uint32_t)(lt & (int64_t)(C.tasks_per_plane - 1));
+        const int rg = C.rep_base + r;
+        if (rg != cur_rep) {
+            if (MODE != 0 && cur_rep >= 0) {
+                flush_acc(P.acc, cur_rep, accb, accm, lane);
+                accb = accm = 0;
+            }
+            cur_rep = rg;
+            if (MODE != 2) {
+                const int slot = C.rep_base + P.r2t[rg];
+                __syncwarp();
+                if (lane < 16) s_thr[wib][lane] = P.thr[slot * 16 + lane];
+                __syncwarp();
+            }
+            int8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
+            own = reinterpret_cast<uint32_t*>(base + (int64_t)colour * C.plane_sites);
+            oth = reinterpret_cast<const uint32_t*>(base + (int64_t)(colour ^ 1) * C.plane_sites);
+            uid = replica_uid(C.L, r);
+        }
+        const int L = C.L;
+        const uint32_t Lm = (uint32_t)L - 1;
+        const int lrw = C.log2_row_words;
+        const uint32_t rwm = (1u << lrw) - 1;
+        const uint32_t w = (tw << 5) + (uint32_t)lane;
+        const uint32_t row = w >> lrw;
+        const uint32_t k4 = w & rwm;
+        uint32_t y, z, p;
+        if (DIM == 3) {
+            y = row & Lm;
+            z = row >> C.log2L;
+            p = (y + z + (uint32_t)colour) & 1u;
+        } else {
+            y = row;
+            z = 0;
+            p = (y + (uint32_t)colour) & 1u;
+        }
+        const uint32_t yp = (y + 1) & Lm, ym = (y - 1) & Lm;
+        uint32_t wa, wyp, wym, wzp = 0, wzm = 0;
+        if (DIM == 3) {
+            const uint32_t zp = (z + 1) & Lm, zm = (z - 1) & Lm;
+            const uint32_t zb = z << C.log2L;
+            wa = __ldg(oth + (((zb + y) << lrw) + k4));
+            wyp = __ldg(oth + (((zb + yp) << lrw) + k4));
+            wym = __ldg(oth + (((zb + ym) << lrw) + k4));
+            wzp = __ldg(oth + ((((zp << C.log2L) + y) << lrw) + k4));
+            wzm = __ldg(oth + ((((zm << C.log2L) + y) << lrw) + k4));
+        } else {
+            wa = __ldg(oth + ((y << lrw) + k4));
+            wyp = __ldg(oth + ((yp << lrw) + k4));
+            wym = __ldg(oth + ((ym << lrw) + k4));
+        }
+        const int lane0 = lane - (int)k4;
+        const uint32_t prev = __shfl_sync(ISG_FULL_MASK, wa, lane0 + (int)((k4 - 1) & rwm));
+        const uint32_t next = __shfl_sync(ISG_FULL_MASK, wa, lane0 + (int)((k4 + 1) & rwm));
+        const uint32_t wx = p ? __funnelshift_r(wa, next, 8) : __funnelshift_l(prev, wa, 8);
+        const uint32_t ow = own[w];
+        uint32_t nw = ow;
+        if (MODE != 2) {
+            uint32_t nd2 = (wx & M2) + (wa & M2) + (wyp & M2) + (wym & M2);
+            if (DIM == 3) nd2 += (wzp & M2) + (wzm & M2);
+            const uint32_t idx4 = (nd2 << 1) + ((ow & M2) << 4);
+            const U4 u = philox10(w, uid, c2, c3, k0, k1);
+            const uint32_t t0 = *reinterpret_cast<const uint32_t*>(tb + (idx4 & 0xFFu));
+            const uint32_t t1 = *reinterpret_cast<const uint32_t*>(tb + ((idx4 >> 8) & 0xFFu));
+            const uint32_t t2 = *reinterpret_cast<const uint32_t*>(tb + ((idx4 >> 16) & 0xFFu));
+            const uint32_t t3 = *reinterpret_cast<const uint32_t*>(tb + (idx4 >> 24));
+            const uint32_t flip = (u.x <= t0 ? 0x00000001u : 0u) | (u.y <= t1 ? 0x00000100u : 0u) |
+                                  (u.z <= t2 ? 0x00010000u : 0u) | (u.w <= t3 ? 0x01000000u : 0u);
+            nw = ow ^ (flip * 0xFEu);
+            own[w] = nw;
+        }
+        if (MODE != 0) {
+            int b = __dp4a((int)nw, (int)wx, 0);
+            b = __dp4a((int)nw, (int)wa, b);
+            b = __dp4a((int)nw, (int)wyp, b);
+            b = __dp4a((int)nw, (int)wym, b);
+            if (DIM == 3) {
+                b = __dp4a((int)nw, (int)wzp, b);
+                b = __dp4a((int)nw, (int)wzm, b);
+            }
+            accb += b;
+            accm += __dp4a((int)nw, 0x01010101, 0) + __dp4a((int)wa, 0x01010101, 0);
+        }
+    }
+    if (MODE != 0) flush_acc(P.acc, cur_rep, accb, accm, lane);
+}
+
+template <int DIM, int MODE>
+__global__ void __launch_bounds__(kMaxThreads)
+    k_ising_sites(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
+    const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
+    const uint32_t c2 = (uint32_t)sweep;
+    const uint32_t c3 = counter_word3(ISG_TAG_ISING, (uint32_t)colour, sweep);
+    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < P.total_sites;
+         g += stride) {
+        int ci = 0;
+        while (P.cls[ci].site_end <= g) ++ci;
+        const IsingClass& C = P.cls[ci];
+        const int64_t lg = g - C.site_base;
+        const int r = (int)(lg / C.plane_sites);
+        const uint32_t i = (uint32_t)(lg - (int64_t)r * C.plane_sites);
+        const int L = C.L;
+        const uint32_t half = (uint32_t)L >> 1;
+        const uint32_t row = i / half;
+        const uint32_t k = i - row * half;
+        uint32_t y, z, p;
+        if (DIM == 3) {
+            y = row % (uint32_t)L;
+            z = row / (uint32_t)L;
+            p = (y + z + (uint32_t)colour) & 1u;
+        } else {
+            y = row;
+            z = 0;
+            p = (y + (uint32_t)colour) & 1u;
+        }
+        const uint32_t x = 2 * k + p;
+        const uint32_t Lu = (uint32_t)L;
+        const uint32_t xp = (x + 1) % Lu, xm = (x + Lu - 1) % Lu;
+        const uint32_t yp = (y + 1) % Lu, ym = (y + Lu - 1) % Lu;
+        int8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
+        int8_t* own = base + (int64_t)colour * C.plane_sites;
+        const int8_t* oth = base + (int64_t)(colour ^ 1) * C.plane_sites;
+        const uint64_t rowL = (uint64_t)(z * Lu + y) * Lu;
+        int nb[6];
+        nb[0] = oth[(rowL + xp) >> 1];
+        nb[1] = oth[(rowL + xm) >> 1];
+        nb[2] = oth[((uint64_t)(z * Lu + yp) * Lu + x) >> 1];
+        nb[3] = oth[((uint64_t)(z * Lu + ym) * Lu + x) >> 1];
+        int nsum = nb[0] + nb[1] + nb[2] + nb[3];
+        int nd = (nb[0] < 0) + (nb[1] < 0) + (nb[2] < 0) + (nb[3] < 0);
+        if (DIM == 3) {
+            const uint32_t zp = (z + 1) % Lu, zm = (z + Lu - 1) % Lu;
+            nb[4] = oth[((uint64_t)(zp * Lu + y) * Lu + x) >> 1];
+            nb[5] = oth[((uint64_t)(zm * Lu + y) * Lu + x) >> 1];
+            nsum += nb[4] + nb[5];
+            nd += (nb[4] < 0) + (nb[5] < 0);
+        }
+        int s = own[i];
+        if (MODE != 2) {
+            const int rg = C.rep_base + r;
+            const int slot = C.rep_base + P.r2t[rg];
+            const uint32_t th = P.thr[slot * 16 + (s < 0 ? 8 : 0) + nd];
+            const U4 u = philox10(i >> 2, replica_uid(L, r), c2, c3, k0, k1);
+            const uint32_t j = i & 3u;
+            const uint32_t uu = j == 0 ? u.x : j == 1 ? u.y : j == 2 ? u.z : u.w;
+            if (uu <= th) {
+                s = -s;
+                own[i] = (int8_t)s;
+            }
+        }
+        if (MODE != 0) {
+            const int rg = C.rep_base + r;
+            const long long b = (long long)(s * nsum);
+            const long long m = (long long)(s + oth[i]);
+            atomicAdd(&P.acc[2 * rg], (unsigned long long)b);
+            atomicAdd(&P.acc[2 * rg + 1], (unsigned long long)m);
+        }
+    }
+}
+
+// Hot start: natural site n of replica r gets -1 if the top bit of word
+// (n & 3) of Philox(n >> 2, uid, 0, INIT) is set, else +1.
+__global__ void k_ising_init(const __grid_constant__ IsingParams P, int dim) {
+    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    const uint32_t c3 = counter_word3(ISG_TAG_INIT, 0, 0);
+    for (int ci = 0; ci < P.n_classes; ++ci) {
+        const IsingClass& C = P.cls[ci];
+        const int64_t nsite = 2 * (int64_t)C.plane_sites;
+        const int64_t total = nsite * C.R;
+        for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+             g += (int64_t)gridDim.x * blockDim.x) {
+            const int r = (int)(g / nsite);
+            const uint32_t n = (uint32_t)(g - (int64_t)r * nsite);
+            const U4 u = philox10(n >> 2, replica_uid(C.L, r), 0, c3, k0, k1);
+            const uint32_t j = n & 3u;
+            const uint32_t wv = j == 0 ? u.x : j == 1 ? u.y : j == 2 ? u.z : u.w;
+            const uint32_t L = (uint32_t)C.L;
+            const uint32_t x = n % L;
+            const uint32_t y = (n / L) % L;
+            const uint32_t z = dim == 3 ? n / (L * L) : 0;
+            const uint32_t c = (x + y + z) & 1u;
+            P.spins[C.spin_off + (int64_t)r * nsite + (int64_t)c * C.plane_sites + (n >> 1)] =
+                (wv >> 31) ? (int8_t)-1 : (int8_t)1;
+        }
+    }
+}
+
+struct PostParams {
+    unsigned long long* acc;  // [replicas][2]
+    int32_t* r2t;
+    int32_t* t2r;
+    const double* betas;      // per slot
+    int32_t* rec_t;
+    long long* rec_b;
+    long long* rec_m;
+    unsigned long long* ctrl; // [0] sweep base, [1+s] records, [1+NC+s] xcount, [1+2NC+s] accepted
+    long long ring_cap;
+    double J, h;
+    uint64_t seed;
+    int R;
+    int n_classes;
+    int replicas_total;
+    int L[kMaxClasses];
+};
+
+// One block per size: record (slot, bond, mag) of every replica, run an
+// exchange pass, zero the accumulators, advance the sweep counter.
+// Exchange arithmetic follows src/parallel_tempering.rs:17-33 in FP64 with
+// explicitly rounded products so the CPU replay matches bit for bit.
+__global__ void k_ising_post(const __grid_constant__ PostParams Q, int do_record, int do_exchange,
+                             int parity, int zero_acc, int advance) {
+    __shared__ double s_e[kMaxReplicas];
+    __shared__ int s_t2r[kMaxReplicas];
+    __shared__ int s_acc;
+    const int s = blockIdx.x;
+    const int R = Q.R;
+    const int base = s * R;
+    const int NC = Q.n_classes;
+    unsigned long long* rec_count = Q.ctrl + 1 + s;
+    unsigned long long* xcount = Q.ctrl + 1 + NC + s;
+    unsigned long long* accepted = Q.ctrl + 1 + 2 * NC + s;
+    if (threadIdx.x == 0) s_acc = 0;
+    for (int r = threadIdx.x; r < R; r += blockDim.x) {
+        const long long b = (long long)Q.acc[2 * (base + r)];
+        const long long m = (long long)Q.acc[2 * (base + r) + 1];
+        const double t1 = __dmul_rn(Q.J, (double)b);
+        const double t2 = __dmul_rn(Q.h, (double)m);
+        s_e[r] = __dsub_rn(-t1, t2);
+        s_t2r[r] = Q.t2r[base + r];
+        if (do_record) {
+            const long long slot = (long long)(*rec_count % (unsigned long long)Q.ring_cap);
+            const long long o = slot * Q.replicas_total + base + r;
+            Q.rec_t[o] = Q.r2t[base + r];
+            Q.rec_b[o] = b;
+            Q.rec_m[o] = m;
+        }
+    }
+    __syncthreads();
+    if (do_exchange) {
+        const unsigned long long xc = *xcount;
+        const int par = parity >= 0 ? (parity & 1) : (int)(xc & 1ull);
+        const uint32_t k0 = (uint32_t)Q.seed, k1 = (uint32_t)(Q.seed >> 32);
+        const uint32_t c3 = counter_word3(ISG_TAG_EXCH, 0, xc);
+        for (int i = par + 2 * threadIdx.x; i + 1 < R; i += 2 * blockDim.x) {
+            const int ri = s_t2r[i], rj = s_t2r[i + 1];
+            const double d = __dmul_rn(__dsub_rn(Q.betas[base + i], Q.betas[base + i + 1]),
+                                       __dsub_rn(s_e[rj], s_e[ri]));
+            bool ok = d < 0.0;
+            if (!ok) {
+                const U4 u = philox10((uint32_t)i, exchange_uid(Q.L[s]), (uint32_t)xc, c3, k0, k1);
+                ok = uniform53(u.x, u.y) < exp(-d);
+            }
+            if (ok) {
+                s_t2r[i] = rj;
+                s_t2r[i + 1] = ri;
+                Q.r2t[base + ri] = i + 1;
+                Q.r2t[base + rj] = i;
+                atomicAdd(&s_acc, 1);
+            }
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < R; r += blockDim.x) Q.t2r[base + r] = s_t2r[r];
+        if (threadIdx.x == 0) {
+            *xcount = xc + 1;
+            *accepted += (unsigned long long)s_acc;
+        }
+    }
+    if (zero_acc)
+        for (int r = threadIdx.x; r < R; r += blockDim.x) {
+            Q.acc[2 * (base + r)] = 0ull;
+            Q.acc[2 * (base + r) + 1] = 0ull;
+        }
+    if (threadIdx.x == 0) {
+        if (do_record) *rec_count += 1ull;
+        if (s == 0 && advance) Q.ctrl[0] += (unsigned long long)advance;
+    }
+}
+
+// ---------------------------------------------------------------- host object
+
+static int num_sms(int dev) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+static int64_t gcd64(int64_t a, int64_t b) {
+    while (b) {
+        int64_t t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+}  // namespace isg
+
+using namespace isg;
+
+struct isg_ising {
+    int device = 0;
+    int dim = 3;
+    int n_classes = 0;
+    int R = 0;
+    int replicas_total = 0;
+    uint64_t seed = 0;
+    std::vector<int> sizes;
+    IsingParams P{};
+    PostParams Q{};
+    int8_t* d_spins = nullptr;
+    int64_t spin_bytes = 0;
+    uint32_t* d_thr = nullptr;
+    int32_t* d_r2t = nullptr;
+    int32_t* d_t2r = nullptr;
+    double* d_betas = nullptr;
+    unsigned long long* d_acc = nullptr;
+    unsigned long long* d_ctrl = nullptr;
+    int64_t ring_cap = 0;
+    int32_t* d_rec_t = nullptr;
+    long long* d_rec_b = nullptr;
+    long long* d_rec_m = nullptr;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    bool temps_set = false;
+    double J = 1.0, h = 0.0;
+    int threads = 256;
+    int blocks_per_sm = 0;
+    int word_grid = 0, site_grid = 0;
+    int sms = 1;
+    // sampling-phase mirror of the device counters
+    uint64_t ksample = 0;
+    uint64_t records_done = 0;  // records already copied out of the ring
+    uint64_t records_made = 0;
+    uint64_t gsweep = 0;
+    // cached cycle graph
+    cudaGraphExec_t graph = nullptr;
+    int graph_ee = 0, graph_me = 0, graph_period = 0;
+};
+
+namespace isg {
+
+static void (*word_kernel(int dim, int mode))(IsingParams, int, int) {
+    if (dim == 3) {
+        if (mode == 0) return k_ising_words<3, 0>;
+        if (mode == 1) return k_ising_words<3, 1>;
+        return k_ising_words<3, 2>;
+    }
+    if (mode == 0) return k_ising_words<2, 0>;
+    if (mode == 1) return k_ising_words<2, 1>;
+    return k_ising_words<2, 2>;
+}
+static void (*site_kernel(int dim, int mode))(IsingParams, int, int) {
+    if (dim == 3) {
+        if (mode == 0) return k_ising_sites<3, 0>;
+        if (mode == 1) return k_ising_sites<3, 1>;
+        return k_ising_sites<3, 2>;
+    }
+    if (mode == 0) return k_ising_sites<2, 0>;
+    if (mode == 1) return k_ising_sites<2, 1>;
+    return k_ising_sites<2, 2>;
+}
+
+static int configure_launch(isg_ising* H) {
+    const int thr = H->threads;
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &occ, (const void*)word_kernel(H->dim, 1), thr, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    if (occ < 1) occ = 1;
+    int bps = H->blocks_per_sm > 0 ? std::min(H->blocks_per_sm, occ) : occ;
+    int64_t max_blocks = (int64_t)H->sms * bps;
+    const int64_t warps_per_block = thr / 32;
+    int64_t need = (H->P.total_tasks + warps_per_block - 1) / warps_per_block;
+    H->word_grid = (int)std::max<int64_t>(1, std::min(max_blocks, need));
+    int64_t sneed = (H->P.total_sites + thr - 1) / thr;
+    H->site_grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)H->sms * 8, sneed));
+    return ISG_OK;
+}
+
+static void launch_half(isg_ising* H, int colour, int sweep_off, int mode) {
+    if (H->P.total_tasks > 0)
+        word_kernel(H->dim, mode)<<<H->word_grid, H->threads, 0, H->stream>>>(H->P, colour,
+                                                                             sweep_off);
+    if (H->P.total_sites > 0)
+        site_kernel(H->dim, mode)<<<H->site_grid, H->threads, 0, H->stream>>>(H->P, colour,
+                                                                             sweep_off);
+}
+
+static void launch_post(isg_ising* H, int do_record, int do_exchange, int parity, int zero_acc,
+                        int advance) {
+    int thr = std::min(1024, std::max(32, ((H->R + 31) / 32) * 32));
+    k_ising_post<<<H->n_classes, thr, 0, H->stream>>>(H->Q, do_record, do_exchange, parity,
+                                                      zero_acc, advance);
+}
+
+static int check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    return ISG_OK;
+}
+
+static void destroy_graph(isg_ising* H) {
+    if (H->graph) cudaGraphExecDestroy(H->graph);
+    H->graph = nullptr;
+    H->graph_period = 0;
+}
+
+// One sampling sweep k (0-based) issued directly.
+static void issue_sample_sweep(isg_ising* H, uint64_t k, int sweep_off, int ee, int me,
+                               int advance) {
+    const bool do_m = ((k + 1) % (uint64_t)me) == 0;
+    const bool do_x = ((k + 1) % (uint64_t)ee) == 0;
+    launch_half(H, 0, sweep_off, 0);
+    launch_half(H, 1, sweep_off, (do_m || do_x) ? 1 : 0);
+    if (do_m || do_x || advance)
+        launch_post(H, do_m ? 1 : 0, do_x ? 1 : 0, -1, (do_m || do_x) ? 1 : 0, advance);
+}
+
+static int build_graph(isg_ising* H, int ee, int me, int period) {
+    destroy_graph(H);
+    cudaGraph_t g = nullptr;
+    ISG_CK(cudaStreamBeginCapture(H->stream, cudaStreamCaptureModeThreadLocal));
+    for (int j = 0; j < period; ++j)
+        issue_sample_sweep(H, (uint64_t)j, j, ee, me, j == period - 1 ? period : 0);
+    cudaError_t e = cudaStreamEndCapture(H->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&H->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        H->graph = nullptr;
+        return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    H->graph_ee = ee;
+    H->graph_me = me;
+    H->graph_period = period;
+    return ISG_OK;
+}
+
+static int drain_records(isg_ising* H, int32_t* tslot, int64_t* bond, int64_t* mag,
+                         int64_t row0) {
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    const int RT = H->replicas_total;
+    uint64_t n = H->records_made - H->records_done;
+    int64_t row = row0;
+    while (n > 0) {
+        uint64_t slot = H->records_done % (uint64_t)H->ring_cap;
+        uint64_t chunk = std::min<uint64_t>(n, (uint64_t)H->ring_cap - slot);
+        size_t cnt = (size_t)chunk * RT;
+        size_t off = (size_t)slot * RT;
+        ISG_CK(cudaMemcpy(tslot + (size_t)row * RT, H->d_rec_t + off, cnt * sizeof(int32_t),
+                          cudaMemcpyDeviceToHost));
+        ISG_CK(cudaMemcpy(bond + (size_t)row * RT, H->d_rec_b + off, cnt * sizeof(int64_t),
+                          cudaMemcpyDeviceToHost));
+        ISG_CK(cudaMemcpy(mag + (size_t)row * RT, H->d_rec_m + off, cnt * sizeof(int64_t),
+                          cudaMemcpyDeviceToHost));
+        H->records_done += chunk;
+        row += (int64_t)chunk;
+        n -= chunk;
+    }
+    return ISG_OK;
+}
+
+}  // namespace isg
+
+// ---------------------------------------------------------------- C ABI
+
+extern "C" {
+
+const char* isg_last_error(void) { return isg::g_last_error.c_str(); }
+int isg_version(void) { return ISG_VERSION; }
+
+int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replicas, int dim,
+                     uint64_t seed) {
+    if (!out) return fail(ISG_ERR_ARG, "isg_ising_create: out is NULL");
+    *out = nullptr;
+    if (!sizes || n_sizes < 1 || n_sizes > kMaxClasses)
+        return fail(ISG_ERR_ARG, "isg_ising_create: need 1.." + std::to_string(kMaxClasses) +
+                                     " sizes");
+    if (replicas < 1 || replicas > kMaxReplicas)
+        return fail(ISG_ERR_ARG, "isg_ising_create: replicas must be 1..1024");
+    if (dim != 2 && dim != 3) return fail(ISG_ERR_ARG, "isg_ising_create: dim must be 2 or 3");
+    for (int s = 0; s < n_sizes; ++s) {
+        const int L = sizes[s];
+        if (L < 2 || L > 1024)
+            return fail(ISG_ERR_ARG, "isg_ising_create: size " + std::to_string(L) +
+                                         " outside 2..1024");
+        for (int q = 0; q < s; ++q)
+            if (sizes[q] == L)
+                return fail(ISG_ERR_ARG, "isg_ising_create: size " + std::to_string(L) +
+                                             " listed twice (sizes share random streams)");
+        if (L & 1)
+            return fail(ISG_ERR_UNSUPPORTED,
+                        "isg_ising_create: odd size " + std::to_string(L) +
+                            " has no checkerboard colouring under periodic boundaries");
+    }
+    isg_ising* H = new (std::nothrow) isg_ising();
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_create: out of host memory");
+    cudaGetDevice(&H->device);
+    H->sms = num_sms(H->device);
+    H->dim = dim;
+    H->n_classes = n_sizes;
+    H->R = replicas;
+    H->replicas_total = n_sizes * replicas;
+    H->seed = seed;
+    H->sizes.assign(sizes, sizes + n_sizes);
+
+    IsingParams& P = H->P;
+    int64_t off = 0, task = 0, site = 0;
+    for (int s = 0; s < n_sizes; ++s) {
+        IsingClass& C = P.cls[s];
+        const int L = sizes[s];
+        C.L = L;
+        C.R = replicas;
+        const int64_t nsite = dim == 3 ? (int64_t)L * L * L : (int64_t)L * L;
+        C.plane_sites = (uint32_t)(nsite / 2);
+        const bool pow2 = (L & (L - 1)) == 0;
+        const int rw = L / 8;
+        C.word_path = (pow2 && L >= 8 && L <= 256 && (32 % rw) == 0 &&
+                       (C.plane_sites / 4) % 32 == 0)
+                          ? 1
+                          : 0;
+        C.log2L = 0;
+        while ((1 << C.log2L) < L) ++C.log2L;
+        C.log2_row_words = 0;
+        if (C.word_path)
+            while ((1 << C.log2_row_words) < rw) ++C.log2_row_words;
+        C.tasks_per_plane = C.word_path ? C.plane_sites / 128 : 0;
+        C.log2_tpp = 0;
+        while (C.word_path && (1u << C.log2_tpp) < C.tasks_per_plane) ++C.log2_tpp;
+        C.rep_base = s * replicas;
+        C.spin_off = off;
+        off += ((2 * (int64_t)C.plane_sites * replicas + 255) / 256) * 256;
+        C.task_base = task;
+        if (C.word_path) task += (int64_t)C.tasks_per_plane * replicas;
+        C.task_end = task;
+        C.site_base = site;
+        if (!C.word_path) site += (int64_t)C.plane_sites * replicas;
+        C.site_end = site;
+    }
+    // sentinel classes so the device class search always terminates
+    for (int s = n_sizes; s < kMaxClasses; ++s) {
+        P.cls[s] = P.cls[n_sizes - 1];
+        P.cls[s].task_base = P.cls[s].task_end = INT64_MAX;
+        P.cls[s].site_base = P.cls[s].site_end = INT64_MAX;
+    }
+    P.n_classes = n_sizes;
+    P.total_tasks = task;
+    P.total_sites = site;
+    P.seed = seed;
+    H->spin_bytes = off;
+
+    const int RT = H->replicas_total;
+    H->ring_cap = std::max<int64_t>(64, std::min<int64_t>(8192, (64ll << 20) / (20ll * RT)));
+    auto cleanup = [&](int code) {
+        isg_ising_destroy(H);
+        return code;
+    };
+    cudaError_t e;
+#define ALLOC(ptr, bytes)                                              \
+    e = cudaMalloc((void**)&(ptr), (bytes));                           \
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMalloc"));
+    ALLOC(H->d_spins, (size_t)off);
+    ALLOC(H->d_thr, sizeof(uint32_t) * 16 * RT);
+    ALLOC(H->d_r2t, sizeof(int32_t) * RT);
+    ALLOC(H->d_t2r, sizeof(int32_t) * RT);
+    ALLOC(H->d_betas, sizeof(double) * RT);
+    ALLOC(H->d_acc, sizeof(unsigned long long) * 2 * RT);
+    ALLOC(H->d_ctrl, sizeof(unsigned long long) * (1 + 3 * kMaxClasses));
+    ALLOC(H->d_rec_t, sizeof(int32_t) * (size_t)H->ring_cap * RT);
+    ALLOC(H->d_rec_b, sizeof(long long) * (size_t)H->ring_cap * RT);
+    ALLOC(H->d_rec_m, sizeof(long long) * (size_t)H->ring_cap * RT);
+#undef ALLOC
+    e = cudaStreamCreateWithFlags(&H->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaStreamCreateWithFlags"));
+    H->stream = H->own_stream;
+
+    P.spins = H->d_spins;
+    P.thr = H->d_thr;
+    P.r2t = H->d_r2t;
+    P.acc = H->d_acc;
+    P.ctrl = H->d_ctrl;
+
+    PostParams& Q = H->Q;
+    Q.acc = H->d_acc;
+    Q.r2t = H->d_r2t;
+    Q.t2r = H->d_t2r;
+    Q.betas = H->d_betas;
+    Q.rec_t = H->d_rec_t;
+    Q.rec_b = H->d_rec_b;
+    Q.rec_m = H->d_rec_m;
+    Q.ctrl = H->d_ctrl;
+    Q.ring_cap = H->ring_cap;
+    Q.seed = seed;
+    Q.R = replicas;
+    Q.n_classes = n_sizes;
+    Q.replicas_total = RT;
+    for (int s = 0; s < kMaxClasses; ++s) Q.L[s] = s < n_sizes ? sizes[s] : 0;
+
+    std::vector<int32_t> ident(RT);
+    for (int i = 0; i < RT; ++i) ident[i] = i % replicas;
+#define CKC(call)                                                      \
+    e = (call);                                                        \
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, #call));
+    CKC(cudaMemsetAsync(H->d_spins, 0, (size_t)off, H->stream));
+    CKC(cudaMemsetAsync(H->d_thr, 0, sizeof(uint32_t) * 16 * RT, H->stream));
+    CKC(cudaMemsetAsync(H->d_acc, 0, sizeof(unsigned long long) * 2 * RT, H->stream));
+    CKC(cudaMemsetAsync(H->d_ctrl, 0, sizeof(unsigned long long) * (1 + 3 * kMaxClasses),
+                        H->stream));
+    CKC(cudaMemcpyAsync(H->d_r2t, ident.data(), sizeof(int32_t) * RT, cudaMemcpyHostToDevice,
+                        H->stream));
+    CKC(cudaMemcpyAsync(H->d_t2r, ident.data(), sizeof(int32_t) * RT, cudaMemcpyHostToDevice,
+                        H->stream));
+    k_ising_init<<<H->sms * 4, 256, 0, H->stream>>>(H->P, dim);
+    CKC(cudaGetLastError());
+    CKC(cudaStreamSynchronize(H->stream));
+#undef CKC
+    int rc = configure_launch(H);
+    if (rc != ISG_OK) return cleanup(rc);
+    *out = H;
+    return ISG_OK;
+}
+
+int isg_ising_destroy(isg_ising* H) {
+    if (!H) return ISG_OK;
+    cudaSetDevice(H->device);
+    if (H->stream) cudaStreamSynchronize(H->stream);
+    destroy_graph(H);
+    cudaFree(H->d_spins);
+    cudaFree(H->d_thr);
+    cudaFree(H->d_r2t);
+    cudaFree(H->d_t2r);
+    cudaFree(H->d_betas);
+    cudaFree(H->d_acc);
+    cudaFree(H->d_ctrl);
+    cudaFree(H->d_rec_t);
+    cudaFree(H->d_rec_b);
+    cudaFree(H->d_rec_m);
+    if (H->own_stream) cudaStreamDestroy(H->own_stream);
+    delete H;
+    return ISG_OK;
+}
+
+int isg_ising_set_stream(isg_ising* H, void* stream) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_set_stream: NULL handle");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    H->stream = stream ? (cudaStream_t)stream : H->own_stream;
+    return ISG_OK;
+}
+
+int isg_ising_set_temperatures(isg_ising* H, const double* temps, double J, double hfield) {
+    if (!H || !temps) return fail(ISG_ERR_ARG, "isg_ising_set_temperatures: NULL argument");
+    cudaSetDevice(H->device);
+    const int RT = H->replicas_total;
+    std::vector<uint32_t> thr(16 * (size_t)RT, 0u);
+    std::vector<double> betas(RT);
+    for (int i = 0; i < RT; ++i) {
+        if (!(temps[i] > 0.0) || !std::isfinite(temps[i]))
+            return fail(ISG_ERR_ARG, "isg_ising_set_temperatures: temperatures must be positive");
+        const double beta = 1.0 / temps[i];
+        betas[i] = beta;
+        for (int od = 0; od < 2; ++od) {
+            const double sgn = od ? -1.0 : 1.0;
+            for (int nd = 0; nd <= 2 * H->dim; ++nd) {
+                const double nb = (double)(2 * H->dim - 2 * nd);
+                const double dE = 2.0 * sgn * (J * nb + hfield);
+                uint32_t t;
+                if (dE <= 0.0) {
+                    t = 0xFFFFFFFFu;
+                } else {
+                    double f = std::floor(std::exp(-beta * dE) * 4294967296.0);
+                    if (f < 1.0) f = 1.0;
+                    t = (uint32_t)(f - 1.0);
+                }
+                thr[(size_t)i * 16 + od * 8 + nd] = t;
+            }
+        }
+    }
+    std::vector<int32_t> ident(RT);
+    for (int i = 0; i < RT; ++i) ident[i] = i % H->R;
+    ISG_CK(cudaMemcpyAsync(H->d_thr, thr.data(), thr.size() * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, H->stream));
+    ISG_CK(cudaMemcpyAsync(H->d_betas, betas.data(), betas.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, H->stream));
+    ISG_CK(cudaMemcpyAsync(H->d_r2t, ident.data(), sizeof(int32_t) * RT, cudaMemcpyHostToDevice,
+                           H->stream));
+    ISG_CK(cudaMemcpyAsync(H->d_t2r, ident.data(), sizeof(int32_t) * RT, cudaMemcpyHostToDevice,
+                           H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    H->J = J;
+    H->h = hfield;
+    H->Q.J = J;
+    H->Q.h = hfield;
+    H->temps_set = true;
+    destroy_graph(H);
+    return ISG_OK;
+}
+
+int isg_ising_step(isg_ising* H, int64_t n_sweeps) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_step: NULL handle");
+    if (!H->temps_set) return fail(ISG_ERR_STATE, "isg_ising_step: temperatures not set");
+    if (n_sweeps < 0) return fail(ISG_ERR_ARG, "isg_ising_step: negative sweep count");
+    if (n_sweeps == 0) return ISG_OK;
+    cudaSetDevice(H->device);
+    int64_t done = 0;
+    while (done < n_sweeps) {
+        const int chunk = (int)std::min<int64_t>(n_sweeps - done, 1 << 20);
+        for (int j = 0; j < chunk; ++j) {
+            launch_half(H, 0, j, 0);
+            launch_half(H, 1, j, 0);
+        }
+        launch_post(H, 0, 0, 0, 0, chunk);
+        done += chunk;
+    }
+    H->gsweep += (uint64_t)n_sweeps;
+    return check_launch("isg_ising_step");
+}
+
+int isg_ising_measure(isg_ising* H, int64_t* bond, int64_t* mag) {
+    if (!H || !bond || !mag) return fail(ISG_ERR_ARG, "isg_ising_measure: NULL argument");
+    cudaSetDevice(H->device);
+    const int RT = H->replicas_total;
+    ISG_CK(cudaMemsetAsync(H->d_acc, 0, sizeof(unsigned long long) * 2 * RT, H->stream));
+    launch_half(H, 1, 0, 2);
+    int rc = check_launch("isg_ising_measure");
+    if (rc) return rc;
+    std::vector<unsigned long long> acc(2 * (size_t)RT);
+    ISG_CK(cudaMemcpyAsync(acc.data(), H->d_acc, acc.size() * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    for (int i = 0; i < RT; ++i) {
+        bond[i] = (int64_t)acc[2 * i];
+        mag[i] = (int64_t)acc[2 * i + 1];
+    }
+    return ISG_OK;
+}
+
+int isg_ising_exchange(isg_ising* H, int parity, int64_t* accepted) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_exchange: NULL handle");
+    if (!H->temps_set) return fail(ISG_ERR_STATE, "isg_ising_exchange: temperatures not set");
+    cudaSetDevice(H->device);
+    const int NC = H->n_classes;
+    std::vector<unsigned long long> before(NC), after(NC);
+    ISG_CK(cudaMemcpyAsync(before.data(), H->d_ctrl + 1 + 2 * NC, NC * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, H->stream));
+    launch_post(H, 0, 1, parity, 1, 0);
+    int rc = check_launch("isg_ising_exchange");
+    if (rc) return rc;
+    ISG_CK(cudaMemcpyAsync(after.data(), H->d_ctrl + 1 + 2 * NC, NC * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    if (accepted)
+        for (int s = 0; s < NC; ++s) accepted[s] = (int64_t)(after[s] - before[s]);
+    return ISG_OK;
+}
+
+int isg_ising_get_r2t(isg_ising* H, int32_t* r2t) {
+    if (!H || !r2t) return fail(ISG_ERR_ARG, "isg_ising_get_r2t: NULL argument");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaMemcpyAsync(r2t, H->d_r2t, sizeof(int32_t) * H->replicas_total,
+                           cudaMemcpyDeviceToHost, H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    return ISG_OK;
+}
+
+int isg_ising_set_r2t(isg_ising* H, const int32_t* r2t) {
+    if (!H || !r2t) return fail(ISG_ERR_ARG, "isg_ising_set_r2t: NULL argument");
+    cudaSetDevice(H->device);
+    const int R = H->R, RT = H->replicas_total;
+    std::vector<int32_t> t2r(RT, -1);
+    for (int s = 0; s < H->n_classes; ++s)
+        for (int r = 0; r < R; ++r) {
+            const int t = r2t[s * R + r];
+            if (t < 0 || t >= R || t2r[s * R + t] != -1)
+                return fail(ISG_ERR_ARG, "isg_ising_set_r2t: not a permutation per size");
+            t2r[s * R + t] = r;
+        }
+    ISG_CK(cudaMemcpyAsync(H->d_r2t, r2t, sizeof(int32_t) * RT, cudaMemcpyHostToDevice,
+                           H->stream));
+    ISG_CK(cudaMemcpyAsync(H->d_t2r, t2r.data(), sizeof(int32_t) * RT, cudaMemcpyHostToDevice,
+                           H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    return ISG_OK;
+}
+
+static int spin_geometry(isg_ising* H, int s, int r, int64_t* nsite, int64_t* base) {
+    if (s < 0 || s >= H->n_classes || r < 0 || r >= H->R)
+        return fail(ISG_ERR_ARG, "spin access: size index or replica out of range");
+    const IsingClass& C = H->P.cls[s];
+    *nsite = 2 * (int64_t)C.plane_sites;
+    *base = C.spin_off + (int64_t)r * *nsite;
+    return ISG_OK;
+}
+
+int isg_ising_get_spins(isg_ising* H, int s, int r, int8_t* out) {
+    if (!H || !out) return fail(ISG_ERR_ARG, "isg_ising_get_spins: NULL argument");
+    cudaSetDevice(H->device);
+    int64_t n, base;
+    int rc = spin_geometry(H, s, r, &n, &base);
+    if (rc) return rc;
+    std::vector<int8_t> planes((size_t)n);
+    ISG_CK(cudaMemcpyAsync(planes.data(), H->d_spins + base, (size_t)n, cudaMemcpyDeviceToHost,
+                           H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    const int L = H->sizes[s];
+    const int64_t half = n / 2;
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t x = i % L, y = (i / L) % L, z = H->dim == 3 ? i / ((int64_t)L * L) : 0;
+        const int c = (int)((x + y + z) & 1);
+        out[i] = planes[(size_t)(c * half + (i >> 1))];
+    }
+    return ISG_OK;
+}
+
+int isg_ising_set_spins(isg_ising* H, int s, int r, const int8_t* in) {
+    if (!H || !in) return fail(ISG_ERR_ARG, "isg_ising_set_spins: NULL argument");
+    cudaSetDevice(H->device);
+    int64_t n, base;
+    int rc = spin_geometry(H, s, r, &n, &base);
+    if (rc) return rc;
+    std::vector<int8_t> planes((size_t)n);
+    const int L = H->sizes[s];
+    const int64_t half = n / 2;
+    for (int64_t i = 0; i < n; ++i) {
+        if (in[i] != 1 && in[i] != -1)
+            return fail(ISG_ERR_ARG, "isg_ising_set_spins: spins must be +1 or -1");
+        const int64_t x = i % L, y = (i / L) % L, z = H->dim == 3 ? i / ((int64_t)L * L) : 0;
+        const int c = (int)((x + y + z) & 1);
+        planes[(size_t)(c * half + (i >> 1))] = in[i];
+    }
+    ISG_CK(cudaMemcpyAsync(H->d_spins + base, planes.data(), (size_t)n, cudaMemcpyHostToDevice,
+                           H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    return ISG_OK;
+}
+
+int isg_ising_reset_sampling(isg_ising* H) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_reset_sampling: NULL handle");
+    cudaSetDevice(H->device);
+    const int NC = H->n_classes;
+    ISG_CK(cudaMemsetAsync(H->d_ctrl + 1, 0, sizeof(unsigned long long) * 3 * NC, H->stream));
+    ISG_CK(cudaMemsetAsync(H->d_acc, 0, sizeof(unsigned long long) * 2 * H->replicas_total,
+                           H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    H->ksample = 0;
+    H->records_done = H->records_made = 0;
+    return ISG_OK;
+}
+
+int isg_ising_pt_run(isg_ising* H, int64_t n_sweeps, int ee, int me, int32_t* tslot,
+                     int64_t* bond, int64_t* mag, int64_t max_records, int64_t* n_records) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_pt_run: NULL handle");
+    if (!H->temps_set) return fail(ISG_ERR_STATE, "isg_ising_pt_run: temperatures not set");
+    if (n_sweeps < 0 || ee < 1 || me < 1)
+        return fail(ISG_ERR_ARG, "isg_ising_pt_run: need n_sweeps >= 0, exchange_every >= 1, "
+                                 "measure_every >= 1");
+    cudaSetDevice(H->device);
+    // keep: records stay in the device ring (newest ring_cap rows), no host sync
+    const bool keep = tslot == nullptr && bond == nullptr && mag == nullptr;
+    const uint64_t k0 = H->ksample;
+    const uint64_t need = (k0 + (uint64_t)n_sweeps) / (uint64_t)me - k0 / (uint64_t)me;
+    if (!keep && need > 0 && (!tslot || !bond || !mag || max_records < (int64_t)need))
+        return fail(ISG_ERR_ARG, "isg_ising_pt_run: record arrays hold " +
+                                     std::to_string(max_records) + " rows, " +
+                                     std::to_string(need) + " needed");
+    if (n_records) *n_records = 0;
+    const int64_t g = gcd64(ee, me);
+    const int64_t lcm = (int64_t)ee / g * me;
+    const int period = lcm <= 1000 ? (int)lcm : 0;
+    const int rec_per_period = period ? period / me : 0;
+    const bool use_graph = period > 0 && rec_per_period <= H->ring_cap / 2;
+    int64_t done = 0, row = 0;
+    while (done < n_sweeps) {
+        const uint64_t k = H->ksample;
+        const int64_t left = n_sweeps - done;
+        const uint64_t pending = H->records_made - H->records_done;
+        const bool whole = use_graph && (k % (uint64_t)period) == 0 && left >= period;
+        const uint64_t adds = whole ? (uint64_t)rec_per_period : 1u;
+        if (pending + adds > (uint64_t)H->ring_cap) {
+            if (keep) {
+                H->records_done = H->records_made + adds - (uint64_t)H->ring_cap;
+            } else {
+                int rc = drain_records(H, tslot, bond, mag, row);
+                if (rc) return rc;
+                row += (int64_t)pending;
+                continue;
+            }
+        }
+        if (whole) {
+            if (!H->graph || H->graph_ee != ee || H->graph_me != me || H->graph_period != period) {
+                int rc = build_graph(H, ee, me, period);
+                if (rc) return rc;
+            }
+            ISG_CK(cudaGraphLaunch(H->graph, H->stream));
+            H->ksample += (uint64_t)period;
+            H->gsweep += (uint64_t)period;
+            H->records_made += (uint64_t)rec_per_period;
+            done += period;
+        } else {
+            const bool do_m = ((k + 1) % (uint64_t)me) == 0;
+            issue_sample_sweep(H, k, 0, ee, me, 1);
+            int rc = check_launch("isg_ising_pt_run");
+            if (rc) return rc;
+            H->ksample += 1;
+            H->gsweep += 1;
+            if (do_m) H->records_made += 1;
+            done += 1;
+        }
+    }
+    if (keep) return check_launch("isg_ising_pt_run");
+    const uint64_t pending = H->records_made - H->records_done;
+    int rc = drain_records(H, tslot, bond, mag, row);
+    if (rc) return rc;
+    row += (int64_t)pending;
+    if (n_records) *n_records = row;
+    return ISG_OK;
+}
+
+int isg_ising_read_records(isg_ising* H, int32_t* tslot, int64_t* bond, int64_t* mag,
+                           int64_t max_records, int64_t* n_records) {
+    if (!H || !tslot || !bond || !mag || !n_records)
+        return fail(ISG_ERR_ARG, "isg_ising_read_records: NULL argument");
+    cudaSetDevice(H->device);
+    const uint64_t pending = H->records_made - H->records_done;
+    if ((int64_t)pending > max_records)
+        H->records_done = H->records_made - (uint64_t)std::max<int64_t>(max_records, 0);
+    const uint64_t n = H->records_made - H->records_done;
+    int rc = drain_records(H, tslot, bond, mag, 0);
+    if (rc) return rc;
+    *n_records = (int64_t)n;
+    return ISG_OK;
+}
+
+int isg_ising_get_accepted(isg_ising* H, int64_t* accepted) {
+    if (!H || !accepted) return fail(ISG_ERR_ARG, "isg_ising_get_accepted: NULL argument");
+    cudaSetDevice(H->device);
+    const int NC = H->n_classes;
+    std::vector<unsigned long long> a(NC);
+    ISG_CK(cudaMemcpyAsync(a.data(), H->d_ctrl + 1 + 2 * NC, NC * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    for (int s = 0; s < NC; ++s) accepted[s] = (int64_t)a[s];
+    return ISG_OK;
+}
+
+int isg_ising_get_sweep(isg_ising* H, uint64_t* sweep) {
+    if (!H || !sweep) return fail(ISG_ERR_ARG, "isg_ising_get_sweep: NULL argument");
+    cudaSetDevice(H->device);
+    unsigned long long v = 0;
+    ISG_CK(cudaMemcpyAsync(&v, H->d_ctrl, sizeof(v), cudaMemcpyDeviceToHost, H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    *sweep = v;
+    return ISG_OK;
+}
+
+int isg_ising_sync(isg_ising* H) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_sync: NULL handle");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    return check_launch("isg_ising_sync");
+}
+
+int isg_ising_set_launch(isg_ising* H, int threads, int blocks_per_sm) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_set_launch: NULL handle");
+    if (threads != 64 && threads != 128 && threads != 256 && threads != 512)
+        return fail(ISG_ERR_ARG, "isg_ising_set_launch: threads must be 64, 128, 256 or 512");
+    if (blocks_per_sm < 0 || blocks_per_sm > 64)
+        return fail(ISG_ERR_ARG, "isg_ising_set_launch: blocks_per_sm must be 0..64");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    H->threads = threads;
+    H->blocks_per_sm = blocks_per_sm;
+    destroy_graph(H);
+    return configure_launch(H);
+}
+
+// Runs n sweeps' worth of half-sweeps on the live buffers, timing each launch,
+// then restores the spins and the sweep counter.
+static int timed_halfsweeps(isg_ising* H, int n_launches, float* avg_ms) {
+    int8_t* backup = nullptr;
+    ISG_CK(cudaMalloc((void**)&backup, (size_t)H->spin_bytes));
+    unsigned long long ctrl0 = 0;
+    cudaError_t e = cudaMemcpyAsync(backup, H->d_spins, (size_t)H->spin_bytes,
+                                    cudaMemcpyDeviceToDevice, H->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&ctrl0, H->d_ctrl, sizeof(ctrl0), cudaMemcpyDeviceToHost, H->stream);
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    float total = 0.f;
+    for (int i = 0; i < n_launches && e == cudaSuccess; ++i) {
+        e = cudaEventRecord(a, H->stream);
+        launch_half(H, i & 1, i >> 1, 0);
+        if (e == cudaSuccess) e = cudaEventRecord(b, H->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+        total += ms;
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(H->d_spins, backup, (size_t)H->spin_bytes, cudaMemcpyDeviceToDevice,
+                            H->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(H->d_ctrl, &ctrl0, sizeof(ctrl0), cudaMemcpyHostToDevice, H->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    cudaFree(backup);
+    if (e != cudaSuccess) return cuda_fail(e, "timed_halfsweeps");
+    *avg_ms = n_launches > 0 ? total / (float)n_launches : 0.f;
+    return ISG_OK;
+}
+
+int isg_ising_time_halfsweep(isg_ising* H, int n_launches, float* avg_ms) {
+    if (!H || !avg_ms || n_launches < 1)
+        return fail(ISG_ERR_ARG, "isg_ising_time_halfsweep: bad argument");
+    if (!H->temps_set) return fail(ISG_ERR_STATE, "isg_ising_time_halfsweep: temperatures not set");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    return timed_halfsweeps(H, n_launches, avg_ms);
+}
+
+int isg_ising_autotune(isg_ising* H, int* best) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_autotune: NULL handle");
+    if (!H->temps_set) return fail(ISG_ERR_STATE, "isg_ising_autotune: temperatures not set");
+    cudaSetDevice(H->device);
+    const int thr_opts[] = {128, 256, 512};
+    const int bps_opts[] = {1, 2, 4, 8, 16, 0};
+    float best_ms = 1e30f;
+    int bt = H->threads, bb = H->blocks_per_sm;
+    for (int t : thr_opts)
+        for (int b : bps_opts) {
+            if (b > 0 && b * t > 2048) continue;
+            int rc = isg_ising_set_launch(H, t, b);
+            if (rc) return rc;
+            float ms = 0.f;
+            rc = timed_halfsweeps(H, 2, &ms);  // warm
+            if (rc) return rc;
+            rc = timed_halfsweeps(H, 8, &ms);
+            if (rc) return rc;
+            if (ms < best_ms) {
+                best_ms = ms;
+                bt = t;
+                bb = b;
+            }
+        }
+    int rc = isg_ising_set_launch(H, bt, bb);
+    if (rc) return rc;
+    if (best) {
+        best[0] = bt;
+        best[1] = bb;
+    }
+    return ISG_OK;
+}
+
+int isg_ising_sites_per_halfsweep(isg_ising* H, int64_t* sites) {
+    if (!H || !sites) return fail(ISG_ERR_ARG, "isg_ising_sites_per_halfsweep: NULL argument");
+    int64_t n = 0;
+    for (int s = 0; s < H->n_classes; ++s) n += (int64_t)H->P.cls[s].plane_sites * H->R;
+    *sites = n;
+    return ISG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,285 @@
+"""ctypes bindings of the CPU oracle (oracle/isg_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the product package.  Build it with
+`make -C oracle` (done by __graft_entry__.build()).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+_LIB = None
+
+i8p = np.ctypeslib.ndpointer(dtype=np.int8, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = _HERE / "lib" / "liboracle.so"
+        if not path.exists():
+            raise RuntimeError(f"oracle not built: {path} missing (run `make -C oracle`)")
+        L = C.CDLL(str(path))
+        L.or_philox4x32_10.argtypes = [u32p, u32p, u32p]
+        L.or_ising_thresholds.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, u32p]
+        L.or_ising_hot_start.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_uint32, i8p]
+        L.or_ising_halfsweep.argtypes = [C.c_int, C.c_int, i8p, C.c_int, C.c_uint64, C.c_uint32,
+                                         C.c_uint64, u32p]
+        L.or_ising_measure.argtypes = [C.c_int, C.c_int, i8p, C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int64)]
+        L.or_replica_uid.argtypes = [C.c_int, C.c_int]
+        L.or_replica_uid.restype = C.c_uint32
+        L.or_exchange_uid.argtypes = [C.c_int]
+        L.or_exchange_uid.restype = C.c_uint32
+        L.or_exchange.argtypes = [C.c_int, f64p, f64p, i32p, i32p, C.c_int, C.c_uint64, C.c_uint32,
+                                  C.c_uint64]
+        L.or_exchange.restype = C.c_int64
+        L.or_ising_pt.argtypes = [C.c_int, C.c_int, C.c_int, i8p, f64p, C.c_double, C.c_double,
+                                  C.c_uint64, i32p, i32p, u64p, u64p, u64p, i64p, C.c_int64,
+                                  C.c_int64, C.c_int, C.c_int, i32p, i64p, i64p, C.c_int64]
+        L.or_ising_pt.restype = C.c_int64
+        L.or_ref_run.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                                 C.c_int64, C.c_int64, f64p, f64p]
+        L.or_ref_bench.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int64, C.c_int, C.c_uint64,
+                                   C.POINTER(C.c_double)]
+        L.or_ref_bench.restype = C.c_double
+        L.or_replay_bench.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int64, C.c_int, C.c_uint64,
+                                      C.POINTER(C.c_double)]
+        L.or_replay_bench.restype = C.c_double
+        L.or_jackknife.argtypes = [f64p, f64p, C.c_int64, C.c_double, C.c_double, C.c_int, f64p]
+        L.or_refbench_create.argtypes = [i32p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                                         C.c_uint64]
+        L.or_refbench_create.restype = C.c_void_p
+        L.or_refbench_step.argtypes = [C.c_void_p, C.c_double, C.POINTER(C.c_double)]
+        L.or_refbench_step.restype = C.c_double
+        L.or_refbench_destroy.argtypes = [C.c_void_p]
+        if hasattr(L, "or_cont_hot_start"):
+            _bind_cont(L)
+        _LIB = L
+    return _LIB
+
+
+def _bind_cont(L):
+    L.or_cont_hot_start.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_uint32, f64p]
+    L.or_cont_overrelax.argtypes = [C.c_int, C.c_int, f64p, C.c_int, C.c_double]
+    L.or_cont_metropolis.argtypes = [C.c_int, C.c_int, f64p, C.c_int, C.c_uint64, C.c_uint32,
+                                     C.c_uint64, C.c_double, C.c_double, C.c_double,
+                                     C.POINTER(C.c_int64)]
+    L.or_cont_measure.argtypes = [C.c_int, C.c_int, f64p, f64p]
+    L.or_cont_ref_run.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_uint64,
+                                  C.c_int64, C.c_int64, f64p, f64p]
+
+
+def nsites(L: int, dim: int = 3) -> int:
+    return L ** dim
+
+
+def philox(ctr, key) -> np.ndarray:
+    out = np.zeros(4, np.uint32)
+    lib().or_philox4x32_10(np.asarray(ctr, np.uint32), np.asarray(key, np.uint32), out)
+    return out
+
+
+def thresholds(dim: int, beta: float, J: float = 1.0, h: float = 0.0) -> np.ndarray:
+    out = np.zeros(16, np.uint32)
+    lib().or_ising_thresholds(dim, beta, J, h, out)
+    return out
+
+
+def replica_uid(L: int, r: int) -> int:
+    return int(lib().or_replica_uid(L, r))
+
+
+def hot_start(L: int, dim: int, seed: int, r: int) -> np.ndarray:
+    s = np.zeros(nsites(L, dim), np.int8)
+    lib().or_ising_hot_start(L, dim, seed, replica_uid(L, r), s)
+    return s
+
+
+def halfsweep(spins: np.ndarray, L: int, dim: int, colour: int, seed: int, r: int, sweep: int,
+              thr: np.ndarray) -> None:
+    lib().or_ising_halfsweep(L, dim, spins, colour, seed, replica_uid(L, r), sweep, thr)
+
+
+def measure(spins: np.ndarray, L: int, dim: int = 3) -> tuple[int, int]:
+    b, m = C.c_int64(), C.c_int64()
+    lib().or_ising_measure(L, dim, spins, C.byref(b), C.byref(m))
+    return b.value, m.value
+
+
+class IsingPT:
+    """Replay of one lattice size of the GPU PT protocol (bit-exact oracle)."""
+
+    def __init__(self, L: int, dim: int, R: int, temps, seed: int, J: float = 1.0, h: float = 0.0):
+        self.L, self.dim, self.R, self.seed, self.J, self.h = L, dim, R, seed, J, h
+        self.temps = np.ascontiguousarray(temps, np.float64)
+        self.spins = np.concatenate([hot_start(L, dim, seed, r) for r in range(R)])
+        self.r2t = np.arange(R, dtype=np.int32)
+        self.t2r = np.arange(R, dtype=np.int32)
+        self.gsweep = np.zeros(1, np.uint64)
+        self.ksample = np.zeros(1, np.uint64)
+        self.xcount = np.zeros(1, np.uint64)
+        self.accepted = np.zeros(1, np.int64)
+
+    def replica_spins(self, r: int) -> np.ndarray:
+        n = nsites(self.L, self.dim)
+        return self.spins[r * n:(r + 1) * n]
+
+    def warmup(self, n: int) -> None:
+        z32 = np.zeros(1, np.int32)
+        z64 = np.zeros(1, np.int64)
+        lib().or_ising_pt(self.L, self.dim, self.R, self.spins, self.temps, self.J, self.h,
+                          self.seed, self.r2t, self.t2r, self.gsweep, self.ksample, self.xcount,
+                          self.accepted, n, 0, 1, 1, z32, z64, z64, 0)
+
+    def reset_sampling(self) -> None:
+        self.ksample[:] = 0
+        self.xcount[:] = 0
+        self.accepted[:] = 0
+
+    def sample(self, n: int, exchange_every: int, measure_every: int):
+        rows = n // measure_every + 2
+        rt = np.zeros(rows * self.R, np.int32)
+        rb = np.zeros(rows * self.R, np.int64)
+        rm = np.zeros(rows * self.R, np.int64)
+        got = lib().or_ising_pt(self.L, self.dim, self.R, self.spins, self.temps, self.J, self.h,
+                                self.seed, self.r2t, self.t2r, self.gsweep, self.ksample,
+                                self.xcount, self.accepted, 0, n, exchange_every, measure_every,
+                                rt, rb, rm, rows)
+        k = got * self.R
+        return rt[:k].reshape(got, self.R), rb[:k].reshape(got, self.R), rm[:k].reshape(got, self.R)
+
+
+def ref_run(L: int, dim: int, T: float, seed: int, warmup: int, samples: int, J=1.0, h=0.0):
+    e = np.zeros(samples, np.float64)
+    m = np.zeros(samples, np.float64)
+    lib().or_ref_run(L, dim, T, J, h, seed, warmup, samples, e, m)
+    return e, m
+
+
+def ref_bench(L: int, dim: int, T: float, sweeps: int, threads: int, seed: int = 42):
+    flips = C.c_double()
+    sec = lib().or_ref_bench(L, dim, T, sweeps, threads, seed, C.byref(flips))
+    return sec, flips.value
+
+
+def replay_bench(L: int, dim: int, T: float, sweeps: int, threads: int, seed: int = 42):
+    flips = C.c_double()
+    sec = lib().or_replay_bench(L, dim, T, sweeps, threads, seed, C.byref(flips))
+    return sec, flips.value
+
+
+class RefBench:
+    """Reference CPU path (random-site Metropolis) on `threads` host threads,
+    each owning one replica of every size; step(sweeps) -> (seconds, flips)."""
+
+    def __init__(self, sizes, dim, tmin, tmax, threads, seed=42):
+        self.threads = threads
+        self._h = lib().or_refbench_create(np.ascontiguousarray(sizes, np.int32), len(sizes), dim,
+                                           tmin, tmax, threads, seed)
+
+    def step(self, sweeps: float = 1.0):
+        f = C.c_double()
+        sec = lib().or_refbench_step(self._h, float(sweeps), C.byref(f))
+        return sec, f.value
+
+    def close(self):
+        if self._h:
+            lib().or_refbench_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def jackknife(e, m, beta: float, n3: float, n_blocks: int) -> np.ndarray:
+    e = np.ascontiguousarray(e, np.float64)
+    m = np.ascontiguousarray(m, np.float64)
+    out = np.zeros(12, np.float64)
+    lib().or_jackknife(e, m, len(e), beta, n3, n_blocks, out)
+    return out
+
+
+def exchange(betas, energies, r2t, t2r, parity: int, seed: int, L: int, xcount: int) -> int:
+    return int(lib().or_exchange(len(betas), np.ascontiguousarray(betas, np.float64),
+                                 np.ascontiguousarray(energies, np.float64), r2t, t2r, parity,
+                                 seed, lib().or_exchange_uid(L), xcount))
+
+
+# ---------------------------------------------------------------- numpy formulas
+# Restated from analysis/scripts/reproduce_validation.py (reference).
+
+def onsager_energy(T: float, J: float = 1.0) -> float:
+    """reproduce_validation.py:71-77."""
+    from scipy.special import ellipk
+    k = J / T
+    ek = 2 * np.sinh(2 * k) / np.cosh(2 * k) ** 2
+    return float(-J * (1.0 / np.tanh(2 * k)) * (1 + (2 / np.pi) * (2 * np.tanh(2 * k) ** 2 - 1)
+                                                 * ellipk(ek ** 2)))
+
+
+def onsager_magnetization(T: float, J: float = 1.0) -> float:
+    """reproduce_validation.py:80-85."""
+    tc = 2 * J / np.log(1 + np.sqrt(2))
+    if T >= tc:
+        return 0.0
+    k = J / T
+    return float((1 - np.sinh(2 * k) ** (-4)) ** (1 / 8))
+
+
+def exact_enumeration(L: int, dim: int, temps, J: float = 1.0) -> list[dict]:
+    """All 2^(L^dim) states, periodic forward bonds; reproduce_validation.py:88-140
+    (2D) generalised to a cubic lattice.  Returns E, M(|m|), M2, M4, Cv, chi_conn per T."""
+    n = L ** dim
+    states = np.arange(2 ** n, dtype=np.int64)
+    spins = (((states[:, None] >> np.arange(n)) & 1) * 2 - 1).astype(np.int8)
+    grid = spins.reshape((-1,) + (L,) * dim)
+    bond = np.zeros(len(states), np.int64)
+    for ax in range(1, dim + 1):
+        bond += (grid * np.roll(grid, -1, axis=ax)).reshape(len(states), -1).sum(1)
+    mag = spins.sum(1).astype(np.float64)
+    energies = -J * bond.astype(np.float64)
+    rows = []
+    for T in temps:
+        beta = 1.0 / T
+        lw = -beta * energies
+        w = np.exp(lw - lw.max())
+        w /= w.sum()
+        e = np.sum(w * energies) / n
+        e2 = np.sum(w * energies ** 2) / n ** 2
+        ma = np.sum(w * np.abs(mag)) / n
+        m2 = np.sum(w * mag ** 2) / n ** 2
+        m4 = np.sum(w * mag ** 4) / n ** 4
+        rows.append(dict(T=T, E=e, M=ma, M2=m2, M4=m4, Cv=beta ** 2 * n * (e2 - e ** 2),
+                         chi=beta * n * (m2 - ma ** 2)))
+    return rows
+
+
+def tau_int(x) -> float:
+    """Windowed integrated autocorrelation time, reproduce_validation.py:143-163."""
+    x = np.asarray(x, float)
+    x = x - x.mean()
+    n = len(x)
+    max_lag = n // 4
+    var = np.var(x)
+    if var < 1e-15:
+        return 0.5
+    f = np.fft.rfft(x, 2 * n)
+    acf = np.fft.irfft(f * np.conj(f))[:max_lag]
+    acf /= var * np.arange(n, n - max_lag, -1)
+    tau = 0.5
+    for t in range(1, len(acf)):
+        tau += acf[t]
+        if t >= 6 * tau:
+            break
+    return float(tau)

@@ -1,0 +1,25 @@
+"""Copies the reference's committed result tables into tests/golden/.
+
+Run in a container where faulknco/ising-rs is checked out (default
+/root/reference).  Sources:
+  analysis/data/gpu_windows_pipeline/publication/gpu_fss_{ising,heisenberg,xy}_N*_summary.csv
+      PT summaries from the reference's own GPU path (scripts/run_gpu_publication.sh:22-50)
+  results/published/classical_validation_full_v1/analysis/data/derived/validation/*.csv
+      exact-enumeration, Onsager and known-limit tables (analysis/scripts/reproduce_validation.py)
+The files are copied byte for byte; tests read only these copies.
+"""
+import shutil
+import sys
+from pathlib import Path
+
+REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+OUT = Path(__file__).resolve().parent
+
+pub = REF / "analysis/data/gpu_windows_pipeline/publication"
+for f in sorted(pub.glob("gpu_fss_*_summary.csv")):
+    shutil.copyfile(f, OUT / f.name)
+val = REF / "results/published/classical_validation_full_v1/analysis/data/derived/validation"
+for name in ["exact_enumeration_comparison.csv", "onsager_comparison.csv",
+             "known_limits_summary.csv", "validation_metrics.csv"]:
+    shutil.copyfile(val / name, OUT / name)
+print("copied to", OUT)

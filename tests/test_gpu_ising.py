@@ -1,0 +1,236 @@
+"""GPU parity of the Ising path: bit-exact against the CPU checkerboard/Philox
+replay (spins, integer bond sums and magnetisations, PT records, exchange
+labels), then size-independent properties at the production sizes and
+statistical agreement with the reference's own GPU summaries."""
+from __future__ import annotations
+
+import ctypes
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden_summary
+
+pytestmark = pytest.mark.gpu
+
+TEMPS3 = [4.40 + (4.62 - 4.40) * i / 31 for i in range(32)]
+
+
+def grid(tmin, tmax, n):
+    return [tmin + (tmax - tmin) * i / (n - 1) for i in range(n)]
+
+
+# ------------------------------------------------------------ Philox pin
+def test_philox_matches_curand(gpu, oracle, tmp_path):
+    """The oracle's Philox4x32-10 equals curand's block function."""
+    so = tmp_path / "libcp.so"
+    subprocess.run(["nvcc", "-gencode=arch=compute_103a,code=sm_103a", "-shared", "-Xcompiler",
+                    "-fPIC", "-o", str(so), str(ROOT / "tests/cuda/philox_curand.cu")], check=True)
+    lib = ctypes.CDLL(str(so))
+    rng = np.random.default_rng(0)
+    n = 4096
+    ctr = rng.integers(0, 2 ** 32, (n, 4), dtype=np.uint64).astype(np.uint32)
+    key = rng.integers(0, 2 ** 32, (n, 2), dtype=np.uint64).astype(np.uint32)
+    ctr[0] = 0
+    key[0] = 0
+    ctr[1] = 0xFFFFFFFF
+    key[1] = 0xFFFFFFFF
+    out = np.zeros((n, 4), np.uint32)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    assert lib.curand_philox_blocks(p(ctr), p(key), p(out), n) == 0
+    for i in range(n):
+        assert np.array_equal(oracle.philox(ctr[i], key[i]), out[i]), i
+
+
+# ------------------------------------------------------------ bit-exact
+@pytest.mark.parametrize("dim,sizes", [(3, [2, 4, 6, 8, 10, 16, 32]), (2, [4, 6, 8, 16, 32, 64])])
+def test_hot_start_bit_exact(gpu, oracle, dim, sizes):
+    b = gpu.IsingBatch(sizes, 3, seed=1234567890123, dim=dim)
+    for s, L in enumerate(sizes):
+        for r in range(3):
+            assert np.array_equal(b.get_spins(s, r), oracle.hot_start(L, dim, 1234567890123, r))
+
+
+@pytest.mark.parametrize("dim,sizes,h", [(3, [2, 4, 6, 8, 10, 16, 32], 0.0),
+                                         (3, [4, 8, 16], 0.35),
+                                         (2, [4, 6, 8, 16, 32, 64], 0.0)])
+def test_sweeps_bit_exact(gpu, oracle, dim, sizes, h):
+    R, seed, J = 3, 42, 1.0
+    temps = [2.0, 4.5, 7.0] if dim == 3 else [1.5, 2.269, 3.5]
+    b = gpu.IsingBatch(sizes, R, seed=seed, dim=dim)
+    b.set_temperatures(temps, J=J, h=h)
+    ref = {(s, r): oracle.hot_start(L, dim, seed, r) for s, L in enumerate(sizes) for r in range(R)}
+    thr = [oracle.thresholds(dim, 1.0 / T, J, h) for T in temps]
+    for sweep in range(7):
+        b.step(1)
+        for (s, r), sp in ref.items():
+            for c in (0, 1):
+                oracle.halfsweep(sp, sizes[s], dim, c, seed, r, sweep, thr[r])
+    bond, mag = b.measure()
+    for (s, r), sp in ref.items():
+        assert np.array_equal(b.get_spins(s, r), sp), (sizes[s], r)
+        ob, om = oracle.measure(sp, sizes[s], dim)
+        assert bond[s * R + r] == ob and mag[s * R + r] == om
+
+
+def test_set_spins_roundtrip_and_ordered_limits(gpu, oracle):
+    """Ground state: E = -3 (3D) / -2 (2D) per site, |m| = 1 at T = 0.1
+    (known_limits_summary.csv, observables.rs:189-216)."""
+    for dim, sizes, e0 in [(3, [8, 16], -3.0), (2, [16, 32], -2.0)]:
+        b = gpu.IsingBatch(sizes, 2, seed=5, dim=dim)
+        b.set_temperatures([0.1, 0.1])
+        for s, L in enumerate(sizes):
+            for r in range(2):
+                b.set_spins(s, r, np.ones(L ** dim, np.int8))
+                assert np.all(b.get_spins(s, r) == 1)
+        b.step(100)
+        bond, mag = b.measure()
+        for s, L in enumerate(sizes):
+            n = L ** dim
+            for r in range(2):
+                assert -bond[s * 2 + r] / n == e0 and abs(mag[s * 2 + r]) / n == 1.0
+
+
+@pytest.mark.parametrize("ee,me", [(10, 5), (3, 2), (1, 1), (7, 3)])
+def test_pt_run_bit_exact(gpu, oracle, ee, me):
+    """Records (slot, bond, mag), exchange labels and final spins of a PT run
+    through the CUDA graph equal the oracle's replay."""
+    sizes, R, dim, seed = [8, 12, 16], 8, 3, 99
+    temps = grid(4.3, 4.7, R)
+    b = gpu.IsingBatch(sizes, R, seed=seed, dim=dim)
+    b.set_temperatures(temps)
+    b.step(15)
+    b.reset_sampling()
+    parts = [b.pt_run(n, ee, me) for n in (23, 40, 1, 36)]
+    rt = np.concatenate([p[0] for p in parts])
+    rb = np.concatenate([p[1] for p in parts])
+    rm = np.concatenate([p[2] for p in parts])
+    r2t = b.r2t()
+    for s, L in enumerate(sizes):
+        pt = oracle.IsingPT(L, dim, R, temps, seed)
+        pt.warmup(15)
+        pt.reset_sampling()
+        ot, ob, om = pt.sample(100, ee, me)
+        sl = slice(s * R, (s + 1) * R)
+        assert rt.shape[0] == ot.shape[0]
+        assert np.array_equal(rt[:, sl], ot)
+        assert np.array_equal(rb[:, sl], ob)
+        assert np.array_equal(rm[:, sl], om)
+        assert np.array_equal(r2t[sl], pt.r2t)
+        for r in range(R):
+            assert np.array_equal(b.get_spins(s, r), pt.replica_spins(r))
+    acc = b.accepted()
+    assert np.all(acc > 0)
+
+
+def test_exchange_api_matches_oracle(gpu, oracle):
+    sizes, R, seed = [8, 16], 6, 7
+    temps = grid(4.0, 5.0, R)
+    b = gpu.IsingBatch(sizes, R, seed=seed)
+    b.set_temperatures(temps)
+    betas = 1.0 / np.array(temps)
+    r2t_o = [np.arange(R, dtype=np.int32) for _ in sizes]
+    t2r_o = [np.arange(R, dtype=np.int32) for _ in sizes]
+    for k in range(12):
+        b.step(3)
+        bond, mag = b.measure()
+        acc = b.exchange(k % 2)
+        for s, L in enumerate(sizes):
+            en = -bond[s * R:(s + 1) * R].astype(np.float64)
+            a = oracle.exchange(betas, en, r2t_o[s], t2r_o[s], k % 2, seed, L, k)
+            assert a == acc[s]
+        got = b.r2t()
+        for s in range(len(sizes)):
+            assert np.array_equal(got[s * R:(s + 1) * R], r2t_o[s])
+
+
+# ------------------------------------------------------------ full-size properties
+def test_production_size_properties(gpu, oracle):
+    """Production configuration (L = 8..128, 32 replicas): fused measurement
+    equals the standalone reduction, spins stay +-1, runs are deterministic and
+    launch-shape independent, and L = 128 replicas match the replay bit for bit."""
+    sizes, R = [8, 16, 32, 64, 128], 32
+    a = gpu.IsingBatch(sizes, R, seed=42)
+    a.set_temperatures(TEMPS3)
+    a.step(20)
+    a.reset_sampling()
+    rt, rb, rm = a.pt_run(10, 10, 5)
+    bond, mag = a.measure()
+    assert np.array_equal(rb[-1], bond) and np.array_equal(rm[-1], mag)
+    s = a.get_spins(4, 31)
+    assert set(np.unique(s)) <= {-1, 1}
+    c = gpu.IsingBatch(sizes, R, seed=42)
+    c.set_temperatures(TEMPS3)
+    c.set_launch(128, 2)
+    c.step(20)
+    c.reset_sampling()
+    rt2, rb2, rm2 = c.pt_run(10, 10, 5)
+    assert np.array_equal(rb, rb2) and np.array_equal(rm, rm2) and np.array_equal(rt, rt2)
+    for si in (0, 4):
+        for r in (0, 17):
+            assert np.array_equal(a.get_spins(si, r), c.get_spins(si, r))
+    # full-size bit-exactness: L = 128 replicas against the replay
+    d = gpu.IsingBatch([128], 2, seed=3)
+    d.set_temperatures([4.5, 4.6])
+    d.step(2)
+    for r, T in enumerate([4.5, 4.6]):
+        sp = oracle.hot_start(128, 3, 3, r)
+        thr = oracle.thresholds(3, 1.0 / T)
+        for k in range(2):
+            for colour in (0, 1):
+                oracle.halfsweep(sp, 128, 3, colour, 3, r, k, thr)
+        assert np.array_equal(d.get_spins(0, r), sp)
+
+
+def test_autotune_keeps_results(gpu):
+    sizes, R = [8, 32, 64], 16
+    a = gpu.IsingBatch(sizes, R, seed=1)
+    a.set_temperatures(grid(4.4, 4.6, R))
+    a.step(5)
+    ref = [a.get_spins(2, r) for r in range(R)]
+    best = a.autotune()
+    assert best[0] in (128, 256, 512)
+    for r in range(R):
+        assert np.array_equal(a.get_spins(2, r), ref[r])
+    assert a.sweep_counter() == 5
+    ms = a.time_halfsweep(6)
+    assert ms > 0
+    for r in range(R):
+        assert np.array_equal(a.get_spins(2, r), ref[r])
+
+
+# ------------------------------------------------------------ statistics
+@pytest.mark.parametrize("L", [8, 16])
+def test_pt_statistics_match_reference_gpu_csv(gpu, L):
+    """Same grid/cadence as the reference's production run
+    (scripts/run_gpu_publication.sh:22-29): E, |M|, M2, chi agree with the
+    reference's own GPU summary CSV within combined jackknife errors."""
+    from helpers import pt_summary
+    g = golden_summary("ising", L)
+    b = gpu.IsingBatch([L], 32, seed=2024)
+    b.set_temperatures(TEMPS3)
+    b.step(5000)
+    b.reset_sampling()
+    rt, rb, rm = b.pt_run(50000, 10, 5)
+    s = pt_summary(rt, -rb.astype(float), rm, L, TEMPS3)
+    for key in ("E", "M", "M2", "chi"):
+        z = (s[key] - g[key]) / np.sqrt(s[key + "_err"] ** 2 + g[key + "_err"] ** 2)
+        assert np.all(np.abs(z) < 5.0), (key, z)
+        assert np.mean(z ** 2) < 3.0, (key, np.mean(z ** 2))
+
+
+def test_lattice_gpu_mirror(gpu, oracle):
+    """LatticeGpu.step / measure_gpu / energy_gpu mirror lattice_gpu.rs."""
+    lat = gpu.LatticeGpu(8, 42)
+    sp = oracle.hot_start(8, 3, 42, 0)
+    thr = oracle.thresholds(3, 1 / 4.5, 1.0, 0.0)
+    for k in range(5):
+        lat.step(1 / 4.5, 1.0, 0.0)
+        for c in (0, 1):
+            oracle.halfsweep(sp, 8, 3, c, 42, 0, k, thr)
+    assert np.array_equal(lat.get_spins(), sp)
+    bnd, mag = oracle.measure(sp, 8)
+    e, m = lat.measure_gpu(1.0)
+    assert e == -bnd / 512 and m == abs(mag) / 512
+    assert lat.energy_gpu(1.0) == -bnd

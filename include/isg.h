@@ -3,7 +3,7 @@
  * parallel-tempering engine for periodic cubic (and square) lattices.
  *
  * This is the drop-in boundary for the GPU backend of faulknco/ising-rs
- * (src/cuda/*.rs + src/parallel_tempering.rs).  Each entry point names the
+ * (the Rust modules of src/cuda/ and src/parallel_tempering.rs).  Each entry point names the
  * reference interface it replaces.  Conventions:
  *
  *   - Every function returns an int status: ISG_OK (0) or a negative ISG_ERR_*
@@ -20,11 +20,13 @@
  * Random numbers (one definition shared by the kernels and any replay):
  *   Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), key = {lo32(seed),
  *   hi32(seed)}, counter = {c0, c1, c2, c3} with
- *     c1 = stream uid: (L << 16) | replica  for a lattice replica,
+ *     c0 = stream uid: (L << 16) | replica  for a lattice replica,
  *                      (L << 16) | 0xFFFF   for the exchange stream of size L,
- *     c3 = (tag << 24) | (colour << 16) | (hi32(step) & 0xFFFF),
+ *     c1 = index (per tag below),
  *     c2 = lo32(step),
- *   and tag / c0 / step as listed with the ISG_TAG_* constants below.
+ *     c3 = (tag << 24) | (colour << 16) | (hi32(step) & 0xFFFF).
+ *   Only c1 varies across a warp, so the first rounds of every block are
+ *   largely warp-uniform and are computed once per replica.
  */
 #ifndef ISG_H
 #define ISG_H
@@ -45,18 +47,18 @@ extern "C" {
 #define ISG_ERR_STATE       -5  /* call order (temperatures not set, ...)           */
 
 /* Philox stream tags (c3 bits 24..31).
- *  INIT : hot start.  c0 = natural site index / 4, step = 0; word (site & 3);
+ *  INIT : hot start.  c1 = natural site index / 4, step = 0; word (site & 3);
  *         spin = -1 if the word's top bit is set, else +1.
- *  ISING: Metropolis half-sweep.  c0 = colour index / 4 (colour index of
+ *  ISING: Metropolis half-sweep.  c1 = colour index / 4 (colour index of
  *         site (x,y,z) = (z*L*L + y*L + x) >> 1), step = global sweep number,
  *         colour = 0 (x+y+z even) or 1; word (colour index & 3) is u, and the
  *         flip is accepted iff u <= threshold[own_down*8 + n_down_neighbours]
  *         with threshold = 0xFFFFFFFF for dE <= 0, else
  *         max(floor(exp(-beta*dE) * 2^32), 1) - 1  (FP64 on the host).
- *  EXCH : replica exchange.  c0 = lower temperature index of the pair,
- *         c1 = exchange uid, step = exchange count of that size;
+ *  EXCH : replica exchange.  c1 = lower temperature index of the pair,
+ *         c0 = exchange uid, step = exchange count of that size;
  *         u = ((w0 << 32 | w1) >> 11) * 2^-53.
- *  CINIT/CMETRO: continuous spins, c0 = natural site index (CINIT) or colour
+ *  CINIT/CMETRO: continuous spins, c1 = natural site index (CINIT) or colour
  *         index (CMETRO), one Philox call per site.
  */
 #define ISG_TAG_INIT   0x01u
@@ -168,6 +170,70 @@ int isg_ising_time_halfsweep(isg_ising* h, int n_launches, float* avg_ms);
 
 /* Sites updated by one half-sweep launch (all sizes and replicas). */
 int isg_ising_sites_per_halfsweep(isg_ising* h, int64_t* sites);
+
+/* ------------------------------------------------------------------------ */
+/* Continuous spins: O(3) Heisenberg (n_comp 3) and O(2) XY (n_comp 2)        */
+/* ------------------------------------------------------------------------ */
+typedef struct isg_cont isg_cont;
+
+/* Replaces ContinuousGpuLattice::new(n, n_comp, seed, device)
+ * (src/cuda/gpu_lattice_continuous.rs:24-88) for every (size, replica) of a
+ * run.  FP32 unit vectors start uniform on the sphere (O(3): z and phi
+ * uniform) or at a uniform angle (O(2)) from the ISG_TAG_CINIT stream. */
+int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas, int n_comp,
+                    uint64_t seed);
+int isg_cont_destroy(isg_cont* h);
+int isg_cont_set_stream(isg_cont* h, void* cuda_stream);
+/* Temperature grid per size (as isg_ising_set_temperatures) and coupling J. */
+int isg_cont_set_temperatures(isg_cont* h, const double* temps, double J);
+
+/* n_sweeps sweeps, each n_overrelax overrelaxation sweeps then one Metropolis
+ * sweep (the reference GPU order, gpu_lattice_continuous.rs:112-173); the
+ * Metropolis proposal rotates the spin uniformly inside a cone of half-angle
+ * delta (O(2): angle step uniform in [-delta, delta]).  Replaces
+ * ContinuousGpuLattice::sweep. */
+int isg_cont_sweep(isg_cont* h, int64_t n_sweeps, double delta, int n_overrelax);
+/* Single half-sweeps: overrelaxation (continuous_spin_kernel.cu:88-142) and
+ * Metropolis (continuous_spin_kernel.cu:9-83) of one colour. */
+int isg_cont_overrelax(isg_cont* h, int colour);
+int isg_cont_metropolis(isg_cont* h, int colour, double delta);
+/* Rescale every spin to unit length. */
+int isg_cont_normalize(isg_cont* h);
+
+/* Observables of every replica, synchronous: energy[r] = -J sum_bonds S.S',
+ * mag[r*3 + k] = sum S_k (k = 2 is 0 for XY), bonds[r*6 + a] (may be NULL) =
+ * sum_i S_i.S_{i+a} for a = x, y, z, then sum_i (S_i x S_{i+a})_z: the
+ * helicity-modulus sums.  Compensated FP32 per block, FP64 combine in a fixed
+ * order (deterministic).  Replaces ContinuousGpuLattice::measure_gpu
+ * (gpu_lattice_continuous.rs:177-240; reduce_kernel.cu:70-151). */
+int isg_cont_measure(isg_cont* h, double* energy, double* mag, double* bonds);
+/* Exchange pass on the energies of the last measurement (as
+ * isg_ising_exchange; src/parallel_tempering.rs:5-36). */
+int isg_cont_exchange(isg_cont* h, int parity, int64_t* accepted);
+int isg_cont_reset_sampling(isg_cont* h);
+
+/* PT sampling as isg_ising_pt_run, with renormalisation of every spin on
+ * sweeps k where (global sweep + 1) % renorm_every == 0 (0 = never).
+ * Records: slot, energy, mag[3], bonds[6] per replica per measured sweep.
+ * Replaces the sampling loop of run_continuous_fss (gpu_fss.rs:494-545). */
+int isg_cont_pt_run(isg_cont* h, int64_t n_sweeps, int exchange_every, int measure_every,
+                    double delta, int n_overrelax, int renorm_every, int32_t* tslot_rec,
+                    double* energy_rec, double* mag_rec, double* bonds_rec, int64_t max_records,
+                    int64_t* n_records);
+int isg_cont_get_r2t(isg_cont* h, int32_t* r2t);
+/* Natural-layout spins, n_comp floats per site interleaved as the reference
+ * stores them (continuous_spin_kernel.cu:6). */
+int isg_cont_get_spins(isg_cont* h, int size_index, int replica, float* out);
+int isg_cont_set_spins(isg_cont* h, int size_index, int replica, const float* in);
+/* Exchange swaps accepted per size; Metropolis moves accepted per replica. */
+int isg_cont_get_accepted(isg_cont* h, int64_t* accepted);
+int isg_cont_get_metro_accepted(isg_cont* h, int64_t* accepted);
+int isg_cont_sync(isg_cont* h);
+/* Mean device ms of one overrelaxation half-sweep, one Metropolis half-sweep
+ * and one measurement (out[3]); the lattices are restored afterwards. */
+int isg_cont_time_kernels(isg_cont* h, int n, float* out_ms);
+/* Site updates of one full sweep of one kind (all sizes and replicas). */
+int isg_cont_sites_per_sweep(isg_cont* h, int64_t* sites);
 
 /* ------------------------------------------------------------------------ */
 /* Statistics used by the drop-in driver                                     */

@@ -83,7 +83,7 @@ def build_all(verbose: bool = False) -> Path:
     so = LIB / "libisinggb.so"
     _run_parallel([[nvcc, ARCH, "-shared", "-o", str(so), *map(str, objs)]])
     driver = PKG / "host" / "gpu_fss.cpp"
-    if driver.exists():
+    if driver.exists() and (CSRC / "isg_cont.cu").exists():
         _run_parallel([[cxx, *CXX_FLAGS, "-I", str(INCLUDE), str(driver), "-o", str(BIN / "gpu_fss"),
                         "-L", str(LIB), "-lisinggb", "-Wl,-rpath,$ORIGIN/../lib"]])
     return so

@@ -1,0 +1,1166 @@
+// isg_cont.cu — continuous-spin O(n) models (n = 3 Heisenberg, n = 2 XY) on
+// periodic cubic lattices: checkerboard Metropolis with a cone proposal,
+// microcanonical overrelaxation, deterministic compensated-FP32 observables
+// with an FP64 combine, device replica exchange and the PT cycle as a graph.
+//
+// Reference path being replaced (faulknco/ising-rs):
+//   src/cuda/continuous_spin_kernel.cu:9-142  Metropolis + overrelaxation
+//   src/cuda/reduce_kernel.cu:70-151          vector M and energy partials
+//   src/cuda/gpu_lattice_continuous.rs:24-240 ContinuousGpuLattice
+//   src/bin/gpu_fss.rs:414-582                run_continuous_fss
+// Proposal: a uniform rotation inside a cone of half-angle delta around the
+// current spin (the reference CPU proposal, heisenberg/metropolis.rs:54-92;
+// the reference GPU kernel perturbs in a box and renormalises,
+// continuous_spin_kernel.cu:58-71).  XY: angle step uniform in
+// [-delta, delta] (delta >= pi gives a uniform new angle).
+//
+// Layout in HBM: per (size, replica) lattice, FP32 component planes split by
+// colour: [colour][component][L^3/2] floats, colour index (z*L*L+y*L+x) >> 1,
+// so a warp reads 128 contiguous bytes per component.  XY spins are stored as
+// (cos, sin) pairs (8 B/site): every neighbour field is then a plain sum, with
+// no trigonometry per neighbour.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "isg_common.cuh"
+
+namespace isg {
+
+constexpr int kCMaxClasses = 16;
+constexpr int kCMaxReplicas = 1024;
+constexpr int kCThreads = 256;
+constexpr int kMeasureChunk = 1024;  // colour-1 sites per measure block
+constexpr int kNQ = 10;              // E, Mx, My, Mz, Cx, Cy, Cz, Sx, Sy, Sz
+
+// n / d for n < 2^31 by multiply-high (Hacker's Delight, round-up method).
+struct FastDiv {
+    uint32_t d, m, s;
+};
+static FastDiv make_div(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    uint32_t l = 0;
+    while ((1ull << l) < d) ++l;
+    f.s = l;
+    f.m = (uint32_t)((((1ull << l) - d) << 32) / d + 1);
+    return f;
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+    return (__umulhi(n, f.m) + n) >> f.s;
+}
+
+struct ContClass {
+    int L;
+    int R;
+    uint32_t plane_sites;
+    FastDiv div_half;  // L/2
+    FastDiv div_L;
+    int rep_base;
+    int64_t off;        // float offset of replica 0
+    int64_t site_base;  // flattened colour-plane sites
+    int64_t site_end;
+    int chunk_base;
+    int chunks_per_rep;
+};
+
+struct ContParams {
+    float* spins;
+    const float* betaf;  // per slot
+    const int32_t* r2t;
+    unsigned long long* ctrl;  // [0] sweep base
+    unsigned long long* metro_acc;
+    double* partials;          // [chunks][kNQ]
+    uint64_t seed;
+    float J;
+    int n_classes;
+    int renorm;
+    int64_t total_sites;
+    int total_chunks;
+    ContClass cls[kCMaxClasses];
+};
+
+struct SiteRef {
+    int ci, r, rg;
+    uint32_t i, x, y, z;
+};
+
+template <int NC>
+__device__ __forceinline__ int64_t plane_off(const ContClass& C, int r, int colour, int comp) {
+    return C.off + (int64_t)r * 2 * NC * C.plane_sites +
+           (int64_t)(colour * NC + comp) * C.plane_sites;
+}
+
+__device__ __forceinline__ SiteRef locate(const ContParams& P, int64_t g, int colour) {
+    SiteRef s;
+    int ci = 0;
+    while (P.cls[ci].site_end <= g) ++ci;
+    const ContClass& C = P.cls[ci];
+    const int64_t lg = g - C.site_base;
+    s.ci = ci;
+    s.r = (int)(lg / C.plane_sites);
+    s.i = (uint32_t)(lg - (int64_t)s.r * C.plane_sites);
+    s.rg = C.rep_base + s.r;
+    const uint32_t row = fdiv(s.i, C.div_half);
+    const uint32_t k = s.i - row * (uint32_t)(C.L >> 1);
+    s.z = fdiv(row, C.div_L);
+    s.y = row - s.z * (uint32_t)C.L;
+    s.x = 2 * k + ((s.y + s.z + (uint32_t)colour) & 1u);
+    return s;
+}
+
+// Colour indices of the six neighbours of (x,y,z): +x, -x, +y, -y, +z, -z.
+__device__ __forceinline__ void neighbours(uint32_t L, uint32_t x, uint32_t y, uint32_t z,
+                                           uint32_t nb[6]) {
+    const uint32_t xp = x + 1 == L ? 0 : x + 1, xm = x == 0 ? L - 1 : x - 1;
+    const uint32_t yp = y + 1 == L ? 0 : y + 1, ym = y == 0 ? L - 1 : y - 1;
+    const uint32_t zp = z + 1 == L ? 0 : z + 1, zm = z == 0 ? L - 1 : z - 1;
+    const uint32_t row = (z * L + y) * L;
+    nb[0] = (row + xp) >> 1;
+    nb[1] = (row + xm) >> 1;
+    nb[2] = ((z * L + yp) * L + x) >> 1;
+    nb[3] = ((z * L + ym) * L + x) >> 1;
+    nb[4] = ((zp * L + y) * L + x) >> 1;
+    nb[5] = ((zm * L + y) * L + x) >> 1;
+}
+
+// Overrelaxation: S' = 2 (S.h)/|h|^2 h - S about the local field
+// (continuous_spin_kernel.cu:88-142; overrelax.rs:16-49 without the
+// per-update renormalisation).
+template <int NC>
+__global__ void __launch_bounds__(kCThreads) k_cont_or(const __grid_constant__ ContParams P,
+                                                       int colour) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < P.total_sites;
+         g += stride) {
+        const SiteRef s = locate(P, g, colour);
+        const ContClass& C = P.cls[s.ci];
+        uint32_t nb[6];
+        neighbours((uint32_t)C.L, s.x, s.y, s.z, nb);
+        float h[NC], v[NC];
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            const float* o = P.spins + plane_off<NC>(C, s.r, colour ^ 1, k);
+            h[k] = ((__ldg(o + nb[0]) + __ldg(o + nb[1])) + (__ldg(o + nb[2]) + __ldg(o + nb[3]))) +
+                   (__ldg(o + nb[4]) + __ldg(o + nb[5]));
+            v[k] = P.spins[plane_off<NC>(C, s.r, colour, k) + s.i];
+        }
+        float h2 = 0.f, sh = 0.f;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            h2 = fmaf(h[k], h[k], h2);
+            sh = fmaf(v[k], h[k], sh);
+        }
+        if (h2 < 1e-20f) continue;
+        const float scale = 2.0f * sh / h2;
+#pragma unroll
+        for (int k = 0; k < NC; ++k)
+            P.spins[plane_off<NC>(C, s.r, colour, k) + s.i] = fmaf(scale, h[k], -v[k]);
+    }
+}
+
+// Metropolis with the cone proposal; on renormalisation sweeps every site of
+// this colour is written back normalised.
+template <int NC>
+__global__ void __launch_bounds__(kCThreads)
+    k_cont_metro(const __grid_constant__ ContParams P, int colour, int sweep_off, float cos_delta,
+                 float delta) {
+    const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
+    const bool renorm_now = P.renorm > 0 && ((sweep + 1) % (uint64_t)P.renorm) == 0;
+    const uint32_t c2 = (uint32_t)sweep;
+    const uint32_t c3 = counter_word3(ISG_TAG_CMETRO, (uint32_t)colour, sweep);
+    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    for (int64_t g0 = (int64_t)blockIdx.x * blockDim.x; g0 < P.total_sites; g0 += stride) {
+        const int64_t g = g0 + threadIdx.x;
+        bool accepted = false;
+        int rg = -1;
+        if (g < P.total_sites) {
+            const SiteRef s = locate(P, g, colour);
+            const ContClass& C = P.cls[s.ci];
+            rg = s.rg;
+            uint32_t nb[6];
+            neighbours((uint32_t)C.L, s.x, s.y, s.z, nb);
+            float h[NC], v[NC], w[NC];
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                const float* o = P.spins + plane_off<NC>(C, s.r, colour ^ 1, k);
+                h[k] = ((__ldg(o + nb[0]) + __ldg(o + nb[1])) +
+                        (__ldg(o + nb[2]) + __ldg(o + nb[3]))) +
+                       (__ldg(o + nb[4]) + __ldg(o + nb[5]));
+                v[k] = P.spins[plane_off<NC>(C, s.r, colour, k) + s.i];
+            }
+            const U4 u = philox10(replica_uid(C.L, s.r), s.i, c2, c3, k0, k1);
+            if (NC == 3) {
+                // cos(theta) uniform in [cos(delta), 1], phi uniform in [0, 2pi)
+                const float ct = 1.0f - uniform24(u.x) * (1.0f - cos_delta);
+                const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+                float sp, cp;
+                sincospif(2.0f * uniform24(u.y), &sp, &cp);
+                // perpendicular frame (heisenberg/metropolis.rs:72-92)
+                const float tx = fabsf(v[0]) < 0.9f ? 1.0f : 0.0f;
+                const float ty = 1.0f - tx;
+                const float ts = tx * v[0] + ty * v[1];
+                float ux = tx - ts * v[0], uy = ty - ts * v[1], uz = -ts * v[2];
+                const float un = rsqrtf(ux * ux + uy * uy + uz * uz);
+                ux *= un;
+                uy *= un;
+                uz *= un;
+                const float vx = v[1] * uz - v[2] * uy;
+                const float vy = v[2] * ux - v[0] * uz;
+                const float vz = v[0] * uy - v[1] * ux;
+                const float a = st * cp, b = st * sp;
+                w[0] = a * ux + b * vx + ct * v[0];
+                w[1] = a * uy + b * vy + ct * v[1];
+                w[2] = a * uz + b * vz + ct * v[2];
+                const float wn = rsqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) w[k] *= wn;
+            } else {
+                float sd, cd;
+                sincosf(delta * (2.0f * uniform24(u.x) - 1.0f), &sd, &cd);
+                w[0] = v[0] * cd - v[1] * sd;
+                w[1] = v[1] * cd + v[0] * sd;
+            }
+            float dot = 0.f;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) dot = fmaf(w[k] - v[k], h[k], dot);
+            const float dE = -P.J * dot;
+            const float beta = P.betaf[C.rep_base + P.r2t[s.rg]];
+            accepted = dE <= 0.0f || uniform24(u.z) < expf(-beta * dE);
+            if (accepted || renorm_now) {
+                float* out[NC];
+#pragma unroll
+                for (int k = 0; k < NC; ++k) out[k] = P.spins + plane_off<NC>(C, s.r, colour, k);
+                float n2 = 0.f;
+#pragma unroll
+                for (int k = 0; k < NC; ++k) {
+                    if (accepted) v[k] = w[k];
+                    n2 = fmaf(v[k], v[k], n2);
+                }
+                const float sc = renorm_now ? rsqrtf(n2) : 1.0f;
+#pragma unroll
+                for (int k = 0; k < NC; ++k) out[k][s.i] = v[k] * sc;
+            }
+        }
+        // per-replica acceptance count: one atomic per uniform warp
+        const int rg0 = __shfl_sync(ISG_FULL_MASK, rg, 0);
+        if (__all_sync(ISG_FULL_MASK, rg == rg0)) {
+            const unsigned cnt = __popc(__ballot_sync(ISG_FULL_MASK, accepted));
+            if (lane == 0 && rg0 >= 0 && cnt) atomicAdd(&P.metro_acc[rg0], (unsigned long long)cnt);
+        } else if (accepted) {
+            atomicAdd(&P.metro_acc[rg], 1ull);
+        }
+    }
+}
+
+// Compensated FP32 pair (sum, error) with TwoSum addition.
+struct CF {
+    float s, c;
+};
+__device__ __forceinline__ CF cf_add(CF a, float b) {
+    const float t = a.s + b;
+    const float bb = t - a.s;
+    const float err = (a.s - (t - bb)) + (b - bb);
+    return CF{t, a.c + err};
+}
+__device__ __forceinline__ CF cf_merge(CF a, CF b) {
+    CF r = cf_add(a, b.s);
+    r.c += b.c;
+    return r;
+}
+
+// Per block: kMeasureChunk colour-1 sites of one replica.  Each colour-1 site
+// owns its six bonds (every bond has exactly one colour-1 end) and, for M, its
+// colour-0 partner at the same colour index.
+template <int NC>
+__global__ void __launch_bounds__(kCThreads) k_cont_measure(const __grid_constant__ ContParams P) {
+    const int chunk = blockIdx.x;
+    int ci = 0;
+    while (ci + 1 < P.n_classes && P.cls[ci + 1].chunk_base <= chunk) ++ci;
+    const ContClass& C = P.cls[ci];
+    const int lc = chunk - C.chunk_base;
+    const int r = lc / C.chunks_per_rep;
+    const uint32_t start = (uint32_t)(lc - r * C.chunks_per_rep) * kMeasureChunk;
+    const uint32_t L = (uint32_t)C.L;
+    CF acc[kNQ];
+#pragma unroll
+    for (int q = 0; q < kNQ; ++q) acc[q] = CF{0.f, 0.f};
+    for (uint32_t i = start + threadIdx.x; i < min(start + kMeasureChunk, C.plane_sites);
+         i += blockDim.x) {
+        const uint32_t row = fdiv(i, C.div_half);
+        const uint32_t k = i - row * (L >> 1);
+        const uint32_t z = fdiv(row, C.div_L);
+        const uint32_t y = row - z * L;
+        const uint32_t x = 2 * k + ((y + z + 1u) & 1u);
+        uint32_t nb[6];
+        neighbours(L, x, y, z, nb);
+        float s[NC], n[6][NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const float* own = P.spins + plane_off<NC>(C, r, 1, c);
+            const float* oth = P.spins + plane_off<NC>(C, r, 0, c);
+            s[c] = own[i];
+#pragma unroll
+            for (int d = 0; d < 6; ++d) n[d][c] = oth[nb[d]];
+            acc[1 + c] = cf_add(acc[1 + c], s[c] + oth[i]);
+        }
+        float e = 0.f;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            // forward bond (i, i+a) is neighbour 2a, backward bond (i-a, i) is 2a+1
+            float cf = 0.f, cb = 0.f;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                cf = fmaf(s[c], n[2 * a][c], cf);
+                cb = fmaf(s[c], n[2 * a + 1][c], cb);
+            }
+            const float sf = s[0] * n[2 * a][1] - s[1] * n[2 * a][0];
+            const float sb = n[2 * a + 1][0] * s[1] - n[2 * a + 1][1] * s[0];
+            e += cf + cb;
+            acc[4 + a] = cf_add(acc[4 + a], cf + cb);
+            acc[7 + a] = cf_add(acc[7 + a], sf + sb);
+        }
+        acc[0] = cf_add(acc[0], -P.J * e);
+    }
+    // warp then block reduction of the compensated pairs
+    __shared__ CF red[kCThreads / 32][kNQ];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < kNQ; ++q) {
+        CF v = acc[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            CF w{__shfl_down_sync(ISG_FULL_MASK, v.s, o), __shfl_down_sync(ISG_FULL_MASK, v.c, o)};
+            v = cf_merge(v, w);
+        }
+        if (lane == 0) red[wid][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNQ) {
+        CF v = red[0][threadIdx.x];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = cf_merge(v, red[w][threadIdx.x]);
+        P.partials[(int64_t)chunk * kNQ + threadIdx.x] = (double)v.s + (double)v.c;
+    }
+}
+
+// FP64 combine of the block partials of each replica, in chunk order.
+__global__ void k_cont_combine(const __grid_constant__ ContParams P, double* out) {
+    const int rg = blockIdx.x * blockDim.x + threadIdx.x;
+    int ci = 0;
+    while (ci + 1 < P.n_classes && P.cls[ci + 1].rep_base <= rg) ++ci;
+    const ContClass& C = P.cls[ci];
+    if (rg >= C.rep_base + C.R) return;
+    const int r = rg - C.rep_base;
+    double q[kNQ];
+    for (int k = 0; k < kNQ; ++k) q[k] = 0.0;
+    const int c0 = C.chunk_base + r * C.chunks_per_rep;
+    for (int c = 0; c < C.chunks_per_rep; ++c)
+        for (int k = 0; k < kNQ; ++k) q[k] += P.partials[(int64_t)(c0 + c) * kNQ + k];
+    for (int k = 0; k < kNQ; ++k) out[(int64_t)rg * kNQ + k] = q[k];
+}
+
+__global__ void k_cont_init(const __grid_constant__ ContParams P, int nc) {
+    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    const uint32_t c3 = counter_word3(ISG_TAG_CINIT, 0, 0);
+    for (int ci = 0; ci < P.n_classes; ++ci) {
+        const ContClass& C = P.cls[ci];
+        const int64_t nsite = 2 * (int64_t)C.plane_sites;
+        const int64_t total = nsite * C.R;
+        for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+             g += (int64_t)gridDim.x * blockDim.x) {
+            const int r = (int)(g / nsite);
+            const uint32_t n = (uint32_t)(g - (int64_t)r * nsite);
+            const U4 u = philox10(replica_uid(C.L, r), n, 0, c3, k0, k1);
+            const uint32_t L = (uint32_t)C.L;
+            const uint32_t x = n % L, y = (n / L) % L, z = n / (L * L);
+            const int c = (int)((x + y + z) & 1u);
+            float v[3];
+            if (nc == 3) {
+                // z uniform in [-1, 1), phi uniform in [0, 2pi): uniform on S^2
+                const float zz = 2.0f * uniform24(u.x) - 1.0f;
+                float sp, cp;
+                sincospif(2.0f * uniform24(u.y), &sp, &cp);
+                const float rr = sqrtf(fmaxf(0.0f, 1.0f - zz * zz));
+                v[0] = rr * cp;
+                v[1] = rr * sp;
+                v[2] = zz;
+            } else {
+                sincospif(2.0f * uniform24(u.x), &v[1], &v[0]);
+                v[2] = 0.f;
+            }
+            for (int k = 0; k < nc; ++k) {
+                const int64_t o = C.off + (int64_t)r * 2 * nc * C.plane_sites +
+                                  (int64_t)(c * nc + k) * C.plane_sites + (n >> 1);
+                P.spins[o] = v[k];
+            }
+        }
+    }
+}
+
+__global__ void k_cont_normalize(const __grid_constant__ ContParams P, int nc) {
+    for (int ci = 0; ci < P.n_classes; ++ci) {
+        const ContClass& C = P.cls[ci];
+        const int64_t total = 2 * (int64_t)C.plane_sites * C.R;
+        for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+             g += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t rc = g / C.plane_sites;  // replica*2 + colour
+            const int64_t i = g - rc * C.plane_sites;
+            float* b = P.spins + C.off + rc * nc * C.plane_sites + i;
+            float n2 = 0.f;
+            for (int k = 0; k < nc; ++k) n2 = fmaf(b[k * C.plane_sites], b[k * C.plane_sites], n2);
+            const float sc = rsqrtf(n2);
+            for (int k = 0; k < nc; ++k) b[k * C.plane_sites] *= sc;
+        }
+    }
+}
+
+struct ContPost {
+    const double* obs;  // [replicas][kNQ]
+    int32_t* r2t;
+    int32_t* t2r;
+    const double* betas;
+    int32_t* rec_t;
+    double* rec_e;
+    double* rec_m;  // [cap][RT][3]
+    double* rec_h;  // [cap][RT][6]
+    unsigned long long* ctrl;
+    long long ring_cap;
+    uint64_t seed;
+    int R, n_classes, replicas_total;
+    int L[kCMaxClasses];
+};
+
+__global__ void k_cont_post(const __grid_constant__ ContPost Q, int do_record, int do_exchange,
+                            int parity, int advance) {
+    __shared__ double s_e[kCMaxReplicas];
+    __shared__ int s_t2r[kCMaxReplicas];
+    __shared__ int s_acc;
+    const int s = blockIdx.x;
+    const int R = Q.R, base = s * R, NC = Q.n_classes;
+    unsigned long long* rec_count = Q.ctrl + 1 + s;
+    unsigned long long* xcount = Q.ctrl + 1 + NC + s;
+    unsigned long long* accepted = Q.ctrl + 1 + 2 * NC + s;
+    if (threadIdx.x == 0) s_acc = 0;
+    for (int r = threadIdx.x; r < R; r += blockDim.x) {
+        const double* o = Q.obs + (int64_t)(base + r) * kNQ;
+        s_e[r] = o[0];
+        s_t2r[r] = Q.t2r[base + r];
+        if (do_record) {
+            const long long slot = (long long)(*rec_count % (unsigned long long)Q.ring_cap);
+            const long long idx = slot * Q.replicas_total + base + r;
+            Q.rec_t[idx] = Q.r2t[base + r];
+            Q.rec_e[idx] = o[0];
+            for (int k = 0; k < 3; ++k) Q.rec_m[idx * 3 + k] = o[1 + k];
+            for (int k = 0; k < 6; ++k) Q.rec_h[idx * 6 + k] = o[4 + k];
+        }
+    }
+    __syncthreads();
+    if (do_exchange) {
+        const unsigned long long xc = *xcount;
+        const int par = parity >= 0 ? (parity & 1) : (int)(xc & 1ull);
+        const uint32_t k0 = (uint32_t)Q.seed, k1 = (uint32_t)(Q.seed >> 32);
+        const uint32_t c3 = counter_word3(ISG_TAG_EXCH, 0, xc);
+        for (int i = par + 2 * threadIdx.x; i + 1 < R; i += 2 * blockDim.x) {
+            const int ri = s_t2r[i], rj = s_t2r[i + 1];
+            const double d = __dmul_rn(__dsub_rn(Q.betas[base + i], Q.betas[base + i + 1]),
+                                       __dsub_rn(s_e[rj], s_e[ri]));
+            bool ok = d < 0.0;
+            if (!ok) {
+                const U4 u = philox10(exchange_uid(Q.L[s]), (uint32_t)i, (uint32_t)xc, c3, k0, k1);
+                ok = uniform53(u.x, u.y) < exp(-d);
+            }
+            if (ok) {
+                s_t2r[i] = rj;
+                s_t2r[i + 1] = ri;
+                Q.r2t[base + ri] = i + 1;
+                Q.r2t[base + rj] = i;
+                atomicAdd(&s_acc, 1);
+            }
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < R; r += blockDim.x) Q.t2r[base + r] = s_t2r[r];
+        if (threadIdx.x == 0) {
+            *xcount = xc + 1;
+            *accepted += (unsigned long long)s_acc;
+        }
+    }
+    if (threadIdx.x == 0) {
+        if (do_record) *rec_count += 1ull;
+        if (s == 0 && advance) Q.ctrl[0] += (unsigned long long)advance;
+    }
+}
+
+}  // namespace isg
+
+using namespace isg;
+
+struct isg_cont {
+    int device = 0;
+    int nc = 3;
+    int n_classes = 0;
+    int R = 0;
+    int RT = 0;
+    uint64_t seed = 0;
+    std::vector<int> sizes;
+    ContParams P{};
+    ContPost Q{};
+    float* d_spins = nullptr;
+    int64_t n_floats = 0;
+    float* d_betaf = nullptr;
+    double* d_betas = nullptr;
+    int32_t* d_r2t = nullptr;
+    int32_t* d_t2r = nullptr;
+    unsigned long long* d_ctrl = nullptr;
+    unsigned long long* d_macc = nullptr;
+    double* d_partials = nullptr;
+    double* d_obs = nullptr;
+    int64_t ring_cap = 0;
+    int32_t* d_rec_t = nullptr;
+    double* d_rec_e = nullptr;
+    double* d_rec_m = nullptr;
+    double* d_rec_h = nullptr;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    bool temps_set = false;
+    double J = 1.0;
+    int sms = 1;
+    int grid = 1;
+    uint64_t ksample = 0, records_made = 0, records_done = 0;
+    cudaGraphExec_t graph = nullptr;
+    int g_ee = 0, g_me = 0, g_period = 0, g_nor = -1, g_renorm = -1;
+    double g_delta = -1.0;
+};
+
+namespace isg {
+
+static void cont_destroy_graph(isg_cont* H) {
+    if (H->graph) cudaGraphExecDestroy(H->graph);
+    H->graph = nullptr;
+    H->g_period = 0;
+}
+
+static void launch_or(isg_cont* H, int colour) {
+    if (H->nc == 3)
+        k_cont_or<3><<<H->grid, kCThreads, 0, H->stream>>>(H->P, colour);
+    else
+        k_cont_or<2><<<H->grid, kCThreads, 0, H->stream>>>(H->P, colour);
+}
+
+static void launch_metro(isg_cont* H, int colour, int sweep_off, double delta) {
+    const float cd = (float)std::cos(std::min(delta, M_PI));
+    if (H->nc == 3)
+        k_cont_metro<3><<<H->grid, kCThreads, 0, H->stream>>>(H->P, colour, sweep_off, cd,
+                                                              (float)delta);
+    else
+        k_cont_metro<2><<<H->grid, kCThreads, 0, H->stream>>>(H->P, colour, sweep_off, cd,
+                                                              (float)delta);
+}
+
+static void launch_measure(isg_cont* H) {
+    if (H->nc == 3)
+        k_cont_measure<3><<<H->P.total_chunks, kCThreads, 0, H->stream>>>(H->P);
+    else
+        k_cont_measure<2><<<H->P.total_chunks, kCThreads, 0, H->stream>>>(H->P);
+    k_cont_combine<<<(H->RT + 127) / 128, 128, 0, H->stream>>>(H->P, H->d_obs);
+}
+
+static void launch_cpost(isg_cont* H, int rec, int xch, int parity, int advance) {
+    const int thr = std::min(1024, std::max(32, ((H->R + 31) / 32) * 32));
+    k_cont_post<<<H->n_classes, thr, 0, H->stream>>>(H->Q, rec, xch, parity, advance);
+}
+
+// One sweep in the reference GPU order: n_or overrelaxation sweeps, then one
+// Metropolis sweep (gpu_lattice_continuous.rs:123-168).
+static void issue_cont_sweep(isg_cont* H, int sweep_off, double delta, int n_or) {
+    for (int k = 0; k < n_or; ++k) {
+        launch_or(H, 0);
+        launch_or(H, 1);
+    }
+    launch_metro(H, 0, sweep_off, delta);
+    launch_metro(H, 1, sweep_off, delta);
+}
+
+static void issue_cont_sample(isg_cont* H, uint64_t k, int sweep_off, int ee, int me,
+                              double delta, int n_or, int advance) {
+    const bool do_m = ((k + 1) % (uint64_t)me) == 0;
+    const bool do_x = ((k + 1) % (uint64_t)ee) == 0;
+    issue_cont_sweep(H, sweep_off, delta, n_or);
+    if (do_m || do_x) launch_measure(H);
+    if (do_m || do_x || advance) launch_cpost(H, do_m ? 1 : 0, do_x ? 1 : 0, -1, advance);
+}
+
+static int cont_check(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    return ISG_OK;
+}
+
+static int cont_drain(isg_cont* H, int32_t* t, double* e, double* m, double* hb, int64_t row0) {
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    const int RT = H->RT;
+    uint64_t n = H->records_made - H->records_done;
+    int64_t row = row0;
+    while (n > 0) {
+        const uint64_t slot = H->records_done % (uint64_t)H->ring_cap;
+        const uint64_t chunk = std::min<uint64_t>(n, (uint64_t)H->ring_cap - slot);
+        const size_t cnt = (size_t)chunk * RT, off = (size_t)slot * RT;
+        ISG_CK(cudaMemcpy(t + (size_t)row * RT, H->d_rec_t + off, cnt * sizeof(int32_t),
+                          cudaMemcpyDeviceToHost));
+        ISG_CK(cudaMemcpy(e + (size_t)row * RT, H->d_rec_e + off, cnt * sizeof(double),
+                          cudaMemcpyDeviceToHost));
+        ISG_CK(cudaMemcpy(m + (size_t)row * RT * 3, H->d_rec_m + off * 3, cnt * 3 * sizeof(double),
+                          cudaMemcpyDeviceToHost));
+        ISG_CK(cudaMemcpy(hb + (size_t)row * RT * 6, H->d_rec_h + off * 6,
+                          cnt * 6 * sizeof(double), cudaMemcpyDeviceToHost));
+        H->records_done += chunk;
+        row += (int64_t)chunk;
+        n -= chunk;
+    }
+    return ISG_OK;
+}
+
+}  // namespace isg
+
+extern "C" {
+
+int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas, int n_comp,
+                    uint64_t seed) {
+    if (!out) return fail(ISG_ERR_ARG, "isg_cont_create: out is NULL");
+    *out = nullptr;
+    if (!sizes || n_sizes < 1 || n_sizes > kCMaxClasses)
+        return fail(ISG_ERR_ARG, "isg_cont_create: need 1..16 sizes");
+    if (replicas < 1 || replicas > kCMaxReplicas)
+        return fail(ISG_ERR_ARG, "isg_cont_create: replicas must be 1..1024");
+    if (n_comp != 2 && n_comp != 3)
+        return fail(ISG_ERR_ARG, "isg_cont_create: n_comp must be 2 (XY) or 3 (Heisenberg)");
+    for (int s = 0; s < n_sizes; ++s) {
+        const int L = sizes[s];
+        if (L < 2 || L > 1024)
+            return fail(ISG_ERR_ARG, "isg_cont_create: size " + std::to_string(L) +
+                                         " outside 2..1024");
+        for (int q = 0; q < s; ++q)
+            if (sizes[q] == L)
+                return fail(ISG_ERR_ARG, "isg_cont_create: size " + std::to_string(L) +
+                                             " listed twice (sizes share random streams)");
+        if (L & 1)
+            return fail(ISG_ERR_UNSUPPORTED,
+                        "isg_cont_create: odd size " + std::to_string(L) +
+                            " has no checkerboard colouring under periodic boundaries");
+    }
+    isg_cont* H = new (std::nothrow) isg_cont();
+    if (!H) return fail(ISG_ERR_ARG, "isg_cont_create: out of host memory");
+    cudaGetDevice(&H->device);
+    cudaDeviceGetAttribute(&H->sms, cudaDevAttrMultiProcessorCount, H->device);
+    if (H->sms < 1) H->sms = 1;
+    H->nc = n_comp;
+    H->n_classes = n_sizes;
+    H->R = replicas;
+    H->RT = n_sizes * replicas;
+    H->seed = seed;
+    H->sizes.assign(sizes, sizes + n_sizes);
+    ContParams& P = H->P;
+    int64_t off = 0, site = 0;
+    int chunk = 0;
+    for (int s = 0; s < n_sizes; ++s) {
+        ContClass& C = P.cls[s];
+        const int L = sizes[s];
+        C.L = L;
+        C.R = replicas;
+        C.plane_sites = (uint32_t)((int64_t)L * L * L / 2);
+        C.div_half = make_div((uint32_t)(L / 2));
+        C.div_L = make_div((uint32_t)L);
+        C.rep_base = s * replicas;
+        C.off = off;
+        off += ((2 * (int64_t)n_comp * C.plane_sites * replicas + 63) / 64) * 64;
+        C.site_base = site;
+        site += (int64_t)C.plane_sites * replicas;
+        C.site_end = site;
+        C.chunks_per_rep = (int)((C.plane_sites + kMeasureChunk - 1) / kMeasureChunk);
+        C.chunk_base = chunk;
+        chunk += C.chunks_per_rep * replicas;
+    }
+    for (int s = n_sizes; s < kCMaxClasses; ++s) {
+        P.cls[s] = P.cls[n_sizes - 1];
+        P.cls[s].site_base = P.cls[s].site_end = INT64_MAX;
+        P.cls[s].chunk_base = INT32_MAX;
+        P.cls[s].rep_base = INT32_MAX;
+    }
+    P.n_classes = n_sizes;
+    P.total_sites = site;
+    P.total_chunks = chunk;
+    P.seed = seed;
+    P.J = 1.0f;
+    P.renorm = 0;
+    H->n_floats = off;
+    const int RT = H->RT;
+    H->ring_cap = std::max<int64_t>(64, std::min<int64_t>(8192, (64ll << 20) / (84ll * RT)));
+    H->grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)H->sms * 8,
+                                                          (site + kCThreads - 1) / kCThreads));
+    auto cleanup = [&](int code) {
+        isg_cont_destroy(H);
+        return code;
+    };
+    cudaError_t e;
+#define ALLOC(ptr, bytes)                                              \
+    e = cudaMalloc((void**)&(ptr), (bytes));                           \
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMalloc"));
+    ALLOC(H->d_spins, sizeof(float) * (size_t)off);
+    ALLOC(H->d_betaf, sizeof(float) * RT);
+    ALLOC(H->d_betas, sizeof(double) * RT);
+    ALLOC(H->d_r2t, sizeof(int32_t) * RT);
+    ALLOC(H->d_t2r, sizeof(int32_t) * RT);
+    ALLOC(H->d_ctrl, sizeof(unsigned long long) * (1 + 3 * kCMaxClasses));
+    ALLOC(H->d_macc, sizeof(unsigned long long) * RT);
+    ALLOC(H->d_partials, sizeof(double) * (size_t)chunk * kNQ);
+    ALLOC(H->d_obs, sizeof(double) * (size_t)RT * kNQ);
+    ALLOC(H->d_rec_t, sizeof(int32_t) * (size_t)H->ring_cap * RT);
+    ALLOC(H->d_rec_e, sizeof(double) * (size_t)H->ring_cap * RT);
+    ALLOC(H->d_rec_m, sizeof(double) * (size_t)H->ring_cap * RT * 3);
+    ALLOC(H->d_rec_h, sizeof(double) * (size_t)H->ring_cap * RT * 6);
+#undef ALLOC
+    e = cudaStreamCreateWithFlags(&H->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaStreamCreateWithFlags"));
+    H->stream = H->own_stream;
+    P.spins = H->d_spins;
+    P.betaf = H->d_betaf;
+    P.r2t = H->d_r2t;
+    P.ctrl = H->d_ctrl;
+    P.metro_acc = H->d_macc;
+    P.partials = H->d_partials;
+    ContPost& Q = H->Q;
+    Q.obs = H->d_obs;
+    Q.r2t = H->d_r2t;
+    Q.t2r = H->d_t2r;
+    Q.betas = H->d_betas;
+    Q.rec_t = H->d_rec_t;
+    Q.rec_e = H->d_rec_e;
+    Q.rec_m = H->d_rec_m;
+    Q.rec_h = H->d_rec_h;
+    Q.ctrl = H->d_ctrl;
+    Q.ring_cap = H->ring_cap;
+    Q.seed = seed;
+    Q.R = replicas;
+    Q.n_classes = n_sizes;
+    Q.replicas_total = RT;
+    for (int s = 0; s < kCMaxClasses; ++s) Q.L[s] = s < n_sizes ? sizes[s] : 0;
+    std::vector<int32_t> ident(RT);
+    for (int i = 0; i < RT; ++i) ident[i] = i % replicas;
+#define CKC(call)                                                      \
+    e = (call);                                                        \
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, #call));
+    CKC(cudaMemsetAsync(H->d_spins, 0, sizeof(float) * (size_t)off, H->stream));
+    CKC(cudaMemsetAsync(H->d_ctrl, 0, sizeof(unsigned long long) * (1 + 3 * kCMaxClasses),
+                        H->stream));
+    CKC(cudaMemsetAsync(H->d_macc, 0, sizeof(unsigned long long) * RT, H->stream));
+    CKC(cudaMemsetAsync(H->d_obs, 0, sizeof(double) * (size_t)RT * kNQ, H->stream));
+    CKC(cudaMemcpyAsync(H->d_r2t, ident.data(), sizeof(int32_t) * RT, cudaMemcpyHostToDevice,
+                        H->stream));
+    CKC(cudaMemcpyAsync(H->d_t2r, ident.data(), sizeof(int32_t) * RT, cudaMemcpyHostToDevice,
+                        H->stream));
+    k_cont_init<<<H->sms * 4, 256, 0, H->stream>>>(H->P, n_comp);
+    CKC(cudaGetLastError());
+    CKC(cudaStreamSynchronize(H->stream));
+#undef CKC
+    *out = H;
+    return ISG_OK;
+}
+
+int isg_cont_destroy(isg_cont* H) {
+    if (!H) return ISG_OK;
+    cudaSetDevice(H->device);
+    if (H->stream) cudaStreamSynchronize(H->stream);
+    cont_destroy_graph(H);
+    cudaFree(H->d_spins);
+    cudaFree(H->d_betaf);
+    cudaFree(H->d_betas);
+    cudaFree(H->d_r2t);
+    cudaFree(H->d_t2r);
+    cudaFree(H->d_ctrl);
+    cudaFree(H->d_macc);
+    cudaFree(H->d_partials);
+    cudaFree(H->d_obs);
+    cudaFree(H->d_rec_t);
+    cudaFree(H->d_rec_e);
+    cudaFree(H->d_rec_m);
+    cudaFree(H->d_rec_h);
+    if (H->own_stream) cudaStreamDestroy(H->own_stream);
+    delete H;
+    return ISG_OK;
+}
+
+int isg_cont_set_stream(isg_cont* H, void* stream) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_cont_set_stream: NULL handle");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    H->stream = stream ? (cudaStream_t)stream : H->own_stream;
+    return ISG_OK;
+}
+
+int isg_cont_set_temperatures(isg_cont* H, const double* temps, double J) {
+    if (!H || !temps) return fail(ISG_ERR_ARG, "isg_cont_set_temperatures: NULL argument");
+    cudaSetDevice(H->device);
+    const int RT = H->RT;
+    std::vector<double> b(RT);
+    std::vector<float> bf(RT);
+    for (int i = 0; i < RT; ++i) {
+        if (!(temps[i] > 0.0) || !std::isfinite(temps[i]))
+            return fail(ISG_ERR_ARG, "isg_cont_set_temperatures: temperatures must be positive");
+        b[i] = 1.0 / temps[i];
+        bf[i] = (float)b[i];
+    }
+    std::vector<int32_t> ident(RT);
+    for (int i = 0; i < RT; ++i) ident[i] = i % H->R;
+    ISG_CK(cudaMemcpyAsync(H->d_betas, b.data(), sizeof(double) * RT, cudaMemcpyHostToDevice,
+                           H->stream));
+    ISG_CK(cudaMemcpyAsync(H->d_betaf, bf.data(), sizeof(float) * RT, cudaMemcpyHostToDevice,
+                           H->stream));
+    ISG_CK(cudaMemcpyAsync(H->d_r2t, ident.data(), sizeof(int32_t) * RT, cudaMemcpyHostToDevice,
+                           H->stream));
+    ISG_CK(cudaMemcpyAsync(H->d_t2r, ident.data(), sizeof(int32_t) * RT, cudaMemcpyHostToDevice,
+                           H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    H->J = J;
+    H->P.J = (float)J;
+    H->temps_set = true;
+    cont_destroy_graph(H);
+    return ISG_OK;
+}
+
+int isg_cont_sweep(isg_cont* H, int64_t n_sweeps, double delta, int n_overrelax) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_cont_sweep: NULL handle");
+    if (!H->temps_set) return fail(ISG_ERR_STATE, "isg_cont_sweep: temperatures not set");
+    if (n_sweeps < 0 || n_overrelax < 0 || !(delta > 0.0))
+        return fail(ISG_ERR_ARG, "isg_cont_sweep: need n_sweeps >= 0, n_overrelax >= 0, delta > 0");
+    cudaSetDevice(H->device);
+    int64_t done = 0;
+    while (done < n_sweeps) {
+        const int chunk = (int)std::min<int64_t>(n_sweeps - done, 1 << 20);
+        for (int j = 0; j < chunk; ++j) issue_cont_sweep(H, j, delta, n_overrelax);
+        launch_cpost(H, 0, 0, 0, chunk);
+        done += chunk;
+    }
+    return cont_check("isg_cont_sweep");
+}
+
+int isg_cont_overrelax(isg_cont* H, int colour) {
+    if (!H || (colour != 0 && colour != 1))
+        return fail(ISG_ERR_ARG, "isg_cont_overrelax: bad argument");
+    cudaSetDevice(H->device);
+    launch_or(H, colour);
+    return cont_check("isg_cont_overrelax");
+}
+
+int isg_cont_metropolis(isg_cont* H, int colour, double delta) {
+    if (!H || (colour != 0 && colour != 1) || !(delta > 0.0))
+        return fail(ISG_ERR_ARG, "isg_cont_metropolis: bad argument");
+    if (!H->temps_set) return fail(ISG_ERR_STATE, "isg_cont_metropolis: temperatures not set");
+    cudaSetDevice(H->device);
+    launch_metro(H, colour, 0, delta);
+    return cont_check("isg_cont_metropolis");
+}
+
+int isg_cont_normalize(isg_cont* H) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_cont_normalize: NULL handle");
+    cudaSetDevice(H->device);
+    k_cont_normalize<<<H->sms * 4, 256, 0, H->stream>>>(H->P, H->nc);
+    return cont_check("isg_cont_normalize");
+}
+
+int isg_cont_measure(isg_cont* H, double* energy, double* mag, double* bonds) {
+    if (!H || !energy || !mag) return fail(ISG_ERR_ARG, "isg_cont_measure: NULL argument");
+    cudaSetDevice(H->device);
+    launch_measure(H);
+    int rc = cont_check("isg_cont_measure");
+    if (rc) return rc;
+    std::vector<double> o((size_t)H->RT * kNQ);
+    ISG_CK(cudaMemcpyAsync(o.data(), H->d_obs, o.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                           H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    for (int r = 0; r < H->RT; ++r) {
+        energy[r] = o[(size_t)r * kNQ];
+        for (int k = 0; k < 3; ++k) mag[r * 3 + k] = o[(size_t)r * kNQ + 1 + k];
+        if (bonds)
+            for (int k = 0; k < 6; ++k) bonds[r * 6 + k] = o[(size_t)r * kNQ + 4 + k];
+    }
+    return ISG_OK;
+}
+
+int isg_cont_exchange(isg_cont* H, int parity, int64_t* accepted) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_cont_exchange: NULL handle");
+    if (!H->temps_set) return fail(ISG_ERR_STATE, "isg_cont_exchange: temperatures not set");
+    cudaSetDevice(H->device);
+    const int NC = H->n_classes;
+    std::vector<unsigned long long> a(NC), b(NC);
+    ISG_CK(cudaMemcpyAsync(a.data(), H->d_ctrl + 1 + 2 * NC, NC * 8, cudaMemcpyDeviceToHost,
+                           H->stream));
+    launch_cpost(H, 0, 1, parity, 0);
+    int rc = cont_check("isg_cont_exchange");
+    if (rc) return rc;
+    ISG_CK(cudaMemcpyAsync(b.data(), H->d_ctrl + 1 + 2 * NC, NC * 8, cudaMemcpyDeviceToHost,
+                           H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    if (accepted)
+        for (int s = 0; s < NC; ++s) accepted[s] = (int64_t)(b[s] - a[s]);
+    return ISG_OK;
+}
+
+int isg_cont_reset_sampling(isg_cont* H) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_cont_reset_sampling: NULL handle");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaMemsetAsync(H->d_ctrl + 1, 0, sizeof(unsigned long long) * 3 * H->n_classes,
+                           H->stream));
+    ISG_CK(cudaMemsetAsync(H->d_macc, 0, sizeof(unsigned long long) * H->RT, H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    H->ksample = H->records_made = H->records_done = 0;
+    return ISG_OK;
+}
+
+int isg_cont_pt_run(isg_cont* H, int64_t n_sweeps, int ee, int me, double delta, int n_or,
+                    int renorm_every, int32_t* tslot, double* energy, double* mag, double* bonds,
+                    int64_t max_records, int64_t* n_records) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_cont_pt_run: NULL handle");
+    if (!H->temps_set) return fail(ISG_ERR_STATE, "isg_cont_pt_run: temperatures not set");
+    if (n_sweeps < 0 || ee < 1 || me < 1 || n_or < 0 || renorm_every < 0 || !(delta > 0.0))
+        return fail(ISG_ERR_ARG, "isg_cont_pt_run: bad cadence or proposal arguments");
+    cudaSetDevice(H->device);
+    const bool keep = !tslot && !energy && !mag && !bonds;
+    const uint64_t k0 = H->ksample;
+    const uint64_t need = (k0 + (uint64_t)n_sweeps) / (uint64_t)me - k0 / (uint64_t)me;
+    if (!keep && need > 0 && (!tslot || !energy || !mag || !bonds || max_records < (int64_t)need))
+        return fail(ISG_ERR_ARG, "isg_cont_pt_run: record arrays too small");
+    if (n_records) *n_records = 0;
+    H->P.renorm = renorm_every;
+    int64_t g = ee, b = me;
+    while (b) {
+        int64_t t = g % b;
+        g = b;
+        b = t;
+    }
+    const int64_t lcm = (int64_t)ee / g * me;
+    const int64_t nodes = lcm * (2 * n_or + 4);
+    const int period = (lcm <= 1000 && nodes <= 20000) ? (int)lcm : 0;
+    const int rec_pp = period ? period / me : 0;
+    const bool use_graph = period > 0 && rec_pp <= H->ring_cap / 2;
+    if (H->graph && (H->g_ee != ee || H->g_me != me || H->g_nor != n_or || H->g_delta != delta ||
+                     H->g_renorm != renorm_every))
+        cont_destroy_graph(H);
+    int64_t done = 0, row = 0;
+    while (done < n_sweeps) {
+        const uint64_t k = H->ksample;
+        const int64_t left = n_sweeps - done;
+        const uint64_t pending = H->records_made - H->records_done;
+        const bool whole = use_graph && (k % (uint64_t)period) == 0 && left >= period;
+        const uint64_t adds = whole ? (uint64_t)rec_pp : 1u;
+        if (pending + adds > (uint64_t)H->ring_cap) {
+            if (keep) {
+                H->records_done = H->records_made + adds - (uint64_t)H->ring_cap;
+            } else {
+                int rc = cont_drain(H, tslot, energy, mag, bonds, row);
+                if (rc) return rc;
+                row += (int64_t)pending;
+                continue;
+            }
+        }
+        if (whole) {
+            if (!H->graph) {
+                cudaGraph_t gr = nullptr;
+                ISG_CK(cudaStreamBeginCapture(H->stream, cudaStreamCaptureModeThreadLocal));
+                for (int j = 0; j < period; ++j)
+                    issue_cont_sample(H, (uint64_t)j, j, ee, me, delta, n_or,
+                                      j == period - 1 ? period : 0);
+                cudaError_t e = cudaStreamEndCapture(H->stream, &gr);
+                if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+                e = cudaGraphInstantiate(&H->graph, gr, 0);
+                cudaGraphDestroy(gr);
+                if (e != cudaSuccess) {
+                    H->graph = nullptr;
+                    return cuda_fail(e, "cudaGraphInstantiate");
+                }
+                H->g_ee = ee;
+                H->g_me = me;
+                H->g_nor = n_or;
+                H->g_delta = delta;
+                H->g_renorm = renorm_every;
+                H->g_period = period;
+            }
+            ISG_CK(cudaGraphLaunch(H->graph, H->stream));
+            H->ksample += (uint64_t)period;
+            H->records_made += (uint64_t)rec_pp;
+            done += period;
+        } else {
+            const bool do_m = ((k + 1) % (uint64_t)me) == 0;
+            issue_cont_sample(H, k, 0, ee, me, delta, n_or, 1);
+            int rc = cont_check("isg_cont_pt_run");
+            if (rc) return rc;
+            H->ksample += 1;
+            if (do_m) H->records_made += 1;
+            done += 1;
+        }
+    }
+    if (keep) return cont_check("isg_cont_pt_run");
+    const uint64_t pending = H->records_made - H->records_done;
+    int rc = cont_drain(H, tslot, energy, mag, bonds, row);
+    if (rc) return rc;
+    row += (int64_t)pending;
+    if (n_records) *n_records = row;
+    return ISG_OK;
+}
+
+int isg_cont_get_r2t(isg_cont* H, int32_t* r2t) {
+    if (!H || !r2t) return fail(ISG_ERR_ARG, "isg_cont_get_r2t: NULL argument");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaMemcpyAsync(r2t, H->d_r2t, sizeof(int32_t) * H->RT, cudaMemcpyDeviceToHost,
+                           H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    return ISG_OK;
+}
+
+static int cont_geom(isg_cont* H, int s, int r, int64_t* n, int64_t* base, uint32_t* ps) {
+    if (s < 0 || s >= H->n_classes || r < 0 || r >= H->R)
+        return fail(ISG_ERR_ARG, "spin access: size index or replica out of range");
+    const ContClass& C = H->P.cls[s];
+    *ps = C.plane_sites;
+    *n = 2 * (int64_t)C.plane_sites;
+    *base = C.off + (int64_t)r * 2 * H->nc * C.plane_sites;
+    return ISG_OK;
+}
+
+int isg_cont_get_spins(isg_cont* H, int s, int r, float* out) {
+    if (!H || !out) return fail(ISG_ERR_ARG, "isg_cont_get_spins: NULL argument");
+    cudaSetDevice(H->device);
+    int64_t n, base;
+    uint32_t ps;
+    int rc = cont_geom(H, s, r, &n, &base, &ps);
+    if (rc) return rc;
+    const int nc = H->nc;
+    std::vector<float> pl((size_t)n * nc);
+    ISG_CK(cudaMemcpyAsync(pl.data(), H->d_spins + base, pl.size() * sizeof(float),
+                           cudaMemcpyDeviceToHost, H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    const int L = H->sizes[s];
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t x = i % L, y = (i / L) % L, z = i / ((int64_t)L * L);
+        const int c = (int)((x + y + z) & 1);
+        for (int k = 0; k < nc; ++k)
+            out[i * nc + k] = pl[(size_t)(c * nc + k) * ps + (size_t)(i >> 1)];
+    }
+    return ISG_OK;
+}
+
+int isg_cont_set_spins(isg_cont* H, int s, int r, const float* in) {
+    if (!H || !in) return fail(ISG_ERR_ARG, "isg_cont_set_spins: NULL argument");
+    cudaSetDevice(H->device);
+    int64_t n, base;
+    uint32_t ps;
+    int rc = cont_geom(H, s, r, &n, &base, &ps);
+    if (rc) return rc;
+    const int nc = H->nc;
+    std::vector<float> pl((size_t)n * nc);
+    const int L = H->sizes[s];
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t x = i % L, y = (i / L) % L, z = i / ((int64_t)L * L);
+        const int c = (int)((x + y + z) & 1);
+        for (int k = 0; k < nc; ++k) {
+            const float v = in[i * nc + k];
+            if (!std::isfinite(v)) return fail(ISG_ERR_ARG, "isg_cont_set_spins: non-finite spin");
+            pl[(size_t)(c * nc + k) * ps + (size_t)(i >> 1)] = v;
+        }
+    }
+    ISG_CK(cudaMemcpyAsync(H->d_spins + base, pl.data(), pl.size() * sizeof(float),
+                           cudaMemcpyHostToDevice, H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    return ISG_OK;
+}
+
+int isg_cont_get_accepted(isg_cont* H, int64_t* accepted) {
+    if (!H || !accepted) return fail(ISG_ERR_ARG, "isg_cont_get_accepted: NULL argument");
+    cudaSetDevice(H->device);
+    const int NC = H->n_classes;
+    std::vector<unsigned long long> a(NC);
+    ISG_CK(cudaMemcpyAsync(a.data(), H->d_ctrl + 1 + 2 * NC, NC * 8, cudaMemcpyDeviceToHost,
+                           H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    for (int s = 0; s < NC; ++s) accepted[s] = (int64_t)a[s];
+    return ISG_OK;
+}
+
+int isg_cont_get_metro_accepted(isg_cont* H, int64_t* accepted) {
+    if (!H || !accepted) return fail(ISG_ERR_ARG, "isg_cont_get_metro_accepted: NULL argument");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaMemcpyAsync(accepted, H->d_macc, sizeof(int64_t) * H->RT, cudaMemcpyDeviceToHost,
+                           H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    return ISG_OK;
+}
+
+int isg_cont_sync(isg_cont* H) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_cont_sync: NULL handle");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    return cont_check("isg_cont_sync");
+}
+
+// Mean device times (ms) of one overrelaxation half-sweep, one Metropolis
+// half-sweep and one measurement, on a copy that is restored afterwards.
+int isg_cont_time_kernels(isg_cont* H, int n, float* out_ms) {
+    if (!H || !out_ms || n < 1) return fail(ISG_ERR_ARG, "isg_cont_time_kernels: bad argument");
+    if (!H->temps_set) return fail(ISG_ERR_STATE, "isg_cont_time_kernels: temperatures not set");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    float* backup = nullptr;
+    ISG_CK(cudaMalloc((void**)&backup, sizeof(float) * (size_t)H->n_floats));
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaError_t e = cudaMemcpyAsync(backup, H->d_spins, sizeof(float) * (size_t)H->n_floats,
+                                    cudaMemcpyDeviceToDevice, H->stream);
+    unsigned long long ctrl0 = 0;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&ctrl0, H->d_ctrl, sizeof(ctrl0), cudaMemcpyDeviceToHost, H->stream);
+    std::vector<unsigned long long> macc(H->RT);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(macc.data(), H->d_macc, 8 * H->RT, cudaMemcpyDeviceToHost, H->stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    for (int which = 0; which < 3 && e == cudaSuccess; ++which) {
+        float total = 0.f;
+        for (int i = 0; i < n && e == cudaSuccess; ++i) {
+            e = cudaEventRecord(a, H->stream);
+            if (which == 0) launch_or(H, i & 1);
+            else if (which == 1) launch_metro(H, i & 1, i >> 1, 0.5);
+            else launch_measure(H);
+            if (e == cudaSuccess) e = cudaEventRecord(b, H->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(b);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+            total += ms;
+        }
+        out_ms[which] = total / (float)n;
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(H->d_spins, backup, sizeof(float) * (size_t)H->n_floats,
+                            cudaMemcpyDeviceToDevice, H->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(H->d_ctrl, &ctrl0, sizeof(ctrl0), cudaMemcpyHostToDevice, H->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(H->d_macc, macc.data(), 8 * H->RT, cudaMemcpyHostToDevice, H->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    cudaFree(backup);
+    if (e != cudaSuccess) return cuda_fail(e, "isg_cont_time_kernels");
+    return ISG_OK;
+}
+
+int isg_cont_sites_per_sweep(isg_cont* H, int64_t* sites) {
+    if (!H || !sites) return fail(ISG_ERR_ARG, "isg_cont_sites_per_sweep: NULL argument");
+    *sites = 2 * H->P.total_sites;
+    return ISG_OK;
+}
+
+}  // extern "C"

@@ -60,31 +60,41 @@ constexpr int kMaxClasses = 16;
 constexpr int kMaxThreads = 512;
 constexpr int kMaxReplicas = 1024;
 
+// Task kinds of a lattice size (one warp task = 32 words = 128 sites of one
+// colour plane of one replica):
+//   kRolling (dim 3, L = 64, 128, 256): a task is the nr = 32/(L/8) rows of
+//     one y-block at one z; consecutive tasks of a size walk z, so a warp
+//     keeps the z-1, z, z+1 words of the other colour in registers.
+//   kFlat    (other power-of-two L with L/8 dividing 32): 32 consecutive words.
+//   kSite    (any other even L): one thread per site (site kernel).
+enum { kSite = 0, kFlat = 1, kRolling = 2 };
+
 struct IsingClass {
     int L;
     int R;
-    int word_path;
-    int log2L;          // word path only
-    int log2_row_words; // word path only (row_words = L/8)
+    int kind;
+    int log2L;
+    int log2_rw;              // rw = L/8 words per row
+    int log2_tpp;             // log2(tasks per plane)
     uint32_t plane_sites;     // L^dim / 2
-    uint32_t tasks_per_plane; // word path: plane_sites / 128 (a power of two)
-    int log2_tpp;             // word path: log2(tasks_per_plane)
+    uint32_t tasks_per_plane; // plane_sites / 128 for word kinds
     int rep_base;             // global replica index of replica 0 (also slot base)
     int64_t spin_off;         // byte offset of replica 0 colour 0
-    int64_t task_base;        // word path: first warp task
+    int64_t task_base;        // word kinds: first warp task
     int64_t task_end;
-    int64_t site_base;        // site path: first site (over colour planes)
+    int64_t site_base;        // site kind: first site (over colour planes)
     int64_t site_end;
 };
 
 struct IsingParams {
-    int8_t* spins;
+    uint8_t* spins;                 // down bits: 1 for s = -1, 0 for s = +1
     const uint32_t* thr;            // [slots][16]
     const int32_t* r2t;             // [replicas]
     unsigned long long* acc;        // [replicas][2] bond, mag
     const unsigned long long* ctrl; // ctrl[0] = global sweep base
     uint64_t seed;
     int n_classes;
+    int dim;
     int64_t total_tasks;
     int64_t total_sites;
     IsingClass cls[kMaxClasses];
@@ -92,14 +102,116 @@ struct IsingParams {
 
 // ---------------------------------------------------------------- kernels
 
-__device__ __forceinline__ void flush_acc(unsigned long long* acc, int rep, int b, int m,
-                                          int lane) {
-    const int sb = __reduce_add_sync(ISG_FULL_MASK, b);
-    const int sm = __reduce_add_sync(ISG_FULL_MASK, m);
+// Philox4x32-10 of counter {uid, w, c2, c3} with the warp-uniform part of the
+// first three rounds (everything that does not depend on w) computed once.
+struct PhiloxPre {
+    uint32_t x0, a1, a2, x2, b0, b1, x3, hi02, lo02;
+};
+
+__device__ __forceinline__ PhiloxPre philox_pre(uint32_t uid, uint32_t c2, uint32_t c3,
+                                                uint32_t k0, uint32_t k1) {
+    PhiloxPre p;
+    // round 0: M0*uid and M1*c2 are uniform
+    const uint32_t hi0 = __umulhi(kPhiloxM0, uid), lo0 = kPhiloxM0 * uid;
+    const uint32_t hi1 = __umulhi(kPhiloxM1, c2), lo1 = kPhiloxM1 * c2;
+    p.x0 = hi1 ^ k0;       // a0 = x0 ^ w
+    p.a1 = lo1;
+    p.a2 = hi0 ^ c3 ^ k1;
+    const uint32_t a3 = lo0;
+    // round 1 (keys + 1*W): M1*a2 uniform
+    const uint32_t k01 = k0 + kPhiloxW0, k11 = k1 + kPhiloxW1;
+    const uint32_t h1 = __umulhi(kPhiloxM1, p.a2), l1 = kPhiloxM1 * p.a2;
+    p.b0 = h1 ^ p.a1 ^ k01;
+    p.b1 = l1;
+    p.x2 = a3 ^ k11;       // b2 = hi(M0*a0) ^ x2, b3 = lo(M0*a0)
+    // round 2 (keys + 2*W): M0*b0 uniform
+    const uint32_t k02 = k0 + 2u * kPhiloxW0, k12 = k1 + 2u * kPhiloxW1;
+    p.hi02 = __umulhi(kPhiloxM0, p.b0) ^ k12;  // c2 = b3 ^ hi02
+    p.lo02 = kPhiloxM0 * p.b0;                 // c3
+    p.x3 = p.b1 ^ k02;                         // c0 = hi(M1*b2) ^ x3
+    return p;
+}
+
+__device__ __forceinline__ U4 philox_w(const PhiloxPre& p, uint32_t w, uint32_t k0, uint32_t k1) {
+    // round 0
+    const uint32_t a0 = p.x0 ^ w;
+    // round 1
+    const uint32_t b2 = __umulhi(kPhiloxM0, a0) ^ p.x2;
+    const uint32_t b3 = kPhiloxM0 * a0;
+    // round 2
+    uint32_t c0 = __umulhi(kPhiloxM1, b2) ^ p.x3;
+    uint32_t c1 = kPhiloxM1 * b2;
+    uint32_t c2 = b3 ^ p.hi02;
+    uint32_t c3 = p.lo02;
+    // rounds 3..9
+    uint32_t q0 = k0 + 3u * kPhiloxW0, q1 = k1 + 3u * kPhiloxW1;
+#pragma unroll
+    for (int r = 3; r < 10; ++r) {
+        const uint32_t hi0 = __umulhi(kPhiloxM0, c0), lo0 = kPhiloxM0 * c0;
+        const uint32_t hi1 = __umulhi(kPhiloxM1, c2), lo1 = kPhiloxM1 * c2;
+        c0 = hi1 ^ c1 ^ q0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ q1;
+        c3 = lo0;
+        q0 += kPhiloxW0;
+        q1 += kPhiloxW1;
+    }
+    return U4{c0, c1, c2, c3};
+}
+
+__device__ __forceinline__ uint32_t lds_u32(uint32_t saddr) {
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(saddr));
+    return v;
+}
+
+// New word of 4 same-colour sites: own down bits ow, down-neighbour counts
+// nd (per byte), table at shared address tbase (256-byte aligned, entry
+// own_down*8 + n_down at byte offset 4*(...)), random words u.
+__device__ __forceinline__ uint32_t metropolis_word(uint32_t ow, uint32_t nd, uint32_t tbase,
+                                                    const U4& u) {
+    const uint32_t idx4 = (nd << 2) + (ow << 5);
+    const uint32_t t0 = lds_u32(__byte_perm(idx4, tbase, 0x7650));
+    const uint32_t t1 = lds_u32(__byte_perm(idx4, tbase, 0x7651));
+    const uint32_t t2 = lds_u32(__byte_perm(idx4, tbase, 0x7652));
+    const uint32_t t3 = lds_u32(__byte_perm(idx4, tbase, 0x7653));
+    uint32_t flip = 0;
+    if (u.x <= t0) flip |= 0x00000001u;
+    if (u.y <= t1) flip |= 0x00000100u;
+    if (u.z <= t2) flip |= 0x00010000u;
+    if (u.w <= t3) flip |= 0x01000000u;
+    return ow ^ flip;
+}
+
+__device__ __forceinline__ void flush_acc(unsigned long long* acc, int rep, long long b,
+                                          long long m, int lane) {
+    // b, m are per-lane partial sums that fit in int32 before the reduction
+    const int sb = __reduce_add_sync(ISG_FULL_MASK, (int)b);
+    const int sm = __reduce_add_sync(ISG_FULL_MASK, (int)m);
     if (lane == 0) {
         atomicAdd(&acc[2 * rep], (unsigned long long)(long long)sb);
         atomicAdd(&acc[2 * rep + 1], (unsigned long long)(long long)sm);
     }
+}
+
+// Per-lane measurement sums of the down-bit words, converted at flush time:
+// bond = 4Z*n - 2Z*So - 2*Snd + 4*Sond, mag = 8*n - 2*(So + Sa).
+struct MeasAcc {
+    int n, so, snd, sond, sa;
+};
+__device__ __forceinline__ void meas_add(MeasAcc& m, uint32_t nw, uint32_t nd, uint32_t wa) {
+    m.n += 1;
+    m.so = __dp4a(nw, 0x01010101u, (unsigned)m.so);
+    m.snd = __dp4a(nd, 0x01010101u, (unsigned)m.snd);
+    m.sond = __dp4a(nw, nd, (unsigned)m.sond);
+    m.sa = __dp4a(wa, 0x01010101u, (unsigned)m.sa);
+}
+__device__ __forceinline__ void meas_flush(unsigned long long* acc, int rep, MeasAcc& m, int Z,
+                                           int lane) {
+    const long long b = 4ll * Z * m.n - 2ll * Z * m.so - 2ll * m.snd + 4ll * m.sond;
+    const long long g = 8ll * m.n - 2ll * (m.so + m.sa);
+    flush_acc(acc, rep, b, g, lane);
+    m = MeasAcc{0, 0, 0, 0, 0};
 }
 
 // MODE 0: update; 1: update then accumulate bond/mag of the new state;
@@ -107,7 +219,7 @@ __device__ __forceinline__ void flush_acc(unsigned long long* acc, int rep, int 
 template <int DIM, int MODE>
 __global__ void __launch_bounds__(kMaxThreads)
     k_ising_words(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
-    __shared__ uint32_t s_thr[kMaxThreads / 32][16];
+    __shared__ __align__(256) uint32_t s_thr[kMaxThreads / 32][64];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -120,29 +232,29 @@ __global__ void __launch_bounds__(kMaxThreads)
     const uint32_t c2 = (uint32_t)sweep;
     const uint32_t c3 = counter_word3(ISG_TAG_ISING, (uint32_t)colour, sweep);
     const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
-    const uint32_t M2 = 0x02020202u;
+    const uint32_t tbase = (uint32_t)__cvta_generic_to_shared(&s_thr[wib][0]);
+    constexpr int Z = 2 * DIM;
 
     int ci = 0;
     while (P.cls[ci].task_end <= t) ++ci;
     int cur_rep = -1;
-    int accb = 0, accm = 0;
+    MeasAcc macc{0, 0, 0, 0, 0};
     uint32_t* own = nullptr;
     const uint32_t* oth = nullptr;
-    uint32_t uid = 0;
-    const char* tb = reinterpret_cast<const char*>(s_thr[wib]);
+    PhiloxPre pre{};
+    // rolling state (kRolling)
+    int64_t next_t = -1;
+    uint32_t zm = 0, za = 0, zp = 0;
 
     for (; t < t_end; ++t) {
         while (P.cls[ci].task_end <= t) ++ci;
         const IsingClass& C = P.cls[ci];
         const int64_t lt = t - C.task_base;
         const int r = (int)(lt >> C.log2_tpp);
-        const uint32_t tw = (uint32_t)(lt & (int64_t)(C.tasks_per_plane - 1));
+        const uint32_t tl = (uint32_t)(lt & (int64_t)(C.tasks_per_plane - 1));
         const int rg = C.rep_base + r;
         if (rg != cur_rep) {
-            if (MODE != 0 && cur_rep >= 0) {
-                flush_acc(P.acc, cur_rep, accb, accm, lane);
-                accb = accm = 0;
-            }
+            if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
             cur_rep = rg;
             if (MODE != 2) {
                 const int slot = C.rep_base + P.r2t[rg];
@@ -150,77 +262,98 @@ __global__ void __launch_bounds__(kMaxThreads)
                 if (lane < 16) s_thr[wib][lane] = P.thr[slot * 16 + lane];
                 __syncwarp();
             }
-            int8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
+            uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
             own = reinterpret_cast<uint32_t*>(base + (int64_t)colour * C.plane_sites);
             oth = reinterpret_cast<const uint32_t*>(base + (int64_t)(colour ^ 1) * C.plane_sites);
-            uid = replica_uid(C.L, r);
+            pre = philox_pre(replica_uid(C.L, r), c2, c3, k0, k1);
+            next_t = -1;
         }
-        const int L = C.L;
-        const uint32_t Lm = (uint32_t)L - 1;
-        const int lrw = C.log2_row_words;
+        const uint32_t L = (uint32_t)C.L;
+        const uint32_t Lm = L - 1;
+        const int lrw = C.log2_rw;
         const uint32_t rwm = (1u << lrw) - 1;
-        const uint32_t w = (tw << 5) + (uint32_t)lane;
-        const uint32_t row = w >> lrw;
-        const uint32_t k4 = w & rwm;
-        uint32_t y, z, p;
-        if (DIM == 3) {
-            y = row & Lm;
-            z = row >> C.log2L;
-            p = (y + z + (uint32_t)colour) & 1u;
+        uint32_t w, y, z, k4, wa, wyp, wym, wzp, wzm;
+        if (DIM == 3 && C.kind == kRolling) {
+            // task tl -> (y-block yb, z), z fastest
+            z = tl & Lm;
+            const uint32_t yb = tl >> C.log2L;
+            const uint32_t pz = L << lrw;  // words per z-plane
+            const uint32_t col = (yb << 5) + (uint32_t)lane;
+            w = z * pz + col;
+            k4 = (uint32_t)lane & rwm;
+            const uint32_t rb = (uint32_t)lane >> lrw;  // row within the block
+            const uint32_t nr = 32u >> lrw;
+            y = (yb * nr + rb);
+            if (t != next_t) {
+                zm = __ldg(oth + ((z - 1) & Lm) * pz + col);
+                za = __ldg(oth + w);
+            } else {
+                zm = za;
+                za = zp;
+            }
+            zp = __ldg(oth + ((z + 1) & Lm) * pz + col);
+            next_t = (z + 1 < L) ? t + 1 : -1;
+            const uint32_t up = __shfl_sync(ISG_FULL_MASK, za, (lane + (1 << lrw)) & 31);
+            const uint32_t dn = __shfl_sync(ISG_FULL_MASK, za, (lane - (1 << lrw)) & 31);
+            if (nr >= 2) {
+                const bool first = rb == 0, last = rb == nr - 1;
+                uint32_t halo = 0;
+                if (first || last) {
+                    const uint32_t hy = first ? ((y - 1) & Lm) : ((y + 1) & Lm);
+                    halo = __ldg(oth + z * pz + (hy << lrw) + k4);
+                }
+                wyp = last ? halo : up;
+                wym = first ? halo : dn;
+            } else {
+                wyp = __ldg(oth + z * pz + (((y + 1) & Lm) << lrw) + k4);
+                wym = __ldg(oth + z * pz + (((y - 1) & Lm) << lrw) + k4);
+            }
+            wa = za;
+            wzp = zp;
+            wzm = zm;
         } else {
-            y = row;
-            z = 0;
-            p = (y + (uint32_t)colour) & 1u;
+            w = (tl << 5) + (uint32_t)lane;
+            const uint32_t row = w >> lrw;
+            k4 = w & rwm;
+            if (DIM == 3) {
+                y = row & Lm;
+                z = row >> C.log2L;
+            } else {
+                y = row;
+                z = 0;
+            }
+            const uint32_t yp = (y + 1) & Lm, ym = (y - 1) & Lm;
+            if (DIM == 3) {
+                const uint32_t zb = z << C.log2L;
+                wa = __ldg(oth + (((zb + y) << lrw) + k4));
+                wyp = __ldg(oth + (((zb + yp) << lrw) + k4));
+                wym = __ldg(oth + (((zb + ym) << lrw) + k4));
+                wzp = __ldg(oth + (((((z + 1) & Lm) << C.log2L) + y) << lrw) + k4);
+                wzm = __ldg(oth + (((((z - 1) & Lm) << C.log2L) + y) << lrw) + k4);
+            } else {
+                wa = __ldg(oth + ((y << lrw) + k4));
+                wyp = __ldg(oth + ((yp << lrw) + k4));
+                wym = __ldg(oth + ((ym << lrw) + k4));
+                wzp = wzm = 0;
+            }
         }
-        const uint32_t yp = (y + 1) & Lm, ym = (y - 1) & Lm;
-        uint32_t wa, wyp, wym, wzp = 0, wzm = 0;
-        if (DIM == 3) {
-            const uint32_t zp = (z + 1) & Lm, zm = (z - 1) & Lm;
-            const uint32_t zb = z << C.log2L;
-            wa = __ldg(oth + (((zb + y) << lrw) + k4));
-            wyp = __ldg(oth + (((zb + yp) << lrw) + k4));
-            wym = __ldg(oth + (((zb + ym) << lrw) + k4));
-            wzp = __ldg(oth + ((((zp << C.log2L) + y) << lrw) + k4));
-            wzm = __ldg(oth + ((((zm << C.log2L) + y) << lrw) + k4));
-        } else {
-            wa = __ldg(oth + ((y << lrw) + k4));
-            wyp = __ldg(oth + ((yp << lrw) + k4));
-            wym = __ldg(oth + ((ym << lrw) + k4));
-        }
+        const uint32_t p = (y + z + (uint32_t)colour) & 1u;
         const int lane0 = lane - (int)k4;
         const uint32_t prev = __shfl_sync(ISG_FULL_MASK, wa, lane0 + (int)((k4 - 1) & rwm));
         const uint32_t next = __shfl_sync(ISG_FULL_MASK, wa, lane0 + (int)((k4 + 1) & rwm));
         const uint32_t wx = p ? __funnelshift_r(wa, next, 8) : __funnelshift_l(prev, wa, 8);
+        uint32_t nd = wx + wa + wyp + wym;
+        if (DIM == 3) nd += wzp + wzm;
         const uint32_t ow = own[w];
         uint32_t nw = ow;
         if (MODE != 2) {
-            uint32_t nd2 = (wx & M2) + (wa & M2) + (wyp & M2) + (wym & M2);
-            if (DIM == 3) nd2 += (wzp & M2) + (wzm & M2);
-            const uint32_t idx4 = (nd2 << 1) + ((ow & M2) << 4);
-            const U4 u = philox10(w, uid, c2, c3, k0, k1);
-            const uint32_t t0 = *reinterpret_cast<const uint32_t*>(tb + (idx4 & 0xFFu));
-            const uint32_t t1 = *reinterpret_cast<const uint32_t*>(tb + ((idx4 >> 8) & 0xFFu));
-            const uint32_t t2 = *reinterpret_cast<const uint32_t*>(tb + ((idx4 >> 16) & 0xFFu));
-            const uint32_t t3 = *reinterpret_cast<const uint32_t*>(tb + (idx4 >> 24));
-            const uint32_t flip = (u.x <= t0 ? 0x00000001u : 0u) | (u.y <= t1 ? 0x00000100u : 0u) |
-                                  (u.z <= t2 ? 0x00010000u : 0u) | (u.w <= t3 ? 0x01000000u : 0u);
-            nw = ow ^ (flip * 0xFEu);
+            const U4 u = philox_w(pre, w, k0, k1);
+            nw = metropolis_word(ow, nd, tbase, u);
             own[w] = nw;
         }
-        if (MODE != 0) {
-            int b = __dp4a((int)nw, (int)wx, 0);
-            b = __dp4a((int)nw, (int)wa, b);
-            b = __dp4a((int)nw, (int)wyp, b);
-            b = __dp4a((int)nw, (int)wym, b);
-            if (DIM == 3) {
-                b = __dp4a((int)nw, (int)wzp, b);
-                b = __dp4a((int)nw, (int)wzm, b);
-            }
-            accb += b;
-            accm += __dp4a((int)nw, 0x01010101, 0) + __dp4a((int)wa, 0x01010101, 0);
-        }
+        if (MODE != 0) meas_add(macc, nw, nd, wa);
     }
-    if (MODE != 0) flush_acc(P.acc, cur_rep, accb, accm, lane);
+    if (MODE != 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
 }
 
 template <int DIM, int MODE>
@@ -257,41 +390,36 @@ __global__ void __launch_bounds__(kMaxThreads)
         const uint32_t Lu = (uint32_t)L;
         const uint32_t xp = (x + 1) % Lu, xm = (x + Lu - 1) % Lu;
         const uint32_t yp = (y + 1) % Lu, ym = (y + Lu - 1) % Lu;
-        int8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
-        int8_t* own = base + (int64_t)colour * C.plane_sites;
-        const int8_t* oth = base + (int64_t)(colour ^ 1) * C.plane_sites;
+        uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
+        uint8_t* own = base + (int64_t)colour * C.plane_sites;
+        const uint8_t* oth = base + (int64_t)(colour ^ 1) * C.plane_sites;
         const uint64_t rowL = (uint64_t)(z * Lu + y) * Lu;
-        int nb[6];
-        nb[0] = oth[(rowL + xp) >> 1];
-        nb[1] = oth[(rowL + xm) >> 1];
-        nb[2] = oth[((uint64_t)(z * Lu + yp) * Lu + x) >> 1];
-        nb[3] = oth[((uint64_t)(z * Lu + ym) * Lu + x) >> 1];
-        int nsum = nb[0] + nb[1] + nb[2] + nb[3];
-        int nd = (nb[0] < 0) + (nb[1] < 0) + (nb[2] < 0) + (nb[3] < 0);
+        int nd = oth[(rowL + xp) >> 1] + oth[(rowL + xm) >> 1] +
+                 oth[((uint64_t)(z * Lu + yp) * Lu + x) >> 1] +
+                 oth[((uint64_t)(z * Lu + ym) * Lu + x) >> 1];
         if (DIM == 3) {
             const uint32_t zp = (z + 1) % Lu, zm = (z + Lu - 1) % Lu;
-            nb[4] = oth[((uint64_t)(zp * Lu + y) * Lu + x) >> 1];
-            nb[5] = oth[((uint64_t)(zm * Lu + y) * Lu + x) >> 1];
-            nsum += nb[4] + nb[5];
-            nd += (nb[4] < 0) + (nb[5] < 0);
+            nd += oth[((uint64_t)(zp * Lu + y) * Lu + x) >> 1] +
+                  oth[((uint64_t)(zm * Lu + y) * Lu + x) >> 1];
         }
-        int s = own[i];
+        int d = own[i];
         if (MODE != 2) {
             const int rg = C.rep_base + r;
             const int slot = C.rep_base + P.r2t[rg];
-            const uint32_t th = P.thr[slot * 16 + (s < 0 ? 8 : 0) + nd];
-            const U4 u = philox10(i >> 2, replica_uid(L, r), c2, c3, k0, k1);
+            const uint32_t th = P.thr[slot * 16 + d * 8 + nd];
+            const U4 u = philox10(replica_uid(L, r), i >> 2, c2, c3, k0, k1);
             const uint32_t j = i & 3u;
             const uint32_t uu = j == 0 ? u.x : j == 1 ? u.y : j == 2 ? u.z : u.w;
             if (uu <= th) {
-                s = -s;
-                own[i] = (int8_t)s;
+                d ^= 1;
+                own[i] = (uint8_t)d;
             }
         }
         if (MODE != 0) {
             const int rg = C.rep_base + r;
-            const long long b = (long long)(s * nsum);
-            const long long m = (long long)(s + oth[i]);
+            const int s = 1 - 2 * d;
+            const long long b = (long long)(s * (2 * DIM - 2 * nd));
+            const long long m = (long long)(s + 1 - 2 * oth[i]);
             atomicAdd(&P.acc[2 * rg], (unsigned long long)b);
             atomicAdd(&P.acc[2 * rg + 1], (unsigned long long)m);
         }
@@ -299,7 +427,8 @@ __global__ void __launch_bounds__(kMaxThreads)
 }
 
 // Hot start: natural site n of replica r gets -1 if the top bit of word
-// (n & 3) of Philox(n >> 2, uid, 0, INIT) is set, else +1.
+// (n & 3) of Philox(uid, n >> 2, 0, INIT) is set, else +1 (stored as the
+// down bit).
 __global__ void k_ising_init(const __grid_constant__ IsingParams P, int dim) {
     const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
     const uint32_t c3 = counter_word3(ISG_TAG_INIT, 0, 0);
@@ -311,7 +440,7 @@ __global__ void k_ising_init(const __grid_constant__ IsingParams P, int dim) {
              g += (int64_t)gridDim.x * blockDim.x) {
             const int r = (int)(g / nsite);
             const uint32_t n = (uint32_t)(g - (int64_t)r * nsite);
-            const U4 u = philox10(n >> 2, replica_uid(C.L, r), 0, c3, k0, k1);
+            const U4 u = philox10(replica_uid(C.L, r), n >> 2, 0, c3, k0, k1);
             const uint32_t j = n & 3u;
             const uint32_t wv = j == 0 ? u.x : j == 1 ? u.y : j == 2 ? u.z : u.w;
             const uint32_t L = (uint32_t)C.L;
@@ -320,7 +449,7 @@ __global__ void k_ising_init(const __grid_constant__ IsingParams P, int dim) {
             const uint32_t z = dim == 3 ? n / (L * L) : 0;
             const uint32_t c = (x + y + z) & 1u;
             P.spins[C.spin_off + (int64_t)r * nsite + (int64_t)c * C.plane_sites + (n >> 1)] =
-                (wv >> 31) ? (int8_t)-1 : (int8_t)1;
+                (uint8_t)(wv >> 31);
         }
     }
 }
@@ -387,7 +516,7 @@ __global__ void k_ising_post(const __grid_constant__ PostParams Q, int do_record
                                        __dsub_rn(s_e[rj], s_e[ri]));
             bool ok = d < 0.0;
             if (!ok) {
-                const U4 u = philox10((uint32_t)i, exchange_uid(Q.L[s]), (uint32_t)xc, c3, k0, k1);
+                const U4 u = philox10(exchange_uid(Q.L[s]), (uint32_t)i, (uint32_t)xc, c3, k0, k1);
                 ok = uniform53(u.x, u.y) < exp(-d);
             }
             if (ok) {
@@ -447,7 +576,7 @@ struct isg_ising {
     std::vector<int> sizes;
     IsingParams P{};
     PostParams Q{};
-    int8_t* d_spins = nullptr;
+    uint8_t* d_spins = nullptr;
     int64_t spin_bytes = 0;
     uint32_t* d_thr = nullptr;
     int32_t* d_r2t = nullptr;
@@ -655,26 +784,25 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         C.plane_sites = (uint32_t)(nsite / 2);
         const bool pow2 = (L & (L - 1)) == 0;
         const int rw = L / 8;
-        C.word_path = (pow2 && L >= 8 && L <= 256 && (32 % rw) == 0 &&
-                       (C.plane_sites / 4) % 32 == 0)
-                          ? 1
-                          : 0;
+        const bool words = pow2 && L >= 8 && L <= 256 && (32 % rw) == 0 &&
+                           (C.plane_sites / 4) % 32 == 0;
+        C.kind = !words ? kSite : (dim == 3 && L >= 64) ? kRolling : kFlat;
         C.log2L = 0;
         while ((1 << C.log2L) < L) ++C.log2L;
-        C.log2_row_words = 0;
-        if (C.word_path)
-            while ((1 << C.log2_row_words) < rw) ++C.log2_row_words;
-        C.tasks_per_plane = C.word_path ? C.plane_sites / 128 : 0;
+        C.log2_rw = 0;
+        if (words)
+            while ((1 << C.log2_rw) < rw) ++C.log2_rw;
+        C.tasks_per_plane = words ? C.plane_sites / 128 : 0;
         C.log2_tpp = 0;
-        while (C.word_path && (1u << C.log2_tpp) < C.tasks_per_plane) ++C.log2_tpp;
+        while (words && (1u << C.log2_tpp) < C.tasks_per_plane) ++C.log2_tpp;
         C.rep_base = s * replicas;
         C.spin_off = off;
         off += ((2 * (int64_t)C.plane_sites * replicas + 255) / 256) * 256;
         C.task_base = task;
-        if (C.word_path) task += (int64_t)C.tasks_per_plane * replicas;
+        if (C.kind != kSite) task += (int64_t)C.tasks_per_plane * replicas;
         C.task_end = task;
         C.site_base = site;
-        if (!C.word_path) site += (int64_t)C.plane_sites * replicas;
+        if (C.kind == kSite) site += (int64_t)C.plane_sites * replicas;
         C.site_end = site;
     }
     // sentinel classes so the device class search always terminates
@@ -684,6 +812,7 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         P.cls[s].site_base = P.cls[s].site_end = INT64_MAX;
     }
     P.n_classes = n_sizes;
+    P.dim = dim;
     P.total_tasks = task;
     P.total_sites = site;
     P.seed = seed;
@@ -938,7 +1067,7 @@ int isg_ising_get_spins(isg_ising* H, int s, int r, int8_t* out) {
     int64_t n, base;
     int rc = spin_geometry(H, s, r, &n, &base);
     if (rc) return rc;
-    std::vector<int8_t> planes((size_t)n);
+    std::vector<uint8_t> planes((size_t)n);
     ISG_CK(cudaMemcpyAsync(planes.data(), H->d_spins + base, (size_t)n, cudaMemcpyDeviceToHost,
                            H->stream));
     ISG_CK(cudaStreamSynchronize(H->stream));
@@ -947,7 +1076,7 @@ int isg_ising_get_spins(isg_ising* H, int s, int r, int8_t* out) {
     for (int64_t i = 0; i < n; ++i) {
         const int64_t x = i % L, y = (i / L) % L, z = H->dim == 3 ? i / ((int64_t)L * L) : 0;
         const int c = (int)((x + y + z) & 1);
-        out[i] = planes[(size_t)(c * half + (i >> 1))];
+        out[i] = planes[(size_t)(c * half + (i >> 1))] ? (int8_t)-1 : (int8_t)1;
     }
     return ISG_OK;
 }
@@ -958,7 +1087,7 @@ int isg_ising_set_spins(isg_ising* H, int s, int r, const int8_t* in) {
     int64_t n, base;
     int rc = spin_geometry(H, s, r, &n, &base);
     if (rc) return rc;
-    std::vector<int8_t> planes((size_t)n);
+    std::vector<uint8_t> planes((size_t)n);
     const int L = H->sizes[s];
     const int64_t half = n / 2;
     for (int64_t i = 0; i < n; ++i) {
@@ -966,7 +1095,7 @@ int isg_ising_set_spins(isg_ising* H, int s, int r, const int8_t* in) {
             return fail(ISG_ERR_ARG, "isg_ising_set_spins: spins must be +1 or -1");
         const int64_t x = i % L, y = (i / L) % L, z = H->dim == 3 ? i / ((int64_t)L * L) : 0;
         const int c = (int)((x + y + z) & 1);
-        planes[(size_t)(c * half + (i >> 1))] = in[i];
+        planes[(size_t)(c * half + (i >> 1))] = in[i] < 0 ? 1 : 0;
     }
     ISG_CK(cudaMemcpyAsync(H->d_spins + base, planes.data(), (size_t)n, cudaMemcpyHostToDevice,
                            H->stream));
@@ -1117,7 +1246,7 @@ int isg_ising_set_launch(isg_ising* H, int threads, int blocks_per_sm) {
 // Runs n sweeps' worth of half-sweeps on the live buffers, timing each launch,
 // then restores the spins and the sweep counter.
 static int timed_halfsweeps(isg_ising* H, int n_launches, float* avg_ms) {
-    int8_t* backup = nullptr;
+    uint8_t* backup = nullptr;
     ISG_CK(cudaMalloc((void**)&backup, (size_t)H->spin_bytes));
     unsigned long long ctrl0 = 0;
     cudaError_t e = cudaMemcpyAsync(backup, H->d_spins, (size_t)H->spin_bytes,

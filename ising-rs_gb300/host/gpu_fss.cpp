@@ -1,0 +1,521 @@
+// gpu_fss — drop-in for the reference's src/bin/gpu_fss.rs on libisinggb.
+//
+// Same flags and defaults (gpu_fss.rs:23-96, unknown flags ignored, malformed
+// --sizes entries dropped), the same validation messages and exit codes
+// (cli.rs:10-28,86-107; gpu_fss.rs:103-109,158-161), the same CSV files:
+//   gpu_fss_{model}_N{n}_timeseries.csv  "temp_idx,E,M" rows, {:.8}
+//   gpu_fss_{model}_N{n}_summary.csv     jackknife table, {:.6}
+// (gpu_fss.rs:212-320, 476-580).  Differences by design:
+//   * all sizes and replicas run together in one batch (one persistent kernel
+//     per half-sweep) instead of one size after another;
+//   * spins start from the seeded Philox stream (the reference's start is
+//     unseeded) and the exchange uses the Philox EXCH stream instead of a host
+//     Xoshiro256++ (gpu_fss.rs:197);
+//   * continuous models propose inside a cone of half-angle --delta
+//     (heisenberg/metropolis.rs:54-69; XY: angle step uniform in [-delta,
+//     delta]) and renormalise every --renorm-every sweeps (new flag,
+//     default 100);
+//   * odd or repeated sizes are rejected/merged (the reference kernel
+//     mapping is wrong for odd N, kernels.cu:28).
+#include <errno.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "isg.h"
+
+namespace {
+
+[[noreturn]] void die(const std::string& msg) {
+    fprintf(stderr, "%s\n", msg.c_str());
+    exit(1);
+}
+
+// Rust's `expect` on an Err: panic message and exit code 101.
+[[noreturn]] void panic_expect(const char* what, const std::string& err) {
+    fprintf(stderr, "thread 'main' panicked at src/bin/gpu_fss.rs:\n%s: %s\n", what, err.c_str());
+    exit(101);
+}
+
+// f64 Display as Rust prints it: shortest round-trip digits, no exponent.
+std::string rust_f64(double x) {
+    if (isnan(x)) return "NaN";
+    if (isinf(x)) return x < 0 ? "-inf" : "inf";
+    if (x == 0.0) return signbit(x) ? "-0" : "0";
+    char buf[64];
+    int p = 1;
+    for (; p <= 17; ++p) {
+        snprintf(buf, sizeof buf, "%.*e", p - 1, x);
+        if (strtod(buf, nullptr) == x) break;
+    }
+    std::string s(buf);
+    bool neg = s[0] == '-';
+    if (neg) s = s.substr(1);
+    size_t epos = s.find('e');
+    int exp10 = atoi(s.c_str() + epos + 1);
+    std::string digits;
+    for (size_t i = 0; i < epos; ++i)
+        if (s[i] != '.') digits += s[i];
+    while (digits.size() > 1 && digits.back() == '0') digits.pop_back();
+    std::string out;
+    if (exp10 >= 0) {
+        if ((int)digits.size() <= exp10 + 1) {
+            out = digits + std::string(exp10 + 1 - digits.size(), '0');
+        } else {
+            out = digits.substr(0, exp10 + 1) + "." + digits.substr(exp10 + 1);
+        }
+    } else {
+        out = "0." + std::string(-exp10 - 1, '0') + digits;
+    }
+    return (neg ? "-" : "") + out;
+}
+
+std::string get_arg(int argc, char** argv, int i, const char* flag) {
+    if (i + 1 >= argc) die(std::string("Error: ") + flag + " requires a value");
+    return argv[i + 1];
+}
+
+// Rust's str::parse::<usize>/<u64>: optional '+', decimal digits only.
+bool parse_unsigned(const std::string& v, uint64_t* out, std::string* err) {
+    if (v.empty()) {
+        *err = "cannot parse integer from empty string";
+        return false;
+    }
+    size_t i = 0;
+    if (v[0] == '+') i = 1;
+    if (i >= v.size()) {
+        *err = "invalid digit found in string";
+        return false;
+    }
+    uint64_t x = 0;
+    for (; i < v.size(); ++i) {
+        if (v[i] < '0' || v[i] > '9') {
+            *err = "invalid digit found in string";
+            return false;
+        }
+        uint64_t d = (uint64_t)(v[i] - '0');
+        if (x > (UINT64_MAX - d) / 10) {
+            *err = "number too large to fit in target type";
+            return false;
+        }
+        x = x * 10 + d;
+    }
+    *out = x;
+    return true;
+}
+
+bool parse_f64(const std::string& v, double* out, std::string* err) {
+    if (v.empty()) {
+        *err = "cannot parse float from empty string";
+        return false;
+    }
+    for (char c : v)
+        if (isspace((unsigned char)c) || c == 'x' || c == 'X' || c == 'p' || c == 'P') {
+            *err = "invalid float literal";
+            return false;
+        }
+    char* end = nullptr;
+    errno = 0;
+    double x = strtod(v.c_str(), &end);
+    if (end == v.c_str() || *end != '\0') {
+        *err = "invalid float literal";
+        return false;
+    }
+    *out = x;
+    return true;
+}
+
+template <class T>
+T parse_arg(int argc, char** argv, int i, const char* flag);
+
+template <>
+uint64_t parse_arg<uint64_t>(int argc, char** argv, int i, const char* flag) {
+    std::string v = get_arg(argc, argv, i, flag), err;
+    uint64_t x = 0;
+    if (!parse_unsigned(v, &x, &err))
+        die("Error: invalid value '" + v + "' for " + flag + ": " + err);
+    return x;
+}
+
+template <>
+double parse_arg<double>(int argc, char** argv, int i, const char* flag) {
+    std::string v = get_arg(argc, argv, i, flag), err;
+    double x = 0;
+    if (!parse_f64(v, &x, &err)) die("Error: invalid value '" + v + "' for " + flag + ": " + err);
+    return x;
+}
+
+std::vector<double> linspace(double a, double b, uint64_t n) {
+    std::vector<double> t;
+    if (n == 1) return {a};
+    for (uint64_t i = 0; i < n; ++i) t.push_back(a + (b - a) * (double)i / (double)(n - 1));
+    return t;
+}
+
+std::string join_path(const std::string& dir, const std::string& name) {
+    if (dir.empty()) return name;
+    if (dir.back() == '/') return dir + name;
+    return dir + "/" + name;
+}
+
+bool mkdirs(const std::string& path, std::string* err) {
+    std::string cur;
+    size_t i = 0;
+    if (!path.empty() && path[0] == '/') cur = "/", i = 1;
+    while (i <= path.size()) {
+        size_t j = path.find('/', i);
+        if (j == std::string::npos) j = path.size();
+        if (j > i) {
+            cur += path.substr(i, j - i);
+            if (mkdir(cur.c_str(), 0777) != 0 && errno != EEXIST) {
+                *err = std::string("Os { code: ") + std::to_string(errno) + ", message: \"" +
+                       strerror(errno) + "\" }";
+                return false;
+            }
+            struct stat st;
+            if (stat(cur.c_str(), &st) != 0 || !S_ISDIR(st.st_mode)) {
+                *err = "Os { code: 17, message: \"File exists\" }";
+                return false;
+            }
+            cur += "/";
+        }
+        i = j + 1;
+    }
+    return true;
+}
+
+struct Series {
+    std::vector<double> e, m;
+};
+
+void write_summary(const std::string& path, const std::vector<double>& temps,
+                   const std::vector<Series>& ts, double n3) {
+    std::string csv = "T,E,E_err,M,M_err,M2,M2_err,M4,M4_err,Cv,Cv_err,chi,chi_err\n";
+    char buf[64];
+    for (size_t t = 0; t < ts.size(); ++t) {
+        if (ts[t].e.empty()) continue;
+        const double beta = 1.0 / temps[t];
+        const int nb = (int)std::min<size_t>(20, ts[t].e.size());
+        double obs[12];
+        isg_jackknife(ts[t].e.data(), ts[t].m.data(), (int64_t)ts[t].e.size(), beta, n3, nb, obs);
+        snprintf(buf, sizeof buf, "%.6f", temps[t]);
+        csv += buf;
+        for (int k = 0; k < 12; ++k) {
+            snprintf(buf, sizeof buf, ",%.6f", obs[k]);
+            csv += buf;
+        }
+        csv += "\n";
+    }
+    FILE* f = fopen(path.c_str(), "w");
+    if (!f) panic_expect("write summary failed", strerror(errno));
+    fwrite(csv.data(), 1, csv.size(), f);
+    fclose(f);
+    fprintf(stderr, "  Wrote %s\n", path.c_str());
+}
+
+struct Run {
+    std::string model;
+    std::vector<int> sizes;
+    double tmin, tmax;
+    uint64_t R, warmup, samples, ee, seed, n_or, me, renorm;
+    std::string outdir;
+    double delta;
+};
+
+FILE* open_ts(const std::string& path) {
+    FILE* f = fopen(path.c_str(), "w");
+    if (!f) panic_expect("create timeseries file failed", strerror(errno));
+    fprintf(f, "temp_idx,E,M\n");
+    return f;
+}
+
+void empty_outputs(const Run& a, int n) {
+    // --replicas 0: header-only files, as the reference loops write them
+    std::string ts = join_path(a.outdir, "gpu_fss_" + a.model + "_N" + std::to_string(n) +
+                                             "_timeseries.csv");
+    fclose(open_ts(ts));
+    fprintf(stderr, "  Wrote %s\n", ts.c_str());
+    std::vector<double> temps;
+    std::vector<Series> none;
+    write_summary(join_path(a.outdir, "gpu_fss_" + a.model + "_N" + std::to_string(n) +
+                                          "_summary.csv"),
+                  temps, none, (double)n * n * n);
+}
+
+void run_ising(const Run& a) {
+    const std::vector<double> temps = linspace(a.tmin, a.tmax, a.R);
+    const int R = (int)a.R;
+    const int NS = (int)a.sizes.size();
+    if (R == 0) {
+        for (int n : a.sizes) empty_outputs(a, n);
+        return;
+    }
+    for (int n : a.sizes) fprintf(stderr, "  N=%d: creating %d replicas...\n", n, R);
+    isg_ising* h = nullptr;
+    if (isg_ising_create(&h, a.sizes.data(), NS, R, 3, a.seed) != ISG_OK)
+        panic_expect("failed to create GPU lattice", isg_last_error());
+    std::vector<double> all_t;
+    for (int s = 0; s < NS; ++s) all_t.insert(all_t.end(), temps.begin(), temps.end());
+    if (isg_ising_set_temperatures(h, all_t.data(), 1.0, 0.0) != ISG_OK)
+        panic_expect("GPU step failed", isg_last_error());
+    fprintf(stderr, "  warming up %llu sweeps...\n", (unsigned long long)a.warmup);
+    for (uint64_t w = 0; w < a.warmup;) {
+        uint64_t chunk = std::min<uint64_t>(1000 - w % 1000, a.warmup - w);
+        if (isg_ising_step(h, (int64_t)chunk) != ISG_OK)
+            panic_expect("GPU step failed", isg_last_error());
+        w += chunk;
+        if (w % 1000 == 0) {
+            isg_ising_sync(h);
+            fprintf(stderr, "    warmup %llu/%llu\n", (unsigned long long)w,
+                    (unsigned long long)a.warmup);
+        }
+    }
+    if (isg_ising_reset_sampling(h) != ISG_OK) panic_expect("GPU step failed", isg_last_error());
+    std::vector<FILE*> tsf(NS);
+    std::vector<std::string> tsp(NS);
+    for (int s = 0; s < NS; ++s) {
+        tsp[s] = join_path(a.outdir, "gpu_fss_ising_N" + std::to_string(a.sizes[s]) +
+                                         "_timeseries.csv");
+        tsf[s] = open_ts(tsp[s]);
+    }
+    if (a.ee == 0) {
+        fprintf(stderr, "thread 'main' panicked at src/bin/gpu_fss.rs:245:30:\n"
+                        "attempt to calculate the remainder with a divisor of zero\n");
+        exit(101);
+    }
+    std::vector<std::vector<Series>> ts(NS, std::vector<Series>(R));
+    const int RT = NS * R;
+    fprintf(stderr, "  sampling %llu sweeps with PT exchange every %llu...\n",
+            (unsigned long long)a.samples, (unsigned long long)a.ee);
+    const uint64_t chunk_sweeps = 10000;
+    std::vector<int32_t> rt;
+    std::vector<int64_t> rb, rm;
+    char line[128];
+    for (uint64_t done = 0; done < a.samples;) {
+        uint64_t n = std::min<uint64_t>(chunk_sweeps - done % chunk_sweeps, a.samples - done);
+        uint64_t rows = n / a.me + 2;
+        rt.assign(rows * RT, 0);
+        rb.assign(rows * RT, 0);
+        rm.assign(rows * RT, 0);
+        int64_t got = 0;
+        if (isg_ising_pt_run(h, (int64_t)n, (int)std::min<uint64_t>(a.ee, 1u << 30),
+                             (int)std::min<uint64_t>(a.me, 1u << 30), rt.data(), rb.data(),
+                             rm.data(), (int64_t)rows, &got) != ISG_OK)
+            panic_expect("GPU step failed", isg_last_error());
+        for (int s = 0; s < NS; ++s) {
+            const double n3 = (double)a.sizes[s] * a.sizes[s] * a.sizes[s];
+            for (int64_t row = 0; row < got; ++row)
+                for (int r = 0; r < R; ++r) {
+                    const size_t o = (size_t)row * RT + (size_t)s * R + r;
+                    const int t = rt[o];
+                    const double e_per = -(double)rb[o] / n3;
+                    const double m_per = fabs((double)rm[o]) / n3;
+                    ts[s][t].e.push_back(e_per);
+                    ts[s][t].m.push_back(m_per);
+                    int k = snprintf(line, sizeof line, "%d,%.8f,%.8f\n", t, e_per, m_per);
+                    fwrite(line, 1, (size_t)k, tsf[s]);
+                }
+        }
+        done += n;
+        if (done % 10000 == 0)
+            fprintf(stderr, "    sweep %llu/%llu\n", (unsigned long long)done,
+                    (unsigned long long)a.samples);
+    }
+    for (int s = 0; s < NS; ++s) {
+        fclose(tsf[s]);
+        fprintf(stderr, "  Wrote %s\n", tsp[s].c_str());
+        const double n3 = (double)a.sizes[s] * a.sizes[s] * a.sizes[s];
+        write_summary(join_path(a.outdir, "gpu_fss_ising_N" + std::to_string(a.sizes[s]) +
+                                              "_summary.csv"),
+                      temps, ts[s], n3);
+    }
+    isg_ising_destroy(h);
+}
+
+void run_continuous(const Run& a, int n_comp) {
+    const std::vector<double> temps = linspace(a.tmin, a.tmax, a.R);
+    const int R = (int)a.R;
+    const int NS = (int)a.sizes.size();
+    if (R == 0) {
+        for (int n : a.sizes) empty_outputs(a, n);
+        return;
+    }
+    for (int n : a.sizes)
+        fprintf(stderr, "  N=%d: creating %d %s replicas...\n", n, R, a.model.c_str());
+    isg_cont* h = nullptr;
+    if (isg_cont_create(&h, a.sizes.data(), NS, R, n_comp, a.seed) != ISG_OK)
+        panic_expect("failed to create continuous GPU lattice", isg_last_error());
+    std::vector<double> all_t;
+    for (int s = 0; s < NS; ++s) all_t.insert(all_t.end(), temps.begin(), temps.end());
+    if (isg_cont_set_temperatures(h, all_t.data(), 1.0) != ISG_OK)
+        panic_expect("sweep failed", isg_last_error());
+    fprintf(stderr, "  warming up %llu sweeps...\n", (unsigned long long)a.warmup);
+    for (uint64_t w = 0; w < a.warmup;) {
+        uint64_t chunk = std::min<uint64_t>(1000 - w % 1000, a.warmup - w);
+        if (isg_cont_sweep(h, (int64_t)chunk, a.delta, (int)a.n_or) != ISG_OK)
+            panic_expect("sweep failed", isg_last_error());
+        w += chunk;
+        if (w % 1000 == 0) {
+            isg_cont_sync(h);
+            fprintf(stderr, "    warmup %llu/%llu\n", (unsigned long long)w,
+                    (unsigned long long)a.warmup);
+        }
+    }
+    if (isg_cont_reset_sampling(h) != ISG_OK) panic_expect("sweep failed", isg_last_error());
+    std::vector<FILE*> tsf(NS);
+    std::vector<std::string> tsp(NS);
+    for (int s = 0; s < NS; ++s) {
+        tsp[s] = join_path(a.outdir, "gpu_fss_" + a.model + "_N" + std::to_string(a.sizes[s]) +
+                                         "_timeseries.csv");
+        tsf[s] = open_ts(tsp[s]);
+    }
+    if (a.ee == 0) {
+        fprintf(stderr, "thread 'main' panicked at src/bin/gpu_fss.rs:504:30:\n"
+                        "attempt to calculate the remainder with a divisor of zero\n");
+        exit(101);
+    }
+    std::vector<std::vector<Series>> ts(NS, std::vector<Series>(R));
+    const int RT = NS * R;
+    fprintf(stderr, "  sampling %llu sweeps with PT (measure every %llu)...\n",
+            (unsigned long long)a.samples, (unsigned long long)a.me);
+    std::vector<int32_t> rt;
+    std::vector<double> re, rmv, rh;
+    char line[128];
+    for (uint64_t done = 0; done < a.samples;) {
+        uint64_t n = std::min<uint64_t>(10000 - done % 10000, a.samples - done);
+        uint64_t rows = n / a.me + 2;
+        rt.assign(rows * RT, 0);
+        re.assign(rows * RT, 0.0);
+        rmv.assign(rows * RT * 3, 0.0);
+        rh.assign(rows * RT * 6, 0.0);
+        int64_t got = 0;
+        if (isg_cont_pt_run(h, (int64_t)n, (int)std::min<uint64_t>(a.ee, 1u << 30),
+                            (int)std::min<uint64_t>(a.me, 1u << 30), a.delta, (int)a.n_or,
+                            (int)std::min<uint64_t>(a.renorm, 1u << 30), rt.data(), re.data(),
+                            rmv.data(), rh.data(), (int64_t)rows, &got) != ISG_OK)
+            panic_expect("sweep failed", isg_last_error());
+        for (int s = 0; s < NS; ++s) {
+            const double n3 = (double)a.sizes[s] * a.sizes[s] * a.sizes[s];
+            for (int64_t row = 0; row < got; ++row)
+                for (int r = 0; r < R; ++r) {
+                    const size_t o = (size_t)row * RT + (size_t)s * R + r;
+                    const int t = rt[o];
+                    const double* m = &rmv[o * 3];
+                    const double e_per = re[o] / n3;
+                    const double m_abs = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]) / n3;
+                    ts[s][t].e.push_back(e_per);
+                    ts[s][t].m.push_back(m_abs);
+                    int k = snprintf(line, sizeof line, "%d,%.8f,%.8f\n", t, e_per, m_abs);
+                    fwrite(line, 1, (size_t)k, tsf[s]);
+                }
+        }
+        done += n;
+        if (done % 10000 == 0)
+            fprintf(stderr, "    sweep %llu/%llu\n", (unsigned long long)done,
+                    (unsigned long long)a.samples);
+    }
+    for (int s = 0; s < NS; ++s) {
+        fclose(tsf[s]);
+        fprintf(stderr, "  Wrote %s\n", tsp[s].c_str());
+        const double n3 = (double)a.sizes[s] * a.sizes[s] * a.sizes[s];
+        write_summary(join_path(a.outdir, "gpu_fss_" + a.model + "_N" +
+                                              std::to_string(a.sizes[s]) + "_summary.csv"),
+                      temps, ts[s], n3);
+    }
+    isg_cont_destroy(h);
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    Run a;
+    a.model = "ising";
+    std::string sizes_str = "8,16,32,64";
+    a.tmin = 4.4;
+    a.tmax = 4.6;
+    a.R = 20;
+    a.warmup = 5000;
+    a.samples = 100000;
+    a.ee = 10;
+    a.seed = 42;
+    a.outdir = "analysis/data";
+    a.delta = 0.5;
+    a.n_or = 5;
+    a.me = 1;
+    a.renorm = 100;
+    int i = 1;
+    while (i < argc) {
+        std::string f = argv[i];
+        if (f == "--model") a.model = get_arg(argc, argv, i, "--model"), i += 2;
+        else if (f == "--sizes") sizes_str = get_arg(argc, argv, i, "--sizes"), i += 2;
+        else if (f == "--tmin") a.tmin = parse_arg<double>(argc, argv, i, "--tmin"), i += 2;
+        else if (f == "--tmax") a.tmax = parse_arg<double>(argc, argv, i, "--tmax"), i += 2;
+        else if (f == "--replicas") a.R = parse_arg<uint64_t>(argc, argv, i, "--replicas"), i += 2;
+        else if (f == "--warmup") a.warmup = parse_arg<uint64_t>(argc, argv, i, "--warmup"), i += 2;
+        else if (f == "--samples") a.samples = parse_arg<uint64_t>(argc, argv, i, "--samples"), i += 2;
+        else if (f == "--exchange-every")
+            a.ee = parse_arg<uint64_t>(argc, argv, i, "--exchange-every"), i += 2;
+        else if (f == "--seed") a.seed = parse_arg<uint64_t>(argc, argv, i, "--seed"), i += 2;
+        else if (f == "--outdir") a.outdir = get_arg(argc, argv, i, "--outdir"), i += 2;
+        else if (f == "--delta") a.delta = parse_arg<double>(argc, argv, i, "--delta"), i += 2;
+        else if (f == "--overrelax") a.n_or = parse_arg<uint64_t>(argc, argv, i, "--overrelax"), i += 2;
+        else if (f == "--measure-every")
+            a.me = parse_arg<uint64_t>(argc, argv, i, "--measure-every"), i += 2;
+        else if (f == "--renorm-every")
+            a.renorm = parse_arg<uint64_t>(argc, argv, i, "--renorm-every"), i += 2;
+        else i += 1;
+    }
+    // sizes: comma-separated, trimmed, malformed entries dropped (gpu_fss.rs:98-101)
+    std::vector<int> sizes_all;
+    size_t p = 0;
+    while (p <= sizes_str.size()) {
+        size_t q = sizes_str.find(',', p);
+        if (q == std::string::npos) q = sizes_str.size();
+        std::string tok = sizes_str.substr(p, q - p);
+        size_t b = tok.find_first_not_of(" \t\n\r"), e = tok.find_last_not_of(" \t\n\r");
+        tok = b == std::string::npos ? "" : tok.substr(b, e - b + 1);
+        uint64_t v = 0;
+        std::string err;
+        if (parse_unsigned(tok, &v, &err) && v <= 0x7FFFFFFF) sizes_all.push_back((int)v);
+        p = q + 1;
+    }
+    // validate_temp_range / validate_samples (cli.rs:86-107), gpu_fss.rs:103-109
+    if (a.tmin <= 0.0) die("Error: --tmin must be positive (got " + rust_f64(a.tmin) + ")");
+    if (a.tmax <= 0.0) die("Error: --tmax must be positive (got " + rust_f64(a.tmax) + ")");
+    if (a.tmin >= a.tmax)
+        die("Error: --tmin (" + rust_f64(a.tmin) + ") must be less than --tmax (" +
+            rust_f64(a.tmax) + ")");
+    if (a.samples == 0) die("Error: --samples must be at least 1");
+    if (a.warmup == 0) die("Error: --warmup must be at least 1");
+    if (a.me == 0) die("Error: --measure-every must be at least 1");
+    std::string err;
+    if (!mkdirs(a.outdir, &err)) panic_expect("failed to create outdir", err);
+    std::string sz = "[";
+    for (size_t k = 0; k < sizes_all.size(); ++k)
+        sz += (k ? ", " : "") + std::to_string(sizes_all[k]);
+    sz += "]";
+    fprintf(stderr, "GPU FSS: model=%s, sizes=%s, T=%s..%s, replicas=%llu\n", a.model.c_str(),
+            sz.c_str(), rust_f64(a.tmin).c_str(), rust_f64(a.tmax).c_str(),
+            (unsigned long long)a.R);
+    if (a.model != "ising" && a.model != "xy" && a.model != "heisenberg")
+        die("Error: --model must be ising, xy, or heisenberg");
+    for (int n : sizes_all) {
+        if (n < 2 || n > 1024 || (n & 1))
+            die("Error: size " + std::to_string(n) +
+                " unsupported: the checkerboard update needs an even size in 2..1024");
+        if (std::find(a.sizes.begin(), a.sizes.end(), n) == a.sizes.end()) a.sizes.push_back(n);
+    }
+    if (a.R > 1024) die("Error: --replicas must be at most 1024");
+    if (a.sizes.size() > 16) die("Error: at most 16 distinct sizes per run");
+    if (a.sizes.empty()) return 0;
+    if (a.model == "ising") run_ising(a);
+    else run_continuous(a, a.model == "xy" ? 2 : 3);
+    return 0;
+}

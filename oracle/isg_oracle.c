@@ -83,10 +83,11 @@ void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out
 #define TAG_CINIT 0x04u
 #define TAG_CMETRO 0x05u
 
-static void stream_words(uint64_t seed, uint32_t c0, uint32_t uid, uint64_t step, uint32_t tag,
+/* counter = {stream uid, index, lo32(step), tag | colour | hi16(step)} */
+static void stream_words(uint64_t seed, uint32_t index, uint32_t uid, uint64_t step, uint32_t tag,
                          uint32_t colour, uint32_t out[4]) {
     uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-    uint32_t ctr[4] = {c0, uid, (uint32_t)step,
+    uint32_t ctr[4] = {uid, index, (uint32_t)step,
                        (tag << 24) | (colour << 16) | ((uint32_t)(step >> 32) & 0xFFFFu)};
     or_philox4x32_10(ctr, key, out);
 }

@@ -76,8 +76,35 @@ def _bind_cont(L):
                                      C.c_uint64, C.c_double, C.c_double, C.c_double,
                                      C.POINTER(C.c_int64)]
     L.or_cont_measure.argtypes = [C.c_int, C.c_int, f64p, f64p]
-    L.or_cont_ref_run.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_uint64,
-                                  C.c_int64, C.c_int64, f64p, f64p]
+    L.or_cont_ref_sweep.argtypes = [C.c_int, f64p, C.c_double, C.c_double, C.c_double,
+                                    C.c_uint64, C.c_uint64, C.c_int]
+
+
+def cont_hot_start(L: int, nc: int, seed: int, r: int) -> np.ndarray:
+    s = np.zeros(L ** 3 * nc, np.float64)
+    lib().or_cont_hot_start(L, nc, seed, replica_uid(L, r), s)
+    return s
+
+
+def cont_overrelax(s: np.ndarray, L: int, nc: int, colour: int, J: float = 1.0) -> None:
+    lib().or_cont_overrelax(L, nc, s, colour, J)
+
+
+def cont_metropolis(s, L, nc, colour, seed, r, sweep, beta, J, delta) -> int:
+    acc = C.c_int64(0)
+    lib().or_cont_metropolis(L, nc, s, colour, seed, replica_uid(L, r), sweep, beta, J, delta,
+                             C.byref(acc))
+    return acc.value
+
+
+def cont_measure(s: np.ndarray, L: int, nc: int) -> np.ndarray:
+    out = np.zeros(10, np.float64)
+    lib().or_cont_measure(L, nc, s, out)
+    return out
+
+
+def cont_ref_sweep(s, L, beta, J, delta, seed, sweep, n_or) -> None:
+    lib().or_cont_ref_sweep(L, s, beta, J, delta, seed, sweep, n_or)
 
 
 def nsites(L: int, dim: int = 3) -> int:

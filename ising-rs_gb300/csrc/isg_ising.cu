@@ -82,6 +82,9 @@ struct IsingClass {
     int64_t spin_off;         // byte offset of replica 0 colour 0
     int64_t task_base;        // word kinds: first warp task
     int64_t task_end;
+    int64_t ctask_base;       // word kinds: first CTA task (8 warp tasks)
+    int64_t ctask_end;
+    int log2_groups;          // rolling: log2(column groups of 8 per replica)
     int64_t site_base;        // site kind: first site (over colour planes)
     int64_t site_end;
 };
@@ -96,65 +99,62 @@ struct IsingParams {
     int n_classes;
     int dim;
     int64_t total_tasks;
+    int64_t total_ctasks;
     int64_t total_sites;
+    uint32_t rk0[10], rk1[10];      // Philox round keys (constant-bank operands)
     IsingClass cls[kMaxClasses];
 };
 
 // ---------------------------------------------------------------- kernels
 
 // Philox4x32-10 of counter {uid, w, c2, c3} with the warp-uniform part of the
-// first three rounds (everything that does not depend on w) computed once.
+// first three rounds (everything that does not depend on w) computed once per
+// replica.  Products are formed as 64-bit values (one wide multiply each).
 struct PhiloxPre {
-    uint32_t x0, a1, a2, x2, b0, b1, x3, hi02, lo02;
+    uint32_t x0, x2, x3, hi02, lo02;
 };
+
+__device__ __forceinline__ uint64_t mulw(uint32_t a, uint32_t b) { return (uint64_t)a * b; }
 
 __device__ __forceinline__ PhiloxPre philox_pre(uint32_t uid, uint32_t c2, uint32_t c3,
                                                 uint32_t k0, uint32_t k1) {
     PhiloxPre p;
     // round 0: M0*uid and M1*c2 are uniform
-    const uint32_t hi0 = __umulhi(kPhiloxM0, uid), lo0 = kPhiloxM0 * uid;
-    const uint32_t hi1 = __umulhi(kPhiloxM1, c2), lo1 = kPhiloxM1 * c2;
-    p.x0 = hi1 ^ k0;       // a0 = x0 ^ w
-    p.a1 = lo1;
-    p.a2 = hi0 ^ c3 ^ k1;
-    const uint32_t a3 = lo0;
-    // round 1 (keys + 1*W): M1*a2 uniform
-    const uint32_t k01 = k0 + kPhiloxW0, k11 = k1 + kPhiloxW1;
-    const uint32_t h1 = __umulhi(kPhiloxM1, p.a2), l1 = kPhiloxM1 * p.a2;
-    p.b0 = h1 ^ p.a1 ^ k01;
-    p.b1 = l1;
-    p.x2 = a3 ^ k11;       // b2 = hi(M0*a0) ^ x2, b3 = lo(M0*a0)
-    // round 2 (keys + 2*W): M0*b0 uniform
-    const uint32_t k02 = k0 + 2u * kPhiloxW0, k12 = k1 + 2u * kPhiloxW1;
-    p.hi02 = __umulhi(kPhiloxM0, p.b0) ^ k12;  // c2 = b3 ^ hi02
-    p.lo02 = kPhiloxM0 * p.b0;                 // c3
-    p.x3 = p.b1 ^ k02;                         // c0 = hi(M1*b2) ^ x3
+    const uint64_t p0 = mulw(kPhiloxM0, uid), p1 = mulw(kPhiloxM1, c2);
+    p.x0 = (uint32_t)(p1 >> 32) ^ k0;  // a0 = x0 ^ w
+    const uint32_t a1 = (uint32_t)p1;
+    const uint32_t a2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+    const uint32_t a3 = (uint32_t)p0;
+    // round 1 (keys + W): M1*a2 uniform
+    const uint64_t q1 = mulw(kPhiloxM1, a2);
+    const uint32_t b0 = (uint32_t)(q1 >> 32) ^ a1 ^ (k0 + kPhiloxW0);
+    const uint32_t b1 = (uint32_t)q1;
+    p.x2 = a3 ^ (k1 + kPhiloxW1);  // b2 = hi(M0*a0) ^ x2, b3 = lo(M0*a0)
+    // round 2 (keys + 2W): M0*b0 uniform
+    const uint64_t q0 = mulw(kPhiloxM0, b0);
+    p.hi02 = (uint32_t)(q0 >> 32) ^ (k1 + 2u * kPhiloxW1);  // c2 = b3 ^ hi02
+    p.lo02 = (uint32_t)q0;                                  // c3
+    p.x3 = b1 ^ (k0 + 2u * kPhiloxW0);                      // c0 = hi(M1*b2) ^ x3
     return p;
 }
 
-__device__ __forceinline__ U4 philox_w(const PhiloxPre& p, uint32_t w, uint32_t k0, uint32_t k1) {
-    // round 0
+__device__ __forceinline__ U4 philox_w(const PhiloxPre& p, const IsingParams& P, uint32_t w) {
     const uint32_t a0 = p.x0 ^ w;
-    // round 1
-    const uint32_t b2 = __umulhi(kPhiloxM0, a0) ^ p.x2;
-    const uint32_t b3 = kPhiloxM0 * a0;
-    // round 2
-    uint32_t c0 = __umulhi(kPhiloxM1, b2) ^ p.x3;
-    uint32_t c1 = kPhiloxM1 * b2;
+    const uint64_t r1 = mulw(kPhiloxM0, a0);
+    const uint32_t b2 = (uint32_t)(r1 >> 32) ^ p.x2;
+    const uint32_t b3 = (uint32_t)r1;
+    const uint64_t r2 = mulw(kPhiloxM1, b2);
+    uint32_t c0 = (uint32_t)(r2 >> 32) ^ p.x3;
+    uint32_t c1 = (uint32_t)r2;
     uint32_t c2 = b3 ^ p.hi02;
     uint32_t c3 = p.lo02;
-    // rounds 3..9
-    uint32_t q0 = k0 + 3u * kPhiloxW0, q1 = k1 + 3u * kPhiloxW1;
 #pragma unroll
     for (int r = 3; r < 10; ++r) {
-        const uint32_t hi0 = __umulhi(kPhiloxM0, c0), lo0 = kPhiloxM0 * c0;
-        const uint32_t hi1 = __umulhi(kPhiloxM1, c2), lo1 = kPhiloxM1 * c2;
-        c0 = hi1 ^ c1 ^ q0;
-        c1 = lo1;
-        c2 = hi0 ^ c3 ^ q1;
-        c3 = lo0;
-        q0 += kPhiloxW0;
-        q1 += kPhiloxW1;
+        const uint64_t m0 = mulw(kPhiloxM0, c0), m1 = mulw(kPhiloxM1, c2);
+        c0 = (uint32_t)(m1 >> 32) ^ c1 ^ P.rk0[r];
+        c1 = (uint32_t)m1;
+        c2 = (uint32_t)(m0 >> 32) ^ c3 ^ P.rk1[r];
+        c3 = (uint32_t)m0;
     }
     return U4{c0, c1, c2, c3};
 }
@@ -175,17 +175,16 @@ __device__ __forceinline__ uint32_t metropolis_word(uint32_t ow, uint32_t nd, ui
     const uint32_t t1 = lds_u32(__byte_perm(idx4, tbase, 0x7651));
     const uint32_t t2 = lds_u32(__byte_perm(idx4, tbase, 0x7652));
     const uint32_t t3 = lds_u32(__byte_perm(idx4, tbase, 0x7653));
-    uint32_t flip = 0;
-    if (u.x <= t0) flip |= 0x00000001u;
-    if (u.y <= t1) flip |= 0x00000100u;
-    if (u.z <= t2) flip |= 0x00010000u;
-    if (u.w <= t3) flip |= 0x01000000u;
-    return ow ^ flip;
+    const uint32_t f0 = u.x <= t0 ? 0x00000001u : 0u;
+    const uint32_t f1 = u.y <= t1 ? 0x00000100u : 0u;
+    const uint32_t f2 = u.z <= t2 ? 0x00010000u : 0u;
+    const uint32_t f3 = u.w <= t3 ? 0x01000000u : 0u;
+    return ow ^ (f0 | f1 | f2 | f3);
 }
 
 __device__ __forceinline__ void flush_acc(unsigned long long* acc, int rep, long long b,
                                           long long m, int lane) {
-    // b, m are per-lane partial sums that fit in int32 before the reduction
+    // per-lane partial sums fit in int32 before the reduction
     const int sb = __reduce_add_sync(ISG_FULL_MASK, (int)b);
     const int sm = __reduce_add_sync(ISG_FULL_MASK, (int)m);
     if (lane == 0) {
@@ -214,107 +213,167 @@ __device__ __forceinline__ void meas_flush(unsigned long long* acc, int rep, Mea
     m = MeasAcc{0, 0, 0, 0, 0};
 }
 
+// One z-step of a rolling column: the word at plane offset `o` (words) of
+// the lane's column, given the other colour's words at z-1, z, z+1 and the
+// halo row(s).  Returns the new own word.
+template <int MODE>
+__device__ __forceinline__ uint32_t rolling_word(const IsingParams& P, const PhiloxPre& pre,
+                                                 uint32_t tbase, uint32_t w, uint32_t ow,
+                                                 uint32_t zm, uint32_t za, uint32_t zp,
+                                                 uint32_t h0, uint32_t h1, bool single_row,
+                                                 bool first, bool last, uint32_t p, int src_up,
+                                                 int src_dn, int src_prev, int src_next,
+                                                 uint32_t& nd_out) {
+    const uint32_t up = __shfl_sync(ISG_FULL_MASK, za, src_up);
+    const uint32_t dn = __shfl_sync(ISG_FULL_MASK, za, src_dn);
+    const uint32_t prev = __shfl_sync(ISG_FULL_MASK, za, src_prev);
+    const uint32_t next = __shfl_sync(ISG_FULL_MASK, za, src_next);
+    const uint32_t wyp = single_row ? h1 : (last ? h0 : up);
+    const uint32_t wym = first ? h0 : dn;
+    const uint32_t wx = p ? __funnelshift_r(za, next, 8) : __funnelshift_l(prev, za, 8);
+    const uint32_t nd = (wx + za + wyp) + (wym + zp + zm);
+    nd_out = nd;
+    if (MODE == 2) return ow;
+    const U4 u = philox_w(pre, P, w);
+    return metropolis_word(ow, nd, tbase, u);
+}
+
 // MODE 0: update; 1: update then accumulate bond/mag of the new state;
 // 2: accumulate only (no update).
+//
+// Work is split into CTA tasks of 8 warp tasks (blocks of 256 threads).  For
+// rolling sizes the 8 warps of a CTA walk 8 adjacent y-block columns through
+// the same z range, so the halo rows a warp needs are the edge rows its
+// neighbours load at the same time (L1 hits); consecutive CTA tasks walk z, so
+// the z-1/z/z+1 words of the other colour stay in registers.  Flat sizes give
+// each warp one 32-word task per CTA task.
 template <int DIM, int MODE>
-__global__ void __launch_bounds__(kMaxThreads)
+__global__ void __launch_bounds__(256, 5)
     k_ising_words(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
-    __shared__ __align__(256) uint32_t s_thr[kMaxThreads / 32][64];
+    __shared__ __align__(256) uint32_t s_thr[8][64];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
-    int64_t t = gw * P.total_tasks / nwarps;
-    const int64_t t_end = (gw + 1) * P.total_tasks / nwarps;
-    if (t >= t_end) return;
+    const int64_t G = P.total_ctasks;
+    int64_t ct = (int64_t)blockIdx.x * G / gridDim.x;
+    const int64_t ct_end = (int64_t)(blockIdx.x + 1) * G / gridDim.x;
 
     const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
     const uint32_t c2 = (uint32_t)sweep;
     const uint32_t c3 = counter_word3(ISG_TAG_ISING, (uint32_t)colour, sweep);
-    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
     const uint32_t tbase = (uint32_t)__cvta_generic_to_shared(&s_thr[wib][0]);
     constexpr int Z = 2 * DIM;
 
     int ci = 0;
-    while (P.cls[ci].task_end <= t) ++ci;
     int cur_rep = -1;
     MeasAcc macc{0, 0, 0, 0, 0};
-    uint32_t* own = nullptr;
-    const uint32_t* oth = nullptr;
     PhiloxPre pre{};
-    // rolling state (kRolling)
-    int64_t next_t = -1;
-    uint32_t zm = 0, za = 0, zp = 0;
 
-    for (; t < t_end; ++t) {
-        while (P.cls[ci].task_end <= t) ++ci;
+    while (ct < ct_end) {
+        while (P.cls[ci].ctask_end <= ct) ++ci;
         const IsingClass& C = P.cls[ci];
-        const int64_t lt = t - C.task_base;
-        const int r = (int)(lt >> C.log2_tpp);
-        const uint32_t tl = (uint32_t)(lt & (int64_t)(C.tasks_per_plane - 1));
-        const int rg = C.rep_base + r;
-        if (rg != cur_rep) {
-            if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
-            cur_rep = rg;
-            if (MODE != 2) {
-                const int slot = C.rep_base + P.r2t[rg];
-                __syncwarp();
-                if (lane < 16) s_thr[wib][lane] = P.thr[slot * 16 + lane];
-                __syncwarp();
+        const int64_t lct = ct - C.ctask_base;
+        const uint32_t L = (uint32_t)C.L, Lm = L - 1;
+        const int lrw = C.log2_rw;
+        const uint32_t rw = 1u << lrw, rwm = rw - 1;
+        const uint32_t k4 = (uint32_t)lane & rwm;
+        const int src_prev = lane - (int)k4 + (int)((k4 - 1) & rwm);
+        const int src_next = lane - (int)k4 + (int)((k4 + 1) & rwm);
+
+        if (DIM == 3 && C.kind == kRolling) {
+            // CTA task -> (replica r, column group g, z), z fastest
+            const int lg = C.log2_groups + C.log2L;
+            const int r = (int)(lct >> lg);
+            const uint32_t rem = (uint32_t)(lct & (((int64_t)1 << lg) - 1));
+            const uint32_t z0 = rem & Lm;
+            const uint32_t g = rem >> C.log2L;
+            const int64_t zlim = (int64_t)z0 + (ct_end - ct);
+            const uint32_t z1 = (uint32_t)(zlim < (int64_t)L ? zlim : (int64_t)L);
+            ct += z1 - z0;
+            const int rg = C.rep_base + r;
+            if (rg != cur_rep) {
+                if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
+                cur_rep = rg;
+                if (MODE != 2) {
+                    const int slot = C.rep_base + P.r2t[rg];
+                    __syncwarp();
+                    if (lane < 16) s_thr[wib][lane] = P.thr[slot * 16 + lane];
+                    __syncwarp();
+                    pre = philox_pre(replica_uid(C.L, r), c2, c3, P.rk0[0], P.rk1[0]);
+                }
             }
             uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
-            own = reinterpret_cast<uint32_t*>(base + (int64_t)colour * C.plane_sites);
-            oth = reinterpret_cast<const uint32_t*>(base + (int64_t)(colour ^ 1) * C.plane_sites);
-            pre = philox_pre(replica_uid(C.L, r), c2, c3, k0, k1);
-            next_t = -1;
-        }
-        const uint32_t L = (uint32_t)C.L;
-        const uint32_t Lm = L - 1;
-        const int lrw = C.log2_rw;
-        const uint32_t rwm = (1u << lrw) - 1;
-        uint32_t w, y, z, k4, wa, wyp, wym, wzp, wzm;
-        if (DIM == 3 && C.kind == kRolling) {
-            // task tl -> (y-block yb, z), z fastest
-            z = tl & Lm;
-            const uint32_t yb = tl >> C.log2L;
-            const uint32_t pz = L << lrw;  // words per z-plane
+            uint32_t* own = reinterpret_cast<uint32_t*>(base + (int64_t)colour * C.plane_sites);
+            const uint32_t* oth =
+                reinterpret_cast<const uint32_t*>(base + (int64_t)(colour ^ 1) * C.plane_sites);
+            const uint32_t yb = (g << 3) + (uint32_t)wib;
+            const uint32_t pz = L << lrw;          // words per z-plane
+            const uint32_t pwm = (pz << C.log2L) - 1;  // plane words - 1 (power of two)
             const uint32_t col = (yb << 5) + (uint32_t)lane;
-            w = z * pz + col;
-            k4 = (uint32_t)lane & rwm;
-            const uint32_t rb = (uint32_t)lane >> lrw;  // row within the block
-            const uint32_t nr = 32u >> lrw;
-            y = (yb * nr + rb);
-            if (t != next_t) {
-                zm = __ldg(oth + ((z - 1) & Lm) * pz + col);
-                za = __ldg(oth + w);
-            } else {
+            const uint32_t rb = (uint32_t)lane >> lrw, nr = 32u >> lrw;
+            const uint32_t y = yb * nr + rb;
+            const bool first = rb == 0, last = rb == nr - 1, single = nr == 1;
+            const uint32_t ha = (((first ? y - 1 : y + 1) & Lm) << lrw) | k4;
+            const uint32_t hb = (((y + 1) & Lm) << lrw) | k4;
+            const int src_up = (lane + (int)rw) & 31, src_dn = (lane - (int)rw) & 31;
+            const uint32_t* oc = oth + col;   // column base pointers
+            const uint32_t* oa = oth + ha;
+            const uint32_t* ob = oth + hb;
+            uint32_t* mc = own + col;
+            uint32_t p = (y + z0 + (uint32_t)colour) & 1u;
+            uint32_t o = z0 * pz;                        // offset of plane z
+            uint32_t zm = __ldg(oc + ((o - pz) & pwm));
+            uint32_t za = __ldg(oc + o);
+            uint32_t zp = __ldg(oc + ((o + pz) & pwm));
+            uint32_t h0 = __ldg(oa + o);
+            uint32_t h1 = single ? __ldg(ob + o) : 0u;
+            uint32_t ow = mc[o];
+            for (uint32_t z = z0; z < z1; ++z) {
+                const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm;
+                const uint32_t n_zp = __ldg(oc + o2);
+                const uint32_t n_h0 = __ldg(oa + o1);
+                const uint32_t n_h1 = single ? __ldg(ob + o1) : 0u;
+                const uint32_t n_ow = mc[o1];
+                uint32_t nd;
+                const uint32_t nw = rolling_word<MODE>(P, pre, tbase, o + col, ow, zm, za, zp, h0,
+                                                       h1, single, first, last, p, src_up, src_dn,
+                                                       src_prev, src_next, nd);
+                if (MODE != 2) mc[o] = nw;
+                if (MODE != 0) meas_add(macc, nw, nd, za);
                 zm = za;
                 za = zp;
+                zp = n_zp;
+                h0 = n_h0;
+                h1 = n_h1;
+                ow = n_ow;
+                p ^= 1u;
+                o = o1;
             }
-            zp = __ldg(oth + ((z + 1) & Lm) * pz + col);
-            next_t = (z + 1 < L) ? t + 1 : -1;
-            const uint32_t up = __shfl_sync(ISG_FULL_MASK, za, (lane + (1 << lrw)) & 31);
-            const uint32_t dn = __shfl_sync(ISG_FULL_MASK, za, (lane - (1 << lrw)) & 31);
-            if (nr >= 2) {
-                const bool first = rb == 0, last = rb == nr - 1;
-                uint32_t halo = 0;
-                if (first || last) {
-                    const uint32_t hy = first ? ((y - 1) & Lm) : ((y + 1) & Lm);
-                    halo = __ldg(oth + z * pz + (hy << lrw) + k4);
-                }
-                wyp = last ? halo : up;
-                wym = first ? halo : dn;
-            } else {
-                wyp = __ldg(oth + z * pz + (((y + 1) & Lm) << lrw) + k4);
-                wym = __ldg(oth + z * pz + (((y - 1) & Lm) << lrw) + k4);
-            }
-            wa = za;
-            wzp = zp;
-            wzm = zm;
         } else {
-            w = (tl << 5) + (uint32_t)lane;
+            // flat: warp task 8*lct + wib of this size
+            const int64_t wt = (lct << 3) + wib;
+            ++ct;
+            if (wt >= C.task_end - C.task_base) continue;
+            const int r = (int)(wt >> C.log2_tpp);
+            const uint32_t tl = (uint32_t)(wt & (int64_t)(C.tasks_per_plane - 1));
+            const int rg = C.rep_base + r;
+            if (rg != cur_rep) {
+                if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
+                cur_rep = rg;
+                if (MODE != 2) {
+                    const int slot = C.rep_base + P.r2t[rg];
+                    __syncwarp();
+                    if (lane < 16) s_thr[wib][lane] = P.thr[slot * 16 + lane];
+                    __syncwarp();
+                    pre = philox_pre(replica_uid(C.L, r), c2, c3, P.rk0[0], P.rk1[0]);
+                }
+            }
+            uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
+            uint32_t* own = reinterpret_cast<uint32_t*>(base + (int64_t)colour * C.plane_sites);
+            const uint32_t* oth =
+                reinterpret_cast<const uint32_t*>(base + (int64_t)(colour ^ 1) * C.plane_sites);
+            const uint32_t w = (tl << 5) + (uint32_t)lane;
             const uint32_t row = w >> lrw;
-            k4 = w & rwm;
+            uint32_t y, z;
             if (DIM == 3) {
                 y = row & Lm;
                 z = row >> C.log2L;
@@ -323,6 +382,7 @@ __global__ void __launch_bounds__(kMaxThreads)
                 z = 0;
             }
             const uint32_t yp = (y + 1) & Lm, ym = (y - 1) & Lm;
+            uint32_t wa, wyp, wym, wzp = 0, wzm = 0;
             if (DIM == 3) {
                 const uint32_t zb = z << C.log2L;
                 wa = __ldg(oth + (((zb + y) << lrw) + k4));
@@ -334,26 +394,24 @@ __global__ void __launch_bounds__(kMaxThreads)
                 wa = __ldg(oth + ((y << lrw) + k4));
                 wyp = __ldg(oth + ((yp << lrw) + k4));
                 wym = __ldg(oth + ((ym << lrw) + k4));
-                wzp = wzm = 0;
             }
+            const uint32_t p = (y + z + (uint32_t)colour) & 1u;
+            const uint32_t prev = __shfl_sync(ISG_FULL_MASK, wa, src_prev);
+            const uint32_t next = __shfl_sync(ISG_FULL_MASK, wa, src_next);
+            const uint32_t wx = p ? __funnelshift_r(wa, next, 8) : __funnelshift_l(prev, wa, 8);
+            uint32_t nd = wx + wa + wyp + wym;
+            if (DIM == 3) nd += wzp + wzm;
+            const uint32_t ow = own[w];
+            uint32_t nw = ow;
+            if (MODE != 2) {
+                const U4 u = philox_w(pre, P, w);
+                nw = metropolis_word(ow, nd, tbase, u);
+                own[w] = nw;
+            }
+            if (MODE != 0) meas_add(macc, nw, nd, wa);
         }
-        const uint32_t p = (y + z + (uint32_t)colour) & 1u;
-        const int lane0 = lane - (int)k4;
-        const uint32_t prev = __shfl_sync(ISG_FULL_MASK, wa, lane0 + (int)((k4 - 1) & rwm));
-        const uint32_t next = __shfl_sync(ISG_FULL_MASK, wa, lane0 + (int)((k4 + 1) & rwm));
-        const uint32_t wx = p ? __funnelshift_r(wa, next, 8) : __funnelshift_l(prev, wa, 8);
-        uint32_t nd = wx + wa + wyp + wym;
-        if (DIM == 3) nd += wzp + wzm;
-        const uint32_t ow = own[w];
-        uint32_t nw = ow;
-        if (MODE != 2) {
-            const U4 u = philox_w(pre, w, k0, k1);
-            nw = metropolis_word(ow, nd, tbase, u);
-            own[w] = nw;
-        }
-        if (MODE != 0) meas_add(macc, nw, nd, wa);
     }
-    if (MODE != 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
+    if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
 }
 
 template <int DIM, int MODE>
@@ -595,6 +653,7 @@ struct isg_ising {
     int threads = 256;
     int blocks_per_sm = 0;
     int word_grid = 0, site_grid = 0;
+    int word_grids[3] = {1, 1, 1};
     int sms = 1;
     // sampling-phase mirror of the device counters
     uint64_t ksample = 0;
@@ -629,18 +688,23 @@ static void (*site_kernel(int dim, int mode))(IsingParams, int, int) {
     return k_ising_sites<2, 2>;
 }
 
+// Word kernels run 256-thread blocks (one CTA task = 8 warp tasks); the
+// grid is SMs x blocks per SM (occupancy maximum unless set), at most one
+// block per CTA task.  `threads` applies to the site kernel.
 static int configure_launch(isg_ising* H) {
     const int thr = H->threads;
-    int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &occ, (const void*)word_kernel(H->dim, 1), thr, 0);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-    if (occ < 1) occ = 1;
-    int bps = H->blocks_per_sm > 0 ? std::min(H->blocks_per_sm, occ) : occ;
-    int64_t max_blocks = (int64_t)H->sms * bps;
-    const int64_t warps_per_block = thr / 32;
-    int64_t need = (H->P.total_tasks + warps_per_block - 1) / warps_per_block;
-    H->word_grid = (int)std::max<int64_t>(1, std::min(max_blocks, need));
+    const int64_t need = H->P.total_ctasks;
+    for (int mode = 0; mode < 3; ++mode) {
+        int occ = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &occ, (const void*)word_kernel(H->dim, mode), 256, 0);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        if (occ < 1) occ = 1;
+        const int bps = H->blocks_per_sm > 0 ? std::min(H->blocks_per_sm, occ) : occ;
+        const int64_t max_blocks = (int64_t)H->sms * bps;
+        H->word_grids[mode] = (int)std::max<int64_t>(1, std::min(max_blocks, need));
+    }
+    H->word_grid = H->word_grids[0];
     int64_t sneed = (H->P.total_sites + thr - 1) / thr;
     H->site_grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)H->sms * 8, sneed));
     return ISG_OK;
@@ -648,7 +712,7 @@ static int configure_launch(isg_ising* H) {
 
 static void launch_half(isg_ising* H, int colour, int sweep_off, int mode) {
     if (H->P.total_tasks > 0)
-        word_kernel(H->dim, mode)<<<H->word_grid, H->threads, 0, H->stream>>>(H->P, colour,
+        word_kernel(H->dim, mode)<<<H->word_grids[mode], 256, 0, H->stream>>>(H->P, colour,
                                                                              sweep_off);
     if (H->P.total_sites > 0)
         site_kernel(H->dim, mode)<<<H->site_grid, H->threads, 0, H->stream>>>(H->P, colour,
@@ -774,7 +838,7 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
     H->sizes.assign(sizes, sizes + n_sizes);
 
     IsingParams& P = H->P;
-    int64_t off = 0, task = 0, site = 0;
+    int64_t off = 0, task = 0, site = 0, ctask = 0;
     for (int s = 0; s < n_sizes; ++s) {
         IsingClass& C = P.cls[s];
         const int L = sizes[s];
@@ -801,6 +865,18 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         C.task_base = task;
         if (C.kind != kSite) task += (int64_t)C.tasks_per_plane * replicas;
         C.task_end = task;
+        C.log2_groups = 0;
+        C.ctask_base = ctask;
+        if (C.kind == kRolling) {
+            // columns of 32/(L/8) rows: L*L/256 per z-plane, in groups of 8
+            const int cols = (L / (32 / rw));
+            int groups = cols / 8;
+            while ((1 << C.log2_groups) < groups) ++C.log2_groups;
+            ctask += (int64_t)replicas * groups * L;
+        } else if (C.kind == kFlat) {
+            ctask += ((int64_t)C.tasks_per_plane * replicas + 7) / 8;
+        }
+        C.ctask_end = ctask;
         C.site_base = site;
         if (C.kind == kSite) site += (int64_t)C.plane_sites * replicas;
         C.site_end = site;
@@ -809,13 +885,19 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
     for (int s = n_sizes; s < kMaxClasses; ++s) {
         P.cls[s] = P.cls[n_sizes - 1];
         P.cls[s].task_base = P.cls[s].task_end = INT64_MAX;
+        P.cls[s].ctask_base = P.cls[s].ctask_end = INT64_MAX;
         P.cls[s].site_base = P.cls[s].site_end = INT64_MAX;
     }
     P.n_classes = n_sizes;
     P.dim = dim;
     P.total_tasks = task;
+    P.total_ctasks = ctask;
     P.total_sites = site;
     P.seed = seed;
+    for (int r = 0; r < 10; ++r) {
+        P.rk0[r] = (uint32_t)seed + (uint32_t)r * kPhiloxW0;
+        P.rk1[r] = (uint32_t)(seed >> 32) + (uint32_t)r * kPhiloxW1;
+    }
     H->spin_bytes = off;
 
     const int RT = H->replicas_total;

@@ -137,6 +137,7 @@ def test_pt_statistics_match_reference_gpu_csv(gpu, model, nc, tmin, tmax, L):
 
 def test_continuous_lattice_mirror(gpu, oracle):
     lat = gpu.ContinuousGpuLattice(8, 3, 42)
-    lat.sweep(1 / 1.45, 1.0, 0.5, 5)
+    for _ in range(50):
+        lat.sweep(1 / 1.45, 1.0, 0.5, 5)
     e, mx, my, mz = lat.measure_gpu(1.0)
-    assert np.isfinite([e, mx, my, mz]).all() and e < 0
+    assert np.isfinite([e, mx, my, mz]).all() and e / 512 < -0.5

@@ -159,6 +159,23 @@ __device__ __forceinline__ U4 philox_w(const PhiloxPre& p, const IsingParams& P,
     return U4{c0, c1, c2, c3};
 }
 
+// Loads issued where they are written (volatile asm keeps the compiler from
+// sinking a prefetch next to its use).
+__device__ __forceinline__ uint32_t ldg_nc(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint32_t ldg_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.global.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint32_t pin(uint32_t x) {
+    asm volatile("mov.b32 %0, %0;" : "+r"(x));
+    return x;
+}
+
 __device__ __forceinline__ uint32_t lds_u32(uint32_t saddr) {
     uint32_t v;
     asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(saddr));
@@ -248,7 +265,7 @@ __device__ __forceinline__ uint32_t rolling_word(const IsingParams& P, const Phi
 // the z-1/z/z+1 words of the other colour stay in registers.  Flat sizes give
 // each warp one 32-word task per CTA task.
 template <int DIM, int MODE>
-__global__ void __launch_bounds__(256, 5)
+__global__ void __launch_bounds__(256, MODE == 1 ? 4 : 5)
     k_ising_words(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
     __shared__ __align__(256) uint32_t s_thr[8][64];
     const int lane = threadIdx.x & 31;
@@ -260,7 +277,7 @@ __global__ void __launch_bounds__(256, 5)
     const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
     const uint32_t c2 = (uint32_t)sweep;
     const uint32_t c3 = counter_word3(ISG_TAG_ISING, (uint32_t)colour, sweep);
-    const uint32_t tbase = (uint32_t)__cvta_generic_to_shared(&s_thr[wib][0]);
+    const uint32_t tbase = pin((uint32_t)__cvta_generic_to_shared(&s_thr[wib][0]));
     constexpr int Z = 2 * DIM;
 
     int ci = 0;
@@ -321,18 +338,20 @@ __global__ void __launch_bounds__(256, 5)
             uint32_t* mc = own + col;
             uint32_t p = (y + z0 + (uint32_t)colour) & 1u;
             uint32_t o = z0 * pz;                        // offset of plane z
-            uint32_t zm = __ldg(oc + ((o - pz) & pwm));
-            uint32_t za = __ldg(oc + o);
-            uint32_t zp = __ldg(oc + ((o + pz) & pwm));
-            uint32_t h0 = __ldg(oa + o);
-            uint32_t h1 = single ? __ldg(ob + o) : 0u;
-            uint32_t ow = mc[o];
-            for (uint32_t z = z0; z < z1; ++z) {
+            uint32_t zm = ldg_nc(oc + ((o - pz) & pwm));
+            uint32_t za = ldg_nc(oc + o);
+            uint32_t zp = ldg_nc(oc + ((o + pz) & pwm));
+            uint32_t h0 = ldg_nc(oa + o);
+            uint32_t h1 = single ? ldg_nc(ob + o) : 0u;
+            uint32_t ow = ldg_u32(mc + o);
+            uint32_t z = z0;
+#pragma unroll 1
+            for (; z < z1; ++z) {
                 const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm;
-                const uint32_t n_zp = __ldg(oc + o2);
-                const uint32_t n_h0 = __ldg(oa + o1);
-                const uint32_t n_h1 = single ? __ldg(ob + o1) : 0u;
-                const uint32_t n_ow = mc[o1];
+                const uint32_t n_zp = ldg_nc(oc + o2);
+                const uint32_t n_h0 = ldg_nc(oa + o1);
+                const uint32_t n_h1 = single ? ldg_nc(ob + o1) : 0u;
+                const uint32_t n_ow = ldg_u32(mc + o1);
                 uint32_t nd;
                 const uint32_t nw = rolling_word<MODE>(P, pre, tbase, o + col, ow, zm, za, zp, h0,
                                                        h1, single, first, last, p, src_up, src_dn,

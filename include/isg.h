@@ -235,6 +235,25 @@ int isg_cont_time_kernels(isg_cont* h, int n, float* out_ms);
 /* Site updates of one full sweep of one kind (all sizes and replicas). */
 int isg_cont_sites_per_sweep(isg_cont* h, int64_t* sites);
 
+/* Observables of continuous-spin lattices that the caller owns, computed
+ * without any allocation by the library.  No counterpart in the reference: it
+ * exists for callers that cannot call cudaMalloc (their device memory comes
+ * from their own pool or framework, or allocation is not allowed where they
+ * run).  d_spins: `replicas` lattices of L^3 sites in the reference's natural
+ * interleaved layout (n_comp floats per site, site z*L*L + y*L + x), device
+ * memory; d_out: device memory for replicas*10 doubles, per replica E, Mx, My,
+ * Mz, then sum_i S_i.S_{i+a} and sum_i (S_i x S_{i+a})_z for a = x, y, z (the
+ * layout of isg_cont_measure).  Work is queued on `stream` (NULL = the legacy
+ * default stream); the call does not synchronise.  Block partials live in a
+ * fixed device array of 16384 blocks of 1024 sites (replicas * ceil(L^3/1024)
+ * must not exceed 16384, i.e. at most 16,777,216 sites per call; larger
+ * requests return ISG_ERR_ARG).  The first call on each device looks up that
+ * array's device address, so make it before capturing a stream into a graph.
+ * All calls share the array: calls that overlap on the GPU (different
+ * streams, no ordering) race and must be serialised by the caller. */
+int isg_cont_observables_static(const float* d_spins, int L, int n_comp, int replicas, double J,
+                                double* d_out, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Statistics used by the drop-in driver                                     */
 /* ------------------------------------------------------------------------ */

@@ -86,7 +86,9 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
 int isg_ising_destroy(isg_ising* h);
 
 /* Work on the caller's CUDA stream (a cudaStream_t passed as void*); NULL
- * restores the handle's own stream. */
+ * restores the handle's own stream.  The caller's stream must stay valid
+ * until it is replaced or the handle is destroyed (destroy then waits for the
+ * whole device rather than for that stream). */
 int isg_ising_set_stream(isg_ising* h, void* cuda_stream);
 
 /* Temperature grid per size (temps[s*replicas + t], slot t), coupling J and
@@ -123,6 +125,11 @@ int isg_ising_set_r2t(isg_ising* h, const int32_t* r2t);
  * LatticeGpu::get_spins (src/cuda/lattice_gpu.rs:110-112). */
 int isg_ising_get_spins(isg_ising* h, int size_index, int replica, int8_t* out);
 int isg_ising_set_spins(isg_ising* h, int size_index, int replica, const int8_t* in);
+
+/* The same, device to device and asynchronous on the handle's stream: d_nat is
+ * a device buffer of L^dim +-1 bytes in natural layout. */
+int isg_ising_load_natural(isg_ising* h, int size_index, int replica, const int8_t* d_nat);
+int isg_ising_store_natural(isg_ising* h, int size_index, int replica, int8_t* d_nat);
 
 /* Parallel-tempering sampling: n_sweeps sweeps continuing the sampling phase;
  * after sampling sweep k (0-based, counted since the last reset) the
@@ -253,6 +260,49 @@ int isg_cont_sites_per_sweep(isg_cont* h, int64_t* sites);
  * streams, no ordering) race and must be serialised by the caller. */
 int isg_cont_observables_static(const float* d_spins, int L, int n_comp, int replicas, double J,
                                 double* d_out, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Learned autoregressive proposal (no reference counterpart)                 */
+/* ------------------------------------------------------------------------ */
+/* A masked-convolution autoregressive network over an H x W raster of +-1
+ * spins (a cubic L^3 lattice is the L^2 x L raster of its z-y rows): layers
+ * 3x3 mask A (1 -> 32), then mask B (32 -> 32) ..., last mask B (32 -> 1
+ * logit), ReLU, BF16 weights, FP32 accumulation.  q(s) = prod sigma(s_i l_i);
+ * proposals use q_sym(s) = (q(s) + q(-s)) / 2 and an exact independence
+ * Metropolis-Hastings test.  Configuration buffers are natural-layout +-1
+ * bytes.  All device work runs on the handle's stream (isg_learned_stream). */
+typedef struct isg_learned isg_learned;
+int isg_learned_create(isg_learned** out, int H, int W, int layers, uint64_t seed);
+int isg_learned_destroy(isg_learned* h);
+int isg_learned_num_params(isg_learned* h, int* n);
+int isg_learned_get_weights(isg_learned* h, float* w);
+int isg_learned_set_weights(isg_learned* h, const float* w);
+/* Mean negative log-likelihood of B host configurations and its gradient. */
+int isg_learned_gradient(isg_learned* h, const int8_t* cfg, int B, float* grad, float* nll);
+/* `steps` Adam steps on batches of B taken cyclically from n device configurations. */
+int isg_learned_train(isg_learned* h, const int8_t* d_cfg_all, int n, int B, int steps, float lr,
+                      float* last_mean_logq);
+/* K samples of q with log q, and log q of their negations (same kernel). */
+int isg_learned_sample(isg_learned* h, int K, uint64_t step, int8_t* d_out, float* d_lq,
+                       float* d_lq_flip);
+/* log q of K device configurations (flip = 1: of their negations). */
+int isg_learned_score(isg_learned* h, const int8_t* d_cfg, int K, int flip, float* d_lq);
+/* Exact bond sums and magnetisations of K device configurations (L^dim, PBC). */
+int isg_learned_energies(isg_learned* h, const int8_t* d_cfg, int K, int L, int dim,
+                         int64_t* d_bond, int64_t* d_mag);
+/* One independence MH pass over K proposals; see isg_learned.cu. */
+int isg_learned_imh(isg_learned* h, const int64_t* d_bond, const int64_t* d_mag,
+                    const float* d_lq, const float* d_lq_flip, int K, double beta, double J,
+                    int64_t* d_state, double* d_ax, int64_t* d_mrec, int64_t* d_brec,
+                    int64_t* d_accepted, double* d_work, uint64_t step);
+/* A = -beta E - log q_sym of one configuration (device scalars). */
+int isg_learned_state_a(isg_learned* h, const float* d_lq, const float* d_lq_flip,
+                        const int64_t* d_bond, double beta, double J, double* d_ax);
+/* Copy proposal d_state[2] (if >= 0) into the current configuration. */
+int isg_learned_adopt(isg_learned* h, const int8_t* d_props, const int64_t* d_state,
+                      int8_t* d_current);
+int isg_learned_sync(isg_learned* h);
+void* isg_learned_stream(isg_learned* h);
 
 /* ------------------------------------------------------------------------ */
 /* Statistics used by the drop-in driver                                     */

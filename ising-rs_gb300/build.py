@@ -30,7 +30,7 @@ NVCC_FLAGS = [
 ]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 
-CU_SOURCES = ["isg_ising.cu", "isg_cont.cu", "isg_noalloc.cu"]
+CU_SOURCES = ["isg_ising.cu", "isg_cont.cu", "isg_noalloc.cu", "isg_learned.cu"]
 CPP_SOURCES = ["isg_stats.cpp"]
 
 

@@ -774,7 +774,12 @@ int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas,
 int isg_cont_destroy(isg_cont* H) {
     if (!H) return ISG_OK;
     cudaSetDevice(H->device);
-    if (H->stream) cudaStreamSynchronize(H->stream);
+    // A caller's stream may already be gone: wait for the device instead.
+    if (H->stream == H->own_stream) {
+        if (H->stream) cudaStreamSynchronize(H->stream);
+    } else {
+        cudaDeviceSynchronize();
+    }
     cont_destroy_graph(H);
     cudaFree(H->d_spins);
     cudaFree(H->d_betaf);

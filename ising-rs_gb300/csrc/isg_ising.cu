@@ -622,6 +622,28 @@ __global__ void k_ising_post(const __grid_constant__ PostParams Q, int do_record
     }
 }
 
+// Natural-layout +-1 bytes <-> colour-split down-bit planes of one replica.
+__global__ void k_ising_nat_to_planes(uint8_t* __restrict__ planes, const int8_t* __restrict__ nat,
+                                      int L, int dim, uint32_t half) {
+    const uint32_t n = 2 * half;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t x = i % (uint32_t)L, y = (i / (uint32_t)L) % (uint32_t)L;
+        const uint32_t z = dim == 3 ? i / ((uint32_t)L * (uint32_t)L) : 0;
+        const uint32_t c = (x + y + z) & 1u;
+        planes[c * half + (i >> 1)] = nat[i] < 0 ? 1 : 0;
+    }
+}
+__global__ void k_ising_planes_to_nat(const uint8_t* __restrict__ planes, int8_t* __restrict__ nat,
+                                      int L, int dim, uint32_t half) {
+    const uint32_t n = 2 * half;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t x = i % (uint32_t)L, y = (i / (uint32_t)L) % (uint32_t)L;
+        const uint32_t z = dim == 3 ? i / ((uint32_t)L * (uint32_t)L) : 0;
+        const uint32_t c = (x + y + z) & 1u;
+        nat[i] = planes[c * half + (i >> 1)] ? (int8_t)-1 : (int8_t)1;
+    }
+}
+
 // ---------------------------------------------------------------- host object
 
 static int num_sms(int dev) {
@@ -993,7 +1015,12 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
 int isg_ising_destroy(isg_ising* H) {
     if (!H) return ISG_OK;
     cudaSetDevice(H->device);
-    if (H->stream) cudaStreamSynchronize(H->stream);
+    // A caller's stream may already be gone: wait for the device instead.
+    if (H->stream == H->own_stream) {
+        if (H->stream) cudaStreamSynchronize(H->stream);
+    } else {
+        cudaDeviceSynchronize();
+    }
     destroy_graph(H);
     cudaFree(H->d_spins);
     cudaFree(H->d_thr);
@@ -1202,6 +1229,28 @@ int isg_ising_set_spins(isg_ising* H, int s, int r, const int8_t* in) {
                            H->stream));
     ISG_CK(cudaStreamSynchronize(H->stream));
     return ISG_OK;
+}
+
+int isg_ising_load_natural(isg_ising* H, int s, int r, const int8_t* d_nat) {
+    if (!H || !d_nat) return fail(ISG_ERR_ARG, "isg_ising_load_natural: NULL argument");
+    cudaSetDevice(H->device);
+    int64_t n, base;
+    int rc = spin_geometry(H, s, r, &n, &base);
+    if (rc) return rc;
+    k_ising_nat_to_planes<<<(int)std::min<int64_t>(1024, (n + 255) / 256), 256, 0, H->stream>>>(
+        H->d_spins + base, d_nat, H->sizes[s], H->dim, (uint32_t)(n / 2));
+    return check_launch("isg_ising_load_natural");
+}
+
+int isg_ising_store_natural(isg_ising* H, int s, int r, int8_t* d_nat) {
+    if (!H || !d_nat) return fail(ISG_ERR_ARG, "isg_ising_store_natural: NULL argument");
+    cudaSetDevice(H->device);
+    int64_t n, base;
+    int rc = spin_geometry(H, s, r, &n, &base);
+    if (rc) return rc;
+    k_ising_planes_to_nat<<<(int)std::min<int64_t>(1024, (n + 255) / 256), 256, 0, H->stream>>>(
+        H->d_spins + base, d_nat, H->sizes[s], H->dim, (uint32_t)(n / 2));
+    return check_launch("isg_ising_store_natural");
 }
 
 int isg_ising_reset_sampling(isg_ising* H) {

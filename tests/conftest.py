@@ -18,10 +18,11 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libisinggb")
 
 
-def _load(name: str, path: Path):
+def _load(name: str, path: Path, package: bool = False):
     if name in sys.modules:
         return sys.modules[name]
-    spec = importlib.util.spec_from_file_location(name, path)
+    spec = importlib.util.spec_from_file_location(
+        name, path, submodule_search_locations=[str(path.parent)] if package else None)
     mod = importlib.util.module_from_spec(spec)
     sys.modules[name] = mod
     spec.loader.exec_module(mod)
@@ -29,7 +30,7 @@ def _load(name: str, path: Path):
 
 
 def load_pkg():
-    return _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
+    return _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py", package=True)
 
 
 def load_oracle():

@@ -356,6 +356,90 @@ def run_gpu(args):
     return 0
 
 
+def jackknife_mean_err(x, nb=20):
+    x = np.asarray(x, float)
+    n = len(x) // nb * nb
+    if n < nb:
+        return float("nan")
+    x = x[:n]
+    full = x.mean()
+    jk = np.array([(x.sum() - x[b * (n // nb):(b + 1) * (n // nb)].sum()) / (n - n // nb)
+                   for b in range(nb)])
+    return float(np.sqrt((nb - 1) / nb * ((jk - full) ** 2).sum()))
+
+
+def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
+    """Config 5: ESS/s of |M| of one chain at T, plain checkerboard PT vs the
+    learned independence proposal (+ interleaved sweeps)."""
+    import torch
+    import importlib
+    lrn = importlib.import_module(pkg.__name__ + ".learned")
+    n = L ** dim
+    H, W = (L, L) if dim == 2 else (L * L, L)
+    # plain PT: 17 replicas on a linear grid with T at the middle slot
+    R = 17
+    width = 0.20 if dim == 2 else 0.10
+    temps = [T - width + 2 * width * i / (R - 1) for i in range(R)]
+    b = pkg.IsingBatch([L], R, seed=SEED, dim=dim)
+    b.set_temperatures(temps)
+    b.step(5000)
+    b.reset_sampling()
+    b.pt_run(2000, 10, 1)
+    b.sync()
+    t0 = time.perf_counter()
+    rt, rb, rm = b.pt_run(pt_sweeps, 10, 1)
+    pt_s = time.perf_counter() - t0
+    mid = R // 2
+    series = np.array([abs(rm[i][rt[i] == mid][0]) / n for i in range(rt.shape[0])], float)
+    tau_pt = tau_int(series)
+    ess_pt = len(series) / (2 * tau_pt) / pt_s
+    # training data from the plain sampler at T, with Z2 partners
+    t1 = time.perf_counter()
+    data = lrn.collect_training_set(L, dim, T, chains=64, rounds=64, gap=20, warmup=2000)
+    q = lrn.LearnedProposal(H, W, layers=6, seed=SEED)
+    steps = 0
+    tt = time.perf_counter()
+    while time.perf_counter() - tt < train_seconds:
+        q.train(data, batch=128, steps=20, lr=1e-3)
+        steps += 20
+    train_s = time.perf_counter() - t1
+    nll = -q.train(data, batch=128, steps=1, lr=1e-4) / n
+    ch = lrn.LearnedChain(q, L, dim, T, K=4096, sweeps=1, fallback_sweeps=20, min_accept=0.002)
+    ch.start(1000)
+    ch.batch()
+    t2 = time.perf_counter()
+    for _ in range(chain_batches):
+        ch.batch()
+    torch.cuda.synchronize()
+    ch_s = time.perf_counter() - t2
+    m = ch.m_series()[4096:]
+    tau_l = tau_int(m)
+    ess_l = len(m) / (2 * tau_l) / ch_s
+    out = {"case": f"{dim}D L={L} T={T}", "plain_pt": {
+        "replicas": R, "T_grid": [temps[0], temps[-1]], "sweeps": pt_sweeps,
+        "seconds": pt_s, "sweeps_per_s": pt_sweeps / pt_s, "tau_int_sweeps": tau_pt,
+        "ess_per_s": ess_pt, "M": float(series.mean()), "M_err": jackknife_mean_err(series)},
+        "learned": {"layers": 6, "channels": 32, "train_steps": steps, "train_s": train_s,
+                    "nll_per_site": nll, "proposals": len(m), "seconds": ch_s,
+                    "acceptance": float(np.mean(ch.batch_accept[1:])),
+                    "tau_int_proposals": tau_l, "ess_per_s": ess_l, "M": float(m.mean()),
+                    "M_err": jackknife_mean_err(m)},
+        "ratio_learned_over_plain": ess_l / ess_pt}
+    ch.close()
+    return out
+
+
+def run_learned(args):
+    import torch
+    torch.cuda.set_device(0)
+    pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
+    cases = [(16, 2, 2.269), (32, 2, 2.269), (8, 3, 4.51)]
+    for L, dim, T in cases:
+        out = learned_case(pkg, L, dim, T, args.train_seconds, args.chain_batches, args.pt_sweeps)
+        print(json.dumps({"metric": "ESS/s of |M| at T (learned vs plain PT)", **out}), flush=True)
+    return 0
+
+
 def ncu_case():
     pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
     b = pkg.IsingBatch([128], 96, seed=SEED)
@@ -375,12 +459,19 @@ def main():
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--cpu-sweeps", type=float, default=1.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0)
+    ap.add_argument("--learned", action="store_true",
+                    help="config 5: learned proposal vs plain PT ESS/s (separate JSON lines)")
+    ap.add_argument("--train-seconds", type=float, default=60.0)
+    ap.add_argument("--chain-batches", type=int, default=40)
+    ap.add_argument("--pt-sweeps", type=int, default=200000)
     ap.add_argument("--ncu-case", action="store_true",
                     help="no timing: a few half-sweeps of L=128 x 96 replicas (201 MB, larger "
                          "than L2) for an ncu capture of the half-sweep kernel")
     args = ap.parse_args()
     if args.ncu_case:
         return ncu_case()
+    if args.learned:
+        return run_learned(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

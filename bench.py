@@ -429,6 +429,80 @@ def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
     return out
 
 
+CONT_WORKLOADS = {
+    # config 3: O(3), L=32,64,96 x 24 replicas on [1.40,1.48], 1 Metropolis (cone) + 4 OR
+    "heisenberg": dict(nc=3, sizes=[32, 64, 96], R=24, tmin=1.40, tmax=1.48, n_or=4, delta=0.5,
+                       bytes_per_update=36),
+    # config 4: O(2), L=32,64,128 x 16 replicas on [2.18,2.22], uniform-angle Metropolis + 2 OR
+    "xy": dict(nc=2, sizes=[32, 64, 128], R=16, tmin=2.18, tmax=2.22, n_or=2, delta=math.pi,
+               bytes_per_update=24),
+}
+
+
+def run_continuous(args):
+    """Configs 3/4: one step = 10 sweeps (each n_or overrelaxation sweeps + one
+    Metropolis sweep), 2 measurements (E, M, helicity sums), 1 exchange."""
+    import torch
+    w = CONT_WORKLOADS[args.workload]
+    torch.cuda.set_device(0)
+    pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
+    stream = torch.cuda.Stream()
+    R = w["R"]
+    T = [w["tmin"] + (w["tmax"] - w["tmin"]) * i / (R - 1) for i in range(R)]
+    b = pkg.ContinuousBatch(w["sizes"], R, w["nc"], seed=SEED)
+    b.set_stream(stream)
+    b.set_temperatures(T)
+    b.sweep(50, w["delta"], w["n_or"])
+    b.reset_sampling()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        b.pt_run(10, 10, 5, w["delta"], w["n_or"], 100)
+    b.reset_sampling()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    with clocks:
+        with torch.cuda.stream(stream):
+            for i in range(args.steps):
+                flush.fill_(i & 0xFF)
+                starts[i].record(stream)
+                _ck = pkg.lib().isg_cont_pt_run(b._h, 10, 10, 5, float(w["delta"]), w["n_or"], 100,
+                                                None, None, None, None, 0, None)
+                pkg._check(_ck)
+                ends[i].record(stream)
+        torch.cuda.synchronize()
+    dev_ms = sum(s_.elapsed_time(e_) for s_, e_ in zip(starts, ends))
+    sites = b.sites_per_sweep()                     # site updates of one full sweep
+    updates = sites * (1 + w["n_or"]) * 10 * args.steps
+    value = updates / (dev_ms * 1e6)
+    kt = b.time_kernels(20)                         # OR half, Metropolis half, measure (ms)
+    half = sites // 2
+    peak, peak_kind = measured_peaks()
+    roof = {}
+    for name, ms in (("overrelax", kt[0]), ("metropolis", kt[1])):
+        ach = half * w["bytes_per_update"] / (ms * 1e-3) / 1e9
+        roof[name] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                      "frac": ach / peak, "launch_ms": float(ms),
+                      "bytes_per_launch": half * w["bytes_per_update"]}
+    meas_bytes = sites * w["nc"] * 4
+    roof["measure"] = {"achieved": meas_bytes / (kt[2] * 1e-3) / 1e9, "launch_ms": float(kt[2]),
+                       "bytes_per_launch": meas_bytes, "unit": "GB/s"}
+    acc = b.metropolis_accepted().sum() / (sites * 10 * args.steps)
+    line = {"metric": f"site updates/ns ({args.workload} PT, Metropolis + {w['n_or']} OR per sweep)",
+            "value": value, "unit": "updates/ns", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic (seeded Philox start)",
+            "config": {"workload": f"{args.workload}: L={w['sizes']} x {R} replicas, T in "
+                                   f"[{w['tmin']},{w['tmax']}], delta {w['delta']:.4g}",
+                       "l2": "flushed (256 MiB write) before every timed step"},
+            "metropolis_acceptance": float(acc), "roofline": roof,
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_learned(args):
     import torch
     torch.cuda.set_device(0)
@@ -459,6 +533,7 @@ def main():
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--cpu-sweeps", type=float, default=1.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0)
+    ap.add_argument("--workload", default="ising", choices=["ising", "heisenberg", "xy"])
     ap.add_argument("--learned", action="store_true",
                     help="config 5: learned proposal vs plain PT ESS/s (separate JSON lines)")
     ap.add_argument("--train-seconds", type=float, default=60.0)
@@ -472,6 +547,8 @@ def main():
         return ncu_case()
     if args.learned:
         return run_learned(args)
+    if args.workload != "ising":
+        return run_continuous(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

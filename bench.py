@@ -476,7 +476,7 @@ def run_continuous(args):
     sites = b.sites_per_sweep()                     # site updates of one full sweep
     updates = sites * (1 + w["n_or"]) * 10 * args.steps
     value = updates / (dev_ms * 1e6)
-    kt = b.time_kernels(20)                         # OR half, Metropolis half, measure (ms)
+    kt = [float(x) for x in b.time_kernels(20)]     # OR half, Metropolis half, measure (ms)
     half = sites // 2
     peak, peak_kind = measured_peaks()
     roof = {}

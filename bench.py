@@ -452,6 +452,9 @@ def run_continuous(args):
     b = pkg.ContinuousBatch(w["sizes"], R, w["nc"], seed=SEED)
     b.set_stream(stream)
     b.set_temperatures(T)
+    if args.workload == "heisenberg":
+        # config 3: cone width tuned for about 50% acceptance during warm-up
+        w = dict(w, delta=pkg.tune_delta(b, w["delta"], w["n_or"], 0.5))
     b.sweep(50, w["delta"], w["n_or"])
     b.reset_sampling()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")

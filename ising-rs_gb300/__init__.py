@@ -468,6 +468,22 @@ class ContinuousBatch:
         return v.value
 
 
+def tune_delta(batch: "ContinuousBatch", delta: float = 0.5, n_overrelax: int = 4,
+               target: float = 0.5, rounds: int = 12, sweeps: int = 20) -> float:
+    """Adjust the Metropolis cone half-angle so that about `target` of the
+    proposals are accepted (averaged over all replicas): delta is scaled by
+    acc/target (clamped to [1/2, 2] per round) after each burst of sweeps.
+    Returns the tuned delta; the sweeps advance the chains (use during warm-up)."""
+    d = float(delta)
+    sites = batch.sites_per_sweep()
+    for _ in range(rounds):
+        a0 = batch.metropolis_accepted().sum()
+        batch.sweep(sweeps, d, n_overrelax)
+        acc = (batch.metropolis_accepted().sum() - a0) / (sites * sweeps)
+        d = min(math.pi, d * min(2.0, max(0.5, acc / target)))
+    return d
+
+
 class ContinuousGpuLattice:
     """Mirror of ContinuousGpuLattice (src/cuda/gpu_lattice_continuous.rs:9-245).
 

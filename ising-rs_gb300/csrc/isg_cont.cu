@@ -59,8 +59,10 @@ struct ContClass {
     int L;
     int R;
     uint32_t plane_sites;
-    FastDiv div_half;  // L/2
+    FastDiv div_half;   // L/2
     FastDiv div_L;
+    FastDiv div_plane;  // plane_sites (used when R * plane_sites < 2^31)
+    int small;
     int rep_base;
     int64_t off;        // float offset of replica 0
     int64_t site_base;  // flattened colour-plane sites
@@ -103,8 +105,14 @@ __device__ __forceinline__ SiteRef locate(const ContParams& P, int64_t g, int co
     const ContClass& C = P.cls[ci];
     const int64_t lg = g - C.site_base;
     s.ci = ci;
-    s.r = (int)(lg / C.plane_sites);
-    s.i = (uint32_t)(lg - (int64_t)s.r * C.plane_sites);
+    if (C.small) {
+        const uint32_t l32 = (uint32_t)lg;
+        s.r = (int)fdiv(l32, C.div_plane);
+        s.i = l32 - (uint32_t)s.r * C.plane_sites;
+    } else {
+        s.r = (int)(lg / C.plane_sites);
+        s.i = (uint32_t)(lg - (int64_t)s.r * C.plane_sites);
+    }
     s.rg = C.rep_base + s.r;
     const uint32_t row = fdiv(s.i, C.div_half);
     const uint32_t k = s.i - row * (uint32_t)(C.L >> 1);
@@ -133,34 +141,61 @@ __device__ __forceinline__ void neighbours(uint32_t L, uint32_t x, uint32_t y, u
 // (continuous_spin_kernel.cu:88-142; overrelax.rs:16-49 without the
 // per-update renormalisation).
 template <int NC>
+__device__ __forceinline__ void or_load(const ContParams& P, int64_t g, int colour, SiteRef& s,
+                                        float h[NC], float v[NC]) {
+    s = locate(P, g, colour);
+    const ContClass& C = P.cls[s.ci];
+    uint32_t nb[6];
+    neighbours((uint32_t)C.L, s.x, s.y, s.z, nb);
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        const float* o = P.spins + plane_off<NC>(C, s.r, colour ^ 1, k);
+        h[k] = ((__ldg(o + nb[0]) + __ldg(o + nb[1])) + (__ldg(o + nb[2]) + __ldg(o + nb[3]))) +
+               (__ldg(o + nb[4]) + __ldg(o + nb[5]));
+        v[k] = P.spins[plane_off<NC>(C, s.r, colour, k) + s.i];
+    }
+}
+
+template <int NC>
+__device__ __forceinline__ void or_store(const ContParams& P, int colour, const SiteRef& s,
+                                         const float h[NC], const float v[NC]) {
+    const ContClass& C = P.cls[s.ci];
+    float h2 = 0.f, sh = 0.f;
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        h2 = fmaf(h[k], h[k], h2);
+        sh = fmaf(v[k], h[k], sh);
+    }
+    if (h2 < 1e-20f) return;
+    const float scale = 2.0f * sh / h2;
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+        P.spins[plane_off<NC>(C, s.r, colour, k) + s.i] = fmaf(scale, h[k], -v[k]);
+}
+
+// Overrelaxation: S' = 2 (S.h)/|h|^2 h - S about the local field
+// (continuous_spin_kernel.cu:88-142; overrelax.rs:16-49 without the
+// per-update renormalisation).  Two sites per thread per iteration so that
+// their loads are in flight together (sites of one colour never depend on
+// each other).
+template <int NC>
 __global__ void __launch_bounds__(kCThreads) k_cont_or(const __grid_constant__ ContParams P,
                                                        int colour) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < P.total_sites;
-         g += stride) {
-        const SiteRef s = locate(P, g, colour);
-        const ContClass& C = P.cls[s.ci];
-        uint32_t nb[6];
-        neighbours((uint32_t)C.L, s.x, s.y, s.z, nb);
-        float h[NC], v[NC];
-#pragma unroll
-        for (int k = 0; k < NC; ++k) {
-            const float* o = P.spins + plane_off<NC>(C, s.r, colour ^ 1, k);
-            h[k] = ((__ldg(o + nb[0]) + __ldg(o + nb[1])) + (__ldg(o + nb[2]) + __ldg(o + nb[3]))) +
-                   (__ldg(o + nb[4]) + __ldg(o + nb[5]));
-            v[k] = P.spins[plane_off<NC>(C, s.r, colour, k) + s.i];
-        }
-        float h2 = 0.f, sh = 0.f;
-#pragma unroll
-        for (int k = 0; k < NC; ++k) {
-            h2 = fmaf(h[k], h[k], h2);
-            sh = fmaf(v[k], h[k], sh);
-        }
-        if (h2 < 1e-20f) continue;
-        const float scale = 2.0f * sh / h2;
-#pragma unroll
-        for (int k = 0; k < NC; ++k)
-            P.spins[plane_off<NC>(C, s.r, colour, k) + s.i] = fmaf(scale, h[k], -v[k]);
+    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; g + stride < P.total_sites; g += 2 * stride) {
+        SiteRef s0, s1;
+        float h0[NC], v0[NC], h1[NC], v1[NC];
+        or_load<NC>(P, g, colour, s0, h0, v0);
+        or_load<NC>(P, g + stride, colour, s1, h1, v1);
+        or_store<NC>(P, colour, s0, h0, v0);
+        or_store<NC>(P, colour, s1, h1, v1);
+    }
+    if (g < P.total_sites) {
+        SiteRef s0;
+        float h0[NC], v0[NC];
+        or_load<NC>(P, g, colour, s0, h0, v0);
+        or_store<NC>(P, colour, s0, h0, v0);
     }
 }
 
@@ -224,7 +259,8 @@ __global__ void __launch_bounds__(kCThreads)
                 for (int k = 0; k < 3; ++k) w[k] *= wn;
             } else {
                 float sd, cd;
-                sincosf(delta * (2.0f * uniform24(u.x) - 1.0f), &sd, &cd);
+                // rotation angle delta*(2u-1), as a multiple of pi
+                sincospif(delta * 0.318309886183790672f * (2.0f * uniform24(u.x) - 1.0f), &sd, &cd);
                 w[0] = v[0] * cd - v[1] * sd;
                 w[1] = v[1] * cd + v[0] * sd;
             }
@@ -675,6 +711,8 @@ int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas,
         C.plane_sites = (uint32_t)((int64_t)L * L * L / 2);
         C.div_half = make_div((uint32_t)(L / 2));
         C.div_L = make_div((uint32_t)L);
+        C.div_plane = make_div(C.plane_sites);
+        C.small = (int64_t)C.plane_sites * replicas < (1ll << 31) ? 1 : 0;
         C.rep_base = s * replicas;
         C.off = off;
         off += ((2 * (int64_t)n_comp * C.plane_sites * replicas + 63) / 64) * 64;

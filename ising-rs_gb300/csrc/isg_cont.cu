@@ -175,23 +175,13 @@ __device__ __forceinline__ void or_store(const ContParams& P, int colour, const 
 
 // Overrelaxation: S' = 2 (S.h)/|h|^2 h - S about the local field
 // (continuous_spin_kernel.cu:88-142; overrelax.rs:16-49 without the
-// per-update renormalisation).  Two sites per thread per iteration so that
-// their loads are in flight together (sites of one colour never depend on
-// each other).
+// per-update renormalisation).
 template <int NC>
 __global__ void __launch_bounds__(kCThreads) k_cont_or(const __grid_constant__ ContParams P,
                                                        int colour) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    for (; g + stride < P.total_sites; g += 2 * stride) {
-        SiteRef s0, s1;
-        float h0[NC], v0[NC], h1[NC], v1[NC];
-        or_load<NC>(P, g, colour, s0, h0, v0);
-        or_load<NC>(P, g + stride, colour, s1, h1, v1);
-        or_store<NC>(P, colour, s0, h0, v0);
-        or_store<NC>(P, colour, s1, h1, v1);
-    }
-    if (g < P.total_sites) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < P.total_sites;
+         g += stride) {
         SiteRef s0;
         float h0[NC], v0[NC];
         or_load<NC>(P, g, colour, s0, h0, v0);

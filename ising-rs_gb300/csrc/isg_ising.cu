@@ -99,7 +99,8 @@ struct IsingParams {
     int n_classes;
     int dim;
     int64_t total_tasks;
-    int64_t total_ctasks;
+    int64_t total_ctasks;     // rolling CTA tasks (contiguous ranges per block)
+    int64_t flat_ctasks;      // flat CTA tasks (round-robin over blocks)
     int64_t total_sites;
     uint32_t rk0[10], rk1[10];      // Philox round keys (constant-bank operands)
     IsingClass cls[kMaxClasses];
@@ -265,7 +266,7 @@ __device__ __forceinline__ uint32_t rolling_word(const IsingParams& P, const Phi
 // the z-1/z/z+1 words of the other colour stay in registers.  Flat sizes give
 // each warp one 32-word task per CTA task.
 template <int DIM, int MODE>
-__global__ void __launch_bounds__(256, MODE == 1 ? 4 : 5)
+__global__ void __launch_bounds__(256, 4)
     k_ising_words(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
     __shared__ __align__(256) uint32_t s_thr[8][64];
     const int lane = threadIdx.x & 31;
@@ -273,6 +274,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? 4 : 5)
     const int64_t G = P.total_ctasks;
     int64_t ct = (int64_t)blockIdx.x * G / gridDim.x;
     const int64_t ct_end = (int64_t)(blockIdx.x + 1) * G / gridDim.x;
+    int64_t ft = blockIdx.x;  // flat CTA tasks: blockIdx.x, + gridDim.x, ...
 
     const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
     const uint32_t c2 = (uint32_t)sweep;
@@ -285,10 +287,16 @@ __global__ void __launch_bounds__(256, MODE == 1 ? 4 : 5)
     MeasAcc macc{0, 0, 0, 0, 0};
     PhiloxPre pre{};
 
-    while (ct < ct_end) {
-        while (P.cls[ci].ctask_end <= ct) ++ci;
+    while (ct < ct_end || ft < P.flat_ctasks) {
+        // flat tasks first (short, latency-bound), spread over all blocks
+        const bool flat_now = ft < P.flat_ctasks;
+        const int64_t key = flat_now ? ft : ct;
+        ci = 0;
+        while (ci < kMaxClasses - 1 &&
+               (P.cls[ci].kind != (flat_now ? kFlat : kRolling) || P.cls[ci].ctask_end <= key))
+            ++ci;
         const IsingClass& C = P.cls[ci];
-        const int64_t lct = ct - C.ctask_base;
+        const int64_t lct = key - C.ctask_base;
         const uint32_t L = (uint32_t)C.L, Lm = L - 1;
         const int lrw = C.log2_rw;
         const uint32_t rw = 1u << lrw, rwm = rw - 1;
@@ -296,7 +304,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? 4 : 5)
         const int src_prev = lane - (int)k4 + (int)((k4 - 1) & rwm);
         const int src_next = lane - (int)k4 + (int)((k4 + 1) & rwm);
 
-        if (DIM == 3 && C.kind == kRolling) {
+        if (DIM == 3 && !flat_now) {
             // CTA task -> (replica r, column group g, z), z fastest
             const int lg = C.log2_groups + C.log2L;
             const int r = (int)(lct >> lg);
@@ -370,7 +378,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? 4 : 5)
         } else {
             // flat: warp task 8*lct + wib of this size
             const int64_t wt = (lct << 3) + wib;
-            ++ct;
+            ft += gridDim.x;
             if (wt >= C.task_end - C.task_base) continue;
             const int r = (int)(wt >> C.log2_tpp);
             const uint32_t tl = (uint32_t)(wt & (int64_t)(C.tasks_per_plane - 1));
@@ -734,7 +742,7 @@ static void (*site_kernel(int dim, int mode))(IsingParams, int, int) {
 // block per CTA task.  `threads` applies to the site kernel.
 static int configure_launch(isg_ising* H) {
     const int thr = H->threads;
-    const int64_t need = H->P.total_ctasks;
+    const int64_t need = std::max<int64_t>(H->P.total_ctasks, H->P.flat_ctasks);
     for (int mode = 0; mode < 3; ++mode) {
         int occ = 0;
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -879,7 +887,7 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
     H->sizes.assign(sizes, sizes + n_sizes);
 
     IsingParams& P = H->P;
-    int64_t off = 0, task = 0, site = 0, ctask = 0;
+    int64_t off = 0, task = 0, site = 0, ctask = 0, fctask = 0;
     for (int s = 0; s < n_sizes; ++s) {
         IsingClass& C = P.cls[s];
         const int L = sizes[s];
@@ -907,17 +915,21 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         if (C.kind != kSite) task += (int64_t)C.tasks_per_plane * replicas;
         C.task_end = task;
         C.log2_groups = 0;
-        C.ctask_base = ctask;
         if (C.kind == kRolling) {
             // columns of 32/(L/8) rows: L*L/256 per z-plane, in groups of 8
             const int cols = (L / (32 / rw));
             int groups = cols / 8;
             while ((1 << C.log2_groups) < groups) ++C.log2_groups;
+            C.ctask_base = ctask;
             ctask += (int64_t)replicas * groups * L;
+            C.ctask_end = ctask;
         } else if (C.kind == kFlat) {
-            ctask += ((int64_t)C.tasks_per_plane * replicas + 7) / 8;
+            C.ctask_base = fctask;
+            fctask += ((int64_t)C.tasks_per_plane * replicas + 7) / 8;
+            C.ctask_end = fctask;
+        } else {
+            C.ctask_base = C.ctask_end = 0;
         }
-        C.ctask_end = ctask;
         C.site_base = site;
         if (C.kind == kSite) site += (int64_t)C.plane_sites * replicas;
         C.site_end = site;
@@ -927,12 +939,14 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         P.cls[s] = P.cls[n_sizes - 1];
         P.cls[s].task_base = P.cls[s].task_end = INT64_MAX;
         P.cls[s].ctask_base = P.cls[s].ctask_end = INT64_MAX;
+        P.cls[s].kind = -1;
         P.cls[s].site_base = P.cls[s].site_end = INT64_MAX;
     }
     P.n_classes = n_sizes;
     P.dim = dim;
     P.total_tasks = task;
     P.total_ctasks = ctask;
+    P.flat_ctasks = fctask;
     P.total_sites = site;
     P.seed = seed;
     for (int r = 0; r < 10; ++r) {

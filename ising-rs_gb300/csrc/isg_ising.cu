@@ -188,7 +188,9 @@ __device__ __forceinline__ uint32_t lds_u32(uint32_t saddr) {
 // own_down*8 + n_down at byte offset 4*(...)), random words u.
 __device__ __forceinline__ uint32_t metropolis_word(uint32_t ow, uint32_t nd, uint32_t tbase,
                                                     const U4& u) {
-    const uint32_t idx4 = (nd << 2) + (ow << 5);
+    // byte offsets 4*(n_down + 8*own_down) <= 56; the mask keeps every shared
+    // load aligned and inside the warp's 256-byte table whatever the bytes hold
+    const uint32_t idx4 = ((nd << 2) + (ow << 5)) & 0x3C3C3C3Cu;
     const uint32_t t0 = lds_u32(__byte_perm(idx4, tbase, 0x7650));
     const uint32_t t1 = lds_u32(__byte_perm(idx4, tbase, 0x7651));
     const uint32_t t2 = lds_u32(__byte_perm(idx4, tbase, 0x7652));
@@ -353,7 +355,7 @@ __global__ void __launch_bounds__(256, 4)
             uint32_t h1 = single ? ldg_nc(ob + o) : 0u;
             uint32_t ow = ldg_u32(mc + o);
             uint32_t z = z0;
-#pragma unroll 1
+#pragma unroll 2
             for (; z < z1; ++z) {
                 const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm;
                 const uint32_t n_zp = ldg_nc(oc + o2);

@@ -311,7 +311,9 @@ def run_gpu(args):
     tau_rec = tau_int(series) if len(series) > 8 else float("nan")
     tau_sweeps = tau_rec * MEASURE_EVERY
     sweeps_per_s = SWEEPS_PER_STEP * args.steps / (dev_ms * 1e-3)
-    ess = sweeps_per_s / tau_sweeps if tau_sweeps > 0 else None
+    # ESS = N / (2 tau_int) with the windowed estimator (tau_int = 1/2 for
+    # independent samples)
+    ess = sweeps_per_s / (2.0 * tau_sweeps) if tau_sweeps > 0 else None
 
     if rank != 0:
         return 0

@@ -508,6 +508,71 @@ def run_continuous(args):
     return 0
 
 
+ANNEAL = dict(sizes=[8, 12, 16, 20, 24, 28], t_min=3.5, t_max=5.5, t_steps=41, warmup=500,
+              samples=200)
+
+
+def run_anneal(args):
+    """`fss --gpu` (src/cuda/fss_gpu.rs:7-39) at the reference's FssConfig defaults
+    (src/fss.rs:20-36): every size anneals from 5.5 down to 3.5 over 41 temperatures,
+    500 warm-up + 200 measured sweeps at each.  One step = the whole schedule
+    through the synchronous C-ABI call isg_fss_anneal (host arrays in and out), so
+    value and e2e are the same wall-clock measurement."""
+    import ctypes as C
+    import torch
+    torch.cuda.set_device(0)
+    pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
+    a = ANNEAL
+    sz = np.ascontiguousarray(a["sizes"], np.int32)
+    out = np.zeros((len(a["sizes"]), a["t_steps"], 7), np.float64)
+
+    def once():
+        pkg._check(pkg.lib().isg_fss_anneal(
+            sz.ctypes.data_as(C.c_void_p), len(sz), 3, a["t_min"], a["t_max"], a["t_steps"], 1.0,
+            0.0, a["warmup"], a["samples"], SEED, out.ctypes.data_as(C.c_void_p)))
+
+    steps, warm = max(1, min(args.steps, 10)), max(1, min(args.warmup, 3))
+    for _ in range(warm):
+        once()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    with clocks:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            once()
+        wall = time.perf_counter() - t0
+    updates = sum(L ** 3 for L in a["sizes"]) * a["t_steps"] * (a["warmup"] + a["samples"])
+    value = updates * steps / wall * 1e-9
+    threads = host_threads()
+    oracle = _load("isg_oracle", ROOT / "oracle" / "oracle.py")
+    rb = oracle.RefBench(a["sizes"], 3, 4.5, 4.5 + 1e-9, threads, seed=SEED)
+    rb.step(0.5)
+    sec, flips = rb.step(200.0)
+    rb.close()
+    cpu = flips / sec * 1e-9
+    d2h = len(a["sizes"]) * a["t_steps"] * a["samples"] * (4 + 8 + 8)
+    h2d = a["t_steps"] * len(a["sizes"]) * (16 * 4 + 8 + 2 * 4)
+    line = {"metric": "spin flips/ns, annealing FSS schedule (fss --gpu defaults)",
+            "value": value, "unit": "flips/ns", "n_gpus": 1, "steps": steps, "warmup": warm,
+            "ms_per_step": wall / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int8", "data": "synthetic (seeded Philox start)",
+            "config": {"workload": f"fss --gpu: L={a['sizes']}, {a['t_steps']} T from "
+                                   f"{a['t_max']} down to {a['t_min']}, {a['warmup']}+"
+                                   f"{a['samples']} sweeps per T",
+                       "timing": "wall clock around the synchronous isg_fss_anneal call",
+                       "l2": "all lattices together (50 KB) stay in L2; the schedule is "
+                             "launch-bound"},
+            "e2e": {"value": value, "unit": "flips/ns", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "cpu_baseline": {"value": cpu, "unit": "flips/ns", "cores": threads, "kind": "port",
+                             "sample": f"200 random-site sweeps of each of L={a['sizes']} per "
+                                       f"host thread at T=4.5 (reference CPU Metropolis path "
+                                       f"restated in C)"},
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_learned(args):
     import torch
     torch.cuda.set_device(0)
@@ -538,7 +603,7 @@ def main():
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--cpu-sweeps", type=float, default=1.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0)
-    ap.add_argument("--workload", default="ising", choices=["ising", "heisenberg", "xy"])
+    ap.add_argument("--workload", default="ising", choices=["ising", "heisenberg", "xy", "anneal"])
     ap.add_argument("--learned", action="store_true",
                     help="config 5: learned proposal vs plain PT ESS/s (separate JSON lines)")
     ap.add_argument("--train-seconds", type=float, default=60.0)
@@ -552,6 +617,8 @@ def main():
         return ncu_case()
     if args.learned:
         return run_learned(args)
+    if args.workload == "anneal":
+        return run_anneal(args)
     if args.workload != "ising":
         return run_continuous(args)
     if args.warmup < 3:

@@ -49,12 +49,20 @@ extern "C" {
 /* Philox stream tags (c3 bits 24..31).
  *  INIT : hot start.  c1 = natural site index / 4, step = 0; word (site & 3);
  *         spin = -1 if the word's top bit is set, else +1.
- *  ISING: Metropolis half-sweep.  c1 = colour index / 4 (colour index of
- *         site (x,y,z) = (z*L*L + y*L + x) >> 1), step = global sweep number,
- *         colour = 0 (x+y+z even) or 1; word (colour index & 3) is u, and the
- *         flip is accepted iff u <= threshold[own_down*8 + n_down_neighbours]
- *         with threshold = 0xFFFFFFFF for dE <= 0, else
+ *  ISING: Metropolis half-sweep, step = global sweep number, colour = 0
+ *         (x+y+z even) or 1.  A site of colour index i = (z*L*L + y*L + x) >> 1
+ *         (2D: (y*L + x) >> 1) flips iff the 32-bit u = coarse << 16 | fine
+ *         satisfies u <= threshold[own_down*8 + n_down_neighbours], with
+ *         threshold = 0xFFFFFFFF for dE <= 0, else
  *         max(floor(exp(-beta*dE) * 2^32), 1) - 1  (FP64 on the host).
+ *         With S = L^(dim-1)/2 sites of one colour per z-plane (3D) or row
+ *         (2D), t = i / S, v = (t >> 1)*S + i % S:
+ *           coarse = 16-bit half (t & 1) (0: bits 0..15, 1: bits 16..31) of
+ *                    word (v & 3) of the block c1 = v >> 2, so one block
+ *                    serves 8 sites, 4 at z (or y) = 2k and 4 at 2k+1;
+ *           fine   = bits 16..31 of word (i & 3) of the block
+ *                    c1 = 0x80000000 | (i >> 2); it only matters when
+ *                    coarse equals the threshold's upper 16 bits.
  *  EXCH : replica exchange.  c1 = lower temperature index of the pair,
  *         c0 = exchange uid, step = exchange count of that size;
  *         u = ((w0 << 32 | w1) >> 11) * 2^-53.
@@ -303,6 +311,29 @@ int isg_learned_adopt(isg_learned* h, const int8_t* d_props, const int64_t* d_st
                       int8_t* d_current);
 int isg_learned_sync(isg_learned* h);
 void* isg_learned_stream(isg_learned* h);
+
+/* ------------------------------------------------------------------------ */
+/* Annealing finite-size scaling (`fss --gpu`)                               */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces run_fss_gpu (src/cuda/fss_gpu.rs:7-39) with LatticeGpu::warm_up
+ * and LatticeGpu::measure (src/cuda/lattice_gpu.rs:184-251).  Every size is
+ * one lattice, annealed from t_max down to t_min through the t_steps
+ * temperatures T_k = t_min + (t_max - t_min)*k/(t_steps - 1): at each one,
+ * `warmup` sweeps, then `samples` sweeps each followed by a measurement of E
+ * and M (fused into the sweep; no spin copies).  out[(i*t_steps + k)*7 + j]
+ * receives for sizes[i], in ascending temperature order k, the Observables
+ * fields (src/observables.rs:5-13) j = 0..6: T, <e>, <|m|>, <m^2>, <m^4>,
+ * Cv = beta^2 (<e^2> - <e>^2) N, chi = beta (<m_s^2> - <m_s>^2) N with the
+ * signed m_s (lattice_gpu.rs:236-240), summed in sample order in FP64.
+ * All sizes run in one batch (one replica each); the stream of size L is
+ * keyed by (seed, L), where the reference seeds size n with seed + n
+ * (fss_gpu.rs:13).  Thresholds use beta = 1/T in FP64 (the reference passes
+ * an f32 beta to the kernel).  A repeated size repeats its rows.  Synchronous;
+ * creates and destroys its own batch. */
+int isg_fss_anneal(const int* sizes, int n_sizes, int dim, double t_min, double t_max,
+                   int t_steps, double J, double hfield, int64_t warmup, int64_t samples,
+                   uint64_t seed, double* out);
 
 /* ------------------------------------------------------------------------ */
 /* Statistics used by the drop-in driver                                     */

@@ -9,6 +9,9 @@ backend for the checkerboard PT path:
   ContinuousGpuLattice  src/cuda/gpu_lattice_continuous.rs:9-245
   linspace_temperatures src/parallel_tempering.rs:39-46
   jackknife_observables src/bin/gpu_fss.rs:327-412
+  FssConfig, Observables, run_fss_gpu
+                        src/fss.rs:6-36, src/observables.rs:5-13,
+                        src/cuda/fss_gpu.rs:7-39 (annealing `fss --gpu`)
   IsingBatch / ContinuousBatch: every (size, replica) lattice of a run in one
   handle (the GB300 replacement of the reference's Vec<LatticeGpu>).
 
@@ -20,6 +23,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+from dataclasses import dataclass, field
 from pathlib import Path
 
 import numpy as np
@@ -87,6 +91,7 @@ def _declare(L):
         "isg_ising_time_halfsweep": [vp, i32, vp],
         "isg_ising_sites_per_halfsweep": [vp, vp],
         "isg_jackknife": [vp, vp, i64, dbl, dbl, i32, vp],
+        "isg_fss_anneal": [vp, i32, i32, dbl, dbl, i32, dbl, dbl, i64, i64, u64, vp],
         "isg_cont_create": [C.POINTER(vp), vp, i32, i32, i32, u64],
         "isg_cont_destroy": [vp],
         "isg_cont_set_stream": [vp, vp],
@@ -142,6 +147,77 @@ def binder(m2: float, m4: float) -> float:
     if m2 <= 1e-15:
         return 0.0
     return 1.0 - m4 / (3.0 * m2 * m2)
+
+
+@dataclass
+class Observables:
+    """src/observables.rs:5-13: per-spin averages at one temperature."""
+    temperature: float
+    energy: float
+    magnetisation: float
+    heat_capacity: float
+    susceptibility: float
+    m2: float
+    m4: float
+
+
+def _observables(temperature: float, bond, mag, J: float, h: float, n3: float) -> Observables:
+    """Per-temperature statistics of LatticeGpu::measure (src/cuda/lattice_gpu.rs:205-251),
+    operation for operation in FP64, from per-sweep integer bond and magnetisation sums."""
+    beta = 1.0 / temperature
+    se = se2 = sm = sm2 = sm4 = sms = sms2 = 0.0
+    for b, m in zip(bond.tolist(), mag.tolist()):
+        e_per = (-J * float(b) - h * float(m)) / n3
+        m_per = abs(float(m) / n3)
+        m_signed = float(m) / n3
+        se += e_per
+        se2 += e_per * e_per
+        sm += m_per
+        sm2 += m_per * m_per
+        sm4 += m_per * m_per * m_per * m_per
+        sms += m_signed
+        sms2 += m_signed * m_signed
+    s = float(len(bond))
+    ae, ae2, am, am2, am4, ams, ams2 = se / s, se2 / s, sm / s, sm2 / s, sm4 / s, sms / s, sms2 / s
+    return Observables(temperature, ae, am, beta * beta * (ae2 - ae * ae) * n3,
+                       beta * (ams2 - ams * ams) * n3, am2, am4)
+
+
+@dataclass
+class FssConfig:
+    """src/fss.rs:6-36 (FssConfig and its Default).  The GPU path is cubic Metropolis;
+    `geometry` and `algorithm` are kept for interface parity and not used by it."""
+    sizes: list = field(default_factory=lambda: [8, 12, 16, 20, 24, 28])
+    geometry: str = "cubic"
+    j: float = 1.0
+    h: float = 0.0
+    t_min: float = 3.5
+    t_max: float = 5.5
+    t_steps: int = 41
+    warmup_sweeps: int = 500
+    sample_sweeps: int = 200
+    seed: int = 42
+    algorithm: str = "wolff"
+
+
+def run_fss_gpu(config: FssConfig, dim: int = 3) -> list:
+    """src/cuda/fss_gpu.rs:7-39 through isg_fss_anneal: for every size, anneal from
+    t_max down to t_min; returns [(n, [Observables in ascending T])]."""
+    sizes = [int(n) for n in config.sizes]
+    if not sizes:
+        return []
+    ts = int(config.t_steps)
+    out = np.zeros((len(sizes), ts, 7), np.float64)
+    sz = np.ascontiguousarray(sizes, np.int32)
+    _check(lib().isg_fss_anneal(_ptr(sz), len(sizes), int(dim), float(config.t_min),
+                                float(config.t_max), ts, float(config.j), float(config.h),
+                                int(config.warmup_sweeps), int(config.sample_sweeps),
+                                int(config.seed), _ptr(out)))
+    def obs(r):  # library row order: T, E, M, M2, M4, Cv, chi
+        return Observables(temperature=float(r[0]), energy=float(r[1]),
+                           magnetisation=float(r[2]), heat_capacity=float(r[5]),
+                           susceptibility=float(r[6]), m2=float(r[3]), m4=float(r[4]))
+    return [(n, [obs(out[i, k]) for k in range(ts)]) for i, n in enumerate(sizes)]
 
 
 def _stream_handle(stream) -> int | None:
@@ -337,6 +413,30 @@ class LatticeGpu:
 
     def get_spins(self) -> np.ndarray:
         return self._b.get_spins(0, 0)
+
+    def measure(self, temperature: float, j: float, h: float, samples: int) -> Observables:
+        """src/cuda/lattice_gpu.rs:190-251: `samples` sweeps at `temperature`, each
+        followed by a measurement of E (with the field term) and M; chi from the
+        signed magnetisation.  E and M come from the sweep's fused integer sums
+        instead of a spin copy per sample."""
+        if samples < 1:
+            raise IsingError(-1, "samples must be at least 1")
+        T = float(temperature)
+        if self._key != ("T", T, float(j), float(h)):
+            self._b.set_temperatures([T], J=float(j), h=float(h))
+            self._key = ("T", T, float(j), float(h))
+        self._b.reset_sampling()
+        _, b, m = self._b.pt_run(int(samples), min(int(samples) + 1, 1 << 30), 1)
+        return _observables(T, b[:, 0], m[:, 0], float(j), float(h), float(self.n) ** 3)
+
+    def domain_wall_density(self) -> float:
+        """src/cuda/lattice_gpu.rs:253-281: fraction of the 3 N^3 forward bonds whose
+        spins differ, from the device bond sum B = (equal - unequal):
+        walls = (3 N^3 - B) / 2."""
+        b, _ = self._b.measure()
+        bonds = 3 * self.n ** 3
+        walls = (bonds - int(b[0])) // 2
+        return walls / bonds
 
 
 class ContinuousBatch:

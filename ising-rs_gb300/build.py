@@ -1,7 +1,7 @@
-"""Build recipe for libisinggb (sm_103a) and the gpu_fss drop-in driver.
+"""Build recipe for libisinggb (sm_103a) and the gpu_fss / fss drop-in drivers.
 
 Compiles every translation unit in parallel with one -gencode
-(arch=compute_103a,code=sm_103a), links lib/libisinggb.so and bin/gpu_fss in
+(arch=compute_103a,code=sm_103a), links lib/libisinggb.so, bin/gpu_fss and bin/fss in
 the package directory.  Host code is compiled with -ffp-contract=off so the
 FP64 threshold tables, exchange energies and jackknife sums round the same on
 x86_64 and aarch64.
@@ -31,7 +31,8 @@ NVCC_FLAGS = [
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 
 CU_SOURCES = ["isg_ising.cu", "isg_cont.cu", "isg_noalloc.cu", "isg_learned.cu"]
-CPP_SOURCES = ["isg_stats.cpp"]
+CPP_SOURCES = ["isg_stats.cpp", "isg_anneal.cpp"]
+DRIVERS = ["gpu_fss", "fss"]   # host/<name>.cpp -> bin/<name>
 
 
 def _cuda_home() -> Path:
@@ -82,10 +83,10 @@ def build_all(verbose: bool = False) -> Path:
     _run_parallel(cmds)
     so = LIB / "libisinggb.so"
     _run_parallel([[nvcc, ARCH, "-shared", "-o", str(so), *map(str, objs)]])
-    driver = PKG / "host" / "gpu_fss.cpp"
-    if driver.exists() and (CSRC / "isg_cont.cu").exists():
-        _run_parallel([[cxx, *CXX_FLAGS, "-I", str(INCLUDE), str(driver), "-o", str(BIN / "gpu_fss"),
-                        "-L", str(LIB), "-lisinggb", "-Wl,-rpath,$ORIGIN/../lib"]])
+    drivers = [[cxx, *CXX_FLAGS, "-I", str(INCLUDE), str(PKG / "host" / f"{name}.cpp"), "-o",
+                str(BIN / name), "-L", str(LIB), "-lisinggb", "-Wl,-rpath,$ORIGIN/../lib"]
+               for name in DRIVERS]
+    _run_parallel(drivers)
     return so
 
 

@@ -183,23 +183,54 @@ __device__ __forceinline__ uint32_t lds_u32(uint32_t saddr) {
     return v;
 }
 
-// New word of 4 same-colour sites: own down bits ow, down-neighbour counts
-// nd (per byte), table at shared address tbase (256-byte aligned, entry
-// own_down*8 + n_down at byte offset 4*(...)), random words u.
+__device__ __forceinline__ uint2 lds_v2(uint32_t saddr) {
+    uint2 v;
+    asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(saddr));
+    return v;
+}
+
+// Per-warp threshold table in shared memory: entry own_down*8 + n_down is 8
+// bytes {thr & 0xFFFF0000, thr}.
+__device__ __forceinline__ void load_table(uint32_t* tab, const IsingParams& P, int slot,
+                                           int lane) {
+    __syncwarp();
+    if (lane < 16) {
+        const uint32_t t = P.thr[slot * 16 + lane];
+        tab[2 * lane] = t & 0xFFFF0000u;
+        tab[2 * lane + 1] = t;
+    }
+    __syncwarp();
+}
+
+// New word of 4 same-colour sites: own down bits ow, down-neighbour counts nd
+// (per byte), table at shared address tbase (256-byte aligned), and the sites'
+// coarse 16-bit randoms in bits 16..31 of U0..U3 (bits 0..15 are ignored).
+// A site flips iff u = coarse << 16 | fine <= thr.  The coarse half decides
+// unless it equals thr's upper half; then (probability 2^-16 per site) the
+// fine halves of the word come from Philox counter 0x80000000 | wfine.
 __device__ __forceinline__ uint32_t metropolis_word(uint32_t ow, uint32_t nd, uint32_t tbase,
-                                                    const U4& u) {
-    // byte offsets 4*(n_down + 8*own_down) <= 56; the mask keeps every shared
+                                                    uint32_t U0, uint32_t U1, uint32_t U2,
+                                                    uint32_t U3, const PhiloxPre& pre,
+                                                    const IsingParams& P, uint32_t wfine) {
+    // byte offsets 8*(n_down + 8*own_down) <= 120; the mask keeps every shared
     // load aligned and inside the warp's 256-byte table whatever the bytes hold
-    const uint32_t idx4 = ((nd << 2) + (ow << 5)) & 0x3C3C3C3Cu;
-    const uint32_t t0 = lds_u32(__byte_perm(idx4, tbase, 0x7650));
-    const uint32_t t1 = lds_u32(__byte_perm(idx4, tbase, 0x7651));
-    const uint32_t t2 = lds_u32(__byte_perm(idx4, tbase, 0x7652));
-    const uint32_t t3 = lds_u32(__byte_perm(idx4, tbase, 0x7653));
-    const uint32_t f0 = u.x <= t0 ? 0x00000001u : 0u;
-    const uint32_t f1 = u.y <= t1 ? 0x00000100u : 0u;
-    const uint32_t f2 = u.z <= t2 ? 0x00010000u : 0u;
-    const uint32_t f3 = u.w <= t3 ? 0x01000000u : 0u;
-    return ow ^ (f0 | f1 | f2 | f3);
+    const uint32_t idx8 = ((nd << 3) + (ow << 6)) & 0x78787878u;
+    const uint2 e0 = lds_v2(__byte_perm(idx8, tbase, 0x7650));
+    const uint2 e1 = lds_v2(__byte_perm(idx8, tbase, 0x7651));
+    const uint2 e2 = lds_v2(__byte_perm(idx8, tbase, 0x7652));
+    const uint2 e3 = lds_v2(__byte_perm(idx8, tbase, 0x7653));
+    uint32_t f = (U0 < e0.x ? 0x00000001u : 0u) | (U1 < e1.x ? 0x00000100u : 0u) |
+                 (U2 < e2.x ? 0x00010000u : 0u) | (U3 < e3.x ? 0x01000000u : 0u);
+    const bool tie = ((U0 ^ e0.x) < 0x10000u) | ((U1 ^ e1.x) < 0x10000u) |
+                     ((U2 ^ e2.x) < 0x10000u) | ((U3 ^ e3.x) < 0x10000u);
+    if (tie) {
+        const U4 fn = philox_w(pre, P, 0x80000000u | wfine);
+        f = ((((U0 & 0xFFFF0000u) | (fn.x >> 16)) <= e0.y) ? 0x00000001u : 0u) |
+            ((((U1 & 0xFFFF0000u) | (fn.y >> 16)) <= e1.y) ? 0x00000100u : 0u) |
+            ((((U2 & 0xFFFF0000u) | (fn.z >> 16)) <= e2.y) ? 0x00010000u : 0u) |
+            ((((U3 & 0xFFFF0000u) | (fn.w >> 16)) <= e3.y) ? 0x01000000u : 0u);
+    }
+    return ow ^ f;
 }
 
 __device__ __forceinline__ void flush_acc(unsigned long long* acc, int rep, long long b,
@@ -233,29 +264,46 @@ __device__ __forceinline__ void meas_flush(unsigned long long* acc, int rep, Mea
     m = MeasAcc{0, 0, 0, 0, 0};
 }
 
-// One z-step of a rolling column: the word at plane offset `o` (words) of
-// the lane's column, given the other colour's words at z-1, z, z+1 and the
-// halo row(s).  Returns the new own word.
-template <int MODE>
-__device__ __forceinline__ uint32_t rolling_word(const IsingParams& P, const PhiloxPre& pre,
-                                                 uint32_t tbase, uint32_t w, uint32_t ow,
-                                                 uint32_t zm, uint32_t za, uint32_t zp,
-                                                 uint32_t h0, uint32_t h1, bool single_row,
-                                                 bool first, bool last, uint32_t p, int src_up,
-                                                 int src_dn, int src_prev, int src_next,
-                                                 uint32_t& nd_out) {
+// One z-step of a rolling column at plane offset `o` (words): the new own
+// word from the other colour's words at z-1, z, z+1 (zm, za, zp) and the halo
+// row(s), with the next plane's loads issued first.  HI selects the upper
+// halves of the z-pair's random words (odd z) instead of the lower (even z).
+template <int MODE, bool HI>
+__device__ __forceinline__ void rolling_step(
+    const IsingParams& P, const PhiloxPre& pre, uint32_t tbase, const U4& uc,
+    const uint32_t* oc, const uint32_t* oa, const uint32_t* ob, uint32_t* mc, uint32_t col,
+    uint32_t pz, uint32_t pwm, bool single, bool first, bool last, int src_up, int src_dn,
+    int src_prev, int src_next, uint32_t& o, uint32_t& p, uint32_t& zm, uint32_t& za,
+    uint32_t& zp, uint32_t& h0, uint32_t& h1, uint32_t& ow, MeasAcc& macc) {
+    const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm;
+    const uint32_t n_zp = ldg_nc(oc + o2);
+    const uint32_t n_h0 = ldg_nc(oa + o1);
+    const uint32_t n_h1 = single ? ldg_nc(ob + o1) : 0u;
+    const uint32_t n_ow = ldg_u32(mc + o1);
     const uint32_t up = __shfl_sync(ISG_FULL_MASK, za, src_up);
     const uint32_t dn = __shfl_sync(ISG_FULL_MASK, za, src_dn);
     const uint32_t prev = __shfl_sync(ISG_FULL_MASK, za, src_prev);
     const uint32_t next = __shfl_sync(ISG_FULL_MASK, za, src_next);
-    const uint32_t wyp = single_row ? h1 : (last ? h0 : up);
+    const uint32_t wyp = single ? h1 : (last ? h0 : up);
     const uint32_t wym = first ? h0 : dn;
     const uint32_t wx = p ? __funnelshift_r(za, next, 8) : __funnelshift_l(prev, za, 8);
     const uint32_t nd = (wx + za + wyp) + (wym + zp + zm);
-    nd_out = nd;
-    if (MODE == 2) return ow;
-    const U4 u = philox_w(pre, P, w);
-    return metropolis_word(ow, nd, tbase, u);
+    uint32_t nw = ow;
+    if (MODE != 2) {
+        nw = HI ? metropolis_word(ow, nd, tbase, uc.x, uc.y, uc.z, uc.w, pre, P, o + col)
+                : metropolis_word(ow, nd, tbase, uc.x << 16, uc.y << 16, uc.z << 16,
+                                  uc.w << 16, pre, P, o + col);
+        mc[o] = nw;
+    }
+    if (MODE != 0) meas_add(macc, nw, nd, za);
+    zm = za;
+    za = zp;
+    zp = n_zp;
+    h0 = n_h0;
+    h1 = n_h1;
+    ow = n_ow;
+    p ^= 1u;
+    o = o1;
 }
 
 // MODE 0: update; 1: update then accumulate bond/mag of the new state;
@@ -268,14 +316,18 @@ __device__ __forceinline__ uint32_t rolling_word(const IsingParams& P, const Phi
 // the z-1/z/z+1 words of the other colour stay in registers.  Flat sizes give
 // each warp one 32-word task per CTA task.
 template <int DIM, int MODE>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, 3)
     k_ising_words(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
     __shared__ __align__(256) uint32_t s_thr[8][64];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
+    // rolling ranges start and end on even CTA tasks, i.e. on even z (L and
+    // every size's task count are even), so each range is whole z pairs
     const int64_t G = P.total_ctasks;
-    int64_t ct = (int64_t)blockIdx.x * G / gridDim.x;
-    const int64_t ct_end = (int64_t)(blockIdx.x + 1) * G / gridDim.x;
+    int64_t ct = ((int64_t)blockIdx.x * G / gridDim.x) & ~(int64_t)1;
+    const int64_t ct_end = blockIdx.x + 1 == gridDim.x
+                               ? G
+                               : (((int64_t)(blockIdx.x + 1) * G / gridDim.x) & ~(int64_t)1);
     int64_t ft = blockIdx.x;  // flat CTA tasks: blockIdx.x, + gridDim.x, ...
 
     const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
@@ -321,10 +373,7 @@ __global__ void __launch_bounds__(256, 4)
                 if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
                 cur_rep = rg;
                 if (MODE != 2) {
-                    const int slot = C.rep_base + P.r2t[rg];
-                    __syncwarp();
-                    if (lane < 16) s_thr[wib][lane] = P.thr[slot * 16 + lane];
-                    __syncwarp();
+                    load_table(s_thr[wib], P, C.rep_base + P.r2t[rg], lane);
                     pre = philox_pre(replica_uid(C.L, r), c2, c3, P.rk0[0], P.rk1[0]);
                 }
             }
@@ -354,28 +403,17 @@ __global__ void __launch_bounds__(256, 4)
             uint32_t h0 = ldg_nc(oa + o);
             uint32_t h1 = single ? ldg_nc(ob + o) : 0u;
             uint32_t ow = ldg_u32(mc + o);
-            uint32_t z = z0;
-#pragma unroll 2
-            for (; z < z1; ++z) {
-                const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm;
-                const uint32_t n_zp = ldg_nc(oc + o2);
-                const uint32_t n_h0 = ldg_nc(oa + o1);
-                const uint32_t n_h1 = single ? ldg_nc(ob + o1) : 0u;
-                const uint32_t n_ow = ldg_u32(mc + o1);
-                uint32_t nd;
-                const uint32_t nw = rolling_word<MODE>(P, pre, tbase, o + col, ow, zm, za, zp, h0,
-                                                       h1, single, first, last, p, src_up, src_dn,
-                                                       src_prev, src_next, nd);
-                if (MODE != 2) mc[o] = nw;
-                if (MODE != 0) meas_add(macc, nw, nd, za);
-                zm = za;
-                za = zp;
-                zp = n_zp;
-                h0 = n_h0;
-                h1 = n_h1;
-                ow = n_ow;
-                p ^= 1u;
-                o = o1;
+            // z pairs (2k, 2k+1) share one Philox block: counter (z>>1)*pz + col,
+            // lower 16-bit halves for even z, upper for odd z
+            for (uint32_t z = z0; z < z1; z += 2) {
+                U4 uc{};
+                if (MODE != 2) uc = philox_w(pre, P, (o >> 1) + col);
+                rolling_step<MODE, false>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm, single,
+                                          first, last, src_up, src_dn, src_prev, src_next, o, p,
+                                          zm, za, zp, h0, h1, ow, macc);
+                rolling_step<MODE, true>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm, single,
+                                         first, last, src_up, src_dn, src_prev, src_next, o, p,
+                                         zm, za, zp, h0, h1, ow, macc);
             }
         } else {
             // flat: warp task 8*lct + wib of this size
@@ -389,10 +427,7 @@ __global__ void __launch_bounds__(256, 4)
                 if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
                 cur_rep = rg;
                 if (MODE != 2) {
-                    const int slot = C.rep_base + P.r2t[rg];
-                    __syncwarp();
-                    if (lane < 16) s_thr[wib][lane] = P.thr[slot * 16 + lane];
-                    __syncwarp();
+                    load_table(s_thr[wib], P, C.rep_base + P.r2t[rg], lane);
                     pre = philox_pre(replica_uid(C.L, r), c2, c3, P.rk0[0], P.rk1[0]);
                 }
             }
@@ -433,8 +468,13 @@ __global__ void __launch_bounds__(256, 4)
             const uint32_t ow = own[w];
             uint32_t nw = ow;
             if (MODE != 2) {
-                const U4 u = philox_w(pre, P, w);
-                nw = metropolis_word(ow, nd, tbase, u);
+                // z (3D) or y (2D) pair of this word: one Philox block, halves by parity
+                const uint32_t t = DIM == 3 ? z : y;
+                const uint32_t slab = DIM == 3 ? (L << lrw) : rw;
+                const U4 u = philox_w(pre, P, w - ((t + 1) >> 1) * slab);
+                const uint32_t sh = (t & 1u) ? 0u : 16u;
+                nw = metropolis_word(ow, nd, tbase, u.x << sh, u.y << sh, u.z << sh, u.w << sh,
+                                     pre, P, w);
                 own[w] = nw;
             }
             if (MODE != 0) meas_add(macc, nw, nd, wa);
@@ -494,10 +534,23 @@ __global__ void __launch_bounds__(kMaxThreads)
             const int rg = C.rep_base + r;
             const int slot = C.rep_base + P.r2t[rg];
             const uint32_t th = P.thr[slot * 16 + d * 8 + nd];
-            const U4 u = philox10(replica_uid(L, r), i >> 2, c2, c3, k0, k1);
-            const uint32_t j = i & 3u;
-            const uint32_t uu = j == 0 ? u.x : j == 1 ? u.y : j == 2 ? u.z : u.w;
-            if (uu <= th) {
+            // slab S = sites of this colour per z-plane (3D) or row (2D); the
+            // slab pair (t, t+1) shares Philox blocks: v = (t>>1)*S + (i mod S)
+            const uint32_t S = C.plane_sites / Lu;
+            const uint32_t t = DIM == 3 ? z : y;
+            const uint32_t v = (t >> 1) * S + (i - t * S);
+            const U4 u = philox10(replica_uid(L, r), v >> 2, c2, c3, k0, k1);
+            const uint32_t jv = v & 3u;
+            const uint32_t uw = jv == 0 ? u.x : jv == 1 ? u.y : jv == 2 ? u.z : u.w;
+            const uint32_t a16 = (t & 1u) ? (uw >> 16) : (uw & 0xFFFFu);
+            bool acc = a16 < (th >> 16);
+            if (a16 == (th >> 16)) {
+                const U4 f = philox10(replica_uid(L, r), 0x80000000u | (i >> 2), c2, c3, k0, k1);
+                const uint32_t ji = i & 3u;
+                const uint32_t fw = ji == 0 ? f.x : ji == 1 ? f.y : ji == 2 ? f.z : f.w;
+                acc = ((a16 << 16) | (fw >> 16)) <= th;
+            }
+            if (acc) {
                 d ^= 1;
                 own[i] = (uint8_t)d;
             }
@@ -714,6 +767,8 @@ struct isg_ising {
     // cached cycle graph
     cudaGraphExec_t graph = nullptr;
     int graph_ee = 0, graph_me = 0, graph_period = 0;
+    // cached graph of kStepGraphSweeps plain sweeps (isg_ising_step)
+    cudaGraphExec_t step_graph = nullptr;
 };
 
 namespace isg {
@@ -787,7 +842,14 @@ static void destroy_graph(isg_ising* H) {
     if (H->graph) cudaGraphExecDestroy(H->graph);
     H->graph = nullptr;
     H->graph_period = 0;
+    if (H->step_graph) cudaGraphExecDestroy(H->step_graph);
+    H->step_graph = nullptr;
 }
+
+// Plain sweeps (no measurement, no exchange) replayed as one graph: every
+// node reads the sweep base from the device counter, so replays continue the
+// random stream.
+constexpr int kStepGraphSweeps = 64;
 
 // One sampling sweep k (0-based) issued directly.
 static void issue_sample_sweep(isg_ising* H, uint64_t k, int sweep_off, int ee, int me,
@@ -1100,12 +1162,14 @@ int isg_ising_set_temperatures(isg_ising* H, const double* temps, double J, doub
     ISG_CK(cudaMemcpyAsync(H->d_t2r, ident.data(), sizeof(int32_t) * RT, cudaMemcpyHostToDevice,
                            H->stream));
     ISG_CK(cudaStreamSynchronize(H->stream));
+    // graph nodes hold J and h by value; thresholds and maps are read from
+    // device memory, so the graphs survive a change of temperatures alone
+    if (!H->temps_set || J != H->J || hfield != H->h) destroy_graph(H);
     H->J = J;
     H->h = hfield;
     H->Q.J = J;
     H->Q.h = hfield;
     H->temps_set = true;
-    destroy_graph(H);
     return ISG_OK;
 }
 
@@ -1116,6 +1180,25 @@ int isg_ising_step(isg_ising* H, int64_t n_sweeps) {
     if (n_sweeps == 0) return ISG_OK;
     cudaSetDevice(H->device);
     int64_t done = 0;
+    if (n_sweeps >= kStepGraphSweeps && !H->step_graph) {
+        cudaGraph_t g = nullptr;
+        ISG_CK(cudaStreamBeginCapture(H->stream, cudaStreamCaptureModeThreadLocal));
+        for (int j = 0; j < kStepGraphSweeps; ++j) {
+            launch_half(H, 0, j, 0);
+            launch_half(H, 1, j, 0);
+        }
+        launch_post(H, 0, 0, 0, 0, kStepGraphSweeps);
+        cudaError_t e = cudaStreamEndCapture(H->stream, &g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&H->step_graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            H->step_graph = nullptr;
+            return cuda_fail(e, "cudaGraphInstantiate");
+        }
+    }
+    for (; n_sweeps - done >= kStepGraphSweeps; done += kStepGraphSweeps)
+        ISG_CK(cudaGraphLaunch(H->step_graph, H->stream));
     while (done < n_sweeps) {
         const int chunk = (int)std::min<int64_t>(n_sweeps - done, 1 << 20);
         for (int j = 0; j < chunk; ++j) {

@@ -17,139 +17,24 @@
 //     default 100);
 //   * odd or repeated sizes are rejected/merged (the reference kernel
 //     mapping is wrong for odd N, kernels.cu:28).
-#include <errno.h>
-#include <math.h>
-#include <stdint.h>
-#include <stdio.h>
-#include <stdlib.h>
-#include <string.h>
-#include <sys/stat.h>
-
 #include <algorithm>
 #include <string>
 #include <vector>
 
 #include "isg.h"
+#include "rust_cli.hpp"
 
 namespace {
 
-[[noreturn]] void die(const std::string& msg) {
-    fprintf(stderr, "%s\n", msg.c_str());
-    exit(1);
-}
+using rcli::die;
+using rcli::get_arg;
+using rcli::join_path;
+using rcli::mkdirs;
+using rcli::parse_arg;
+using rcli::rust_f64;
 
-// Rust's `expect` on an Err: panic message and exit code 101.
 [[noreturn]] void panic_expect(const char* what, const std::string& err) {
-    fprintf(stderr, "thread 'main' panicked at src/bin/gpu_fss.rs:\n%s: %s\n", what, err.c_str());
-    exit(101);
-}
-
-// f64 Display as Rust prints it: shortest round-trip digits, no exponent.
-std::string rust_f64(double x) {
-    if (isnan(x)) return "NaN";
-    if (isinf(x)) return x < 0 ? "-inf" : "inf";
-    if (x == 0.0) return signbit(x) ? "-0" : "0";
-    char buf[64];
-    int p = 1;
-    for (; p <= 17; ++p) {
-        snprintf(buf, sizeof buf, "%.*e", p - 1, x);
-        if (strtod(buf, nullptr) == x) break;
-    }
-    std::string s(buf);
-    bool neg = s[0] == '-';
-    if (neg) s = s.substr(1);
-    size_t epos = s.find('e');
-    int exp10 = atoi(s.c_str() + epos + 1);
-    std::string digits;
-    for (size_t i = 0; i < epos; ++i)
-        if (s[i] != '.') digits += s[i];
-    while (digits.size() > 1 && digits.back() == '0') digits.pop_back();
-    std::string out;
-    if (exp10 >= 0) {
-        if ((int)digits.size() <= exp10 + 1) {
-            out = digits + std::string(exp10 + 1 - digits.size(), '0');
-        } else {
-            out = digits.substr(0, exp10 + 1) + "." + digits.substr(exp10 + 1);
-        }
-    } else {
-        out = "0." + std::string(-exp10 - 1, '0') + digits;
-    }
-    return (neg ? "-" : "") + out;
-}
-
-std::string get_arg(int argc, char** argv, int i, const char* flag) {
-    if (i + 1 >= argc) die(std::string("Error: ") + flag + " requires a value");
-    return argv[i + 1];
-}
-
-// Rust's str::parse::<usize>/<u64>: optional '+', decimal digits only.
-bool parse_unsigned(const std::string& v, uint64_t* out, std::string* err) {
-    if (v.empty()) {
-        *err = "cannot parse integer from empty string";
-        return false;
-    }
-    size_t i = 0;
-    if (v[0] == '+') i = 1;
-    if (i >= v.size()) {
-        *err = "invalid digit found in string";
-        return false;
-    }
-    uint64_t x = 0;
-    for (; i < v.size(); ++i) {
-        if (v[i] < '0' || v[i] > '9') {
-            *err = "invalid digit found in string";
-            return false;
-        }
-        uint64_t d = (uint64_t)(v[i] - '0');
-        if (x > (UINT64_MAX - d) / 10) {
-            *err = "number too large to fit in target type";
-            return false;
-        }
-        x = x * 10 + d;
-    }
-    *out = x;
-    return true;
-}
-
-bool parse_f64(const std::string& v, double* out, std::string* err) {
-    if (v.empty()) {
-        *err = "cannot parse float from empty string";
-        return false;
-    }
-    for (char c : v)
-        if (isspace((unsigned char)c) || c == 'x' || c == 'X' || c == 'p' || c == 'P') {
-            *err = "invalid float literal";
-            return false;
-        }
-    char* end = nullptr;
-    errno = 0;
-    double x = strtod(v.c_str(), &end);
-    if (end == v.c_str() || *end != '\0') {
-        *err = "invalid float literal";
-        return false;
-    }
-    *out = x;
-    return true;
-}
-
-template <class T>
-T parse_arg(int argc, char** argv, int i, const char* flag);
-
-template <>
-uint64_t parse_arg<uint64_t>(int argc, char** argv, int i, const char* flag) {
-    std::string v = get_arg(argc, argv, i, flag), err;
-    uint64_t x = 0;
-    if (!parse_unsigned(v, &x, &err))
-        die("Error: invalid value '" + v + "' for " + flag + ": " + err);
-    return x;
-}
-
-template <>
-double parse_arg<double>(int argc, char** argv, int i, const char* flag) {
-    std::string v = get_arg(argc, argv, i, flag), err;
-    double x = 0;
-    if (!parse_f64(v, &x, &err)) die("Error: invalid value '" + v + "' for " + flag + ": " + err);
-    return x;
+    rcli::panic_expect("src/bin/gpu_fss.rs", what, err);
 }
 
 std::vector<double> linspace(double a, double b, uint64_t n) {
@@ -157,38 +42,6 @@ std::vector<double> linspace(double a, double b, uint64_t n) {
     if (n == 1) return {a};
     for (uint64_t i = 0; i < n; ++i) t.push_back(a + (b - a) * (double)i / (double)(n - 1));
     return t;
-}
-
-std::string join_path(const std::string& dir, const std::string& name) {
-    if (dir.empty()) return name;
-    if (dir.back() == '/') return dir + name;
-    return dir + "/" + name;
-}
-
-bool mkdirs(const std::string& path, std::string* err) {
-    std::string cur;
-    size_t i = 0;
-    if (!path.empty() && path[0] == '/') cur = "/", i = 1;
-    while (i <= path.size()) {
-        size_t j = path.find('/', i);
-        if (j == std::string::npos) j = path.size();
-        if (j > i) {
-            cur += path.substr(i, j - i);
-            if (mkdir(cur.c_str(), 0777) != 0 && errno != EEXIST) {
-                *err = std::string("Os { code: ") + std::to_string(errno) + ", message: \"" +
-                       strerror(errno) + "\" }";
-                return false;
-            }
-            struct stat st;
-            if (stat(cur.c_str(), &st) != 0 || !S_ISDIR(st.st_mode)) {
-                *err = "Os { code: 17, message: \"File exists\" }";
-                return false;
-            }
-            cur += "/";
-        }
-        i = j + 1;
-    }
-    return true;
 }
 
 struct Series {
@@ -473,19 +326,7 @@ int main(int argc, char** argv) {
         else i += 1;
     }
     // sizes: comma-separated, trimmed, malformed entries dropped (gpu_fss.rs:98-101)
-    std::vector<int> sizes_all;
-    size_t p = 0;
-    while (p <= sizes_str.size()) {
-        size_t q = sizes_str.find(',', p);
-        if (q == std::string::npos) q = sizes_str.size();
-        std::string tok = sizes_str.substr(p, q - p);
-        size_t b = tok.find_first_not_of(" \t\n\r"), e = tok.find_last_not_of(" \t\n\r");
-        tok = b == std::string::npos ? "" : tok.substr(b, e - b + 1);
-        uint64_t v = 0;
-        std::string err;
-        if (parse_unsigned(tok, &v, &err) && v <= 0x7FFFFFFF) sizes_all.push_back((int)v);
-        p = q + 1;
-    }
+    std::vector<int> sizes_all = rcli::parse_sizes(sizes_str, true);
     // validate_temp_range / validate_samples (cli.rs:86-107), gpu_fss.rs:103-109
     if (a.tmin <= 0.0) die("Error: --tmin must be positive (got " + rust_f64(a.tmin) + ")");
     if (a.tmax <= 0.0) die("Error: --tmax must be positive (got " + rust_f64(a.tmax) + ")");

@@ -135,11 +135,23 @@ static inline int64_t site_index(int L, int dim, int x, int y, int z) {
     return dim == 3 ? ((int64_t)z * L + y) * L + x : (int64_t)y * L + x;
 }
 
-/* One colour of a checkerboard sweep on natural-layout spins. */
+/* One colour of a checkerboard sweep on natural-layout spins.
+ *
+ * The 32-bit random u of a site at colour index ci = natural index >> 1 is
+ * assembled from two Philox blocks of the ISING stream (the GPU kernels'
+ * definition, include/isg.h):
+ *   S = L^(dim-1)/2 sites of one colour per z-plane (3D) or row (2D),
+ *   t = ci / S, j = ci % S, v = (t >> 1) * S + j;
+ *   coarse = bits 16*(t & 1) .. +15 of word (v & 3) of block c1 = v >> 2;
+ *   fine   = bits 16..31 of word (ci & 3) of block c1 = 0x80000000 | (ci >> 2);
+ *   u = coarse << 16 | fine, and the site flips iff u <= thr.
+ * The fine block is only drawn when coarse equals thr's upper half (otherwise
+ * the comparison is already decided). */
 void or_ising_halfsweep(int L, int dim, int8_t* spins, int colour, uint64_t seed, uint32_t uid,
                         uint64_t sweep, const uint32_t thr[16]) {
     int zmax = dim == 3 ? L : 1;
-    uint32_t w[4];
+    const int64_t S = (dim == 3 ? (int64_t)L * L : (int64_t)L) / 2;
+    uint32_t w[4], fw[4];
     int64_t cached_block = -1;
     for (int z = 0; z < zmax; ++z)
         for (int y = 0; y < L; ++y)
@@ -160,13 +172,23 @@ void or_ising_halfsweep(int L, int dim, int8_t* spins, int colour, uint64_t seed
                     nd += spins[site_index(L, dim, x, y, zm)] < 0;
                 }
                 int od = spins[idx] < 0;
-                if ((ci >> 2) != cached_block) {
-                    cached_block = ci >> 2;
+                const uint32_t th = thr[od * 8 + nd];
+                const int64_t t = ci / S, v = (t >> 1) * S + (ci - t * S);
+                if ((v >> 2) != cached_block) {
+                    cached_block = v >> 2;
                     stream_words(seed, (uint32_t)cached_block, uid, sweep, TAG_ISING,
                                  (uint32_t)colour, w);
                 }
-                uint32_t u = w[ci & 3];
-                if (u <= thr[od * 8 + nd]) spins[idx] = (int8_t)(-spins[idx]);
+                const uint32_t coarse = (t & 1) ? (w[v & 3] >> 16) : (w[v & 3] & 0xFFFFu);
+                int flip;
+                if (coarse != (th >> 16)) {
+                    flip = coarse < (th >> 16);
+                } else {
+                    stream_words(seed, 0x80000000u | (uint32_t)(ci >> 2), uid, sweep, TAG_ISING,
+                                 (uint32_t)colour, fw);
+                    flip = ((coarse << 16) | (fw[ci & 3] >> 16)) <= th;
+                }
+                if (flip) spins[idx] = (int8_t)(-spins[idx]);
             }
 }
 

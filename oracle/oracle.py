@@ -187,6 +187,51 @@ class IsingPT:
         return rt[:k].reshape(got, self.R), rb[:k].reshape(got, self.R), rm[:k].reshape(got, self.R)
 
 
+def measure_observables(T: float, bond, mag, J: float, h: float, n3: float) -> list[float]:
+    """LatticeGpu::measure (src/cuda/lattice_gpu.rs:205-251) restated: per-sample
+    e = E/N with E = sum_i(-J s_i nb_i / 2 - h s_i) = -J*bond - h*M (exact for the
+    integer sums), m = |M/N|, m_s = M/N; FP64 running sums in sample order;
+    [T, <e>, <m>, <m^2>, <m^4>, Cv, chi] with chi from the signed m_s."""
+    beta = 1.0 / T
+    se = se2 = sm = sm2 = sm4 = sms = sms2 = 0.0
+    for b, m in zip(np.asarray(bond).tolist(), np.asarray(mag).tolist()):
+        e_per = (-J * float(b) - h * float(m)) / n3
+        m_per = abs(float(m) / n3)
+        m_signed = float(m) / n3
+        se += e_per
+        se2 += e_per * e_per
+        sm += m_per
+        sm2 += m_per * m_per
+        sm4 += m_per * m_per * m_per * m_per
+        sms += m_signed
+        sms2 += m_signed * m_signed
+    n = float(len(bond))
+    ae, ae2, am, am2, am4, ams, ams2 = se / n, se2 / n, sm / n, sm2 / n, sm4 / n, sms / n, sms2 / n
+    return [T, ae, am, am2, am4, beta * beta * (ae2 - ae * ae) * n3, beta * (ams2 - ams * ams) * n3]
+
+
+def fss_anneal(sizes, dim: int, t_min: float, t_max: float, t_steps: int, J: float, h: float,
+               warmup: int, samples: int, seed: int) -> np.ndarray:
+    """The `fss --gpu` schedule (src/cuda/fss_gpu.rs:7-39) replayed on the GPU stream
+    definition: per size one replica, temperatures from t_max down to t_min
+    (T_k = t_min + (t_max - t_min)*k/(t_steps-1)), `warmup` sweeps then `samples`
+    measured sweeps at each.  Returns [n_sizes, t_steps, 7] in ascending T."""
+    out = np.zeros((len(sizes), t_steps, 7), np.float64)
+    for i, L in enumerate(sizes):
+        n3 = float(L ** dim)
+        pt = IsingPT(L, dim, 1, [t_max], seed, J, h)
+        for k in range(t_steps - 1, -1, -1):
+            T = t_min + (t_max - t_min) * float(k) / float(t_steps - 1)
+            pt.temps[:] = T
+            pt.r2t[:] = 0
+            pt.t2r[:] = 0
+            pt.warmup(warmup)
+            pt.reset_sampling()
+            _, b, m = pt.sample(samples, samples + 1, 1)
+            out[i, k] = measure_observables(T, b[:, 0], m[:, 0], J, h, n3)
+    return out
+
+
 def ref_run(L: int, dim: int, T: float, seed: int, warmup: int, samples: int, J=1.0, h=0.0):
     e = np.zeros(samples, np.float64)
     m = np.zeros(samples, np.float64)

@@ -155,6 +155,24 @@ int isg_ising_pt_run(isg_ising* h, int64_t n_sweeps, int exchange_every, int mea
                      int32_t* tslot_rec, int64_t* bond_rec, int64_t* mag_rec,
                      int64_t max_records, int64_t* n_records);
 
+/* A temperature schedule on every lattice of the batch: n_sweeps full sweeps,
+ * sweep k at temperature temps[k] for all lattices (temps NULL: every lattice
+ * at its current slot temperature), no exchange.  After sweep k with
+ * measure_every > 0 and k % measure_every == measure_phase, one record row of
+ * (bond_sum, magnetisation) per lattice (index s*replicas + r) is appended to
+ * bond/mag (max_records rows; *n_records returns the rows written).  With
+ * temps given, every slot holds temps[n_sweeps-1] afterwards.  Lattices of at
+ * most 65536 sites per colour run the whole schedule in one launch, one
+ * thread-block cluster per lattice; larger ones sweep with the half-sweep
+ * kernels.  Same random stream and results as isg_ising_step.  Synchronous
+ * when records are written.  Replaces the sweep-by-sweep temperature loops of
+ * src/cuda/fss_gpu.rs:19-33, src/cuda/kz_gpu.rs:17-40 and
+ * src/cuda/coarsening_gpu.rs:10-28 (LatticeGpu::step per sweep, with a
+ * full spin copy per measurement). */
+int isg_ising_run_schedule(isg_ising* h, const double* temps, int64_t n_sweeps, int measure_every,
+                           int measure_phase, int64_t* bond_rec, int64_t* mag_rec,
+                           int64_t max_records, int64_t* n_records);
+
 /* Copy the records still held in the device ring (at most max_records, the
  * newest ones) to the caller's arrays; synchronous. */
 int isg_ising_read_records(isg_ising* h, int32_t* tslot_rec, int64_t* bond_rec, int64_t* mag_rec,
@@ -334,6 +352,36 @@ void* isg_learned_stream(isg_learned* h);
 int isg_fss_anneal(const int* sizes, int n_sizes, int dim, double t_min, double t_max,
                    int t_steps, double J, double hfield, int64_t warmup, int64_t samples,
                    uint64_t seed, double* out);
+
+/* ------------------------------------------------------------------------ */
+/* Quench protocols (`kz --gpu`, `coarsening --gpu`)                         */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces run_kz_sweep_gpu / run_kz_gpu (src/cuda/kz_gpu.rs:9-95) on a cubic
+ * n^3 lattice: for every tau_q[i], n_trials lattices are warmed up for
+ * warmup_sweeps sweeps at t_start, ramped linearly over tau_q[i] sweeps
+ * (sweep k at max(t_start + (t_end - t_start)*(k+1)/tau_q, 0.01),
+ * kibble_zurek.rs:78-84), then held freeze_sweeps sweeps at
+ * max(freeze_temperature, 0.01); the final domain-wall density
+ * rho = walls / (3 n^3) over the forward bonds (lattice_gpu.rs:253-281) gives
+ * out[2*i] = mean and out[2*i+1] = standard error over the trials
+ * (mean_and_std_err, kibble_zurek.rs:86-100).  Trial t of tau_q uses replica
+ * t of a batch keyed by base_seed + tau_q (the reference seeds it with
+ * base_seed + tau_q + t).  All tau_q values run concurrently, each schedule
+ * in one launch for n^3 <= 131072.  Synchronous. */
+int isg_kz_sweep(int n, double J, double t_start, double t_end, const int64_t* tau_q, int n_tau,
+                 int n_trials, int64_t warmup_sweeps, int64_t freeze_sweeps,
+                 double freeze_temperature, uint64_t base_seed, double* out);
+
+/* Replaces run_coarsening_gpu (src/cuda/coarsening_gpu.rs:6-31) on a cubic
+ * n^3 lattice: warmup_sweeps sweeps at t_high, then total_steps sweeps at
+ * max(t_quench, 0.01); after sweep `step` with step % sample_every == 0 the
+ * point (step, rho) is written to steps_out / rho_out (max_points entries,
+ * *n_points returns the count), rho being the domain-wall density of the
+ * forward bonds from the fused bond sum.  Synchronous. */
+int isg_coarsening(int n, double J, double t_high, double t_quench, int64_t warmup_sweeps,
+                   int64_t total_steps, int64_t sample_every, uint64_t seed, int64_t* steps_out,
+                   double* rho_out, int64_t max_points, int64_t* n_points);
 
 /* ------------------------------------------------------------------------ */
 /* Statistics used by the drop-in driver                                     */

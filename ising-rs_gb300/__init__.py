@@ -12,6 +12,10 @@ backend for the checkerboard PT path:
   FssConfig, Observables, run_fss_gpu
                         src/fss.rs:6-36, src/observables.rs:5-13,
                         src/cuda/fss_gpu.rs:7-39 (annealing `fss --gpu`)
+  KzProtocol, KzSweepPoint, run_kz_sweep_gpu
+                        src/kibble_zurek.rs:11-76, src/cuda/kz_gpu.rs:46-95
+  CoarseningConfig, CoarseningPoint, run_coarsening_gpu
+                        src/coarsening.rs:14-56, src/cuda/coarsening_gpu.rs:6-31
   IsingBatch / ContinuousBatch: every (size, replica) lattice of a run in one
   handle (the GB300 replacement of the reference's Vec<LatticeGpu>).
 
@@ -81,6 +85,7 @@ def _declare(L):
         "isg_ising_get_spins": [vp, i32, i32, vp],
         "isg_ising_set_spins": [vp, i32, i32, vp],
         "isg_ising_pt_run": [vp, i64, i32, i32, vp, vp, vp, i64, vp],
+        "isg_ising_run_schedule": [vp, vp, i64, i32, i32, vp, vp, i64, vp],
         "isg_ising_read_records": [vp, vp, vp, vp, i64, vp],
         "isg_ising_reset_sampling": [vp],
         "isg_ising_get_accepted": [vp, vp],
@@ -92,6 +97,8 @@ def _declare(L):
         "isg_ising_sites_per_halfsweep": [vp, vp],
         "isg_jackknife": [vp, vp, i64, dbl, dbl, i32, vp],
         "isg_fss_anneal": [vp, i32, i32, dbl, dbl, i32, dbl, dbl, i64, i64, u64, vp],
+        "isg_kz_sweep": [i32, dbl, dbl, dbl, vp, i32, i32, i64, i64, dbl, u64, vp],
+        "isg_coarsening": [i32, dbl, dbl, dbl, i64, i64, i64, u64, vp, vp, i64, vp],
         "isg_cont_create": [C.POINTER(vp), vp, i32, i32, i32, u64],
         "isg_cont_destroy": [vp],
         "isg_cont_set_stream": [vp, vp],
@@ -220,6 +227,81 @@ def run_fss_gpu(config: FssConfig, dim: int = 3) -> list:
     return [(n, [obs(out[i, k]) for k in range(ts)]) for i, n in enumerate(sizes)]
 
 
+@dataclass
+class KzProtocol:
+    """src/kibble_zurek.rs:11-34."""
+    warmup_sweeps: int = 200
+    freeze_sweeps: int = 0
+    freeze_temperature: float = 0.01
+
+    def describe(self) -> str:
+        return (f"warmup={self.warmup_sweeps} sweeps, ramp endpoint measurement, "
+                f"freeze={self.freeze_sweeps} sweeps at T={self.freeze_temperature:.4f}")
+
+
+@dataclass
+class KzSweepPoint:
+    """src/kibble_zurek.rs:63-69."""
+    tau_q: int
+    rho: float
+    rho_err: float
+    n_trials: int
+
+
+def run_kz_sweep_gpu(n: int, geometry: str, j: float, t_start: float, t_end: float,
+                     tau_q_values, n_trials: int, protocol: KzProtocol | None = None,
+                     base_seed: int = 42) -> list:
+    """src/cuda/kz_gpu.rs:46-95 through isg_kz_sweep (cubic only, as the reference)."""
+    if geometry not in ("cubic", "Cubic3D"):
+        raise IsingError(-4, "GPU KZ only supports cubic geometry")
+    protocol = protocol or KzProtocol()
+    taus = np.ascontiguousarray([int(t) for t in tau_q_values], np.int64)
+    if len(taus) == 0:
+        return []
+    out = np.zeros((len(taus), 2), np.float64)
+    _check(lib().isg_kz_sweep(int(n), float(j), float(t_start), float(t_end), _ptr(taus),
+                              len(taus), int(n_trials), int(protocol.warmup_sweeps),
+                              int(protocol.freeze_sweeps), float(protocol.freeze_temperature),
+                              int(base_seed), _ptr(out)))
+    return [KzSweepPoint(int(t), float(r), float(e), int(n_trials))
+            for t, (r, e) in zip(taus.tolist(), out)]
+
+
+@dataclass
+class CoarseningConfig:
+    """src/coarsening.rs:14-50 (CoarseningConfig and its Default)."""
+    n: int = 30
+    geometry: str = "cubic"
+    j: float = 1.0
+    t_high: float = 10.0
+    t_quench: float = 0.5
+    warmup_sweeps: int = 200
+    total_steps: int = 50_000
+    sample_every: int = 100
+    seed: int = 42
+
+
+@dataclass
+class CoarseningPoint:
+    """src/coarsening.rs:52-56."""
+    step: int
+    rho: float
+
+
+def run_coarsening_gpu(config: CoarseningConfig) -> list:
+    """src/cuda/coarsening_gpu.rs:6-31 through isg_coarsening (cubic lattice)."""
+    pts = (int(config.total_steps) - 1) // int(config.sample_every) + 1 \
+        if config.total_steps > 0 and config.sample_every > 0 else 0
+    st = np.zeros(max(pts, 1), np.int64)
+    rho = np.zeros(max(pts, 1), np.float64)
+    n = C.c_int64()
+    _check(lib().isg_coarsening(int(config.n), float(config.j), float(config.t_high),
+                                float(config.t_quench), int(config.warmup_sweeps),
+                                int(config.total_steps), int(config.sample_every), int(config.seed),
+                                _ptr(st), _ptr(rho), pts, C.byref(n)))
+    return [CoarseningPoint(int(a), float(b)) for a, b in zip(st[:n.value], rho[:n.value])]
+
+
 def _stream_handle(stream) -> int | None:
     if stream is None:
         return None
@@ -326,6 +408,33 @@ class IsingBatch:
         k = n.value
         return t[:k], b[:k], m[:k]
 
+    def run_schedule(self, temps=None, n_sweeps: int | None = None, measure_every: int = 0,
+                     measure_phase: int = 0):
+        """Sweep k at temps[k] for every lattice (temps None: current temperatures,
+        n_sweeps sweeps); returns (bond, mag) records of shape (rows, n_total) for the
+        sweeps with k % measure_every == measure_phase."""
+        if temps is not None:
+            t = np.ascontiguousarray(temps, np.float64)
+            n_sweeps = len(t) if n_sweeps is None else int(n_sweeps)
+            if len(t) < n_sweeps:
+                raise IsingError(-1, "need one temperature per sweep")
+            tp = _ptr(t)
+        else:
+            tp = None
+        n_sweeps = int(n_sweeps or 0)
+        rows = 0
+        if measure_every > 0 and n_sweeps > measure_phase:
+            rows = (n_sweeps - 1 - measure_phase) // measure_every + 1
+        b = np.zeros((max(rows, 1), self.n_total), np.int64)
+        m = np.zeros((max(rows, 1), self.n_total), np.int64)
+        n = C.c_int64()
+        _check(lib().isg_ising_run_schedule(self._h, tp, n_sweeps, int(measure_every),
+                                            int(measure_phase), _ptr(b), _ptr(m), rows,
+                                            C.byref(n)))
+        if temps is not None:
+            self.temps = np.full((len(self.sizes), self.replicas), float(t[n_sweeps - 1]))
+        return b[:n.value], m[:n.value]
+
     def pt_launch(self, n_sweeps: int, exchange_every: int, measure_every: int) -> None:
         """Asynchronous PT sweeps; records stay on the device (read_records)."""
         _check(lib().isg_ising_pt_run(self._h, int(n_sweeps), int(exchange_every),
@@ -425,8 +534,7 @@ class LatticeGpu:
         if self._key != ("T", T, float(j), float(h)):
             self._b.set_temperatures([T], J=float(j), h=float(h))
             self._key = ("T", T, float(j), float(h))
-        self._b.reset_sampling()
-        _, b, m = self._b.pt_run(int(samples), min(int(samples) + 1, 1 << 30), 1)
+        b, m = self._b.run_schedule(None, int(samples), 1, 0)
         return _observables(T, b[:, 0], m[:, 0], float(j), float(h), float(self.n) ** 3)
 
     def domain_wall_density(self) -> float:

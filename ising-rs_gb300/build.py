@@ -1,8 +1,9 @@
-"""Build recipe for libisinggb (sm_103a) and the gpu_fss / fss drop-in drivers.
+"""Build recipe for libisinggb (sm_103a) and the drop-in drivers (gpu_fss, fss, kz,
+coarsening).
 
 Compiles every translation unit in parallel with one -gencode
-(arch=compute_103a,code=sm_103a), links lib/libisinggb.so, bin/gpu_fss and bin/fss in
-the package directory.  Host code is compiled with -ffp-contract=off so the
+(arch=compute_103a,code=sm_103a), links lib/libisinggb.so and bin/<driver> in the package
+directory.  Host code is compiled with -ffp-contract=off so the
 FP64 threshold tables, exchange energies and jackknife sums round the same on
 x86_64 and aarch64.
 
@@ -31,8 +32,8 @@ NVCC_FLAGS = [
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 
 CU_SOURCES = ["isg_ising.cu", "isg_cont.cu", "isg_noalloc.cu", "isg_learned.cu"]
-CPP_SOURCES = ["isg_stats.cpp", "isg_anneal.cpp"]
-DRIVERS = ["gpu_fss", "fss"]   # host/<name>.cpp -> bin/<name>
+CPP_SOURCES = ["isg_stats.cpp", "isg_anneal.cpp", "isg_quench.cpp"]
+DRIVERS = ["gpu_fss", "fss", "kz", "coarsening"]   # host/<name>.cpp -> bin/<name>
 
 
 def _cuda_home() -> Path:

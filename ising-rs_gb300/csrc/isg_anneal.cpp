@@ -9,9 +9,10 @@
 //                                    and a host E/M sum (energy_magnetisation_host,
 //                                    lattice_gpu.rs:285-306)
 //
-// Here every size is one replica of a single batch, so each sweep of all sizes
-// is one half-sweep launch per colour, and E/M come from the integer sums the
-// half-sweep kernel fuses into the second colour (no spin copies).  The
+// Here every size is one replica of a single batch and each temperature's
+// warm-up and sampling sweeps are isg_ising_run_schedule calls: small lattices
+// run them in one launch (one thread-block cluster per lattice), and E/M come
+// from integer sums fused into the sweep (no spin copies).  The
 // per-temperature statistics follow lattice_gpu.rs:205-251 operation for
 // operation in FP64 (host code compiled with -ffp-contract=off):
 //   e = E/N, m = |M|/N, m_s = M/N; running sums of e, e^2, m, m^2,
@@ -50,25 +51,24 @@ int anneal_group(const std::vector<int>& sizes, int dim, double t_min, double t_
     if (rc) return isg::fail(rc, std::string("isg_ising_create: ") + isg_last_error());
     std::vector<double> temps(ns);
     const int64_t chunk = std::min<int64_t>(samples, (int64_t)1 << 16);
-    std::vector<int32_t> rt((size_t)chunk * ns);
     std::vector<int64_t> rb((size_t)chunk * ns), rm((size_t)chunk * ns);
     std::vector<double> nsites(ns);
     for (int s = 0; s < ns; ++s)
         nsites[s] = dim == 3 ? (double)sizes[s] * sizes[s] * sizes[s] : (double)sizes[s] * sizes[s];
-    // the exchange pass never fires inside one temperature's sampling run
-    const int ee = (int)std::min<int64_t>(samples + 1, 1 << 30);
     std::vector<Sums> acc(ns);
     for (int step = t_steps - 1; step >= 0 && rc == 0; --step) {
         const double t = t_min + (t_max - t_min) * (double)step / (double)(t_steps - 1);
         std::fill(temps.begin(), temps.end(), t);
         if ((rc = isg_ising_set_temperatures(h, temps.data(), J, hfield))) break;
-        if (warmup > 0 && (rc = isg_ising_step(h, warmup))) break;
-        if ((rc = isg_ising_reset_sampling(h))) break;
+        if (warmup > 0 &&
+            (rc = isg_ising_run_schedule(h, nullptr, warmup, 0, 0, nullptr, nullptr, 0, nullptr)))
+            break;
         std::fill(acc.begin(), acc.end(), Sums{});
         for (int64_t done = 0; done < samples && rc == 0;) {
             const int64_t n = std::min<int64_t>(chunk, samples - done);
             int64_t got = 0;
-            if ((rc = isg_ising_pt_run(h, n, ee, 1, rt.data(), rb.data(), rm.data(), chunk, &got)))
+            if ((rc = isg_ising_run_schedule(h, nullptr, n, 1, 0, rb.data(), rm.data(), chunk,
+                                             &got)))
                 break;
             if (got != n) {
                 rc = isg::fail(ISG_ERR_STATE, "isg_fss_anneal: short record set");

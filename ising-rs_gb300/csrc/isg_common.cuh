@@ -69,6 +69,25 @@ __device__ __forceinline__ float uniform24(uint32_t w) {
     return (float)(w >> 8) * (1.0f / 16777216.0f);
 }
 
+// n / d for n < 2^31 and a fixed divisor 1 <= d < 2^31 by one multiply-high
+// (Hacker's Delight, round-up method): (umulhi(n, m) + n) >> s with
+// s = ceil(log2 d), m = floor(2^32 (2^s - d) / d) + 1.
+struct FastDiv {
+    uint32_t d, m, s;
+};
+static inline FastDiv make_div(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    uint32_t l = 0;
+    while ((1ull << l) < d) ++l;
+    f.s = l;
+    f.m = (uint32_t)((((1ull << l) - d) << 32) / d + 1);
+    return f;
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+    return (__umulhi(n, f.m) + n) >> f.s;
+}
+
 // ---------------------------------------------------------------- errors
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);

@@ -38,23 +38,6 @@ constexpr int kCThreads = 256;
 constexpr int kMeasureChunk = 1024;  // colour-1 sites per measure block
 constexpr int kNQ = 10;              // E, Mx, My, Mz, Cx, Cy, Cz, Sx, Sy, Sz
 
-// n / d for n < 2^31 by multiply-high (Hacker's Delight, round-up method).
-struct FastDiv {
-    uint32_t d, m, s;
-};
-static FastDiv make_div(uint32_t d) {
-    FastDiv f;
-    f.d = d;
-    uint32_t l = 0;
-    while ((1ull << l) < d) ++l;
-    f.s = l;
-    f.m = (uint32_t)((((1ull << l) - d) << 32) / d + 1);
-    return f;
-}
-__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
-    return (__umulhi(n, f.m) + n) >> f.s;
-}
-
 struct ContClass {
     int L;
     int R;

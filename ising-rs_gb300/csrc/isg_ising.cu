@@ -483,6 +483,76 @@ __global__ void __launch_bounds__(256, 3)
     if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
 }
 
+template <bool CG>
+__device__ __forceinline__ int ld_spin(const uint8_t* p) {
+    if (CG) return (int)__ldcg(p);
+    return (int)*p;
+}
+
+// Metropolis update of the site at colour index i of one colour plane (any
+// even L): own / oth are the lattice's planes of this colour and the other,
+// tab its 16-entry threshold table.  Returns the site's down bit after the
+// update (before it when !update) and its down-neighbour count in nd_out.
+// CG loads the other colour through L2 only (planes written by other CTAs of
+// a cluster).
+template <int DIM, bool CG>
+__device__ __forceinline__ int site_update(uint8_t* own, const uint8_t* oth, uint32_t i, uint32_t L,
+                                           uint32_t plane, uint32_t colour, const uint32_t* tab,
+                                           uint32_t uid, uint32_t c2, uint32_t c3, uint32_t k0,
+                                           uint32_t k1, bool update, int& nd_out) {
+    const uint32_t half = L >> 1;
+    const uint32_t row = i / half;
+    const uint32_t k = i - row * half;
+    uint32_t y, z, p;
+    if (DIM == 3) {
+        y = row % L;
+        z = row / L;
+        p = (y + z + colour) & 1u;
+    } else {
+        y = row;
+        z = 0;
+        p = (y + colour) & 1u;
+    }
+    const uint32_t x = 2 * k + p;
+    const uint32_t xp = (x + 1) % L, xm = (x + L - 1) % L;
+    const uint32_t yp = (y + 1) % L, ym = (y + L - 1) % L;
+    const uint64_t rowL = (uint64_t)(z * L + y) * L;
+    int nd = ld_spin<CG>(oth + ((rowL + xp) >> 1)) + ld_spin<CG>(oth + ((rowL + xm) >> 1)) +
+             ld_spin<CG>(oth + (((uint64_t)(z * L + yp) * L + x) >> 1)) +
+             ld_spin<CG>(oth + (((uint64_t)(z * L + ym) * L + x) >> 1));
+    if (DIM == 3) {
+        const uint32_t zp = (z + 1) % L, zm = (z + L - 1) % L;
+        nd += ld_spin<CG>(oth + (((uint64_t)(zp * L + y) * L + x) >> 1)) +
+              ld_spin<CG>(oth + (((uint64_t)(zm * L + y) * L + x) >> 1));
+    }
+    nd_out = nd;
+    int d = own[i];
+    if (update) {
+        const uint32_t th = tab[d * 8 + nd];
+        // slab S = sites of this colour per z-plane (3D) or row (2D); the
+        // slab pair (t, t+1) shares Philox blocks: v = (t>>1)*S + (i mod S)
+        const uint32_t S = plane / L;
+        const uint32_t t = DIM == 3 ? z : y;
+        const uint32_t v = (t >> 1) * S + (i - t * S);
+        const U4 u = philox10(uid, v >> 2, c2, c3, k0, k1);
+        const uint32_t jv = v & 3u;
+        const uint32_t uw = jv == 0 ? u.x : jv == 1 ? u.y : jv == 2 ? u.z : u.w;
+        const uint32_t a16 = (t & 1u) ? (uw >> 16) : (uw & 0xFFFFu);
+        bool acc = a16 < (th >> 16);
+        if (a16 == (th >> 16)) {
+            const U4 f = philox10(uid, 0x80000000u | (i >> 2), c2, c3, k0, k1);
+            const uint32_t ji = i & 3u;
+            const uint32_t fw = ji == 0 ? f.x : ji == 1 ? f.y : ji == 2 ? f.z : f.w;
+            acc = ((a16 << 16) | (fw >> 16)) <= th;
+        }
+        if (acc) {
+            d ^= 1;
+            own[i] = (uint8_t)d;
+        }
+    }
+    return d;
+}
+
 template <int DIM, int MODE>
 __global__ void __launch_bounds__(kMaxThreads)
     k_ising_sites(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
@@ -499,70 +569,237 @@ __global__ void __launch_bounds__(kMaxThreads)
         const int64_t lg = g - C.site_base;
         const int r = (int)(lg / C.plane_sites);
         const uint32_t i = (uint32_t)(lg - (int64_t)r * C.plane_sites);
-        const int L = C.L;
-        const uint32_t half = (uint32_t)L >> 1;
-        const uint32_t row = i / half;
-        const uint32_t k = i - row * half;
-        uint32_t y, z, p;
-        if (DIM == 3) {
-            y = row % (uint32_t)L;
-            z = row / (uint32_t)L;
-            p = (y + z + (uint32_t)colour) & 1u;
-        } else {
-            y = row;
-            z = 0;
-            p = (y + (uint32_t)colour) & 1u;
-        }
-        const uint32_t x = 2 * k + p;
-        const uint32_t Lu = (uint32_t)L;
-        const uint32_t xp = (x + 1) % Lu, xm = (x + Lu - 1) % Lu;
-        const uint32_t yp = (y + 1) % Lu, ym = (y + Lu - 1) % Lu;
         uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
         uint8_t* own = base + (int64_t)colour * C.plane_sites;
         const uint8_t* oth = base + (int64_t)(colour ^ 1) * C.plane_sites;
-        const uint64_t rowL = (uint64_t)(z * Lu + y) * Lu;
-        int nd = oth[(rowL + xp) >> 1] + oth[(rowL + xm) >> 1] +
-                 oth[((uint64_t)(z * Lu + yp) * Lu + x) >> 1] +
-                 oth[((uint64_t)(z * Lu + ym) * Lu + x) >> 1];
-        if (DIM == 3) {
-            const uint32_t zp = (z + 1) % Lu, zm = (z + Lu - 1) % Lu;
-            nd += oth[((uint64_t)(zp * Lu + y) * Lu + x) >> 1] +
-                  oth[((uint64_t)(zm * Lu + y) * Lu + x) >> 1];
-        }
-        int d = own[i];
-        if (MODE != 2) {
-            const int rg = C.rep_base + r;
-            const int slot = C.rep_base + P.r2t[rg];
-            const uint32_t th = P.thr[slot * 16 + d * 8 + nd];
-            // slab S = sites of this colour per z-plane (3D) or row (2D); the
-            // slab pair (t, t+1) shares Philox blocks: v = (t>>1)*S + (i mod S)
-            const uint32_t S = C.plane_sites / Lu;
-            const uint32_t t = DIM == 3 ? z : y;
-            const uint32_t v = (t >> 1) * S + (i - t * S);
-            const U4 u = philox10(replica_uid(L, r), v >> 2, c2, c3, k0, k1);
-            const uint32_t jv = v & 3u;
-            const uint32_t uw = jv == 0 ? u.x : jv == 1 ? u.y : jv == 2 ? u.z : u.w;
-            const uint32_t a16 = (t & 1u) ? (uw >> 16) : (uw & 0xFFFFu);
-            bool acc = a16 < (th >> 16);
-            if (a16 == (th >> 16)) {
-                const U4 f = philox10(replica_uid(L, r), 0x80000000u | (i >> 2), c2, c3, k0, k1);
-                const uint32_t ji = i & 3u;
-                const uint32_t fw = ji == 0 ? f.x : ji == 1 ? f.y : ji == 2 ? f.z : f.w;
-                acc = ((a16 << 16) | (fw >> 16)) <= th;
-            }
-            if (acc) {
-                d ^= 1;
-                own[i] = (uint8_t)d;
-            }
-        }
+        const int rg = C.rep_base + r;
+        const uint32_t* tab = P.thr + (int64_t)(C.rep_base + (MODE != 2 ? P.r2t[rg] : 0)) * 16;
+        int nd;
+        const int d = site_update<DIM, false>(own, oth, i, (uint32_t)C.L, C.plane_sites,
+                                              (uint32_t)colour, tab, replica_uid(C.L, r), c2, c3,
+                                              k0, k1, MODE != 2, nd);
         if (MODE != 0) {
-            const int rg = C.rep_base + r;
             const int s = 1 - 2 * d;
             const long long b = (long long)(s * (2 * DIM - 2 * nd));
             const long long m = (long long)(s + 1 - 2 * oth[i]);
             atomicAdd(&P.acc[2 * rg], (unsigned long long)b);
             atomicAdd(&P.acc[2 * rg + 1], (unsigned long long)m);
         }
+    }
+}
+
+// Small lattices, whole schedules in one launch: one thread-block cluster per
+// lattice (lattice l = size l / R, replica l % R).  CTA c of the cluster keeps
+// colour indices [c*chunk, (c+1)*chunk) of both colour planes in its shared
+// memory for the whole launch; neighbours owned by other CTAs are read through
+// distributed shared memory (mapa + ld.shared::cluster), and hardware cluster
+// barriers (release / acquire at cluster scope) separate the half-sweeps.
+// Spins are loaded from HBM at the start and written back at the end.  Same
+// per-site update rule and random stream as the site kernel (site_update), so
+// any launch shape gives the same bits.
+constexpr int kResidentThreads = 1024;
+
+struct ResidentParams {
+    const uint32_t* tables;   // [n][16] threshold tables
+    const int32_t* sched;     // per-sweep table index, or null: the lattice's slot table
+    unsigned long long* rec;  // [rows][lattices][2] bond, mag (zeroed before the launch)
+    uint64_t sweep0;          // global sweep number of sweep 0
+    int64_t n_sweeps;
+    int measure_every;        // 0: no records
+    int measure_phase;        // record after sweep k iff k % every == phase
+    int lattices;
+    int cs;                   // CTAs per lattice (the cluster size)
+    int log2_chunk;           // colour indices per CTA and plane: 1 << log2_chunk
+    FastDiv div_half[kMaxClasses];  // L/2
+    FastDiv div_L[kMaxClasses];
+};
+
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;"
+                 ::: "memory");
+}
+__device__ __forceinline__ void cluster_arrive() {
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Byte j of colour plane `pl` of the cluster's lattice: owner CTA j >> lc.
+__device__ __forceinline__ int dsm_spin(uint32_t sbase, uint32_t pl, uint32_t j, int lc) {
+    const uint32_t local = sbase + (pl << lc) + (j & ((1u << lc) - 1u));
+    uint32_t remote, v;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(j >> lc));
+    asm volatile("ld.shared::cluster.u8 %0, [%1];" : "=r"(v) : "r"(remote) : "memory");
+    return (int)v;
+}
+
+// Neighbour colour indices, Philox block and word/half selector of the site at
+// colour index i (see site_update).
+template <int DIM>
+__device__ __forceinline__ void resident_geom(uint32_t i, uint32_t L, uint32_t half, uint32_t S,
+                                              const FastDiv& dh, const FastDiv& dL,
+                                              uint32_t colour, uint32_t (&nb)[6], uint32_t& c1,
+                                              uint32_t& sel) {
+    const uint32_t row = fdiv(i, dh);
+    const uint32_t k = i - row * half;
+    uint32_t y, z;
+    if (DIM == 3) {
+        z = fdiv(row, dL);
+        y = row - z * L;
+    } else {
+        y = row;
+        z = 0;
+    }
+    const uint32_t x = 2 * k + ((y + z + colour) & 1u);
+    const uint32_t xp = x + 1 == L ? 0 : x + 1, xm = x == 0 ? L - 1 : x - 1;
+    const uint32_t yp = y + 1 == L ? 0 : y + 1, ym = y == 0 ? L - 1 : y - 1;
+    const uint32_t rowL = (z * L + y) * L;
+    nb[0] = (rowL + xp) >> 1;
+    nb[1] = (rowL + xm) >> 1;
+    nb[2] = ((z * L + yp) * L + x) >> 1;
+    nb[3] = ((z * L + ym) * L + x) >> 1;
+    if (DIM == 3) {
+        const uint32_t zp = z + 1 == L ? 0 : z + 1, zm = z == 0 ? L - 1 : z - 1;
+        nb[4] = ((zp * L + y) * L + x) >> 1;
+        nb[5] = ((zm * L + y) * L + x) >> 1;
+    } else {
+        nb[4] = nb[5] = 0;
+    }
+    const uint32_t t = DIM == 3 ? z : y;
+    const uint32_t v = (t >> 1) * S + (i - t * S);
+    c1 = v >> 2;
+    sel = (v & 3u) | ((t & 1u) << 2);
+}
+
+template <int DIM>
+__device__ __forceinline__ int resident_nd(uint32_t sbase, uint32_t pl, int lc,
+                                           const uint32_t (&nb)[6]) {
+    int nd = dsm_spin(sbase, pl, nb[0], lc) + dsm_spin(sbase, pl, nb[1], lc) +
+             dsm_spin(sbase, pl, nb[2], lc) + dsm_spin(sbase, pl, nb[3], lc);
+    if (DIM == 3) nd += dsm_spin(sbase, pl, nb[4], lc) + dsm_spin(sbase, pl, nb[5], lc);
+    return nd;
+}
+
+// New down bit of a site with down bit d and nd down neighbours.
+__device__ __forceinline__ int resident_decide(uint32_t i, int d, int nd, const uint32_t* tab,
+                                               uint32_t uid, uint32_t c1, uint32_t sel,
+                                               uint32_t c2, uint32_t c3, uint32_t k0,
+                                               uint32_t k1) {
+    const uint32_t th = tab[d * 8 + nd];
+    const U4 u = philox10(uid, c1, c2, c3, k0, k1);
+    const uint32_t jv = sel & 3u;
+    const uint32_t uw = jv == 0 ? u.x : jv == 1 ? u.y : jv == 2 ? u.z : u.w;
+    const uint32_t a16 = (sel & 4u) ? (uw >> 16) : (uw & 0xFFFFu);
+    bool acc = a16 < (th >> 16);
+    if (a16 == (th >> 16)) {
+        const U4 f = philox10(uid, 0x80000000u | (i >> 2), c2, c3, k0, k1);
+        const uint32_t ji = i & 3u;
+        const uint32_t fw = ji == 0 ? f.x : ji == 1 ? f.y : ji == 2 ? f.z : f.w;
+        acc = ((a16 << 16) | (fw >> 16)) <= th;
+    }
+    return acc ? d ^ 1 : d;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kResidentThreads, 1)
+    k_ising_resident(const __grid_constant__ IsingParams P, const __grid_constant__ ResidentParams Q) {
+    extern __shared__ __align__(16) uint8_t s_spin[];  // [2][chunk]
+    __shared__ uint32_t s_tab[2][16];                  // tables of sweeps k and k+1
+    const int lid = blockIdx.x / Q.cs;
+    const int crank = blockIdx.x - lid * Q.cs;
+    const int R = P.cls[0].R;
+    const int s = lid / R, r = lid - s * R;
+    const IsingClass& C = P.cls[s];
+    const FastDiv dh = Q.div_half[s], dL = Q.div_L[s];
+    const uint32_t plane = C.plane_sites, L = (uint32_t)C.L, half = L >> 1;
+    const uint32_t S = plane / L;
+    const int lc = Q.log2_chunk;
+    const uint32_t chunk = 1u << lc;
+    const uint32_t i0 = min(plane, (uint32_t)crank << lc), i1 = min(plane, i0 + chunk);
+    uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * plane;
+    const uint32_t uid = replica_uid(C.L, r);
+    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    const int rg = C.rep_base + r;
+    const int lane = threadIdx.x & 31;
+    const uint32_t bd = blockDim.x;
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(s_spin);
+    for (uint32_t j = threadIdx.x; j < i1 - i0; j += bd) {
+        s_spin[j] = base[i0 + j];
+        s_spin[chunk + j] = base[plane + i0 + j];
+    }
+    // sweep k uses s_tab[k & 1]; the table of sweep k+1 is fetched during sweep k
+    if (threadIdx.x < 16) {
+        const int64_t t0 = Q.sched ? (int64_t)Q.sched[0] : (int64_t)(C.rep_base + P.r2t[rg]);
+        const uint32_t v = Q.tables[t0 * 16 + threadIdx.x];
+        s_tab[0][threadIdx.x] = v;
+        s_tab[1][threadIdx.x] = v;
+    }
+    cluster_sync_all();
+    for (int64_t k = 0; k < Q.n_sweeps; ++k) {
+        const uint32_t* tab = s_tab[k & 1];
+        uint32_t tnext = 0;
+        const bool fetch = Q.sched && threadIdx.x < 16 && k + 1 < Q.n_sweeps;
+        if (fetch) tnext = Q.tables[(int64_t)Q.sched[k + 1] * 16 + threadIdx.x];
+        const uint64_t sweep = Q.sweep0 + (uint64_t)k;
+        const bool meas = Q.measure_every > 0 && (k % Q.measure_every) == Q.measure_phase;
+#pragma unroll 1
+        for (uint32_t colour = 0; colour < 2; ++colour) {
+            const uint32_t c2 = (uint32_t)sweep;
+            const uint32_t c3 = counter_word3(ISG_TAG_ISING, colour, sweep);
+            uint8_t* own = s_spin + (colour << lc) - i0;  // own[i] for i in [i0, i1)
+            const uint32_t oc = colour ^ 1u;
+            const bool mc = colour == 1 && meas;
+            int bsum = 0, msum = 0;
+            // two sites per thread in flight: A = i, B = i + bd
+#pragma unroll 1
+            for (uint32_t i = i0 + threadIdx.x; i < i1; i += 2 * bd) {
+                const bool hasB = i + bd < i1;
+                const uint32_t iB = hasB ? i + bd : i;
+                uint32_t nbA[6], nbB[6], c1A, c1B, selA, selB;
+                resident_geom<DIM>(i, L, half, S, dh, dL, colour, nbA, c1A, selA);
+                resident_geom<DIM>(iB, L, half, S, dh, dL, colour, nbB, c1B, selB);
+                const int ndA = resident_nd<DIM>(sbase, oc, lc, nbA);
+                const int ndB = resident_nd<DIM>(sbase, oc, lc, nbB);
+                const int dA0 = own[i], dB0 = own[iB];
+                const int dA = resident_decide(i, dA0, ndA, tab, uid, c1A, selA, c2, c3, k0, k1);
+                if (dA != dA0) own[i] = (uint8_t)dA;
+                if (mc) {
+                    const int sp = 1 - 2 * dA;
+                    bsum += sp * (2 * DIM - 2 * ndA);
+                    msum += sp + 1 - 2 * (int)s_spin[(oc << lc) + (i - i0)];
+                }
+                if (hasB) {
+                    const int dB =
+                        resident_decide(iB, dB0, ndB, tab, uid, c1B, selB, c2, c3, k0, k1);
+                    if (dB != dB0) own[iB] = (uint8_t)dB;
+                    if (mc) {
+                        const int sp = 1 - 2 * dB;
+                        bsum += sp * (2 * DIM - 2 * ndB);
+                        msum += sp + 1 - 2 * (int)s_spin[(oc << lc) + (iB - i0)];
+                    }
+                }
+            }
+            if (colour == 1 && fetch) s_tab[(k + 1) & 1][threadIdx.x] = tnext;
+            if (mc) {
+                bsum = __reduce_add_sync(ISG_FULL_MASK, bsum);
+                msum = __reduce_add_sync(ISG_FULL_MASK, msum);
+            }
+            // the record atomics go out between arrive and wait: the release
+            // orders the shared-memory spins, the atomics overlap the barrier
+            cluster_arrive();
+            if (mc && lane == 0 && (bsum != 0 || msum != 0)) {
+                const int64_t row = k / Q.measure_every;
+                unsigned long long* rp = Q.rec + (row * Q.lattices + lid) * 2;
+                atomicAdd(rp, (unsigned long long)(long long)bsum);
+                atomicAdd(rp + 1, (unsigned long long)(long long)msum);
+            }
+            cluster_wait();
+        }
+    }
+    for (uint32_t j = threadIdx.x; j < i1 - i0; j += bd) {
+        base[i0 + j] = s_spin[j];
+        base[plane + i0 + j] = s_spin[chunk + j];
     }
 }
 
@@ -769,6 +1006,13 @@ struct isg_ising {
     int graph_ee = 0, graph_me = 0, graph_period = 0;
     // cached graph of kStepGraphSweeps plain sweeps (isg_ising_step)
     cudaGraphExec_t step_graph = nullptr;
+    // schedule buffers (isg_ising_run_schedule)
+    uint32_t* d_sched_tab = nullptr;
+    int64_t sched_tab_cap = 0;
+    int32_t* d_sched = nullptr;
+    int64_t sched_cap = 0;
+    unsigned long long* d_srec = nullptr;
+    int64_t srec_cap = 0;
 };
 
 namespace isg {
@@ -1110,6 +1354,9 @@ int isg_ising_destroy(isg_ising* H) {
     cudaFree(H->d_rec_t);
     cudaFree(H->d_rec_b);
     cudaFree(H->d_rec_m);
+    cudaFree(H->d_sched_tab);
+    cudaFree(H->d_sched);
+    cudaFree(H->d_srec);
     if (H->own_stream) cudaStreamDestroy(H->own_stream);
     delete H;
     return ISG_OK;
@@ -1123,6 +1370,34 @@ int isg_ising_set_stream(isg_ising* H, void* stream) {
     return ISG_OK;
 }
 
+}  // extern "C"
+
+namespace isg {
+// The 16-entry acceptance table of temperature T: entry own_down*8 + n_down.
+static void threshold_table(int dim, double T, double J, double hfield, uint32_t* thr) {
+    const double beta = 1.0 / T;
+    for (int e = 0; e < 16; ++e) thr[e] = 0u;
+    for (int od = 0; od < 2; ++od) {
+        const double sgn = od ? -1.0 : 1.0;
+        for (int nd = 0; nd <= 2 * dim; ++nd) {
+            const double nb = (double)(2 * dim - 2 * nd);
+            const double dE = 2.0 * sgn * (J * nb + hfield);
+            uint32_t t;
+            if (dE <= 0.0) {
+                t = 0xFFFFFFFFu;
+            } else {
+                double f = std::floor(std::exp(-beta * dE) * 4294967296.0);
+                if (f < 1.0) f = 1.0;
+                t = (uint32_t)(f - 1.0);
+            }
+            thr[od * 8 + nd] = t;
+        }
+    }
+}
+}  // namespace isg
+
+extern "C" {
+
 int isg_ising_set_temperatures(isg_ising* H, const double* temps, double J, double hfield) {
     if (!H || !temps) return fail(ISG_ERR_ARG, "isg_ising_set_temperatures: NULL argument");
     cudaSetDevice(H->device);
@@ -1132,24 +1407,8 @@ int isg_ising_set_temperatures(isg_ising* H, const double* temps, double J, doub
     for (int i = 0; i < RT; ++i) {
         if (!(temps[i] > 0.0) || !std::isfinite(temps[i]))
             return fail(ISG_ERR_ARG, "isg_ising_set_temperatures: temperatures must be positive");
-        const double beta = 1.0 / temps[i];
-        betas[i] = beta;
-        for (int od = 0; od < 2; ++od) {
-            const double sgn = od ? -1.0 : 1.0;
-            for (int nd = 0; nd <= 2 * H->dim; ++nd) {
-                const double nb = (double)(2 * H->dim - 2 * nd);
-                const double dE = 2.0 * sgn * (J * nb + hfield);
-                uint32_t t;
-                if (dE <= 0.0) {
-                    t = 0xFFFFFFFFu;
-                } else {
-                    double f = std::floor(std::exp(-beta * dE) * 4294967296.0);
-                    if (f < 1.0) f = 1.0;
-                    t = (uint32_t)(f - 1.0);
-                }
-                thr[(size_t)i * 16 + od * 8 + nd] = t;
-            }
-        }
+        betas[i] = 1.0 / temps[i];
+        threshold_table(H->dim, temps[i], J, hfield, &thr[(size_t)i * 16]);
     }
     std::vector<int32_t> ident(RT);
     for (int i = 0; i < RT; ++i) ident[i] = i % H->R;
@@ -1578,6 +1837,263 @@ int isg_ising_sites_per_halfsweep(isg_ising* H, int64_t* sites) {
     for (int s = 0; s < H->n_classes; ++s) n += (int64_t)H->P.cls[s].plane_sites * H->R;
     *sites = n;
     return ISG_OK;
+}
+
+// ------------------------------------------------------------ schedules
+
+}  // extern "C"
+
+namespace isg {
+
+// Lattices up to this many sites per colour plane run whole schedules in the
+// cluster-resident kernel; larger ones sweep with the half-sweep kernels.
+constexpr uint32_t kResidentMaxPlane = 1u << 16;
+
+static int grow(void** p, int64_t* cap, int64_t need_bytes) {
+    if (*cap >= need_bytes) return ISG_OK;
+    cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc(p, (size_t)need_bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    *cap = need_bytes;
+    return ISG_OK;
+}
+
+// Every slot's table (and exchange beta) set to temperature T.
+static int all_slots_to(isg_ising* H, double T) {
+    const int RT = H->replicas_total;
+    std::vector<uint32_t> thr(16 * (size_t)RT);
+    threshold_table(H->dim, T, H->J, H->h, thr.data());
+    for (int i = 1; i < RT; ++i) std::copy(thr.begin(), thr.begin() + 16, thr.begin() + 16 * i);
+    std::vector<double> betas(RT, 1.0 / T);
+    ISG_CK(cudaMemcpyAsync(H->d_thr, thr.data(), thr.size() * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, H->stream));
+    ISG_CK(cudaMemcpyAsync(H->d_betas, betas.data(), betas.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, H->stream));
+    return ISG_OK;
+}
+
+static int64_t count_rows(int64_t n, int every, int phase) {
+    if (every <= 0 || n <= phase) return 0;
+    return (n - 1 - phase) / every + 1;
+}
+
+static int copy_records(isg_ising* H, const unsigned long long* d_rec, int64_t rows,
+                        int64_t row0, int64_t* bond, int64_t* mag) {
+    const int RT = H->replicas_total;
+    std::vector<unsigned long long> buf((size_t)rows * RT * 2);
+    ISG_CK(cudaMemcpyAsync(buf.data(), d_rec, buf.size() * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    for (int64_t row = 0; row < rows; ++row)
+        for (int l = 0; l < RT; ++l) {
+            const size_t o = ((size_t)row * RT + l) * 2;
+            bond[(size_t)(row0 + row) * RT + l] = (int64_t)buf[o];
+            mag[(size_t)(row0 + row) * RT + l] = (int64_t)buf[o + 1];
+        }
+    return ISG_OK;
+}
+
+static int schedule_resident(isg_ising* H, const double* temps, int64_t n_sweeps, int every,
+                             int phase, int64_t* bond, int64_t* mag) {
+    const int RT = H->replicas_total;
+    uint32_t max_plane = 0;
+    for (int s = 0; s < H->n_classes; ++s) max_plane = std::max(max_plane, H->P.cls[s].plane_sites);
+    // about 256 sites per CTA and colour plane (power-of-two chunks), at most
+    // 16 CTAs per cluster (non-portable sizes above 8 where the GPU allows them)
+    const void* kfun = H->dim == 3 ? (const void*)k_ising_resident<3>
+                                   : (const void*)k_ising_resident<2>;
+    if (cudaFuncSetAttribute(kfun, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+        cudaSuccess)
+        cudaGetLastError();  // portable sizes only; the occupancy check below shrinks them
+    // distinct temperatures -> tables
+    std::vector<uint32_t> tabs;
+    std::vector<int32_t> idx;
+    if (temps) {
+        std::vector<std::pair<double, int32_t>> seen;
+        idx.resize((size_t)n_sweeps);
+        for (int64_t k = 0; k < n_sweeps; ++k) {
+            if (k > 0 && temps[k] == temps[k - 1]) {
+                idx[k] = idx[k - 1];
+                continue;
+            }
+            int32_t found = -1;
+            if (!seen.empty() && seen.back().first == temps[k]) found = seen.back().second;
+            if (found < 0) {
+                found = (int32_t)(tabs.size() / 16);
+                tabs.resize(tabs.size() + 16);
+                threshold_table(H->dim, temps[k], H->J, H->h, &tabs[tabs.size() - 16]);
+                seen.emplace_back(temps[k], found);
+            }
+            idx[k] = found;
+        }
+        int rc = grow((void**)&H->d_sched_tab, &H->sched_tab_cap,
+                      (int64_t)tabs.size() * (int64_t)sizeof(uint32_t));
+        if (rc) return rc;
+        rc = grow((void**)&H->d_sched, &H->sched_cap, n_sweeps * (int64_t)sizeof(int32_t));
+        if (rc) return rc;
+        ISG_CK(cudaMemcpyAsync(H->d_sched_tab, tabs.data(), tabs.size() * sizeof(uint32_t),
+                               cudaMemcpyHostToDevice, H->stream));
+        ISG_CK(cudaMemcpyAsync(H->d_sched, idx.data(), idx.size() * sizeof(int32_t),
+                               cudaMemcpyHostToDevice, H->stream));
+    }
+    // launches of whole multiples of `every` sweeps keep the record phase
+    const int64_t span = every > 0 ? std::max<int64_t>(every, ((int64_t)1 << 16) / every * every)
+                                   : ((int64_t)1 << 16);
+    const int64_t max_rows = count_rows(std::min(span, n_sweeps), every, phase);
+    if (max_rows > 0) {
+        int rc = grow((void**)&H->d_srec, &H->srec_cap,
+                      max_rows * RT * 2 * (int64_t)sizeof(unsigned long long));
+        if (rc) return rc;
+    }
+    int64_t row0 = 0;
+    for (int64_t k0 = 0; k0 < n_sweeps; k0 += span) {
+        const int64_t n = std::min(span, n_sweeps - k0);
+        const int64_t rows = count_rows(n, every, phase);
+        if (rows > 0)
+            ISG_CK(cudaMemsetAsync(H->d_srec, 0, rows * RT * 2 * sizeof(unsigned long long),
+                                   H->stream));
+        ResidentParams Q;
+        Q.tables = temps ? H->d_sched_tab : H->d_thr;
+        Q.sched = temps ? H->d_sched + k0 : nullptr;
+        Q.rec = H->d_srec;
+        Q.sweep0 = H->gsweep;
+        Q.n_sweeps = n;
+        Q.measure_every = rows > 0 ? every : 0;
+        Q.measure_phase = phase;
+        Q.lattices = RT;
+        for (int c = 0; c < kMaxClasses; ++c) {
+            const int L = H->P.cls[c < H->n_classes ? c : 0].L;
+            Q.div_half[c] = make_div((uint32_t)(L / 2));
+            Q.div_L[c] = make_div((uint32_t)L);
+        }
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        cfg.blockDim = dim3(kResidentThreads, 1, 1);
+        cfg.stream = H->stream;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        // largest cluster that fits a GPC: target 16, 8, 4, 2, 1 CTAs
+        bool placed = false;
+        for (int target = 16; target >= 1 && !placed; target /= 2) {
+            int lc = 0;
+            while ((1u << lc) * (uint32_t)target < max_plane) ++lc;
+            if (lc < 8 && target > 1) continue;  // fewer than 256 sites per CTA: smaller cluster
+            const int cs = (int)((max_plane + (1u << lc) - 1) >> lc);
+            const size_t smem = (size_t)2 << lc;
+            if (smem > 200 * 1024) break;
+            if (smem > 48 * 1024 &&
+                cudaFuncSetAttribute(kfun, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            Q.cs = cs;
+            Q.log2_chunk = lc;
+            cfg.gridDim = dim3((unsigned)(RT * cs), 1, 1);
+            cfg.dynamicSmemBytes = smem;
+            attr[0].val.clusterDim.x = (unsigned)cs;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            int active = 0;
+            cudaError_t oe = cudaOccupancyMaxActiveClusters(&active, kfun, &cfg);
+            if (oe != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            placed = active > 0;
+        }
+        if (!placed)
+            return fail(ISG_ERR_UNSUPPORTED, "isg_ising_run_schedule: no cluster shape fits");
+        cudaError_t e = H->dim == 3 ? cudaLaunchKernelEx(&cfg, k_ising_resident<3>, H->P, Q)
+                                    : cudaLaunchKernelEx(&cfg, k_ising_resident<2>, H->P, Q);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchKernelEx(k_ising_resident)");
+        launch_post(H, 0, 0, 0, 0, (int)n);  // device sweep counter
+        H->gsweep += (uint64_t)n;
+        int rc = check_launch("isg_ising_run_schedule");
+        if (rc) return rc;
+        if (rows > 0) {
+            rc = copy_records(H, H->d_srec, rows, row0, bond, mag);
+            if (rc) return rc;
+            row0 += rows;
+        }
+    }
+    return ISG_OK;
+}
+
+// Larger lattices: half-sweep kernels sweep by sweep, the measurement fused
+// into the second half-sweep of a recorded sweep.
+static int schedule_sweeps(isg_ising* H, const double* temps, int64_t n_sweeps, int every,
+                           int phase, int64_t* bond, int64_t* mag) {
+    const int RT = H->replicas_total;
+    int64_t row = 0;
+    for (int64_t k = 0; k < n_sweeps; ++k) {
+        if (temps && (k == 0 || temps[k] != temps[k - 1])) {
+            int rc = all_slots_to(H, temps[k]);
+            if (rc) return rc;
+        }
+        const bool meas = every > 0 && k % every == phase;
+        if (meas)
+            ISG_CK(cudaMemsetAsync(H->d_acc, 0, sizeof(unsigned long long) * 2 * RT, H->stream));
+        launch_half(H, 0, 0, 0);
+        launch_half(H, 1, 0, meas ? 1 : 0);
+        launch_post(H, 0, 0, 0, 0, 1);
+        H->gsweep += 1;
+        int rc = check_launch("isg_ising_run_schedule");
+        if (rc) return rc;
+        if (meas) {
+            rc = copy_records(H, H->d_acc, 1, row, bond, mag);
+            if (rc) return rc;
+            ++row;
+        }
+    }
+    return ISG_OK;
+}
+
+}  // namespace isg
+
+extern "C" {
+
+int isg_ising_run_schedule(isg_ising* H, const double* temps, int64_t n_sweeps, int measure_every,
+                           int measure_phase, int64_t* bond, int64_t* mag, int64_t max_rows,
+                           int64_t* n_rows) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_run_schedule: NULL handle");
+    if (!temps && !H->temps_set)
+        return fail(ISG_ERR_STATE, "isg_ising_run_schedule: temperatures not set");
+    if (n_sweeps < 0 || n_sweeps > ((int64_t)1 << 40) || measure_every < 0 ||
+        (measure_every > 0 && (measure_phase < 0 || measure_phase >= measure_every)))
+        return fail(ISG_ERR_ARG, "isg_ising_run_schedule: need n_sweeps >= 0, measure_every >= 0 "
+                                 "and 0 <= measure_phase < measure_every");
+    if (temps)
+        for (int64_t k = 0; k < n_sweeps; ++k)
+            if (!(temps[k] > 0.0) || !std::isfinite(temps[k]))
+                return fail(ISG_ERR_ARG, "isg_ising_run_schedule: temperatures must be positive");
+    const int64_t rows = count_rows(n_sweeps, measure_every, measure_phase);
+    if (rows > 0 && (!bond || !mag || max_rows < rows))
+        return fail(ISG_ERR_ARG, "isg_ising_run_schedule: record arrays hold " +
+                                     std::to_string(max_rows) + " rows, " + std::to_string(rows) +
+                                     " needed");
+    if (n_rows) *n_rows = 0;
+    if (n_sweeps == 0) return ISG_OK;
+    cudaSetDevice(H->device);
+    bool resident = true;
+    for (int s = 0; s < H->n_classes; ++s)
+        resident = resident && H->P.cls[s].plane_sites <= kResidentMaxPlane;
+    const int every = rows > 0 ? measure_every : 0;
+    int rc = ISG_OK;
+    // the resident kernel reads schedule tables, not the slot tables, so the
+    // slots take the final temperature up front (an upload after the launch
+    // would wait for it); the sweep-by-sweep path sets them as it goes
+    if (temps && resident) rc = all_slots_to(H, temps[n_sweeps - 1]);
+    if (rc) return rc;
+    rc = resident ? schedule_resident(H, temps, n_sweeps, every, measure_phase, bond, mag)
+                  : schedule_sweeps(H, temps, n_sweeps, every, measure_phase, bond, mag);
+    if (rc) return rc;
+    if (temps) H->temps_set = true;
+    if (n_rows) *n_rows = rows;
+    return check_launch("isg_ising_run_schedule");
 }
 
 }  // extern "C"

@@ -174,6 +174,21 @@ class IsingPT:
         self.xcount[:] = 0
         self.accepted[:] = 0
 
+    def schedule(self, temps, n: int, measure_every: int = 0, measure_phase: int = 0):
+        """isg_ising_run_schedule replayed: sweep k at temps[k] for every replica
+        (temps None: current temperatures), no exchange; (bond, mag) records of shape
+        (rows, R) after the sweeps with k % measure_every == measure_phase."""
+        b, m = [], []
+        for k in range(n):
+            if temps is not None:
+                self.temps[:] = temps[k]
+            self.warmup(1)
+            if measure_every > 0 and k % measure_every == measure_phase:
+                bm = [measure(self.replica_spins(r), self.L, self.dim) for r in range(self.R)]
+                b.append([x[0] for x in bm])
+                m.append([x[1] for x in bm])
+        return (np.array(b, np.int64).reshape(-1, self.R), np.array(m, np.int64).reshape(-1, self.R))
+
     def sample(self, n: int, exchange_every: int, measure_every: int):
         rows = n // measure_every + 2
         rt = np.zeros(rows * self.R, np.int32)
@@ -230,6 +245,55 @@ def fss_anneal(sizes, dim: int, t_min: float, t_max: float, t_steps: int, J: flo
             _, b, m = pt.sample(samples, samples + 1, 1)
             out[i, k] = measure_observables(T, b[:, 0], m[:, 0], J, h, n3)
     return out
+
+
+def wall_density(bond: int, L: int) -> float:
+    """domain_wall_density (src/cuda/lattice_gpu.rs:253-281) from the bond sum B of
+    the 3 L^3 forward bonds: walls = (3 L^3 - B) / 2."""
+    bonds = 3 * L ** 3
+    return ((bonds - int(bond)) // 2) / bonds
+
+
+def kz_sweep(n: int, J: float, t_start: float, t_end: float, taus, n_trials: int, warmup: int,
+             freeze: int, freeze_t: float, base_seed: int) -> np.ndarray:
+    """run_kz_sweep_gpu (src/cuda/kz_gpu.rs:46-95) replayed on the GPU stream
+    definition: per tau_q a batch of n_trials replicas keyed by base_seed + tau_q,
+    warm-up at t_start, the linear ramp of kibble_zurek.rs:78-84 floored at 0.01,
+    optional freeze; [len(taus), 2] = mean and standard error of rho."""
+    out = np.zeros((len(taus), 2))
+    for i, tau in enumerate(taus):
+        temps = [t_start] * warmup
+        temps += [max(t_start + (t_end - t_start) * (float(k + 1) / float(tau)), 0.01)
+                  for k in range(tau)]
+        temps += [max(freeze_t, 0.01)] * freeze
+        pt = IsingPT(n, 3, n_trials, [t_start] * n_trials, base_seed + tau, J, 0.0)
+        pt.schedule(temps, len(temps))
+        rho = [wall_density(measure(pt.replica_spins(r), n, 3)[0], n) for r in range(n_trials)]
+        # plain left-to-right sums (Rust's Iterator::sum); Python's sum() of floats
+        # is compensated and rounds differently
+        acc = 0.0
+        for x in rho:
+            acc += x
+        mean = acc / float(n_trials)
+        err = 0.0
+        if n_trials > 1:
+            ss = 0.0
+            for x in rho:
+                ss += (x - mean) * (x - mean)
+            var = ss / (float(n_trials) - 1.0)
+            err = float(np.sqrt(var)) / float(np.sqrt(float(n_trials)))
+        out[i] = (mean, err)
+    return out
+
+
+def coarsening(n: int, J: float, t_high: float, t_quench: float, warmup: int, steps: int,
+               every: int, seed: int):
+    """run_coarsening_gpu (src/cuda/coarsening_gpu.rs:6-31) replayed: (steps, rho)."""
+    pt = IsingPT(n, 3, 1, [t_high], seed, J, 0.0)
+    pt.warmup(warmup)
+    pt.temps[:] = max(t_quench, 0.01)
+    b, _ = pt.schedule(None, steps, every, 0)
+    return (np.arange(len(b)) * every, np.array([wall_density(x, n) for x in b[:, 0]]))
 
 
 def ref_run(L: int, dim: int, T: float, seed: int, warmup: int, samples: int, J=1.0, h=0.0):

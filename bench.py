@@ -573,6 +573,109 @@ def run_anneal(args):
     return 0
 
 
+KZ = dict(n=20, t_start=6.0, t_end=1.0, tau_min=100, tau_max=100000, tau_steps=20, trials=5,
+          warmup=200)
+COARSEN = dict(n=30, t_high=10.0, t_quench=0.5, warmup=200, steps=50000, every=100)
+
+
+def _quench_line(metric, workload, value, steps, warm, wall, h2d, d2h, cpu, sample, clocks):
+    return {"metric": metric, "value": value, "unit": "flips/ns", "n_gpus": 1, "steps": steps,
+            "warmup": warm, "ms_per_step": wall / steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int8",
+            "data": "synthetic (seeded Philox start)",
+            "config": {"workload": workload,
+                       "timing": "wall clock around the synchronous C-ABI call",
+                       "l2": "lattices (<= 27 KB each) stay on chip (distributed shared memory)"},
+            "e2e": {"value": value, "unit": "flips/ns", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "cpu_baseline": {"value": cpu, "unit": "flips/ns", "cores": host_threads(),
+                             "kind": "port", "sample": sample},
+            "clocks": clocks}
+
+
+def run_quench(args):
+    """`kz --gpu` and `coarsening --gpu` at the reference CLIs' defaults
+    (src/bin/kz.rs:63-75, src/coarsening.rs:36-50).  One step = the whole protocol
+    through isg_kz_sweep / isg_coarsening (host arrays in and out)."""
+    import ctypes as C
+    import torch
+    torch.cuda.set_device(0)
+    pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
+    oracle = _load("isg_oracle", ROOT / "oracle" / "oracle.py")
+    L = pkg.lib()
+    steps, warm = max(1, min(args.steps, 5)), max(1, min(args.warmup, 2))
+    threads = host_threads()
+    if args.workload == "kz":
+        k = KZ
+        lmin, lmax = math.log(k["tau_min"]), math.log(k["tau_max"])
+        taus = np.array([round(math.exp(lmin + (lmax - lmin) * i / (k["tau_steps"] - 1)))
+                         for i in range(k["tau_steps"])], np.int64)
+        out = np.zeros((len(taus), 2))
+
+        def once():
+            pkg._check(L.isg_kz_sweep(k["n"], 1.0, k["t_start"], k["t_end"],
+                                      taus.ctypes.data_as(C.c_void_p), len(taus), k["trials"],
+                                      k["warmup"], 0, 0.01, SEED, out.ctypes.data_as(C.c_void_p)))
+        updates = int((taus + k["warmup"]).sum()) * k["trials"] * k["n"] ** 3
+        workload = (f"kz --gpu: N={k['n']}, {k['tau_steps']} tau_q log-spaced in "
+                    f"[{k['tau_min']},{k['tau_max']}], {k['trials']} trials, warm-up "
+                    f"{k['warmup']}, ramp {k['t_start']} -> {k['t_end']}")
+        h2d = int((taus + k["warmup"]).sum()) * 4 + len(taus) * 64
+        d2h = len(taus) * k["trials"] * 16
+        metric = "spin flips/ns, Kibble-Zurek quench sweep (kz --gpu defaults)"
+        size = [k["n"]]
+    else:
+        k = COARSEN
+        pts = (k["steps"] - 1) // k["every"] + 1
+        st = np.zeros(pts, np.int64)
+        rho = np.zeros(pts)
+        npt = C.c_int64()
+
+        def once():
+            pkg._check(L.isg_coarsening(k["n"], 1.0, k["t_high"], k["t_quench"], k["warmup"],
+                                        k["steps"], k["every"], SEED,
+                                        st.ctypes.data_as(C.c_void_p),
+                                        rho.ctypes.data_as(C.c_void_p), pts, C.byref(npt)))
+        updates = (k["warmup"] + k["steps"]) * k["n"] ** 3
+        workload = (f"coarsening --gpu: N={k['n']}, warm-up {k['warmup']} at T={k['t_high']}, "
+                    f"{k['steps']} sweeps at T={k['t_quench']}, rho every {k['every']}")
+        h2d = 2 * (16 * 4 + 8)
+        d2h = pts * 16
+        metric = "spin flips/ns, coarsening after a quench (coarsening --gpu defaults)"
+        size = [k["n"]]
+    for _ in range(warm):
+        once()
+    clocks = ClockSampler(0)
+    with clocks:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            once()
+        wall = time.perf_counter() - t0
+    value = updates * steps / wall * 1e-9
+    rb = oracle.RefBench(size, 3, 3.5, 3.5 + 1e-9, threads, seed=SEED)
+    rb.step(0.5)
+    sec, flips = rb.step(200.0)
+    rb.close()
+    sample = (f"200 random-site sweeps of L={size[0]} per host thread at T=3.5 (reference CPU "
+              f"Metropolis path restated in C)")
+    line = _quench_line(metric, workload, value, steps, warm, wall, h2d, d2h,
+                        flips / sec * 1e-9, sample, clocks.summary())
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def ncu_case_resident():
+    """No timing: one schedule of 2000 sweeps of one L=30 lattice (the coarsening
+    default size) for an ncu capture of the cluster-resident kernel."""
+    pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
+    b = pkg.IsingBatch([30], 1, seed=SEED)
+    b.set_temperatures([0.5])
+    b.run_schedule(None, 2000)
+    b.sync()
+    print("ncu case done")
+    return 0
+
+
 def run_learned(args):
     import torch
     torch.cuda.set_device(0)
@@ -603,22 +706,28 @@ def main():
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--cpu-sweeps", type=float, default=1.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0)
-    ap.add_argument("--workload", default="ising", choices=["ising", "heisenberg", "xy", "anneal"])
+    ap.add_argument("--workload", default="ising",
+                    choices=["ising", "heisenberg", "xy", "anneal", "kz", "coarsening"])
     ap.add_argument("--learned", action="store_true",
                     help="config 5: learned proposal vs plain PT ESS/s (separate JSON lines)")
     ap.add_argument("--train-seconds", type=float, default=60.0)
     ap.add_argument("--chain-batches", type=int, default=40)
     ap.add_argument("--pt-sweeps", type=int, default=200000)
-    ap.add_argument("--ncu-case", action="store_true",
-                    help="no timing: a few half-sweeps of L=128 x 96 replicas (201 MB, larger "
-                         "than L2) for an ncu capture of the half-sweep kernel")
+    ap.add_argument("--ncu-case", nargs="?", const="words", choices=["words", "resident"],
+                    help="no timing: 'words' = a few half-sweeps of L=128 x 96 replicas (201 MB, "
+                         "larger than L2) for an ncu capture of the half-sweep kernel; "
+                         "'resident' = one 2000-sweep schedule of an L=30 lattice")
     args = ap.parse_args()
+    if args.ncu_case == "resident":
+        return ncu_case_resident()
     if args.ncu_case:
         return ncu_case()
     if args.learned:
         return run_learned(args)
     if args.workload == "anneal":
         return run_anneal(args)
+    if args.workload in ("kz", "coarsening"):
+        return run_quench(args)
     if args.workload != "ising":
         return run_continuous(args)
     if args.warmup < 3:

@@ -177,6 +177,15 @@ __device__ __forceinline__ uint32_t pin(uint32_t x) {
     return x;
 }
 
+__device__ __forceinline__ uint32_t lds_u8(uint32_t saddr) {
+    uint32_t v;
+    asm volatile("ld.shared.u8 %0, [%1];" : "=r"(v) : "r"(saddr) : "memory");
+    return v;
+}
+__device__ __forceinline__ void sts_u8(uint32_t saddr, uint32_t v) {
+    asm volatile("st.shared.u8 [%0], %1;" ::"r"(saddr), "r"(v) : "memory");
+}
+
 __device__ __forceinline__ uint32_t lds_u32(uint32_t saddr) {
     uint32_t v;
     asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(saddr));
@@ -672,6 +681,62 @@ __device__ __forceinline__ void resident_geom(uint32_t i, uint32_t L, uint32_t h
     sel = (v & 3u) | ((t & 1u) << 2);
 }
 
+__device__ __forceinline__ uint32_t dsm_map(uint32_t local, uint32_t rank) {
+    uint32_t remote;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(rank));
+    return remote;
+}
+__device__ __forceinline__ int dsm_ld(uint32_t remote) {
+    uint32_t v;
+    asm volatile("ld.shared::cluster.u8 %0, [%1];" : "=r"(v) : "r"(remote) : "memory");
+    return (int)v;
+}
+
+// Flip decision from the site's coarse block u (word/half selector sel) and, on
+// a tie with the threshold's upper half, the fine block of counter
+// 0x80000000 | (i >> 2) drawn with the same hoisted rounds.
+__device__ __forceinline__ bool resident_accept(const U4& u, uint32_t sel, uint32_t th,
+                                                uint32_t i, const PhiloxPre& pre,
+                                                const IsingParams& P) {
+    const uint32_t jv = sel & 3u;
+    const uint32_t uw = jv == 0 ? u.x : jv == 1 ? u.y : jv == 2 ? u.z : u.w;
+    const uint32_t a16 = (sel & 4u) ? (uw >> 16) : (uw & 0xFFFFu);
+    bool acc = a16 < (th >> 16);
+    if (a16 == (th >> 16)) {
+        const U4 f = philox_w(pre, P, 0x80000000u | (i >> 2));
+        const uint32_t ji = i & 3u;
+        const uint32_t fw = ji == 0 ? f.x : ji == 1 ? f.y : ji == 2 ? f.z : f.w;
+        acc = ((a16 << 16) | (fw >> 16)) <= th;
+    }
+    return acc;
+}
+
+// One half-sweep of the fast path: the thread's site (if any) of this colour,
+// with its neighbour addresses, Philox index and selector fixed for the launch.
+template <int DIM, int COLOUR>
+__device__ __forceinline__ void resident_fast_half(
+    const IsingParams& P, const uint32_t* tab, uint32_t uid, uint64_t sweep, bool has, uint32_t i,
+    const uint32_t (&na)[6], uint32_t own_addr, uint32_t oth_addr, uint32_t c1, uint32_t sel,
+    bool meas, int& bsum, int& msum) {
+    const uint32_t c3 = counter_word3(ISG_TAG_ISING, (uint32_t)COLOUR, sweep);
+    const PhiloxPre pre = philox_pre(uid, (uint32_t)sweep, c3, P.rk0[0], P.rk1[0]);
+    if (!has) return;
+    int nd = dsm_ld(na[0]) + dsm_ld(na[1]) + dsm_ld(na[2]) + dsm_ld(na[3]);
+    if (DIM == 3) nd += dsm_ld(na[4]) + dsm_ld(na[5]);
+    int d = (int)lds_u8(own_addr);
+    const uint32_t th = tab[d * 8 + nd];
+    const U4 u = philox_w(pre, P, c1);
+    if (resident_accept(u, sel, th, i, pre, P)) {
+        d ^= 1;
+        sts_u8(own_addr, (uint32_t)d);
+    }
+    if (COLOUR == 1 && meas) {
+        const int sp = 1 - 2 * d;
+        bsum += sp * (2 * DIM - 2 * nd);
+        msum += sp + 1 - 2 * (int)lds_u8(oth_addr);
+    }
+}
+
 template <int DIM>
 __device__ __forceinline__ int resident_nd(uint32_t sbase, uint32_t pl, int lc,
                                            const uint32_t (&nb)[6]) {
@@ -679,26 +744,6 @@ __device__ __forceinline__ int resident_nd(uint32_t sbase, uint32_t pl, int lc,
              dsm_spin(sbase, pl, nb[2], lc) + dsm_spin(sbase, pl, nb[3], lc);
     if (DIM == 3) nd += dsm_spin(sbase, pl, nb[4], lc) + dsm_spin(sbase, pl, nb[5], lc);
     return nd;
-}
-
-// New down bit of a site with down bit d and nd down neighbours.
-__device__ __forceinline__ int resident_decide(uint32_t i, int d, int nd, const uint32_t* tab,
-                                               uint32_t uid, uint32_t c1, uint32_t sel,
-                                               uint32_t c2, uint32_t c3, uint32_t k0,
-                                               uint32_t k1) {
-    const uint32_t th = tab[d * 8 + nd];
-    const U4 u = philox10(uid, c1, c2, c3, k0, k1);
-    const uint32_t jv = sel & 3u;
-    const uint32_t uw = jv == 0 ? u.x : jv == 1 ? u.y : jv == 2 ? u.z : u.w;
-    const uint32_t a16 = (sel & 4u) ? (uw >> 16) : (uw & 0xFFFFu);
-    bool acc = a16 < (th >> 16);
-    if (a16 == (th >> 16)) {
-        const U4 f = philox10(uid, 0x80000000u | (i >> 2), c2, c3, k0, k1);
-        const uint32_t ji = i & 3u;
-        const uint32_t fw = ji == 0 ? f.x : ji == 1 ? f.y : ji == 2 ? f.z : f.w;
-        acc = ((a16 << 16) | (fw >> 16)) <= th;
-    }
-    return acc ? d ^ 1 : d;
 }
 
 template <int DIM>
@@ -719,7 +764,6 @@ __global__ void __launch_bounds__(kResidentThreads, 1)
     const uint32_t i0 = min(plane, (uint32_t)crank << lc), i1 = min(plane, i0 + chunk);
     uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * plane;
     const uint32_t uid = replica_uid(C.L, r);
-    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
     const int rg = C.rep_base + r;
     const int lane = threadIdx.x & 31;
     const uint32_t bd = blockDim.x;
@@ -736,6 +780,53 @@ __global__ void __launch_bounds__(kResidentThreads, 1)
         s_tab[1][threadIdx.x] = v;
     }
     cluster_sync_all();
+    if (chunk <= bd) {
+        // at most one site per thread and colour: addresses fixed for the launch
+        const uint32_t i = i0 + threadIdx.x;
+        const bool has = i < i1;
+        constexpr int NB = 2 * DIM;
+        uint32_t na0[6] = {0, 0, 0, 0, 0, 0}, na1[6] = {0, 0, 0, 0, 0, 0};
+        uint32_t c10 = 0, c11 = 0, sel0 = 0, sel1 = 0;
+        if (has) {
+            uint32_t nb[6];
+            resident_geom<DIM>(i, L, half, S, dh, dL, 0u, nb, c10, sel0);
+#pragma unroll
+            for (int j = 0; j < NB; ++j)
+                na0[j] = dsm_map(sbase + chunk + (nb[j] & (chunk - 1u)), nb[j] >> lc);
+            resident_geom<DIM>(i, L, half, S, dh, dL, 1u, nb, c11, sel1);
+#pragma unroll
+            for (int j = 0; j < NB; ++j)
+                na1[j] = dsm_map(sbase + (nb[j] & (chunk - 1u)), nb[j] >> lc);
+        }
+        const uint32_t a0 = sbase + (i - i0), a1 = sbase + chunk + (i - i0);
+        for (int64_t k = 0; k < Q.n_sweeps; ++k) {
+            const uint32_t* tab = s_tab[k & 1];
+            uint32_t tnext = 0;
+            const bool fetch = Q.sched && threadIdx.x < 16 && k + 1 < Q.n_sweeps;
+            if (fetch) tnext = Q.tables[(int64_t)Q.sched[k + 1] * 16 + threadIdx.x];
+            const uint64_t sweep = Q.sweep0 + (uint64_t)k;
+            const bool meas = Q.measure_every > 0 && (k % Q.measure_every) == Q.measure_phase;
+            int bsum = 0, msum = 0;
+            resident_fast_half<DIM, 0>(P, tab, uid, sweep, has, i, na0, a0, a1, c10, sel0, meas,
+                                       bsum, msum);
+            cluster_sync_all();
+            resident_fast_half<DIM, 1>(P, tab, uid, sweep, has, i, na1, a1, a0, c11, sel1, meas,
+                                       bsum, msum);
+            if (fetch) s_tab[(k + 1) & 1][threadIdx.x] = tnext;
+            if (meas) {
+                bsum = __reduce_add_sync(ISG_FULL_MASK, bsum);
+                msum = __reduce_add_sync(ISG_FULL_MASK, msum);
+            }
+            cluster_arrive();
+            if (meas && lane == 0 && (bsum != 0 || msum != 0)) {
+                const int64_t row = k / Q.measure_every;
+                unsigned long long* rp = Q.rec + (row * Q.lattices + lid) * 2;
+                atomicAdd(rp, (unsigned long long)(long long)bsum);
+                atomicAdd(rp + 1, (unsigned long long)(long long)msum);
+            }
+            cluster_wait();
+        }
+    } else {
     for (int64_t k = 0; k < Q.n_sweeps; ++k) {
         const uint32_t* tab = s_tab[k & 1];
         uint32_t tnext = 0;
@@ -751,33 +842,23 @@ __global__ void __launch_bounds__(kResidentThreads, 1)
             const uint32_t oc = colour ^ 1u;
             const bool mc = colour == 1 && meas;
             int bsum = 0, msum = 0;
-            // two sites per thread in flight: A = i, B = i + bd
+            const PhiloxPre pre = philox_pre(uid, c2, c3, P.rk0[0], P.rk1[0]);
 #pragma unroll 1
-            for (uint32_t i = i0 + threadIdx.x; i < i1; i += 2 * bd) {
-                const bool hasB = i + bd < i1;
-                const uint32_t iB = hasB ? i + bd : i;
-                uint32_t nbA[6], nbB[6], c1A, c1B, selA, selB;
-                resident_geom<DIM>(i, L, half, S, dh, dL, colour, nbA, c1A, selA);
-                resident_geom<DIM>(iB, L, half, S, dh, dL, colour, nbB, c1B, selB);
-                const int ndA = resident_nd<DIM>(sbase, oc, lc, nbA);
-                const int ndB = resident_nd<DIM>(sbase, oc, lc, nbB);
-                const int dA0 = own[i], dB0 = own[iB];
-                const int dA = resident_decide(i, dA0, ndA, tab, uid, c1A, selA, c2, c3, k0, k1);
-                if (dA != dA0) own[i] = (uint8_t)dA;
-                if (mc) {
-                    const int sp = 1 - 2 * dA;
-                    bsum += sp * (2 * DIM - 2 * ndA);
-                    msum += sp + 1 - 2 * (int)s_spin[(oc << lc) + (i - i0)];
+            for (uint32_t i = i0 + threadIdx.x; i < i1; i += bd) {
+                uint32_t nb[6], c1, sel;
+                resident_geom<DIM>(i, L, half, S, dh, dL, colour, nb, c1, sel);
+                const int nd = resident_nd<DIM>(sbase, oc, lc, nb);
+                int d = own[i];
+                const uint32_t th = tab[d * 8 + nd];
+                const U4 u = philox_w(pre, P, c1);
+                if (resident_accept(u, sel, th, i, pre, P)) {
+                    d ^= 1;
+                    own[i] = (uint8_t)d;
                 }
-                if (hasB) {
-                    const int dB =
-                        resident_decide(iB, dB0, ndB, tab, uid, c1B, selB, c2, c3, k0, k1);
-                    if (dB != dB0) own[iB] = (uint8_t)dB;
-                    if (mc) {
-                        const int sp = 1 - 2 * dB;
-                        bsum += sp * (2 * DIM - 2 * ndB);
-                        msum += sp + 1 - 2 * (int)s_spin[(oc << lc) + (iB - i0)];
-                    }
+                if (mc) {
+                    const int sp = 1 - 2 * d;
+                    bsum += sp * (2 * DIM - 2 * nd);
+                    msum += sp + 1 - 2 * (int)s_spin[(oc << lc) + (i - i0)];
                 }
             }
             if (colour == 1 && fetch) s_tab[(k + 1) & 1][threadIdx.x] = tnext;
@@ -796,6 +877,7 @@ __global__ void __launch_bounds__(kResidentThreads, 1)
             }
             cluster_wait();
         }
+    }
     }
     for (uint32_t j = threadIdx.x; j < i1 - i0; j += bd) {
         base[i0 + j] = s_spin[j];

@@ -329,7 +329,7 @@ def run_gpu(args):
                                                  "(one CUDA graph)",
                    "sites_per_sweep": nsweep_sites, "l2": "flushed (256 MiB write) before "
                                                           "every timed step",
-                   "launch": "persistent word kernel, grid = SMs x occupancy"},
+                   "launch": "persistent word kernel, grid = SMs x occupancy; rolling loads two planes ahead (2 blocks/SM) because the batch fits in L2"},
         "sweeps_per_s": sweeps_per_s,
         "hbm_gbs_algorithmic": value * BYTES_PER_UPDATE,
         "ess_per_s": {"value": ess, "observable": "|M|", "L": 128, "T": T[slot],

@@ -193,8 +193,14 @@ int isg_ising_sync(isg_ising* h);
 /* Launch shape of the half-sweep kernel: threads per block and blocks per SM
  * (0 = occupancy maximum).  Results never depend on it. */
 int isg_ising_set_launch(isg_ising* h, int threads, int blocks_per_sm);
-/* Time every supported launch shape on a scratch copy of the lattices and
- * keep the fastest.  best[0..1] (may be NULL) receives threads, blocks/SM. */
+/* Prefetch depth of the rolling half-sweep (3D, L = 64..256): 1 = loads one
+ * plane ahead, 3 blocks per SM; 2 = two planes ahead, 2 blocks per SM;
+ * 0 = automatic (2 when all spin planes fit in 96 MiB, else 1).  Results never
+ * depend on it. */
+int isg_ising_set_prefetch(isg_ising* h, int depth);
+/* Time every supported launch shape (prefetch depth x site-kernel threads x
+ * blocks per SM) on a scratch copy of the lattices and keep the fastest.
+ * best[0..2] (may be NULL) receives threads, blocks/SM, prefetch depth. */
 int isg_ising_autotune(isg_ising* h, int* best);
 
 /* Mean device time (ms, CUDA events on the handle's stream) of one half-sweep

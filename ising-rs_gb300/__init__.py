@@ -93,6 +93,7 @@ def _declare(L):
         "isg_ising_sync": [vp],
         "isg_ising_set_launch": [vp, i32, i32],
         "isg_ising_autotune": [vp, vp],
+        "isg_ising_set_prefetch": [vp, i32],
         "isg_ising_time_halfsweep": [vp, i32, vp],
         "isg_ising_sites_per_halfsweep": [vp, vp],
         "isg_jackknife": [vp, vp, i64, dbl, dbl, i32, vp],
@@ -466,10 +467,15 @@ class IsingBatch:
     def set_launch(self, threads: int, blocks_per_sm: int = 0) -> None:
         _check(lib().isg_ising_set_launch(self._h, threads, blocks_per_sm))
 
-    def autotune(self) -> tuple[int, int]:
-        best = np.zeros(2, np.int32)
+    def set_prefetch(self, depth: int = 0) -> None:
+        """Rolling prefetch depth 1 or 2 (0 = automatic); results never depend on it."""
+        _check(lib().isg_ising_set_prefetch(self._h, int(depth)))
+
+    def autotune(self) -> tuple[int, int, int]:
+        """Fastest (site threads, blocks per SM, prefetch depth), kept for the batch."""
+        best = np.zeros(3, np.int32)
         _check(lib().isg_ising_autotune(self._h, _ptr(best)))
-        return int(best[0]), int(best[1])
+        return int(best[0]), int(best[1]), int(best[2])
 
     def time_halfsweep(self, n_launches: int = 20) -> float:
         v = C.c_float()

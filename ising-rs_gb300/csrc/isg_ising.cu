@@ -315,6 +315,51 @@ __device__ __forceinline__ void rolling_step(
     o = o1;
 }
 
+// The same step with the loads issued two planes ahead (own word and halo of
+// plane z+2, other colour at z+3): one more word of each kind in flight per lane.
+template <int MODE, bool HI>
+__device__ __forceinline__ void rolling_step2(
+    const IsingParams& P, const PhiloxPre& pre, uint32_t tbase, const U4& uc,
+    const uint32_t* oc, const uint32_t* oa, const uint32_t* ob, uint32_t* mc, uint32_t col,
+    uint32_t pz, uint32_t pwm, bool single, bool first, bool last, int src_up, int src_dn,
+    int src_prev, int src_next, uint32_t& o, uint32_t& p, uint32_t& zm, uint32_t& za,
+    uint32_t& zp, uint32_t& qzp, uint32_t& h0, uint32_t& qh0, uint32_t& h1, uint32_t& qh1,
+    uint32_t& ow, uint32_t& qow, MeasAcc& macc) {
+    const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm, o3 = (o + 3 * pz) & pwm;
+    const uint32_t n_zp = ldg_nc(oc + o3);
+    const uint32_t n_h0 = ldg_nc(oa + o2);
+    const uint32_t n_h1 = single ? ldg_nc(ob + o2) : 0u;
+    const uint32_t n_ow = ldg_u32(mc + o2);
+    const uint32_t up = __shfl_sync(ISG_FULL_MASK, za, src_up);
+    const uint32_t dn = __shfl_sync(ISG_FULL_MASK, za, src_dn);
+    const uint32_t prev = __shfl_sync(ISG_FULL_MASK, za, src_prev);
+    const uint32_t next = __shfl_sync(ISG_FULL_MASK, za, src_next);
+    const uint32_t wyp = single ? h1 : (last ? h0 : up);
+    const uint32_t wym = first ? h0 : dn;
+    const uint32_t wx = p ? __funnelshift_r(za, next, 8) : __funnelshift_l(prev, za, 8);
+    const uint32_t nd = (wx + za + wyp) + (wym + zp + zm);
+    uint32_t nw = ow;
+    if (MODE != 2) {
+        nw = HI ? metropolis_word(ow, nd, tbase, uc.x, uc.y, uc.z, uc.w, pre, P, o + col)
+                : metropolis_word(ow, nd, tbase, uc.x << 16, uc.y << 16, uc.z << 16,
+                                  uc.w << 16, pre, P, o + col);
+        mc[o] = nw;
+    }
+    if (MODE != 0) meas_add(macc, nw, nd, za);
+    zm = za;
+    za = zp;
+    zp = qzp;
+    qzp = n_zp;
+    h0 = qh0;
+    qh0 = n_h0;
+    h1 = qh1;
+    qh1 = n_h1;
+    ow = qow;
+    qow = n_ow;
+    p ^= 1u;
+    o = o1;
+}
+
 // MODE 0: update; 1: update then accumulate bond/mag of the new state;
 // 2: accumulate only (no update).
 //
@@ -324,8 +369,11 @@ __device__ __forceinline__ void rolling_step(
 // neighbours load at the same time (L1 hits); consecutive CTA tasks walk z, so
 // the z-1/z/z+1 words of the other colour stay in registers.  Flat sizes give
 // each warp one 32-word task per CTA task.
-template <int DIM, int MODE>
-__global__ void __launch_bounds__(256, 3)
+// PF: rolling loads issued PF planes ahead (1: 3 blocks per SM, 2: 2 blocks
+// per SM with more loads in flight per warp); chosen per batch (configure_launch,
+// isg_ising_autotune).
+template <int DIM, int MODE, int PF>
+__global__ void __launch_bounds__(256, PF == 1 ? 3 : 2)
     k_ising_words(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
     __shared__ __align__(256) uint32_t s_thr[8][64];
     const int lane = threadIdx.x & 31;
@@ -414,15 +462,34 @@ __global__ void __launch_bounds__(256, 3)
             uint32_t ow = ldg_u32(mc + o);
             // z pairs (2k, 2k+1) share one Philox block: counter (z>>1)*pz + col,
             // lower 16-bit halves for even z, upper for odd z
-            for (uint32_t z = z0; z < z1; z += 2) {
-                U4 uc{};
-                if (MODE != 2) uc = philox_w(pre, P, (o >> 1) + col);
-                rolling_step<MODE, false>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm, single,
-                                          first, last, src_up, src_dn, src_prev, src_next, o, p,
-                                          zm, za, zp, h0, h1, ow, macc);
-                rolling_step<MODE, true>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm, single,
-                                         first, last, src_up, src_dn, src_prev, src_next, o, p,
-                                         zm, za, zp, h0, h1, ow, macc);
+            if constexpr (PF == 1) {
+                for (uint32_t z = z0; z < z1; z += 2) {
+                    U4 uc{};
+                    if (MODE != 2) uc = philox_w(pre, P, (o >> 1) + col);
+                    rolling_step<MODE, false>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm,
+                                              single, first, last, src_up, src_dn, src_prev,
+                                              src_next, o, p, zm, za, zp, h0, h1, ow, macc);
+                    rolling_step<MODE, true>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm,
+                                             single, first, last, src_up, src_dn, src_prev,
+                                             src_next, o, p, zm, za, zp, h0, h1, ow, macc);
+                }
+            } else {
+                uint32_t qzp = ldg_nc(oc + ((o + 2 * pz) & pwm));
+                uint32_t qh0 = ldg_nc(oa + ((o + pz) & pwm));
+                uint32_t qh1 = single ? ldg_nc(ob + ((o + pz) & pwm)) : 0u;
+                uint32_t qow = ldg_u32(mc + ((o + pz) & pwm));
+                for (uint32_t z = z0; z < z1; z += 2) {
+                    U4 uc{};
+                    if (MODE != 2) uc = philox_w(pre, P, (o >> 1) + col);
+                    rolling_step2<MODE, false>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm,
+                                               single, first, last, src_up, src_dn, src_prev,
+                                               src_next, o, p, zm, za, zp, qzp, h0, qh0, h1,
+                                               qh1, ow, qow, macc);
+                    rolling_step2<MODE, true>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm,
+                                              single, first, last, src_up, src_dn, src_prev,
+                                              src_next, o, p, zm, za, zp, qzp, h0, qh0, h1, qh1,
+                                              ow, qow, macc);
+                }
             }
         } else {
             // flat: warp task 8*lct + wib of this size
@@ -1075,6 +1142,8 @@ struct isg_ising {
     double J = 1.0, h = 0.0;
     int threads = 256;
     int blocks_per_sm = 0;
+    int prefetch = 0;          // rolling prefetch depth as set (0: automatic)
+    int pf = 1;                // depth in use
     int word_grid = 0, site_grid = 0;
     int word_grids[3] = {1, 1, 1};
     int sms = 1;
@@ -1099,15 +1168,21 @@ struct isg_ising {
 
 namespace isg {
 
-static void (*word_kernel(int dim, int mode))(IsingParams, int, int) {
+static void (*word_kernel(int dim, int mode, int pf))(IsingParams, int, int) {
     if (dim == 3) {
-        if (mode == 0) return k_ising_words<3, 0>;
-        if (mode == 1) return k_ising_words<3, 1>;
-        return k_ising_words<3, 2>;
+        if (pf == 2) {
+            if (mode == 0) return k_ising_words<3, 0, 2>;
+            if (mode == 1) return k_ising_words<3, 1, 2>;
+            return k_ising_words<3, 2, 2>;
+        }
+        if (mode == 0) return k_ising_words<3, 0, 1>;
+        if (mode == 1) return k_ising_words<3, 1, 1>;
+        return k_ising_words<3, 2, 1>;
     }
-    if (mode == 0) return k_ising_words<2, 0>;
-    if (mode == 1) return k_ising_words<2, 1>;
-    return k_ising_words<2, 2>;
+    // no rolling tasks in 2D: one prefetch form
+    if (mode == 0) return k_ising_words<2, 0, 1>;
+    if (mode == 1) return k_ising_words<2, 1, 1>;
+    return k_ising_words<2, 2, 1>;
 }
 static void (*site_kernel(int dim, int mode))(IsingParams, int, int) {
     if (dim == 3) {
@@ -1122,14 +1197,19 @@ static void (*site_kernel(int dim, int mode))(IsingParams, int, int) {
 
 // Word kernels run 256-thread blocks (one CTA task = 8 warp tasks); the
 // grid is SMs x blocks per SM (occupancy maximum unless set), at most one
-// block per CTA task.  `threads` applies to the site kernel.
+// block per CTA task.  `threads` applies to the site kernel.  Prefetch depth:
+// as set, else 2 when the batch's spins fit in L2 (latency of L2 hits is
+// hidden better by loads further ahead) and 1 otherwise (three blocks per SM
+// keep more DRAM requests in flight) — measured on both kinds of workload.
 static int configure_launch(isg_ising* H) {
     const int thr = H->threads;
     const int64_t need = std::max<int64_t>(H->P.total_ctasks, H->P.flat_ctasks);
+    H->pf = H->prefetch > 0 ? H->prefetch : (H->spin_bytes <= ((int64_t)96 << 20) ? 2 : 1);
+    if (H->dim != 3) H->pf = 1;
     for (int mode = 0; mode < 3; ++mode) {
         int occ = 0;
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ, (const void*)word_kernel(H->dim, mode), 256, 0);
+            &occ, (const void*)word_kernel(H->dim, mode, H->pf), 256, 0);
         if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
         if (occ < 1) occ = 1;
         const int bps = H->blocks_per_sm > 0 ? std::min(H->blocks_per_sm, occ) : occ;
@@ -1144,7 +1224,7 @@ static int configure_launch(isg_ising* H) {
 
 static void launch_half(isg_ising* H, int colour, int sweep_off, int mode) {
     if (H->P.total_tasks > 0)
-        word_kernel(H->dim, mode)<<<H->word_grids[mode], 256, 0, H->stream>>>(H->P, colour,
+        word_kernel(H->dim, mode, H->pf)<<<H->word_grids[mode], 256, 0, H->stream>>>(H->P, colour,
                                                                              sweep_off);
     if (H->P.total_sites > 0)
         site_kernel(H->dim, mode)<<<H->site_grid, H->threads, 0, H->stream>>>(H->P, colour,
@@ -1880,6 +1960,16 @@ int isg_ising_time_halfsweep(isg_ising* H, int n_launches, float* avg_ms) {
     return timed_halfsweeps(H, n_launches, avg_ms);
 }
 
+int isg_ising_set_prefetch(isg_ising* H, int depth) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_set_prefetch: NULL handle");
+    if (depth < 0 || depth > 2) return fail(ISG_ERR_ARG, "isg_ising_set_prefetch: depth must be 0..2");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    H->prefetch = depth;
+    destroy_graph(H);
+    return configure_launch(H);
+}
+
 int isg_ising_autotune(isg_ising* H, int* best) {
     if (!H) return fail(ISG_ERR_ARG, "isg_ising_autotune: NULL handle");
     if (!H->temps_set) return fail(ISG_ERR_STATE, "isg_ising_autotune: temperatures not set");
@@ -1887,28 +1977,34 @@ int isg_ising_autotune(isg_ising* H, int* best) {
     const int thr_opts[] = {128, 256, 512};
     const int bps_opts[] = {1, 2, 4, 8, 16, 0};
     float best_ms = 1e30f;
-    int bt = H->threads, bb = H->blocks_per_sm;
-    for (int t : thr_opts)
-        for (int b : bps_opts) {
-            if (b > 0 && b * t > 2048) continue;
-            int rc = isg_ising_set_launch(H, t, b);
-            if (rc) return rc;
-            float ms = 0.f;
-            rc = timed_halfsweeps(H, 2, &ms);  // warm
-            if (rc) return rc;
-            rc = timed_halfsweeps(H, 8, &ms);
-            if (rc) return rc;
-            if (ms < best_ms) {
-                best_ms = ms;
-                bt = t;
-                bb = b;
+    int bt = H->threads, bb = H->blocks_per_sm, bp = H->prefetch;
+    const int npf = H->dim == 3 ? 2 : 1;
+    for (int pf = 1; pf <= npf; ++pf)
+        for (int t : thr_opts)
+            for (int b : bps_opts) {
+                if (b > 0 && b * t > 2048) continue;
+                H->prefetch = pf;
+                int rc = isg_ising_set_launch(H, t, b);
+                if (rc) return rc;
+                float ms = 0.f;
+                rc = timed_halfsweeps(H, 2, &ms);  // warm
+                if (rc) return rc;
+                rc = timed_halfsweeps(H, 8, &ms);
+                if (rc) return rc;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    bt = t;
+                    bb = b;
+                    bp = pf;
+                }
             }
-        }
+    H->prefetch = bp;
     int rc = isg_ising_set_launch(H, bt, bb);
     if (rc) return rc;
     if (best) {
         best[0] = bt;
         best[1] = bb;
+        best[2] = bp;
     }
     return ISG_OK;
 }

@@ -183,6 +183,22 @@ def test_production_size_properties(gpu, oracle):
         assert np.array_equal(d.get_spins(0, r), sp)
 
 
+def test_prefetch_depth_keeps_results(gpu):
+    """Both rolling prefetch depths give the same bits (L = 64 and 128 are rolling)."""
+    sizes, R = [64, 128], 2
+    out = []
+    for depth in (1, 2):
+        b = gpu.IsingBatch(sizes, R, seed=13)
+        b.set_prefetch(depth)
+        b.set_temperatures(grid(4.4, 4.6, R))
+        b.step(4)
+        _, bb, mm = b.pt_run(6, 3, 2)
+        out.append((bb, mm, [b.get_spins(s, r) for s in range(2) for r in range(R)]))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    for x, y in zip(out[0][2], out[1][2]):
+        assert np.array_equal(x, y)
+
+
 def test_autotune_keeps_results(gpu):
     sizes, R = [8, 32, 64], 16
     a = gpu.IsingBatch(sizes, R, seed=1)
@@ -190,7 +206,7 @@ def test_autotune_keeps_results(gpu):
     a.step(5)
     ref = [a.get_spins(2, r) for r in range(R)]
     best = a.autotune()
-    assert best[0] in (128, 256, 512)
+    assert best[0] in (128, 256, 512) and best[2] in (1, 2)
     for r in range(R):
         assert np.array_equal(a.get_spins(2, r), ref[r])
     assert a.sweep_counter() == 5

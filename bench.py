@@ -171,6 +171,26 @@ def tau_int(x) -> float:
     return float(tau)
 
 
+def max_over_ranks(value: float, device="cpu") -> float:
+    """The slowest rank's value (the job's timed region ends with the last rank);
+    the value itself on a single process."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_flips_per_ns(sites_per_sweep_per_rank: int, sweeps: int, world: int,
+                     max_ms: float) -> float:
+    """Whole-job throughput: every rank advances its own replicas (replicas only,
+    no data exchange), so the job does world x the per-rank work in the slowest
+    rank's time."""
+    return sites_per_sweep_per_rank * sweeps * world / (max_ms * 1e6)
+
+
 def dist_info():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -265,13 +285,8 @@ def run_gpu(args):
     if ws > 1:
         torch.distributed.barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    dev_ms = float(sum(step_ms))
-    if ws > 1:
-        t = torch.tensor([dev_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms = float(t.item())
-    flips = nsweep_sites * SWEEPS_PER_STEP * args.steps * ws
-    value = flips / (dev_ms * 1e6)
+    dev_ms = max_over_ranks(float(sum(step_ms)), dev)
+    value = job_flips_per_ns(nsweep_sites, SWEEPS_PER_STEP * args.steps, ws, dev_ms)
 
     # e2e: the C-ABI call with host record buffers, records copied back each step
     b2 = pkg.IsingBatch(SIZES, REPLICAS, seed=SEED + 1000 + rank)

@@ -52,7 +52,15 @@ struct ContClass {
     int64_t site_end;
     int chunk_base;
     int chunks_per_rep;
+    int nseg;           // z segments of kColZ planes per column
+    int64_t col_base;   // column tasks (replica, z segment, colour index in a z-plane)
+    int64_t col_end;
 };
+
+// Column tasks of the half-sweep kernels: a thread updates the sites of one
+// colour at colour index col of z-planes [zseg*kColZ, min(L, (zseg+1)*kColZ))
+// of one replica, walking z; a warp covers 32 consecutive col values.
+constexpr int kColZ = 8;
 
 struct ContParams {
     float* spins;
@@ -66,6 +74,7 @@ struct ContParams {
     int n_classes;
     int renorm;
     int64_t total_sites;
+    int64_t total_cols;
     int total_chunks;
     ContClass cls[kCMaxClasses];
 };
@@ -266,6 +275,211 @@ __global__ void __launch_bounds__(kCThreads)
         } else if (accepted) {
             atomicAdd(&P.metro_acc[rg], 1ull);
         }
+    }
+}
+
+// Position of a column task.
+struct ColRef {
+    int ci, r, rg;
+    uint32_t col, y, k, z0, z1, Pz;
+};
+__device__ __forceinline__ bool col_locate(const ContParams& P, int64_t t, ColRef& c) {
+    if (t >= P.total_cols) return false;
+    int ci = 0;
+    while (P.cls[ci].col_end <= t) ++ci;
+    const ContClass& C = P.cls[ci];
+    const uint32_t L = (uint32_t)C.L, half = L >> 1;
+    c.ci = ci;
+    c.Pz = L * half;  // colour sites per z-plane
+    const int64_t tl = t - C.col_base;
+    const int64_t rem = tl / c.Pz;
+    c.col = (uint32_t)(tl - rem * c.Pz);
+    const int zseg = (int)(rem % C.nseg);
+    c.r = (int)(rem / C.nseg);
+    c.rg = C.rep_base + c.r;
+    c.y = fdiv(c.col, C.div_half);
+    c.k = c.col - c.y * half;
+    c.z0 = (uint32_t)zseg * kColZ;
+    c.z1 = min(L, c.z0 + (uint32_t)kColZ);
+    return true;
+}
+
+// Neighbour field of the site at (colour index col, plane z) of colour
+// `colour`, summed in the order x+, x-, y+, y-, z+, z- as
+// ((x+ + x-) + (y+ + y-)) + (z+ + z-).  zc = other colour at (z, col) (one of
+// the two x-neighbours), zm = at (z-1, col); returns z+ = at (z+1, col) in zp.
+template <int NC>
+__device__ __forceinline__ void col_field(const float* oth, uint32_t plane, uint32_t zb,
+                                          uint32_t zpb, uint32_t col, uint32_t xo, uint32_t colp,
+                                          uint32_t colm, uint32_t p, const float (&zc)[NC],
+                                          const float (&zm)[NC], float (&zp)[NC], float (&h)[NC]) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        const float* o = oth + (size_t)k * plane;
+        const float xn = __ldg(o + zb + xo);
+        const float yp = __ldg(o + zb + colp);
+        const float ym = __ldg(o + zb + colm);
+        zp[k] = __ldg(o + zpb + col);
+        const float xp = p ? xn : zc[k], xm = p ? zc[k] : xn;
+        h[k] = ((xp + xm) + (yp + ym)) + (zp[k] + zm[k]);
+    }
+}
+
+// Overrelaxation half-sweep on column tasks (same update as or_store).
+template <int NC>
+__global__ void __launch_bounds__(kCThreads) k_cont_or_col(const __grid_constant__ ContParams P,
+                                                           int colour) {
+    ColRef c;
+    if (!col_locate(P, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, c)) return;
+    const ContClass& C = P.cls[c.ci];
+    const uint32_t L = (uint32_t)C.L, half = L >> 1, plane = C.plane_sites;
+    float* own = P.spins + plane_off<NC>(C, c.r, colour, 0);
+    const float* oth = P.spins + plane_off<NC>(C, c.r, colour ^ 1, 0);
+    const uint32_t row = c.y * half;
+    const uint32_t xo1 = row + (c.k + 1 == half ? 0 : c.k + 1);  // x+ when the site is odd
+    const uint32_t xo0 = row + (c.k == 0 ? half - 1 : c.k - 1);  // x- when the site is even
+    const uint32_t colp = (c.y + 1 == L ? 0 : c.y + 1) * half + c.k;
+    const uint32_t colm = (c.y == 0 ? L - 1 : c.y - 1) * half + c.k;
+    float zm[NC], zc[NC];
+    const uint32_t zmb = (c.z0 == 0 ? L - 1 : c.z0 - 1) * c.Pz;
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        zm[k] = __ldg(oth + (size_t)k * plane + zmb + c.col);
+        zc[k] = __ldg(oth + (size_t)k * plane + c.z0 * c.Pz + c.col);
+    }
+    for (uint32_t z = c.z0; z < c.z1; ++z) {
+        const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
+        const uint32_t zb = z * c.Pz, zpb = (z + 1 == L ? 0 : z + 1) * c.Pz;
+        float h[NC], zp[NC], v[NC];
+        col_field<NC>(oth, plane, zb, zpb, c.col, p ? xo1 : xo0, colp, colm, p, zc, zm, zp, h);
+        float h2 = 0.f, sh = 0.f;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            v[k] = own[(size_t)k * plane + zb + c.col];
+            h2 = fmaf(h[k], h[k], h2);
+            sh = fmaf(v[k], h[k], sh);
+        }
+        if (h2 >= 1e-20f) {
+            const float scale = 2.0f * sh / h2;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) own[(size_t)k * plane + zb + c.col] = fmaf(scale, h[k], -v[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            zm[k] = zc[k];
+            zc[k] = zp[k];
+        }
+    }
+}
+
+// Metropolis with the cone proposal on column tasks (same update, random
+// stream and renormalisation as k_cont_metro: Philox counter = colour index).
+template <int NC>
+__global__ void __launch_bounds__(kCThreads)
+    k_cont_metro_col(const __grid_constant__ ContParams P, int colour, int sweep_off,
+                     float cos_delta, float delta) {
+    const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
+    const bool renorm_now = P.renorm > 0 && ((sweep + 1) % (uint64_t)P.renorm) == 0;
+    const uint32_t c2 = (uint32_t)sweep;
+    const uint32_t c3 = counter_word3(ISG_TAG_CMETRO, (uint32_t)colour, sweep);
+    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    const int lane = threadIdx.x & 31;
+    ColRef c;
+    const bool live = col_locate(P, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, c);
+    unsigned n_acc = 0;
+    int rg = -1;
+    if (live) {
+        const ContClass& C = P.cls[c.ci];
+        rg = c.rg;
+        const uint32_t L = (uint32_t)C.L, half = L >> 1, plane = C.plane_sites;
+        float* own = P.spins + plane_off<NC>(C, c.r, colour, 0);
+        const float* oth = P.spins + plane_off<NC>(C, c.r, colour ^ 1, 0);
+        const uint32_t row = c.y * half;
+        const uint32_t xo1 = row + (c.k + 1 == half ? 0 : c.k + 1);
+        const uint32_t xo0 = row + (c.k == 0 ? half - 1 : c.k - 1);
+        const uint32_t colp = (c.y + 1 == L ? 0 : c.y + 1) * half + c.k;
+        const uint32_t colm = (c.y == 0 ? L - 1 : c.y - 1) * half + c.k;
+        const uint32_t uid = replica_uid(C.L, c.r);
+        const float beta = P.betaf[C.rep_base + P.r2t[c.rg]];
+        float zm[NC], zc[NC];
+        const uint32_t zmb = (c.z0 == 0 ? L - 1 : c.z0 - 1) * c.Pz;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            zm[k] = __ldg(oth + (size_t)k * plane + zmb + c.col);
+            zc[k] = __ldg(oth + (size_t)k * plane + c.z0 * c.Pz + c.col);
+        }
+        for (uint32_t z = c.z0; z < c.z1; ++z) {
+            const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
+            const uint32_t zb = z * c.Pz, zpb = (z + 1 == L ? 0 : z + 1) * c.Pz;
+            const uint32_t i = zb + c.col;
+            float h[NC], zp[NC], v[NC], w[NC];
+            col_field<NC>(oth, plane, zb, zpb, c.col, p ? xo1 : xo0, colp, colm, p, zc, zm, zp,
+                          h);
+#pragma unroll
+            for (int k = 0; k < NC; ++k) v[k] = own[(size_t)k * plane + i];
+            const U4 u = philox10(uid, i, c2, c3, k0, k1);
+            if (NC == 3) {
+                const float ct = 1.0f - uniform24(u.x) * (1.0f - cos_delta);
+                const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+                float sp, cp;
+                sincospif(2.0f * uniform24(u.y), &sp, &cp);
+                const float tx = fabsf(v[0]) < 0.9f ? 1.0f : 0.0f;
+                const float ty = 1.0f - tx;
+                const float ts = tx * v[0] + ty * v[1];
+                float ux = tx - ts * v[0], uy = ty - ts * v[1], uz = -ts * v[2];
+                const float un = rsqrtf(ux * ux + uy * uy + uz * uz);
+                ux *= un;
+                uy *= un;
+                uz *= un;
+                const float vx = v[1] * uz - v[2] * uy;
+                const float vy = v[2] * ux - v[0] * uz;
+                const float vz = v[0] * uy - v[1] * ux;
+                const float a = st * cp, b = st * sp;
+                w[0] = a * ux + b * vx + ct * v[0];
+                w[1] = a * uy + b * vy + ct * v[1];
+                w[2] = a * uz + b * vz + ct * v[2];
+                const float wn = rsqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) w[k] *= wn;
+            } else {
+                float sd, cd;
+                sincospif(delta * 0.318309886183790672f * (2.0f * uniform24(u.x) - 1.0f), &sd,
+                          &cd);
+                w[0] = v[0] * cd - v[1] * sd;
+                w[1] = v[1] * cd + v[0] * sd;
+            }
+            float dot = 0.f;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) dot = fmaf(w[k] - v[k], h[k], dot);
+            const float dE = -P.J * dot;
+            const bool accepted = dE <= 0.0f || uniform24(u.z) < expf(-beta * dE);
+            n_acc += accepted ? 1u : 0u;
+            if (accepted || renorm_now) {
+                float n2 = 0.f;
+#pragma unroll
+                for (int k = 0; k < NC; ++k) {
+                    if (accepted) v[k] = w[k];
+                    n2 = fmaf(v[k], v[k], n2);
+                }
+                const float sc = renorm_now ? rsqrtf(n2) : 1.0f;
+#pragma unroll
+                for (int k = 0; k < NC; ++k) own[(size_t)k * plane + i] = v[k] * sc;
+            }
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                zm[k] = zc[k];
+                zc[k] = zp[k];
+            }
+        }
+    }
+    // per-replica acceptance count: a warp covers one replica (32 | colour
+    // sites per z-plane), so one atomic per warp
+    const int rg0 = __shfl_sync(ISG_FULL_MASK, rg, 0);
+    const unsigned cnt = __reduce_add_sync(ISG_FULL_MASK, n_acc);
+    if (__all_sync(ISG_FULL_MASK, rg == rg0 || rg < 0)) {
+        if (lane == 0 && rg0 >= 0 && cnt) atomicAdd(&P.metro_acc[rg0], (unsigned long long)cnt);
+    } else if (rg >= 0 && n_acc) {
+        atomicAdd(&P.metro_acc[rg], (unsigned long long)n_acc);
     }
 }
 
@@ -555,20 +769,22 @@ static void cont_destroy_graph(isg_cont* H) {
 }
 
 static void launch_or(isg_cont* H, int colour) {
+    const unsigned grid = (unsigned)((H->P.total_cols + kCThreads - 1) / kCThreads);
     if (H->nc == 3)
-        k_cont_or<3><<<H->grid, kCThreads, 0, H->stream>>>(H->P, colour);
+        k_cont_or_col<3><<<grid, kCThreads, 0, H->stream>>>(H->P, colour);
     else
-        k_cont_or<2><<<H->grid, kCThreads, 0, H->stream>>>(H->P, colour);
+        k_cont_or_col<2><<<grid, kCThreads, 0, H->stream>>>(H->P, colour);
 }
 
 static void launch_metro(isg_cont* H, int colour, int sweep_off, double delta) {
     const float cd = (float)std::cos(std::min(delta, M_PI));
+    const unsigned grid = (unsigned)((H->P.total_cols + kCThreads - 1) / kCThreads);
     if (H->nc == 3)
-        k_cont_metro<3><<<H->grid, kCThreads, 0, H->stream>>>(H->P, colour, sweep_off, cd,
-                                                              (float)delta);
+        k_cont_metro_col<3><<<grid, kCThreads, 0, H->stream>>>(H->P, colour, sweep_off, cd,
+                                                               (float)delta);
     else
-        k_cont_metro<2><<<H->grid, kCThreads, 0, H->stream>>>(H->P, colour, sweep_off, cd,
-                                                              (float)delta);
+        k_cont_metro_col<2><<<grid, kCThreads, 0, H->stream>>>(H->P, colour, sweep_off, cd,
+                                                               (float)delta);
 }
 
 static void launch_measure(isg_cont* H) {
@@ -676,6 +892,7 @@ int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas,
     ContParams& P = H->P;
     int64_t off = 0, site = 0;
     int chunk = 0;
+    P.total_cols = 0;
     for (int s = 0; s < n_sizes; ++s) {
         ContClass& C = P.cls[s];
         const int L = sizes[s];
@@ -687,6 +904,10 @@ int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas,
         C.div_plane = make_div(C.plane_sites);
         C.small = (int64_t)C.plane_sites * replicas < (1ll << 31) ? 1 : 0;
         C.rep_base = s * replicas;
+        C.nseg = (L + kColZ - 1) / kColZ;
+        C.col_base = P.total_cols;
+        P.total_cols += (int64_t)replicas * C.nseg * ((int64_t)L * L / 2);
+        C.col_end = P.total_cols;
         C.off = off;
         off += ((2 * (int64_t)n_comp * C.plane_sites * replicas + 63) / 64) * 64;
         C.site_base = site;
@@ -699,6 +920,7 @@ int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas,
     for (int s = n_sizes; s < kCMaxClasses; ++s) {
         P.cls[s] = P.cls[n_sizes - 1];
         P.cls[s].site_base = P.cls[s].site_end = INT64_MAX;
+        P.cls[s].col_base = P.cls[s].col_end = INT64_MAX;
         P.cls[s].chunk_base = INT32_MAX;
         P.cls[s].rep_base = INT32_MAX;
     }

@@ -35,7 +35,6 @@ namespace isg {
 constexpr int kCMaxClasses = 16;
 constexpr int kCMaxReplicas = 1024;
 constexpr int kCThreads = 256;
-constexpr int kMeasureChunk = 1024;  // colour-1 sites per measure block
 constexpr int kNQ = 10;              // E, Mx, My, Mz, Cx, Cy, Cz, Sx, Sy, Sz
 
 struct ContClass {
@@ -499,9 +498,11 @@ __device__ __forceinline__ CF cf_merge(CF a, CF b) {
     return r;
 }
 
-// Per block: kMeasureChunk colour-1 sites of one replica.  Each colour-1 site
-// owns its six bonds (every bond has exactly one colour-1 end) and, for M, its
-// colour-0 partner at the same colour index.
+// Per block: kCThreads column tasks of one replica (chunks_per_rep blocks per
+// replica), each walking up to kColZ z-planes of colour-1 sites.  Each
+// colour-1 site owns its six bonds (every bond has exactly one colour-1 end)
+// and, for M, its colour-0 partner at the same colour index.  The summation
+// order is fixed by the task layout, so the result is deterministic.
 template <int NC>
 __global__ void __launch_bounds__(kCThreads) k_cont_measure(const __grid_constant__ ContParams P) {
     const int chunk = blockIdx.x;
@@ -510,47 +511,71 @@ __global__ void __launch_bounds__(kCThreads) k_cont_measure(const __grid_constan
     const ContClass& C = P.cls[ci];
     const int lc = chunk - C.chunk_base;
     const int r = lc / C.chunks_per_rep;
-    const uint32_t start = (uint32_t)(lc - r * C.chunks_per_rep) * kMeasureChunk;
-    const uint32_t L = (uint32_t)C.L;
+    const uint32_t L = (uint32_t)C.L, half = L >> 1, Pz = L * half, plane = C.plane_sites;
+    const uint32_t u = (uint32_t)(lc - r * C.chunks_per_rep) * kCThreads + threadIdx.x;
     CF acc[kNQ];
 #pragma unroll
     for (int q = 0; q < kNQ; ++q) acc[q] = CF{0.f, 0.f};
-    for (uint32_t i = start + threadIdx.x; i < min(start + kMeasureChunk, C.plane_sites);
-         i += blockDim.x) {
-        const uint32_t row = fdiv(i, C.div_half);
-        const uint32_t k = i - row * (L >> 1);
-        const uint32_t z = fdiv(row, C.div_L);
-        const uint32_t y = row - z * L;
-        const uint32_t x = 2 * k + ((y + z + 1u) & 1u);
-        uint32_t nb[6];
-        neighbours(L, x, y, z, nb);
-        float s[NC], n[6][NC];
+    if (u < (uint32_t)C.nseg * Pz) {
+        const uint32_t zseg = u / Pz, col = u - zseg * Pz;
+        const uint32_t y = fdiv(col, C.div_half), k = col - y * half;
+        const uint32_t z0 = zseg * kColZ, z1 = min(L, z0 + (uint32_t)kColZ);
+        const float* own = P.spins + plane_off<NC>(C, r, 1, 0);
+        const float* oth = P.spins + plane_off<NC>(C, r, 0, 0);
+        const uint32_t row = y * half;
+        const uint32_t xo1 = row + (k + 1 == half ? 0 : k + 1);
+        const uint32_t xo0 = row + (k == 0 ? half - 1 : k - 1);
+        const uint32_t colp = (y + 1 == L ? 0 : y + 1) * half + k;
+        const uint32_t colm = (y == 0 ? L - 1 : y - 1) * half + k;
+        float zm[NC], zc[NC];
+        const uint32_t zmb = (z0 == 0 ? L - 1 : z0 - 1) * Pz;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
-            const float* own = P.spins + plane_off<NC>(C, r, 1, c);
-            const float* oth = P.spins + plane_off<NC>(C, r, 0, c);
-            s[c] = own[i];
-#pragma unroll
-            for (int d = 0; d < 6; ++d) n[d][c] = oth[nb[d]];
-            acc[1 + c] = cf_add(acc[1 + c], s[c] + oth[i]);
+            zm[c] = __ldg(oth + (size_t)c * plane + zmb + col);
+            zc[c] = __ldg(oth + (size_t)c * plane + z0 * Pz + col);
         }
-        float e = 0.f;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            // forward bond (i, i+a) is neighbour 2a, backward bond (i-a, i) is 2a+1
-            float cf = 0.f, cb = 0.f;
+        for (uint32_t z = z0; z < z1; ++z) {
+            const uint32_t p = (y + z + 1u) & 1u;
+            const uint32_t zb = z * Pz, zpb = (z + 1 == L ? 0 : z + 1) * Pz;
+            const uint32_t xo = p ? xo1 : xo0;
+            float s[NC], n[6][NC], zp[NC];
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
-                cf = fmaf(s[c], n[2 * a][c], cf);
-                cb = fmaf(s[c], n[2 * a + 1][c], cb);
+                const float* o = oth + (size_t)c * plane;
+                const float xn = __ldg(o + zb + xo);
+                n[2][c] = __ldg(o + zb + colp);
+                n[3][c] = __ldg(o + zb + colm);
+                zp[c] = __ldg(o + zpb + col);
+                s[c] = __ldg(own + (size_t)c * plane + zb + col);
+                n[0][c] = p ? xn : zc[c];
+                n[1][c] = p ? zc[c] : xn;
+                n[4][c] = zp[c];
+                n[5][c] = zm[c];
+                acc[1 + c] = cf_add(acc[1 + c], s[c] + zc[c]);
             }
-            const float sf = s[0] * n[2 * a][1] - s[1] * n[2 * a][0];
-            const float sb = n[2 * a + 1][0] * s[1] - n[2 * a + 1][1] * s[0];
-            e += cf + cb;
-            acc[4 + a] = cf_add(acc[4 + a], cf + cb);
-            acc[7 + a] = cf_add(acc[7 + a], sf + sb);
+            float e = 0.f;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                // forward bond (i, i+a) is neighbour 2a, backward bond (i-a, i) is 2a+1
+                float cf = 0.f, cb = 0.f;
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    cf = fmaf(s[c], n[2 * a][c], cf);
+                    cb = fmaf(s[c], n[2 * a + 1][c], cb);
+                }
+                const float sf = s[0] * n[2 * a][1] - s[1] * n[2 * a][0];
+                const float sb = n[2 * a + 1][0] * s[1] - n[2 * a + 1][1] * s[0];
+                e += cf + cb;
+                acc[4 + a] = cf_add(acc[4 + a], cf + cb);
+                acc[7 + a] = cf_add(acc[7 + a], sf + sb);
+            }
+            acc[0] = cf_add(acc[0], -P.J * e);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                zm[c] = zc[c];
+                zc[c] = zp[c];
+            }
         }
-        acc[0] = cf_add(acc[0], -P.J * e);
     }
     // warp then block reduction of the compensated pairs
     __shared__ CF red[kCThreads / 32][kNQ];
@@ -913,7 +938,8 @@ int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas,
         C.site_base = site;
         site += (int64_t)C.plane_sites * replicas;
         C.site_end = site;
-        C.chunks_per_rep = (int)((C.plane_sites + kMeasureChunk - 1) / kMeasureChunk);
+        C.chunks_per_rep =
+            (int)(((int64_t)C.nseg * ((int64_t)L * L / 2) + kCThreads - 1) / kCThreads);
         C.chunk_base = chunk;
         chunk += C.chunks_per_rep * replicas;
     }

@@ -324,7 +324,8 @@ __device__ __forceinline__ void col_field(const float* oth, uint32_t plane, uint
     }
 }
 
-// Overrelaxation half-sweep on column tasks (same update as or_store).
+// Overrelaxation half-sweep on column tasks (same update as or_store).  The
+// next z-step's loads are issued before the current step's arithmetic.
 template <int NC>
 __global__ void __launch_bounds__(kCThreads) k_cont_or_col(const __grid_constant__ ContParams P,
                                                            int colour) {
@@ -341,20 +342,46 @@ __global__ void __launch_bounds__(kCThreads) k_cont_or_col(const __grid_constant
     const uint32_t colm = (c.y == 0 ? L - 1 : c.y - 1) * half + c.k;
     float zm[NC], zc[NC];
     const uint32_t zmb = (c.z0 == 0 ? L - 1 : c.z0 - 1) * c.Pz;
+    // loads of step z: x-neighbour (not at col), y+, y-, z+ (other colour), own
+    float lx[NC], lyp[NC], lym[NC], lzp[NC], lv[NC];
+    auto load_step = [&](uint32_t z) {
+        const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
+        const uint32_t zb = z * c.Pz, zpb = (z + 1 == L ? 0 : z + 1) * c.Pz;
+        const uint32_t xo = p ? xo1 : xo0;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            const float* o = oth + (size_t)k * plane;
+            lx[k] = __ldg(o + zb + xo);
+            lyp[k] = __ldg(o + zb + colp);
+            lym[k] = __ldg(o + zb + colm);
+            lzp[k] = __ldg(o + zpb + c.col);
+            lv[k] = own[(size_t)k * plane + zb + c.col];
+        }
+    };
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
         zm[k] = __ldg(oth + (size_t)k * plane + zmb + c.col);
         zc[k] = __ldg(oth + (size_t)k * plane + c.z0 * c.Pz + c.col);
     }
+    load_step(c.z0);
     for (uint32_t z = c.z0; z < c.z1; ++z) {
         const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
-        const uint32_t zb = z * c.Pz, zpb = (z + 1 == L ? 0 : z + 1) * c.Pz;
-        float h[NC], zp[NC], v[NC];
-        col_field<NC>(oth, plane, zb, zpb, c.col, p ? xo1 : xo0, colp, colm, p, zc, zm, zp, h);
-        float h2 = 0.f, sh = 0.f;
+        const uint32_t zb = z * c.Pz;
+        float xn[NC], yp[NC], ym[NC], zp[NC], v[NC];
 #pragma unroll
         for (int k = 0; k < NC; ++k) {
-            v[k] = own[(size_t)k * plane + zb + c.col];
+            xn[k] = lx[k];
+            yp[k] = lyp[k];
+            ym[k] = lym[k];
+            zp[k] = lzp[k];
+            v[k] = lv[k];
+        }
+        if (z + 1 < c.z1) load_step(z + 1);
+        float h[NC], h2 = 0.f, sh = 0.f;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            const float xp = p ? xn[k] : zc[k], xm = p ? zc[k] : xn[k];
+            h[k] = ((xp + xm) + (yp[k] + ym[k])) + (zp[k] + zm[k]);
             h2 = fmaf(h[k], h[k], h2);
             sh = fmaf(v[k], h[k], sh);
         }

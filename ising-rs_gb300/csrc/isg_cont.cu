@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(kCThreads) k_cont_or_col(const __grid_constant
 // Metropolis with the cone proposal on column tasks (same update, random
 // stream and renormalisation as k_cont_metro: Philox counter = colour index).
 template <int NC>
-__global__ void __launch_bounds__(kCThreads)
+__global__ void __launch_bounds__(kCThreads, 3)
     k_cont_metro_col(const __grid_constant__ ContParams P, int colour, int sweep_off,
                      float cos_delta, float delta) {
     const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
@@ -429,20 +429,42 @@ __global__ void __launch_bounds__(kCThreads)
         const float beta = P.betaf[C.rep_base + P.r2t[c.rg]];
         float zm[NC], zc[NC];
         const uint32_t zmb = (c.z0 == 0 ? L - 1 : c.z0 - 1) * c.Pz;
+        // loads of step z, issued one step ahead
+        float lx[NC], lyp[NC], lym[NC], lzp[NC], lv[NC];
+        auto load_step = [&](uint32_t z) {
+            const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
+            const uint32_t zb = z * c.Pz, zpb = (z + 1 == L ? 0 : z + 1) * c.Pz;
+            const uint32_t xo = p ? xo1 : xo0;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                const float* o = oth + (size_t)k * plane;
+                lx[k] = __ldg(o + zb + xo);
+                lyp[k] = __ldg(o + zb + colp);
+                lym[k] = __ldg(o + zb + colm);
+                lzp[k] = __ldg(o + zpb + c.col);
+                lv[k] = own[(size_t)k * plane + zb + c.col];
+            }
+        };
 #pragma unroll
         for (int k = 0; k < NC; ++k) {
             zm[k] = __ldg(oth + (size_t)k * plane + zmb + c.col);
             zc[k] = __ldg(oth + (size_t)k * plane + c.z0 * c.Pz + c.col);
         }
+        load_step(c.z0);
         for (uint32_t z = c.z0; z < c.z1; ++z) {
             const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
-            const uint32_t zb = z * c.Pz, zpb = (z + 1 == L ? 0 : z + 1) * c.Pz;
+            const uint32_t zb = z * c.Pz;
             const uint32_t i = zb + c.col;
             float h[NC], zp[NC], v[NC], w[NC];
-            col_field<NC>(oth, plane, zb, zpb, c.col, p ? xo1 : xo0, colp, colm, p, zc, zm, zp,
-                          h);
 #pragma unroll
-            for (int k = 0; k < NC; ++k) v[k] = own[(size_t)k * plane + i];
+            for (int k = 0; k < NC; ++k) {
+                const float xn = lx[k];
+                const float xp = p ? xn : zc[k], xm = p ? zc[k] : xn;
+                zp[k] = lzp[k];
+                h[k] = ((xp + xm) + (lyp[k] + lym[k])) + (zp[k] + zm[k]);
+                v[k] = lv[k];
+            }
+            if (z + 1 < c.z1) load_step(z + 1);
             const U4 u = philox10(uid, i, c2, c3, k0, k1);
             if (NC == 3) {
                 const float ct = 1.0f - uniform24(u.x) * (1.0f - cos_delta);

@@ -74,6 +74,12 @@ extern "C" {
 #define ISG_TAG_EXCH   0x03u
 #define ISG_TAG_CINIT  0x04u
 #define ISG_TAG_CMETRO 0x05u
+/* GRAPH: Ising on a graph (isg_graph_*).  c0 = replica, c1 = node / 4, word
+ *        (node & 3), step = global sweep, colour field = colour class of the
+ *        node (0xFE with step 0: hot start, spin -1 iff the top bit is set);
+ *        flip iff u <= threshold[own_down][degree][n_down_neighbours].
+ *        Exchanges use the EXCH tag with c0 = 0xFFFFFFFF. */
+#define ISG_TAG_GRAPH  0x07u
 
 const char* isg_last_error(void);
 int isg_version(void);
@@ -388,6 +394,40 @@ int isg_kz_sweep(int n, double J, double t_start, double t_end, const int64_t* t
 int isg_coarsening(int n, double J, double t_high, double t_quench, int64_t warmup_sweeps,
                    int64_t total_steps, int64_t sample_every, uint64_t seed, int64_t* steps_out,
                    double* rho_out, int64_t max_points, int64_t* n_points);
+
+/* ------------------------------------------------------------------------ */
+/* Ising parallel tempering on graphs (`gpu_jfit --model ising`)             */
+/* ------------------------------------------------------------------------ */
+typedef struct isg_graph isg_graph;
+
+/* Replaces the replica set of run_ising_jfit (src/bin/gpu_jfit.rs:172-213) on
+ * a graph given as an edge list (GraphDef, src/graph.rs:4-79): edges[2e],
+ * edges[2e+1] are the ends of edge e (no self-loops, degree at most 12,
+ * n_nodes <= 65536).  `replicas` copies start hot from the GRAPH stream.
+ * Sites are updated colour class by colour class of a greedy proper colouring
+ * (node order; isg_graph_num_colours), one CTA per replica. */
+int isg_graph_create(isg_graph** out, int n_nodes, const int32_t* edges, int n_edges,
+                     int replicas, uint64_t seed);
+int isg_graph_destroy(isg_graph* h);
+int isg_graph_num_colours(isg_graph* h, int* n_colours);
+/* Temperature of slot t (temps[t], `replicas` entries) and coupling J; resets
+ * the replica <-> temperature maps to the identity. */
+int isg_graph_set_temperatures(isg_graph* h, const double* temps, double J);
+/* Warm-up sweeps (no measurement, no exchange). */
+int isg_graph_step(isg_graph* h, int64_t n_sweeps);
+int isg_graph_reset_sampling(isg_graph* h);
+/* Sampling as isg_ising_pt_run: after sampling sweep k, records (slot, bond
+ * sum, magnetisation) per replica if (k+1) % measure_every == 0, and an
+ * exchange pass (src/parallel_tempering.rs:5-36, energies E = -J * bond of the
+ * last sweep, parity = exchange count % 2) if (k+1) % exchange_every == 0.
+ * Replaces the sampling loop of run_ising_jfit (gpu_jfit.rs:225-262).
+ * Synchronous. */
+int isg_graph_pt_run(isg_graph* h, int64_t n_sweeps, int exchange_every, int measure_every,
+                     int32_t* tslot_rec, int64_t* bond_rec, int64_t* mag_rec,
+                     int64_t max_records, int64_t* n_records);
+int isg_graph_get_accepted(isg_graph* h, int64_t* accepted);
+int isg_graph_get_spins(isg_graph* h, int replica, int8_t* out);
+int isg_graph_get_r2t(isg_graph* h, int32_t* r2t);
 
 /* ------------------------------------------------------------------------ */
 /* Statistics used by the drop-in driver                                     */

@@ -16,6 +16,9 @@ backend for the checkerboard PT path:
                         src/kibble_zurek.rs:11-76, src/cuda/kz_gpu.rs:46-95
   CoarseningConfig, CoarseningPoint, run_coarsening_gpu
                         src/coarsening.rs:14-56, src/cuda/coarsening_gpu.rs:6-31
+  GraphDef              src/graph.rs:4-79 (JSON / edge-CSV readers) with BCC,
+                        FCC and diluted-cubic builders
+  GraphBatch            Ising PT on a graph (src/bin/gpu_jfit.rs:172-297)
   IsingBatch / ContinuousBatch: every (size, replica) lattice of a run in one
   handle (the GB300 replacement of the reference's Vec<LatticeGpu>).
 
@@ -99,6 +102,16 @@ def _declare(L):
         "isg_jackknife": [vp, vp, i64, dbl, dbl, i32, vp],
         "isg_fss_anneal": [vp, i32, i32, dbl, dbl, i32, dbl, dbl, i64, i64, u64, vp],
         "isg_kz_sweep": [i32, dbl, dbl, dbl, vp, i32, i32, i64, i64, dbl, u64, vp],
+        "isg_graph_create": [C.POINTER(vp), i32, vp, i32, i32, u64],
+        "isg_graph_destroy": [vp],
+        "isg_graph_num_colours": [vp, vp],
+        "isg_graph_set_temperatures": [vp, vp, dbl],
+        "isg_graph_step": [vp, i64],
+        "isg_graph_reset_sampling": [vp],
+        "isg_graph_pt_run": [vp, i64, i32, i32, vp, vp, vp, i64, vp],
+        "isg_graph_get_accepted": [vp, vp],
+        "isg_graph_get_spins": [vp, i32, vp],
+        "isg_graph_get_r2t": [vp, vp],
         "isg_coarsening": [i32, dbl, dbl, dbl, i64, i64, i64, u64, vp, vp, i64, vp],
         "isg_cont_create": [C.POINTER(vp), vp, i32, i32, i32, u64],
         "isg_cont_destroy": [vp],
@@ -486,6 +499,204 @@ class IsingBatch:
         v = C.c_int64()
         _check(lib().isg_ising_sites_per_halfsweep(self._h, C.byref(v)))
         return v.value
+
+
+class GraphDef:
+    """Node count + edge list (src/graph.rs:4-79): `edges` is an (m, 2) int array.
+
+    from_json / from_edge_csv read the reference's two graph formats with its
+    error messages; bcc / fcc / diluted_cubic build the periodic crystal graphs
+    its J-fitting runs on (N^3 cells; two, four and one node per cell)."""
+
+    def __init__(self, n_nodes: int, edges):
+        self.n_nodes = int(n_nodes)
+        self.edges = np.asarray(edges, np.int64).reshape(-1, 2)
+
+    @staticmethod
+    def from_json(content: str) -> "GraphDef":
+        """{"n_nodes": N, "edges": [[a, b], ...]} (graph.rs:44-79)."""
+        import json
+
+        root = json.loads(content)
+
+        def u64(v):
+            return isinstance(v, int) and not isinstance(v, bool) and v >= 0
+
+        n = root.get("n_nodes") if isinstance(root, dict) else None
+        if not u64(n):
+            raise ValueError("missing n_nodes")
+        ev = root.get("edges")
+        if not isinstance(ev, list):
+            raise ValueError("missing edges")
+        edges = []
+        for e in ev:
+            if not isinstance(e, list):
+                raise ValueError("edge entry is not a 2-element array")
+            if len(e) != 2:
+                raise ValueError("edge entry must have exactly 2 indices")
+            if not (u64(e[0]) and u64(e[1])):
+                raise ValueError("edge index is not an integer")
+            edges.append((e[0], e[1]))
+        return GraphDef(n, np.array(edges, np.int64).reshape(-1, 2))
+
+    @staticmethod
+    def from_edge_csv(content: str) -> "GraphDef":
+        """Lines "i,j" ('#' comments and blank lines skipped); n_nodes = max
+        index + 1 (graph.rs:11-41)."""
+        edges, top = [], 0
+        for line in content.splitlines():
+            t = line.strip()
+            if not t or t.startswith("#"):
+                continue
+            parts = t.split(",")
+            if len(parts) < 2:
+                raise ValueError(f"bad edge line: {t}")
+            i, j = int(parts[0].strip()), int(parts[1].strip())
+            if i < 0 or j < 0:
+                raise ValueError(f"bad edge line: {t}")
+            top = max(top, i, j)
+            edges.append((i, j))
+        return GraphDef(top + 1, np.array(edges, np.int64).reshape(-1, 2))
+
+    def to_json(self) -> str:
+        pairs = ", ".join(f"[{int(a)}, {int(b)}]" for a, b in self.edges)
+        return f'{{"n_nodes": {self.n_nodes}, "edges": [{pairs}]}}'
+
+    def degrees(self) -> np.ndarray:
+        d = np.zeros(self.n_nodes, np.int64)
+        np.add.at(d, self.edges[:, 0], 1)
+        np.add.at(d, self.edges[:, 1], 1)
+        return d
+
+    @staticmethod
+    def bcc(n: int) -> "GraphDef":
+        """Body-centred cubic, n^3 cells (n >= 2): corner node (x,y,z) is
+        (x n + y) n + z, the centre of cell (x,y,z) is n^3 + that; each centre
+        bonds to the 8 corners of its cell (coordination 8, 4 n^3 bonds)."""
+        if n < 2:
+            raise ValueError("bcc needs n >= 2")
+        x, y, z = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+        cell = ((x * n + y) * n + z).reshape(-1)
+        out = []
+        for dx in (0, 1):
+            for dy in (0, 1):
+                for dz in (0, 1):
+                    corner = ((((x + dx) % n) * n + (y + dy) % n) * n + (z + dz) % n).reshape(-1)
+                    out.append(np.stack([corner, n ** 3 + cell], 1))
+        return GraphDef(2 * n ** 3, np.concatenate(out))
+
+    @staticmethod
+    def fcc(n: int) -> "GraphDef":
+        """Face-centred cubic, n^3 cells (n >= 2): the points (a,b,c) of a 2n
+        periodic grid with a+b+c even, numbered in (a,b,c) order, each bonded to
+        the 12 points at (+-1,+-1,0) and its permutations (12 n^3 bonds)."""
+        if n < 2:
+            raise ValueError("fcc needs n >= 2")
+        m = 2 * n
+        a, b, c = np.meshgrid(np.arange(m), np.arange(m), np.arange(m), indexing="ij")
+        keep = ((a + b + c) % 2 == 0).reshape(-1)
+        index = np.full(m ** 3, -1, np.int64)
+        index[keep] = np.arange(int(keep.sum()))
+        pa, pb, pc = a.reshape(-1)[keep], b.reshape(-1)[keep], c.reshape(-1)[keep]
+        me = index[((pa * m + pb) * m + pc)]
+        out = []
+        for da, db, dc in ((1, 1, 0), (1, -1, 0), (1, 0, 1), (1, 0, -1), (0, 1, 1), (0, 1, -1)):
+            nb = index[((((pa + da) % m) * m + (pb + db) % m) * m + (pc + dc) % m)]
+            out.append(np.stack([me, nb], 1))
+        return GraphDef(4 * n ** 3, np.concatenate(out))
+
+    @staticmethod
+    def diluted_cubic(n: int, p_remove: float, seed: int = 0) -> "GraphDef":
+        """Periodic simple cubic n^3 (n >= 3) with round(p_remove * 3 n^3) of its
+        3 n^3 bonds removed, chosen by a permutation from numpy's PCG64 stream
+        of `seed`; the kept bonds stay in lattice order."""
+        if n < 3:
+            raise ValueError("diluted_cubic needs n >= 3")
+        x, y, z = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+        me = ((x * n + y) * n + z).reshape(-1)
+        out = [np.stack([me, ((((x + 1) % n) * n + y) * n + z).reshape(-1)], 1),
+               np.stack([me, ((x * n + (y + 1) % n) * n + z).reshape(-1)], 1),
+               np.stack([me, ((x * n + y) * n + (z + 1) % n).reshape(-1)], 1)]
+        e = np.concatenate(out)
+        if not 0.0 <= p_remove <= 1.0:
+            raise ValueError("p_remove must be in [0, 1]")
+        drop = int(round(p_remove * len(e)))
+        keep = np.ones(len(e), bool)
+        keep[np.random.default_rng(seed).permutation(len(e))[:drop]] = False
+        return GraphDef(n ** 3, e[keep])
+
+
+class GraphBatch:
+    """`replicas` Ising replicas of one graph (node count + edge list, GraphDef of
+    src/graph.rs:4-79) with device replica exchange: the GB300 form of
+    run_ising_jfit (src/bin/gpu_jfit.rs:172-297).
+
+    Sites are updated colour class by colour class of a greedy proper colouring
+    in node order (num_colours()); at most 65536 nodes, degree 12 and 1024
+    replicas; self-loops are rejected."""
+
+    def __init__(self, n_nodes: int, edges, replicas: int, seed: int = 42):
+        e = np.ascontiguousarray(edges, np.int32).reshape(-1)
+        self.n, self.replicas = int(n_nodes), int(replicas)
+        h = C.c_void_p()
+        _check(lib().isg_graph_create(C.byref(h), self.n, _ptr(e) if len(e) else None,
+                                      len(e) // 2, self.replicas, int(seed)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().isg_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def num_colours(self) -> int:
+        v = C.c_int()
+        _check(lib().isg_graph_num_colours(self._h, C.byref(v)))
+        return v.value
+
+    def set_temperatures(self, temps, J: float = 1.0) -> None:
+        t = np.ascontiguousarray(temps, np.float64)
+        if len(t) != self.replicas:
+            raise IsingError(-1, "need one temperature per replica slot")
+        _check(lib().isg_graph_set_temperatures(self._h, _ptr(t), float(J)))
+
+    def step(self, n_sweeps: int = 1) -> None:
+        _check(lib().isg_graph_step(self._h, int(n_sweeps)))
+
+    def reset_sampling(self) -> None:
+        _check(lib().isg_graph_reset_sampling(self._h))
+
+    def pt_run(self, n_sweeps: int, exchange_every: int, measure_every: int = 1):
+        """(slot, bond, mag) records of shape (rows, replicas)."""
+        rows = n_sweeps // measure_every + 1
+        t = np.zeros((rows, self.replicas), np.int32)
+        b = np.zeros((rows, self.replicas), np.int64)
+        m = np.zeros((rows, self.replicas), np.int64)
+        n = C.c_int64()
+        _check(lib().isg_graph_pt_run(self._h, int(n_sweeps), int(exchange_every),
+                                      int(measure_every), _ptr(t), _ptr(b), _ptr(m), rows,
+                                      C.byref(n)))
+        return t[:n.value], b[:n.value], m[:n.value]
+
+    def accepted(self) -> int:
+        v = C.c_int64()
+        _check(lib().isg_graph_get_accepted(self._h, C.byref(v)))
+        return v.value
+
+    def get_spins(self, r: int) -> np.ndarray:
+        out = np.zeros(self.n, np.int8)
+        _check(lib().isg_graph_get_spins(self._h, int(r), _ptr(out)))
+        return out
+
+    def r2t(self) -> np.ndarray:
+        out = np.zeros(self.replicas, np.int32)
+        _check(lib().isg_graph_get_r2t(self._h, _ptr(out)))
+        return out
 
 
 class LatticeGpu:

@@ -1,5 +1,5 @@
 """Build recipe for libisinggb (sm_103a) and the drop-in drivers (gpu_fss, fss, kz,
-coarsening).
+coarsening, gpu_jfit).
 
 Compiles every translation unit in parallel with one -gencode
 (arch=compute_103a,code=sm_103a), links lib/libisinggb.so and bin/<driver> in the package
@@ -31,9 +31,9 @@ NVCC_FLAGS = [
 ]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 
-CU_SOURCES = ["isg_ising.cu", "isg_cont.cu", "isg_noalloc.cu", "isg_learned.cu"]
+CU_SOURCES = ["isg_ising.cu", "isg_cont.cu", "isg_noalloc.cu", "isg_learned.cu", "isg_graph.cu"]
 CPP_SOURCES = ["isg_stats.cpp", "isg_anneal.cpp", "isg_quench.cpp"]
-DRIVERS = ["gpu_fss", "fss", "kz", "coarsening"]   # host/<name>.cpp -> bin/<name>
+DRIVERS = ["gpu_fss", "fss", "kz", "coarsening", "gpu_jfit"]   # host/<name>.cpp -> bin/<name>
 
 
 def _cuda_home() -> Path:

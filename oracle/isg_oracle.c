@@ -651,3 +651,244 @@ void or_refbench_destroy(void* h) {
     for (int s = 0; s < b->n_sizes; ++s) free(b->nb[s]);
     free(b->spins); free(b->rng); free(b->beta); free(b);
 }
+
+/* ------------------------------------------------------------------ 7 */
+/* Ising on graphs: replay of isg_graph_* (stream tag GRAPH = 7) and the
+ * reference's CPU algorithm on a graph (src/bin/gpu_jfit.rs:172-297). */
+#define TAG_GRAPH 0x07u
+#define GMAXDEG 12
+#define GTAB (2 * (GMAXDEG + 1) * (GMAXDEG + 1))
+
+/* CSR adjacency in edge-list order (both directions) and the greedy proper
+ * colouring in node order (smallest class unused by coloured neighbours).
+ * rowptr[n+1], adj[2m], colour[n]; returns the number of classes, or -1 for
+ * a bad edge list or a degree above 12. */
+int or_graph_build(int n, const int32_t* edges, int m, int32_t* rowptr, int32_t* adj,
+                   int32_t* colour) {
+    for (int v = 0; v <= n; ++v) rowptr[v] = 0;
+    for (int e = 0; e < m; ++e) {
+        int a = edges[2 * e], b = edges[2 * e + 1];
+        if (a < 0 || b < 0 || a >= n || b >= n || a == b) return -1;
+        ++rowptr[a + 1];
+        ++rowptr[b + 1];
+    }
+    for (int v = 0; v < n; ++v) {
+        if (rowptr[v + 1] > GMAXDEG) return -1;
+        rowptr[v + 1] += rowptr[v];
+    }
+    int32_t* fill = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+    for (int v = 0; v < n; ++v) fill[v] = rowptr[v];
+    for (int e = 0; e < m; ++e) {
+        int a = edges[2 * e], b = edges[2 * e + 1];
+        adj[fill[a]++] = b;
+        adj[fill[b]++] = a;
+    }
+    free(fill);
+    int ncol = 0;
+    for (int v = 0; v < n; ++v) colour[v] = -1;
+    for (int v = 0; v < n; ++v) {
+        uint32_t used = 0;
+        for (int j = rowptr[v]; j < rowptr[v + 1]; ++j)
+            if (colour[adj[j]] >= 0) used |= 1u << colour[adj[j]];
+        int c = 0;
+        while ((used >> c) & 1u) ++c;
+        colour[v] = c;
+        if (c + 1 > ncol) ncol = c + 1;
+    }
+    return ncol;
+}
+
+/* threshold[(own_down*13 + degree)*13 + n_down] at temperature T. */
+void or_graph_thresholds(double T, double J, uint32_t tab[GTAB]) {
+    double beta = 1.0 / T;
+    for (int i = 0; i < GTAB; ++i) tab[i] = 0;
+    for (int od = 0; od < 2; ++od)
+        for (int dg = 0; dg <= GMAXDEG; ++dg)
+            for (int nd = 0; nd <= dg; ++nd) {
+                double dE = 2.0 * J * (od ? -1.0 : 1.0) * (double)(dg - 2 * nd);
+                uint32_t th;
+                if (dE <= 0.0) {
+                    th = 0xFFFFFFFFu;
+                } else {
+                    double f = floor(exp(-beta * dE) * 4294967296.0);
+                    if (f < 1.0) f = 1.0;
+                    th = (uint32_t)(f - 1.0);
+                }
+                tab[(od * (GMAXDEG + 1) + dg) * (GMAXDEG + 1) + nd] = th;
+            }
+}
+
+/* Hot start: down bit of node v of replica r = top bit of word (v & 3) of
+ * Philox(c0 = r, c1 = v >> 2, step 0, colour 0xFE). */
+void or_graph_hot_start(int n, int R, uint64_t seed, uint8_t* spins) {
+    uint32_t w[4];
+    for (int r = 0; r < R; ++r)
+        for (int v = 0; v < n; ++v) {
+            if ((v & 3) == 0) stream_words(seed, (uint32_t)v >> 2, (uint32_t)r, 0, TAG_GRAPH, 0xFEu, w);
+            spins[(size_t)r * n + v] = (uint8_t)(w[v & 3] >> 31);
+        }
+}
+
+/* One sweep of replica r (down bits sp[n]): colour classes in order, nodes of
+ * a class independent of each other. */
+void or_graph_sweep(int n, const int32_t* rowptr, const int32_t* adj, const int32_t* colour,
+                    int ncol, uint8_t* sp, uint32_t replica, uint64_t seed, uint64_t sweep,
+                    const uint32_t* tab) {
+    uint32_t w[4];
+    for (int c = 0; c < ncol; ++c)
+        for (int v = 0; v < n; ++v) {
+            if (colour[v] != c) continue;
+            int nd = 0;
+            for (int j = rowptr[v]; j < rowptr[v + 1]; ++j) nd += sp[adj[j]];
+            int d = sp[v];
+            int deg = rowptr[v + 1] - rowptr[v];
+            uint32_t th = tab[(d * (GMAXDEG + 1) + deg) * (GMAXDEG + 1) + nd];
+            stream_words(seed, (uint32_t)v >> 2, replica, sweep, TAG_GRAPH, (uint32_t)c, w);
+            if (w[v & 3] <= th) sp[v] = (uint8_t)(d ^ 1);
+        }
+}
+
+/* Bond sum over edges and magnetisation. */
+void or_graph_measure(int n, const int32_t* rowptr, const int32_t* adj, const uint8_t* sp,
+                      int64_t* bond, int64_t* mag) {
+    int64_t b = 0, m = 0;
+    for (int v = 0; v < n; ++v) {
+        int s = 1 - 2 * (int)sp[v];
+        for (int j = rowptr[v]; j < rowptr[v + 1]; ++j)
+            if (adj[j] > v) b += s * (1 - 2 * (int)sp[adj[j]]);
+        m += s;
+    }
+    *bond = b;
+    *mag = m;
+}
+
+/* Full replay of isg_graph_step (n_warm) followed by isg_graph_pt_run
+ * (n_sample, ee, me) with the counters carried in/out as in or_ising_pt. */
+int64_t or_graph_pt(int n, const int32_t* edges, int m, int R, uint8_t* spins,
+                    const double* temps, double J, uint64_t seed, int32_t* r2t, int32_t* t2r,
+                    uint64_t* gsweep, uint64_t* ksample, uint64_t* xcount, int64_t* accepted,
+                    int64_t n_warm, int64_t n_sample, int ee, int me, int32_t* rec_t,
+                    int64_t* rec_b, int64_t* rec_m, int64_t max_rec) {
+    int32_t* rowptr = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n + 1));
+    int32_t* adj = (int32_t*)malloc(sizeof(int32_t) * (size_t)(2 * m > 0 ? 2 * m : 1));
+    int32_t* colour = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    int ncol = or_graph_build(n, edges, m, rowptr, adj, colour);
+    uint32_t* tab = (uint32_t*)malloc(sizeof(uint32_t) * GTAB * (size_t)R);
+    double* betas = (double*)malloc(sizeof(double) * (size_t)R);
+    double* en = (double*)malloc(sizeof(double) * (size_t)R);
+    for (int t = 0; t < R; ++t) {
+        or_graph_thresholds(temps[t], J, tab + (size_t)t * GTAB);
+        betas[t] = 1.0 / temps[t];
+    }
+    int64_t rows = 0;
+    for (int64_t w = 0; w < n_warm; ++w) {
+        for (int r = 0; r < R; ++r)
+            or_graph_sweep(n, rowptr, adj, colour, ncol, spins + (size_t)r * n, (uint32_t)r, seed,
+                           *gsweep, tab + (size_t)r2t[r] * GTAB);
+        ++*gsweep;
+    }
+    for (int64_t s = 0; s < n_sample; ++s) {
+        for (int r = 0; r < R; ++r)
+            or_graph_sweep(n, rowptr, adj, colour, ncol, spins + (size_t)r * n, (uint32_t)r, seed,
+                           *gsweep, tab + (size_t)r2t[r] * GTAB);
+        const int do_m = ((*ksample + 1) % (uint64_t)me) == 0;
+        const int do_x = ((*ksample + 1) % (uint64_t)ee) == 0;
+        if (do_m || do_x) {
+            for (int r = 0; r < R; ++r) {
+                int64_t b, mg;
+                or_graph_measure(n, rowptr, adj, spins + (size_t)r * n, &b, &mg);
+                en[r] = -(J * (double)b);
+                if (do_m && rows < max_rec) {
+                    rec_t[rows * R + r] = r2t[r];
+                    rec_b[rows * R + r] = b;
+                    rec_m[rows * R + r] = mg;
+                }
+            }
+            if (do_m) ++rows;
+        }
+        if (do_x) {
+            *accepted += or_exchange(R, betas, en, r2t, t2r, (int)(*xcount & 1), seed,
+                                     0xFFFFFFFFu, *xcount);
+            ++*xcount;
+        }
+        ++*ksample;
+        ++*gsweep;
+    }
+    free(rowptr); free(adj); free(colour); free(tab); free(betas); free(en);
+    return rows;
+}
+
+/* The reference's CPU algorithm on a graph (gpu_jfit.rs:172-262 with
+ * metropolis.rs:8-27): R replicas hot-started from Xoshiro256++ seeded
+ * seed + 1000 r, one shared Xoshiro256++(seed) for all sweeps and exchanges,
+ * random-site Metropolis sweeps of n attempts, E and M every sample,
+ * exchange every ee samples.  Writes per-temperature sums
+ * out[t*6 + {0..5}] = sum e, sum e^2, sum |m|, sum m^2, sum m^4, count. */
+void or_graph_ref_pt(int n, const int32_t* edges, int m, int R, const double* temps, double J,
+                     uint64_t seed, int64_t warmup, int64_t samples, int ee, double* out) {
+    int32_t* rowptr = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n + 1));
+    int32_t* adj = (int32_t*)malloc(sizeof(int32_t) * (size_t)(2 * m > 0 ? 2 * m : 1));
+    int32_t* colour = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    or_graph_build(n, edges, m, rowptr, adj, colour);
+    int8_t* sp = (int8_t*)malloc((size_t)n * R);
+    int32_t* r2t = (int32_t*)malloc(sizeof(int32_t) * R);
+    int32_t* t2r = (int32_t*)malloc(sizeof(int32_t) * R);
+    double* betas = (double*)malloc(sizeof(double) * R);
+    double* en = (double*)malloc(sizeof(double) * R);
+    for (int r = 0; r < R; ++r) {
+        xo256 gr;
+        or_xo_seed(&gr, seed + (uint64_t)r * 1000u);
+        or_ref_randomise(sp + (size_t)r * n, n, &gr);
+        r2t[r] = t2r[r] = r;
+        betas[r] = 1.0 / temps[r];
+    }
+    for (int i = 0; i < 6 * R; ++i) out[i] = 0.0;
+    xo256 g;
+    or_xo_seed(&g, seed);
+    const double nn = (double)n;
+    for (int64_t s = -warmup; s < samples; ++s) {
+        for (int r = 0; r < R; ++r) {
+            int8_t* x = sp + (size_t)r * n;
+            double beta = betas[r2t[r]];
+            for (int a = 0; a < n; ++a) {
+                int idx = (int)xo_range(&g, (uint64_t)n);
+                double sum = 0.0;
+                for (int j = rowptr[idx]; j < rowptr[idx + 1]; ++j) sum += (double)x[adj[j]];
+                double dE = 2.0 * (double)x[idx] * (J * sum);
+                if (dE < 0.0 || xo_f64(&g) < exp(-beta * dE)) x[idx] = (int8_t)(-x[idx]);
+            }
+            if (s < 0) continue;
+            int64_t b = 0, mg = 0;
+            for (int v = 0; v < n; ++v) {
+                for (int j = rowptr[v]; j < rowptr[v + 1]; ++j)
+                    if (adj[j] > v) b += x[v] * x[adj[j]];
+                mg += x[v];
+            }
+            double e = -J * (double)b;
+            double e_per = e / nn, m_per = fabs((double)mg / nn);
+            en[r] = e;
+            double* o = out + (size_t)r2t[r] * 6;
+            o[0] += e_per;
+            o[1] += e_per * e_per;
+            o[2] += m_per;
+            o[3] += m_per * m_per;
+            o[4] += (m_per * m_per) * (m_per * m_per);
+            o[5] += 1.0;
+        }
+        if (s >= 0 && (s + 1) % ee == 0) {
+            /* replica_exchange (parallel_tempering.rs:5-36) drawing from the
+             * shared generator */
+            for (int i = (int)((s / ee) & 1); i + 1 < R; i += 2) {
+                int ri = t2r[i], rj = t2r[i + 1];
+                double d = (betas[i] - betas[i + 1]) * (en[rj] - en[ri]);
+                if (d < 0.0 || xo_f64(&g) < exp(-d)) {
+                    t2r[i] = rj;
+                    t2r[i + 1] = ri;
+                    r2t[ri] = i + 1;
+                    r2t[rj] = i;
+                }
+            }
+        }
+    }
+    free(rowptr); free(adj); free(colour); free(sp); free(r2t); free(t2r); free(betas); free(en);
+}

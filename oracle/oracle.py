@@ -15,6 +15,7 @@ _HERE = Path(__file__).resolve().parent
 _LIB = None
 
 i8p = np.ctypeslib.ndpointer(dtype=np.int8, flags="C_CONTIGUOUS")
+u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
@@ -32,6 +33,7 @@ def lib():
         L = C.CDLL(str(path))
         L.or_philox4x32_10.argtypes = [u32p, u32p, u32p]
         L.or_ising_thresholds.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, u32p]
+        _bind_graph(L)
         L.or_ising_hot_start.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_uint32, i8p]
         L.or_ising_halfsweep.argtypes = [C.c_int, C.c_int, i8p, C.c_int, C.c_uint64, C.c_uint32,
                                          C.c_uint64, u32p]
@@ -294,6 +296,83 @@ def coarsening(n: int, J: float, t_high: float, t_quench: float, warmup: int, st
     pt.temps[:] = max(t_quench, 0.01)
     b, _ = pt.schedule(None, steps, every, 0)
     return (np.arange(len(b)) * every, np.array([wall_density(x, n) for x in b[:, 0]]))
+
+
+def _bind_graph(L):
+    L.or_graph_build.argtypes = [C.c_int, i32p, C.c_int, i32p, i32p, i32p]
+    L.or_graph_build.restype = C.c_int
+    L.or_graph_hot_start.argtypes = [C.c_int, C.c_int, C.c_uint64, u8p]
+    L.or_graph_pt.argtypes = [C.c_int, i32p, C.c_int, C.c_int, u8p, f64p, C.c_double, C.c_uint64,
+                              i32p, i32p, u64p, u64p, u64p, i64p, C.c_int64, C.c_int64, C.c_int,
+                              C.c_int, i32p, i64p, i64p, C.c_int64]
+    L.or_graph_pt.restype = C.c_int64
+    L.or_graph_ref_pt.argtypes = [C.c_int, i32p, C.c_int, C.c_int, f64p, C.c_double, C.c_uint64,
+                                  C.c_int64, C.c_int64, C.c_int, f64p]
+
+
+def graph_colouring(n: int, edges) -> tuple[int, np.ndarray]:
+    """Greedy proper colouring in node order (the device's): (classes, colour[n])."""
+    e = np.ascontiguousarray(edges, np.int32).reshape(-1)
+    rowptr = np.zeros(n + 1, np.int32)
+    adj = np.zeros(max(len(e), 1), np.int32)
+    col = np.zeros(n, np.int32)
+    k = lib().or_graph_build(n, e, len(e) // 2, rowptr, adj, col)
+    return k, col
+
+
+class GraphPT:
+    """Replay of the graph PT engine (isg_graph_*): bit-exact oracle."""
+
+    def __init__(self, n: int, edges, R: int, temps, seed: int, J: float = 1.0):
+        self.n, self.R, self.seed, self.J = n, R, seed, J
+        self.edges = np.ascontiguousarray(edges, np.int32).reshape(-1)
+        self.temps = np.ascontiguousarray(temps, np.float64)
+        self.spins = np.zeros(n * R, np.uint8)
+        lib().or_graph_hot_start(n, R, seed, self.spins)
+        self.r2t = np.arange(R, dtype=np.int32)
+        self.t2r = np.arange(R, dtype=np.int32)
+        self.gsweep = np.zeros(1, np.uint64)
+        self.ksample = np.zeros(1, np.uint64)
+        self.xcount = np.zeros(1, np.uint64)
+        self.accepted = np.zeros(1, np.int64)
+
+    def _run(self, warm: int, samples: int, ee: int, me: int):
+        rows = samples // me + 2
+        rt = np.zeros(rows * self.R, np.int32)
+        rb = np.zeros(rows * self.R, np.int64)
+        rm = np.zeros(rows * self.R, np.int64)
+        got = lib().or_graph_pt(self.n, self.edges, len(self.edges) // 2, self.R, self.spins,
+                                self.temps, self.J, self.seed, self.r2t, self.t2r, self.gsweep,
+                                self.ksample, self.xcount, self.accepted, warm, samples, ee, me,
+                                rt, rb, rm, rows)
+        k = got * self.R
+        return rt[:k].reshape(got, self.R), rb[:k].reshape(got, self.R), rm[:k].reshape(got, self.R)
+
+    def warmup(self, n: int) -> None:
+        self._run(n, 0, 1, 1)
+
+    def reset_sampling(self) -> None:
+        self.ksample[:] = 0
+        self.xcount[:] = 0
+        self.accepted[:] = 0
+
+    def sample(self, n: int, exchange_every: int, measure_every: int):
+        return self._run(0, n, exchange_every, measure_every)
+
+    def replica_spins(self, r: int) -> np.ndarray:
+        d = self.spins[r * self.n:(r + 1) * self.n]
+        return np.where(d == 1, -1, 1).astype(np.int8)
+
+
+def graph_ref_pt(n: int, edges, temps, J: float, seed: int, warmup: int, samples: int,
+                 ee: int) -> np.ndarray:
+    """The reference's CPU algorithm on a graph (gpu_jfit.rs:172-262): per
+    temperature [sum e, sum e^2, sum |m|, sum m^2, sum m^4, count]."""
+    e = np.ascontiguousarray(edges, np.int32).reshape(-1)
+    t = np.ascontiguousarray(temps, np.float64)
+    out = np.zeros(6 * len(t), np.float64)
+    lib().or_graph_ref_pt(n, e, len(e) // 2, len(t), t, J, seed, warmup, samples, ee, out)
+    return out.reshape(len(t), 6)
 
 
 def ref_run(L: int, dim: int, T: float, seed: int, warmup: int, samples: int, J=1.0, h=0.0):

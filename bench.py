@@ -679,6 +679,90 @@ def run_quench(args):
     return 0
 
 
+JFIT = dict(graph_n=8, replicas=20, warmup=5000, samples=50000, exchange_every=10,
+            temps={"ising": (6.0, 6.7), "heisenberg": (1.5, 3.0), "xy": (1.5, 3.0)})
+
+
+def run_jfit(args):
+    """`gpu_jfit --model ising|heisenberg|xy` at the reference CLI's defaults
+    (src/bin/gpu_jfit.rs:25-35: 20 replicas, 5000 + 50000 samples, exchange
+    every 10) on a BCC graph of 8^3 cells (1024 nodes, coordination 8).  One
+    step = the whole protocol through the C ABI: create, warm-up, sampling with
+    the (slot, E, M) records of every replica and sample copied to the host.
+    The unit is the reference's unit of work, one replica sample (a sweep of N
+    attempts, or one Wolff cluster for xy, followed by a measurement)."""
+    import torch
+    torch.cuda.set_device(0)
+    pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
+    oracle = _load("isg_oracle", ROOT / "oracle" / "oracle.py")
+    model = args.workload.split("-", 1)[1] if "-" in args.workload else "ising"
+    k = JFIT
+    g = pkg.GraphDef.bcc(k["graph_n"])
+    R, warmup, samples, ee = k["replicas"], k["warmup"], k["samples"], k["exchange_every"]
+    tmin, tmax = k["temps"][model]
+    temps = pkg.linspace_temperatures(tmin, tmax, R)
+    nc = {"ising": 1, "heisenberg": 3, "xy": 2}[model]
+    chunk = 10000
+
+    def once():
+        if model == "ising":
+            b = pkg.GraphBatch(g.n_nodes, g.edges, R, seed=SEED)
+        else:
+            b = pkg.ContinuousGraphBatch(g.n_nodes, g.edges, R, nc, seed=SEED)
+        b.set_temperatures(temps)
+        b.step(warmup)
+        b.reset_sampling()
+        done = 0
+        while done < samples:
+            n = min(chunk, samples - done)
+            b.pt_run(n, ee, 1)
+            done += n
+        b.close()
+
+    steps, warm = max(1, min(args.steps, 5)), max(1, min(args.warmup, 2))
+    for _ in range(warm):
+        once()
+    clocks = ClockSampler(0)
+    with clocks:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            once()
+        wall = time.perf_counter() - t0
+    per_step = R * (warmup + samples)
+    value = per_step * steps / wall * 1e-3
+    h2d = g.edges.size * 4 + R * 8
+    rec = 4 + 8 + 8 * max(nc, 1)
+    d2h = samples * R * rec
+    # reference CPU algorithm (one thread, one shared generator), bounded sample
+    cpu_samples = {"ising": 6000, "heisenberg": 2000, "xy": 8000}[model]
+    t0 = time.perf_counter()
+    if model == "ising":
+        oracle.graph_ref_pt(g.n_nodes, g.edges, temps, 1.0, SEED, 0, cpu_samples, ee)
+    else:
+        oracle.cgraph_ref_pt(g.n_nodes, g.edges, nc, temps, 1.0, SEED, 0, cpu_samples, ee)
+    cpu = R * cpu_samples / (time.perf_counter() - t0) * 1e-3
+    line = {"metric": f"replica samples/ms, gpu_jfit --model {model} defaults on BCC N="
+                      f"{k['graph_n']} ({g.n_nodes} nodes)",
+            "value": value, "unit": "samples/ms", "n_gpus": 1, "steps": steps, "warmup": warm,
+            "ms_per_step": wall / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int8" if model == "ising" else "f32 (f64 sums)",
+            "data": "synthetic (seeded Philox start)",
+            "config": {"workload": f"gpu_jfit --model {model}: BCC {k['graph_n']}^3 cells, "
+                                   f"{R} replicas, T in [{tmin}, {tmax}], warm-up {warmup}, "
+                                   f"{samples} samples, exchange every {ee}",
+                       "timing": "wall clock around the whole protocol (C ABI, host records)",
+                       "l2": "the graph and the replicas' spins (< 1 MB) stay on chip"},
+            "e2e": {"value": value, "unit": "samples/ms", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "cpu_baseline": {"value": cpu, "unit": "samples/ms", "cores": 1, "kind": "port",
+                             "sample": f"{cpu_samples} samples of all {R} replicas, the "
+                                       "reference's CPU algorithm restated in C "
+                                       "(gpu_jfit.rs run loop, one shared Xoshiro256++)"},
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def ncu_case_resident():
     """No timing: one schedule of 2000 sweeps of one L=30 lattice (the coarsening
     default size) for an ncu capture of the cluster-resident kernel."""
@@ -722,7 +806,8 @@ def main():
     ap.add_argument("--cpu-sweeps", type=float, default=1.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0)
     ap.add_argument("--workload", default="ising",
-                    choices=["ising", "heisenberg", "xy", "anneal", "kz", "coarsening"])
+                    choices=["ising", "heisenberg", "xy", "anneal", "kz", "coarsening",
+                             "jfit", "jfit-heisenberg", "jfit-xy"])
     ap.add_argument("--learned", action="store_true",
                     help="config 5: learned proposal vs plain PT ESS/s (separate JSON lines)")
     ap.add_argument("--train-seconds", type=float, default=60.0)
@@ -743,6 +828,8 @@ def main():
         return run_anneal(args)
     if args.workload in ("kz", "coarsening"):
         return run_quench(args)
+    if args.workload.startswith("jfit"):
+        return run_jfit(args)
     if args.workload != "ising":
         return run_continuous(args)
     if args.warmup < 3:

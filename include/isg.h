@@ -80,6 +80,20 @@ extern "C" {
  *        flip iff u <= threshold[own_down][degree][n_down_neighbours].
  *        Exchanges use the EXCH tag with c0 = 0xFFFFFFFF. */
 #define ISG_TAG_GRAPH  0x07u
+/* CGRAPH: continuous spins on a graph (isg_cgraph_*).  c0 = replica,
+ *        step = global sweep; field (colour bits) and c1:
+ *          0xFE, c1 = node, step 0: hot start, O(3) z = 2 u0 - 1,
+ *                phi = 2 pi u1; O(2) phi = 2 pi u0;
+ *          class c, c1 = node: O(3) cone Metropolis, cos(theta) =
+ *                1 - u0 (1 - cos delta), phi = 2 pi u1, accept iff dE <= 0
+ *                or u2 < exp(-beta dE);
+ *          0xFD, c1 = 0xFFFFFFFF: O(2) Wolff mirror angle 2 pi u0 and seed
+ *                node (w1 * n) >> 32;
+ *          0xC0 + k/4, c1 = node i, word k % 4: O(2) bond test of adjacency
+ *                slot k of i, bond iff same-sign projections and
+ *                u < 1 - exp(-2 beta J |p_i| |p_j|).
+ *        u = 24-bit uniforms (w >> 8) 2^-24. */
+#define ISG_TAG_CGRAPH 0x08u
 
 const char* isg_last_error(void);
 int isg_version(void);
@@ -428,6 +442,45 @@ int isg_graph_pt_run(isg_graph* h, int64_t n_sweeps, int exchange_every, int mea
 int isg_graph_get_accepted(isg_graph* h, int64_t* accepted);
 int isg_graph_get_spins(isg_graph* h, int replica, int8_t* out);
 int isg_graph_get_r2t(isg_graph* h, int32_t* r2t);
+
+/* ------------------------------------------------------------------------ */
+/* Continuous spins on graphs (`gpu_jfit --model heisenberg|xy`)             */
+/* ------------------------------------------------------------------------ */
+typedef struct isg_cgraph isg_cgraph;
+
+/* Replaces the replica sets of run_heisenberg_jfit (n_comp = 3,
+ * src/bin/gpu_jfit.rs:414-447) and run_xy_jfit (n_comp = 2,
+ * gpu_jfit.rs:299-330): `replicas` copies of a graph (edge list as
+ * isg_graph_create; degree at most 64, n_nodes <= 16384) with FP32 unit spins,
+ * hot from the CGRAPH stream.  One CTA per replica holds its spins in shared
+ * memory.  O(3) sweeps are cone Metropolis (half-angle isg_cgraph_set_delta,
+ * default 0.5 as gpu_jfit.rs:450) by colour class of a greedy proper
+ * colouring; an O(2) sweep is one single-cluster Wolff flip
+ * (src/xy/wolff.rs:15-78) grown breadth-first by the CTA. */
+int isg_cgraph_create(isg_cgraph** out, int n_nodes, const int32_t* edges, int n_edges,
+                      int replicas, int n_comp, uint64_t seed);
+int isg_cgraph_destroy(isg_cgraph* h);
+int isg_cgraph_num_colours(isg_cgraph* h, int* n_colours);
+/* Temperature of slot t and coupling J; resets the ladder to the identity. */
+int isg_cgraph_set_temperatures(isg_cgraph* h, const double* temps, double J);
+int isg_cgraph_set_delta(isg_cgraph* h, double delta);
+int isg_cgraph_step(isg_cgraph* h, int64_t n_sweeps);
+int isg_cgraph_reset_sampling(isg_cgraph* h);
+/* As isg_graph_pt_run with per-record energy E = -J sum_bonds S.S' (FP64 sum
+ * of FP32 node terms) and magnetisation vector m_rec[(row*R + r)*n_comp + k];
+ * replaces the sampling loops of gpu_jfit.rs:349-377 and 462-490. */
+int isg_cgraph_pt_run(isg_cgraph* h, int64_t n_sweeps, int exchange_every, int measure_every,
+                      int32_t* tslot_rec, double* e_rec, double* m_rec, int64_t max_records,
+                      int64_t* n_records);
+int isg_cgraph_get_accepted(isg_cgraph* h, int64_t* accepted);
+/* Per replica since the last reset: accepted rotations (O(3)) or the summed
+ * cluster sizes (O(2)). */
+int isg_cgraph_get_moves(isg_cgraph* h, int64_t* moves);
+/* Spins of one replica, natural layout out[node*n_comp + k]. */
+int isg_cgraph_get_spins(isg_cgraph* h, int replica, float* out);
+int isg_cgraph_set_spins(isg_cgraph* h, int replica, const float* in);
+int isg_cgraph_get_r2t(isg_cgraph* h, int32_t* r2t);
+int isg_cgraph_get_sweep(isg_cgraph* h, uint64_t* sweep);
 
 /* ------------------------------------------------------------------------ */
 /* Statistics used by the drop-in driver                                     */

@@ -19,6 +19,7 @@ backend for the checkerboard PT path:
   GraphDef              src/graph.rs:4-79 (JSON / edge-CSV readers) with BCC,
                         FCC and diluted-cubic builders
   GraphBatch            Ising PT on a graph (src/bin/gpu_jfit.rs:172-297)
+  ContinuousGraphBatch  Heisenberg / XY PT on a graph (gpu_jfit.rs:298-524)
   IsingBatch / ContinuousBatch: every (size, replica) lattice of a run in one
   handle (the GB300 replacement of the reference's Vec<LatticeGpu>).
 
@@ -112,6 +113,20 @@ def _declare(L):
         "isg_graph_get_accepted": [vp, vp],
         "isg_graph_get_spins": [vp, i32, vp],
         "isg_graph_get_r2t": [vp, vp],
+        "isg_cgraph_create": [C.POINTER(vp), i32, vp, i32, i32, i32, u64],
+        "isg_cgraph_destroy": [vp],
+        "isg_cgraph_num_colours": [vp, vp],
+        "isg_cgraph_set_temperatures": [vp, vp, dbl],
+        "isg_cgraph_set_delta": [vp, dbl],
+        "isg_cgraph_step": [vp, i64],
+        "isg_cgraph_reset_sampling": [vp],
+        "isg_cgraph_pt_run": [vp, i64, i32, i32, vp, vp, vp, i64, vp],
+        "isg_cgraph_get_accepted": [vp, vp],
+        "isg_cgraph_get_moves": [vp, vp],
+        "isg_cgraph_get_spins": [vp, i32, vp],
+        "isg_cgraph_set_spins": [vp, i32, vp],
+        "isg_cgraph_get_r2t": [vp, vp],
+        "isg_cgraph_get_sweep": [vp, vp],
         "isg_coarsening": [i32, dbl, dbl, dbl, i64, i64, i64, u64, vp, vp, i64, vp],
         "isg_cont_create": [C.POINTER(vp), vp, i32, i32, i32, u64],
         "isg_cont_destroy": [vp],
@@ -697,6 +712,96 @@ class GraphBatch:
         out = np.zeros(self.replicas, np.int32)
         _check(lib().isg_graph_get_r2t(self._h, _ptr(out)))
         return out
+
+
+class ContinuousGraphBatch:
+    """`replicas` continuous-spin replicas of one graph with device replica
+    exchange: n_comp = 3 is run_heisenberg_jfit (cone Metropolis, half-angle
+    `set_delta`, default 0.5; src/bin/gpu_jfit.rs:414-524), n_comp = 2 is
+    run_xy_jfit (one single-cluster Wolff flip per sweep; gpu_jfit.rs:298-412).
+
+    At most 16384 nodes, degree 64 and 1024 replicas; spins are FP32 unit
+    vectors, energies and magnetisations FP64 sums."""
+
+    def __init__(self, n_nodes: int, edges, replicas: int, n_comp: int, seed: int = 42):
+        e = np.ascontiguousarray(edges, np.int32).reshape(-1)
+        self.n, self.replicas, self.nc = int(n_nodes), int(replicas), int(n_comp)
+        h = C.c_void_p()
+        _check(lib().isg_cgraph_create(C.byref(h), self.n, _ptr(e) if len(e) else None,
+                                       len(e) // 2, self.replicas, self.nc, int(seed)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().isg_cgraph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def num_colours(self) -> int:
+        v = C.c_int()
+        _check(lib().isg_cgraph_num_colours(self._h, C.byref(v)))
+        return v.value
+
+    def set_temperatures(self, temps, J: float = 1.0) -> None:
+        t = np.ascontiguousarray(temps, np.float64)
+        if len(t) != self.replicas:
+            raise IsingError(-1, "need one temperature per replica slot")
+        _check(lib().isg_cgraph_set_temperatures(self._h, _ptr(t), float(J)))
+
+    def set_delta(self, delta: float) -> None:
+        _check(lib().isg_cgraph_set_delta(self._h, float(delta)))
+
+    def step(self, n_sweeps: int = 1) -> None:
+        _check(lib().isg_cgraph_step(self._h, int(n_sweeps)))
+
+    def reset_sampling(self) -> None:
+        _check(lib().isg_cgraph_reset_sampling(self._h))
+
+    def pt_run(self, n_sweeps: int, exchange_every: int, measure_every: int = 1):
+        """(slot (rows, R), energy (rows, R), magnetisation (rows, R, n_comp))."""
+        rows = n_sweeps // measure_every + 1
+        t = np.zeros((rows, self.replicas), np.int32)
+        e = np.zeros((rows, self.replicas), np.float64)
+        m = np.zeros((rows, self.replicas, self.nc), np.float64)
+        n = C.c_int64()
+        _check(lib().isg_cgraph_pt_run(self._h, int(n_sweeps), int(exchange_every),
+                                       int(measure_every), _ptr(t), _ptr(e), _ptr(m), rows,
+                                       C.byref(n)))
+        return t[:n.value], e[:n.value], m[:n.value]
+
+    def accepted(self) -> int:
+        v = C.c_int64()
+        _check(lib().isg_cgraph_get_accepted(self._h, C.byref(v)))
+        return v.value
+
+    def moves(self) -> np.ndarray:
+        out = np.zeros(self.replicas, np.int64)
+        _check(lib().isg_cgraph_get_moves(self._h, _ptr(out)))
+        return out
+
+    def get_spins(self, r: int) -> np.ndarray:
+        out = np.zeros((self.n, self.nc), np.float32)
+        _check(lib().isg_cgraph_get_spins(self._h, int(r), _ptr(out)))
+        return out
+
+    def set_spins(self, r: int, spins) -> None:
+        a = np.ascontiguousarray(spins, np.float32).reshape(self.n, self.nc)
+        _check(lib().isg_cgraph_set_spins(self._h, int(r), _ptr(a)))
+
+    def r2t(self) -> np.ndarray:
+        out = np.zeros(self.replicas, np.int32)
+        _check(lib().isg_cgraph_get_r2t(self._h, _ptr(out)))
+        return out
+
+    def sweep_count(self) -> int:
+        v = C.c_uint64()
+        _check(lib().isg_cgraph_get_sweep(self._h, C.byref(v)))
+        return v.value
 
 
 class LatticeGpu:

@@ -53,7 +53,8 @@ struct GraphParams {
     long long* rec_b;        // [rows][R] bond sums (one record per measured sweep)
     long long* rec_m;
     int32_t* rec_t;
-    long long* last_b;       // [R] bond sum after the launch's last sweep
+    double* last_e;          // [R] energy -J * bond after the launch's last sweep
+    double J;
     uint64_t seed;
     uint64_t sweep0;         // global sweep of the launch's first sweep
     int n, R, n_classes;
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(kGThreads) k_graph_sweeps(const __grid_constan
     }
     long long bb, mm;
     g_measure(P, g_sp, red, bb, mm);
-    if (threadIdx.x == 0) P.last_b[r] = bb;
+    if (threadIdx.x == 0) P.last_e[r] = -__dmul_rn(P.J, (double)bb);
     for (int v = threadIdx.x; v < P.n; v += blockDim.x) spins[v] = g_sp[v];
 }
 
@@ -161,21 +162,23 @@ __global__ void k_graph_init(uint8_t* spins, int n, int R, uint64_t seed) {
 }
 
 // Exchange pass over the temperature ladder (src/parallel_tempering.rs:16-33)
-// on E = -J * bond, FP64 with explicitly rounded products.
-__global__ void k_graph_exchange(const long long* last_b, int32_t* r2t, int32_t* t2r,
-                                 const double* betas, double J, int R, int parity,
-                                 unsigned long long* ctrl, uint64_t seed) {
+// on the energies of the replicas' last sweeps, FP64 with explicitly rounded
+// products; the parity is the exchange count's.  Shared by the Ising and the
+// continuous-spin graph engines.
+__global__ void k_graph_exchange(const double* energies, int32_t* r2t, int32_t* t2r,
+                                 const double* betas, int R, unsigned long long* ctrl,
+                                 uint64_t seed) {
     __shared__ double s_e[kGMaxReplicas];
     __shared__ int s_t2r[kGMaxReplicas];
     __shared__ int s_acc;
     if (threadIdx.x == 0) s_acc = 0;
     for (int r = threadIdx.x; r < R; r += blockDim.x) {
-        s_e[r] = -__dmul_rn(J, (double)last_b[r]);
+        s_e[r] = energies[r];
         s_t2r[r] = t2r[r];
     }
     __syncthreads();
     const unsigned long long xc = ctrl[0];
-    const int par = parity >= 0 ? (parity & 1) : (int)(xc & 1ull);
+    const int par = (int)(xc & 1ull);
     const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
     const uint32_t c3 = counter_word3(ISG_TAG_EXCH, 0, xc);
     for (int i = par + 2 * threadIdx.x; i + 1 < R; i += 2 * blockDim.x) {
@@ -202,6 +205,13 @@ __global__ void k_graph_exchange(const long long* last_b, int32_t* r2t, int32_t*
     }
 }
 
+cudaError_t launch_graph_exchange(const double* energies, int32_t* r2t, int32_t* t2r,
+                                  const double* betas, int R, unsigned long long* ctrl,
+                                  uint64_t seed, cudaStream_t stream) {
+    k_graph_exchange<<<1, 256, 0, stream>>>(energies, r2t, t2r, betas, R, ctrl, seed);
+    return cudaGetLastError();
+}
+
 }  // namespace isg
 
 using namespace isg;
@@ -223,7 +233,7 @@ struct isg_graph {
     int32_t* d_r2t = nullptr;
     int32_t* d_t2r = nullptr;
     double* d_betas = nullptr;
-    long long* d_last_b = nullptr;
+    double* d_last_e = nullptr;
     unsigned long long* d_ctrl = nullptr;  // [0] exchange count, [1] accepted
     long long* d_rec_b = nullptr;
     long long* d_rec_m = nullptr;
@@ -247,7 +257,7 @@ int g_destroy(isg_graph* H) {
     cudaFree(H->d_r2t);
     cudaFree(H->d_t2r);
     cudaFree(H->d_betas);
-    cudaFree(H->d_last_b);
+    cudaFree(H->d_last_e);
     cudaFree(H->d_ctrl);
     cudaFree(H->d_rec_b);
     cudaFree(H->d_rec_m);
@@ -269,7 +279,8 @@ GraphParams g_params(isg_graph* H) {
     P.rec_b = H->d_rec_b;
     P.rec_m = H->d_rec_m;
     P.rec_t = H->d_rec_t;
-    P.last_b = H->d_last_b;
+    P.last_e = H->d_last_e;
+    P.J = H->J;
     P.seed = H->seed;
     P.n = H->n;
     P.R = H->R;
@@ -373,7 +384,7 @@ int isg_graph_create(isg_graph** out, int n_nodes, const int32_t* edges, int n_e
     GALLOC(H->d_r2t, sizeof(int32_t) * replicas);
     GALLOC(H->d_t2r, sizeof(int32_t) * replicas);
     GALLOC(H->d_betas, sizeof(double) * replicas);
-    GALLOC(H->d_last_b, sizeof(long long) * replicas);
+    GALLOC(H->d_last_e, sizeof(double) * replicas);
     GALLOC(H->d_ctrl, sizeof(unsigned long long) * 2);
 #undef GALLOC
     e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);
@@ -537,10 +548,8 @@ int isg_graph_pt_run(isg_graph* h, int64_t n_sweeps, int exchange_every, int mea
         h->ksample += (uint64_t)n;
         done += n;
         if (h->ksample % (uint64_t)exchange_every == 0) {
-            k_graph_exchange<<<1, 256, 0, h->stream>>>(h->d_last_b, h->d_r2t, h->d_t2r,
-                                                       h->d_betas, h->J, h->R, -1, h->d_ctrl,
-                                                       h->seed);
-            cudaError_t e = cudaGetLastError();
+            cudaError_t e = launch_graph_exchange(h->d_last_e, h->d_r2t, h->d_t2r, h->d_betas,
+                                                  h->R, h->d_ctrl, h->seed, h->stream);
             if (e != cudaSuccess) return cuda_fail(e, "k_graph_exchange");
         }
     }

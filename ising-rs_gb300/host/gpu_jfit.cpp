@@ -1,23 +1,27 @@
-// gpu_jfit — drop-in for the reference's `gpu_jfit --model ising`
-// (src/bin/gpu_jfit.rs) on libisinggb: parallel tempering of an Ising model on a
-// graph read from {"n_nodes": N, "edges": [[a, b], ...]} (GraphDef::from_json,
+// gpu_jfit — drop-in for the reference's `gpu_jfit` (src/bin/gpu_jfit.rs) on
+// libisinggb: parallel tempering of Ising (--model ising), XY (--model xy) or
+// Heisenberg (--model heisenberg) spins on a graph read from
+// {"n_nodes": N, "edges": [[a, b], ...]} (GraphDef::from_json,
 // src/graph.rs:44-79).
 //
 // Same flags and defaults (gpu_jfit.rs:22-90, unknown flags skipped), the same
 // validation messages (gpu_jfit.rs:92-110; cli.rs), the same progress lines and
-// the same output <outdir>/gpu_jfit_ising_<graph>.csv with the reference's
+// the same output <outdir>/gpu_jfit_<model>_<graph>.csv with the reference's
 // columns, T with 4 decimals, the rest with 6 and the error columns written as
-// 0.0 (gpu_jfit.rs:269-297): per temperature index the running means of e, |m|,
-// m^2, m^4 over every sampling sweep, Cv = beta^2 (<e^2> - <e>^2) N and
-// chi = beta (<m^2> - <|m|>^2) N.
+// 0.0 (gpu_jfit.rs:269-297, 385-411, 498-524): per temperature index the
+// running means of e, |m|, m^2, m^4 over every sampling sweep,
+// Cv = beta^2 (<e^2> - <e>^2) N and chi = beta (<m^2> - <|m|>^2) N.
 //
-// Differences by design:
-//   * the replicas run on the GPU (isg_graph_*): sites updated colour class by
-//     colour class of a greedy proper colouring with the Philox GRAPH stream
-//     instead of random-site sweeps with one shared Xoshiro256++; the exchange
-//     rule and cadence are the reference's;
-//   * --model xy and --model heisenberg (continuous spins on graphs) are not in
-//     this build and exit 1.
+// Differences by design: the replicas run on the GPU (isg_graph_*,
+// isg_cgraph_*) with Philox streams instead of one shared Xoshiro256++:
+//   * ising: sites updated colour class by colour class of a greedy proper
+//     colouring instead of random-site sweeps;
+//   * heisenberg: the same cone Metropolis (half-angle 0.5) by colour class;
+//   * xy: one single-cluster Wolff flip per sample, as the reference, grown
+//     breadth-first on the device;
+// the exchange rule and cadence are the reference's.  Graphs are limited to
+// 65536 nodes of degree <= 12 (ising) or 16384 nodes of degree <= 64 (xy,
+// heisenberg), and to 1024 replicas; self-loops are rejected.
 #include <algorithm>
 #include <cctype>
 #include <fstream>
@@ -169,10 +173,8 @@ int main(int argc, char** argv) {
     fprintf(stderr, "jfit: model=%s, graph=%s, N=%d, T=%s..%s, replicas=%llu, exchange_every=%llu\n",
             model.c_str(), name.c_str(), n, rust_f64(t_min).c_str(), rust_f64(t_max).c_str(),
             (unsigned long long)R, (unsigned long long)ee);
-    if (model == "xy" || model == "heisenberg")
-        die("Error: --model " + model + " (continuous spins on graphs) is not provided by this "
-            "GPU build; use --model ising");
-    if (model != "ising") die("Error: --model must be ising, xy, or heisenberg");
+    if (model != "ising" && model != "xy" && model != "heisenberg")
+        die("Error: --model must be ising, xy, or heisenberg");
     if (R == 0) die("Error: --replicas must be at least 1");
     if (R > 1024) die("Error: --replicas must be at most 1024");
     if (ee == 0) {
@@ -185,47 +187,80 @@ int main(int argc, char** argv) {
     std::vector<double> temps(R);
     for (uint64_t t = 0; t < R; ++t)
         temps[t] = R == 1 ? t_min : t_min + (t_max - t_min) * (double)t / (double)(R - 1);
-    isg_graph* h = nullptr;
-    if (isg_graph_create(&h, n, edges.data(), (int)(edges.size() / 2), (int)R, seed) != ISG_OK)
-        panic_expect("failed to create the graph replicas", isg_last_error());
-    if (isg_graph_set_temperatures(h, temps.data(), j) != ISG_OK ||
-        isg_graph_step(h, (int64_t)warmup) != ISG_OK || isg_graph_reset_sampling(h) != ISG_OK)
-        panic_expect("GPU sweep failed", isg_last_error());
     const double nn = (double)n;
     std::vector<double> se(R, 0.0), se2(R, 0.0), sm(R, 0.0), sm2(R, 0.0), sm4(R, 0.0);
     std::vector<uint64_t> cnt(R, 0);
+    auto add = [&](int t, double e_per, double m_per) {
+        se[t] += e_per;
+        se2[t] += e_per * e_per;
+        sm[t] += m_per;
+        sm2[t] += m_per * m_per;
+        sm4[t] += (m_per * m_per) * (m_per * m_per);
+        ++cnt[t];
+    };
     const uint64_t chunk = 10000;
+    const int every = (int)std::min<uint64_t>(ee, 1u << 30);
     std::vector<int32_t> rt;
-    std::vector<int64_t> rb, rm;
-    for (uint64_t done = 0; done < samples;) {
-        const uint64_t nsw = std::min(chunk, samples - done);
-        rt.assign(nsw * R, 0);
-        rb.assign(nsw * R, 0);
-        rm.assign(nsw * R, 0);
-        int64_t got = 0;
-        if (isg_graph_pt_run(h, (int64_t)nsw, (int)std::min<uint64_t>(ee, 1u << 30), 1, rt.data(),
-                             rb.data(), rm.data(), (int64_t)nsw, &got) != ISG_OK)
-            panic_expect("GPU sweep failed", isg_last_error());
-        for (int64_t row = 0; row < got; ++row)
-            for (uint64_t r = 0; r < R; ++r) {
-                const size_t o = (size_t)row * R + r;
-                const int t = rt[o];
-                const double e_per = -(j * (double)rb[o]) / nn;
-                const double m_per = std::fabs((double)rm[o] / nn);
-                se[t] += e_per;
-                se2[t] += e_per * e_per;
-                sm[t] += m_per;
-                sm2[t] += m_per * m_per;
-                sm4[t] += (m_per * m_per) * (m_per * m_per);
-                ++cnt[t];
-            }
-        done += nsw;
-    }
     int64_t acc = 0;
-    isg_graph_get_accepted(h, &acc);
-    isg_graph_destroy(h);
+    if (model == "ising") {
+        isg_graph* h = nullptr;
+        if (isg_graph_create(&h, n, edges.data(), (int)(edges.size() / 2), (int)R, seed) != ISG_OK)
+            panic_expect("failed to create the graph replicas", isg_last_error());
+        if (isg_graph_set_temperatures(h, temps.data(), j) != ISG_OK ||
+            isg_graph_step(h, (int64_t)warmup) != ISG_OK || isg_graph_reset_sampling(h) != ISG_OK)
+            panic_expect("GPU sweep failed", isg_last_error());
+        std::vector<int64_t> rb, rm;
+        for (uint64_t done = 0; done < samples;) {
+            const uint64_t nsw = std::min(chunk, samples - done);
+            rt.assign(nsw * R, 0);
+            rb.assign(nsw * R, 0);
+            rm.assign(nsw * R, 0);
+            int64_t got = 0;
+            if (isg_graph_pt_run(h, (int64_t)nsw, every, 1, rt.data(), rb.data(), rm.data(),
+                                 (int64_t)nsw, &got) != ISG_OK)
+                panic_expect("GPU sweep failed", isg_last_error());
+            for (int64_t row = 0; row < got; ++row)
+                for (uint64_t r = 0; r < R; ++r) {
+                    const size_t o = (size_t)row * R + r;
+                    add(rt[o], -(j * (double)rb[o]) / nn, std::fabs((double)rm[o] / nn));
+                }
+            done += nsw;
+        }
+        isg_graph_get_accepted(h, &acc);
+        isg_graph_destroy(h);
+    } else {
+        const int nc = model == "heisenberg" ? 3 : 2;
+        isg_cgraph* h = nullptr;
+        if (isg_cgraph_create(&h, n, edges.data(), (int)(edges.size() / 2), (int)R, nc, seed) !=
+            ISG_OK)
+            panic_expect("failed to create the graph replicas", isg_last_error());
+        if (isg_cgraph_set_temperatures(h, temps.data(), j) != ISG_OK ||
+            isg_cgraph_step(h, (int64_t)warmup) != ISG_OK || isg_cgraph_reset_sampling(h) != ISG_OK)
+            panic_expect("GPU sweep failed", isg_last_error());
+        std::vector<double> re, rmv;
+        for (uint64_t done = 0; done < samples;) {
+            const uint64_t nsw = std::min(chunk, samples - done);
+            rt.assign(nsw * R, 0);
+            re.assign(nsw * R, 0.0);
+            rmv.assign(nsw * R * nc, 0.0);
+            int64_t got = 0;
+            if (isg_cgraph_pt_run(h, (int64_t)nsw, every, 1, rt.data(), re.data(), rmv.data(),
+                                  (int64_t)nsw, &got) != ISG_OK)
+                panic_expect("GPU sweep failed", isg_last_error());
+            for (int64_t row = 0; row < got; ++row)
+                for (uint64_t r = 0; r < R; ++r) {
+                    const size_t o = (size_t)row * R + r;
+                    double m2 = 0.0;
+                    for (int k = 0; k < nc; ++k) m2 += rmv[o * nc + k] * rmv[o * nc + k];
+                    add(rt[o], re[o] / nn, std::sqrt(m2) / nn);
+                }
+            done += nsw;
+        }
+        isg_cgraph_get_accepted(h, &acc);
+        isg_cgraph_destroy(h);
+    }
 
-    const std::string path = join_path(outdir, "gpu_jfit_ising_" + name + ".csv");
+    const std::string path = join_path(outdir, "gpu_jfit_" + model + "_" + name + ".csv");
     std::string csv = "T,E,E_err,M,M_err,M2,M2_err,M4,M4_err,Cv,Cv_err,chi,chi_err\n";
     char buf[256];
     for (uint64_t t = 0; t < R; ++t) {

@@ -353,6 +353,10 @@ static inline double xo_f64(xo256* g) {
     return (double)(xo_next(g) >> 11) * (1.0 / 9007199254740992.0);
 }
 
+/* The same generator for the other oracle files. */
+uint64_t or_xo_range(xo256* g, uint64_t range) { return xo_range(g, range); }
+double or_xo_f64(xo256* g) { return xo_f64(g); }
+
 /* Neighbour table: reference order (-x,+x,-y,+y,-z,+z in lattice.rs terms). */
 int32_t* or_ref_neighbours(int L, int dim) {
     int64_t n = nsites(L, dim);

@@ -34,6 +34,7 @@ def lib():
         L.or_philox4x32_10.argtypes = [u32p, u32p, u32p]
         L.or_ising_thresholds.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, u32p]
         _bind_graph(L)
+        _bind_cgraph(L)
         L.or_ising_hot_start.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_uint32, i8p]
         L.or_ising_halfsweep.argtypes = [C.c_int, C.c_int, i8p, C.c_int, C.c_uint64, C.c_uint32,
                                          C.c_uint64, u32p]
@@ -372,6 +373,81 @@ def graph_ref_pt(n: int, edges, temps, J: float, seed: int, warmup: int, samples
     t = np.ascontiguousarray(temps, np.float64)
     out = np.zeros(6 * len(t), np.float64)
     lib().or_graph_ref_pt(n, e, len(e) // 2, len(t), t, J, seed, warmup, samples, ee, out)
+    return out.reshape(len(t), 6)
+
+
+def _bind_cgraph(L):
+    L.or_cgraph_build.argtypes = [C.c_int, i32p, C.c_int, i32p, i32p, i32p]
+    L.or_cgraph_build.restype = C.c_int
+    L.or_cgraph_hot_start.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64, f64p]
+    L.or_cgraph_metro_sweep.argtypes = [C.c_int, i32p, i32p, i32p, C.c_int, f64p, C.c_uint32,
+                                        C.c_uint64, C.c_uint64, C.c_double, C.c_double,
+                                        C.c_double, C.POINTER(C.c_double)]
+    L.or_cgraph_metro_sweep.restype = C.c_int64
+    L.or_cgraph_wolff_sweep.argtypes = [C.c_int, i32p, i32p, f64p, C.c_uint32, C.c_uint64,
+                                        C.c_uint64, C.c_double, C.c_double,
+                                        C.POINTER(C.c_double)]
+    L.or_cgraph_wolff_sweep.restype = C.c_int
+    L.or_cgraph_measure.argtypes = [C.c_int, i32p, i32p, f64p, C.c_int, C.c_double,
+                                    C.POINTER(C.c_double), f64p]
+    L.or_cgraph_ref_pt.argtypes = [C.c_int, i32p, C.c_int, C.c_int, C.c_int, f64p, C.c_double,
+                                   C.c_uint64, C.c_int64, C.c_int64, C.c_int, C.c_double, f64p]
+
+
+class CGraphReplay:
+    """Per-sweep FP64 replay of the continuous graph engine (isg_cgraph_*):
+    hot start, one sweep of a replica (O(3) cone Metropolis by colour class,
+    O(2) single-cluster Wolff), E and M.  `sweep` returns (moves, margin):
+    accepted rotations or cluster size, and the smallest decision margin."""
+
+    def __init__(self, n: int, edges, nc: int, seed: int):
+        self.n, self.nc, self.seed = n, nc, seed
+        e = np.ascontiguousarray(edges, np.int32).reshape(-1)
+        self.rowptr = np.zeros(n + 1, np.int32)
+        self.adj = np.zeros(max(len(e), 1), np.int32)
+        self.colour = np.zeros(n, np.int32)
+        self.ncol = lib().or_cgraph_build(n, e, len(e) // 2, self.rowptr, self.adj, self.colour)
+        if self.ncol < 0:
+            raise ValueError("bad graph")
+
+    def hot_start(self, R: int) -> np.ndarray:
+        out = np.zeros(R * self.n * self.nc, np.float64)
+        lib().or_cgraph_hot_start(self.n, R, self.nc, self.seed, out)
+        return out.reshape(R, self.n, self.nc)
+
+    def sweep(self, sp: np.ndarray, replica: int, sweep: int, beta: float, J: float = 1.0,
+              cos_delta: float | None = None):
+        assert sp.dtype == np.float64 and sp.flags.c_contiguous and sp.size == self.n * self.nc
+        margin = C.c_double(1e300)
+        if self.nc == 3:
+            cd = float(np.float32(np.cos(0.5))) if cos_delta is None else cos_delta
+            mv = lib().or_cgraph_metro_sweep(self.n, self.rowptr, self.adj, self.colour, self.ncol,
+                                             sp.reshape(-1), replica, self.seed, sweep, beta, J, cd,
+                                             C.byref(margin))
+        else:
+            mv = lib().or_cgraph_wolff_sweep(self.n, self.rowptr, self.adj, sp.reshape(-1),
+                                             replica, self.seed, sweep, beta, J, C.byref(margin))
+        return int(mv), margin.value
+
+    def measure(self, sp: np.ndarray, J: float = 1.0):
+        e = C.c_double()
+        m = np.zeros(self.nc, np.float64)
+        lib().or_cgraph_measure(self.n, self.rowptr, self.adj,
+                                np.ascontiguousarray(sp, np.float64).reshape(-1), self.nc, J,
+                                C.byref(e), m)
+        return e.value, m
+
+
+def cgraph_ref_pt(n: int, edges, nc: int, temps, J: float, seed: int, warmup: int, samples: int,
+                  ee: int, delta: float = 0.5) -> np.ndarray:
+    """The reference's CPU algorithms on a graph (run_heisenberg_jfit for nc = 3,
+    run_xy_jfit for nc = 2, gpu_jfit.rs:298-524): per temperature
+    [sum e, sum e^2, sum |m|, sum m^2, sum m^4, count]."""
+    e = np.ascontiguousarray(edges, np.int32).reshape(-1)
+    t = np.ascontiguousarray(temps, np.float64)
+    out = np.zeros(6 * len(t), np.float64)
+    lib().or_cgraph_ref_pt(n, e, len(e) // 2, len(t), nc, t, J, seed, warmup, samples, ee, delta,
+                           out)
     return out.reshape(len(t), 6)
 
 

@@ -209,9 +209,7 @@ def test_jfit_bad_json_and_models(pkg, tmp_path):
     assert r.returncode == 101 and "failed to parse graph JSON: missing edges" in r.stderr
     good = tmp_path / "ring.json"
     good.write_text(pkg.GraphDef(4, [(0, 1), (1, 2), (2, 3), (3, 0)]).to_json())
-    for model, frag in [("xy", "not provided by this GPU build"),
-                        ("heisenberg", "not provided by this GPU build"),
-                        ("potts", "Error: --model must be ising, xy, or heisenberg")]:
+    for model, frag in [("potts", "Error: --model must be ising, xy, or heisenberg")]:
         r = run(["--graph", str(good), "--model", model, "--outdir", str(tmp_path / "o")])
         assert r.returncode == 1 and frag in r.stderr, r.stderr
         assert f"jfit: model={model}, graph=ring, N=4, T=6..6.7, replicas=20, " \

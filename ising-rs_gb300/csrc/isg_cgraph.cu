@@ -71,6 +71,7 @@ struct CGraphParams {
     const int32_t* adj;      // [2m]
     const int32_t* order;    // nodes by colour class
     const int32_t* cstart;   // [n_classes+1]
+    const int32_t* nlow;     // O(3): neighbours of lower colour, listed first in adj
     float* spins;            // [R][NC][n]
     const float* betaf;      // [slots]
     const int32_t* r2t;      // [R]
@@ -83,75 +84,90 @@ struct CGraphParams {
     uint64_t sweep0;
     float J, cos_delta;
     int n, R, n_classes;
+    int max_deg;             // largest node degree (>= 1)
     int n_sweeps;
     int measure_every, measure_phase;
     int64_t row0;
 };
 
-__device__ __forceinline__ double block_sum_d(double v, double* red) {
+// Component planes of one replica's spins in shared memory.
+struct Planes {
+    float* x;
+    float* y;
+    float* z;
+    __device__ __forceinline__ float* operator[](int k) const { return k == 0 ? x : k == 1 ? y : z; }
+};
+
+// Warp sum of a 64-bit int, stored in the warp's slot of slots[32].
+__device__ __forceinline__ void warp_store_ll(long long v, long long* slots) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(ISG_FULL_MASK, v, o);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) red[w] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (threadIdx.x < 32) {
-        t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(ISG_FULL_MASK, t, o);
-    }
-    return t;  // valid in thread 0
+    if ((threadIdx.x & 31) == 0) slots[threadIdx.x >> 5] = v;
 }
 
-// E = -J sum_bonds S.S' (as half the sum over nodes of S.h) and M.
-template <int NC>
-__device__ void cg_measure(const CGraphParams& P, float* const* s, double* red, double& e_out,
-                           double* m_out) {
-    double e = 0.0, m[NC];
-#pragma unroll
-    for (int k = 0; k < NC; ++k) m[k] = 0.0;
+// Fixed point of the measurement sums: 2^40 units per spin component.  Every
+// node term (|S.h| <= 64, |S_k| <= 1) converts exactly up to 2^-41, the int64
+// sums are exact and independent of their order (|sum| < 2^61).
+constexpr float kFixScale = 1099511627776.0f;
+constexpr double kFixInv = 1.0 / 1099511627776.0;
+
+__device__ __forceinline__ long long fix(float x) { return __float2ll_rn(x * kFixScale); }
+
+// O(2) measurement by gathering every node's neighbour field: per-warp sums
+// of sum_v S_v.h_v (twice the bond sum) and M in acc[0..2][32] (all threads
+// call).
+__device__ __forceinline__ void cg_measure_xy(const CGraphParams& P, const Planes& s,
+                                              long long (*acc)[32]) {
+    long long e = 0, m0 = 0, m1 = 0;
     for (int v = threadIdx.x; v < P.n; v += blockDim.x) {
         const int r0 = __ldg(P.rowptr + v), r1 = __ldg(P.rowptr + v + 1);
-        float h[NC];
-#pragma unroll
-        for (int k = 0; k < NC; ++k) h[k] = 0.f;
+        float hx = 0.f, hy = 0.f;
         for (int j = r0; j < r1; ++j) {
             const int u = __ldg(P.adj + j);
-#pragma unroll
-            for (int k = 0; k < NC; ++k) h[k] += s[k][u];
+            hx += s[0][u];
+            hy += s[1][u];
         }
-        float d = 0.f;
-#pragma unroll
-        for (int k = 0; k < NC; ++k) {
-            d = fmaf(s[k][v], h[k], d);
-            m[k] += (double)s[k][v];
-        }
-        e += (double)d;
+        const float sx = s[0][v], sy = s[1][v];
+        e += fix(fmaf(sx, hx, sy * hy));
+        m0 += fix(sx);
+        m1 += fix(sy);
     }
-    const double te = block_sum_d(e, red);
-    e_out = -0.5 * (double)P.J * te;
-#pragma unroll
-    for (int k = 0; k < NC; ++k) m_out[k] = block_sum_d(m[k], red);
+    warp_store_ll(e, acc[0]);
+    warp_store_ll(m0, acc[1]);
+    warp_store_ll(m1, acc[2]);
 }
 
-// One cone-Metropolis sweep of an O(3) replica (spins in shared memory).
-__device__ void cg_metropolis(const CGraphParams& P, float* const* s, int r, uint64_t sweep,
-                              float beta, unsigned long long& acc) {
+// One cone-Metropolis sweep of an O(3) replica (spins in shared memory).  With
+// `meas`, also adds sum_v S_v.h<_v (h< = the field of the lower-colour
+// neighbours, final when v is updated, so every bond counts once with final
+// spins) and M as per-warp sums in acc[0..3][32] before the last class's
+// barrier.
+__device__ __forceinline__ void cg_metropolis(const CGraphParams& P, const Planes& s, int r,
+                                              uint64_t sweep, float beta, bool meas,
+                                              long long (*acc)[32], unsigned long long& moves) {
     const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    long long pe = 0, pm0 = 0, pm1 = 0, pm2 = 0;
     for (int c = 0; c < P.n_classes; ++c) {
         const uint32_t c3 = counter_word3(kTagCGraph, (uint32_t)c, sweep);
         const int a = __ldg(P.cstart + c), b = __ldg(P.cstart + c + 1);
         for (int q = a + threadIdx.x; q < b; q += blockDim.x) {
             const int v = __ldg(P.order + q);
             const int r0 = __ldg(P.rowptr + v), r1 = __ldg(P.rowptr + v + 1);
-            float h[3] = {0.f, 0.f, 0.f};
-            for (int j = r0; j < r1; ++j) {
+            const int rl = r0 + __ldg(P.nlow + v);
+            float l0 = 0.f, l1 = 0.f, l2 = 0.f, h0 = 0.f, h1 = 0.f, h2 = 0.f;
+            for (int j = r0; j < rl; ++j) {
                 const int u = __ldg(P.adj + j);
-                h[0] += s[0][u];
-                h[1] += s[1][u];
-                h[2] += s[2][u];
+                l0 += s[0][u];
+                l1 += s[1][u];
+                l2 += s[2][u];
             }
+            for (int j = rl; j < r1; ++j) {
+                const int u = __ldg(P.adj + j);
+                h0 += s[0][u];
+                h1 += s[1][u];
+                h2 += s[2][u];
+            }
+            const float hx = l0 + h0, hy = l1 + h1, hz = l2 + h2;
             const float v0 = s[0][v], v1 = s[1][v], v2 = s[2][v];
             const U4 u = philox10((uint32_t)r, (uint32_t)v, (uint32_t)sweep, c3, k0, k1);
             const float ct = 1.0f - uniform24(u.x) * (1.0f - P.cos_delta);
@@ -178,23 +194,42 @@ __device__ void cg_metropolis(const CGraphParams& P, float* const* s, int r, uin
             w0 *= wn;
             w1 *= wn;
             w2 *= wn;
-            float dot = (w0 - v0) * h[0];
-            dot = fmaf(w1 - v1, h[1], dot);
-            dot = fmaf(w2 - v2, h[2], dot);
+            float dot = (w0 - v0) * hx;
+            dot = fmaf(w1 - v1, hy, dot);
+            dot = fmaf(w2 - v2, hz, dot);
             const float dE = -P.J * dot;
+            float f0 = v0, f1 = v1, f2 = v2;
             if (dE <= 0.0f || uniform24(u.z) < expf(-beta * dE)) {
                 s[0][v] = w0;
                 s[1][v] = w1;
                 s[2][v] = w2;
-                ++acc;
+                f0 = w0;
+                f1 = w1;
+                f2 = w2;
+                ++moves;
             }
+            if (meas) {
+                pe += fix(fmaf(f0, l0, fmaf(f1, l1, f2 * l2)));
+                pm0 += fix(f0);
+                pm1 += fix(f1);
+                pm2 += fix(f2);
+            }
+        }
+        if (meas && c == P.n_classes - 1) {
+            warp_store_ll(pe, acc[0]);
+            warp_store_ll(pm0, acc[1]);
+            warp_store_ll(pm1, acc[2]);
+            warp_store_ll(pm2, acc[3]);
         }
         __syncthreads();
     }
 }
 
-// One single-cluster Wolff flip of an O(2) replica.
-__device__ void cg_wolff(const CGraphParams& P, float* const* s, uint32_t* inb, int32_t* queue,
+// One single-cluster Wolff flip of an O(2) replica.  Level-synchronous
+// growth with one barrier per level: level L holds queue[base, base + cnt)
+// and appends level L+1 after it through counter ctl[(L+1) % 3]; the counter
+// of level L+2 is cleared during level L, when no thread reads or bumps it.
+__device__ __forceinline__ void cg_wolff(const CGraphParams& P, const Planes& s, uint32_t* inb, int32_t* queue,
                          int* ctl, int r, uint64_t sweep, float beta) {
     const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
     const int nwords = (P.n + 31) >> 5;
@@ -211,44 +246,51 @@ __device__ void cg_wolff(const CGraphParams& P, float* const* s, uint32_t* inb, 
         const int seed_node = (int)(((uint64_t)u.y * (uint64_t)P.n) >> 32);
         inb[seed_node >> 5] = 1u << (seed_node & 31);
         queue[0] = seed_node;
-        ctl[0] = 1;  // queue tail
+        ctl[0] = 1;  // level 0: the seed
+        ctl[1] = 0;
+        ctl[2] = 0;
     }
+    __syncthreads();
     const float twobj = 2.0f * beta * P.J;
-    int head = 0;
-    for (;;) {
-        __syncthreads();
-        const int tail = ctl[0];
-        if (head == tail) break;
-        __syncthreads();  // every thread has read the tail before it grows
-        const float rx = s_r[0], ry = s_r[1];
-        for (int q = head + threadIdx.x; q < tail; q += blockDim.x) {
-            const int i = queue[q];
+    const float rx = s_r[0], ry = s_r[1];
+    int base = 0, level = 0;
+    int cnt = ctl[0];
+    // a level-L node is at distance L from the seed, so there are at most n levels
+    while (cnt > 0 && level < P.n) {
+        int* next = &ctl[(level + 1) % 3];
+        if (threadIdx.x == 0) ctl[(level + 2) % 3] = 0;
+        const int end = base + cnt;
+        // one (frontier node, adjacency slot) test per thread
+        const int tasks = cnt * P.max_deg;
+        for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+            const int qo = t / P.max_deg;
+            const int k = t - qo * P.max_deg;
+            const int i = queue[base + qo];
+            const int r0 = __ldg(P.rowptr + i);
+            if (k >= __ldg(P.rowptr + i + 1) - r0) continue;
+            const int j = __ldg(P.adj + r0 + k);
+            const uint32_t bit = 1u << (j & 31);
+            if (inb[j >> 5] & bit) continue;
             const float pi = s[0][i] * rx + s[1][i] * ry;
-            const int r0 = __ldg(P.rowptr + i), r1 = __ldg(P.rowptr + i + 1);
-            U4 u{0u, 0u, 0u, 0u};
-            for (int k = 0; k < r1 - r0; ++k) {
-                const int j = __ldg(P.adj + r0 + k);
-                if ((k & 3) == 0)
-                    u = philox10((uint32_t)r, (uint32_t)i, (uint32_t)sweep,
-                                 counter_word3(kTagCGraph, 0xC0u + ((uint32_t)k >> 2), sweep), k0,
-                                 k1);
-                const uint32_t bit = 1u << (j & 31);
-                if (inb[j >> 5] & bit) continue;
-                const float pj = s[0][j] * rx + s[1][j] * ry;
-                if (pi * pj <= 0.0f) continue;
-                const float p = 1.0f - expf(-twobj * fabsf(pi) * fabsf(pj));
-                const uint32_t wk = (k & 3) == 0 ? u.x : (k & 3) == 1 ? u.y : (k & 3) == 2 ? u.z : u.w;
-                if (uniform24(wk) < p) {
-                    const uint32_t old = atomicOr(&inb[j >> 5], bit);
-                    if (!(old & bit)) queue[atomicAdd(&ctl[0], 1)] = j;
-                }
+            const float pj = s[0][j] * rx + s[1][j] * ry;
+            if (pi * pj <= 0.0f) continue;
+            const float p = 1.0f - expf(-twobj * fabsf(pi) * fabsf(pj));
+            const U4 u = philox10((uint32_t)r, (uint32_t)i, (uint32_t)sweep,
+                                  counter_word3(kTagCGraph, 0xC0u + ((uint32_t)k >> 2), sweep), k0,
+                                  k1);
+            const uint32_t wk = (k & 3) == 0 ? u.x : (k & 3) == 1 ? u.y : (k & 3) == 2 ? u.z : u.w;
+            if (uniform24(wk) < p) {
+                const uint32_t old = atomicOr(&inb[j >> 5], bit);
+                if (!(old & bit)) queue[end + atomicAdd(next, 1)] = j;
             }
         }
-        head = tail;
+        __syncthreads();
+        base = end;
+        cnt = *next;
+        ++level;
     }
-    // reflect the cluster and renormalise
-    const float rx = s_r[0], ry = s_r[1];
-    for (int q = threadIdx.x; q < head; q += blockDim.x) {
+    // reflect the cluster (queue[0, base)) and renormalise
+    for (int q = threadIdx.x; q < base; q += blockDim.x) {
         const int i = queue[q];
         float a = s[0][i], b = s[1][i];
         const float d = a * rx + b * ry;
@@ -258,18 +300,24 @@ __device__ void cg_wolff(const CGraphParams& P, float* const* s, uint32_t* inb, 
         s[0][i] = a * nr;
         s[1][i] = b * nr;
     }
+    if (threadIdx.x == 0) ctl[0] = base;  // cluster size for the move counter
     __syncthreads();
 }
 
+// n_sweeps sweeps of every replica (block = replica).  A measured sweep's
+// per-warp sums go to one of two alternating slot sets; thread 0 adds them
+// after the barrier that follows, and the set is written again two
+// measurements later, after another barrier.
 template <int NC>
-__global__ void __launch_bounds__(kCGThreads) k_cgraph_sweeps(const __grid_constant__ CGraphParams P) {
+__global__ void __launch_bounds__(kCGThreads, 1) k_cgraph_sweeps(const __grid_constant__ CGraphParams P) {
     extern __shared__ float cg_smem[];
-    __shared__ double red[32];
-    __shared__ int ctl[1];
+    __shared__ long long s_acc[2][4][32];
+    __shared__ int ctl[3];
     const int r = blockIdx.x;
-    float* s[NC];
-#pragma unroll
-    for (int k = 0; k < NC; ++k) s[k] = cg_smem + (size_t)k * P.n;
+    Planes s;
+    s.x = cg_smem;
+    s.y = cg_smem + P.n;
+    s.z = NC == 3 ? cg_smem + 2 * (size_t)P.n : cg_smem;
     uint32_t* inb = reinterpret_cast<uint32_t*>(cg_smem + (size_t)NC * P.n);
     int32_t* queue = reinterpret_cast<int32_t*>(inb + ((P.n + 31) >> 5));
     float* g = P.spins + (size_t)r * NC * P.n;
@@ -279,29 +327,47 @@ __global__ void __launch_bounds__(kCGThreads) k_cgraph_sweeps(const __grid_const
     __syncthreads();
     unsigned long long moves = 0;
     int64_t row = P.row0;
+    int mb = 0;
     for (int k = 0; k < P.n_sweeps; ++k) {
         const uint64_t sweep = P.sweep0 + (uint64_t)k;
+        const bool rec = P.measure_every > 0 && k % P.measure_every == P.measure_phase;
+        const bool meas = rec || k == P.n_sweeps - 1;
         if (NC == 3) {
-            cg_metropolis(P, s, r, sweep, beta, moves);
+            cg_metropolis(P, s, r, sweep, beta, meas, s_acc[mb], moves);
         } else {
             cg_wolff(P, s, inb, queue, ctl, r, sweep, beta);
             if (threadIdx.x == 0) moves += (unsigned long long)ctl[0];
-        }
-        if (P.measure_every > 0 && k % P.measure_every == P.measure_phase) {
-            double e, m[NC];
-            cg_measure<NC>(P, s, red, e, m);
-            if (threadIdx.x == 0) {
-                P.rec_e[row * P.R + r] = e;
-#pragma unroll
-                for (int c = 0; c < NC; ++c) P.rec_m[(row * P.R + r) * NC + c] = m[c];
-                P.rec_t[row * P.R + r] = slot;
+            if (meas) {
+                cg_measure_xy(P, s, s_acc[mb]);
+                __syncthreads();
             }
-            ++row;
         }
+        if (meas) {
+            if (threadIdx.x == 0) {
+                long long a[NC + 1];
+#pragma unroll
+                for (int c = 0; c <= NC; ++c) a[c] = 0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+#pragma unroll
+                    for (int c = 0; c <= NC; ++c) a[c] += s_acc[mb][c][w];
+                // O(3): each bond once; O(2): every bond from both ends
+                const double bonds = (double)a[0] * kFixInv * (NC == 3 ? 1.0 : 0.5);
+                const double e = -(double)P.J * bonds;
+                double m[NC];
+#pragma unroll
+                for (int c = 0; c < NC; ++c) m[c] = (double)a[1 + c] * kFixInv;
+                if (rec) {
+                    P.rec_e[row * P.R + r] = e;
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) P.rec_m[(row * P.R + r) * NC + c] = m[c];
+                    P.rec_t[row * P.R + r] = slot;
+                }
+                if (k == P.n_sweeps - 1) P.last_e[r] = e;
+            }
+            mb ^= 1;
+        }
+        if (rec) ++row;
     }
-    double e, m[NC];
-    cg_measure<NC>(P, s, red, e, m);
-    if (threadIdx.x == 0) P.last_e[r] = e;
     // per-replica move counter: warp sums then one atomic per warp
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) moves += __shfl_down_sync(ISG_FULL_MASK, moves, o);
@@ -343,7 +409,7 @@ using namespace isg;
 
 struct isg_cgraph {
     int device = 0;
-    int n = 0, m = 0, R = 0, nc = 3, n_classes = 0;
+    int n = 0, m = 0, R = 0, nc = 3, n_classes = 0, max_deg = 1;
     uint64_t seed = 0;
     double J = 1.0, delta = 0.5;
     bool temps_set = false;
@@ -354,6 +420,7 @@ struct isg_cgraph {
     int32_t* d_adj = nullptr;
     int32_t* d_order = nullptr;
     int32_t* d_cstart = nullptr;
+    int32_t* d_nlow = nullptr;
     float* d_spins = nullptr;
     float* d_betaf = nullptr;
     double* d_betas = nullptr;
@@ -379,6 +446,7 @@ int cg_destroy(isg_cgraph* H) {
     cudaFree(H->d_adj);
     cudaFree(H->d_order);
     cudaFree(H->d_cstart);
+    cudaFree(H->d_nlow);
     cudaFree(H->d_spins);
     cudaFree(H->d_betaf);
     cudaFree(H->d_betas);
@@ -401,6 +469,7 @@ int cg_launch(isg_cgraph* H, int n_sweeps, int every, int phase, int64_t row0) {
     P.adj = H->d_adj;
     P.order = H->d_order;
     P.cstart = H->d_cstart;
+    P.nlow = H->d_nlow;
     P.spins = H->d_spins;
     P.betaf = H->d_betaf;
     P.r2t = H->d_r2t;
@@ -416,6 +485,7 @@ int cg_launch(isg_cgraph* H, int n_sweeps, int every, int phase, int64_t row0) {
     P.n = H->n;
     P.R = H->R;
     P.n_classes = H->n_classes;
+    P.max_deg = H->max_deg;
     P.n_sweeps = n_sweeps;
     P.measure_every = every;
     P.measure_phase = phase;
@@ -484,6 +554,20 @@ int isg_cgraph_create(isg_cgraph** out, int n_nodes, const int32_t* edges, int n
         col[v] = c;
         ncol = std::max(ncol, c + 1);
     }
+    // O(3): each node's lower-colour neighbours first (stable), counted in nlow
+    std::vector<int32_t> nlow(n_nodes, 0);
+    if (n_comp == 3) {
+        std::vector<int32_t> tmp;
+        for (int v = 0; v < n_nodes; ++v) {
+            tmp.clear();
+            for (int j = rowptr[v]; j < rowptr[v + 1]; ++j)
+                if (col[adj[j]] < col[v]) tmp.push_back(adj[j]);
+            nlow[v] = (int32_t)tmp.size();
+            for (int j = rowptr[v]; j < rowptr[v + 1]; ++j)
+                if (col[adj[j]] > col[v]) tmp.push_back(adj[j]);
+            std::copy(tmp.begin(), tmp.end(), adj.begin() + rowptr[v]);
+        }
+    }
     std::vector<int32_t> cstart(ncol + 1, 0), order(n_nodes);
     for (int v = 0; v < n_nodes; ++v) ++cstart[col[v] + 1];
     for (int c = 0; c < ncol; ++c) cstart[c + 1] += cstart[c];
@@ -499,6 +583,7 @@ int isg_cgraph_create(isg_cgraph** out, int n_nodes, const int32_t* edges, int n
     H->nc = n_comp;
     H->seed = seed;
     H->n_classes = ncol;
+    H->max_deg = std::max(1, *std::max_element(deg.begin(), deg.end()));
     // spins (+ cluster bitmask and queue for O(2)) in dynamic shared memory
     H->smem = sizeof(float) * (size_t)n_comp * n_nodes;
     if (n_comp == 2) H->smem += sizeof(uint32_t) * ((n_nodes + 31) / 32) + sizeof(int32_t) * n_nodes;
@@ -513,6 +598,7 @@ int isg_cgraph_create(isg_cgraph** out, int n_nodes, const int32_t* edges, int n
     CGALLOC(H->d_adj, sizeof(int32_t) * adj.size());
     CGALLOC(H->d_order, sizeof(int32_t) * n_nodes);
     CGALLOC(H->d_cstart, sizeof(int32_t) * (ncol + 1));
+    CGALLOC(H->d_nlow, sizeof(int32_t) * n_nodes);
     CGALLOC(H->d_spins, sizeof(float) * (size_t)n_comp * n_nodes * replicas);
     CGALLOC(H->d_betaf, sizeof(float) * replicas);
     CGALLOC(H->d_betas, sizeof(double) * replicas);
@@ -555,6 +641,8 @@ int isg_cgraph_create(isg_cgraph** out, int n_nodes, const int32_t* edges, int n
     CGCK(cudaMemcpyAsync(H->d_order, order.data(), sizeof(int32_t) * n_nodes,
                          cudaMemcpyHostToDevice, H->stream));
     CGCK(cudaMemcpyAsync(H->d_cstart, cstart.data(), sizeof(int32_t) * cstart.size(),
+                         cudaMemcpyHostToDevice, H->stream));
+    CGCK(cudaMemcpyAsync(H->d_nlow, nlow.data(), sizeof(int32_t) * n_nodes,
                          cudaMemcpyHostToDevice, H->stream));
     CGCK(cudaMemcpyAsync(H->d_r2t, ident.data(), sizeof(int32_t) * replicas,
                          cudaMemcpyHostToDevice, H->stream));

@@ -54,6 +54,8 @@ struct GraphParams {
     long long* rec_m;
     int32_t* rec_t;
     double* last_e;          // [R] energy -J * bond after the launch's last sweep
+    long long* last_bm;      // [R][2] bond sum and magnetisation after the last sweep
+    int bm_known;            // last_bm holds the current state (else measure first)
     double J;
     uint64_t seed;
     uint64_t sweep0;         // global sweep of the launch's first sweep
@@ -63,18 +65,22 @@ struct GraphParams {
     int64_t row0;            // record row of the first measured sweep
 };
 
-__device__ __forceinline__ int g_block_sum(int v, int* red) {
-    v = __reduce_add_sync(ISG_FULL_MASK, v);
+// Block sums of two ints in one pass (valid in thread 0); red holds 64 ints.
+__device__ __forceinline__ void g_block_sum2(int& a, int& b, int* red) {
+    a = __reduce_add_sync(ISG_FULL_MASK, a);
+    b = __reduce_add_sync(ISG_FULL_MASK, b);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     __syncthreads();
-    if (lane == 0) red[w] = v;
-    __syncthreads();
-    int t = 0;
-    if (threadIdx.x < 32) {
-        t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0;
-        t = __reduce_add_sync(ISG_FULL_MASK, t);
+    if (lane == 0) {
+        red[w] = a;
+        red[32 + w] = b;
     }
-    return t;  // valid in thread 0
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const bool in = threadIdx.x < (blockDim.x >> 5);
+        a = __reduce_add_sync(ISG_FULL_MASK, in ? red[threadIdx.x] : 0);
+        b = __reduce_add_sync(ISG_FULL_MASK, in ? red[32 + threadIdx.x] : 0);
+    }
 }
 
 // Bond sum sum_edges s_u s_v = (1/2) sum_v s_v (deg_v - 2 n_down(v)) and
@@ -90,18 +96,32 @@ __device__ __forceinline__ void g_measure(const GraphParams& P, const uint8_t* s
         b += s * ((r1 - r0) - 2 * nd);
         m += s;
     }
-    const int tb = g_block_sum(b, red);
-    const int tm = g_block_sum(m, red);
-    bond = tb / 2;
-    mag = tm;
+    g_block_sum2(b, m, red);
+    bond = b / 2;
+    mag = m;
+}
+
+// Warp sum of a 64-bit int, stored in the warp's slot of slots[32].
+__device__ __forceinline__ void g_warp_store(long long v, long long* slots) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(ISG_FULL_MASK, v, o);
+    if ((threadIdx.x & 31) == 0) slots[threadIdx.x >> 5] = v;
 }
 
 // n_sweeps sweeps of every replica (block = replica), spins staged in shared
-// memory; records after the measured sweeps and the final bond sum.
+// memory; records after the measured sweeps and the final energy.  The bond
+// sum and magnetisation of the previous launch (or one measurement on the
+// first launch) are advanced by the exact integer change of every flip,
+// -2 s (deg - 2 n_down) and -2 s: the nodes of a class share no edge, so the
+// changes of one class add up.  A record costs one warp reduction per warp
+// before the last class's barrier (each warp stores its sum in its slot of
+// one of two alternating slot sets) and thread 0 adds the slots after it;
+// a slot set is written again two measurements later, after another barrier.
 __global__ void __launch_bounds__(kGThreads) k_graph_sweeps(const __grid_constant__ GraphParams P) {
     extern __shared__ uint8_t g_sp[];
     __shared__ uint32_t s_tab[kGTab];
-    __shared__ int red[32];
+    __shared__ int red[64];
+    __shared__ long long s_acc[2][2][32];
     const int r = blockIdx.x;
     uint8_t* spins = P.spins + (size_t)r * P.n;
     for (int v = threadIdx.x; v < P.n; v += blockDim.x) g_sp[v] = spins[v];
@@ -109,9 +129,21 @@ __global__ void __launch_bounds__(kGThreads) k_graph_sweeps(const __grid_constan
     for (int e = threadIdx.x; e < kGTab; e += blockDim.x) s_tab[e] = P.thr[(size_t)slot * kGTab + e];
     __syncthreads();
     const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    long long bond0 = 0, mag0 = 0;  // valid in thread 0
+    if (P.bm_known) {
+        bond0 = P.last_bm[2 * r];
+        mag0 = P.last_bm[2 * r + 1];
+    } else {
+        g_measure(P, g_sp, red, bond0, mag0);
+    }
+    long long db = 0, dm = 0;  // this thread's flips since the launch start
+    int mb = 0;
     int64_t row = P.row0;
+    const int last_class = P.n_classes - 1;
     for (int k = 0; k < P.n_sweeps; ++k) {
         const uint64_t sweep = P.sweep0 + (uint64_t)k;
+        const bool rec = P.measure_every > 0 && k % P.measure_every == P.measure_phase;
+        const bool meas = rec || k == P.n_sweeps - 1;
         for (int c = 0; c < P.n_classes; ++c) {
             const uint32_t c3 = counter_word3(ISG_TAG_GRAPH, (uint32_t)c, sweep);
             const int a = __ldg(P.cstart + c), b = __ldg(P.cstart + c + 1);
@@ -125,24 +157,41 @@ __global__ void __launch_bounds__(kGThreads) k_graph_sweeps(const __grid_constan
                 const U4 u = philox10((uint32_t)r, (uint32_t)v >> 2, (uint32_t)sweep, c3, k0, k1);
                 const uint32_t jv = (uint32_t)v & 3u;
                 const uint32_t uw = jv == 0 ? u.x : jv == 1 ? u.y : jv == 2 ? u.z : u.w;
-                if (uw <= th) g_sp[v] = (uint8_t)(d ^ 1);
+                if (uw <= th) {
+                    g_sp[v] = (uint8_t)(d ^ 1);
+                    const int s_old = 1 - 2 * d;
+                    db -= 2 * s_old * ((r1 - r0) - 2 * nd);
+                    dm -= 2 * s_old;
+                }
+            }
+            if (meas && c == last_class) {
+                g_warp_store(db, s_acc[mb][0]);
+                g_warp_store(dm, s_acc[mb][1]);
             }
             __syncthreads();
         }
-        if (P.measure_every > 0 && k % P.measure_every == P.measure_phase) {
-            long long bb, mm;
-            g_measure(P, g_sp, red, bb, mm);
+        if (meas) {
             if (threadIdx.x == 0) {
-                P.rec_b[row * P.R + r] = bb;
-                P.rec_m[row * P.R + r] = mm;
-                P.rec_t[row * P.R + r] = slot;
+                long long bb = bond0, mm = mag0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+                    bb += s_acc[mb][0][w];
+                    mm += s_acc[mb][1][w];
+                }
+                if (rec) {
+                    P.rec_b[row * P.R + r] = bb;
+                    P.rec_m[row * P.R + r] = mm;
+                    P.rec_t[row * P.R + r] = slot;
+                }
+                if (k == P.n_sweeps - 1) {
+                    P.last_e[r] = -__dmul_rn(P.J, (double)bb);
+                    P.last_bm[2 * r] = bb;
+                    P.last_bm[2 * r + 1] = mm;
+                }
             }
-            ++row;
+            mb ^= 1;
         }
+        if (rec) ++row;
     }
-    long long bb, mm;
-    g_measure(P, g_sp, red, bb, mm);
-    if (threadIdx.x == 0) P.last_e[r] = -__dmul_rn(P.J, (double)bb);
     for (int v = threadIdx.x; v < P.n; v += blockDim.x) spins[v] = g_sp[v];
 }
 
@@ -234,6 +283,8 @@ struct isg_graph {
     int32_t* d_t2r = nullptr;
     double* d_betas = nullptr;
     double* d_last_e = nullptr;
+    long long* d_last_bm = nullptr;
+    bool bm_known = false;
     unsigned long long* d_ctrl = nullptr;  // [0] exchange count, [1] accepted
     long long* d_rec_b = nullptr;
     long long* d_rec_m = nullptr;
@@ -258,6 +309,7 @@ int g_destroy(isg_graph* H) {
     cudaFree(H->d_t2r);
     cudaFree(H->d_betas);
     cudaFree(H->d_last_e);
+    cudaFree(H->d_last_bm);
     cudaFree(H->d_ctrl);
     cudaFree(H->d_rec_b);
     cudaFree(H->d_rec_m);
@@ -280,6 +332,8 @@ GraphParams g_params(isg_graph* H) {
     P.rec_m = H->d_rec_m;
     P.rec_t = H->d_rec_t;
     P.last_e = H->d_last_e;
+    P.last_bm = H->d_last_bm;
+    P.bm_known = H->bm_known ? 1 : 0;
     P.J = H->J;
     P.seed = H->seed;
     P.n = H->n;
@@ -299,6 +353,7 @@ int g_launch(isg_graph* H, int n_sweeps, int every, int phase, int64_t row0) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "k_graph_sweeps");
     H->gsweep += (uint64_t)n_sweeps;
+    if (n_sweeps > 0) H->bm_known = true;
     return ISG_OK;
 }
 
@@ -385,6 +440,7 @@ int isg_graph_create(isg_graph** out, int n_nodes, const int32_t* edges, int n_e
     GALLOC(H->d_t2r, sizeof(int32_t) * replicas);
     GALLOC(H->d_betas, sizeof(double) * replicas);
     GALLOC(H->d_last_e, sizeof(double) * replicas);
+    GALLOC(H->d_last_bm, sizeof(long long) * 2 * replicas);
     GALLOC(H->d_ctrl, sizeof(unsigned long long) * 2);
 #undef GALLOC
     e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);

@@ -483,6 +483,79 @@ int isg_cgraph_get_r2t(isg_cgraph* h, int32_t* r2t);
 int isg_cgraph_get_sweep(isg_cgraph* h, uint64_t* sweep);
 
 /* ------------------------------------------------------------------------ */
+/* Energy histograms and reweighting (the consumers of the PT timeseries)    */
+/* ------------------------------------------------------------------------ */
+
+/* Device energy histograms of an Ising batch, accumulated by every record of
+ * isg_ising_pt_run (not by isg_ising_run_schedule): per size and temperature
+ * slot, exact bins of the bond sum B (bin b holds B = 4 b - dN, d = dim,
+ * N = L^d; B + dN is always a multiple of 4 on a periodic even lattice), each
+ * with 4 uint64 counters: samples, and the sums of |m|, m^2, m^4 (m = M / N) in
+ * units of 2^-32 (each term rounded to nearest).  With h = 0 the energy of a bin
+ * is E = -J B, so histogram reweighting in temperature is exact.  Replaces the
+ * per-sample (E, |m|) timeseries that analysis/scripts/analyze_gpu_fss.py:60-83
+ * reads for reweighting.  Full-range bins: dN/2 + 1 per slot, 32 bytes each.
+ * enable = 0 frees them; enabling again clears them. */
+int isg_ising_hist_enable(isg_ising* h, int enable);
+int isg_ising_hist_reset(isg_ising* h);
+/* Visited bins of (size, slot): *bond_lo = B of the lowest, *n_bins = number
+ * from the lowest to the highest (0 if no record yet). */
+int isg_ising_hist_range(isg_ising* h, int size_index, int slot, int64_t* bond_lo,
+                         int64_t* n_bins);
+/* out[4*i + {0..3}] = counters of the bin with B = bond_lo + 4 i. */
+int isg_ising_hist_read(isg_ising* h, int size_index, int slot, int64_t bond_lo, int64_t n_bins,
+                        uint64_t* out);
+
+/* Multiple-histogram (WHAM) reweighting, analysis/scripts/reweighting.py:45-105
+ * and analyze_gpu_fss.py:160-243, on the GPU in FP64.  P points: energy e[p]
+ * (total), weight c[p] (1 for a sample, the count of a histogram bin), moment
+ * sums mom[p*n_mom + j] (n_mom <= 8; e.g. the point's sums of |m|, m^2, m^4).
+ * K simulations: beta[k], sample counts n_k[k].  The free energies f_k
+ * (f_0 = 0) iterate as the reference does (at most n_iter rounds, stop when
+ * max |f' - f| < tol; the weights use the last round's denominators).  For T
+ * targets beta_t: out[t*(3+n_mom) + {0, 1, 2, 3+j}] = log Z, <E>, <E^2>, <mom_j>
+ * with <mom_j> = sum_p w_p mom_pj / sum_p w_p c_p.  f_out[K], iters_out may be
+ * NULL. */
+int isg_wham(const double* e, const double* c, const double* mom, int n_mom, int64_t P,
+             const double* beta, const double* n_k, int K, int n_iter, double tol,
+             const double* beta_t, int T, double* out, double* f_out, int* iters_out);
+/* The reference's normalised per-point weights at one target (wham_reweight's
+ * w): w[p] = c_p exp(-beta_t E_p - log_denom_p) / Z. */
+int isg_wham_weights(const double* e, const double* c, int64_t P, const double* beta,
+                     const double* n_k, int K, int n_iter, double tol, double beta_t, double* w,
+                     double* f_out, int* iters_out);
+/* Single-histogram reweighting (reweighting.py:15-43, analyze_gpu_fss.py:86-157):
+ * target t reweights the points [p0[t], p1[t]) of the simulation at beta_ref[t],
+ * leaving out [x0[t], x1[t]) (x0 = x1 = NULL: none; a jackknife block), by
+ * exp(-(beta_t - beta_ref) E); out as isg_wham. */
+int isg_reweight_single(const double* e, const double* c, const double* mom, int n_mom, int64_t P,
+                        const int64_t* p0, const int64_t* p1, const int64_t* x0, const int64_t* x1,
+                        const double* beta_ref, const double* beta_t, int T, double* out);
+
+/* Binary timeseries file (the compact form of gpu_fss_{model}_N{n}_timeseries.csv,
+ * src/bin/gpu_fss.rs:212-290), little-endian:
+ *   char magic[8] = "ISGTSER1"; uint32 header_bytes = 32 + 8 n_temps;
+ *   uint32 model (0 ising, 1 heisenberg, 2 xy); uint32 n; uint32 n_temps;
+ *   uint64 reserved = 0; double temps[n_temps];
+ *   then records to the end of the file, 24 bytes each:
+ *   uint32 temp_idx; uint32 replica; double E (per spin); double M (|m| per spin).
+ * Host-only calls (no device work). */
+typedef struct isg_ts isg_ts;
+int isg_ts_open(isg_ts** out, const char* path, int model, int n, const double* temps,
+                int n_temps);
+int isg_ts_append(isg_ts* f, const int32_t* temp_idx, const int32_t* replica, const double* e,
+                  const double* m, int64_t count);
+int isg_ts_close(isg_ts* f);
+/* Histogram file (gpu_fss_ising_N{n}_hist.bin), little-endian:
+ *   char magic[8] = "ISGHIST1"; uint32 header_bytes = 32 + 8 n_temps;
+ *   uint32 dim; uint32 n; uint32 n_temps; double J; double temps[n_temps];
+ *   then per temperature: int64 bond_lo; int64 n_bins; n_bins x 4 uint64
+ *   (the isg_ising_hist_read counters).  counters holds the temperatures'
+ *   blocks one after another. */
+int isg_hist_write(const char* path, int dim, int n, double J, const double* temps, int n_temps,
+                   const int64_t* bond_lo, const int64_t* n_bins, const uint64_t* counters);
+
+/* ------------------------------------------------------------------------ */
 /* Statistics used by the drop-in driver                                     */
 /* ------------------------------------------------------------------------ */
 

@@ -20,6 +20,13 @@ backend for the checkerboard PT path:
                         FCC and diluted-cubic builders
   GraphBatch            Ising PT on a graph (src/bin/gpu_jfit.rs:172-297)
   ContinuousGraphBatch  Heisenberg / XY PT on a graph (gpu_jfit.rs:298-524)
+  single_histogram, reweight_observable, wham_reweight, reweight_binder
+                        analysis/scripts/reweighting.py:15-143 (on the GPU)
+  reweight_single_histogram, wham_reweight_fine
+                        analysis/scripts/analyze_gpu_fss.py:86-243
+  IsingBatch.hist_*, wham_histograms, read/write_timeseries, read_histograms
+                        device energy histograms and the binary files of the
+                        PT timeseries (include/isg.h)
   IsingBatch / ContinuousBatch: every (size, replica) lattice of a run in one
   handle (the GB300 replacement of the reference's Vec<LatticeGpu>).
 
@@ -128,6 +135,17 @@ def _declare(L):
         "isg_cgraph_get_r2t": [vp, vp],
         "isg_cgraph_get_sweep": [vp, vp],
         "isg_coarsening": [i32, dbl, dbl, dbl, i64, i64, i64, u64, vp, vp, i64, vp],
+        "isg_ising_hist_enable": [vp, i32],
+        "isg_ising_hist_reset": [vp],
+        "isg_ising_hist_range": [vp, i32, i32, vp, vp],
+        "isg_ising_hist_read": [vp, i32, i32, i64, i64, vp],
+        "isg_wham": [vp, vp, vp, i32, i64, vp, vp, i32, i32, dbl, vp, i32, vp, vp, vp],
+        "isg_wham_weights": [vp, vp, i64, vp, vp, i32, i32, dbl, dbl, vp, vp, vp],
+        "isg_reweight_single": [vp, vp, vp, i32, i64, vp, vp, vp, vp, vp, vp, i32, vp],
+        "isg_ts_open": [C.POINTER(vp), C.c_char_p, i32, i32, vp, i32],
+        "isg_ts_append": [vp, vp, vp, vp, vp, i64],
+        "isg_ts_close": [vp],
+        "isg_hist_write": [C.c_char_p, i32, i32, dbl, vp, i32, vp, vp, vp],
         "isg_cont_create": [C.POINTER(vp), vp, i32, i32, i32, u64],
         "isg_cont_destroy": [vp],
         "isg_cont_set_stream": [vp, vp],
@@ -492,6 +510,26 @@ class IsingBatch:
     def sync(self) -> None:
         _check(lib().isg_ising_sync(self._h))
 
+    def hist_enable(self, enable: bool = True) -> None:
+        """Exact energy histograms of every (size, slot), accumulated by each
+        record of pt_run: bins of the bond sum with the sums of |m|, m^2, m^4."""
+        _check(lib().isg_ising_hist_enable(self._h, int(bool(enable))))
+
+    def hist_reset(self) -> None:
+        _check(lib().isg_ising_hist_reset(self._h))
+
+    def histogram(self, size_index: int, slot: int):
+        """(bond sums, counters (n, 4) uint64) of the visited bins of (size,
+        slot): samples and the sums of |m|, m^2, m^4 in units of 2^-32."""
+        lo, nb = C.c_int64(), C.c_int64()
+        _check(lib().isg_ising_hist_range(self._h, int(size_index), int(slot), C.byref(lo),
+                                          C.byref(nb)))
+        out = np.zeros((nb.value, 4), np.uint64)
+        if nb.value:
+            _check(lib().isg_ising_hist_read(self._h, int(size_index), int(slot), lo.value,
+                                             nb.value, _ptr(out)))
+        return lo.value + 4 * np.arange(nb.value, dtype=np.int64), out
+
     def set_launch(self, threads: int, blocks_per_sm: int = 0) -> None:
         _check(lib().isg_ising_set_launch(self._h, threads, blocks_per_sm))
 
@@ -802,6 +840,250 @@ class ContinuousGraphBatch:
         v = C.c_uint64()
         _check(lib().isg_cgraph_get_sweep(self._h, C.byref(v)))
         return v.value
+
+
+# ----------------------------------------------------------------- reweighting
+# GPU forms of analysis/scripts/reweighting.py and of the reweighting steps of
+# analysis/scripts/analyze_gpu_fss.py (names, arguments and results as there;
+# the fine-grid tables are dicts of columns instead of DataFrames).
+
+_MOM_SCALE = 2.0 ** -32
+
+
+def _points(energy_lists):
+    e = np.ascontiguousarray(np.concatenate([np.asarray(x, np.float64) for x in energy_lists]))
+    nk = np.array([len(x) for x in energy_lists], np.float64)
+    return e, np.ones(len(e)), nk
+
+
+def _wham_call(e, c, mom, n_mom, beta, nk, beta_t, n_iter=100, tol=1e-8):
+    bt = np.ascontiguousarray(beta_t, np.float64)
+    out = np.zeros((len(bt), 3 + n_mom))
+    f = np.zeros(len(beta))
+    it = C.c_int()
+    b = np.ascontiguousarray(beta, np.float64)
+    mom_p = _ptr(mom) if n_mom else None
+    _check(lib().isg_wham(_ptr(e), _ptr(c), mom_p, n_mom, len(e), _ptr(b),
+                          _ptr(np.ascontiguousarray(nk, np.float64)), len(b), int(n_iter),
+                          float(tol), _ptr(bt), len(bt), _ptr(out), _ptr(f), C.byref(it)))
+    return out, f, it.value
+
+
+def single_histogram(energies, beta_sim, beta_target):
+    """reweighting.py:15-37: normalised weights exp(-(beta_target - beta_sim) E)."""
+    e = np.ascontiguousarray(energies, np.float64)
+    w = np.zeros(len(e))
+    b = np.array([float(beta_sim)])
+    _check(lib().isg_wham_weights(_ptr(e), _ptr(np.ones(len(e))), len(e), _ptr(b),
+                                  _ptr(np.array([float(len(e))])), 1, 1, 1e-8,
+                                  float(beta_target), _ptr(w), None, None))
+    return w
+
+
+def reweight_observable(observable, weights):
+    """reweighting.py:40-42."""
+    return np.sum(observable * weights)
+
+
+def wham_reweight(energy_lists, beta_list, beta_target, n_iter=100, tol=1e-8):
+    """reweighting.py:45-105: (normalised weights of all samples, simulation index)."""
+    e, c, nk = _points(energy_lists)
+    b = np.ascontiguousarray(beta_list, np.float64)
+    w = np.zeros(len(e))
+    _check(lib().isg_wham_weights(_ptr(e), _ptr(c), len(e), _ptr(b), _ptr(nk), len(b),
+                                  int(n_iter), float(tol), float(beta_target), _ptr(w), None,
+                                  None))
+    sim = np.concatenate([np.full(len(x), k) for k, x in enumerate(energy_lists)])
+    return w, sim
+
+
+def reweight_binder(energy_lists, mag_lists, beta_list, beta_targets):
+    """reweighting.py:108-143: (T, U) at the target betas (one WHAM solve)."""
+    e, c, nk = _points(energy_lists)
+    m = np.concatenate([np.asarray(x, np.float64) for x in mag_lists])
+    mom = np.ascontiguousarray(np.stack([m * m, (m * m) * (m * m)], axis=1))
+    bt = np.asarray(beta_targets, np.float64)
+    out, _, _ = _wham_call(e, c, mom, 2, beta_list, nk, bt)
+    m2, m4 = out[:, 3], out[:, 4]
+    U = np.where(m2 > 0, 1.0 - m4 / (3.0 * np.where(m2 > 0, m2, 1.0) ** 2), 0.0)
+    return 1.0 / bt, U
+
+
+def _fine_table(T_fine, beta_list, V, avg, e_lists, m_lists):
+    """Columns of analyze_gpu_fss.py's fine-grid tables from averages avg[t] =
+    (logZ, <E>, <E^2>, <m>, <m^2>, <m^4>) and the leave-one-block-out
+    single-histogram jackknife (20 blocks) of the closest simulation."""
+    b = np.asarray(beta_list, np.float64)
+    T = np.asarray(T_fine, np.float64)
+    bt = 1.0 / T
+    kb = np.array([int(np.argmin(np.abs(1.0 / b - t))) for t in T])
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in e_lists])])
+    e, c, _ = _points(e_lists)
+    m = np.concatenate([np.asarray(x, np.float64) for x in m_lists])
+    mom = np.ascontiguousarray(np.stack([m, m * m, (m * m) * (m * m)], axis=1))
+    nb = 20
+    rows = len(T) * nb
+    p0 = np.repeat(offs[kb], nb).astype(np.int64)
+    bs = np.repeat(np.array([len(e_lists[k]) for k in kb]) // nb, nb).astype(np.int64)
+    blk = np.tile(np.arange(nb, dtype=np.int64), len(T))
+    p1 = p0 + nb * bs
+    x0 = p0 + blk * bs
+    x1 = x0 + bs
+    jk = np.zeros((rows, 6))
+    _check(lib().isg_reweight_single(_ptr(e), _ptr(c), _ptr(mom), 3, len(e), _ptr(p0), _ptr(p1),
+                                     _ptr(x0), _ptr(x1),
+                                     _ptr(np.ascontiguousarray(np.repeat(b[kb], nb))),
+                                     _ptr(np.ascontiguousarray(np.repeat(bt, nb))), rows,
+                                     _ptr(jk)))
+    jk = jk.reshape(len(T), nb, 6)
+    am, am2, am4 = avg[:, 3], avg[:, 4], avg[:, 5]
+    ae, ae2 = avg[:, 1], avg[:, 2]
+    chi = bt * V * (am2 - am ** 2)
+    U = np.where(am2 > 1e-15, 1.0 - am4 / (3.0 * np.where(am2 > 1e-15, am2, 1.0) ** 2), 0.0)
+    j1, j2, j4 = jk[:, :, 3], jk[:, :, 4], jk[:, :, 5]
+    jc = bt[:, None] * V * (j2 - j1 ** 2)
+    ju = np.where(j2 > 1e-15, 1.0 - j4 / (3.0 * np.where(j2 > 1e-15, j2, 1.0) ** 2), 0.0)
+    f = (nb - 1.0) / nb
+    return {"T": T, "M": am, "M2": am2, "M4": am4, "chi_conn": chi,
+            "chi_err": np.sqrt(f * np.sum((jc - chi[:, None]) ** 2, axis=1)),
+            "Cv": bt ** 2 * (ae2 - ae ** 2) / V, "U": U, "E": ae / V,
+            "M_err": np.sqrt(f * np.sum((j1 - am[:, None]) ** 2, axis=1)),
+            "U_err": np.sqrt(f * np.sum((ju - U[:, None]) ** 2, axis=1))}
+
+
+def reweight_single_histogram(energy_lists, mag_lists, beta_list, T_fine, n: int):
+    """analyze_gpu_fss.py:86-157: every T of the fine grid reweighted from the
+    closest simulation (total energies, |m| per spin, V = n^3)."""
+    b = np.asarray(beta_list, np.float64)
+    T = np.asarray(T_fine, np.float64)
+    kb = np.array([int(np.argmin(np.abs(1.0 / b - t))) for t in T])
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in energy_lists])])
+    e, c, _ = _points(energy_lists)
+    m = np.concatenate([np.asarray(x, np.float64) for x in mag_lists])
+    mom = np.ascontiguousarray(np.stack([m, m * m, (m * m) * (m * m)], axis=1))
+    avg = np.zeros((len(T), 6))
+    p0 = np.ascontiguousarray(offs[kb], np.int64)
+    p1 = np.ascontiguousarray(offs[kb + 1], np.int64)
+    _check(lib().isg_reweight_single(_ptr(e), _ptr(c), _ptr(mom), 3, len(e), _ptr(p0), _ptr(p1),
+                                     None, None, _ptr(np.ascontiguousarray(b[kb])),
+                                     _ptr(np.ascontiguousarray(1.0 / T)), len(T), _ptr(avg)))
+    return _fine_table(T, b, float(n) ** 3, avg, energy_lists, mag_lists)
+
+
+def wham_reweight_fine(energy_lists, mag_lists, beta_list, T_fine, n: int, n_iter=100,
+                       tol=1e-8):
+    """analyze_gpu_fss.py:160-243: WHAM over all simulations at every T of the
+    fine grid; errors from the closest simulation's jackknife."""
+    e, c, nk = _points(energy_lists)
+    m = np.concatenate([np.asarray(x, np.float64) for x in mag_lists])
+    mom = np.ascontiguousarray(np.stack([m, m * m, (m * m) * (m * m)], axis=1))
+    T = np.asarray(T_fine, np.float64)
+    avg, _, _ = _wham_call(e, c, mom, 3, beta_list, nk, 1.0 / T, n_iter, tol)
+    return _fine_table(T, beta_list, float(n) ** 3, avg, energy_lists, mag_lists)
+
+
+def wham_histograms(bonds, counters, temps, J: float, n_sites: float, T_fine, n_iter=100,
+                    tol=1e-8):
+    """WHAM over the exact energy histograms of one size (IsingBatch.histogram
+    per slot: bonds[k], counters[k]): identical to WHAM over the samples, since
+    every sample of a bin has the same energy E = -J B.  Returns columns T, E
+    (per spin), Cv, M, M2, M4, U, chi_conn as analyze_gpu_fss.py defines them."""
+    allb = np.unique(np.concatenate([np.asarray(x, np.int64) for x in bonds]))
+    idx = {int(v): i for i, v in enumerate(allb)}
+    P = len(allb)
+    c = np.zeros(P)
+    mom = np.zeros((P, 3))
+    nk = np.zeros(len(temps))
+    for k, (bk, ck) in enumerate(zip(bonds, counters)):
+        pos = np.array([idx[int(v)] for v in bk], np.int64)
+        ck = np.asarray(ck, np.uint64)
+        np.add.at(c, pos, ck[:, 0].astype(np.float64))
+        for j in range(3):
+            np.add.at(mom[:, j], pos, ck[:, 1 + j].astype(np.float64) * _MOM_SCALE)
+        nk[k] = float(ck[:, 0].sum())
+    e = np.ascontiguousarray(-float(J) * allb.astype(np.float64))
+    T = np.asarray(T_fine, np.float64)
+    bt = 1.0 / T
+    avg, f, it = _wham_call(e, np.ascontiguousarray(c), np.ascontiguousarray(mom), 3,
+                            1.0 / np.asarray(temps, np.float64), nk, bt, n_iter, tol)
+    V = float(n_sites)
+    am, am2, am4 = avg[:, 3], avg[:, 4], avg[:, 5]
+    return {"T": T, "E": avg[:, 1] / V, "Cv": bt ** 2 * (avg[:, 2] - avg[:, 1] ** 2) / V,
+            "M": am, "M2": am2, "M4": am4,
+            "U": np.where(am2 > 1e-15, 1.0 - am4 / (3.0 * np.where(am2 > 1e-15, am2, 1.0) ** 2),
+                          0.0),
+            "chi_conn": bt * V * (am2 - am ** 2), "f": f, "iterations": it}
+
+
+# ----------------------------------------------------------------- binary files
+
+TS_DTYPE = np.dtype([("temp_idx", "<u4"), ("replica", "<u4"), ("E", "<f8"), ("M", "<f8")])
+MODELS = ("ising", "heisenberg", "xy")
+
+
+def write_timeseries(path, model: str, n: int, temps, temp_idx, replica, E, M) -> None:
+    """Binary timeseries through isg_ts_* (the layout include/isg.h documents)."""
+    t = np.ascontiguousarray(temps, np.float64)
+    h = C.c_void_p()
+    _check(lib().isg_ts_open(C.byref(h), str(path).encode(), MODELS.index(model), int(n),
+                             _ptr(t), len(t)))
+    try:
+        ti = np.ascontiguousarray(temp_idx, np.int32)
+        rp = np.ascontiguousarray(replica, np.int32)
+        ee = np.ascontiguousarray(E, np.float64)
+        mm = np.ascontiguousarray(M, np.float64)
+        _check(lib().isg_ts_append(h, _ptr(ti), _ptr(rp), _ptr(ee), _ptr(mm), len(ti)))
+    finally:
+        _check(lib().isg_ts_close(h))
+
+
+def read_timeseries(path) -> dict:
+    """A binary timeseries: {model, n, temps, records (TS_DTYPE array)}."""
+    raw = Path(path).read_bytes()
+    if raw[:8] != b"ISGTSER1":
+        raise ValueError(f"{path}: not an ISGTSER1 timeseries")
+    hb, model, n, nt = np.frombuffer(raw, "<u4", 4, 8)
+    temps = np.frombuffer(raw, "<f8", int(nt), 32)
+    rec = np.frombuffer(raw, TS_DTYPE, offset=int(hb))
+    return {"model": MODELS[int(model)], "n": int(n), "temps": temps.copy(), "records": rec}
+
+
+def timeseries_lists(ts: dict):
+    """(energy_lists, mag_lists, beta_list) of a timeseries as
+    analyze_gpu_fss.py:60-83 builds them: total energies E V and |m|, per
+    temperature index in order."""
+    V = float(ts["n"]) ** 3
+    rec = ts["records"]
+    el, ml, bl = [], [], []
+    for t, T in enumerate(ts["temps"]):
+        sel = rec["temp_idx"] == t
+        if not sel.any():
+            continue
+        el.append(rec["E"][sel] * V)
+        ml.append(rec["M"][sel].copy())
+        bl.append(1.0 / T)
+    return el, ml, np.array(bl)
+
+
+def read_histograms(path) -> dict:
+    """A histogram file: {dim, n, J, temps, bonds[t], counters[t] (n, 4)}."""
+    raw = Path(path).read_bytes()
+    if raw[:8] != b"ISGHIST1":
+        raise ValueError(f"{path}: not an ISGHIST1 histogram file")
+    hb, dim, n, nt = np.frombuffer(raw, "<u4", 4, 8)
+    J = float(np.frombuffer(raw, "<f8", 1, 24)[0])
+    temps = np.frombuffer(raw, "<f8", int(nt), 32).copy()
+    off = int(hb)
+    bonds, cnt = [], []
+    for _ in range(int(nt)):
+        lo, nbins = np.frombuffer(raw, "<i8", 2, off)
+        off += 16
+        c = np.frombuffer(raw, "<u8", 4 * int(nbins), off).reshape(-1, 4).copy()
+        off += 32 * int(nbins)
+        bonds.append(int(lo) + 4 * np.arange(int(nbins), dtype=np.int64))
+        cnt.append(c)
+    return {"dim": int(dim), "n": int(n), "J": J, "temps": temps, "bonds": bonds,
+            "counters": cnt}
 
 
 class LatticeGpu:

@@ -32,8 +32,8 @@ NVCC_FLAGS = [
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 
 CU_SOURCES = ["isg_ising.cu", "isg_cont.cu", "isg_noalloc.cu", "isg_learned.cu", "isg_graph.cu",
-              "isg_cgraph.cu"]
-CPP_SOURCES = ["isg_stats.cpp", "isg_anneal.cpp", "isg_quench.cpp"]
+              "isg_cgraph.cu", "isg_reweight.cu"]
+CPP_SOURCES = ["isg_stats.cpp", "isg_anneal.cpp", "isg_quench.cpp", "isg_io.cpp"]
 DRIVERS = ["gpu_fss", "fss", "kz", "coarsening", "gpu_jfit"]   # host/<name>.cpp -> bin/<name>
 
 

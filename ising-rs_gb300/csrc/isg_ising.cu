@@ -996,6 +996,15 @@ struct PostParams {
     int n_classes;
     int replicas_total;
     int L[kMaxClasses];
+    // energy histograms (NULL when off): per size s and slot t, bins b of the
+    // bond sum B = 4 b - dN_s (B + dN is a multiple of 4 on a periodic even
+    // lattice), 4 counters per bin: samples, and the sums of |m|, m^2, m^4 in
+    // units of 2^-32; hist_rng[2 (s R + t) + {0, 1}] = lowest / highest bin seen
+    unsigned long long* hist;
+    int32_t* hist_rng;
+    long long hist_off[kMaxClasses];   // first bin of size s
+    long long hist_dn[kMaxClasses];    // dim * N_s
+    double hist_nsite[kMaxClasses];    // N_s
 };
 
 // One block per size: record (slot, bond, mag) of every replica, run an
@@ -1025,9 +1034,27 @@ __global__ void k_ising_post(const __grid_constant__ PostParams Q, int do_record
         if (do_record) {
             const long long slot = (long long)(*rec_count % (unsigned long long)Q.ring_cap);
             const long long o = slot * Q.replicas_total + base + r;
-            Q.rec_t[o] = Q.r2t[base + r];
+            const int t = Q.r2t[base + r];
+            Q.rec_t[o] = t;
             Q.rec_b[o] = b;
             Q.rec_m[o] = m;
+            if (Q.hist) {
+                // one replica per slot, so no two threads share a bin row
+                const long long dn = Q.hist_dn[s];
+                const long long bin = (b + dn) >> 2;
+                unsigned long long* hb =
+                    Q.hist + 4 * (Q.hist_off[s] + (long long)t * ((dn >> 1) + 1) + bin);
+                const double m1 = __ddiv_rn(fabs((double)m), Q.hist_nsite[s]);
+                const double m2 = __dmul_rn(m1, m1);
+                const double m4 = __dmul_rn(m2, m2);
+                hb[0] += 1ull;
+                hb[1] += __double2ull_rn(__dmul_rn(m1, 4294967296.0));
+                hb[2] += __double2ull_rn(__dmul_rn(m2, 4294967296.0));
+                hb[3] += __double2ull_rn(__dmul_rn(m4, 4294967296.0));
+                int32_t* rg = Q.hist_rng + 2 * (base + t);
+                rg[0] = min(rg[0], (int32_t)bin);
+                rg[1] = max(rg[1], (int32_t)bin);
+            }
         }
     }
     __syncthreads();
@@ -1164,6 +1191,10 @@ struct isg_ising {
     int64_t sched_cap = 0;
     unsigned long long* d_srec = nullptr;
     int64_t srec_cap = 0;
+    // energy histograms (isg_ising_hist_*)
+    unsigned long long* d_hist = nullptr;
+    int32_t* d_hist_rng = nullptr;
+    int64_t hist_bins = 0;  // all sizes and slots
 };
 
 namespace isg {
@@ -1519,6 +1550,8 @@ int isg_ising_destroy(isg_ising* H) {
     cudaFree(H->d_sched_tab);
     cudaFree(H->d_sched);
     cudaFree(H->d_srec);
+    cudaFree(H->d_hist);
+    cudaFree(H->d_hist_rng);
     if (H->own_stream) cudaStreamDestroy(H->own_stream);
     delete H;
     return ISG_OK;
@@ -2272,6 +2305,111 @@ int isg_ising_run_schedule(isg_ising* H, const double* temps, int64_t n_sweeps, 
     if (temps) H->temps_set = true;
     if (n_rows) *n_rows = rows;
     return check_launch("isg_ising_run_schedule");
+}
+
+// ------------------------------------------------------------ histograms
+
+static int hist_clear(isg_ising* H) {
+    ISG_CK(cudaMemsetAsync(H->d_hist, 0, sizeof(unsigned long long) * 4 * H->hist_bins, H->stream));
+    std::vector<int32_t> rng(2 * (size_t)H->replicas_total);
+    for (size_t i = 0; i < rng.size(); i += 2) {
+        rng[i] = INT32_MAX;
+        rng[i + 1] = -1;
+    }
+    ISG_CK(cudaMemcpyAsync(H->d_hist_rng, rng.data(), sizeof(int32_t) * rng.size(),
+                           cudaMemcpyHostToDevice, H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    return ISG_OK;
+}
+
+int isg_ising_hist_enable(isg_ising* H, int enable) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_hist_enable: NULL handle");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    // cached graphs hold the record kernel's parameters: capture them again
+    destroy_graph(H);
+    if (!enable) {
+        cudaFree(H->d_hist);
+        cudaFree(H->d_hist_rng);
+        H->d_hist = nullptr;
+        H->d_hist_rng = nullptr;
+        H->hist_bins = 0;
+        H->Q.hist = nullptr;
+        H->Q.hist_rng = nullptr;
+        return ISG_OK;
+    }
+    if (H->d_hist) return hist_clear(H);
+    int64_t total = 0;
+    for (int s = 0; s < H->n_classes; ++s) {
+        const int64_t L = H->sizes[s];
+        const int64_t nsite = H->dim == 3 ? L * L * L : L * L;
+        const int64_t dn = H->dim * nsite;
+        if (dn > ((int64_t)1 << 33))
+            return fail(ISG_ERR_UNSUPPORTED, "isg_ising_hist_enable: lattice too large");
+        H->Q.hist_off[s] = (long long)total;
+        H->Q.hist_dn[s] = (long long)dn;
+        H->Q.hist_nsite[s] = (double)nsite;
+        total += (int64_t)H->R * (dn / 2 + 1);
+    }
+    ISG_CK(cudaMalloc((void**)&H->d_hist, sizeof(unsigned long long) * 4 * total));
+    cudaError_t e = cudaMalloc((void**)&H->d_hist_rng, sizeof(int32_t) * 2 * H->replicas_total);
+    if (e != cudaSuccess) {
+        cudaFree(H->d_hist);
+        H->d_hist = nullptr;
+        return cuda_fail(e, "cudaMalloc");
+    }
+    H->hist_bins = total;
+    H->Q.hist = H->d_hist;
+    H->Q.hist_rng = H->d_hist_rng;
+    return hist_clear(H);
+}
+
+int isg_ising_hist_reset(isg_ising* H) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_hist_reset: NULL handle");
+    if (!H->d_hist) return fail(ISG_ERR_STATE, "isg_ising_hist_reset: histograms are off");
+    cudaSetDevice(H->device);
+    return hist_clear(H);
+}
+
+int isg_ising_hist_range(isg_ising* H, int size_index, int slot, int64_t* bond_lo,
+                         int64_t* n_bins) {
+    if (!H || !bond_lo || !n_bins || size_index < 0 || size_index >= H->n_classes || slot < 0 ||
+        slot >= H->R)
+        return fail(ISG_ERR_ARG, "isg_ising_hist_range: bad argument");
+    if (!H->d_hist) return fail(ISG_ERR_STATE, "isg_ising_hist_range: histograms are off");
+    cudaSetDevice(H->device);
+    int32_t rg[2];
+    ISG_CK(cudaMemcpyAsync(rg, H->d_hist_rng + 2 * ((int64_t)size_index * H->R + slot),
+                           sizeof(rg), cudaMemcpyDeviceToHost, H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    const int64_t dn = H->Q.hist_dn[size_index];
+    if (rg[1] < rg[0]) {
+        *bond_lo = -dn;
+        *n_bins = 0;
+    } else {
+        *bond_lo = 4 * (int64_t)rg[0] - dn;
+        *n_bins = (int64_t)rg[1] - rg[0] + 1;
+    }
+    return ISG_OK;
+}
+
+int isg_ising_hist_read(isg_ising* H, int size_index, int slot, int64_t bond_lo, int64_t n_bins,
+                        uint64_t* out) {
+    if (!H || size_index < 0 || size_index >= H->n_classes || slot < 0 || slot >= H->R ||
+        n_bins < 0 || (n_bins > 0 && !out))
+        return fail(ISG_ERR_ARG, "isg_ising_hist_read: bad argument");
+    if (!H->d_hist) return fail(ISG_ERR_STATE, "isg_ising_hist_read: histograms are off");
+    const int64_t dn = H->Q.hist_dn[size_index];
+    if (((bond_lo + dn) & 3) != 0 || bond_lo < -dn || bond_lo + 4 * (n_bins - 1) > dn)
+        return fail(ISG_ERR_ARG, "isg_ising_hist_read: bins must lie in [-dN, dN] with "
+                                 "bond_lo + dN a multiple of 4");
+    if (n_bins == 0) return ISG_OK;
+    cudaSetDevice(H->device);
+    const int64_t row = H->Q.hist_off[size_index] + (int64_t)slot * (dn / 2 + 1) + (bond_lo + dn) / 4;
+    ISG_CK(cudaMemcpyAsync(out, H->d_hist + 4 * row, sizeof(unsigned long long) * 4 * n_bins,
+                           cudaMemcpyDeviceToHost, H->stream));
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    return ISG_OK;
 }
 
 }  // extern "C"

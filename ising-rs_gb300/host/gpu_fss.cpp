@@ -17,6 +17,13 @@
 //     default 100);
 //   * odd or repeated sizes are rejected/merged (the reference kernel
 //     mapping is wrong for odd N, kernels.cu:28).
+// Two new flags for the reweighting consumers:
+//   --timeseries-format csv|bin|both  (default csv) also or instead writes
+//     gpu_fss_{model}_N{n}_timeseries.bin, the exact FP64 records in the
+//     binary layout of include/isg.h (isg_ts_*);
+//   --histograms (ising) accumulates exact energy histograms on the device
+//     and writes gpu_fss_ising_N{n}_hist.bin (isg_ising_hist_*,
+//     isg_hist_write).
 #include <algorithm>
 #include <string>
 #include <vector>
@@ -80,6 +87,8 @@ struct Run {
     uint64_t R, warmup, samples, ee, seed, n_or, me, renorm;
     std::string outdir;
     double delta;
+    std::string ts_format = "csv";
+    bool hist = false;
 };
 
 FILE* open_ts(const std::string& path) {
@@ -89,13 +98,75 @@ FILE* open_ts(const std::string& path) {
     return f;
 }
 
+// The timeseries of one size in the requested formats.
+struct TsOut {
+    FILE* csv = nullptr;
+    isg_ts* bin = nullptr;
+    std::string csv_path, bin_path;
+    std::vector<int32_t> bt, br;
+    std::vector<double> be, bm;
+    char line[128];
+
+    void open(const Run& a, int n, const std::vector<double>& temps) {
+        const std::string stem = join_path(a.outdir, "gpu_fss_" + a.model + "_N" + std::to_string(n) +
+                                                         "_timeseries");
+        if (a.ts_format != "bin") {
+            csv_path = stem + ".csv";
+            csv = open_ts(csv_path);
+        }
+        if (a.ts_format != "csv") {
+            bin_path = stem + ".bin";
+            const int model = a.model == "ising" ? 0 : a.model == "heisenberg" ? 1 : 2;
+            if (isg_ts_open(&bin, bin_path.c_str(), model, n, temps.data(), (int)temps.size()) !=
+                ISG_OK)
+                panic_expect("create timeseries file failed", isg_last_error());
+        }
+    }
+    void add(int t, int r, double e, double m) {
+        if (csv) {
+            int k = snprintf(line, sizeof line, "%d,%.8f,%.8f\n", t, e, m);
+            fwrite(line, 1, (size_t)k, csv);
+        }
+        if (bin) {
+            bt.push_back(t);
+            br.push_back(r);
+            be.push_back(e);
+            bm.push_back(m);
+        }
+    }
+    void flush() {
+        if (bin && !bt.empty()) {
+            if (isg_ts_append(bin, bt.data(), br.data(), be.data(), bm.data(), (int64_t)bt.size()) !=
+                ISG_OK)
+                panic_expect("write timeseries row failed", isg_last_error());
+            bt.clear();
+            br.clear();
+            be.clear();
+            bm.clear();
+        }
+    }
+    void close() {
+        flush();
+        if (csv) {
+            fclose(csv);
+            fprintf(stderr, "  Wrote %s\n", csv_path.c_str());
+        }
+        if (bin) {
+            if (isg_ts_close(bin) != ISG_OK)
+                panic_expect("flush timeseries failed", isg_last_error());
+            fprintf(stderr, "  Wrote %s\n", bin_path.c_str());
+        }
+        csv = nullptr;
+        bin = nullptr;
+    }
+};
+
 void empty_outputs(const Run& a, int n) {
     // --replicas 0: header-only files, as the reference loops write them
-    std::string ts = join_path(a.outdir, "gpu_fss_" + a.model + "_N" + std::to_string(n) +
-                                             "_timeseries.csv");
-    fclose(open_ts(ts));
-    fprintf(stderr, "  Wrote %s\n", ts.c_str());
     std::vector<double> temps;
+    TsOut out;
+    out.open(a, n, temps);
+    out.close();
     std::vector<Series> none;
     write_summary(join_path(a.outdir, "gpu_fss_" + a.model + "_N" + std::to_string(n) +
                                           "_summary.csv"),
@@ -131,13 +202,10 @@ void run_ising(const Run& a) {
         }
     }
     if (isg_ising_reset_sampling(h) != ISG_OK) panic_expect("GPU step failed", isg_last_error());
-    std::vector<FILE*> tsf(NS);
-    std::vector<std::string> tsp(NS);
-    for (int s = 0; s < NS; ++s) {
-        tsp[s] = join_path(a.outdir, "gpu_fss_ising_N" + std::to_string(a.sizes[s]) +
-                                         "_timeseries.csv");
-        tsf[s] = open_ts(tsp[s]);
-    }
+    if (a.hist && isg_ising_hist_enable(h, 1) != ISG_OK)
+        panic_expect("GPU step failed", isg_last_error());
+    std::vector<TsOut> tsf(NS);
+    for (int s = 0; s < NS; ++s) tsf[s].open(a, a.sizes[s], temps);
     if (a.ee == 0) {
         fprintf(stderr, "thread 'main' panicked at src/bin/gpu_fss.rs:245:30:\n"
                         "attempt to calculate the remainder with a divisor of zero\n");
@@ -150,7 +218,6 @@ void run_ising(const Run& a) {
     const uint64_t chunk_sweeps = 10000;
     std::vector<int32_t> rt;
     std::vector<int64_t> rb, rm;
-    char line[128];
     for (uint64_t done = 0; done < a.samples;) {
         uint64_t n = std::min<uint64_t>(chunk_sweeps - done % chunk_sweeps, a.samples - done);
         uint64_t rows = n / a.me + 2;
@@ -172,9 +239,9 @@ void run_ising(const Run& a) {
                     const double m_per = fabs((double)rm[o]) / n3;
                     ts[s][t].e.push_back(e_per);
                     ts[s][t].m.push_back(m_per);
-                    int k = snprintf(line, sizeof line, "%d,%.8f,%.8f\n", t, e_per, m_per);
-                    fwrite(line, 1, (size_t)k, tsf[s]);
+                    tsf[s].add(t, r, e_per, m_per);
                 }
+            tsf[s].flush();
         }
         done += n;
         if (done % 10000 == 0)
@@ -182,12 +249,29 @@ void run_ising(const Run& a) {
                     (unsigned long long)a.samples);
     }
     for (int s = 0; s < NS; ++s) {
-        fclose(tsf[s]);
-        fprintf(stderr, "  Wrote %s\n", tsp[s].c_str());
+        tsf[s].close();
         const double n3 = (double)a.sizes[s] * a.sizes[s] * a.sizes[s];
         write_summary(join_path(a.outdir, "gpu_fss_ising_N" + std::to_string(a.sizes[s]) +
                                               "_summary.csv"),
                       temps, ts[s], n3);
+        if (a.hist) {
+            std::vector<int64_t> lo(R), nb(R);
+            std::vector<uint64_t> cnt;
+            for (int t = 0; t < R; ++t) {
+                if (isg_ising_hist_range(h, s, t, &lo[t], &nb[t]) != ISG_OK)
+                    panic_expect("GPU step failed", isg_last_error());
+                const size_t at = cnt.size();
+                cnt.resize(at + 4 * (size_t)nb[t]);
+                if (nb[t] > 0 && isg_ising_hist_read(h, s, t, lo[t], nb[t], cnt.data() + at) != ISG_OK)
+                    panic_expect("GPU step failed", isg_last_error());
+            }
+            const std::string hp = join_path(a.outdir, "gpu_fss_ising_N" +
+                                                           std::to_string(a.sizes[s]) + "_hist.bin");
+            if (isg_hist_write(hp.c_str(), 3, a.sizes[s], 1.0, temps.data(), R, lo.data(),
+                               nb.data(), cnt.data()) != ISG_OK)
+                panic_expect("write histogram file failed", isg_last_error());
+            fprintf(stderr, "  Wrote %s\n", hp.c_str());
+        }
     }
     isg_ising_destroy(h);
 }
@@ -222,13 +306,8 @@ void run_continuous(const Run& a, int n_comp) {
         }
     }
     if (isg_cont_reset_sampling(h) != ISG_OK) panic_expect("sweep failed", isg_last_error());
-    std::vector<FILE*> tsf(NS);
-    std::vector<std::string> tsp(NS);
-    for (int s = 0; s < NS; ++s) {
-        tsp[s] = join_path(a.outdir, "gpu_fss_" + a.model + "_N" + std::to_string(a.sizes[s]) +
-                                         "_timeseries.csv");
-        tsf[s] = open_ts(tsp[s]);
-    }
+    std::vector<TsOut> tsf(NS);
+    for (int s = 0; s < NS; ++s) tsf[s].open(a, a.sizes[s], temps);
     if (a.ee == 0) {
         fprintf(stderr, "thread 'main' panicked at src/bin/gpu_fss.rs:504:30:\n"
                         "attempt to calculate the remainder with a divisor of zero\n");
@@ -240,7 +319,6 @@ void run_continuous(const Run& a, int n_comp) {
             (unsigned long long)a.samples, (unsigned long long)a.me);
     std::vector<int32_t> rt;
     std::vector<double> re, rmv, rh;
-    char line[128];
     for (uint64_t done = 0; done < a.samples;) {
         uint64_t n = std::min<uint64_t>(10000 - done % 10000, a.samples - done);
         uint64_t rows = n / a.me + 2;
@@ -265,9 +343,9 @@ void run_continuous(const Run& a, int n_comp) {
                     const double m_abs = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]) / n3;
                     ts[s][t].e.push_back(e_per);
                     ts[s][t].m.push_back(m_abs);
-                    int k = snprintf(line, sizeof line, "%d,%.8f,%.8f\n", t, e_per, m_abs);
-                    fwrite(line, 1, (size_t)k, tsf[s]);
+                    tsf[s].add(t, r, e_per, m_abs);
                 }
+            tsf[s].flush();
         }
         done += n;
         if (done % 10000 == 0)
@@ -275,8 +353,7 @@ void run_continuous(const Run& a, int n_comp) {
                     (unsigned long long)a.samples);
     }
     for (int s = 0; s < NS; ++s) {
-        fclose(tsf[s]);
-        fprintf(stderr, "  Wrote %s\n", tsp[s].c_str());
+        tsf[s].close();
         const double n3 = (double)a.sizes[s] * a.sizes[s] * a.sizes[s];
         write_summary(join_path(a.outdir, "gpu_fss_" + a.model + "_N" +
                                               std::to_string(a.sizes[s]) + "_summary.csv"),
@@ -323,6 +400,9 @@ int main(int argc, char** argv) {
             a.me = parse_arg<uint64_t>(argc, argv, i, "--measure-every"), i += 2;
         else if (f == "--renorm-every")
             a.renorm = parse_arg<uint64_t>(argc, argv, i, "--renorm-every"), i += 2;
+        else if (f == "--timeseries-format")
+            a.ts_format = get_arg(argc, argv, i, "--timeseries-format"), i += 2;
+        else if (f == "--histograms") a.hist = true, i += 1;
         else i += 1;
     }
     // sizes: comma-separated, trimmed, malformed entries dropped (gpu_fss.rs:98-101)
@@ -336,6 +416,10 @@ int main(int argc, char** argv) {
     if (a.samples == 0) die("Error: --samples must be at least 1");
     if (a.warmup == 0) die("Error: --warmup must be at least 1");
     if (a.me == 0) die("Error: --measure-every must be at least 1");
+    if (a.ts_format != "csv" && a.ts_format != "bin" && a.ts_format != "both")
+        die("Error: --timeseries-format must be csv, bin or both");
+    if (a.hist && a.model != "ising")
+        die("Error: --histograms needs --model ising (exact energy bins)");
     std::string err;
     if (!mkdirs(a.outdir, &err)) panic_expect("failed to create outdir", err);
     std::string sz = "[";

@@ -574,3 +574,132 @@ def tau_int(x) -> float:
         if t >= 6 * tau:
             break
     return float(tau)
+
+
+# --------------------------------------------------------------- reweighting
+# numpy restatement of the reference's reweighting consumers: the checker of
+# the device reweighting (isg_wham, isg_wham_weights, isg_reweight_single).
+
+
+def _lse(x, axis=None):
+    m = np.max(x, axis=axis, keepdims=True)
+    out = m + np.log(np.sum(np.exp(x - m), axis=axis, keepdims=True))
+    return np.squeeze(out, axis=axis) if axis is not None else float(out.reshape(()))
+
+
+def rw_single_histogram(energies, beta_sim, beta_target):
+    """analysis/scripts/reweighting.py:15-37: normalised exp(-(b' - b) E)."""
+    lw = -(beta_target - beta_sim) * np.asarray(energies, np.float64)
+    w = np.exp(lw - lw.max())
+    return w / w.sum()
+
+
+def _rw_wham_solve(energy_lists, beta_list, n_iter=100, tol=1e-8):
+    """reweighting.py:69-95: the f_k iteration; returns (f, log_denom of the
+    last round, all energies)."""
+    b = np.asarray(beta_list, np.float64)
+    nk = np.array([len(x) for x in energy_lists], np.float64)
+    E = np.concatenate([np.asarray(x, np.float64) for x in energy_lists])
+    f = np.zeros(len(b))
+    ld = None
+    for _ in range(n_iter):
+        ld = _lse((np.log(nk) + f)[None, :] - b[None, :] * E[:, None], axis=1)
+        fn = np.array([-_lse(-bk * E - ld) for bk in b])
+        fn -= fn[0]
+        done = np.max(np.abs(fn - f)) < tol
+        f = fn
+        if done:
+            break
+    return f, ld, E
+
+
+def rw_wham(energy_lists, beta_list, beta_target, n_iter=100, tol=1e-8):
+    """reweighting.py:45-105: (normalised weights, simulation index)."""
+    _, ld, E = _rw_wham_solve(energy_lists, beta_list, n_iter, tol)
+    lw = -beta_target * E - ld
+    w = np.exp(lw - lw.max())
+    w /= w.sum()
+    sim = np.concatenate([np.full(len(x), k) for k, x in enumerate(energy_lists)])
+    return w, sim
+
+
+def rw_binder(energy_lists, mag_lists, beta_list, beta_targets):
+    """reweighting.py:108-143: (T, U) with U = 1 - <m^4> / (3 <m^2>^2)."""
+    m = np.concatenate([np.asarray(x, np.float64) for x in mag_lists])
+    T, U = [], []
+    for bt in beta_targets:
+        w, _ = rw_wham(energy_lists, beta_list, bt)
+        m2 = np.sum(w * m ** 2)
+        m4 = np.sum(w * m ** 4)
+        T.append(1.0 / bt)
+        U.append(1.0 - m4 / (3.0 * m2 ** 2) if m2 > 0 else 0.0)
+    return np.array(T), np.array(U)
+
+
+def _rw_fine_row(T, beta_t, V, w, e, m, e_sim, m_sim, db):
+    """Observables of one target (analyze_gpu_fss.py:103-155 / 218-241):
+    averages from weights w over (e, m); errors from the leave-one-block-out
+    single-histogram jackknife (20 blocks) of the closest simulation."""
+    am, am2, am4 = w @ m, w @ m ** 2, w @ m ** 4
+    ae, ae2 = w @ e, w @ e ** 2
+    chi = beta_t * V * (am2 - am ** 2)
+    cv = beta_t ** 2 * (ae2 - ae ** 2) / V
+    U = 1.0 - am4 / (3.0 * am2 ** 2) if am2 > 1e-15 else 0.0
+    nb = 20
+    bs = len(e_sim) // nb
+    jc, jm, ju = np.zeros(nb), np.zeros(nb), np.zeros(nb)
+    for k in range(nb):
+        idx = np.concatenate([np.arange(0, k * bs), np.arange((k + 1) * bs, nb * bs)])
+        ej, mj = e_sim[idx], m_sim[idx]
+        lw = -db * ej
+        wj = np.exp(lw - lw.max())
+        wj /= wj.sum()
+        j1, j2, j4 = np.sum(wj * mj), np.sum(wj * mj ** 2), np.sum(wj * mj ** 4)
+        jc[k] = beta_t * V * (j2 - j1 ** 2)
+        jm[k] = j1
+        ju[k] = 1.0 - j4 / (3.0 * j2 ** 2) if j2 > 1e-15 else 0.0
+    f = (nb - 1.0) / nb
+    return {"T": T, "M": am, "M2": am2, "M4": am4, "chi_conn": chi,
+            "chi_err": np.sqrt(f * np.sum((jc - chi) ** 2)), "Cv": cv, "U": U, "E": ae / V,
+            "M_err": np.sqrt(f * np.sum((jm - am) ** 2)),
+            "U_err": np.sqrt(f * np.sum((ju - U) ** 2))}
+
+
+def _rw_table(rows):
+    return {k: np.array([r[k] for r in rows]) for k in rows[0]}
+
+
+def rw_single_fine(energy_lists, mag_lists, beta_list, T_fine, n):
+    """analyze_gpu_fss.py:86-157: single-histogram reweighting of the closest
+    simulation to every T of a fine grid (energies are totals, V = n^3)."""
+    V = n ** 3
+    b = np.asarray(beta_list, np.float64)
+    rows = []
+    for T in T_fine:
+        bt = 1.0 / T
+        k = int(np.argmin(np.abs(1.0 / b - T)))
+        e = np.asarray(energy_lists[k], np.float64)
+        m = np.asarray(mag_lists[k], np.float64)
+        w = rw_single_histogram(e, b[k], bt)
+        rows.append(_rw_fine_row(T, bt, V, w, e, m, e, m, bt - b[k]))
+    return _rw_table(rows)
+
+
+def rw_wham_fine(energy_lists, mag_lists, beta_list, T_fine, n, n_iter=100, tol=1e-8):
+    """analyze_gpu_fss.py:160-243: WHAM over all simulations at every T of a
+    fine grid, errors from the closest simulation's single-histogram jackknife."""
+    V = n ** 3
+    b = np.asarray(beta_list, np.float64)
+    _, ld, E = _rw_wham_solve(energy_lists, b, n_iter, tol)
+    M = np.concatenate([np.asarray(x, np.float64) for x in mag_lists])
+    rows = []
+    for T in T_fine:
+        bt = 1.0 / T
+        lw = -bt * E - ld
+        w = np.exp(lw - lw.max())
+        w /= w.sum()
+        k = int(np.argmin(np.abs(1.0 / b - T)))
+        e_sim = np.asarray(energy_lists[k], np.float64)
+        m_sim = np.asarray(mag_lists[k], np.float64)
+        rows.append(_rw_fine_row(T, bt, V, w, E, M, e_sim, m_sim, bt - b[k]))
+    return _rw_table(rows)

@@ -763,6 +763,67 @@ def run_jfit(args):
     return 0
 
 
+RW = dict(sims=20, samples=100000, targets=200, n=16, cpu_fraction=0.05)
+
+
+def run_reweight(args):
+    """The reweighting consumer of a gpu_fss run (analysis/scripts/
+    analyze_gpu_fss.py:160-243, wham_reweight_fine): WHAM over 20 simulations
+    x 100,000 samples (the gpu_fss default sample count) and the observables
+    with their jackknife errors on a 200-point temperature grid.  One step =
+    one call through the Python mirror with host arrays in and out (the
+    samples are uploaded in the timed region).  The samples are synthetic
+    overlapping Gaussian energies and |m| of an N = 16^3 lattice."""
+    import torch
+    torch.cuda.set_device(0)
+    pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
+    oracle = _load("isg_oracle", ROOT / "oracle" / "oracle.py")
+    k = RW
+    V = k["n"] ** 3
+    rng = np.random.default_rng(SEED)
+    betas = np.linspace(1 / 4.60, 1 / 4.40, k["sims"])
+    el, ml = [], []
+    for b in betas:
+        el.append(rng.normal(-1.0 * V - 60000.0 * (b - betas[0]), 90.0, k["samples"]))
+        ml.append(np.clip(rng.normal(0.3 + 30.0 * (b - betas[0]), 0.05, k["samples"]), 0, 1))
+    T = np.linspace(4.40, 4.60, k["targets"])
+    steps, warm = max(1, min(args.steps, 5)), max(1, min(args.warmup, 2))
+    for _ in range(warm):
+        pkg.wham_reweight_fine(el, ml, betas, T, k["n"])
+    clocks = ClockSampler(0)
+    with clocks:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            pkg.wham_reweight_fine(el, ml, betas, T, k["n"])
+        wall = time.perf_counter() - t0
+    ms = wall / steps * 1e3
+    # the reference algorithm in numpy on a bounded sample (every 20th sample
+    # of each simulation); its cost is linear in the sample count
+    frac = k["cpu_fraction"]
+    sub = max(1, int(round(1 / frac)))
+    t0 = time.perf_counter()
+    oracle.rw_wham_fine([x[::sub] for x in el], [x[::sub] for x in ml], betas, T, k["n"])
+    cpu_ms = (time.perf_counter() - t0) * 1e3 * sub
+    P = k["sims"] * k["samples"]
+    line = {"metric": "ms per WHAM reweighting of a gpu_fss run (wham_reweight_fine)",
+            "value": ms, "unit": "ms", "n_gpus": 1, "steps": steps, "warmup": warm,
+            "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian samples)",
+            "config": {"workload": f"wham_reweight_fine: {k['sims']} simulations x "
+                                   f"{k['samples']} samples (N = {k['n']}^3), "
+                                   f"{k['targets']} target temperatures, 20 jackknife blocks",
+                       "timing": "wall clock through the Python mirror (host arrays)"},
+            "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": P * 8 * 5,
+                    "d2h_bytes_per_step": k["targets"] * 21 * 6 * 8},
+            "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": 1, "kind": "port",
+                             "sample": f"the reference's numpy algorithm (restated) on every "
+                                       f"{sub}th sample, time scaled by {sub} (linear in the "
+                                       "sample count)"},
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def ncu_case_resident():
     """No timing: one schedule of 2000 sweeps of one L=30 lattice (the coarsening
     default size) for an ncu capture of the cluster-resident kernel."""
@@ -807,7 +868,7 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=90.0)
     ap.add_argument("--workload", default="ising",
                     choices=["ising", "heisenberg", "xy", "anneal", "kz", "coarsening",
-                             "jfit", "jfit-heisenberg", "jfit-xy"])
+                             "jfit", "jfit-heisenberg", "jfit-xy", "reweight"])
     ap.add_argument("--learned", action="store_true",
                     help="config 5: learned proposal vs plain PT ESS/s (separate JSON lines)")
     ap.add_argument("--train-seconds", type=float, default=60.0)
@@ -830,6 +891,8 @@ def main():
         return run_quench(args)
     if args.workload.startswith("jfit"):
         return run_jfit(args)
+    if args.workload == "reweight":
+        return run_reweight(args)
     if args.workload != "ising":
         return run_continuous(args)
     if args.warmup < 3:

@@ -27,10 +27,10 @@
 //   points of simulation k (single histogram), X = max_p x_p.
 //
 // GPU form: one thread per point for log_denom (a loop over the K
-// simulations), one block per simulation or per target for the sums over
-// points: thread-strided running log-sum-exp / max-shifted sums combined in
-// a fixed tree, so results do not depend on timing.  FP64 throughout (the
-// exponents reach 10^5-10^6).
+// simulations); for f', blocks over (simulation, slice of the points) whose
+// running log-sum-exps merge in slice order; one block per target for the
+// averages.  Every sum runs over a fixed partition in a fixed tree, so results
+// do not depend on timing.  FP64 throughout (the exponents reach 10^5-10^6).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -100,20 +100,38 @@ __device__ __forceinline__ void block_lse(double& m, double& s, double* sm, doub
     }
 }
 
-// f_k' = -logsumexp_p (log c_p - beta_k E_p - ld_p); one block per k.
-__global__ void k_rw_fnew(const double* __restrict__ e, const double* __restrict__ c, int64_t P,
-                          const double* __restrict__ ld, const double* __restrict__ beta,
-                          double* __restrict__ fnew) {
+// Partial log-sum-exps of f_k' = -logsumexp_p (log c_p - beta_k E_p - ld_p):
+// block (k, g) covers the g-th of gridDim.y equal slices of the points and
+// writes (m, s) to part[(k * gridDim.y + g) * 2].
+__global__ void k_rw_fnew_part(const double* __restrict__ e, const double* __restrict__ c,
+                               int64_t P, const double* __restrict__ ld,
+                               const double* __restrict__ beta, double* __restrict__ part) {
     __shared__ double sm[32], ss[32];
-    const int k = blockIdx.x;
+    const int k = blockIdx.x, g = blockIdx.y, G = gridDim.y;
+    const int64_t per = (P + G - 1) / G;
+    const int64_t lo = (int64_t)g * per, hi = min(P, lo + per);
     const double bk = beta[k];
     double m = 0.0, s = 0.0;
-    for (int64_t p = threadIdx.x; p < P; p += blockDim.x) {
+    for (int64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
         if (!(c[p] > 0.0)) continue;
         lse_merge(m, s, log(c[p]) - bk * e[p] - ld[p], 1.0);
     }
     block_lse(m, s, sm, ss);
-    if (threadIdx.x == 0) fnew[k] = s > 0.0 ? -(m + log(s)) : INFINITY;
+    if (threadIdx.x == 0) {
+        part[2 * ((size_t)k * G + g)] = m;
+        part[2 * ((size_t)k * G + g) + 1] = s;
+    }
+}
+
+// Merge the G partials of every k in slice order: fnew[k] = -(m + log s).
+__global__ void k_rw_fnew_merge(const double* __restrict__ part, int K, int G,
+                                double* __restrict__ fnew) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
+        double m = 0.0, s = 0.0;
+        for (int g = 0; g < G; ++g)
+            lse_merge(m, s, part[2 * ((size_t)k * G + g)], part[2 * ((size_t)k * G + g) + 1]);
+        fnew[k] = s > 0.0 ? -(m + log(s)) : INFINITY;
+    }
 }
 
 // Averages at target t (one block per target): out[t*(3+n_mom) + ...] =
@@ -200,10 +218,10 @@ __global__ void k_rw_weights(const double* __restrict__ e, const double* __restr
 struct RwBuf {
     double *e = nullptr, *c = nullptr, *mom = nullptr, *ld = nullptr, *a = nullptr,
            *beta = nullptr, *fnew = nullptr, *bt = nullptr, *bref = nullptr, *out = nullptr,
-           *w = nullptr;
+           *w = nullptr, *part = nullptr;
     int64_t *p0 = nullptr, *p1 = nullptr, *x0 = nullptr, *x1 = nullptr;
     ~RwBuf() {
-        for (double* p : {e, c, mom, ld, a, beta, fnew, bt, bref, out, w}) cudaFree(p);
+        for (double* p : {e, c, mom, ld, a, beta, fnew, bt, bref, out, w, part}) cudaFree(p);
         for (int64_t* p : {p0, p1, x0, x1}) cudaFree(p);
     }
 };
@@ -222,12 +240,22 @@ int rw_solve(RwBuf& B, const double* beta, const double* n_k, int K, int64_t P, 
     std::vector<double> f(K, 0.0), fn(K), a(K);
     int it = 0;
     const int grid = rw_grid(P);
+    // slices per simulation: about four blocks per SM in all, at least 2048
+    // points per slice
+    int sms = 1, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int G = (int)std::max<int64_t>(
+        1, std::min<int64_t>((4 * (int64_t)sms + K - 1) / K, (P + 2047) / 2048));
+    ISG_CK(cudaMalloc((void**)&B.part, sizeof(double) * 2 * (size_t)K * G));
     for (it = 0; it < std::max(1, n_iter); ++it) {
         for (int k = 0; k < K; ++k) a[k] = std::log(n_k[k]) + f[k];
         ISG_CK(cudaMemcpyAsync(B.a, a.data(), sizeof(double) * K, cudaMemcpyHostToDevice, st));
         k_rw_denom<<<grid, kRwThreads, 0, st>>>(B.e, P, B.a, B.beta, K, B.ld);
         ISG_CK(cudaGetLastError());
-        k_rw_fnew<<<K, kRwThreads, 0, st>>>(B.e, B.c, P, B.ld, B.beta, B.fnew);
+        k_rw_fnew_part<<<dim3(K, G), kRwThreads, 0, st>>>(B.e, B.c, P, B.ld, B.beta, B.part);
+        ISG_CK(cudaGetLastError());
+        k_rw_fnew_merge<<<(K + 127) / 128, 128, 0, st>>>(B.part, K, G, B.fnew);
         ISG_CK(cudaGetLastError());
         ISG_CK(cudaMemcpyAsync(fn.data(), B.fnew, sizeof(double) * K, cudaMemcpyDeviceToHost, st));
         ISG_CK(cudaStreamSynchronize(st));

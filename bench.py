@@ -847,6 +847,37 @@ def run_learned(args):
     return 0
 
 
+def ncu_case_graph(kind: str):
+    """No timing: cases for ncu captures of the graph and reweighting kernels.
+    graph / cgraph3 / cgraph2: one 100-sweep launch on every replica of a BCC
+    8^3 graph (1024 nodes, 20 replicas) with a record every sweep;
+    reweight: one WHAM analysis of 20 x 100,000 samples."""
+    pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
+    if kind == "reweight":
+        V = 16 ** 3
+        rng = np.random.default_rng(SEED)
+        betas = np.linspace(1 / 4.60, 1 / 4.40, 20)
+        el = [rng.normal(-1.0 * V - 60000.0 * (b - betas[0]), 90.0, 100000) for b in betas]
+        ml = [np.clip(rng.normal(0.3 + 30.0 * (b - betas[0]), 0.05, 100000), 0, 1) for b in betas]
+        pkg.wham_reweight_fine(el, ml, betas, np.linspace(4.40, 4.60, 200), 16)
+        print("ncu case done")
+        return 0
+    g = pkg.GraphDef.bcc(8)
+    R = 20
+    if kind == "graph":
+        b = pkg.GraphBatch(g.n_nodes, g.edges, R, seed=SEED)
+        b.set_temperatures(pkg.linspace_temperatures(6.0, 6.7, R))
+    else:
+        b = pkg.ContinuousGraphBatch(g.n_nodes, g.edges, R, 3 if kind == "cgraph3" else 2,
+                                     seed=SEED)
+        b.set_temperatures(pkg.linspace_temperatures(1.5, 3.0, R))
+    b.step(50)
+    b.reset_sampling()
+    b.pt_run(100, 100, 1)
+    print("ncu case done")
+    return 0
+
+
 def ncu_case():
     pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
     b = pkg.IsingBatch([128], 96, seed=SEED)
@@ -874,13 +905,18 @@ def main():
     ap.add_argument("--train-seconds", type=float, default=60.0)
     ap.add_argument("--chain-batches", type=int, default=40)
     ap.add_argument("--pt-sweeps", type=int, default=200000)
-    ap.add_argument("--ncu-case", nargs="?", const="words", choices=["words", "resident"],
+    ap.add_argument("--ncu-case", nargs="?", const="words",
+                    choices=["words", "resident", "graph", "cgraph3", "cgraph2", "reweight"],
                     help="no timing: 'words' = a few half-sweeps of L=128 x 96 replicas (201 MB, "
                          "larger than L2) for an ncu capture of the half-sweep kernel; "
-                         "'resident' = one 2000-sweep schedule of an L=30 lattice")
+                         "'resident' = one 2000-sweep schedule of an L=30 lattice; "
+                         "'graph'/'cgraph3'/'cgraph2' = one 100-sweep launch of the graph "
+                         "kernels (BCC 8^3, 20 replicas); 'reweight' = one WHAM analysis")
     args = ap.parse_args()
     if args.ncu_case == "resident":
         return ncu_case_resident()
+    if args.ncu_case in ("graph", "cgraph3", "cgraph2", "reweight"):
+        return ncu_case_graph(args.ncu_case)
     if args.ncu_case:
         return ncu_case()
     if args.learned:

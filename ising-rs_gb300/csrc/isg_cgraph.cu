@@ -108,10 +108,16 @@ __device__ __forceinline__ void warp_store_ll(long long v, long long* slots) {
 // Fixed point of the measurement sums: 2^40 units per spin component.  Every
 // node term (|S.h| <= 64, |S_k| <= 1) converts exactly up to 2^-41, the int64
 // sums are exact and independent of their order (|sum| < 2^61).
-constexpr float kFixScale = 1099511627776.0f;
 constexpr double kFixInv = 1.0 / 1099511627776.0;
 
-__device__ __forceinline__ long long fix(float x) { return __float2ll_rn(x * kFixScale); }
+// round(x 2^40) for |x| <= 64 from two 32-bit conversions (the FP32 pipe; a
+// 64-bit conversion would run on the slow FP64 pipe): with h = floor(x 2^20),
+// x 2^20 - h is exact, so h 2^20 + round((x 2^20 - h) 2^20) = round(x 2^40).
+__device__ __forceinline__ long long fix(float x) {
+    const float y = x * 1048576.0f;
+    const float h = floorf(y);
+    return ((long long)__float2int_rn(h) << 20) + __float2int_rn((y - h) * 1048576.0f);
+}
 
 // O(2) measurement by gathering every node's neighbour field: per-warp sums
 // of sum_v S_v.h_v (twice the bond sum) and M in acc[0..2][32] (all threads

@@ -46,7 +46,8 @@ namespace isg {
 constexpr int kRwThreads = 256;
 constexpr int kRwMaxMom = 8;
 
-// (m, s) represents m + log s; merge two running log-sum-exps.
+// (m, s) represents m + log s; merge two running log-sum-exps.  A side more
+// than kLseCut below the other only rescales or drops (see k_rw_denom).
 __device__ __forceinline__ void lse_merge(double& m, double& s, double m2, double s2) {
     if (s2 == 0.0) return;
     if (s == 0.0) {
@@ -55,12 +56,17 @@ __device__ __forceinline__ void lse_merge(double& m, double& s, double m2, doubl
         return;
     }
     if (m2 > m) {
-        s = s * exp(m - m2) + s2;
+        s = (m - m2 > -40.0 ? s * exp(m - m2) : 0.0) + s2;
         m = m2;
-    } else {
+    } else if (m2 - m > -40.0) {
         s = s + s2 * exp(m2 - m);
     }
 }
+
+// Terms more than kLseCut below the largest of a log-sum-exp are left out:
+// e^-40 = 4e-18 is below half an ulp of the sum (>= 1), so an FP64 sum changes
+// by at most an ulp while most of the exp calls (on the slow FP64 pipe) go away.
+constexpr double kLseCut = 40.0;
 
 __global__ void k_rw_denom(const double* __restrict__ e, int64_t P, const double* __restrict__ a,
                            const double* __restrict__ beta, int K, double* __restrict__ ld) {
@@ -70,7 +76,10 @@ __global__ void k_rw_denom(const double* __restrict__ e, int64_t P, const double
         double mx = -INFINITY;
         for (int k = 0; k < K; ++k) mx = fmax(mx, a[k] - beta[k] * E);
         double s = 0.0;
-        for (int k = 0; k < K; ++k) s += exp(a[k] - beta[k] * E - mx);
+        for (int k = 0; k < K; ++k) {
+            const double d = a[k] - beta[k] * E - mx;
+            if (d > -kLseCut) s += exp(d);
+        }
         ld[p] = mx + log(s);
     }
 }
@@ -113,8 +122,9 @@ __global__ void k_rw_fnew_part(const double* __restrict__ e, const double* __res
     const double bk = beta[k];
     double m = 0.0, s = 0.0;
     for (int64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
-        if (!(c[p] > 0.0)) continue;
-        lse_merge(m, s, log(c[p]) - bk * e[p] - ld[p], 1.0);
+        const double cp = c[p];
+        if (!(cp > 0.0)) continue;
+        lse_merge(m, s, (cp == 1.0 ? 0.0 : log(cp)) - bk * e[p] - ld[p], 1.0);
     }
     block_lse(m, s, sm, ss);
     if (threadIdx.x == 0) {
@@ -176,6 +186,7 @@ __global__ void k_rw_obs(const double* __restrict__ e, const double* __restrict_
     for (int64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
         if (!(c[p] > 0.0) || (p >= xlo && p < xhi)) continue;
         const double x = mode == 1 ? -db * e[p] : -b * e[p] - ld[p];
+        if (x - X <= -kLseCut) continue;
         const double w = exp(x - X);
         const double wc = w * c[p];
         acc[0] += wc;

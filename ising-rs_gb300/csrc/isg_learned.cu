@@ -16,6 +16,10 @@
 // (the logit).  Hidden layers use ReLU; zero padding at the lattice edges.
 // Weights are stored in BF16 and all products accumulate in FP32; training
 // keeps FP32 master weights (Adam) and refreshes the BF16 copy every step.
+// Sampling and scoring run on the tensor cores (k_ar_mma, BF16 activations
+// between layers) when the network's activation rings fit in shared memory,
+// else on the CUDA cores (k_ar_run, FP32 activations); either way the same
+// kernel produces a proposal and scores it, so log q is consistent.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -390,6 +394,242 @@ __global__ void k_adopt(const int8_t* __restrict__ props, const long long* __res
         cur[i] = props[j * (long long)n + i];
 }
 
+// -------------------------------------------------- tensor-core AR kernel
+// The same network and random stream as k_ar_run, 16 configurations per CTA:
+// at every raster position each hidden layer is one [16 configs x 160] x
+// [160 x 32] product (5 taps x 32 input channels) on the tensor cores
+// (mma.sync m16n8k16, BF16 operands, FP32 accumulation), fed by ldmatrix from
+// the activation rings; layer 0 (1 input channel) runs on the CUDA cores.
+// Rings hold the last W+2 positions of every hidden layer's BF16 output, 64 B
+// per configuration row with the 16-byte chunks XOR-swizzled by (row >> 1) & 3
+// so that ldmatrix reads are conflict-free; the transposed weights (rows =
+// output channel, 160 k values, padded to 336 B rows) are staged once per CTA.
+// An M >= 64 tcgen05 tile would need >= 680 KB of ring history per CTA, so the
+// warp-level tensor instructions are the ones this per-position chain fits.
+constexpr int kMmaRows = 16;
+constexpr int kBtRow = 168;  // bf16 per transposed weight row (160 + 8 pad)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3,
+                                        uint32_t addr) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+}
+__device__ __forceinline__ void ldsm_x2(uint32_t& r0, uint32_t& r1, uint32_t addr) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n"
+                 : "=r"(r0), "=r"(r1)
+                 : "r"(addr));
+}
+__device__ __forceinline__ void mma_bf16(float* d, uint32_t a0, uint32_t a1, uint32_t a2,
+                                         uint32_t a3, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+// byte offset of (row, 16-byte chunk) in a ring slot tile of 16 rows x 64 B
+__device__ __forceinline__ uint32_t ring_off(int row, int chunk) {
+    return (uint32_t)(row * 64 + ((chunk ^ ((row >> 1) & 3)) << 4));
+}
+
+struct MmaSmem {
+    size_t rings, bt, btlast, w0, bias, spins, total;
+};
+__host__ __device__ inline MmaSmem mma_layout(int D, int W) {
+    MmaSmem m{};
+    const size_t slot = (size_t)kMmaRows * 64;
+    m.rings = 0;
+    m.bt = m.rings + (size_t)(D - 1) * (W + 2) * slot;
+    m.btlast = m.bt + (size_t)(D - 2) * kC * kBtRow * 2;
+    m.w0 = m.btlast + (size_t)8 * kBtRow * 2;
+    m.bias = m.w0 + sizeof(float) * 4 * kC;
+    m.spins = m.bias + sizeof(float) * ((size_t)(D - 1) * kC + 1);
+    m.total = m.spins + (size_t)(W + 2) * kMmaRows;
+    m.total = (m.total + 15) & ~(size_t)15;
+    return m;
+}
+
+// One tap (two k-steps of 16 input channels) of the 16 x 32 ring tile `tile`
+// into the 8-output-channel accumulator `acc`; `wrow` = the first of the 8
+// transposed weight rows of this output tile.
+__device__ __forceinline__ void mma_tap(float* acc, const unsigned char* tile,
+                                        const __nv_bfloat16* wrow, int t, int lane) {
+    // x4 over the tap's 32 k values: (n, k0-7) (n, k8-15) (n, k16-23) (n, k24-31)
+    uint32_t b0, b1, b2, b3;
+    ldsm_x4(b0, b1, b2, b3, smem_u32(wrow + (lane & 7) * kBtRow + t * kC + (lane >> 3) * 8));
+#pragma unroll
+    for (int kb = 0; kb < 2; ++kb) {
+        uint32_t a0, a1, a2, a3;
+        ldsm_x4(a0, a1, a2, a3, smem_u32(tile + ring_off(lane & 15, 2 * kb + (lane >> 4))));
+        if (kb == 0)
+            mma_bf16(acc, a0, a1, a2, a3, b0, b1);
+        else
+            mma_bf16(acc, a0, a1, a2, a3, b2, b3);
+    }
+}
+
+// mode / flip / stream exactly as k_ar_run.  A CTA of four warps owns 16
+// configurations: warp w computes output channels 8w..8w+7 of every hidden
+// layer (one n-tile), so all four SM sub-partitions issue tensor instructions
+// while the CTA's rings (the shared-memory limit) hold one group.  At every
+// position the four taps that look back at earlier positions are accumulated
+// first for all layers (independent work); only the centre tap, which needs
+// the layer below at this position, stays on the layer-to-layer critical path.
+template <int D>
+__global__ void __launch_bounds__(128)
+    k_ar_mma(const __nv_bfloat16* __restrict__ w, NetShape S, int H, int W, int mode, int flip,
+             int8_t* __restrict__ spins, float* __restrict__ logq, int n_cfg, uint64_t seed,
+             uint64_t step) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const MmaSmem L = mma_layout(D, W);
+    unsigned char* rings = smem + L.rings;
+    __nv_bfloat16* bt = reinterpret_cast<__nv_bfloat16*>(smem + L.bt);
+    __nv_bfloat16* btl = reinterpret_cast<__nv_bfloat16*>(smem + L.btlast);
+    float* w0 = reinterpret_cast<float*>(smem + L.w0);
+    float* bias = reinterpret_cast<float*>(smem + L.bias);
+    int8_t* sring = reinterpret_cast<int8_t*>(smem + L.spins);
+    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
+    const int ring = W + 2;
+    const size_t slot_bytes = (size_t)kMmaRows * 64;
+    const int HW = H * W;
+    const int cfg0 = blockIdx.x * kMmaRows;
+    // stage the weights: hidden layers l = 1..D-2 as bt[l-1][n][tap*32 + ci],
+    // the last layer as btl[n][..] (only n = 0 nonzero), layer 0 and biases FP32
+    for (int l = 1; l < D - 1; ++l) {
+        __nv_bfloat16* b = bt + (size_t)(l - 1) * kC * kBtRow;
+        for (int i = tid; i < kC * kBtRow; i += blockDim.x) {
+            const int n = i / kBtRow, k = i - n * kBtRow;
+            b[i] = k < 5 * kC ? w[S.woff[l] + k * kC + n] : __float2bfloat16(0.f);
+        }
+    }
+    for (int i = tid; i < 8 * kBtRow; i += blockDim.x) {
+        const int n = i / kBtRow, k = i - n * kBtRow;
+        btl[i] = (n == 0 && k < 5 * kC) ? w[S.woff[D - 1] + k] : __float2bfloat16(0.f);
+    }
+    for (int i = tid; i < 4 * kC; i += blockDim.x) w0[i] = bf(w, S.woff[0] + i);
+    for (int l = 0; l < D - 1; ++l)
+        for (int i = tid; i < kC; i += blockDim.x) bias[l * kC + i] = bf(w, S.boff[l] + i);
+    if (tid == 0) bias[(D - 1) * kC] = bf(w, S.boff[D - 1]);
+    __syncthreads();
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    const uint32_t c3 = counter_word3(kTagLearn, 0, step);
+    const int g = lane >> 2, q4 = lane & 3;
+    // warp 0, lanes 4g: configurations g and g+8 (logit rows of the last layer)
+    const int ca = cfg0 + g, cb = cfg0 + g + 8;
+    float lqa = 0.f, lqb = 0.f;
+    for (int p = 0; p < HW; ++p) {
+        const int y = p / W, x = p - y * W;
+        const int slot = p % ring;
+        const bool up = y > 0, left = x > 0, right = x + 1 < W;
+        // mask-B taps (-1,-1) (-1,0) (-1,+1) (0,-1); the centre (0,0) is `slot`
+        const int ts0 = (p - W - 1 + 2 * ring) % ring, ts1 = (p - W + 2 * ring) % ring;
+        const int ts2 = (p - W + 1 + 2 * ring) % ring, ts3 = (p - 1 + ring) % ring;
+        const bool ok0 = up && left, ok1 = up, ok2 = up && right, ok3 = left;
+        // phase 1: look-back taps of every layer (the last layer on warp 0)
+        float acc[D - 1][4];
+#pragma unroll
+        for (int l = 1; l < D; ++l) {
+            const bool last = l == D - 1;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[l - 1][e] = 0.f;
+            if (last && wp != 0) continue;
+            const unsigned char* in = rings + (size_t)(l - 1) * ring * slot_bytes;
+            const __nv_bfloat16* wrow =
+                last ? btl : bt + ((size_t)(l - 1) * kC + 8 * wp) * kBtRow;
+            if (ok0) mma_tap(acc[l - 1], in + ts0 * slot_bytes, wrow, 0, lane);
+            if (ok1) mma_tap(acc[l - 1], in + ts1 * slot_bytes, wrow, 1, lane);
+            if (ok2) mma_tap(acc[l - 1], in + ts2 * slot_bytes, wrow, 2, lane);
+            if (ok3) mma_tap(acc[l - 1], in + ts3 * slot_bytes, wrow, 3, lane);
+        }
+        // layer 0 (mask A, 1 -> 32): thread = 8 r + j computes channels 4j..4j+3
+        {
+            const int r = tid >> 3, j = tid & 7;
+            const float sv0 = ok0 ? (float)sring[ts0 * kMmaRows + r] : 0.f;
+            const float sv1 = ok1 ? (float)sring[ts1 * kMmaRows + r] : 0.f;
+            const float sv2 = ok2 ? (float)sring[ts2 * kMmaRows + r] : 0.f;
+            const float sv3 = ok3 ? (float)sring[ts3 * kMmaRows + r] : 0.f;
+            uint32_t packed[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                float v[2];
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const int co = 4 * j + 2 * h + e;
+                    float a = bias[co];
+                    a = fmaf(w0[0 * kC + co], sv0, a);
+                    a = fmaf(w0[1 * kC + co], sv1, a);
+                    a = fmaf(w0[2 * kC + co], sv2, a);
+                    a = fmaf(w0[3 * kC + co], sv3, a);
+                    v[e] = fmaxf(a, 0.f);
+                }
+                __nv_bfloat162 b2 = __floats2bfloat162_rn(v[0], v[1]);
+                packed[h] = *reinterpret_cast<uint32_t*>(&b2);
+            }
+            unsigned char* base = rings + (size_t)slot * slot_bytes;
+            *reinterpret_cast<uint2*>(base + ring_off(r, j >> 1) + (j & 1) * 8) =
+                make_uint2(packed[0], packed[1]);
+        }
+        __syncthreads();
+        // phase 2: centre tap layer by layer
+#pragma unroll
+        for (int l = 1; l < D; ++l) {
+            const bool last = l == D - 1;
+            const unsigned char* in = rings + ((size_t)(l - 1) * ring + slot) * slot_bytes;
+            if (!last) {
+                mma_tap(acc[l - 1], in, bt + ((size_t)(l - 1) * kC + 8 * wp) * kBtRow, 4, lane);
+                unsigned char* out = rings + ((size_t)l * ring + slot) * slot_bytes;
+                const int col = wp * 8 + 2 * q4;
+                const float b0 = bias[l * kC + col], b1 = bias[l * kC + col + 1];
+                __nv_bfloat162 lo = __floats2bfloat162_rn(fmaxf(acc[l - 1][0] + b0, 0.f),
+                                                          fmaxf(acc[l - 1][1] + b1, 0.f));
+                __nv_bfloat162 hi = __floats2bfloat162_rn(fmaxf(acc[l - 1][2] + b0, 0.f),
+                                                          fmaxf(acc[l - 1][3] + b1, 0.f));
+                *reinterpret_cast<__nv_bfloat162*>(out + ring_off(g, wp) + q4 * 4) = lo;
+                *reinterpret_cast<__nv_bfloat162*>(out + ring_off(g + 8, wp) + q4 * 4) = hi;
+                __syncthreads();
+            } else if (wp == 0) {
+                mma_tap(acc[l - 1], in, btl, 4, lane);
+                if (q4 == 0) {
+                    const float bl = bias[(D - 1) * kC];
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const int c = e == 0 ? ca : cb;
+                        const float z = (e == 0 ? acc[l - 1][0] : acc[l - 1][2]) + bl;
+                        const int row = e == 0 ? g : g + 8;
+                        int8_t sv = 1;
+                        if (c < n_cfg) {
+                            if (mode == 0) {
+                                const U4 u = philox10((uint32_t)c, (uint32_t)p, (uint32_t)step, c3,
+                                                      k0, k1);
+                                const float pr = 1.0f / (1.0f + __expf(-z));
+                                sv = uniform24(u.x) < pr ? (int8_t)1 : (int8_t)-1;
+                                spins[(size_t)c * HW + p] = sv;
+                            } else {
+                                sv = spins[(size_t)c * HW + p];
+                                if (flip) sv = (int8_t)-sv;
+                            }
+                            if (e == 0)
+                                lqa += log_sigmoid((float)sv * z);
+                            else
+                                lqb += log_sigmoid((float)sv * z);
+                        }
+                        sring[slot * kMmaRows + row] = sv;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (wp == 0 && q4 == 0) {
+        if (ca < n_cfg) logq[ca] = lqa;
+        if (cb < n_cfg) logq[cb] = lqb;
+    }
+}
+
 __global__ void k_to_float(const int8_t* __restrict__ s, float* __restrict__ f, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -431,8 +671,46 @@ static int grid_for(int64_t n, int thr) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((n + thr - 1) / thr, 152 * 32));
 }
 
-static size_t ar_smem(const isg_learned* h, int G) {
-    return (size_t)(h->D - 1) * (h->W + 2) * G * kC * sizeof(float) + (size_t)G * h->H * h->W;
+// The tensor-core kernel when its rings and weights fit in shared memory.
+static bool use_mma(const isg_learned* h) {
+    return h->D >= 2 && h->D <= 8 && mma_layout(h->D, h->W).total <= 232448;
+}
+
+template <int D>
+static int launch_mma(isg_learned* h, int mode, int flip, int8_t* spins, float* lq, int K,
+                      uint64_t step) {
+    const size_t smem = mma_layout(D, h->W).total;
+    ISG_CK(cudaFuncSetAttribute(k_ar_mma<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+    k_ar_mma<D><<<(K + kMmaRows - 1) / kMmaRows, 128, smem, h->stream>>>(
+        h->d_wbf, h->S, h->H, h->W, mode, flip, spins, lq, K, h->seed, step);
+    ISG_CK(cudaGetLastError());
+    return ISG_OK;
+}
+
+static int launch_ar(isg_learned* h, int mode, int flip, int8_t* spins, float* lq, int K,
+                     uint64_t step) {
+    if (use_mma(h)) {
+        switch (h->D) {
+            case 2: return launch_mma<2>(h, mode, flip, spins, lq, K, step);
+            case 3: return launch_mma<3>(h, mode, flip, spins, lq, K, step);
+            case 4: return launch_mma<4>(h, mode, flip, spins, lq, K, step);
+            case 5: return launch_mma<5>(h, mode, flip, spins, lq, K, step);
+            case 6: return launch_mma<6>(h, mode, flip, spins, lq, K, step);
+            case 7: return launch_mma<7>(h, mode, flip, spins, lq, K, step);
+            default: return launch_mma<8>(h, mode, flip, spins, lq, K, step);
+        }
+    } else {
+        constexpr int G = 4;
+        const size_t smem = (size_t)(h->D - 1) * (h->W + 2) * G * kC * sizeof(float) +
+                            (size_t)G * h->H * h->W;
+        ISG_CK(cudaFuncSetAttribute(k_ar_run<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+        k_ar_run<G><<<(K + G - 1) / G, G * kC, smem, h->stream>>>(
+            h->d_wbf, h->S, h->H, h->W, mode, flip, spins, lq, K, h->seed, step);
+    }
+    ISG_CK(cudaGetLastError());
+    return ISG_OK;
 }
 
 static int ensure_train(isg_learned* h, int B) {
@@ -681,18 +959,9 @@ int isg_learned_sample(isg_learned* h, int K, uint64_t step, int8_t* d_out, floa
                        float* d_lq_flip) {
     if (!h || !d_out || !d_lq || K < 1) return fail(ISG_ERR_ARG, "isg_learned_sample: bad argument");
     cudaSetDevice(h->device);
-    constexpr int G = 4;
-    const size_t smem = ar_smem(h, G);
-    ISG_CK(cudaFuncSetAttribute(k_ar_run<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem));
-    const int blocks = (K + G - 1) / G;
-    k_ar_run<G><<<blocks, G * kC, smem, h->stream>>>(h->d_wbf, h->S, h->H, h->W, 0, 0, d_out,
-                                                      d_lq, K, h->seed, step);
-    if (d_lq_flip)
-        k_ar_run<G><<<blocks, G * kC, smem, h->stream>>>(h->d_wbf, h->S, h->H, h->W, 1, 1, d_out,
-                                                          d_lq_flip, K, h->seed, step);
-    ISG_CK(cudaGetLastError());
-    return ISG_OK;
+    int rc = launch_ar(h, 0, 0, d_out, d_lq, K, step);
+    if (!rc && d_lq_flip) rc = launch_ar(h, 1, 1, d_out, d_lq_flip, K, step);
+    return rc;
 }
 
 // log q of K given configurations (device, natural layout): scoring mode of
@@ -700,15 +969,7 @@ int isg_learned_sample(isg_learned* h, int K, uint64_t step, int8_t* d_out, floa
 int isg_learned_score(isg_learned* h, const int8_t* d_cfg, int K, int flip, float* d_lq) {
     if (!h || !d_cfg || !d_lq || K < 1) return fail(ISG_ERR_ARG, "isg_learned_score: bad argument");
     cudaSetDevice(h->device);
-    constexpr int G = 4;
-    const size_t smem = ar_smem(h, G);
-    ISG_CK(cudaFuncSetAttribute(k_ar_run<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem));
-    k_ar_run<G><<<(K + G - 1) / G, G * kC, smem, h->stream>>>(
-        h->d_wbf, h->S, h->H, h->W, 1, flip ? 1 : 0, const_cast<int8_t*>(d_cfg), d_lq, K, h->seed,
-        0);
-    ISG_CK(cudaGetLastError());
-    return ISG_OK;
+    return launch_ar(h, 1, flip ? 1 : 0, const_cast<int8_t*>(d_cfg), d_lq, K, 0);
 }
 
 // Exact energies (bond sum, magnetisation) of K configurations of a periodic

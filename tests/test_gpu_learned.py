@@ -6,7 +6,8 @@ Metropolis-Hastings chain checked against exact enumeration.
 
 Tolerances: gradients 2e-3 relative to the largest gradient of the layer plus
 1e-5 absolute (FP32 accumulation in different orders); torch log q agreement
-2e-3 absolute per configuration; normalisation 1e-4."""
+2e-3 absolute per configuration (the sampling kernel's BF16 hidden activations
+restated in torch); normalisation 1e-4."""
 from __future__ import annotations
 
 import itertools
@@ -22,8 +23,10 @@ def learned(pkg):
     return importlib.import_module(pkg.__name__ + ".learned")
 
 
-def torch_logq(w, D, H, W, cfg):
-    """torch FP32 restatement of the network (masks as zeroed 3x3 taps)."""
+def torch_logq(w, D, H, W, cfg, bf16_acts=False):
+    """torch FP32 restatement of the network (masks as zeroed 3x3 taps);
+    bf16_acts rounds the hidden activations to BF16 as the tensor-core
+    sampling kernel stores them."""
     import torch
     import torch.nn.functional as F
     taps = [(-1, -1), (-1, 0), (-1, 1), (0, -1), (0, 0)]
@@ -46,6 +49,8 @@ def torch_logq(w, D, H, W, cfg):
         x = F.conv2d(x, K, b, padding=1)
         if l < D - 1:
             x = torch.relu(x)
+            if bf16_acts:
+                x = x.to(torch.bfloat16).float()
     logits = x.view(-1, H * W)
     return F.logsigmoid(cfg.view(-1, H * W) * logits).sum(1)
 
@@ -83,7 +88,7 @@ def test_sample_score_identical_and_matches_torch(gpu):
     q.sync()
     assert torch.equal(lq, s1) and torch.equal(lqf, s2)
     assert set(torch.unique(props).tolist()) <= {-1, 1}
-    ref = torch_logq(torch.tensor(q.weights()), 6, H, W, props.cpu().float())
+    ref = torch_logq(torch.tensor(q.weights()), 6, H, W, props.cpu().float(), bf16_acts=True)
     assert torch.max(torch.abs(ref - lq.cpu())) < 2e-3
     # the same step reproduces the same proposals; another step gives others
     p2, l2, _ = q.sample(64, 3)

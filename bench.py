@@ -848,11 +848,23 @@ def run_learned(args):
 
 
 def ncu_case_graph(kind: str):
-    """No timing: cases for ncu captures of the graph and reweighting kernels.
-    graph / cgraph3 / cgraph2: one 100-sweep launch on every replica of a BCC
-    8^3 graph (1024 nodes, 20 replicas) with a record every sweep;
-    reweight: one WHAM analysis of 20 x 100,000 samples."""
+    """No timing: cases for ncu captures of the graph, reweighting and learned
+    kernels.  graph / cgraph3 / cgraph2: one 100-sweep launch on every replica
+    of a BCC 8^3 graph (1024 nodes, 20 replicas) with a record every sweep;
+    reweight: one WHAM analysis of 20 x 100,000 samples; learned: 4096
+    proposals of the untrained 2D L=32 network (sampling, then the flipped
+    scores)."""
     pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
+    if kind == "learned":
+        import importlib
+        import torch
+        torch.cuda.set_device(0)
+        lrn = importlib.import_module(pkg.__name__ + ".learned")
+        q = lrn.LearnedProposal(32, 32, layers=6, seed=SEED)
+        q.sample(4096, 1)
+        q.sync()
+        print("ncu case done")
+        return 0
     if kind == "reweight":
         V = 16 ** 3
         rng = np.random.default_rng(SEED)
@@ -906,16 +918,18 @@ def main():
     ap.add_argument("--chain-batches", type=int, default=40)
     ap.add_argument("--pt-sweeps", type=int, default=200000)
     ap.add_argument("--ncu-case", nargs="?", const="words",
-                    choices=["words", "resident", "graph", "cgraph3", "cgraph2", "reweight"],
+                    choices=["words", "resident", "graph", "cgraph3", "cgraph2", "reweight",
+                             "learned"],
                     help="no timing: 'words' = a few half-sweeps of L=128 x 96 replicas (201 MB, "
                          "larger than L2) for an ncu capture of the half-sweep kernel; "
                          "'resident' = one 2000-sweep schedule of an L=30 lattice; "
                          "'graph'/'cgraph3'/'cgraph2' = one 100-sweep launch of the graph "
-                         "kernels (BCC 8^3, 20 replicas); 'reweight' = one WHAM analysis")
+                         "kernels (BCC 8^3, 20 replicas); 'reweight' = one WHAM analysis; "
+                         "'learned' = 4096 proposals of the L=32 network (sample + score)")
     args = ap.parse_args()
     if args.ncu_case == "resident":
         return ncu_case_resident()
-    if args.ncu_case in ("graph", "cgraph3", "cgraph2", "reweight"):
+    if args.ncu_case in ("graph", "cgraph3", "cgraph2", "reweight", "learned"):
         return ncu_case_graph(args.ncu_case)
     if args.ncu_case:
         return ncu_case()

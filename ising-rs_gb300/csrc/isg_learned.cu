@@ -418,11 +418,6 @@ __device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2
                  : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
                  : "r"(addr));
 }
-__device__ __forceinline__ void ldsm_x2(uint32_t& r0, uint32_t& r1, uint32_t addr) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n"
-                 : "=r"(r0), "=r"(r1)
-                 : "r"(addr));
-}
 __device__ __forceinline__ void mma_bf16(float* d, uint32_t a0, uint32_t a1, uint32_t a2,
                                          uint32_t a3, uint32_t b0, uint32_t b1) {
     asm volatile(
@@ -453,23 +448,19 @@ __host__ __device__ inline MmaSmem mma_layout(int D, int W) {
     return m;
 }
 
-// One tap (two k-steps of 16 input channels) of the 16 x 32 ring tile `tile`
-// into the 8-output-channel accumulator `acc`; `wrow` = the first of the 8
-// transposed weight rows of this output tile.
-__device__ __forceinline__ void mma_tap(float* acc, const unsigned char* tile,
-                                        const __nv_bfloat16* wrow, int t, int lane) {
+// One tap (two k-steps of 16 input channels) of a 16 x 32 ring tile into the
+// 8-output-channel accumulator `acc`.  Shared-memory byte addresses: `tile` =
+// the tile, `aoff0/1` = this lane's ldmatrix row/chunk offsets for k-steps 0/1,
+// `wrow` = this lane's row/column in the tap's block of transposed weights.
+__device__ __forceinline__ void mma_tap(float* acc, uint32_t tile, uint32_t aoff0, uint32_t aoff1,
+                                        uint32_t wrow) {
     // x4 over the tap's 32 k values: (n, k0-7) (n, k8-15) (n, k16-23) (n, k24-31)
-    uint32_t b0, b1, b2, b3;
-    ldsm_x4(b0, b1, b2, b3, smem_u32(wrow + (lane & 7) * kBtRow + t * kC + (lane >> 3) * 8));
-#pragma unroll
-    for (int kb = 0; kb < 2; ++kb) {
-        uint32_t a0, a1, a2, a3;
-        ldsm_x4(a0, a1, a2, a3, smem_u32(tile + ring_off(lane & 15, 2 * kb + (lane >> 4))));
-        if (kb == 0)
-            mma_bf16(acc, a0, a1, a2, a3, b0, b1);
-        else
-            mma_bf16(acc, a0, a1, a2, a3, b2, b3);
-    }
+    uint32_t b0, b1, b2, b3, a0, a1, a2, a3;
+    ldsm_x4(b0, b1, b2, b3, wrow);
+    ldsm_x4(a0, a1, a2, a3, tile + aoff0);
+    mma_bf16(acc, a0, a1, a2, a3, b0, b1);
+    ldsm_x4(a0, a1, a2, a3, tile + aoff1);
+    mma_bf16(acc, a0, a1, a2, a3, b2, b3);
 }
 
 // mode / flip / stream exactly as k_ar_run.  A CTA of four warps owns 16
@@ -479,6 +470,8 @@ __device__ __forceinline__ void mma_tap(float* acc, const unsigned char* tile,
 // position the four taps that look back at earlier positions are accumulated
 // first for all layers (independent work); only the centre tap, which needs
 // the layer below at this position, stays on the layer-to-layer critical path.
+// Addresses are 32-bit shared-memory offsets fixed per lane; the layer-0
+// weights and the epilogue biases of a thread live in registers.
 template <int D>
 __global__ void __launch_bounds__(128)
     k_ar_mma(const __nv_bfloat16* __restrict__ w, NetShape S, int H, int W, int mode, int flip,
@@ -489,16 +482,16 @@ __global__ void __launch_bounds__(128)
     unsigned char* rings = smem + L.rings;
     __nv_bfloat16* bt = reinterpret_cast<__nv_bfloat16*>(smem + L.bt);
     __nv_bfloat16* btl = reinterpret_cast<__nv_bfloat16*>(smem + L.btlast);
-    float* w0 = reinterpret_cast<float*>(smem + L.w0);
-    float* bias = reinterpret_cast<float*>(smem + L.bias);
     int8_t* sring = reinterpret_cast<int8_t*>(smem + L.spins);
     const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
     const int ring = W + 2;
-    const size_t slot_bytes = (size_t)kMmaRows * 64;
+    constexpr uint32_t kSlot = kMmaRows * 64;        // bytes of one ring slot
+    constexpr uint32_t kWRow = kBtRow * 2;           // bytes of one weight row
+    const uint32_t lstride = (uint32_t)ring * kSlot; // bytes of one layer's ring
     const int HW = H * W;
     const int cfg0 = blockIdx.x * kMmaRows;
     // stage the weights: hidden layers l = 1..D-2 as bt[l-1][n][tap*32 + ci],
-    // the last layer as btl[n][..] (only n = 0 nonzero), layer 0 and biases FP32
+    // the last layer as btl[n][..] (only n = 0 nonzero)
     for (int l = 1; l < D - 1; ++l) {
         __nv_bfloat16* b = bt + (size_t)(l - 1) * kC * kBtRow;
         for (int i = tid; i < kC * kBtRow; i += blockDim.x) {
@@ -510,25 +503,50 @@ __global__ void __launch_bounds__(128)
         const int n = i / kBtRow, k = i - n * kBtRow;
         btl[i] = (n == 0 && k < 5 * kC) ? w[S.woff[D - 1] + k] : __float2bfloat16(0.f);
     }
-    for (int i = tid; i < 4 * kC; i += blockDim.x) w0[i] = bf(w, S.woff[0] + i);
-    for (int l = 0; l < D - 1; ++l)
-        for (int i = tid; i < kC; i += blockDim.x) bias[l * kC + i] = bf(w, S.boff[l] + i);
-    if (tid == 0) bias[(D - 1) * kC] = bf(w, S.boff[D - 1]);
+    // layer 0: thread = 8 r + j computes channels 4j..4j+3 of configuration r
+    const int r0 = tid >> 3, j0 = tid & 7;
+    float w0r[4][4], b0r[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        b0r[e] = bf(w, S.boff[0] + 4 * j0 + e);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) w0r[t][e] = bf(w, S.woff[0] + t * kC + 4 * j0 + e);
+    }
+    const int g = lane >> 2, q4 = lane & 3;
+    // epilogue biases of this lane's two columns in every hidden layer
+    float bh[D > 2 ? D - 2 : 1][2];
+#pragma unroll
+    for (int l = 1; l < D - 1; ++l) {
+        bh[l - 1][0] = bf(w, S.boff[l] + wp * 8 + 2 * q4);
+        bh[l - 1][1] = bf(w, S.boff[l] + wp * 8 + 2 * q4 + 1);
+    }
+    const float blast = bf(w, S.boff[D - 1]);
     __syncthreads();
+    const uint32_t rings_s = smem_u32(rings);
+    const uint32_t aoff0 = (uint32_t)ring_off(lane & 15, lane >> 4);
+    const uint32_t aoff1 = (uint32_t)ring_off(lane & 15, 2 + (lane >> 4));
+    const uint32_t blane = (uint32_t)((lane & 7) * kWRow + (lane >> 3) * 16);
+    const uint32_t wbase = smem_u32(bt) + (uint32_t)(8 * wp) * kWRow + blane;
+    const uint32_t wlast = smem_u32(btl) + blane;
+    const uint32_t eoff0 = (uint32_t)ring_off(g, wp) + 4 * q4;
+    const uint32_t eoff1 = (uint32_t)ring_off(g + 8, wp) + 4 * q4;
+    const uint32_t l0off = (uint32_t)ring_off(r0, j0 >> 1) + (j0 & 1) * 8;
     const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
     const uint32_t c3 = counter_word3(kTagLearn, 0, step);
-    const int g = lane >> 2, q4 = lane & 3;
     // warp 0, lanes 4g: configurations g and g+8 (logit rows of the last layer)
     const int ca = cfg0 + g, cb = cfg0 + g + 8;
     float lqa = 0.f, lqb = 0.f;
+    int y = 0, x = 0;
     for (int p = 0; p < HW; ++p) {
-        const int y = p / W, x = p - y * W;
         const int slot = p % ring;
         const bool up = y > 0, left = x > 0, right = x + 1 < W;
         // mask-B taps (-1,-1) (-1,0) (-1,+1) (0,-1); the centre (0,0) is `slot`
         const int ts0 = (p - W - 1 + 2 * ring) % ring, ts1 = (p - W + 2 * ring) % ring;
         const int ts2 = (p - W + 1 + 2 * ring) % ring, ts3 = (p - 1 + ring) % ring;
         const bool ok0 = up && left, ok1 = up, ok2 = up && right, ok3 = left;
+        const uint32_t o0 = rings_s + (uint32_t)ts0 * kSlot, o1 = rings_s + (uint32_t)ts1 * kSlot;
+        const uint32_t o2 = rings_s + (uint32_t)ts2 * kSlot, o3 = rings_s + (uint32_t)ts3 * kSlot;
+        const uint32_t oc = rings_s + (uint32_t)slot * kSlot;
         // phase 1: look-back taps of every layer (the last layer on warp 0)
         float acc[D - 1][4];
 #pragma unroll
@@ -537,68 +555,58 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
             for (int e = 0; e < 4; ++e) acc[l - 1][e] = 0.f;
             if (last && wp != 0) continue;
-            const unsigned char* in = rings + (size_t)(l - 1) * ring * slot_bytes;
-            const __nv_bfloat16* wrow =
-                last ? btl : bt + ((size_t)(l - 1) * kC + 8 * wp) * kBtRow;
-            if (ok0) mma_tap(acc[l - 1], in + ts0 * slot_bytes, wrow, 0, lane);
-            if (ok1) mma_tap(acc[l - 1], in + ts1 * slot_bytes, wrow, 1, lane);
-            if (ok2) mma_tap(acc[l - 1], in + ts2 * slot_bytes, wrow, 2, lane);
-            if (ok3) mma_tap(acc[l - 1], in + ts3 * slot_bytes, wrow, 3, lane);
+            const uint32_t lo = (uint32_t)(l - 1) * lstride;
+            const uint32_t wr = last ? wlast : wbase + (uint32_t)((l - 1) * kC) * kWRow;
+            if (ok0) mma_tap(acc[l - 1], o0 + lo, aoff0, aoff1, wr + 0 * kC * 2);
+            if (ok1) mma_tap(acc[l - 1], o1 + lo, aoff0, aoff1, wr + 1 * kC * 2);
+            if (ok2) mma_tap(acc[l - 1], o2 + lo, aoff0, aoff1, wr + 2 * kC * 2);
+            if (ok3) mma_tap(acc[l - 1], o3 + lo, aoff0, aoff1, wr + 3 * kC * 2);
         }
-        // layer 0 (mask A, 1 -> 32): thread = 8 r + j computes channels 4j..4j+3
+        // layer 0 (mask A, 1 -> 32)
         {
-            const int r = tid >> 3, j = tid & 7;
-            const float sv0 = ok0 ? (float)sring[ts0 * kMmaRows + r] : 0.f;
-            const float sv1 = ok1 ? (float)sring[ts1 * kMmaRows + r] : 0.f;
-            const float sv2 = ok2 ? (float)sring[ts2 * kMmaRows + r] : 0.f;
-            const float sv3 = ok3 ? (float)sring[ts3 * kMmaRows + r] : 0.f;
-            uint32_t packed[2];
+            const float sv0 = ok0 ? (float)sring[ts0 * kMmaRows + r0] : 0.f;
+            const float sv1 = ok1 ? (float)sring[ts1 * kMmaRows + r0] : 0.f;
+            const float sv2 = ok2 ? (float)sring[ts2 * kMmaRows + r0] : 0.f;
+            const float sv3 = ok3 ? (float)sring[ts3 * kMmaRows + r0] : 0.f;
+            float v[4];
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                float v[2];
-#pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    const int co = 4 * j + 2 * h + e;
-                    float a = bias[co];
-                    a = fmaf(w0[0 * kC + co], sv0, a);
-                    a = fmaf(w0[1 * kC + co], sv1, a);
-                    a = fmaf(w0[2 * kC + co], sv2, a);
-                    a = fmaf(w0[3 * kC + co], sv3, a);
-                    v[e] = fmaxf(a, 0.f);
-                }
-                __nv_bfloat162 b2 = __floats2bfloat162_rn(v[0], v[1]);
-                packed[h] = *reinterpret_cast<uint32_t*>(&b2);
+            for (int e = 0; e < 4; ++e) {
+                float a = b0r[e];
+                a = fmaf(w0r[0][e], sv0, a);
+                a = fmaf(w0r[1][e], sv1, a);
+                a = fmaf(w0r[2][e], sv2, a);
+                a = fmaf(w0r[3][e], sv3, a);
+                v[e] = fmaxf(a, 0.f);
             }
-            unsigned char* base = rings + (size_t)slot * slot_bytes;
-            *reinterpret_cast<uint2*>(base + ring_off(r, j >> 1) + (j & 1) * 8) =
-                make_uint2(packed[0], packed[1]);
+            __nv_bfloat162 p0 = __floats2bfloat162_rn(v[0], v[1]);
+            __nv_bfloat162 p1 = __floats2bfloat162_rn(v[2], v[3]);
+            *reinterpret_cast<uint2*>(rings + (size_t)slot * kSlot + l0off) =
+                make_uint2(*reinterpret_cast<uint32_t*>(&p0), *reinterpret_cast<uint32_t*>(&p1));
         }
         __syncthreads();
         // phase 2: centre tap layer by layer
 #pragma unroll
         for (int l = 1; l < D; ++l) {
             const bool last = l == D - 1;
-            const unsigned char* in = rings + ((size_t)(l - 1) * ring + slot) * slot_bytes;
+            const uint32_t in = oc + (uint32_t)(l - 1) * lstride;
             if (!last) {
-                mma_tap(acc[l - 1], in, bt + ((size_t)(l - 1) * kC + 8 * wp) * kBtRow, 4, lane);
-                unsigned char* out = rings + ((size_t)l * ring + slot) * slot_bytes;
-                const int col = wp * 8 + 2 * q4;
-                const float b0 = bias[l * kC + col], b1 = bias[l * kC + col + 1];
-                __nv_bfloat162 lo = __floats2bfloat162_rn(fmaxf(acc[l - 1][0] + b0, 0.f),
-                                                          fmaxf(acc[l - 1][1] + b1, 0.f));
-                __nv_bfloat162 hi = __floats2bfloat162_rn(fmaxf(acc[l - 1][2] + b0, 0.f),
-                                                          fmaxf(acc[l - 1][3] + b1, 0.f));
-                *reinterpret_cast<__nv_bfloat162*>(out + ring_off(g, wp) + q4 * 4) = lo;
-                *reinterpret_cast<__nv_bfloat162*>(out + ring_off(g + 8, wp) + q4 * 4) = hi;
+                mma_tap(acc[l - 1], in, aoff0, aoff1,
+                        wbase + (uint32_t)((l - 1) * kC) * kWRow + 4 * kC * 2);
+                unsigned char* out = rings + (size_t)l * lstride + (size_t)slot * kSlot;
+                __nv_bfloat162 lo = __floats2bfloat162_rn(fmaxf(acc[l - 1][0] + bh[l - 1][0], 0.f),
+                                                          fmaxf(acc[l - 1][1] + bh[l - 1][1], 0.f));
+                __nv_bfloat162 hi = __floats2bfloat162_rn(fmaxf(acc[l - 1][2] + bh[l - 1][0], 0.f),
+                                                          fmaxf(acc[l - 1][3] + bh[l - 1][1], 0.f));
+                *reinterpret_cast<__nv_bfloat162*>(out + eoff0) = lo;
+                *reinterpret_cast<__nv_bfloat162*>(out + eoff1) = hi;
                 __syncthreads();
             } else if (wp == 0) {
-                mma_tap(acc[l - 1], in, btl, 4, lane);
+                mma_tap(acc[l - 1], in, aoff0, aoff1, wlast + 4 * kC * 2);
                 if (q4 == 0) {
-                    const float bl = bias[(D - 1) * kC];
 #pragma unroll
                     for (int e = 0; e < 2; ++e) {
                         const int c = e == 0 ? ca : cb;
-                        const float z = (e == 0 ? acc[l - 1][0] : acc[l - 1][2]) + bl;
+                        const float z = (e == 0 ? acc[l - 1][0] : acc[l - 1][2]) + blast;
                         const int row = e == 0 ? g : g + 8;
                         int8_t sv = 1;
                         if (c < n_cfg) {
@@ -623,6 +631,10 @@ __global__ void __launch_bounds__(128)
             }
         }
         __syncthreads();
+        if (++x == W) {
+            x = 0;
+            ++y;
+        }
     }
     if (wp == 0 && q4 == 0) {
         if (ca < n_cfg) logq[ca] = lqa;

@@ -74,7 +74,7 @@ struct CGraphParams {
     const int32_t* nlow;     // O(3): neighbours of lower colour, listed first in adj
     float* spins;            // [R][NC][n]
     const float* betaf;      // [slots]
-    const int32_t* r2t;      // [R]
+    int32_t* r2t;            // [R]
     double* rec_e;           // [rows][R]
     double* rec_m;           // [rows][R][NC]
     int32_t* rec_t;          // [rows][R]
@@ -310,41 +310,35 @@ __device__ __forceinline__ void cg_wolff(const CGraphParams& P, const Planes& s,
     __syncthreads();
 }
 
-// n_sweeps sweeps of every replica (block = replica).  A measured sweep's
-// per-warp sums go to one of two alternating slot sets; thread 0 adds them
-// after the barrier that follows, and the set is written again two
-// measurements later, after another barrier.
+// Running state of one replica's sweeps within a launch.
+struct CGState {
+    int mb;                     // slot set of the next measurement
+    int64_t row;                // next record row
+    unsigned long long moves;   // this thread's accepted rotations / cluster sizes
+};
+
+// n sweeps of replica r from global sweep sweep0, recording after local sweep
+// k when every > 0 and k % every == phase; the energy after the last sweep
+// ends up in e_last (thread 0).  A measured sweep's per-warp sums go to one
+// of two alternating slot sets; thread 0 adds them after the barrier that
+// follows, and the set is written again two measurements later, after
+// another barrier.
 template <int NC>
-__global__ void __launch_bounds__(kCGThreads, 1) k_cgraph_sweeps(const __grid_constant__ CGraphParams P) {
-    extern __shared__ float cg_smem[];
-    __shared__ long long s_acc[2][4][32];
-    __shared__ int ctl[3];
-    const int r = blockIdx.x;
-    Planes s;
-    s.x = cg_smem;
-    s.y = cg_smem + P.n;
-    s.z = NC == 3 ? cg_smem + 2 * (size_t)P.n : cg_smem;
-    uint32_t* inb = reinterpret_cast<uint32_t*>(cg_smem + (size_t)NC * P.n);
-    int32_t* queue = reinterpret_cast<int32_t*>(inb + ((P.n + 31) >> 5));
-    float* g = P.spins + (size_t)r * NC * P.n;
-    for (int i = threadIdx.x; i < NC * P.n; i += blockDim.x) cg_smem[i] = g[i];
-    const int slot = P.r2t[r];
-    const float beta = P.betaf[slot];
-    __syncthreads();
-    unsigned long long moves = 0;
-    int64_t row = P.row0;
-    int mb = 0;
-    for (int k = 0; k < P.n_sweeps; ++k) {
-        const uint64_t sweep = P.sweep0 + (uint64_t)k;
-        const bool rec = P.measure_every > 0 && k % P.measure_every == P.measure_phase;
-        const bool meas = rec || k == P.n_sweeps - 1;
+__device__ __forceinline__ void cg_run(const CGraphParams& P, const Planes& s, uint32_t* inb,
+                                       int32_t* queue, int* ctl, long long (*s_acc)[4][32], int r,
+                                       int slot, float beta, uint64_t sweep0, int n, int every,
+                                       int phase, CGState& st, double& e_last) {
+    for (int k = 0; k < n; ++k) {
+        const uint64_t sweep = sweep0 + (uint64_t)k;
+        const bool rec = every > 0 && k % every == phase;
+        const bool meas = rec || k == n - 1;
         if (NC == 3) {
-            cg_metropolis(P, s, r, sweep, beta, meas, s_acc[mb], moves);
+            cg_metropolis(P, s, r, sweep, beta, meas, s_acc[st.mb], st.moves);
         } else {
             cg_wolff(P, s, inb, queue, ctl, r, sweep, beta);
-            if (threadIdx.x == 0) moves += (unsigned long long)ctl[0];
+            if (threadIdx.x == 0) st.moves += (unsigned long long)ctl[0];
             if (meas) {
-                cg_measure_xy(P, s, s_acc[mb]);
+                cg_measure_xy(P, s, s_acc[st.mb]);
                 __syncthreads();
             }
         }
@@ -355,31 +349,146 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgraph_sweeps(const __grid_co
                 for (int c = 0; c <= NC; ++c) a[c] = 0;
                 for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
 #pragma unroll
-                    for (int c = 0; c <= NC; ++c) a[c] += s_acc[mb][c][w];
+                    for (int c = 0; c <= NC; ++c) a[c] += s_acc[st.mb][c][w];
                 // O(3): each bond once; O(2): every bond from both ends
                 const double bonds = (double)a[0] * kFixInv * (NC == 3 ? 1.0 : 0.5);
                 const double e = -(double)P.J * bonds;
-                double m[NC];
-#pragma unroll
-                for (int c = 0; c < NC; ++c) m[c] = (double)a[1 + c] * kFixInv;
                 if (rec) {
-                    P.rec_e[row * P.R + r] = e;
+                    P.rec_e[st.row * P.R + r] = e;
 #pragma unroll
-                    for (int c = 0; c < NC; ++c) P.rec_m[(row * P.R + r) * NC + c] = m[c];
-                    P.rec_t[row * P.R + r] = slot;
+                    for (int c = 0; c < NC; ++c)
+                        P.rec_m[(st.row * P.R + r) * NC + c] = (double)a[1 + c] * kFixInv;
+                    P.rec_t[st.row * P.R + r] = slot;
                 }
-                if (k == P.n_sweeps - 1) P.last_e[r] = e;
+                e_last = e;
             }
-            mb ^= 1;
+            st.mb ^= 1;
         }
-        if (rec) ++row;
+        if (rec) ++st.row;
     }
-    // per-replica move counter: warp sums then one atomic per warp
+}
+
+// Shared-memory planes of a replica and its staging from global memory.
+template <int NC>
+__device__ __forceinline__ Planes cg_stage(const CGraphParams& P, float* cg_smem, int r) {
+    Planes s;
+    s.x = cg_smem;
+    s.y = cg_smem + P.n;
+    s.z = NC == 3 ? cg_smem + 2 * (size_t)P.n : cg_smem;
+    const float* g = P.spins + (size_t)r * NC * P.n;
+    for (int i = threadIdx.x; i < NC * P.n; i += blockDim.x) cg_smem[i] = g[i];
+    __syncthreads();
+    return s;
+}
+
+// Move counter (warp sums, one atomic per warp) and spins back to global.
+template <int NC>
+__device__ __forceinline__ void cg_finish(const CGraphParams& P, const float* cg_smem, int r,
+                                          unsigned long long moves) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) moves += __shfl_down_sync(ISG_FULL_MASK, moves, o);
     if ((threadIdx.x & 31) == 0 && moves) atomicAdd(&P.moves[r], moves);
     __syncthreads();
+    float* g = P.spins + (size_t)r * NC * P.n;
     for (int i = threadIdx.x; i < NC * P.n; i += blockDim.x) g[i] = cg_smem[i];
+}
+
+// n_sweeps sweeps of every replica (block = replica) between exchange points.
+template <int NC>
+__global__ void __launch_bounds__(kCGThreads, 1) k_cgraph_sweeps(const __grid_constant__ CGraphParams P) {
+    extern __shared__ float cg_smem[];
+    __shared__ long long s_acc[2][4][32];
+    __shared__ int ctl[3];
+    const int r = blockIdx.x;
+    const Planes s = cg_stage<NC>(P, cg_smem, r);
+    uint32_t* inb = reinterpret_cast<uint32_t*>(cg_smem + (size_t)NC * P.n);
+    int32_t* queue = reinterpret_cast<int32_t*>(inb + ((P.n + 31) >> 5));
+    const int slot = P.r2t[r];
+    CGState st{0, P.row0, 0ull};
+    double e = 0.0;
+    cg_run<NC>(P, s, inb, queue, ctl, s_acc, r, slot, P.betaf[slot], P.sweep0, P.n_sweeps,
+               P.measure_every, P.measure_phase, st, e);
+    if (threadIdx.x == 0) P.last_e[r] = e;
+    cg_finish<NC>(P, cg_smem, r, st.moves);
+}
+
+// A whole sampling run in one cooperative launch, as k_graph_pt: sweeps between
+// exchange points, then every block publishes its energy, all meet at the
+// bounded grid barrier and every block computes the same exchange pass
+// (the rule of k_graph_exchange) on its own copy of the ladder.
+template <int NC>
+__global__ void __launch_bounds__(kCGThreads, 1)
+    k_cgraph_pt(const __grid_constant__ CGraphParams P, const __grid_constant__ GraphPtParams X) {
+    extern __shared__ float cg_smem[];
+    __shared__ long long s_acc[2][4][32];
+    __shared__ int ctl[3];
+    __shared__ int s_t2r[kCGMaxReplicas];
+    __shared__ int s_slot, s_acc_x;
+    const int r = blockIdx.x, R = P.R;
+    for (int i = threadIdx.x; i < R; i += blockDim.x) s_t2r[i] = X.t2r[i];
+    const Planes s = cg_stage<NC>(P, cg_smem, r);
+    uint32_t* inb = reinterpret_cast<uint32_t*>(cg_smem + (size_t)NC * P.n);
+    int32_t* queue = reinterpret_cast<int32_t*>(inb + ((P.n + 31) >> 5));
+    int slot = P.r2t[r];
+    CGState st{0, 0, 0ull};
+    unsigned long long xc = X.ctrl[0];
+    int accepted = 0;
+    uint64_t k = X.ksample0;
+    int64_t done = 0;
+    double e = 0.0;
+    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    while (done < X.n_sweeps) {
+        const uint64_t to_x = (uint64_t)X.ee - (k % (uint64_t)X.ee);
+        const int n = (int)min(to_x, (uint64_t)(X.n_sweeps - done));
+        const int phase = (int)(((uint64_t)X.me - 1u - (k % (uint64_t)X.me)) % (uint64_t)X.me);
+        cg_run<NC>(P, s, inb, queue, ctl, s_acc, r, slot, P.betaf[slot], P.sweep0 + (uint64_t)done,
+                   n, X.me, phase, st, e);
+        k += (uint64_t)n;
+        done += n;
+        if (k % (uint64_t)X.ee != 0) continue;
+        double* eb = X.ebuf + (size_t)(xc & 1ull) * R;
+        if (threadIdx.x == 0) {
+            eb[r] = e;
+            s_acc_x = 0;
+        }
+        if (!grid_barrier(X.bar, X.err, gridDim.x)) return;
+        const int par = (int)(xc & 1ull);
+        const uint32_t c3 = counter_word3(ISG_TAG_EXCH, 0, xc);
+        for (int i = par + 2 * threadIdx.x; i + 1 < R; i += 2 * blockDim.x) {
+            const int ri = s_t2r[i], rj = s_t2r[i + 1];
+            const double d = __dmul_rn(__dsub_rn(X.betas[i], X.betas[i + 1]),
+                                       __dsub_rn(__ldcg(eb + rj), __ldcg(eb + ri)));
+            bool ok = d < 0.0;
+            if (!ok) {
+                const U4 u = philox10(0xFFFFFFFFu, (uint32_t)i, (uint32_t)xc, c3, k0, k1);
+                ok = uniform53(u.x, u.y) < exp(-d);
+            }
+            if (ok) {
+                s_t2r[i] = rj;
+                s_t2r[i + 1] = ri;
+                atomicAdd(&s_acc_x, 1);
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < R; i += blockDim.x)
+            if (s_t2r[i] == r) s_slot = i;
+        accepted += s_acc_x;
+        ++xc;
+        __syncthreads();
+        slot = s_slot;
+    }
+    if (threadIdx.x == 0) {
+        P.last_e[r] = e;
+        P.r2t[r] = slot;
+    }
+    cg_finish<NC>(P, cg_smem, r, st.moves);
+    if (r == 0) {
+        for (int i = threadIdx.x; i < R; i += blockDim.x) X.t2r[i] = s_t2r[i];
+        if (threadIdx.x == 0) {
+            X.ctrl[0] = xc;
+            X.ctrl[1] += (unsigned long long)accepted;
+        }
+    }
 }
 
 // Hot start of every replica: [R][NC][n].
@@ -434,6 +543,11 @@ struct isg_cgraph {
     int32_t* d_t2r = nullptr;
     double* d_last_e = nullptr;
     unsigned long long* d_moves = nullptr;
+    // persistent runs (k_cgraph_pt): energy buffers, barrier, error flag
+    double* d_ebuf = nullptr;
+    unsigned int* d_bar = nullptr;
+    int* d_err = nullptr;
+    bool coop = false;         // all replicas can be resident at once
     unsigned long long* d_ctrl = nullptr;  // [0] exchange count, [1] accepted
     double* d_rec_e = nullptr;
     double* d_rec_m = nullptr;
@@ -460,6 +574,9 @@ int cg_destroy(isg_cgraph* H) {
     cudaFree(H->d_t2r);
     cudaFree(H->d_last_e);
     cudaFree(H->d_moves);
+    cudaFree(H->d_ebuf);
+    cudaFree(H->d_bar);
+    cudaFree(H->d_err);
     cudaFree(H->d_ctrl);
     cudaFree(H->d_rec_e);
     cudaFree(H->d_rec_m);
@@ -469,7 +586,7 @@ int cg_destroy(isg_cgraph* H) {
     return ISG_OK;
 }
 
-int cg_launch(isg_cgraph* H, int n_sweeps, int every, int phase, int64_t row0) {
+CGraphParams cg_params(isg_cgraph* H, int n_sweeps, int every, int phase, int64_t row0) {
     CGraphParams P{};
     P.rowptr = H->d_rowptr;
     P.adj = H->d_adj;
@@ -496,6 +613,11 @@ int cg_launch(isg_cgraph* H, int n_sweeps, int every, int phase, int64_t row0) {
     P.measure_every = every;
     P.measure_phase = phase;
     P.row0 = row0;
+    return P;
+}
+
+int cg_launch(isg_cgraph* H, int n_sweeps, int every, int phase, int64_t row0) {
+    const CGraphParams P = cg_params(H, n_sweeps, every, phase, row0);
     if (H->nc == 3)
         k_cgraph_sweeps<3><<<H->R, kCGThreads, H->smem, H->stream>>>(P);
     else
@@ -612,6 +734,9 @@ int isg_cgraph_create(isg_cgraph** out, int n_nodes, const int32_t* edges, int n
     CGALLOC(H->d_t2r, sizeof(int32_t) * replicas);
     CGALLOC(H->d_last_e, sizeof(double) * replicas);
     CGALLOC(H->d_moves, sizeof(unsigned long long) * replicas);
+    CGALLOC(H->d_ebuf, sizeof(double) * 2 * replicas);
+    CGALLOC(H->d_bar, sizeof(unsigned int) * 2);
+    CGALLOC(H->d_err, sizeof(int));
     CGALLOC(H->d_ctrl, sizeof(unsigned long long) * 2);
 #undef CGALLOC
     e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);
@@ -620,16 +745,32 @@ int isg_cgraph_create(isg_cgraph** out, int n_nodes, const int32_t* edges, int n
         return cuda_fail(e, "cudaStreamCreateWithFlags");
     }
     if (H->smem > 48 * 1024) {
-        e = n_comp == 3 ? cudaFuncSetAttribute(k_cgraph_sweeps<3>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+        const int a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+        e = n_comp == 3 ? cudaFuncSetAttribute(k_cgraph_sweeps<3>, (cudaFuncAttribute)a,
                                                (int)H->smem)
-                        : cudaFuncSetAttribute(k_cgraph_sweeps<2>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                        : cudaFuncSetAttribute(k_cgraph_sweeps<2>, (cudaFuncAttribute)a,
                                                (int)H->smem);
+        if (e == cudaSuccess)
+            e = n_comp == 3 ? cudaFuncSetAttribute(k_cgraph_pt<3>, (cudaFuncAttribute)a, (int)H->smem)
+                            : cudaFuncSetAttribute(k_cgraph_pt<2>, (cudaFuncAttribute)a, (int)H->smem);
         if (e != cudaSuccess) {
             cg_destroy(H);
             return cuda_fail(e, "cudaFuncSetAttribute");
         }
+    }
+    {
+        // a persistent run needs every replica resident at once
+        int coop_attr = 0, sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&coop_attr, cudaDevAttrCooperativeLaunch, H->device);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->device);
+        const cudaError_t oe =
+            n_comp == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgraph_pt<3>,
+                                                                        kCGThreads, H->smem)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgraph_pt<2>,
+                                                                        kCGThreads, H->smem);
+        if (oe != cudaSuccess) per_sm = 0;
+        cudaGetLastError();
+        H->coop = coop_attr && (int64_t)per_sm * sms >= replicas;
     }
     std::vector<int32_t> ident(replicas);
     for (int r = 0; r < replicas; ++r) ident[r] = r;
@@ -656,6 +797,8 @@ int isg_cgraph_create(isg_cgraph** out, int n_nodes, const int32_t* edges, int n
                          cudaMemcpyHostToDevice, H->stream));
     CGCK(cudaMemsetAsync(H->d_ctrl, 0, sizeof(unsigned long long) * 2, H->stream));
     CGCK(cudaMemsetAsync(H->d_moves, 0, sizeof(unsigned long long) * replicas, H->stream));
+    CGCK(cudaMemsetAsync(H->d_bar, 0, sizeof(unsigned int) * 2, H->stream));
+    CGCK(cudaMemsetAsync(H->d_err, 0, sizeof(int), H->stream));
     k_cgraph_init<<<std::max(1, std::min(1024, (n_nodes * replicas + 255) / 256)), 256, 0,
                     H->stream>>>(H->d_spins, n_nodes, replicas, n_comp, seed);
     CGCK(cudaGetLastError());
@@ -763,6 +906,35 @@ int isg_cgraph_pt_run(isg_cgraph* h, int64_t n_sweeps, int exchange_every, int m
         h->rec_cap = need;
     }
     int64_t done = 0, row = 0;
+    if (h->coop && exchange_every <= 100000 && n_sweeps > 0) {
+        // the whole run in one cooperative launch (k_cgraph_pt)
+        CGraphParams P = cg_params(h, 0, measure_every, 0, 0);
+        GraphPtParams X{};
+        X.betas = h->d_betas;
+        X.t2r = h->d_t2r;
+        X.ctrl = h->d_ctrl;
+        X.ebuf = h->d_ebuf;
+        X.bar = h->d_bar;
+        X.err = h->d_err;
+        X.n_sweeps = n_sweeps;
+        X.ksample0 = h->ksample;
+        X.ee = exchange_every;
+        X.me = measure_every;
+        void* args[] = {&P, &X};
+        const void* fn = h->nc == 3 ? (const void*)k_cgraph_pt<3> : (const void*)k_cgraph_pt<2>;
+        ISG_CK(cudaLaunchCooperativeKernel(fn, dim3(h->R), dim3(kCGThreads), args, h->smem,
+                                           h->stream));
+        int err = 0;
+        ISG_CK(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        ISG_CK(cudaStreamSynchronize(h->stream));
+        if (err)
+            return fail(ISG_ERR_TIMEOUT, "isg_cgraph_pt_run: a replica did not reach the exchange "
+                                         "barrier in time");
+        h->gsweep += (uint64_t)n_sweeps;
+        h->ksample += (uint64_t)n_sweeps;
+        done = n_sweeps;
+        row = need;
+    }
     while (done < n_sweeps) {
         const uint64_t k = h->ksample;
         const uint64_t to_x = (uint64_t)exchange_every - (k % (uint64_t)exchange_every);

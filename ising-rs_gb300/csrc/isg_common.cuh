@@ -88,6 +88,58 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
     return (__umulhi(n, f.m) + n) >> f.s;
 }
 
+// ------------------------------------------------- persistent graph runs
+// Shared by the graph engines' cooperative launches (isg_graph.cu,
+// isg_cgraph.cu): a bounded grid barrier and the exchange parameters.
+constexpr long long kBarrierCycles = 1ll << 34;  // ~8 s at 2 GHz
+
+struct GraphPtParams {
+    const double* betas;     // per slot
+    int32_t* t2r;
+    unsigned long long* ctrl;  // [0] exchange count, [1] accepted
+    double* ebuf;            // [2][R]
+    unsigned int* bar;       // [0] arrivals, [1] generation
+    int* err;
+    int64_t n_sweeps;
+    uint64_t ksample0;       // sampling sweeps before this run
+    int ee, me;
+};
+
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err, unsigned int nblocks) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* vgen = bar + 1;
+        const unsigned int gen = *vgen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(bar, 1u) + 1u == nblocks) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*vgen == gen) {
+                if (*(volatile int*)err != 0) {
+                    ok = 0;
+                    break;
+                }
+                if (clock64() - t0 > kBarrierCycles) {
+                    atomicExch(err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+        s_ok = ok && *(volatile int*)err == 0;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+
 // ---------------------------------------------------------------- errors
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);

@@ -49,7 +49,7 @@ struct GraphParams {
     const int32_t* cstart;   // class starts in `order`, [n_classes+1]
     uint8_t* spins;          // [R][n] down bits
     const uint32_t* thr;     // [slots][kGTab]
-    const int32_t* r2t;      // [R]
+    int32_t* r2t;            // [R]
     long long* rec_b;        // [rows][R] bond sums (one record per measured sweep)
     long long* rec_m;
     int32_t* rec_t;
@@ -108,42 +108,33 @@ __device__ __forceinline__ void g_warp_store(long long v, long long* slots) {
     if ((threadIdx.x & 31) == 0) slots[threadIdx.x >> 5] = v;
 }
 
-// n_sweeps sweeps of every replica (block = replica), spins staged in shared
-// memory; records after the measured sweeps and the final energy.  The bond
-// sum and magnetisation of the previous launch (or one measurement on the
-// first launch) are advanced by the exact integer change of every flip,
-// -2 s (deg - 2 n_down) and -2 s: the nodes of a class share no edge, so the
-// changes of one class add up.  A record costs one warp reduction per warp
-// before the last class's barrier (each warp stores its sum in its slot of
-// one of two alternating slot sets) and thread 0 adds the slots after it;
-// a slot set is written again two measurements later, after another barrier.
-__global__ void __launch_bounds__(kGThreads) k_graph_sweeps(const __grid_constant__ GraphParams P) {
-    extern __shared__ uint8_t g_sp[];
-    __shared__ uint32_t s_tab[kGTab];
-    __shared__ int red[64];
-    __shared__ long long s_acc[2][2][32];
-    const int r = blockIdx.x;
-    uint8_t* spins = P.spins + (size_t)r * P.n;
-    for (int v = threadIdx.x; v < P.n; v += blockDim.x) g_sp[v] = spins[v];
-    const int slot = P.r2t[r];
-    for (int e = threadIdx.x; e < kGTab; e += blockDim.x) s_tab[e] = P.thr[(size_t)slot * kGTab + e];
-    __syncthreads();
+// Running bond sum / magnetisation of one replica during a launch: the values
+// at the launch start (thread 0) and every thread's exact integer change since
+// (-2 s (deg - 2 n_down) and -2 s per flip: the nodes of a class share no edge,
+// so the changes of one class add up).
+struct GState {
+    long long bond0, mag0, db, dm;
+    int mb;       // slot set of the next measurement
+    int64_t row;  // next record row
+};
+
+// n sweeps of replica r (spins in shared memory) from global sweep sweep0,
+// recording after local sweep k when every > 0 and k % every == phase.  The
+// bond sum and magnetisation after the last sweep end up in bb, mm (thread 0).
+// A measurement costs one warp reduction per warp before the last class's
+// barrier (each warp stores its sum in its slot of one of two alternating
+// slot sets) and thread 0 adds the slots after it; a slot set is written again
+// two measurements later, after another barrier.
+__device__ __forceinline__ void graph_run(const GraphParams& P, int r, int slot, uint8_t* g_sp,
+                                          const uint32_t* s_tab, long long (*s_acc)[2][32],
+                                          uint64_t sweep0, int n, int every, int phase, GState& st,
+                                          long long& bb, long long& mm) {
     const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
-    long long bond0 = 0, mag0 = 0;  // valid in thread 0
-    if (P.bm_known) {
-        bond0 = P.last_bm[2 * r];
-        mag0 = P.last_bm[2 * r + 1];
-    } else {
-        g_measure(P, g_sp, red, bond0, mag0);
-    }
-    long long db = 0, dm = 0;  // this thread's flips since the launch start
-    int mb = 0;
-    int64_t row = P.row0;
     const int last_class = P.n_classes - 1;
-    for (int k = 0; k < P.n_sweeps; ++k) {
-        const uint64_t sweep = P.sweep0 + (uint64_t)k;
-        const bool rec = P.measure_every > 0 && k % P.measure_every == P.measure_phase;
-        const bool meas = rec || k == P.n_sweeps - 1;
+    for (int k = 0; k < n; ++k) {
+        const uint64_t sweep = sweep0 + (uint64_t)k;
+        const bool rec = every > 0 && k % every == phase;
+        const bool meas = rec || k == n - 1;
         for (int c = 0; c < P.n_classes; ++c) {
             const uint32_t c3 = counter_word3(ISG_TAG_GRAPH, (uint32_t)c, sweep);
             const int a = __ldg(P.cstart + c), b = __ldg(P.cstart + c + 1);
@@ -160,39 +151,167 @@ __global__ void __launch_bounds__(kGThreads) k_graph_sweeps(const __grid_constan
                 if (uw <= th) {
                     g_sp[v] = (uint8_t)(d ^ 1);
                     const int s_old = 1 - 2 * d;
-                    db -= 2 * s_old * ((r1 - r0) - 2 * nd);
-                    dm -= 2 * s_old;
+                    st.db -= 2 * s_old * ((r1 - r0) - 2 * nd);
+                    st.dm -= 2 * s_old;
                 }
             }
             if (meas && c == last_class) {
-                g_warp_store(db, s_acc[mb][0]);
-                g_warp_store(dm, s_acc[mb][1]);
+                g_warp_store(st.db, s_acc[st.mb][0]);
+                g_warp_store(st.dm, s_acc[st.mb][1]);
             }
             __syncthreads();
         }
         if (meas) {
             if (threadIdx.x == 0) {
-                long long bb = bond0, mm = mag0;
+                long long b2 = st.bond0, m2 = st.mag0;
                 for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-                    bb += s_acc[mb][0][w];
-                    mm += s_acc[mb][1][w];
+                    b2 += s_acc[st.mb][0][w];
+                    m2 += s_acc[st.mb][1][w];
                 }
                 if (rec) {
-                    P.rec_b[row * P.R + r] = bb;
-                    P.rec_m[row * P.R + r] = mm;
-                    P.rec_t[row * P.R + r] = slot;
+                    P.rec_b[st.row * P.R + r] = b2;
+                    P.rec_m[st.row * P.R + r] = m2;
+                    P.rec_t[st.row * P.R + r] = slot;
                 }
-                if (k == P.n_sweeps - 1) {
-                    P.last_e[r] = -__dmul_rn(P.J, (double)bb);
-                    P.last_bm[2 * r] = bb;
-                    P.last_bm[2 * r + 1] = mm;
-                }
+                bb = b2;
+                mm = m2;
             }
-            mb ^= 1;
+            st.mb ^= 1;
         }
-        if (rec) ++row;
+        if (rec) ++st.row;
     }
+}
+
+// Stage replica r's spins and threshold table; the starting bond sum and
+// magnetisation come from the previous launch or one measurement.
+__device__ __forceinline__ void graph_stage(const GraphParams& P, int r, int slot, uint8_t* g_sp,
+                                            uint32_t* s_tab, int* red, GState& st) {
+    const uint8_t* spins = P.spins + (size_t)r * P.n;
+    for (int v = threadIdx.x; v < P.n; v += blockDim.x) g_sp[v] = spins[v];
+    for (int e = threadIdx.x; e < kGTab; e += blockDim.x) s_tab[e] = P.thr[(size_t)slot * kGTab + e];
+    __syncthreads();
+    st.bond0 = st.mag0 = st.db = st.dm = 0;
+    st.mb = 0;
+    st.row = P.row0;
+    if (P.bm_known) {
+        st.bond0 = P.last_bm[2 * r];
+        st.mag0 = P.last_bm[2 * r + 1];
+    } else {
+        g_measure(P, g_sp, red, st.bond0, st.mag0);
+    }
+}
+
+// Energy, carried state and spins of replica r at the end of a launch.
+__device__ __forceinline__ void graph_finish(const GraphParams& P, int r, const uint8_t* g_sp,
+                                             long long bb, long long mm) {
+    if (threadIdx.x == 0) {
+        P.last_e[r] = -__dmul_rn(P.J, (double)bb);
+        P.last_bm[2 * r] = bb;
+        P.last_bm[2 * r + 1] = mm;
+    }
+    uint8_t* spins = P.spins + (size_t)r * P.n;
     for (int v = threadIdx.x; v < P.n; v += blockDim.x) spins[v] = g_sp[v];
+}
+
+// n_sweeps sweeps of every replica (block = replica) between exchange points.
+__global__ void __launch_bounds__(kGThreads) k_graph_sweeps(const __grid_constant__ GraphParams P) {
+    extern __shared__ uint8_t g_sp[];
+    __shared__ uint32_t s_tab[kGTab];
+    __shared__ int red[64];
+    __shared__ long long s_acc[2][2][32];
+    const int r = blockIdx.x;
+    const int slot = P.r2t[r];
+    GState st;
+    graph_stage(P, r, slot, g_sp, s_tab, red, st);
+    long long bb = 0, mm = 0;
+    graph_run(P, r, slot, g_sp, s_tab, s_acc, P.sweep0, P.n_sweeps, P.measure_every,
+              P.measure_phase, st, bb, mm);
+    graph_finish(P, r, g_sp, bb, mm);
+}
+
+// ------------------------------------------------------ persistent PT run
+// A whole sampling run in one cooperative launch: between exchange points the
+// replicas sweep as above; at an exchange point every block publishes its
+// energy, all meet at a grid barrier, and every block computes the same
+// exchange pass (the rule of k_graph_exchange) on its own copy of the ladder,
+// so the launch needs no second barrier.  Energies alternate between two
+// buffers: a block can only rewrite one after every block has passed the
+// barrier that follows its reads.  Waits are bounded (kBarrierCycles); a
+// timeout sets *err, and every block returns at its next barrier.
+__global__ void __launch_bounds__(kGThreads)
+    k_graph_pt(const __grid_constant__ GraphParams P, const __grid_constant__ GraphPtParams X) {
+    extern __shared__ uint8_t g_sp[];
+    __shared__ uint32_t s_tab[kGTab];
+    __shared__ int red[64];
+    __shared__ long long s_acc[2][2][32];
+    __shared__ int s_t2r[kGMaxReplicas];
+    __shared__ int s_slot, s_acc_x;
+    const int r = blockIdx.x, R = P.R;
+    for (int i = threadIdx.x; i < R; i += blockDim.x) s_t2r[i] = X.t2r[i];
+    int slot = P.r2t[r];
+    GState st;
+    graph_stage(P, r, slot, g_sp, s_tab, red, st);
+    unsigned long long xc = X.ctrl[0];
+    int accepted = 0;
+    uint64_t k = X.ksample0;
+    int64_t done = 0;
+    long long bb = 0, mm = 0;
+    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    while (done < X.n_sweeps) {
+        const uint64_t to_x = (uint64_t)X.ee - (k % (uint64_t)X.ee);
+        const int n = (int)min(to_x, (uint64_t)(X.n_sweeps - done));
+        const int phase = (int)(((uint64_t)X.me - 1u - (k % (uint64_t)X.me)) % (uint64_t)X.me);
+        graph_run(P, r, slot, g_sp, s_tab, s_acc, P.sweep0 + (uint64_t)done, n, X.me, phase, st,
+                  bb, mm);
+        k += (uint64_t)n;
+        done += n;
+        if (k % (uint64_t)X.ee != 0) continue;
+        // exchange point
+        double* eb = X.ebuf + (size_t)(xc & 1ull) * R;
+        if (threadIdx.x == 0) {
+            eb[r] = -__dmul_rn(P.J, (double)bb);
+            s_acc_x = 0;
+        }
+        if (!grid_barrier(X.bar, X.err, gridDim.x)) return;
+        const int par = (int)(xc & 1ull);
+        const uint32_t c3 = counter_word3(ISG_TAG_EXCH, 0, xc);
+        for (int i = par + 2 * threadIdx.x; i + 1 < R; i += 2 * blockDim.x) {
+            const int ri = s_t2r[i], rj = s_t2r[i + 1];
+            const double d = __dmul_rn(__dsub_rn(X.betas[i], X.betas[i + 1]),
+                                       __dsub_rn(__ldcg(eb + rj), __ldcg(eb + ri)));
+            bool ok = d < 0.0;
+            if (!ok) {
+                const U4 u = philox10(0xFFFFFFFFu, (uint32_t)i, (uint32_t)xc, c3, k0, k1);
+                ok = uniform53(u.x, u.y) < exp(-d);
+            }
+            if (ok) {
+                s_t2r[i] = rj;
+                s_t2r[i + 1] = ri;
+                atomicAdd(&s_acc_x, 1);
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < R; i += blockDim.x)
+            if (s_t2r[i] == r) s_slot = i;
+        accepted += s_acc_x;
+        ++xc;
+        __syncthreads();
+        if (s_slot != slot) {
+            slot = s_slot;
+            for (int e = threadIdx.x; e < kGTab; e += blockDim.x)
+                s_tab[e] = P.thr[(size_t)slot * kGTab + e];
+            __syncthreads();
+        }
+    }
+    graph_finish(P, r, g_sp, bb, mm);
+    if (threadIdx.x == 0) P.r2t[r] = slot;
+    if (r == 0) {
+        for (int i = threadIdx.x; i < R; i += blockDim.x) X.t2r[i] = s_t2r[i];
+        if (threadIdx.x == 0) {
+            X.ctrl[0] = xc;
+            X.ctrl[1] += (unsigned long long)accepted;
+        }
+    }
 }
 
 // Hot start of every replica.
@@ -285,6 +404,11 @@ struct isg_graph {
     double* d_last_e = nullptr;
     long long* d_last_bm = nullptr;
     bool bm_known = false;
+    // persistent runs (k_graph_pt): energy buffers, barrier, error flag
+    double* d_ebuf = nullptr;
+    unsigned int* d_bar = nullptr;
+    int* d_err = nullptr;
+    bool coop = false;         // all replicas can be resident at once
     unsigned long long* d_ctrl = nullptr;  // [0] exchange count, [1] accepted
     long long* d_rec_b = nullptr;
     long long* d_rec_m = nullptr;
@@ -310,6 +434,9 @@ int g_destroy(isg_graph* H) {
     cudaFree(H->d_betas);
     cudaFree(H->d_last_e);
     cudaFree(H->d_last_bm);
+    cudaFree(H->d_ebuf);
+    cudaFree(H->d_bar);
+    cudaFree(H->d_err);
     cudaFree(H->d_ctrl);
     cudaFree(H->d_rec_b);
     cudaFree(H->d_rec_m);
@@ -441,6 +568,9 @@ int isg_graph_create(isg_graph** out, int n_nodes, const int32_t* edges, int n_e
     GALLOC(H->d_betas, sizeof(double) * replicas);
     GALLOC(H->d_last_e, sizeof(double) * replicas);
     GALLOC(H->d_last_bm, sizeof(long long) * 2 * replicas);
+    GALLOC(H->d_ebuf, sizeof(double) * 2 * replicas);
+    GALLOC(H->d_bar, sizeof(unsigned int) * 2);
+    GALLOC(H->d_err, sizeof(int));
     GALLOC(H->d_ctrl, sizeof(unsigned long long) * 2);
 #undef GALLOC
     e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking);
@@ -451,10 +581,24 @@ int isg_graph_create(isg_graph** out, int n_nodes, const int32_t* edges, int n_e
     if (n_nodes > 32768) {
         e = cudaFuncSetAttribute(k_graph_sweeps, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  n_nodes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_graph_pt, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     n_nodes);
         if (e != cudaSuccess) {
             g_destroy(H);
             return cuda_fail(e, "cudaFuncSetAttribute");
         }
+    }
+    {
+        // a persistent run needs every replica resident at once
+        int coop_attr = 0, sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&coop_attr, cudaDevAttrCooperativeLaunch, H->device);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->device);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_graph_pt, kGThreads,
+                                                          (size_t)n_nodes) != cudaSuccess)
+            per_sm = 0;
+        cudaGetLastError();
+        H->coop = coop_attr && (int64_t)per_sm * sms >= replicas;
     }
     std::vector<int32_t> ident(replicas);
     for (int r = 0; r < replicas; ++r) ident[r] = r;
@@ -478,6 +622,8 @@ int isg_graph_create(isg_graph** out, int n_nodes, const int32_t* edges, int n_e
     GCK(cudaMemcpyAsync(H->d_t2r, ident.data(), sizeof(int32_t) * replicas,
                         cudaMemcpyHostToDevice, H->stream));
     GCK(cudaMemsetAsync(H->d_ctrl, 0, sizeof(unsigned long long) * 2, H->stream));
+    GCK(cudaMemsetAsync(H->d_bar, 0, sizeof(unsigned int) * 2, H->stream));
+    GCK(cudaMemsetAsync(H->d_err, 0, sizeof(int), H->stream));
     k_graph_init<<<std::max(1, std::min(1024, (n_nodes * replicas + 255) / 256)), 256, 0,
                    H->stream>>>(H->d_spins, n_nodes, replicas, seed);
     GCK(cudaGetLastError());
@@ -589,8 +735,42 @@ int isg_graph_pt_run(isg_graph* h, int64_t n_sweeps, int exchange_every, int mea
         ISG_CK(cudaMalloc((void**)&h->d_rec_t, sizeof(int32_t) * need * h->R));
         h->rec_cap = need;
     }
-    // runs of sweeps between exchange points; each ends with the exchange pass
     int64_t done = 0, row = 0;
+    if (h->coop && exchange_every <= 100000 && n_sweeps > 0) {
+        // the whole run in one cooperative launch (k_graph_pt)
+        GraphParams P = g_params(h);
+        P.sweep0 = h->gsweep;
+        P.n_sweeps = 0;
+        P.measure_every = measure_every;
+        P.measure_phase = 0;
+        P.row0 = 0;
+        GraphPtParams X{};
+        X.betas = h->d_betas;
+        X.t2r = h->d_t2r;
+        X.ctrl = h->d_ctrl;
+        X.ebuf = h->d_ebuf;
+        X.bar = h->d_bar;
+        X.err = h->d_err;
+        X.n_sweeps = n_sweeps;
+        X.ksample0 = h->ksample;
+        X.ee = exchange_every;
+        X.me = measure_every;
+        void* args[] = {&P, &X};
+        ISG_CK(cudaLaunchCooperativeKernel((const void*)k_graph_pt, dim3(h->R), dim3(kGThreads),
+                                           args, (size_t)h->n, h->stream));
+        int err = 0;
+        ISG_CK(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        ISG_CK(cudaStreamSynchronize(h->stream));
+        if (err)
+            return fail(ISG_ERR_TIMEOUT, "isg_graph_pt_run: a replica did not reach the exchange "
+                                         "barrier in time");
+        h->gsweep += (uint64_t)n_sweeps;
+        h->ksample += (uint64_t)n_sweeps;
+        h->bm_known = true;
+        done = n_sweeps;
+        row = need;
+    }
+    // runs of sweeps between exchange points; each ends with the exchange pass
     while (done < n_sweeps) {
         const uint64_t k = h->ksample;
         const uint64_t to_x = (uint64_t)exchange_every - (k % (uint64_t)exchange_every);

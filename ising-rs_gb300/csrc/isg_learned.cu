@@ -536,13 +536,16 @@ __global__ void __launch_bounds__(128)
     // warp 0, lanes 4g: configurations g and g+8 (logit rows of the last layer)
     const int ca = cfg0 + g, cb = cfg0 + g + 8;
     float lqa = 0.f, lqb = 0.f;
-    int y = 0, x = 0;
+    int y = 0, x = 0, slot = 0;
     for (int p = 0; p < HW; ++p) {
-        const int slot = p % ring;
         const bool up = y > 0, left = x > 0, right = x + 1 < W;
-        // mask-B taps (-1,-1) (-1,0) (-1,+1) (0,-1); the centre (0,0) is `slot`
-        const int ts0 = (p - W - 1 + 2 * ring) % ring, ts1 = (p - W + 2 * ring) % ring;
-        const int ts2 = (p - W + 1 + 2 * ring) % ring, ts3 = (p - 1 + ring) % ring;
+        // mask-B taps (-1,-1) (-1,0) (-1,+1) (0,-1) sit at p - W - 1 .. p - 1,
+        // i.e. ring slots slot + 1, + 2, + 3 and slot - 1 (mod W + 2); the
+        // centre (0,0) is `slot`
+        const int ts0 = slot + 1 < ring ? slot + 1 : slot + 1 - ring;
+        const int ts1 = slot + 2 < ring ? slot + 2 : slot + 2 - ring;
+        const int ts2 = slot + 3 < ring ? slot + 3 : slot + 3 - ring;
+        const int ts3 = slot > 0 ? slot - 1 : ring - 1;
         const bool ok0 = up && left, ok1 = up, ok2 = up && right, ok3 = left;
         const uint32_t o0 = rings_s + (uint32_t)ts0 * kSlot, o1 = rings_s + (uint32_t)ts1 * kSlot;
         const uint32_t o2 = rings_s + (uint32_t)ts2 * kSlot, o3 = rings_s + (uint32_t)ts3 * kSlot;
@@ -635,6 +638,7 @@ __global__ void __launch_bounds__(128)
             x = 0;
             ++y;
         }
+        if (++slot == ring) slot = 0;
     }
     if (wp == 0 && q4 == 0) {
         if (ca < n_cfg) logq[ca] = lqa;

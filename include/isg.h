@@ -442,6 +442,14 @@ int isg_graph_pt_run(isg_graph* h, int64_t n_sweeps, int exchange_every, int mea
 int isg_graph_get_accepted(isg_graph* h, int64_t* accepted);
 int isg_graph_get_spins(isg_graph* h, int replica, int8_t* out);
 int isg_graph_get_r2t(isg_graph* h, int32_t* r2t);
+/* When all replicas fit on the GPU at once (and exchange_every <= 100000),
+ * isg_graph_pt_run and isg_cgraph_pt_run run as one cooperative launch whose
+ * replicas meet at a grid barrier at every exchange point.  Every wait there is
+ * bounded (about 8 s of clock cycles); when one runs out the call returns
+ * ISG_ERR_TIMEOUT.  isg_barrier_selftest launches `blocks` blocks that wait at
+ * that barrier for `expected` arrivals with a limit of `limit_cycles`:
+ * *timed_out = 1 when the waits ran out (expected > blocks), else 0. */
+int isg_barrier_selftest(int blocks, int expected, int64_t limit_cycles, int* timed_out);
 
 /* ------------------------------------------------------------------------ */
 /* Continuous spins on graphs (`gpu_jfit --model heisenberg|xy`)             */

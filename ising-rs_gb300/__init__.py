@@ -120,6 +120,7 @@ def _declare(L):
         "isg_graph_get_accepted": [vp, vp],
         "isg_graph_get_spins": [vp, i32, vp],
         "isg_graph_get_r2t": [vp, vp],
+        "isg_barrier_selftest": [i32, i32, i64, vp],
         "isg_cgraph_create": [C.POINTER(vp), i32, vp, i32, i32, i32, u64],
         "isg_cgraph_destroy": [vp],
         "isg_cgraph_num_colours": [vp, vp],

@@ -105,7 +105,8 @@ struct GraphPtParams {
     int ee, me;
 };
 
-__device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err, unsigned int nblocks) {
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err, unsigned int nblocks,
+                                             long long limit = kBarrierCycles) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -124,7 +125,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err, unsign
                     ok = 0;
                     break;
                 }
-                if (clock64() - t0 > kBarrierCycles) {
+                if (clock64() - t0 > limit) {
                     atomicExch(err, 1);
                     ok = 0;
                     break;

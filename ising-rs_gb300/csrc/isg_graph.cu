@@ -373,6 +373,15 @@ __global__ void k_graph_exchange(const double* energies, int32_t* r2t, int32_t* 
     }
 }
 
+// Barrier check: `blocks` co-resident blocks meet at a barrier that expects
+// `expected` arrivals, twice.  With expected > blocks nobody releases them, so
+// every wait must run out after `limit` cycles and set *err.
+__global__ void k_barrier_probe(unsigned int* bar, int* err, unsigned int expected,
+                                long long limit) {
+    if (!grid_barrier(bar, err, expected, limit)) return;
+    grid_barrier(bar, err, expected, limit);
+}
+
 cudaError_t launch_graph_exchange(const double* energies, int32_t* r2t, int32_t* t2r,
                                   const double* betas, int R, unsigned long long* ctrl,
                                   uint64_t seed, cudaStream_t stream) {
@@ -821,6 +830,36 @@ int isg_graph_get_spins(isg_graph* h, int replica, int8_t* out) {
                            cudaMemcpyDeviceToHost, h->stream));
     ISG_CK(cudaStreamSynchronize(h->stream));
     for (int v = 0; v < h->n; ++v) out[v] = d[v] ? (int8_t)-1 : (int8_t)1;
+    return ISG_OK;
+}
+
+int isg_barrier_selftest(int blocks, int expected, int64_t limit_cycles, int* timed_out) {
+    if (blocks < 1 || expected < 1 || limit_cycles < 1 || !timed_out)
+        return fail(ISG_ERR_ARG, "isg_barrier_selftest: bad argument");
+    int dev = 0, sms = 0, coop = 0;
+    ISG_CK(cudaGetDevice(&dev));
+    ISG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    ISG_CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) return fail(ISG_ERR_UNSUPPORTED, "isg_barrier_selftest: no cooperative launch");
+    if (blocks > sms) return fail(ISG_ERR_ARG, "isg_barrier_selftest: blocks must fit one per SM");
+    unsigned int* bar = nullptr;
+    int* err = nullptr;
+    ISG_CK(cudaMalloc((void**)&bar, sizeof(unsigned int) * 2));
+    cudaError_t e = cudaMalloc((void**)&err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(bar, 0, sizeof(unsigned int) * 2);
+    if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(int));
+    unsigned int ex = (unsigned int)expected;
+    long long lim = (long long)limit_cycles;
+    void* args[] = {&bar, &err, &ex, &lim};
+    if (e == cudaSuccess)
+        e = cudaLaunchCooperativeKernel((const void*)k_barrier_probe, dim3(blocks), dim3(64), args,
+                                        0, nullptr);
+    int host_err = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&host_err, err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(bar);
+    cudaFree(err);
+    if (e != cudaSuccess) return cuda_fail(e, "isg_barrier_selftest");
+    *timed_out = host_err;
     return ISG_OK;
 }
 

@@ -322,3 +322,21 @@ def test_jfit_cli_csv_matches_mirror(gpu, tmp_path):
     assert f"PT exchanges accepted: {b.accepted()}" in r.stderr
     assert "jfit: model=ising, graph=bcc_N4, N=128, T=6..6.7, replicas=6, " \
            "exchange_every=7" in r.stderr
+
+
+@pytest.mark.gpu
+def test_exchange_barrier_waits_are_bounded(gpu):
+    """The grid barrier of the persistent graph runs: released when every block
+    arrives, and when a block never arrives (one more expected than launched)
+    every wait runs out after its cycle limit and reports it, with the GPU left
+    usable (a plain run follows)."""
+    import ctypes as C
+    L = gpu.lib()
+    flag = C.c_int(-1)
+    assert L.isg_barrier_selftest(4, 4, 1 << 30, C.byref(flag)) == 0 and flag.value == 0
+    assert L.isg_barrier_selftest(4, 5, 1 << 21, C.byref(flag)) == 0 and flag.value == 1
+    g = gpu.GraphDef.bcc(2)
+    b = gpu.GraphBatch(g.n_nodes, g.edges, 3, seed=1)
+    b.set_temperatures([5.0, 6.0, 7.0])
+    rt, _, _ = b.pt_run(20, 5, 1)
+    assert rt.shape == (20, 3)

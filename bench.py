@@ -146,6 +146,19 @@ def cpu_sample(threads: int, sweeps: float = 1.0):
     return flips / sec * 1e-9, sec, flips
 
 
+def cpu_replay(threads: int) -> dict:
+    """The checkerboard/Philox update of this path restated in C (the oracle's
+    replay: same random stream, thresholds and colour order) on the host threads,
+    one L=64 replica per thread, 20 sweeps each: what the GPU algorithm itself
+    costs on the CPU, beside the reference's random-site path."""
+    oracle = _load("isg_oracle", ROOT / "oracle" / "oracle.py")
+    oracle.replay_bench(64, 3, 4.5, 1, threads)
+    sec, flips = oracle.replay_bench(64, 3, 4.5, 20, threads)
+    return {"value": flips / sec * 1e-9, "unit": "flips/ns", "cores": threads,
+            "sample": f"{threads} threads x 20 checkerboard sweeps of L=64 ({flips:.3g} flips, "
+                      f"{sec:.2f} s)"}
+
+
 def host_threads() -> int:
     try:
         return len(os.sched_getaffinity(0))
@@ -363,6 +376,7 @@ def run_gpu(args):
                          "sample": f"{threads} threads x {args.cpu_sweeps:g} random-site sweeps "
                                    f"of L=8..128 each ({cpu_f:.3g} flips, {cpu_s:.1f} s); "
                                    f"reference CPU path restated in C"},
+        "cpu_replay": cpu_replay(threads),
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks.summary(),
         "wall_s": wall,

@@ -446,7 +446,8 @@ int isg_graph_get_r2t(isg_graph* h, int32_t* r2t);
  * isg_graph_pt_run and isg_cgraph_pt_run run as one cooperative launch whose
  * replicas meet at a grid barrier at every exchange point.  Every wait there is
  * bounded (about 8 s of clock cycles); when one runs out the call returns
- * ISG_ERR_TIMEOUT.  isg_barrier_selftest launches `blocks` blocks that wait at
+ * ISG_ERR_TIMEOUT and the handle's state is undefined (destroy it).
+ * isg_barrier_selftest launches `blocks` blocks that wait at
  * that barrier for `expected` arrivals with a limit of `limit_cycles`:
  * *timed_out = 1 when the waits ran out (expected > blocks), else 0. */
 int isg_barrier_selftest(int blocks, int expected, int64_t limit_cycles, int* timed_out);

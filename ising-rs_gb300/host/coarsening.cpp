@@ -9,7 +9,7 @@
 // protocol itself is isg_coarsening.
 //
 // Differences by design:
-//   * this build provides the GPU path only: without --gpu (the CPU
+//   * this drop-in provides the GPU path only: without --gpu (the CPU
 //     run_coarsening) it exits with an error;
 //   * odd sizes are rejected (the reference kernel's thread->site mapping is
 //     wrong for odd n, kernels.cu:22-29); --geometry is parsed and validated
@@ -39,7 +39,7 @@ const char* kUsage =
     "    --steps <N>          Sweeps after the quench [default: 50000]\n"
     "    --sample-every <N>   Domain-wall density every N sweeps [default: 100]\n"
     "    --seed <N>           Seed of the Philox streams [default: 42]\n"
-    "    --gpu                Run on the GPU (required by this build)\n"
+    "    --gpu                Run on the GPU (required: only the GPU path is provided)\n"
     "    --outdir <DIR>       Output directory [default: analysis/data]\n"
     "    --help, -h           Show this help message";
 
@@ -88,7 +88,7 @@ int main(int argc, char** argv) {
     if (t_quench <= 0.0 || t_high <= 0.0) die("Error: temperatures must be positive");
     if (steps == 0) die("Error: --steps must be at least 1");
     if (sample_every == 0) die("Error: --sample-every must be at least 1");
-    if (!use_gpu) die("Error: this build provides only the GPU path; pass --gpu");
+    if (!use_gpu) die("Error: this drop-in provides only the GPU path; pass --gpu");
     if (n > 1024 || (n & 1))
         die("Error: size " + std::to_string(n) +
             " unsupported: the checkerboard update needs an even size in 2..1024");

@@ -9,7 +9,7 @@
 // ascending.  The annealing schedule itself is isg_fss_anneal.
 //
 // Differences by design:
-//   * this build provides the GPU path only: without --gpu (the CPU
+//   * this drop-in provides the GPU path only: without --gpu (the CPU
 //     Metropolis/Wolff run_fss), or with --raw (CPU Wolff time series), it
 //     exits with an error instead of running on the host;
 //   * all sizes anneal together in one batch; size L uses the Philox stream
@@ -44,8 +44,8 @@ const char* kUsage =
     "    --samples <N>        Measured sweeps per temperature [default: 200]\n"
     "    --seed <N>           Seed of the Philox streams [default: 42]\n"
     "    --wolff              Accepted for compatibility (CPU algorithm choice)\n"
-    "    --raw                CPU Wolff time series: not in this build\n"
-    "    --gpu                Run on the GPU (required by this build)\n"
+    "    --raw                CPU Wolff time series: not provided by this drop-in\n"
+    "    --gpu                Run on the GPU (required: only the GPU path is provided)\n"
     "    --outdir <DIR>       Output directory [default: analysis/data]\n"
     "    --help, -h           Show this help message";
 
@@ -125,7 +125,7 @@ int main(int argc, char** argv) {
         if (n < 2) die("Error: --n must be at least 2 (got " + std::to_string(n) + ")");
     if (raw && use_gpu) fprintf(stderr, "Warning: --raw mode does not support --gpu; ignoring --gpu\n");
     if (raw) die("Error: --raw (CPU Wolff time series) is not provided by this GPU build");
-    if (!use_gpu) die("Error: this build provides only the GPU path; pass --gpu");
+    if (!use_gpu) die("Error: this drop-in provides only the GPU path; pass --gpu");
     for (int n : sizes)
         if (n > 1024 || (n & 1))
             die("Error: size " + std::to_string(n) +

@@ -10,7 +10,7 @@
 // isg_kz_sweep.
 //
 // Differences by design:
-//   * this build provides the GPU path only: without --gpu (the CPU run_kz_sweep)
+//   * this drop-in provides the GPU path only: without --gpu (the CPU run_kz_sweep)
 //     it exits with an error;
 //   * every tau_q's trials run as one batch and all tau_q values run at the
 //     same time, so the per-tau_q progress lines come out together; trial t
@@ -47,7 +47,7 @@ const char* kUsage =
     "    --freeze-sweeps <N>       Sweeps at the freeze temperature after the ramp [default: 0]\n"
     "    --freeze-temperature <T>  Freeze temperature [default: 0.01]\n"
     "    --seed <N>                Seed of the Philox streams [default: 42]\n"
-    "    --gpu                     Run on the GPU (required by this build)\n"
+    "    --gpu                     Run on the GPU (required: only the GPU path is provided)\n"
     "    --outdir <DIR>            Output directory [default: analysis/data]\n"
     "    --help, -h                Show this help message";
 
@@ -116,7 +116,7 @@ int main(int argc, char** argv) {
         die("Error: --tau-min must be >= 1 and <= --tau-max");
     if (use_gpu && geometry != "cubic")
         die("Error: --gpu KZ currently supports only --geometry cubic");
-    if (!use_gpu) die("Error: this build provides only the GPU path; pass --gpu");
+    if (!use_gpu) die("Error: this drop-in provides only the GPU path; pass --gpu");
     if (n > 1024 || (n & 1))
         die("Error: size " + std::to_string(n) +
             " unsupported: the checkerboard update needs an even size in 2..1024");

@@ -426,15 +426,19 @@ def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
     ess_pt = len(series) / (2 * tau_pt) / pt_s
     # training data from the plain sampler at T, with Z2 partners
     t1 = time.perf_counter()
-    data = lrn.collect_training_set(L, dim, T, chains=64, rounds=64, gap=20, warmup=2000)
+    # streaming maximum-likelihood training: every step sees fresh
+    # configurations of the plain sampler at T (256 chains, a snapshot every 10
+    # sweeps, with negations), so the network cannot memorise a fixed set
+    stream = lrn.TrainingStream(L, dim, T, chains=256, gap=10, warmup=2000)
     q = lrn.LearnedProposal(H, W, layers=6, seed=SEED)
     steps = 0
     tt = time.perf_counter()
     while time.perf_counter() - tt < train_seconds:
-        q.train(data, batch=128, steps=20, lr=1e-3)
-        steps += 20
+        q.train(stream.next(), batch=128, steps=4, lr=1e-3)
+        steps += 4
     train_s = time.perf_counter() - t1
-    nll = -q.train(data, batch=128, steps=1, lr=1e-4) / n
+    nll = -q.train(stream.next(), batch=128, steps=1, lr=1e-4) / n  # held-out batch
+    stream.close()
     ch = lrn.LearnedChain(q, L, dim, T, K=4096, sweeps=1, fallback_sweeps=20, min_accept=0.002)
     ch.start(1000)
     ch.batch()
@@ -869,13 +873,18 @@ def ncu_case_graph(kind: str):
     proposals of the untrained 2D L=32 network (sampling, then the flipped
     scores)."""
     pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
-    if kind == "learned":
+    if kind in ("learned", "learned-train"):
         import importlib
         import torch
         torch.cuda.set_device(0)
         lrn = importlib.import_module(pkg.__name__ + ".learned")
         q = lrn.LearnedProposal(32, 32, layers=6, seed=SEED)
-        q.sample(4096, 1)
+        if kind == "learned-train":
+            data = lrn.collect_training_set(32, 2, 2.269, chains=16, rounds=8, gap=10,
+                                            warmup=200)
+            q.train(data, batch=128, steps=3, lr=1e-3)
+        else:
+            q.sample(4096, 1)
         q.sync()
         print("ncu case done")
         return 0
@@ -933,17 +942,18 @@ def main():
     ap.add_argument("--pt-sweeps", type=int, default=200000)
     ap.add_argument("--ncu-case", nargs="?", const="words",
                     choices=["words", "resident", "graph", "cgraph3", "cgraph2", "reweight",
-                             "learned"],
+                             "learned", "learned-train"],
                     help="no timing: 'words' = a few half-sweeps of L=128 x 96 replicas (201 MB, "
                          "larger than L2) for an ncu capture of the half-sweep kernel; "
                          "'resident' = one 2000-sweep schedule of an L=30 lattice; "
                          "'graph'/'cgraph3'/'cgraph2' = one 100-sweep launch of the graph "
                          "kernels (BCC 8^3, 20 replicas); 'reweight' = one WHAM analysis; "
-                         "'learned' = 4096 proposals of the L=32 network (sample + score)")
+                         "'learned' = 4096 proposals of the L=32 network (sample + score); "
+                         "'learned-train' = three training steps of that network")
     args = ap.parse_args()
     if args.ncu_case == "resident":
         return ncu_case_resident()
-    if args.ncu_case in ("graph", "cgraph3", "cgraph2", "reweight", "learned"):
+    if args.ncu_case in ("graph", "cgraph3", "cgraph2", "reweight", "learned", "learned-train"):
         return ncu_case_graph(args.ncu_case)
     if args.ncu_case:
         return ncu_case()

@@ -158,6 +158,8 @@ int isg_ising_set_spins(isg_ising* h, int size_index, int replica, const int8_t*
  * a device buffer of L^dim +-1 bytes in natural layout. */
 int isg_ising_load_natural(isg_ising* h, int size_index, int replica, const int8_t* d_nat);
 int isg_ising_store_natural(isg_ising* h, int size_index, int replica, int8_t* d_nat);
+/* Every replica of one size: d_nat[r * N + i] (N = L^dim), in one call. */
+int isg_ising_store_natural_all(isg_ising* h, int size_index, int8_t* d_nat);
 
 /* Parallel-tempering sampling: n_sweeps sweeps continuing the sampling phase;
  * after sampling sweep k (0-based, counted since the last reset) the

@@ -1806,6 +1806,22 @@ int isg_ising_store_natural(isg_ising* H, int s, int r, int8_t* d_nat) {
     return check_launch("isg_ising_store_natural");
 }
 
+int isg_ising_store_natural_all(isg_ising* H, int s, int8_t* d_nat) {
+    if (!H || !d_nat) return fail(ISG_ERR_ARG, "isg_ising_store_natural_all: NULL argument");
+    if (s < 0 || s >= H->n_classes)
+        return fail(ISG_ERR_ARG, "isg_ising_store_natural_all: bad size index");
+    cudaSetDevice(H->device);
+    for (int r = 0; r < H->R; ++r) {
+        int64_t n, base;
+        int rc = spin_geometry(H, s, r, &n, &base);
+        if (rc) return rc;
+        k_ising_planes_to_nat<<<(int)std::min<int64_t>(1024, (n + 255) / 256), 256, 0,
+                                H->stream>>>(H->d_spins + base, d_nat + (size_t)r * n,
+                                             H->sizes[s], H->dim, (uint32_t)(n / 2));
+    }
+    return check_launch("isg_ising_store_natural_all");
+}
+
 int isg_ising_reset_sampling(isg_ising* H) {
     if (!H) return fail(ISG_ERR_ARG, "isg_ising_reset_sampling: NULL handle");
     cudaSetDevice(H->device);

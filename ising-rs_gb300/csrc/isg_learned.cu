@@ -243,30 +243,54 @@ __global__ void k_tf_dgrad(const __nv_bfloat16* __restrict__ w, NetShape S, int 
 // Weight and bias gradient partials of layer l: block k covers positions
 // [k*chunk, (k+1)*chunk) of the flattened batch; thread j accumulates weights
 // j, j + blockDim, ...  (tap, ci, co), plus the biases.
+// Weight and bias gradient partials of layer l over one chunk of `chunk`
+// flattened positions bp = b*HW + p (one block per chunk): the chunk's output
+// gradients and the input rows its taps reach (bp - W - 1 .. bp) are staged in
+// shared memory with a per-position tap-validity mask, then every thread
+// accumulates its weights over the chunk.  part[block][j], j = weights then
+// biases, summed in block order by k_sum_parts.
 __global__ void k_tf_wgrad(NetShape S, int l, int H, int W, int B, const float* __restrict__ in,
                            const float* __restrict__ dz, int chunk, float* __restrict__ part) {
+    extern __shared__ float wg_sm[];
     const int HW = H * W;
     const int cin = S.cin[l], cout = S.cout[l], taps = S.taps[l];
     const int nw = taps * cin * cout + cout;
     const int64_t n = (int64_t)B * HW;
     const int64_t start = (int64_t)blockIdx.x * chunk;
-    const int64_t stop = start + chunk < n ? start + chunk : n;
+    const int cnt = (int)(start + chunk < n ? chunk : n - start);
+    const int halo = W + 1;
+    float* s_dz = wg_sm;                              // [chunk][cout]
+    float* s_in = s_dz + (size_t)chunk * cout;        // [halo + chunk][cin]
+    unsigned char* s_ok = reinterpret_cast<unsigned char*>(s_in + (size_t)(halo + chunk) * cin);
+    for (int i = threadIdx.x; i < cnt * cout; i += blockDim.x) s_dz[i] = dz[start * cout + i];
+    for (int i = threadIdx.x; i < (halo + cnt) * cin; i += blockDim.x) {
+        const int64_t row = start - halo + i / cin;
+        s_in[i] = row >= 0 ? in[row * cin + i % cin] : 0.f;
+    }
+    for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+        const int p = (int)((start + q) % HW);
+        const int y = p / W, x = p - y * W;
+        unsigned char m = 0;
+        for (int t = 0; t < taps; ++t) {
+            const int yy = y + tap_dy(t), xx = x + tap_dx(t);
+            if (yy >= 0 && xx >= 0 && xx < W) m |= (unsigned char)(1u << t);
+        }
+        s_ok[q] = m;
+    }
+    __syncthreads();
     for (int j = threadIdx.x; j < nw; j += blockDim.x) {
         float acc = 0.f;
         if (j < taps * cin * cout) {
             const int co = j % cout;
             const int ci = (j / cout) % cin;
             const int t = j / (cout * cin);
-            for (int64_t bp = start; bp < stop; ++bp) {
-                const int p = (int)(bp % HW);
-                const int y = p / W, x = p - y * W;
-                const int yy = y + tap_dy(t), xx = x + tap_dx(t);
-                if (yy < 0 || xx < 0 || xx >= W) continue;
-                acc = fmaf(in[(bp - p + yy * W + xx) * cin + ci], dz[bp * cout + co], acc);
-            }
+            const int off = halo + tap_dy(t) * W + tap_dx(t);  // s_in row of q's tap
+            const unsigned char bit = (unsigned char)(1u << t);
+            for (int q = 0; q < cnt; ++q)
+                if (s_ok[q] & bit) acc = fmaf(s_in[(q + off) * cin + ci], s_dz[q * cout + co], acc);
         } else {
             const int co = j - taps * cin * cout;
-            for (int64_t bp = start; bp < stop; ++bp) acc += dz[bp * cout + co];
+            for (int q = 0; q < cnt; ++q) acc += s_dz[q * cout + co];
         }
         part[(int64_t)blockIdx.x * nw + j] = acc;
     }
@@ -767,8 +791,10 @@ static int forward_backward(isg_learned* h, int B, float* mean_lq) {
                                      h->d_lq);
     float* dz = h->d_dz;
     float* dn = h->d_dz2;
-    const int chunk = 2048;
+    const int chunk = 128;
     const int nparts = (int)(((int64_t)B * HW + chunk - 1) / chunk);
+    const size_t wg_smem = sizeof(float) * ((size_t)chunk * kC + (size_t)(h->W + 1 + chunk) * kC) +
+                           (size_t)chunk;
     for (int l = h->D - 1; l >= 0; --l) {
         const int nw = h->S.taps[l] * h->S.cin[l] * h->S.cout[l] + h->S.cout[l];
         if ((int64_t)nparts * nw > h->part_cap) {
@@ -776,8 +802,11 @@ static int forward_backward(isg_learned* h, int B, float* mean_lq) {
             h->part_cap = nparts * nw;
             ISG_CK(cudaMalloc((void**)&h->d_part, sizeof(float) * h->part_cap));
         }
-        k_tf_wgrad<<<nparts, 256, 0, st>>>(h->S, l, h->H, h->W, B, h->d_act + l * stride, dz,
-                                           chunk, h->d_part);
+        if (wg_smem > 48 * 1024)
+            ISG_CK(cudaFuncSetAttribute(k_tf_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)wg_smem));
+        k_tf_wgrad<<<nparts, 256, wg_smem, st>>>(h->S, l, h->H, h->W, B, h->d_act + l * stride, dz,
+                                                 chunk, h->d_part);
         k_sum_parts<<<(nw + 255) / 256, 256, 0, st>>>(h->d_part, nparts, nw,
                                                       h->d_grad + h->S.woff[l]);
         if (l > 0) {

@@ -43,6 +43,7 @@ def _declare_learned(L):
         "isg_learned_sync": [vp],
         "isg_ising_load_natural": [vp, i32, i32, vp],
         "isg_ising_store_natural": [vp, i32, i32, vp],
+        "isg_ising_store_natural_all": [vp, i32, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -279,3 +280,36 @@ def collect_training_set(L: int, dim: int, T: float, chains: int = 64, rounds: i
     out[k:] = -out[:k]
     perm = torch.randperm(out.shape[0], device=dev)
     return out[perm].contiguous()
+
+
+class TrainingStream:
+    """Fresh training configurations from the plain checkerboard sampler at
+    temperature T: `chains` independent replicas advance `gap` sweeps between
+    snapshots, so a network trained on the stream never sees a configuration
+    twice.  next() returns the snapshot and its negations (Z2) as a torch
+    int8 tensor (2 * chains, L^dim) on the GPU, in a shuffled order."""
+
+    def __init__(self, L: int, dim: int, T: float, chains: int = 256, gap: int = 10,
+                 warmup: int = 2000, seed: int = 3):
+        import torch
+        self.n = L ** dim
+        self.chains, self.gap = int(chains), int(gap)
+        self.b = IsingBatch([L], self.chains, seed=seed, dim=dim)
+        self.b.set_temperatures([T] * self.chains)
+        self.b.step(warmup)
+        self.dev = torch.device("cuda", torch.cuda.current_device())
+        self.buf = torch.empty((2 * self.chains, self.n), dtype=torch.int8, device=self.dev)
+        self.gen = torch.Generator(device=self.dev)
+        self.gen.manual_seed(seed)
+
+    def next(self):
+        import torch
+        self.b.step(self.gap)
+        _check(_lib().isg_ising_store_natural_all(self.b._h, 0, _tptr(self.buf)))
+        self.b.sync()
+        self.buf[self.chains:] = -self.buf[:self.chains]
+        perm = torch.randperm(2 * self.chains, device=self.dev, generator=self.gen)
+        return self.buf[perm].contiguous()
+
+    def close(self):
+        self.b.close()

@@ -18,8 +18,10 @@
 // keeps FP32 master weights (Adam) and refreshes the BF16 copy every step.
 // Sampling and scoring run on the tensor cores (k_ar_mma, BF16 activations
 // between layers) when the network's activation rings fit in shared memory,
-// else on the CUDA cores (k_ar_run, FP32 activations); either way the same
-// kernel produces a proposal and scores it, so log q is consistent.
+// else on the CUDA cores (k_ar_run, FP32 activations).  Scoring given
+// configurations uses k_ar_score (all positions of a layer at once) when its
+// buffers fit; it repeats k_ar_mma's arithmetic element by element, so a
+// proposal's log q is the same whichever kernel computes it.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -670,6 +672,191 @@ __global__ void __launch_bounds__(128)
     }
 }
 
+// ------------------------------------- tensor-core scoring (implicit GEMM)
+// log q of given configurations with every position of a layer at once: a CTA
+// stages the weights once and scores configurations blockIdx.x, + gridDim.x,
+// ...; rows of the tensor-core tiles = 16 positions.  Each
+// output element follows exactly the sampler's chain (taps 0..4 in order,
+// two k-steps each, bias after, ReLU, BF16), a tap outside the lattice adding
+// an exact zero (its A row points at a zero row), and the per-position log
+// sigmoid terms are summed in position order by one thread; so log q is
+// bit-identical to k_ar_mma's for the same configuration.
+struct ScoreSmem {
+    size_t act, zero, bt, btlast, w0, bias, spin, term, total;
+};
+__host__ __device__ inline ScoreSmem score_layout(int D, int HW) {
+    ScoreSmem m{};
+    const size_t tiles = (size_t)(HW + 15) / 16;  // 16 positions x 64 B per tile
+    m.act = 0;
+    m.zero = m.act + 2 * tiles * 1024;
+    m.bt = m.zero + 64;
+    m.btlast = m.bt + (size_t)(D - 2) * kC * kBtRow * 2;
+    m.w0 = m.btlast + (size_t)8 * kBtRow * 2;
+    m.bias = m.w0 + sizeof(float) * 4 * kC;
+    m.term = m.bias + sizeof(float) * ((size_t)(D - 1) * kC + 4);
+    m.spin = m.term + sizeof(float) * (size_t)HW;
+    m.total = (m.spin + (size_t)HW + 15) & ~(size_t)15;
+    return m;
+}
+
+template <int D>
+__global__ void __launch_bounds__(256, 1)
+    k_ar_score(const __nv_bfloat16* __restrict__ w, NetShape S, int H, int W, int flip,
+               const int8_t* __restrict__ spins, float* __restrict__ logq, int n_cfg) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int HW = H * W;
+    const ScoreSmem L = score_layout(D, HW);
+    unsigned char* act = smem + L.act;
+    __nv_bfloat16* bt = reinterpret_cast<__nv_bfloat16*>(smem + L.bt);
+    __nv_bfloat16* btl = reinterpret_cast<__nv_bfloat16*>(smem + L.btlast);
+    float* w0 = reinterpret_cast<float*>(smem + L.w0);
+    float* bias = reinterpret_cast<float*>(smem + L.bias);
+    float* term = reinterpret_cast<float*>(smem + L.term);
+    int8_t* sp = reinterpret_cast<int8_t*>(smem + L.spin);
+    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
+    constexpr uint32_t kWRow = kBtRow * 2;
+    for (int l = 1; l < D - 1; ++l) {
+        __nv_bfloat16* b = bt + (size_t)(l - 1) * kC * kBtRow;
+        for (int i = tid; i < kC * kBtRow; i += blockDim.x) {
+            const int n = i / kBtRow, k = i - n * kBtRow;
+            b[i] = k < 5 * kC ? w[S.woff[l] + k * kC + n] : __float2bfloat16(0.f);
+        }
+    }
+    for (int i = tid; i < 8 * kBtRow; i += blockDim.x) {
+        const int n = i / kBtRow, k = i - n * kBtRow;
+        btl[i] = (n == 0 && k < 5 * kC) ? w[S.woff[D - 1] + k] : __float2bfloat16(0.f);
+    }
+    for (int i = tid; i < 4 * kC; i += blockDim.x) w0[i] = bf(w, S.woff[0] + i);
+    for (int l = 0; l < D - 1; ++l)
+        for (int i = tid; i < kC; i += blockDim.x) bias[l * kC + i] = bf(w, S.boff[l] + i);
+    if (tid == 0) bias[(D - 1) * kC] = bf(w, S.boff[D - 1]);
+    if (tid < 16) reinterpret_cast<uint32_t*>(smem + L.zero)[tid] = 0u;
+    // the staged weights serve every configuration this CTA scores
+    for (int c = blockIdx.x; c < n_cfg; c += gridDim.x) {
+    __syncthreads();
+    for (int p = tid; p < HW; p += blockDim.x) {
+        const int8_t v = spins[(size_t)c * HW + p];
+        sp[p] = flip ? (int8_t)-v : v;
+    }
+    __syncthreads();
+    // layer 0 (mask A, 1 -> 32), as the sampler: a = bias; fma over taps 0..3
+    for (int i = tid; i < HW * 4; i += blockDim.x) {
+        const int p = i >> 2, j2 = i & 3;  // channels 8 j2 .. 8 j2 + 7 (one chunk)
+        const int y = p / W, x = p - y * W;
+        const bool up = y > 0, left = x > 0, right = x + 1 < W;
+        const float s0 = (up && left) ? (float)sp[p - W - 1] : 0.f;
+        const float s1 = up ? (float)sp[p - W] : 0.f;
+        const float s2 = (up && right) ? (float)sp[p - W + 1] : 0.f;
+        const float s3 = left ? (float)sp[p - 1] : 0.f;
+        uint32_t packed[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            float v[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int co = 8 * j2 + 2 * h + e;
+                float a = bias[co];
+                a = fmaf(w0[0 * kC + co], s0, a);
+                a = fmaf(w0[1 * kC + co], s1, a);
+                a = fmaf(w0[2 * kC + co], s2, a);
+                a = fmaf(w0[3 * kC + co], s3, a);
+                v[e] = fmaxf(a, 0.f);
+            }
+            __nv_bfloat162 b2 = __floats2bfloat162_rn(v[0], v[1]);
+            packed[h] = *reinterpret_cast<uint32_t*>(&b2);
+        }
+        *reinterpret_cast<uint4*>(act + ring_off(p & 15, j2) + (size_t)(p >> 4) * 1024) =
+            make_uint4(packed[0], packed[1], packed[2], packed[3]);
+    }
+    __syncthreads();
+    const uint32_t act_s = smem_u32(act), zero_s = smem_u32(smem + L.zero);
+    const int mtiles = (HW + 15) / 16;
+    const uint32_t layer_bytes = (uint32_t)mtiles * 1024;
+    const int g = lane >> 2, q4 = lane & 3;
+    for (int l = 1; l < D; ++l) {
+        const bool last = l == D - 1;
+        const uint32_t in_s = act_s + (uint32_t)((l - 1) & 1) * layer_bytes;
+        unsigned char* out = act + (size_t)(l & 1) * layer_bytes;
+        const uint32_t wl = smem_u32(last ? btl : bt + (size_t)(l - 1) * kC * kBtRow);
+        for (int mt = wp; mt < mtiles; mt += (int)(blockDim.x >> 5)) {
+            // this lane's A row: position pr = 16 mt + (lane & 15)
+            // (rows past the lattice read zeros; their outputs are never used)
+            const int pr = mt * 16 + (lane & 15);
+            const bool live = pr < HW;
+            const int yr = pr / W, xr = pr - yr * W;
+            const bool up = yr > 0, left = xr > 0, right = xr + 1 < W;
+            const int ch = lane >> 4;  // chunk within a k-step
+            uint32_t arow[5];
+            const int tp[5] = {pr - W - 1, pr - W, pr - W + 1, pr - 1, pr};
+            const bool tv[5] = {live && up && left, live && up, live && up && right,
+                                live && left, live};
+#pragma unroll
+            for (int t = 0; t < 5; ++t)
+                arow[t] = tv[t] ? in_s + (uint32_t)(tp[t] >> 4) * 1024 +
+                                      (uint32_t)((tp[t] & 15) * 64)
+                                : 0xFFFFFFFFu;
+            float acc[4][4];
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
+#pragma unroll
+            for (int t = 0; t < 5; ++t) {
+                // B of this tap: x4 over its 32 k values for every output tile
+                uint32_t bw[4][4];
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt) {
+                    if (last && nt > 0) break;
+                    ldsm_x4(bw[nt][0], bw[nt][1], bw[nt][2], bw[nt][3],
+                            wl + (uint32_t)(nt * 8 + (lane & 7)) * kWRow + (uint32_t)(t * kC) * 2 +
+                                (lane >> 3) * 16);
+                }
+#pragma unroll
+                for (int kb = 0; kb < 2; ++kb) {
+                    const int chunk = 2 * kb + ch;
+                    const uint32_t aaddr =
+                        arow[t] == 0xFFFFFFFFu
+                            ? zero_s + (uint32_t)chunk * 16
+                            : arow[t] + (uint32_t)((chunk ^ ((tp[t] >> 1) & 3)) << 4);
+                    uint32_t a0, a1, a2, a3;
+                    ldsm_x4(a0, a1, a2, a3, aaddr);
+#pragma unroll
+                    for (int nt = 0; nt < 4; ++nt) {
+                        if (last && nt > 0) break;
+                        mma_bf16(acc[nt], a0, a1, a2, a3, bw[nt][2 * kb], bw[nt][2 * kb + 1]);
+                    }
+                }
+            }
+            if (!last) {
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt) {
+                    const int col = nt * 8 + 2 * q4;
+                    const float b0 = bias[l * kC + col], b1 = bias[l * kC + col + 1];
+                    __nv_bfloat162 lo = __floats2bfloat162_rn(fmaxf(acc[nt][0] + b0, 0.f),
+                                                              fmaxf(acc[nt][1] + b1, 0.f));
+                    __nv_bfloat162 hi = __floats2bfloat162_rn(fmaxf(acc[nt][2] + b0, 0.f),
+                                                              fmaxf(acc[nt][3] + b1, 0.f));
+                    unsigned char* tile = out + (size_t)mt * 1024;
+                    *reinterpret_cast<__nv_bfloat162*>(tile + ring_off(g, nt) + q4 * 4) = lo;
+                    *reinterpret_cast<__nv_bfloat162*>(tile + ring_off(g + 8, nt) + q4 * 4) = hi;
+                }
+            } else if (q4 == 0) {
+                const float bl = bias[(D - 1) * kC];
+                const int pa = mt * 16 + g, pb = pa + 8;
+                if (pa < HW) term[pa] = log_sigmoid((float)sp[pa] * (acc[0][0] + bl));
+                if (pb < HW) term[pb] = log_sigmoid((float)sp[pb] * (acc[0][2] + bl));
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        float lq = 0.f;
+        for (int p = 0; p < HW; ++p) lq += term[p];
+        logq[c] = lq;
+    }
+    }
+}
+
 __global__ void k_to_float(const int8_t* __restrict__ s, float* __restrict__ f, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -728,8 +915,37 @@ static int launch_mma(isg_learned* h, int mode, int flip, int8_t* spins, float* 
     return ISG_OK;
 }
 
+// Scoring with all positions of a layer at once when its buffers fit.
+static bool use_score(const isg_learned* h) {
+    return use_mma(h) && score_layout(h->D, h->H * h->W).total <= 232448;
+}
+
+template <int D>
+static int launch_score(isg_learned* h, int flip, const int8_t* spins, float* lq, int K) {
+    const size_t smem = score_layout(D, h->H * h->W).total;
+    ISG_CK(cudaFuncSetAttribute(k_ar_score<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    k_ar_score<D><<<std::min(K, sms), 256, smem, h->stream>>>(h->d_wbf, h->S, h->H, h->W, flip,
+                                                             spins, lq, K);
+    ISG_CK(cudaGetLastError());
+    return ISG_OK;
+}
+
 static int launch_ar(isg_learned* h, int mode, int flip, int8_t* spins, float* lq, int K,
                      uint64_t step) {
+    if (mode == 1 && use_score(h)) {
+        switch (h->D) {
+            case 2: return launch_score<2>(h, flip, spins, lq, K);
+            case 3: return launch_score<3>(h, flip, spins, lq, K);
+            case 4: return launch_score<4>(h, flip, spins, lq, K);
+            case 5: return launch_score<5>(h, flip, spins, lq, K);
+            case 6: return launch_score<6>(h, flip, spins, lq, K);
+            case 7: return launch_score<7>(h, flip, spins, lq, K);
+            default: return launch_score<8>(h, flip, spins, lq, K);
+        }
+    }
     if (use_mma(h)) {
         switch (h->D) {
             case 2: return launch_mma<2>(h, mode, flip, spins, lq, K, step);

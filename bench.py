@@ -184,6 +184,19 @@ def tau_int(x) -> float:
     return float(tau)
 
 
+def tau_blocking(x, nb=20) -> float:
+    """tau_int from the spread of nb block means: var(block mean) = 2 tau
+    var(x) / B for blocks of B samples much longer than tau.  Unlike the
+    windowed sum it sees rare long excursions (a sticky independence chain)."""
+    x = np.asarray(x, float)
+    B = len(x) // nb
+    var = np.var(x)
+    if B < 2 or var < 1e-15:
+        return 0.5
+    bm = x[:B * nb].reshape(nb, B).mean(1)
+    return float(max(0.5, B * np.var(bm, ddof=1) / (2 * var)))
+
+
 def max_over_ranks(value: float, device="cpu") -> float:
     """The slowest rank's value (the job's timed region ends with the last rank);
     the value itself on a single process."""
@@ -422,7 +435,9 @@ def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
     pt_s = time.perf_counter() - t0
     mid = R // 2
     series = np.array([abs(rm[i][rt[i] == mid][0]) / n for i in range(rt.shape[0])], float)
-    tau_pt = tau_int(series)
+    # the larger of the windowed and the blocking estimate, on both sides
+    tau_pt_w, tau_pt_b = tau_int(series), tau_blocking(series)
+    tau_pt = max(tau_pt_w, tau_pt_b)
     ess_pt = len(series) / (2 * tau_pt) / pt_s
     # training data from the plain sampler at T, with Z2 partners
     t1 = time.perf_counter()
@@ -448,17 +463,22 @@ def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
     torch.cuda.synchronize()
     ch_s = time.perf_counter() - t2
     m = ch.m_series()[4096:]
-    tau_l = tau_int(m)
+    tau_l_w, tau_l_b = tau_int(m), tau_blocking(m)
+    tau_l = max(tau_l_w, tau_l_b)
     ess_l = len(m) / (2 * tau_l) / ch_s
+    m_err_l, m_err_pt = jackknife_mean_err(m), jackknife_mean_err(series)
     out = {"case": f"{dim}D L={L} T={T}", "plain_pt": {
         "replicas": R, "T_grid": [temps[0], temps[-1]], "sweeps": pt_sweeps,
         "seconds": pt_s, "sweeps_per_s": pt_sweeps / pt_s, "tau_int_sweeps": tau_pt,
-        "ess_per_s": ess_pt, "M": float(series.mean()), "M_err": jackknife_mean_err(series)},
+        "tau_windowed": tau_pt_w, "tau_blocking": tau_pt_b,
+        "ess_per_s": ess_pt, "M": float(series.mean()), "M_err": m_err_pt},
         "learned": {"layers": 6, "channels": 32, "train_steps": steps, "train_s": train_s,
                     "nll_per_site": nll, "proposals": len(m), "seconds": ch_s,
                     "acceptance": float(np.mean(ch.batch_accept[1:])),
-                    "tau_int_proposals": tau_l, "ess_per_s": ess_l, "M": float(m.mean()),
-                    "M_err": jackknife_mean_err(m)},
+                    "tau_int_proposals": tau_l, "tau_windowed": tau_l_w, "tau_blocking": tau_l_b,
+                    "ess_per_s": ess_l, "M": float(m.mean()), "M_err": m_err_l},
+        # both chains sample the same distribution: their |M| must agree
+        "M_diff_sigma": float((m.mean() - series.mean()) / np.hypot(m_err_l, m_err_pt)),
         "ratio_learned_over_plain": ess_l / ess_pt}
     ch.close()
     return out
@@ -938,7 +958,7 @@ def main():
     ap.add_argument("--learned", action="store_true",
                     help="config 5: learned proposal vs plain PT ESS/s (separate JSON lines)")
     ap.add_argument("--train-seconds", type=float, default=60.0)
-    ap.add_argument("--chain-batches", type=int, default=40)
+    ap.add_argument("--chain-batches", type=int, default=800)
     ap.add_argument("--pt-sweeps", type=int, default=200000)
     ap.add_argument("--ncu-case", nargs="?", const="words",
                     choices=["words", "resident", "graph", "cgraph3", "cgraph2", "reweight",

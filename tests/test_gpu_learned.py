@@ -166,3 +166,45 @@ def test_trained_network_gains_over_untrained(gpu):
         rates[trained] = float(np.mean(ch.batch_accept))
         ch.close()
     assert rates[True] > 0.05 and rates[True] > 5 * rates[False], rates
+
+
+def test_long_chain_matches_plain_sampler(gpu):
+    """Exactness where the proposal is far from perfect: on 2D L = 8 at T_c the
+    briefly trained chain (IMH + one sweep per batch, 600k proposals) and 64
+    independent plain Metropolis chains agree on <|m|> and <e> within 4.5
+    combined standard errors (the chain's from 20 block means, which include
+    its long sticky stretches)."""
+    import torch
+    L = learned(gpu)
+    Ls, T = 8, 2.269
+    n = Ls * Ls
+    stream = L.TrainingStream(Ls, 2, T, chains=128, gap=10, warmup=1000)
+    q = L.LearnedProposal(Ls, Ls, layers=6, seed=5)
+    for _ in range(60):
+        q.train(stream.next(), batch=128, steps=4, lr=2e-3)
+    stream.close()
+    ch = L.LearnedChain(q, Ls, 2, T, K=2048, sweeps=1, fallback_sweeps=20, min_accept=0.002)
+    ch.start(1000)
+    for _ in range(300):
+        ch.batch()
+    m, e = ch.m_series(), ch.e_series()
+    assert np.mean(ch.batch_accept) > 0.02
+    ch.close()
+
+    ref = gpu.IsingBatch([Ls], 64, seed=9, dim=2)
+    ref.set_temperatures([T] * 64)
+    ref.step(2000)
+    rb, rm = ref.run_schedule(None, 40000, measure_every=10)
+    ref.close()
+    rmag = np.abs(rm).astype(float) / n
+    ren = -rb.astype(float) / n
+
+    def block_err(x, nb=20):
+        B = len(x) // nb
+        return x[:B * nb].reshape(nb, B).mean(1).std(ddof=1) / np.sqrt(nb)
+
+    for name, a, r in (("|m|", m, rmag), ("e", e, ren)):
+        ea = block_err(a)
+        er = r.mean(0).std(ddof=1) / np.sqrt(r.shape[1])
+        diff = a.mean() - r.mean()
+        assert abs(diff) < 4.5 * np.hypot(ea, er), (name, a.mean(), ea, r.mean(), er)

@@ -454,7 +454,10 @@ def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
     train_s = time.perf_counter() - t1
     nll = -q.train(stream.next(), batch=128, steps=1, lr=1e-4) / n  # held-out batch
     stream.close()
-    ch = lrn.LearnedChain(q, L, dim, T, K=4096, sweeps=1, fallback_sweeps=20, min_accept=0.002)
+    # 20 checkerboard sweeps between batches: with a single sweep the
+    # independence chain at L = 32 had not left the ordered states the network
+    # over-represents after 10M proposals; 20 cost under 5% of a batch
+    ch = lrn.LearnedChain(q, L, dim, T, K=4096, sweeps=20, fallback_sweeps=50, min_accept=0.002)
     ch.start(1000)
     ch.batch()
     t2 = time.perf_counter()

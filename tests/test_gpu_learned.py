@@ -97,6 +97,20 @@ def test_sample_score_identical_and_matches_torch(gpu):
     assert torch.equal(p2, props) and torch.equal(l2, lq) and not torch.equal(p3, props)
 
 
+@pytest.mark.parametrize("H,W,D", [(16, 16, 6), (32, 32, 6), (64, 8, 6), (12, 20, 4)])
+def test_sample_score_identical_at_chain_sizes(gpu, H, W, D):
+    """The sampler and the whole-lattice scorer give bit-identical log q (and
+    log q of the negation) at the raster sizes the chains use."""
+    import torch
+    L = learned(gpu)
+    q = L.LearnedProposal(H, W, layers=D, seed=21)
+    props, lq, lqf = q.sample(300, 5)
+    s1 = q.score(props)
+    s2 = q.score(props, flip=True)
+    q.sync()
+    assert torch.equal(lq, s1) and torch.equal(lqf, s2)
+
+
 def test_distribution_is_normalised(gpu):
     import torch
     L = learned(gpu)

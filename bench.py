@@ -457,7 +457,7 @@ def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
     # 20 checkerboard sweeps between batches: with a single sweep the
     # independence chain at L = 32 had not left the ordered states the network
     # over-represents after 10M proposals; 20 cost under 5% of a batch
-    ch = lrn.LearnedChain(q, L, dim, T, K=4096, sweeps=20, fallback_sweeps=50, min_accept=0.002)
+    ch = lrn.LearnedChain(q, L, dim, T, K=None, sweeps=20, fallback_sweeps=50, min_accept=0.002)
     ch.start(1000)
     ch.batch()
     t2 = time.perf_counter()
@@ -465,7 +465,7 @@ def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
         ch.batch()
     torch.cuda.synchronize()
     ch_s = time.perf_counter() - t2
-    m = ch.m_series()[4096:]
+    m = ch.m_series()[ch.K:]
     tau_l_w, tau_l_b = tau_int(m), tau_blocking(m)
     tau_l = max(tau_l_w, tau_l_b)
     ess_l = len(m) / (2 * tau_l) / ch_s
@@ -476,7 +476,8 @@ def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
         "tau_windowed": tau_pt_w, "tau_blocking": tau_pt_b,
         "ess_per_s": ess_pt, "M": float(series.mean()), "M_err": m_err_pt},
         "learned": {"layers": 6, "channels": 32, "train_steps": steps, "train_s": train_s,
-                    "nll_per_site": nll, "proposals": len(m), "seconds": ch_s,
+                    "nll_per_site": nll, "batch_K": ch.K, "sweeps_per_batch": ch.sweeps,
+                    "proposals": len(m), "seconds": ch_s,
                     "acceptance": float(np.mean(ch.batch_accept[1:])),
                     "tau_int_proposals": tau_l, "tau_windowed": tau_l_w, "tau_blocking": tau_l_b,
                     "ess_per_s": ess_l, "M": float(m.mean()), "M_err": m_err_l},

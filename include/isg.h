@@ -339,6 +339,9 @@ int isg_learned_train(isg_learned* h, const int8_t* d_cfg_all, int n, int B, int
 /* K samples of q with log q, and log q of their negations (same kernel). */
 int isg_learned_sample(isg_learned* h, int K, uint64_t step, int8_t* d_out, float* d_lq,
                        float* d_lq_flip);
+/* Proposals per full wave of the sampling kernel on this device: batches of a
+ * multiple of it leave no SM idle in the last wave. */
+int isg_learned_batch_quantum(isg_learned* h, int* quantum);
 /* log q of K device configurations (flip = 1: of their negations). */
 int isg_learned_score(isg_learned* h, const int8_t* d_cfg, int K, int flip, float* d_lq);
 /* Exact bond sums and magnetisations of K device configurations (L^dim, PBC). */

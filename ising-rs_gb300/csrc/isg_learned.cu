@@ -1225,6 +1225,38 @@ int isg_learned_sample(isg_learned* h, int K, uint64_t step, int8_t* d_out, floa
     return rc;
 }
 
+// Proposals per full wave of the sampling kernel: configurations per CTA x
+// resident CTAs per SM x SMs.  A sampling pass costs the same for any K up to
+// a multiple of this, so batches sized in these units waste no SM.
+int isg_learned_batch_quantum(isg_learned* h, int* quantum) {
+    if (!h || !quantum) return fail(ISG_ERR_ARG, "isg_learned_batch_quantum: bad argument");
+    cudaSetDevice(h->device);
+    int sms = 1;
+    ISG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+    int per_sm = 1, rows = kMmaRows;
+    if (use_mma(h)) {
+        const size_t smem = mma_layout(h->D, h->W).total;
+        void (*k)(const __nv_bfloat16*, NetShape, int, int, int, int, int8_t*, float*, int,
+                  uint64_t, uint64_t) = nullptr;
+        switch (h->D) {
+            case 2: k = k_ar_mma<2>; break;
+            case 3: k = k_ar_mma<3>; break;
+            case 4: k = k_ar_mma<4>; break;
+            case 5: k = k_ar_mma<5>; break;
+            case 6: k = k_ar_mma<6>; break;
+            case 7: k = k_ar_mma<7>; break;
+            default: k = k_ar_mma<8>; break;
+        }
+        ISG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        ISG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, smem));
+    } else {
+        rows = 4;  // the CUDA-core kernel: 4 configurations per block
+        per_sm = 1;
+    }
+    *quantum = rows * std::max(per_sm, 1) * sms;
+    return ISG_OK;
+}
+
 // log q of K given configurations (device, natural layout): scoring mode of
 // the sampling kernel; flip = 1 scores the negated configurations.
 int isg_learned_score(isg_learned* h, const int8_t* d_cfg, int K, int flip, float* d_lq) {

@@ -36,6 +36,7 @@ def _declare_learned(L):
         "isg_learned_train": [vp, vp, i32, i32, i32, f32, vp],
         "isg_learned_sample": [vp, i32, u64, vp, vp, vp],
         "isg_learned_score": [vp, vp, i32, i32, vp],
+        "isg_learned_batch_quantum": [vp, vp],
         "isg_learned_energies": [vp, vp, i32, i32, i32, vp, vp],
         "isg_learned_imh": [vp, vp, vp, vp, vp, i32, dbl, dbl, vp, vp, vp, vp, vp, vp, u64],
         "isg_learned_state_a": [vp, vp, vp, vp, dbl, dbl, vp],
@@ -133,6 +134,12 @@ class LearnedProposal:
                                          _tptr(lqf)))
         return out, lq, lqf
 
+    def batch_quantum(self) -> int:
+        """Proposals per full wave of the sampling kernel on this GPU."""
+        v = C.c_int(0)
+        _check(_lib().isg_learned_batch_quantum(self._h, C.byref(v)))
+        return v.value
+
     def score(self, d_cfg, flip: bool = False):
         import torch
         lq = torch.empty(d_cfg.shape[0], dtype=torch.float32, device=d_cfg.device)
@@ -148,10 +155,14 @@ class LearnedChain:
     """Exact MCMC at temperature T: learned independence proposals + sweeps."""
 
     def __init__(self, proposal: LearnedProposal, L: int, dim: int, T: float, J: float = 1.0,
-                 K: int = 4096, sweeps: int = 1, fallback_sweeps: int = 20,
+                 K: int | None = 4096, sweeps: int = 1, fallback_sweeps: int = 20,
                  min_accept: float = 0.002, seed: int = 11):
         import torch
         self.q, self.L, self.dim, self.T, self.J = proposal, int(L), int(dim), float(T), float(J)
+        if K is None:
+            # at least 4096 proposals, in whole waves of the sampling kernel
+            qn = proposal.batch_quantum()
+            K = -(-4096 // qn) * qn
         self.K, self.sweeps, self.fallback, self.min_accept = int(K), int(sweeps), \
             int(fallback_sweeps), float(min_accept)
         self.n = self.L ** self.dim

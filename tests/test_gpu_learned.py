@@ -222,3 +222,13 @@ def test_long_chain_matches_plain_sampler(gpu):
         er = r.mean(0).std(ddof=1) / np.sqrt(r.shape[1])
         diff = a.mean() - r.mean()
         assert abs(diff) < 4.5 * np.hypot(ea, er), (name, a.mean(), ea, r.mean(), er)
+
+
+def test_batch_quantum_is_whole_waves(gpu):
+    import torch
+    L = learned(gpu)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    for H, W in ((16, 16), (32, 32)):
+        q = L.LearnedProposal(H, W, layers=6, seed=1)
+        k = q.batch_quantum()
+        assert k % (16 * sms) == 0 and k >= 16 * sms, (H, W, k, sms)

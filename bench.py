@@ -893,9 +893,9 @@ def ncu_case_graph(kind: str):
     """No timing: cases for ncu captures of the graph, reweighting and learned
     kernels.  graph / cgraph3 / cgraph2: one 100-sweep launch on every replica
     of a BCC 8^3 graph (1024 nodes, 20 replicas) with a record every sweep;
-    reweight: one WHAM analysis of 20 x 100,000 samples; learned: 4096
-    proposals of the untrained 2D L=32 network (sampling, then the flipped
-    scores)."""
+    reweight: one WHAM analysis of 20 x 100,000 samples; learned: one chain
+    batch (4096 rounded up to whole waves of the sampler) of the untrained 2D
+    L=32 network (sampling, then the flipped scores)."""
     pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
     if kind in ("learned", "learned-train"):
         import importlib
@@ -908,7 +908,8 @@ def ncu_case_graph(kind: str):
                                             warmup=200)
             q.train(data, batch=128, steps=3, lr=1e-3)
         else:
-            q.sample(4096, 1)
+            qn = q.batch_quantum()
+            q.sample(-(-4096 // qn) * qn, 1)
         q.sync()
         print("ncu case done")
         return 0

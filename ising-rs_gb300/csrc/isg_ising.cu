@@ -230,8 +230,8 @@ __device__ __forceinline__ uint32_t metropolis_word(uint32_t ow, uint32_t nd, ui
     const uint2 e3 = lds_v2(__byte_perm(idx8, tbase, 0x7653));
     uint32_t f = (U0 < e0.x ? 0x00000001u : 0u) | (U1 < e1.x ? 0x00000100u : 0u) |
                  (U2 < e2.x ? 0x00010000u : 0u) | (U3 < e3.x ? 0x01000000u : 0u);
-    const bool tie = ((U0 ^ e0.x) < 0x10000u) | ((U1 ^ e1.x) < 0x10000u) |
-                     ((U2 ^ e2.x) < 0x10000u) | ((U3 ^ e3.x) < 0x10000u);
+    // tie: equal upper halves, i.e. U - T < 2^16 (T's lower half is zero)
+    const bool tie = min(min(U0 - e0.x, U1 - e1.x), min(U2 - e2.x, U3 - e3.x)) < 0x10000u;
     if (tie) {
         const U4 fn = philox_w(pre, P, 0x80000000u | wfine);
         f = ((((U0 & 0xFFFF0000u) | (fn.x >> 16)) <= e0.y) ? 0x00000001u : 0u) |
@@ -282,8 +282,8 @@ __device__ __forceinline__ void rolling_step(
     const IsingParams& P, const PhiloxPre& pre, uint32_t tbase, const U4& uc,
     const uint32_t* oc, const uint32_t* oa, const uint32_t* ob, uint32_t* mc, uint32_t col,
     uint32_t pz, uint32_t pwm, bool single, bool first, bool last, int src_up, int src_dn,
-    int src_prev, int src_next, uint32_t& o, uint32_t& p, uint32_t& zm, uint32_t& za,
-    uint32_t& zp, uint32_t& h0, uint32_t& h1, uint32_t& ow, MeasAcc& macc) {
+    int src_x, uint32_t sel_x, uint32_t& o, uint32_t& zm, uint32_t& za, uint32_t& zp,
+    uint32_t& h0, uint32_t& h1, uint32_t& ow, MeasAcc& macc) {
     const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm;
     const uint32_t n_zp = ldg_nc(oc + o2);
     const uint32_t n_h0 = ldg_nc(oa + o1);
@@ -291,11 +291,10 @@ __device__ __forceinline__ void rolling_step(
     const uint32_t n_ow = ldg_u32(mc + o1);
     const uint32_t up = __shfl_sync(ISG_FULL_MASK, za, src_up);
     const uint32_t dn = __shfl_sync(ISG_FULL_MASK, za, src_dn);
-    const uint32_t prev = __shfl_sync(ISG_FULL_MASK, za, src_prev);
-    const uint32_t next = __shfl_sync(ISG_FULL_MASK, za, src_next);
+    const uint32_t nx = __shfl_sync(ISG_FULL_MASK, za, src_x);
     const uint32_t wyp = single ? h1 : (last ? h0 : up);
     const uint32_t wym = first ? h0 : dn;
-    const uint32_t wx = p ? __funnelshift_r(za, next, 8) : __funnelshift_l(prev, za, 8);
+    const uint32_t wx = __byte_perm(za, nx, sel_x);
     const uint32_t nd = (wx + za + wyp) + (wym + zp + zm);
     uint32_t nw = ow;
     if (MODE != 2) {
@@ -311,7 +310,6 @@ __device__ __forceinline__ void rolling_step(
     h0 = n_h0;
     h1 = n_h1;
     ow = n_ow;
-    p ^= 1u;
     o = o1;
 }
 
@@ -322,9 +320,9 @@ __device__ __forceinline__ void rolling_step2(
     const IsingParams& P, const PhiloxPre& pre, uint32_t tbase, const U4& uc,
     const uint32_t* oc, const uint32_t* oa, const uint32_t* ob, uint32_t* mc, uint32_t col,
     uint32_t pz, uint32_t pwm, bool single, bool first, bool last, int src_up, int src_dn,
-    int src_prev, int src_next, uint32_t& o, uint32_t& p, uint32_t& zm, uint32_t& za,
-    uint32_t& zp, uint32_t& qzp, uint32_t& h0, uint32_t& qh0, uint32_t& h1, uint32_t& qh1,
-    uint32_t& ow, uint32_t& qow, MeasAcc& macc) {
+    int src_x, uint32_t sel_x, uint32_t& o, uint32_t& zm, uint32_t& za, uint32_t& zp,
+    uint32_t& qzp, uint32_t& h0, uint32_t& qh0, uint32_t& h1, uint32_t& qh1, uint32_t& ow,
+    uint32_t& qow, MeasAcc& macc) {
     const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm, o3 = (o + 3 * pz) & pwm;
     const uint32_t n_zp = ldg_nc(oc + o3);
     const uint32_t n_h0 = ldg_nc(oa + o2);
@@ -332,11 +330,10 @@ __device__ __forceinline__ void rolling_step2(
     const uint32_t n_ow = ldg_u32(mc + o2);
     const uint32_t up = __shfl_sync(ISG_FULL_MASK, za, src_up);
     const uint32_t dn = __shfl_sync(ISG_FULL_MASK, za, src_dn);
-    const uint32_t prev = __shfl_sync(ISG_FULL_MASK, za, src_prev);
-    const uint32_t next = __shfl_sync(ISG_FULL_MASK, za, src_next);
+    const uint32_t nx = __shfl_sync(ISG_FULL_MASK, za, src_x);
     const uint32_t wyp = single ? h1 : (last ? h0 : up);
     const uint32_t wym = first ? h0 : dn;
-    const uint32_t wx = p ? __funnelshift_r(za, next, 8) : __funnelshift_l(prev, za, 8);
+    const uint32_t wx = __byte_perm(za, nx, sel_x);
     const uint32_t nd = (wx + za + wyp) + (wym + zp + zm);
     uint32_t nw = ow;
     if (MODE != 2) {
@@ -356,7 +353,6 @@ __device__ __forceinline__ void rolling_step2(
     qh1 = n_h1;
     ow = qow;
     qow = n_ow;
-    p ^= 1u;
     o = o1;
 }
 
@@ -452,7 +448,14 @@ __global__ void __launch_bounds__(256, PF == 1 ? 3 : 2)
             const uint32_t* oa = oth + ha;
             const uint32_t* ob = oth + hb;
             uint32_t* mc = own + col;
-            uint32_t p = (y + z0 + (uint32_t)colour) & 1u;
+            // x neighbours: with p = (y + z + colour) & 1 (z0 is even), the
+            // other colour's bytes at x - 1 + p come from this word and the next
+            // (p = 1) or previous (p = 0) word of the row, one shuffle and one
+            // byte permute: bytes {1,2,3} of za + byte 0 of next, or byte 3 of
+            // prev + bytes {0,1,2} of za
+            const bool pe = ((y + (uint32_t)colour) & 1u) != 0;  // p at even z
+            const int src_lo = pe ? src_next : src_prev, src_hi = pe ? src_prev : src_next;
+            const uint32_t sel_lo = pe ? 0x4321u : 0x2107u, sel_hi = pe ? 0x2107u : 0x4321u;
             uint32_t o = z0 * pz;                        // offset of plane z
             uint32_t zm = ldg_nc(oc + ((o - pz) & pwm));
             uint32_t za = ldg_nc(oc + o);
@@ -467,11 +470,11 @@ __global__ void __launch_bounds__(256, PF == 1 ? 3 : 2)
                     U4 uc{};
                     if (MODE != 2) uc = philox_w(pre, P, (o >> 1) + col);
                     rolling_step<MODE, false>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm,
-                                              single, first, last, src_up, src_dn, src_prev,
-                                              src_next, o, p, zm, za, zp, h0, h1, ow, macc);
+                                              single, first, last, src_up, src_dn, src_lo,
+                                              sel_lo, o, zm, za, zp, h0, h1, ow, macc);
                     rolling_step<MODE, true>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm,
-                                             single, first, last, src_up, src_dn, src_prev,
-                                             src_next, o, p, zm, za, zp, h0, h1, ow, macc);
+                                             single, first, last, src_up, src_dn, src_hi,
+                                             sel_hi, o, zm, za, zp, h0, h1, ow, macc);
                 }
             } else {
                 uint32_t qzp = ldg_nc(oc + ((o + 2 * pz) & pwm));
@@ -482,13 +485,13 @@ __global__ void __launch_bounds__(256, PF == 1 ? 3 : 2)
                     U4 uc{};
                     if (MODE != 2) uc = philox_w(pre, P, (o >> 1) + col);
                     rolling_step2<MODE, false>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm,
-                                               single, first, last, src_up, src_dn, src_prev,
-                                               src_next, o, p, zm, za, zp, qzp, h0, qh0, h1,
-                                               qh1, ow, qow, macc);
+                                               single, first, last, src_up, src_dn, src_lo,
+                                               sel_lo, o, zm, za, zp, qzp, h0, qh0, h1, qh1, ow,
+                                               qow, macc);
                     rolling_step2<MODE, true>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm,
-                                              single, first, last, src_up, src_dn, src_prev,
-                                              src_next, o, p, zm, za, zp, qzp, h0, qh0, h1, qh1,
-                                              ow, qow, macc);
+                                              single, first, last, src_up, src_dn, src_hi,
+                                              sel_hi, o, zm, za, zp, qzp, h0, qh0, h1, qh1, ow,
+                                              qow, macc);
                 }
             }
         } else {

@@ -273,86 +273,87 @@ __device__ __forceinline__ void meas_flush(unsigned long long* acc, int rep, Mea
     m = MeasAcc{0, 0, 0, 0, 0};
 }
 
-// One z-step of a rolling column at plane offset `o` (words): the new own
-// word from the other colour's words at z-1, z, z+1 (zm, za, zp) and the halo
-// row(s), with the next plane's loads issued first.  HI selects the upper
-// halves of the z-pair's random words (odd z) instead of the lower (even z).
-template <int MODE, bool HI>
-__device__ __forceinline__ void rolling_step(
-    const IsingParams& P, const PhiloxPre& pre, uint32_t tbase, const U4& uc,
-    const uint32_t* oc, const uint32_t* oa, const uint32_t* ob, uint32_t* mc, uint32_t col,
-    uint32_t pz, uint32_t pwm, bool single, bool first, bool last, int src_up, int src_dn,
-    int src_x, uint32_t sel_x, uint32_t& o, uint32_t& zm, uint32_t& za, uint32_t& zp,
-    uint32_t& h0, uint32_t& h1, uint32_t& ow, MeasAcc& macc) {
-    const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm;
-    const uint32_t n_zp = ldg_nc(oc + o2);
-    const uint32_t n_h0 = ldg_nc(oa + o1);
-    const uint32_t n_h1 = single ? ldg_nc(ob + o1) : 0u;
-    const uint32_t n_ow = ldg_u32(mc + o1);
-    const uint32_t up = __shfl_sync(ISG_FULL_MASK, za, src_up);
-    const uint32_t dn = __shfl_sync(ISG_FULL_MASK, za, src_dn);
-    const uint32_t nx = __shfl_sync(ISG_FULL_MASK, za, src_x);
-    const uint32_t wyp = single ? h1 : (last ? h0 : up);
-    const uint32_t wym = first ? h0 : dn;
-    const uint32_t wx = __byte_perm(za, nx, sel_x);
-    const uint32_t nd = (wx + za + wyp) + (wym + zp + zm);
-    uint32_t nw = ow;
-    if (MODE != 2) {
-        nw = HI ? metropolis_word(ow, nd, tbase, uc.x, uc.y, uc.z, uc.w, pre, P, o + col)
-                : metropolis_word(ow, nd, tbase, uc.x << 16, uc.y << 16, uc.z << 16,
-                                  uc.w << 16, pre, P, o + col);
-        mc[o] = nw;
-    }
-    if (MODE != 0) meas_add(macc, nw, nd, za);
-    zm = za;
-    za = zp;
-    zp = n_zp;
-    h0 = n_h0;
-    h1 = n_h1;
-    ow = n_ow;
-    o = o1;
+__device__ __forceinline__ uint2 ldg_nc2(const uint32_t* p) {
+    uint2 v;
+    asm volatile("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint2 ldg_u2(const uint32_t* p) {
+    uint2 v;
+    asm volatile("ld.global.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
 }
 
-// The same step with the loads issued two planes ahead (own word and halo of
-// plane z+2, other colour at z+3): one more word of each kind in flight per lane.
-template <int MODE, bool HI>
-__device__ __forceinline__ void rolling_step2(
-    const IsingParams& P, const PhiloxPre& pre, uint32_t tbase, const U4& uc,
-    const uint32_t* oc, const uint32_t* oa, const uint32_t* ob, uint32_t* mc, uint32_t col,
-    uint32_t pz, uint32_t pwm, bool single, bool first, bool last, int src_up, int src_dn,
-    int src_x, uint32_t sel_x, uint32_t& o, uint32_t& zm, uint32_t& za, uint32_t& zp,
-    uint32_t& qzp, uint32_t& h0, uint32_t& qh0, uint32_t& h1, uint32_t& qh1, uint32_t& ow,
-    uint32_t& qow, MeasAcc& macc) {
-    const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm, o3 = (o + 3 * pz) & pwm;
-    const uint32_t n_zp = ldg_nc(oc + o3);
-    const uint32_t n_h0 = ldg_nc(oa + o2);
-    const uint32_t n_h1 = single ? ldg_nc(ob + o2) : 0u;
-    const uint32_t n_ow = ldg_u32(mc + o2);
-    const uint32_t up = __shfl_sync(ISG_FULL_MASK, za, src_up);
-    const uint32_t dn = __shfl_sync(ISG_FULL_MASK, za, src_dn);
-    const uint32_t nx = __shfl_sync(ISG_FULL_MASK, za, src_x);
-    const uint32_t wyp = single ? h1 : (last ? h0 : up);
-    const uint32_t wym = first ? h0 : dn;
-    const uint32_t wx = __byte_perm(za, nx, sel_x);
-    const uint32_t nd = (wx + za + wyp) + (wym + zp + zm);
-    uint32_t nw = ow;
-    if (MODE != 2) {
-        nw = HI ? metropolis_word(ow, nd, tbase, uc.x, uc.y, uc.z, uc.w, pre, P, o + col)
-                : metropolis_word(ow, nd, tbase, uc.x << 16, uc.y << 16, uc.z << 16,
-                                  uc.w << 16, pre, P, o + col);
-        mc[o] = nw;
+// One z-step of a rolling column at plane offset `o` (words).  A lane owns two
+// adjacent words (x, y) of a row: their new own words from the other colour's
+// word pairs at z-1, z, z+1 (zm, za, zp) and the halo pair h0 (row y-1 on the
+// first row of the task, y+1 on the last), with the loads of plane z+PF (own,
+// halo) and z+PF+1 (other colour) issued first; PF = 2 keeps one more pair of
+// each in flight (q*).  HI selects the upper halves of the z pair's random
+// words (odd z).  x neighbours: with px = (y + z + colour) & 1 the other
+// colour's bytes at x - 1 + px are bytes {1,2,3} of a word + byte 0 of the
+// next word (px = 1), or byte 3 of the previous word + bytes {0,1,2} (px = 0);
+// one of the two is the lane's own other word, the other comes by one shuffle
+// from the neighbour lane of the row (src_x, whose px is the same).
+template <int MODE, bool HI, int PF>
+__device__ __forceinline__ void rolling_pair_step(
+    const IsingParams& P, const PhiloxPre& pre, uint32_t tbase, const U4& ua, const U4& ub,
+    const uint32_t* oc, const uint32_t* oa, uint32_t* mc, uint32_t col, uint32_t pz,
+    uint32_t pwm, bool first, bool last, int src_up, int src_dn, int src_x, bool px,
+    uint32_t sel_x, uint32_t& o, uint2& zm, uint2& za, uint2& zp, uint2& qzp, uint2& h0,
+    uint2& qh0, uint2& ow, uint2& qow, MeasAcc& macc) {
+    const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm;
+    uint2 n_zp, n_h0, n_ow;
+    if constexpr (PF == 1) {
+        n_zp = ldg_nc2(oc + o2);
+        n_h0 = ldg_nc2(oa + o1);
+        n_ow = ldg_u2(mc + o1);
+    } else {
+        const uint32_t o3 = (o + 3 * pz) & pwm;
+        n_zp = ldg_nc2(oc + o3);
+        n_h0 = ldg_nc2(oa + o2);
+        n_ow = ldg_u2(mc + o2);
     }
-    if (MODE != 0) meas_add(macc, nw, nd, za);
+    const uint32_t upx = __shfl_sync(ISG_FULL_MASK, za.x, src_up);
+    const uint32_t upy = __shfl_sync(ISG_FULL_MASK, za.y, src_up);
+    const uint32_t dnx = __shfl_sync(ISG_FULL_MASK, za.x, src_dn);
+    const uint32_t dny = __shfl_sync(ISG_FULL_MASK, za.y, src_dn);
+    const uint32_t nb = __shfl_sync(ISG_FULL_MASK, px ? za.x : za.y, src_x);
+    const uint32_t wx0 = __byte_perm(za.x, px ? za.y : nb, sel_x);
+    const uint32_t wx1 = __byte_perm(za.y, px ? nb : za.x, sel_x);
+    const uint32_t nd0 = (wx0 + za.x + (last ? h0.x : upx)) + ((first ? h0.x : dnx) + zp.x + zm.x);
+    const uint32_t nd1 = (wx1 + za.y + (last ? h0.y : upy)) + ((first ? h0.y : dny) + zp.y + zm.y);
+    uint2 nw = ow;
+    if (MODE != 2) {
+        if (HI) {
+            nw.x = metropolis_word(ow.x, nd0, tbase, ua.x, ua.y, ua.z, ua.w, pre, P, o + col);
+            nw.y = metropolis_word(ow.y, nd1, tbase, ub.x, ub.y, ub.z, ub.w, pre, P, o + col + 1);
+        } else {
+            nw.x = metropolis_word(ow.x, nd0, tbase, ua.x << 16, ua.y << 16, ua.z << 16,
+                                   ua.w << 16, pre, P, o + col);
+            nw.y = metropolis_word(ow.y, nd1, tbase, ub.x << 16, ub.y << 16, ub.z << 16,
+                                   ub.w << 16, pre, P, o + col + 1);
+        }
+        *reinterpret_cast<uint2*>(mc + o) = nw;
+    }
+    if (MODE != 0) {
+        meas_add(macc, nw.x, nd0, za.x);
+        meas_add(macc, nw.y, nd1, za.y);
+    }
     zm = za;
     za = zp;
-    zp = qzp;
-    qzp = n_zp;
-    h0 = qh0;
-    qh0 = n_h0;
-    h1 = qh1;
-    qh1 = n_h1;
-    ow = qow;
-    qow = n_ow;
+    if constexpr (PF == 1) {
+        zp = n_zp;
+        h0 = n_h0;
+        ow = n_ow;
+    } else {
+        zp = qzp;
+        qzp = n_zp;
+        h0 = qh0;
+        qh0 = n_h0;
+        ow = qow;
+        qow = n_ow;
+    }
     o = o1;
 }
 
@@ -434,65 +435,58 @@ __global__ void __launch_bounds__(256, PF == 1 ? 3 : 2)
             uint32_t* own = reinterpret_cast<uint32_t*>(base + (int64_t)colour * C.plane_sites);
             const uint32_t* oth =
                 reinterpret_cast<const uint32_t*>(base + (int64_t)(colour ^ 1) * C.plane_sites);
+            // a warp task: 64 words (nr rows of rw words), two adjacent words
+            // per lane; rw >= 8 (L >= 64), so every row has >= 4 lanes and a
+            // task >= 2 rows (L <= 256)
             const uint32_t yb = (g << 3) + (uint32_t)wib;
             const uint32_t pz = L << lrw;          // words per z-plane
             const uint32_t pwm = (pz << C.log2L) - 1;  // plane words - 1 (power of two)
-            const uint32_t col = (yb << 5) + (uint32_t)lane;
-            const uint32_t rb = (uint32_t)lane >> lrw, nr = 32u >> lrw;
+            const int lh = lrw - 1;                // log2(lanes per row)
+            const uint32_t k2 = (uint32_t)lane & ((1u << lh) - 1);
+            const uint32_t col = (yb << 6) + 2 * (uint32_t)lane;  // the lane's first word
+            const uint32_t rb = (uint32_t)lane >> lh, nr = 32u >> lh;
             const uint32_t y = yb * nr + rb;
-            const bool first = rb == 0, last = rb == nr - 1, single = nr == 1;
-            const uint32_t ha = (((first ? y - 1 : y + 1) & Lm) << lrw) | k4;
-            const uint32_t hb = (((y + 1) & Lm) << lrw) | k4;
-            const int src_up = (lane + (int)rw) & 31, src_dn = (lane - (int)rw) & 31;
+            const bool first = rb == 0, last = rb == nr - 1;
+            const uint32_t ha = (((first ? y - 1 : y + 1) & Lm) << lrw) | (2 * k2);
+            const int src_up = (lane + (1 << lh)) & 31, src_dn = (lane - (1 << lh)) & 31;
+            const uint32_t km = (1u << lh) - 1;
+            const int src_prev = lane - (int)k2 + (int)((k2 - 1) & km);
+            const int src_next = lane - (int)k2 + (int)((k2 + 1) & km);
             const uint32_t* oc = oth + col;   // column base pointers
             const uint32_t* oa = oth + ha;
-            const uint32_t* ob = oth + hb;
             uint32_t* mc = own + col;
-            // x neighbours: with p = (y + z + colour) & 1 (z0 is even), the
-            // other colour's bytes at x - 1 + p come from this word and the next
-            // (p = 1) or previous (p = 0) word of the row, one shuffle and one
-            // byte permute: bytes {1,2,3} of za + byte 0 of next, or byte 3 of
-            // prev + bytes {0,1,2} of za
-            const bool pe = ((y + (uint32_t)colour) & 1u) != 0;  // p at even z
+            // x-neighbour parity at even z (z0 is even) and at odd z
+            const bool pe = ((y + (uint32_t)colour) & 1u) != 0;
             const int src_lo = pe ? src_next : src_prev, src_hi = pe ? src_prev : src_next;
             const uint32_t sel_lo = pe ? 0x4321u : 0x2107u, sel_hi = pe ? 0x2107u : 0x4321u;
             uint32_t o = z0 * pz;                        // offset of plane z
-            uint32_t zm = ldg_nc(oc + ((o - pz) & pwm));
-            uint32_t za = ldg_nc(oc + o);
-            uint32_t zp = ldg_nc(oc + ((o + pz) & pwm));
-            uint32_t h0 = ldg_nc(oa + o);
-            uint32_t h1 = single ? ldg_nc(ob + o) : 0u;
-            uint32_t ow = ldg_u32(mc + o);
-            // z pairs (2k, 2k+1) share one Philox block: counter (z>>1)*pz + col,
-            // lower 16-bit halves for even z, upper for odd z
-            if constexpr (PF == 1) {
-                for (uint32_t z = z0; z < z1; z += 2) {
-                    U4 uc{};
-                    if (MODE != 2) uc = philox_w(pre, P, (o >> 1) + col);
-                    rolling_step<MODE, false>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm,
-                                              single, first, last, src_up, src_dn, src_lo,
-                                              sel_lo, o, zm, za, zp, h0, h1, ow, macc);
-                    rolling_step<MODE, true>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm,
-                                             single, first, last, src_up, src_dn, src_hi,
-                                             sel_hi, o, zm, za, zp, h0, h1, ow, macc);
+            uint2 zm = ldg_nc2(oc + ((o - pz) & pwm));
+            uint2 za = ldg_nc2(oc + o);
+            uint2 zp = ldg_nc2(oc + ((o + pz) & pwm));
+            uint2 h0 = ldg_nc2(oa + o);
+            uint2 ow = ldg_u2(mc + o);
+            uint2 qzp{0u, 0u}, qh0{0u, 0u}, qow{0u, 0u};
+            if constexpr (PF == 2) {
+                qzp = ldg_nc2(oc + ((o + 2 * pz) & pwm));
+                qh0 = ldg_nc2(oa + ((o + pz) & pwm));
+                qow = ldg_u2(mc + ((o + pz) & pwm));
+            }
+            // z pairs (2k, 2k+1) share one Philox block per word: counter
+            // (z>>1)*pz + word, lower 16-bit halves for even z, upper for odd z
+            for (uint32_t z = z0; z < z1; z += 2) {
+                U4 ua{}, ub{};
+                if (MODE != 2) {
+                    ua = philox_w(pre, P, (o >> 1) + col);
+                    ub = philox_w(pre, P, (o >> 1) + col + 1);
                 }
-            } else {
-                uint32_t qzp = ldg_nc(oc + ((o + 2 * pz) & pwm));
-                uint32_t qh0 = ldg_nc(oa + ((o + pz) & pwm));
-                uint32_t qh1 = single ? ldg_nc(ob + ((o + pz) & pwm)) : 0u;
-                uint32_t qow = ldg_u32(mc + ((o + pz) & pwm));
-                for (uint32_t z = z0; z < z1; z += 2) {
-                    U4 uc{};
-                    if (MODE != 2) uc = philox_w(pre, P, (o >> 1) + col);
-                    rolling_step2<MODE, false>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm,
-                                               single, first, last, src_up, src_dn, src_lo,
-                                               sel_lo, o, zm, za, zp, qzp, h0, qh0, h1, qh1, ow,
-                                               qow, macc);
-                    rolling_step2<MODE, true>(P, pre, tbase, uc, oc, oa, ob, mc, col, pz, pwm,
-                                              single, first, last, src_up, src_dn, src_hi,
-                                              sel_hi, o, zm, za, zp, qzp, h0, qh0, h1, qh1, ow,
-                                              qow, macc);
-                }
+                rolling_pair_step<MODE, false, PF>(P, pre, tbase, ua, ub, oc, oa, mc, col, pz,
+                                                   pwm, first, last, src_up, src_dn, src_lo, pe,
+                                                   sel_lo, o, zm, za, zp, qzp, h0, qh0, ow, qow,
+                                                   macc);
+                rolling_pair_step<MODE, true, PF>(P, pre, tbase, ua, ub, oc, oa, mc, col, pz,
+                                                  pwm, first, last, src_up, src_dn, src_hi, !pe,
+                                                  sel_hi, o, zm, za, zp, qzp, h0, qh0, ow, qow,
+                                                  macc);
             }
         } else {
             // flat: warp task 8*lct + wib of this size
@@ -1420,8 +1414,9 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         C.task_end = task;
         C.log2_groups = 0;
         if (C.kind == kRolling) {
-            // columns of 32/(L/8) rows: L*L/256 per z-plane, in groups of 8
-            const int cols = (L / (32 / rw));
+            // warp tasks of 64 words = 64/(L/8) rows: L*L/512 per z-plane, in
+            // groups of 8
+            const int cols = (L / (64 / rw));
             int groups = cols / 8;
             while ((1 << C.log2_groups) < groups) ++C.log2_groups;
             C.ctask_base = ctask;

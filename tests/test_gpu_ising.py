@@ -183,6 +183,25 @@ def test_production_size_properties(gpu, oracle):
         assert np.array_equal(d.get_spins(0, r), sp)
 
 
+@pytest.mark.parametrize("depth", [1, 2])
+def test_rolling_sizes_match_replay(gpu, oracle, depth):
+    """Every rolling size (L = 64: 8-row tasks; L = 256: 2-row tasks, the
+    first/last halo rows of every lane pair) against the replay, bit for bit,
+    at both prefetch depths."""
+    for L in (64, 256):
+        d = gpu.IsingBatch([L], 1, seed=5)
+        d.set_prefetch(depth)
+        d.set_temperatures([4.51])
+        d.step(2)
+        sp = oracle.hot_start(L, 3, 5, 0)
+        thr = oracle.thresholds(3, 1.0 / 4.51)
+        for k in range(2):
+            for colour in (0, 1):
+                oracle.halfsweep(sp, L, 3, colour, 5, 0, k, thr)
+        assert np.array_equal(d.get_spins(0, 0), sp), L
+        d.close()
+
+
 def test_prefetch_depth_keeps_results(gpu):
     """Both rolling prefetch depths give the same bits (L = 64 and 128 are rolling)."""
     sizes, R = [64, 128], 2

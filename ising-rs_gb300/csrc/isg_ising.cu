@@ -60,12 +60,14 @@ constexpr int kMaxClasses = 16;
 constexpr int kMaxThreads = 512;
 constexpr int kMaxReplicas = 1024;
 
-// Task kinds of a lattice size (one warp task = 32 words = 128 sites of one
-// colour plane of one replica):
-//   kRolling (dim 3, L = 64, 128, 256): a task is the nr = 32/(L/8) rows of
-//     one y-block at one z; consecutive tasks of a size walk z, so a warp
-//     keeps the z-1, z, z+1 words of the other colour in registers.
-//   kFlat    (other power-of-two L with L/8 dividing 32): 32 consecutive words.
+// Task kinds of a lattice size (words of 4 same-colour sites of one colour
+// plane of one replica):
+//   kRolling (dim 3, L = 64, 128, 256): a warp task is the nr = 64/(L/8) rows
+//     of one y-block at one z, two adjacent words per lane; consecutive tasks
+//     of a size walk z, so a warp keeps the z-1, z, z+1 words of the other
+//     colour in registers.
+//   kFlat    (other power-of-two L with L/8 dividing 32): 32 consecutive words,
+//     one per lane.
 //   kSite    (any other even L): one thread per site (site kernel).
 enum { kSite = 0, kFlat = 1, kRolling = 2 };
 
@@ -364,8 +366,8 @@ __device__ __forceinline__ void rolling_pair_step(
 // rolling sizes the 8 warps of a CTA walk 8 adjacent y-block columns through
 // the same z range, so the halo rows a warp needs are the edge rows its
 // neighbours load at the same time (L1 hits); consecutive CTA tasks walk z, so
-// the z-1/z/z+1 words of the other colour stay in registers.  Flat sizes give
-// each warp one 32-word task per CTA task.
+// the z-1/z/z+1 words of the other colour stay in registers (64 words per warp
+// task).  Flat sizes give each warp one 32-word task per CTA task.
 // PF: rolling loads issued PF planes ahead (1: 3 blocks per SM, 2: 2 blocks
 // per SM with more loads in flight per warp); chosen per batch (configure_launch,
 // isg_ising_autotune).

@@ -398,6 +398,143 @@ __global__ void __launch_bounds__(kCThreads) k_cont_or_col(const __grid_constant
     }
 }
 
+// Overrelaxation on column tasks of two adjacent sites (colour indices k, k+1
+// of one row; every size a multiple of 4, so rows hold an even number of
+// colour sites): pair task t is column task 2t.  Own, y+, y-, z+ words are
+// 64-bit loads of the pair; of the x neighbours, one per site is the other
+// site's same-index word (zc) and one scalar load per pair brings the outer
+// one.  Each site's arithmetic is k_cont_or_col's, in the same order; a site
+// whose field vanishes is written back unchanged.
+template <int NC>
+__global__ void __launch_bounds__(kCThreads) k_cont_or_col2(const __grid_constant__ ContParams P,
+                                                            int colour) {
+    ColRef c;
+    if (!col_locate(P, 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x), c)) return;
+    const ContClass& C = P.cls[c.ci];
+    const uint32_t L = (uint32_t)C.L, half = L >> 1, plane = C.plane_sites;
+    float* own = P.spins + plane_off<NC>(C, c.r, colour, 0);
+    const float* oth = P.spins + plane_off<NC>(C, c.r, colour ^ 1, 0);
+    const uint32_t row = c.y * half;
+    const uint32_t xo1 = row + (c.k + 2 == half ? 0 : c.k + 2);  // x+ of site k+1 (p = 1)
+    const uint32_t xo0 = row + (c.k == 0 ? half - 1 : c.k - 1);  // x- of site k (p = 0)
+    const uint32_t colp = (c.y + 1 == L ? 0 : c.y + 1) * half + c.k;
+    const uint32_t colm = (c.y == 0 ? L - 1 : c.y - 1) * half + c.k;
+    float2 zm[NC], zc[NC];
+    const uint32_t zmb = (c.z0 == 0 ? L - 1 : c.z0 - 1) * c.Pz;
+    float lx[NC];
+    float2 lyp[NC], lym[NC], lzp[NC], lv[NC];
+    auto ld2 = [](const float* q) { return __ldg(reinterpret_cast<const float2*>(q)); };
+    auto load_step = [&](uint32_t z) {
+        const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
+        const uint32_t zb = z * c.Pz, zpb = (z + 1 == L ? 0 : z + 1) * c.Pz;
+        const uint32_t xo = p ? xo1 : xo0;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            const float* o = oth + (size_t)k * plane;
+            lx[k] = __ldg(o + zb + xo);
+            lyp[k] = ld2(o + zb + colp);
+            lym[k] = ld2(o + zb + colm);
+            lzp[k] = ld2(o + zpb + c.col);
+            lv[k] = *reinterpret_cast<const float2*>(own + (size_t)k * plane + zb + c.col);
+        }
+    };
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        zm[k] = ld2(oth + (size_t)k * plane + zmb + c.col);
+        zc[k] = ld2(oth + (size_t)k * plane + c.z0 * c.Pz + c.col);
+    }
+    load_step(c.z0);
+    for (uint32_t z = c.z0; z < c.z1; ++z) {
+        const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
+        const uint32_t zb = z * c.Pz;
+        float xn[NC];
+        float2 yp[NC], ym[NC], zp[NC], v[NC];
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            xn[k] = lx[k];
+            yp[k] = lyp[k];
+            ym[k] = lym[k];
+            zp[k] = lzp[k];
+            v[k] = lv[k];
+        }
+        if (z + 1 < c.z1) load_step(z + 1);
+        float ha[NC], hb[NC], h2a = 0.f, sha = 0.f, h2b = 0.f, shb = 0.f;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            // site k: x neighbours (zc.y, zc.x) for p = 1, (zc.x, xn) for p = 0
+            const float xpa = p ? zc[k].y : zc[k].x, xma = p ? zc[k].x : xn[k];
+            // site k+1: (xn, zc.y) for p = 1, (zc.y, zc.x) for p = 0
+            const float xpb = p ? xn[k] : zc[k].y, xmb = p ? zc[k].y : zc[k].x;
+            ha[k] = ((xpa + xma) + (yp[k].x + ym[k].x)) + (zp[k].x + zm[k].x);
+            hb[k] = ((xpb + xmb) + (yp[k].y + ym[k].y)) + (zp[k].y + zm[k].y);
+            h2a = fmaf(ha[k], ha[k], h2a);
+            sha = fmaf(v[k].x, ha[k], sha);
+            h2b = fmaf(hb[k], hb[k], h2b);
+            shb = fmaf(v[k].y, hb[k], shb);
+        }
+        const bool ua = h2a >= 1e-20f, ub = h2b >= 1e-20f;
+        if (ua || ub) {
+            const float sca = ua ? 2.0f * sha / h2a : 0.f, scb = ub ? 2.0f * shb / h2b : 0.f;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                float2 w;
+                w.x = ua ? fmaf(sca, ha[k], -v[k].x) : v[k].x;
+                w.y = ub ? fmaf(scb, hb[k], -v[k].y) : v[k].y;
+                *reinterpret_cast<float2*>(own + (size_t)k * plane + zb + c.col) = w;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            zm[k] = zc[k];
+            zc[k] = zp[k];
+        }
+    }
+}
+
+// The Metropolis move of one site (k_cont_metro_col and its two-site form):
+// the cone proposal w of spin v from Philox block u (O(3): polar angle with
+// cos uniform in [cos delta, 1], azimuth uniform, about v; O(2): rotation by
+// an angle uniform in [-delta, delta]), and the test against field h.
+template <int NC>
+__device__ __forceinline__ bool cone_test(const float (&v)[NC], const float (&h)[NC], const U4& u,
+                                          float cos_delta, float delta, float beta, float J,
+                                          float (&w)[NC]) {
+    if constexpr (NC == 3) {
+        const float ct = 1.0f - uniform24(u.x) * (1.0f - cos_delta);
+        const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+        float sp, cp;
+        sincospif(2.0f * uniform24(u.y), &sp, &cp);
+        const float tx = fabsf(v[0]) < 0.9f ? 1.0f : 0.0f;
+        const float ty = 1.0f - tx;
+        const float ts = tx * v[0] + ty * v[1];
+        float ux = tx - ts * v[0], uy = ty - ts * v[1], uz = -ts * v[2];
+        const float un = rsqrtf(ux * ux + uy * uy + uz * uz);
+        ux *= un;
+        uy *= un;
+        uz *= un;
+        const float vx = v[1] * uz - v[2] * uy;
+        const float vy = v[2] * ux - v[0] * uz;
+        const float vz = v[0] * uy - v[1] * ux;
+        const float a = st * cp, b = st * sp;
+        w[0] = a * ux + b * vx + ct * v[0];
+        w[1] = a * uy + b * vy + ct * v[1];
+        w[2] = a * uz + b * vz + ct * v[2];
+        const float wn = rsqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) w[k] *= wn;
+    } else {
+        float sd, cd;
+        sincospif(delta * 0.318309886183790672f * (2.0f * uniform24(u.x) - 1.0f), &sd, &cd);
+        w[0] = v[0] * cd - v[1] * sd;
+        w[1] = v[1] * cd + v[0] * sd;
+    }
+    float dot = 0.f;
+#pragma unroll
+    for (int k = 0; k < NC; ++k) dot = fmaf(w[k] - v[k], h[k], dot);
+    const float dE = -J * dot;
+    return dE <= 0.0f || uniform24(u.z) < expf(-beta * dE);
+}
+
 // Metropolis with the cone proposal on column tasks (same update, random
 // stream and renormalisation as k_cont_metro: Philox counter = colour index).
 template <int NC>
@@ -466,41 +603,7 @@ __global__ void __launch_bounds__(kCThreads, 3)
             }
             if (z + 1 < c.z1) load_step(z + 1);
             const U4 u = philox10(uid, i, c2, c3, k0, k1);
-            if (NC == 3) {
-                const float ct = 1.0f - uniform24(u.x) * (1.0f - cos_delta);
-                const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
-                float sp, cp;
-                sincospif(2.0f * uniform24(u.y), &sp, &cp);
-                const float tx = fabsf(v[0]) < 0.9f ? 1.0f : 0.0f;
-                const float ty = 1.0f - tx;
-                const float ts = tx * v[0] + ty * v[1];
-                float ux = tx - ts * v[0], uy = ty - ts * v[1], uz = -ts * v[2];
-                const float un = rsqrtf(ux * ux + uy * uy + uz * uz);
-                ux *= un;
-                uy *= un;
-                uz *= un;
-                const float vx = v[1] * uz - v[2] * uy;
-                const float vy = v[2] * ux - v[0] * uz;
-                const float vz = v[0] * uy - v[1] * ux;
-                const float a = st * cp, b = st * sp;
-                w[0] = a * ux + b * vx + ct * v[0];
-                w[1] = a * uy + b * vy + ct * v[1];
-                w[2] = a * uz + b * vz + ct * v[2];
-                const float wn = rsqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-#pragma unroll
-                for (int k = 0; k < 3; ++k) w[k] *= wn;
-            } else {
-                float sd, cd;
-                sincospif(delta * 0.318309886183790672f * (2.0f * uniform24(u.x) - 1.0f), &sd,
-                          &cd);
-                w[0] = v[0] * cd - v[1] * sd;
-                w[1] = v[1] * cd + v[0] * sd;
-            }
-            float dot = 0.f;
-#pragma unroll
-            for (int k = 0; k < NC; ++k) dot = fmaf(w[k] - v[k], h[k], dot);
-            const float dE = -P.J * dot;
-            const bool accepted = dE <= 0.0f || uniform24(u.z) < expf(-beta * dE);
+            const bool accepted = cone_test<NC>(v, h, u, cos_delta, delta, beta, P.J, w);
             n_acc += accepted ? 1u : 0u;
             if (accepted || renorm_now) {
                 float n2 = 0.f;
@@ -522,6 +625,120 @@ __global__ void __launch_bounds__(kCThreads, 3)
     }
     // per-replica acceptance count: a warp covers one replica (32 | colour
     // sites per z-plane), so one atomic per warp
+    const int rg0 = __shfl_sync(ISG_FULL_MASK, rg, 0);
+    const unsigned cnt = __reduce_add_sync(ISG_FULL_MASK, n_acc);
+    if (__all_sync(ISG_FULL_MASK, rg == rg0 || rg < 0)) {
+        if (lane == 0 && rg0 >= 0 && cnt) atomicAdd(&P.metro_acc[rg0], (unsigned long long)cnt);
+    } else if (rg >= 0 && n_acc) {
+        atomicAdd(&P.metro_acc[rg], (unsigned long long)n_acc);
+    }
+}
+
+// Metropolis on column tasks of two adjacent sites (the pair layout of
+// k_cont_or_col2): each site draws from its own Philox counter (its colour
+// index) and goes through cone_test exactly as in k_cont_metro_col; a site
+// neither accepted nor renormalised is written back unchanged.
+template <int NC>
+__global__ void __launch_bounds__(kCThreads, 2)
+    k_cont_metro_col2(const __grid_constant__ ContParams P, int colour, int sweep_off,
+                      float cos_delta, float delta) {
+    const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
+    const bool renorm_now = P.renorm > 0 && ((sweep + 1) % (uint64_t)P.renorm) == 0;
+    const uint32_t c2 = (uint32_t)sweep;
+    const uint32_t c3 = counter_word3(ISG_TAG_CMETRO, (uint32_t)colour, sweep);
+    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    const int lane = threadIdx.x & 31;
+    ColRef c;
+    const bool live = col_locate(P, 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x), c);
+    unsigned n_acc = 0;
+    int rg = -1;
+    if (live) {
+        const ContClass& C = P.cls[c.ci];
+        rg = c.rg;
+        const uint32_t L = (uint32_t)C.L, half = L >> 1, plane = C.plane_sites;
+        float* own = P.spins + plane_off<NC>(C, c.r, colour, 0);
+        const float* oth = P.spins + plane_off<NC>(C, c.r, colour ^ 1, 0);
+        const uint32_t row = c.y * half;
+        const uint32_t xo1 = row + (c.k + 2 == half ? 0 : c.k + 2);  // x+ of site k+1 (p = 1)
+        const uint32_t xo0 = row + (c.k == 0 ? half - 1 : c.k - 1);  // x- of site k (p = 0)
+        const uint32_t colp = (c.y + 1 == L ? 0 : c.y + 1) * half + c.k;
+        const uint32_t colm = (c.y == 0 ? L - 1 : c.y - 1) * half + c.k;
+        const uint32_t uid = replica_uid(C.L, c.r);
+        const float beta = P.betaf[C.rep_base + P.r2t[c.rg]];
+        float2 zm[NC], zc[NC];
+        const uint32_t zmb = (c.z0 == 0 ? L - 1 : c.z0 - 1) * c.Pz;
+        float lx[NC];
+        float2 lyp[NC], lym[NC], lzp[NC], lv[NC];
+        auto ld2 = [](const float* q) { return __ldg(reinterpret_cast<const float2*>(q)); };
+        auto load_step = [&](uint32_t z) {
+            const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
+            const uint32_t zb = z * c.Pz, zpb = (z + 1 == L ? 0 : z + 1) * c.Pz;
+            const uint32_t xo = p ? xo1 : xo0;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                const float* o = oth + (size_t)k * plane;
+                lx[k] = __ldg(o + zb + xo);
+                lyp[k] = ld2(o + zb + colp);
+                lym[k] = ld2(o + zb + colm);
+                lzp[k] = ld2(o + zpb + c.col);
+                lv[k] = *reinterpret_cast<const float2*>(own + (size_t)k * plane + zb + c.col);
+            }
+        };
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            zm[k] = ld2(oth + (size_t)k * plane + zmb + c.col);
+            zc[k] = ld2(oth + (size_t)k * plane + c.z0 * c.Pz + c.col);
+        }
+        load_step(c.z0);
+        for (uint32_t z = c.z0; z < c.z1; ++z) {
+            const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
+            const uint32_t i = z * c.Pz + c.col;  // site k; site k+1 is i + 1
+            float ha[NC], hb[NC], va[NC], vb[NC], wa[NC], wb[NC];
+            float2 zp[NC];
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                const float xn = lx[k];
+                const float xpa = p ? zc[k].y : zc[k].x, xma = p ? zc[k].x : xn;
+                const float xpb = p ? xn : zc[k].y, xmb = p ? zc[k].y : zc[k].x;
+                zp[k] = lzp[k];
+                ha[k] = ((xpa + xma) + (lyp[k].x + lym[k].x)) + (zp[k].x + zm[k].x);
+                hb[k] = ((xpb + xmb) + (lyp[k].y + lym[k].y)) + (zp[k].y + zm[k].y);
+                va[k] = lv[k].x;
+                vb[k] = lv[k].y;
+            }
+            if (z + 1 < c.z1) load_step(z + 1);
+            const U4 u0 = philox10(uid, i, c2, c3, k0, k1);
+            const U4 u1 = philox10(uid, i + 1, c2, c3, k0, k1);
+            const bool acc_a = cone_test<NC>(va, ha, u0, cos_delta, delta, beta, P.J, wa);
+            const bool acc_b = cone_test<NC>(vb, hb, u1, cos_delta, delta, beta, P.J, wb);
+            n_acc += (acc_a ? 1u : 0u) + (acc_b ? 1u : 0u);
+            const bool wr_a = acc_a || renorm_now, wr_b = acc_b || renorm_now;
+            if (wr_a || wr_b) {
+                float n2a = 0.f, n2b = 0.f;
+#pragma unroll
+                for (int k = 0; k < NC; ++k) {
+                    if (acc_a) va[k] = wa[k];
+                    if (acc_b) vb[k] = wb[k];
+                    n2a = fmaf(va[k], va[k], n2a);
+                    n2b = fmaf(vb[k], vb[k], n2b);
+                }
+                const float sca = renorm_now ? rsqrtf(n2a) : 1.0f;
+                const float scb = renorm_now ? rsqrtf(n2b) : 1.0f;
+#pragma unroll
+                for (int k = 0; k < NC; ++k) {
+                    float2 o2;
+                    o2.x = wr_a ? va[k] * sca : va[k];
+                    o2.y = wr_b ? vb[k] * scb : vb[k];
+                    *reinterpret_cast<float2*>(own + (size_t)k * plane + i) = o2;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                zm[k] = zc[k];
+                zc[k] = zp[k];
+            }
+        }
+    }
     const int rg0 = __shfl_sync(ISG_FULL_MASK, rg, 0);
     const unsigned cnt = __reduce_add_sync(ISG_FULL_MASK, n_acc);
     if (__all_sync(ISG_FULL_MASK, rg == rg0 || rg < 0)) {
@@ -828,6 +1045,7 @@ struct isg_cont {
     double J = 1.0;
     int sms = 1;
     int grid = 1;
+    bool pairs = false;  // every size a multiple of 4: two-site column kernels
     uint64_t ksample = 0, records_made = 0, records_done = 0;
     cudaGraphExec_t graph = nullptr;
     int g_ee = 0, g_me = 0, g_period = 0, g_nor = -1, g_renorm = -1;
@@ -843,6 +1061,15 @@ static void cont_destroy_graph(isg_cont* H) {
 }
 
 static void launch_or(isg_cont* H, int colour) {
+    if (H->pairs) {
+        const int64_t n = H->P.total_cols / 2;
+        const unsigned g2 = (unsigned)((n + kCThreads - 1) / kCThreads);
+        if (H->nc == 3)
+            k_cont_or_col2<3><<<g2, kCThreads, 0, H->stream>>>(H->P, colour);
+        else
+            k_cont_or_col2<2><<<g2, kCThreads, 0, H->stream>>>(H->P, colour);
+        return;
+    }
     const unsigned grid = (unsigned)((H->P.total_cols + kCThreads - 1) / kCThreads);
     if (H->nc == 3)
         k_cont_or_col<3><<<grid, kCThreads, 0, H->stream>>>(H->P, colour);
@@ -852,6 +1079,17 @@ static void launch_or(isg_cont* H, int colour) {
 
 static void launch_metro(isg_cont* H, int colour, int sweep_off, double delta) {
     const float cd = (float)std::cos(std::min(delta, M_PI));
+    if (H->pairs) {
+        const int64_t n = H->P.total_cols / 2;
+        const unsigned g2 = (unsigned)((n + kCThreads - 1) / kCThreads);
+        if (H->nc == 3)
+            k_cont_metro_col2<3><<<g2, kCThreads, 0, H->stream>>>(H->P, colour, sweep_off, cd,
+                                                                  (float)delta);
+        else
+            k_cont_metro_col2<2><<<g2, kCThreads, 0, H->stream>>>(H->P, colour, sweep_off, cd,
+                                                                  (float)delta);
+        return;
+    }
     const unsigned grid = (unsigned)((H->P.total_cols + kCThreads - 1) / kCThreads);
     if (H->nc == 3)
         k_cont_metro_col<3><<<grid, kCThreads, 0, H->stream>>>(H->P, colour, sweep_off, cd,
@@ -967,9 +1205,11 @@ int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas,
     int64_t off = 0, site = 0;
     int chunk = 0;
     P.total_cols = 0;
+    H->pairs = true;
     for (int s = 0; s < n_sizes; ++s) {
         ContClass& C = P.cls[s];
         const int L = sizes[s];
+        if (L % 4 != 0) H->pairs = false;
         C.L = L;
         C.R = replicas;
         C.plane_sites = (uint32_t)((int64_t)L * L * L / 2);

@@ -32,9 +32,12 @@ def test_hot_start_matches_oracle(gpu, oracle, nc):
             assert np.max(np.abs(g - o)) < 2e-6
 
 
+@pytest.mark.parametrize("sizes", [[4, 6, 8, 10, 16], [4, 8, 12, 16]])
 @pytest.mark.parametrize("nc", [3, 2])
-def test_halfsweeps_match_oracle(gpu, oracle, nc):
-    sizes, R, seed, J = [4, 6, 8, 10, 16], 2, 5, 1.0
+def test_halfsweeps_match_oracle(gpu, oracle, nc, sizes):
+    """Sizes all multiples of 4 run the two-site column kernels; a size that
+    is not runs the one-site kernels."""
+    R, seed, J = 2, 5, 1.0
     temps = [1.2, 2.0] if nc == 3 else [1.8, 2.5]
     delta = 0.7 if nc == 3 else 1.3
     b = gpu.ContinuousBatch(sizes, R, nc, seed=seed)
@@ -64,6 +67,30 @@ def test_halfsweeps_match_oracle(gpu, oracle, nc):
             assert abs(e[k] - q[0]) < tol
             assert np.all(np.abs(m[k, :nc] - q[1:1 + nc]) < tol)
             assert np.all(np.abs(hb[k] - q[4:10]) < tol)
+
+
+@pytest.mark.parametrize("nc", [3, 2])
+def test_two_site_kernels_match_one_site(gpu, nc):
+    """Random streams are keyed per (L, replica), so L = 8 and 16 evolve the
+    same in a batch of multiples of 4 (two-site overrelaxation and Metropolis
+    kernels) and in one with an L = 6 added last (one-site kernels): bit for
+    bit, through sweeps, exchanges and renormalisation."""
+    R, temps = 2, ([1.3, 1.6] if nc == 3 else [1.9, 2.4])
+    out = []
+    for sizes in ([8, 16], [8, 16, 6]):
+        b = gpu.ContinuousBatch(sizes, R, nc, seed=31)
+        b.set_temperatures(temps)
+        for _ in range(3):
+            b.overrelax(0)
+            b.overrelax(1)
+            b.metropolis(0, 0.6)
+            b.metropolis(1, 0.6)
+        # exchange and renormalisation (every 2 sweeps) through the PT loop
+        b.pt_run(6, 3, 3, delta=0.6, n_overrelax=1, renorm_every=2)
+        out.append([b.get_spins(si, r) for si in range(2) for r in range(R)])
+        b.close()
+    for x, y in zip(out[0], out[1]):
+        assert np.array_equal(x, y)
 
 
 @pytest.mark.parametrize("nc", [3, 2])

@@ -764,6 +764,51 @@ __device__ __forceinline__ CF cf_merge(CF a, CF b) {
     return r;
 }
 
+// The six bonds of one colour-1 site s with neighbours n (x+, x-, y+, y-,
+// z+, z-) into the compensated sums: per axis a the forward bond (i, i+a) and
+// the backward bond (i-a, i), C_a += S.S, S_a += (S x S')_z, E += -J S.S.
+template <int NC>
+__device__ __forceinline__ void meas_bonds(CF (&acc)[kNQ], const float (&s)[NC],
+                                           const float (&n)[6][NC], float J) {
+    float e = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float cf = 0.f, cb = 0.f;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            cf = fmaf(s[c], n[2 * a][c], cf);
+            cb = fmaf(s[c], n[2 * a + 1][c], cb);
+        }
+        const float sf = s[0] * n[2 * a][1] - s[1] * n[2 * a][0];
+        const float sb = n[2 * a + 1][0] * s[1] - n[2 * a + 1][1] * s[0];
+        e += cf + cb;
+        acc[4 + a] = cf_add(acc[4 + a], cf + cb);
+        acc[7 + a] = cf_add(acc[7 + a], sf + sb);
+    }
+    acc[0] = cf_add(acc[0], -J * e);
+}
+
+// Block reduction of the compensated sums into one FP64 partial per quantity.
+__device__ __forceinline__ void meas_block_store(const ContParams& P, CF (&acc)[kNQ], int chunk) {
+    __shared__ CF red[kCThreads / 32][kNQ];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < kNQ; ++q) {
+        CF v = acc[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            CF w{__shfl_down_sync(ISG_FULL_MASK, v.s, o), __shfl_down_sync(ISG_FULL_MASK, v.c, o)};
+            v = cf_merge(v, w);
+        }
+        if (lane == 0) red[wid][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNQ) {
+        CF v = red[0][threadIdx.x];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = cf_merge(v, red[w][threadIdx.x]);
+        P.partials[(int64_t)chunk * kNQ + threadIdx.x] = (double)v.s + (double)v.c;
+    }
+}
+
 // Per block: kCThreads column tasks of one replica (chunks_per_rep blocks per
 // replica), each walking up to kColZ z-planes of colour-1 sites.  Each
 // colour-1 site owns its six bonds (every bond has exactly one colour-1 end)
@@ -819,23 +864,7 @@ __global__ void __launch_bounds__(kCThreads) k_cont_measure(const __grid_constan
                 n[5][c] = zm[c];
                 acc[1 + c] = cf_add(acc[1 + c], s[c] + zc[c]);
             }
-            float e = 0.f;
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                // forward bond (i, i+a) is neighbour 2a, backward bond (i-a, i) is 2a+1
-                float cf = 0.f, cb = 0.f;
-#pragma unroll
-                for (int c = 0; c < NC; ++c) {
-                    cf = fmaf(s[c], n[2 * a][c], cf);
-                    cb = fmaf(s[c], n[2 * a + 1][c], cb);
-                }
-                const float sf = s[0] * n[2 * a][1] - s[1] * n[2 * a][0];
-                const float sb = n[2 * a + 1][0] * s[1] - n[2 * a + 1][1] * s[0];
-                e += cf + cb;
-                acc[4 + a] = cf_add(acc[4 + a], cf + cb);
-                acc[7 + a] = cf_add(acc[7 + a], sf + sb);
-            }
-            acc[0] = cf_add(acc[0], -P.J * e);
+            meas_bonds<NC>(acc, s, n, P.J);
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
                 zm[c] = zc[c];
@@ -843,24 +872,87 @@ __global__ void __launch_bounds__(kCThreads) k_cont_measure(const __grid_constan
             }
         }
     }
-    // warp then block reduction of the compensated pairs
-    __shared__ CF red[kCThreads / 32][kNQ];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    meas_block_store(P, acc, chunk);
+}
+
+// The same measurement with two adjacent colour-1 sites (k, k+1 of a row)
+// per thread, for batches whose sizes are all multiples of 4: 64-bit loads,
+// and the block reduction spread over twice the sites.  Per z the thread adds
+// site k's terms, then site k+1's.
+template <int NC>
+__global__ void __launch_bounds__(kCThreads) k_cont_measure2(const __grid_constant__ ContParams P) {
+    const int chunk = blockIdx.x;
+    int ci = 0;
+    while (ci + 1 < P.n_classes && P.cls[ci + 1].chunk_base <= chunk) ++ci;
+    const ContClass& C = P.cls[ci];
+    const int lc = chunk - C.chunk_base;
+    const int r = lc / C.chunks_per_rep;
+    const uint32_t L = (uint32_t)C.L, half = L >> 1, Pz = L * half, plane = C.plane_sites;
+    const uint32_t u = (uint32_t)(lc - r * C.chunks_per_rep) * kCThreads + threadIdx.x;
+    CF acc[kNQ];
 #pragma unroll
-    for (int q = 0; q < kNQ; ++q) {
-        CF v = acc[q];
-        for (int o = 16; o > 0; o >>= 1) {
-            CF w{__shfl_down_sync(ISG_FULL_MASK, v.s, o), __shfl_down_sync(ISG_FULL_MASK, v.c, o)};
-            v = cf_merge(v, w);
+    for (int q = 0; q < kNQ; ++q) acc[q] = CF{0.f, 0.f};
+    if (u < (uint32_t)C.nseg * (Pz / 2)) {
+        const uint32_t zseg = u / (Pz / 2), col = 2 * (u - zseg * (Pz / 2));
+        const uint32_t y = fdiv(col, C.div_half), k = col - y * half;
+        const uint32_t z0 = zseg * kColZ, z1 = min(L, z0 + (uint32_t)kColZ);
+        const float* own = P.spins + plane_off<NC>(C, r, 1, 0);
+        const float* oth = P.spins + plane_off<NC>(C, r, 0, 0);
+        const uint32_t row = y * half;
+        const uint32_t xo1 = row + (k + 2 == half ? 0 : k + 2);  // x+ of site k+1 (p = 1)
+        const uint32_t xo0 = row + (k == 0 ? half - 1 : k - 1);  // x- of site k (p = 0)
+        const uint32_t colp = (y + 1 == L ? 0 : y + 1) * half + k;
+        const uint32_t colm = (y == 0 ? L - 1 : y - 1) * half + k;
+        auto ld2 = [](const float* q) { return __ldg(reinterpret_cast<const float2*>(q)); };
+        float2 zm[NC], zc[NC];
+        const uint32_t zmb = (z0 == 0 ? L - 1 : z0 - 1) * Pz;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            zm[c] = ld2(oth + (size_t)c * plane + zmb + col);
+            zc[c] = ld2(oth + (size_t)c * plane + z0 * Pz + col);
         }
-        if (lane == 0) red[wid][q] = v;
+        for (uint32_t z = z0; z < z1; ++z) {
+            const uint32_t p = (y + z + 1u) & 1u;
+            const uint32_t zb = z * Pz, zpb = (z + 1 == L ? 0 : z + 1) * Pz;
+            const uint32_t xo = p ? xo1 : xo0;
+            float sa[NC], sb[NC], na[6][NC], nb[6][NC];
+            float2 zp[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const float* o = oth + (size_t)c * plane;
+                const float xn = __ldg(o + zb + xo);
+                const float2 yp = ld2(o + zb + colp), ym = ld2(o + zb + colm);
+                zp[c] = ld2(o + zpb + col);
+                const float2 sv = ld2(own + (size_t)c * plane + zb + col);
+                sa[c] = sv.x;
+                sb[c] = sv.y;
+                na[0][c] = p ? zc[c].y : zc[c].x;
+                na[1][c] = p ? zc[c].x : xn;
+                nb[0][c] = p ? xn : zc[c].y;
+                nb[1][c] = p ? zc[c].y : zc[c].x;
+                na[2][c] = yp.x;
+                nb[2][c] = yp.y;
+                na[3][c] = ym.x;
+                nb[3][c] = ym.y;
+                na[4][c] = zp[c].x;
+                nb[4][c] = zp[c].y;
+                na[5][c] = zm[c].x;
+                nb[5][c] = zm[c].y;
+            }
+#pragma unroll
+            for (int c = 0; c < NC; ++c) acc[1 + c] = cf_add(acc[1 + c], sa[c] + zc[c].x);
+            meas_bonds<NC>(acc, sa, na, P.J);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) acc[1 + c] = cf_add(acc[1 + c], sb[c] + zc[c].y);
+            meas_bonds<NC>(acc, sb, nb, P.J);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                zm[c] = zc[c];
+                zc[c] = zp[c];
+            }
+        }
     }
-    __syncthreads();
-    if (threadIdx.x < kNQ) {
-        CF v = red[0][threadIdx.x];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = cf_merge(v, red[w][threadIdx.x]);
-        P.partials[(int64_t)chunk * kNQ + threadIdx.x] = (double)v.s + (double)v.c;
-    }
+    meas_block_store(P, acc, chunk);
 }
 
 // FP64 combine of the block partials of each replica, in chunk order.
@@ -1100,6 +1192,14 @@ static void launch_metro(isg_cont* H, int colour, int sweep_off, double delta) {
 }
 
 static void launch_measure(isg_cont* H) {
+    if (H->pairs) {
+        if (H->nc == 3)
+            k_cont_measure2<3><<<H->P.total_chunks, kCThreads, 0, H->stream>>>(H->P);
+        else
+            k_cont_measure2<2><<<H->P.total_chunks, kCThreads, 0, H->stream>>>(H->P);
+        k_cont_combine<<<(H->RT + 127) / 128, 128, 0, H->stream>>>(H->P, H->d_obs);
+        return;
+    }
     if (H->nc == 3)
         k_cont_measure<3><<<H->P.total_chunks, kCThreads, 0, H->stream>>>(H->P);
     else
@@ -1206,10 +1306,12 @@ int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas,
     int chunk = 0;
     P.total_cols = 0;
     H->pairs = true;
+    for (int s = 0; s < n_sizes; ++s)
+        if (sizes[s] % 4 != 0) H->pairs = false;
+    const int64_t per_task = H->pairs ? 2 : 1;  // column tasks per measurement thread
     for (int s = 0; s < n_sizes; ++s) {
         ContClass& C = P.cls[s];
         const int L = sizes[s];
-        if (L % 4 != 0) H->pairs = false;
         C.L = L;
         C.R = replicas;
         C.plane_sites = (uint32_t)((int64_t)L * L * L / 2);
@@ -1227,8 +1329,8 @@ int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas,
         C.site_base = site;
         site += (int64_t)C.plane_sites * replicas;
         C.site_end = site;
-        C.chunks_per_rep =
-            (int)(((int64_t)C.nseg * ((int64_t)L * L / 2) + kCThreads - 1) / kCThreads);
+        C.chunks_per_rep = (int)(((int64_t)C.nseg * ((int64_t)L * L / 2) / per_task + kCThreads - 1) /
+                                 kCThreads);
         C.chunk_base = chunk;
         chunk += C.chunks_per_rep * replicas;
     }

@@ -810,7 +810,8 @@ __device__ __forceinline__ void meas_block_store(const ContParams& P, CF (&acc)[
 }
 
 // Per block: kCThreads column tasks of one replica (chunks_per_rep blocks per
-// replica), each walking up to kColZ z-planes of colour-1 sites.  Each
+// replica; two-site tasks in k_cont_measure2), each walking up to kColZ
+// z-planes of colour-1 sites.  Each
 // colour-1 site owns its six bonds (every bond has exactly one colour-1 end)
 // and, for M, its colour-0 partner at the same colour index.  The summation
 // order is fixed by the task layout, so the result is deterministic.

@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(kCThreads) k_cont_or_col(const __grid_constant
 // one.  Each site's arithmetic is k_cont_or_col's, in the same order; a site
 // whose field vanishes is written back unchanged.
 template <int NC>
-__global__ void __launch_bounds__(kCThreads) k_cont_or_col2(const __grid_constant__ ContParams P,
+__global__ void __launch_bounds__(kCThreads, 3) k_cont_or_col2(const __grid_constant__ ContParams P,
                                                             int colour) {
     ColRef c;
     if (!col_locate(P, 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x), c)) return;
@@ -881,7 +881,7 @@ __global__ void __launch_bounds__(kCThreads) k_cont_measure(const __grid_constan
 // and the block reduction spread over twice the sites.  Per z the thread adds
 // site k's terms, then site k+1's.
 template <int NC>
-__global__ void __launch_bounds__(kCThreads) k_cont_measure2(const __grid_constant__ ContParams P) {
+__global__ void __launch_bounds__(kCThreads, 3) k_cont_measure2(const __grid_constant__ ContParams P) {
     const int chunk = blockIdx.x;
     int ci = 0;
     while (ci + 1 < P.n_classes && P.cls[ci + 1].chunk_base <= chunk) ++ci;

@@ -78,203 +78,10 @@ struct ContParams {
     ContClass cls[kCMaxClasses];
 };
 
-struct SiteRef {
-    int ci, r, rg;
-    uint32_t i, x, y, z;
-};
-
 template <int NC>
 __device__ __forceinline__ int64_t plane_off(const ContClass& C, int r, int colour, int comp) {
     return C.off + (int64_t)r * 2 * NC * C.plane_sites +
            (int64_t)(colour * NC + comp) * C.plane_sites;
-}
-
-__device__ __forceinline__ SiteRef locate(const ContParams& P, int64_t g, int colour) {
-    SiteRef s;
-    int ci = 0;
-    while (P.cls[ci].site_end <= g) ++ci;
-    const ContClass& C = P.cls[ci];
-    const int64_t lg = g - C.site_base;
-    s.ci = ci;
-    if (C.small) {
-        const uint32_t l32 = (uint32_t)lg;
-        s.r = (int)fdiv(l32, C.div_plane);
-        s.i = l32 - (uint32_t)s.r * C.plane_sites;
-    } else {
-        s.r = (int)(lg / C.plane_sites);
-        s.i = (uint32_t)(lg - (int64_t)s.r * C.plane_sites);
-    }
-    s.rg = C.rep_base + s.r;
-    const uint32_t row = fdiv(s.i, C.div_half);
-    const uint32_t k = s.i - row * (uint32_t)(C.L >> 1);
-    s.z = fdiv(row, C.div_L);
-    s.y = row - s.z * (uint32_t)C.L;
-    s.x = 2 * k + ((s.y + s.z + (uint32_t)colour) & 1u);
-    return s;
-}
-
-// Colour indices of the six neighbours of (x,y,z): +x, -x, +y, -y, +z, -z.
-__device__ __forceinline__ void neighbours(uint32_t L, uint32_t x, uint32_t y, uint32_t z,
-                                           uint32_t nb[6]) {
-    const uint32_t xp = x + 1 == L ? 0 : x + 1, xm = x == 0 ? L - 1 : x - 1;
-    const uint32_t yp = y + 1 == L ? 0 : y + 1, ym = y == 0 ? L - 1 : y - 1;
-    const uint32_t zp = z + 1 == L ? 0 : z + 1, zm = z == 0 ? L - 1 : z - 1;
-    const uint32_t row = (z * L + y) * L;
-    nb[0] = (row + xp) >> 1;
-    nb[1] = (row + xm) >> 1;
-    nb[2] = ((z * L + yp) * L + x) >> 1;
-    nb[3] = ((z * L + ym) * L + x) >> 1;
-    nb[4] = ((zp * L + y) * L + x) >> 1;
-    nb[5] = ((zm * L + y) * L + x) >> 1;
-}
-
-// Overrelaxation: S' = 2 (S.h)/|h|^2 h - S about the local field
-// (continuous_spin_kernel.cu:88-142; overrelax.rs:16-49 without the
-// per-update renormalisation).
-template <int NC>
-__device__ __forceinline__ void or_load(const ContParams& P, int64_t g, int colour, SiteRef& s,
-                                        float h[NC], float v[NC]) {
-    s = locate(P, g, colour);
-    const ContClass& C = P.cls[s.ci];
-    uint32_t nb[6];
-    neighbours((uint32_t)C.L, s.x, s.y, s.z, nb);
-#pragma unroll
-    for (int k = 0; k < NC; ++k) {
-        const float* o = P.spins + plane_off<NC>(C, s.r, colour ^ 1, k);
-        h[k] = ((__ldg(o + nb[0]) + __ldg(o + nb[1])) + (__ldg(o + nb[2]) + __ldg(o + nb[3]))) +
-               (__ldg(o + nb[4]) + __ldg(o + nb[5]));
-        v[k] = P.spins[plane_off<NC>(C, s.r, colour, k) + s.i];
-    }
-}
-
-template <int NC>
-__device__ __forceinline__ void or_store(const ContParams& P, int colour, const SiteRef& s,
-                                         const float h[NC], const float v[NC]) {
-    const ContClass& C = P.cls[s.ci];
-    float h2 = 0.f, sh = 0.f;
-#pragma unroll
-    for (int k = 0; k < NC; ++k) {
-        h2 = fmaf(h[k], h[k], h2);
-        sh = fmaf(v[k], h[k], sh);
-    }
-    if (h2 < 1e-20f) return;
-    const float scale = 2.0f * sh / h2;
-#pragma unroll
-    for (int k = 0; k < NC; ++k)
-        P.spins[plane_off<NC>(C, s.r, colour, k) + s.i] = fmaf(scale, h[k], -v[k]);
-}
-
-// Overrelaxation: S' = 2 (S.h)/|h|^2 h - S about the local field
-// (continuous_spin_kernel.cu:88-142; overrelax.rs:16-49 without the
-// per-update renormalisation).
-template <int NC>
-__global__ void __launch_bounds__(kCThreads) k_cont_or(const __grid_constant__ ContParams P,
-                                                       int colour) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < P.total_sites;
-         g += stride) {
-        SiteRef s0;
-        float h0[NC], v0[NC];
-        or_load<NC>(P, g, colour, s0, h0, v0);
-        or_store<NC>(P, colour, s0, h0, v0);
-    }
-}
-
-// Metropolis with the cone proposal; on renormalisation sweeps every site of
-// this colour is written back normalised.
-template <int NC>
-__global__ void __launch_bounds__(kCThreads)
-    k_cont_metro(const __grid_constant__ ContParams P, int colour, int sweep_off, float cos_delta,
-                 float delta) {
-    const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
-    const bool renorm_now = P.renorm > 0 && ((sweep + 1) % (uint64_t)P.renorm) == 0;
-    const uint32_t c2 = (uint32_t)sweep;
-    const uint32_t c3 = counter_word3(ISG_TAG_CMETRO, (uint32_t)colour, sweep);
-    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int lane = threadIdx.x & 31;
-    for (int64_t g0 = (int64_t)blockIdx.x * blockDim.x; g0 < P.total_sites; g0 += stride) {
-        const int64_t g = g0 + threadIdx.x;
-        bool accepted = false;
-        int rg = -1;
-        if (g < P.total_sites) {
-            const SiteRef s = locate(P, g, colour);
-            const ContClass& C = P.cls[s.ci];
-            rg = s.rg;
-            uint32_t nb[6];
-            neighbours((uint32_t)C.L, s.x, s.y, s.z, nb);
-            float h[NC], v[NC], w[NC];
-#pragma unroll
-            for (int k = 0; k < NC; ++k) {
-                const float* o = P.spins + plane_off<NC>(C, s.r, colour ^ 1, k);
-                h[k] = ((__ldg(o + nb[0]) + __ldg(o + nb[1])) +
-                        (__ldg(o + nb[2]) + __ldg(o + nb[3]))) +
-                       (__ldg(o + nb[4]) + __ldg(o + nb[5]));
-                v[k] = P.spins[plane_off<NC>(C, s.r, colour, k) + s.i];
-            }
-            const U4 u = philox10(replica_uid(C.L, s.r), s.i, c2, c3, k0, k1);
-            if (NC == 3) {
-                // cos(theta) uniform in [cos(delta), 1], phi uniform in [0, 2pi)
-                const float ct = 1.0f - uniform24(u.x) * (1.0f - cos_delta);
-                const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
-                float sp, cp;
-                sincospif(2.0f * uniform24(u.y), &sp, &cp);
-                // perpendicular frame (heisenberg/metropolis.rs:72-92)
-                const float tx = fabsf(v[0]) < 0.9f ? 1.0f : 0.0f;
-                const float ty = 1.0f - tx;
-                const float ts = tx * v[0] + ty * v[1];
-                float ux = tx - ts * v[0], uy = ty - ts * v[1], uz = -ts * v[2];
-                const float un = rsqrtf(ux * ux + uy * uy + uz * uz);
-                ux *= un;
-                uy *= un;
-                uz *= un;
-                const float vx = v[1] * uz - v[2] * uy;
-                const float vy = v[2] * ux - v[0] * uz;
-                const float vz = v[0] * uy - v[1] * ux;
-                const float a = st * cp, b = st * sp;
-                w[0] = a * ux + b * vx + ct * v[0];
-                w[1] = a * uy + b * vy + ct * v[1];
-                w[2] = a * uz + b * vz + ct * v[2];
-                const float wn = rsqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-#pragma unroll
-                for (int k = 0; k < 3; ++k) w[k] *= wn;
-            } else {
-                float sd, cd;
-                // rotation angle delta*(2u-1), as a multiple of pi
-                sincospif(delta * 0.318309886183790672f * (2.0f * uniform24(u.x) - 1.0f), &sd, &cd);
-                w[0] = v[0] * cd - v[1] * sd;
-                w[1] = v[1] * cd + v[0] * sd;
-            }
-            float dot = 0.f;
-#pragma unroll
-            for (int k = 0; k < NC; ++k) dot = fmaf(w[k] - v[k], h[k], dot);
-            const float dE = -P.J * dot;
-            const float beta = P.betaf[C.rep_base + P.r2t[s.rg]];
-            accepted = dE <= 0.0f || uniform24(u.z) < expf(-beta * dE);
-            if (accepted || renorm_now) {
-                float* out[NC];
-#pragma unroll
-                for (int k = 0; k < NC; ++k) out[k] = P.spins + plane_off<NC>(C, s.r, colour, k);
-                float n2 = 0.f;
-#pragma unroll
-                for (int k = 0; k < NC; ++k) {
-                    if (accepted) v[k] = w[k];
-                    n2 = fmaf(v[k], v[k], n2);
-                }
-                const float sc = renorm_now ? rsqrtf(n2) : 1.0f;
-#pragma unroll
-                for (int k = 0; k < NC; ++k) out[k][s.i] = v[k] * sc;
-            }
-        }
-        // per-replica acceptance count: one atomic per uniform warp
-        const int rg0 = __shfl_sync(ISG_FULL_MASK, rg, 0);
-        if (__all_sync(ISG_FULL_MASK, rg == rg0)) {
-            const unsigned cnt = __popc(__ballot_sync(ISG_FULL_MASK, accepted));
-            if (lane == 0 && rg0 >= 0 && cnt) atomicAdd(&P.metro_acc[rg0], (unsigned long long)cnt);
-        } else if (accepted) {
-            atomicAdd(&P.metro_acc[rg], 1ull);
-        }
-    }
 }
 
 // Position of a column task.
@@ -324,7 +131,9 @@ __device__ __forceinline__ void col_field(const float* oth, uint32_t plane, uint
     }
 }
 
-// Overrelaxation half-sweep on column tasks (same update as or_store).  The
+// Overrelaxation half-sweep on column tasks: S' = 2 (S.h)/|h|^2 h - S about the
+// local field (continuous_spin_kernel.cu:88-142; overrelax.rs:16-49 without the
+// per-update renormalisation), skipped where |h|^2 < 1e-20.  The
 // next z-step's loads are issued before the current step's arithmetic.
 template <int NC>
 __global__ void __launch_bounds__(kCThreads) k_cont_or_col(const __grid_constant__ ContParams P,
@@ -535,8 +344,10 @@ __device__ __forceinline__ bool cone_test(const float (&v)[NC], const float (&h)
     return dE <= 0.0f || uniform24(u.z) < expf(-beta * dE);
 }
 
-// Metropolis with the cone proposal on column tasks (same update, random
-// stream and renormalisation as k_cont_metro: Philox counter = colour index).
+// Metropolis with the cone proposal on column tasks (continuous_spin_kernel.cu:9-83
+// with the cone proposal of heisenberg/metropolis.rs:54-69): one Philox block per
+// site, counter = colour index; on renormalisation sweeps every site of this
+// colour is written back normalised.
 template <int NC>
 __global__ void __launch_bounds__(kCThreads, 3)
     k_cont_metro_col(const __grid_constant__ ContParams P, int colour, int sweep_off,

@@ -435,10 +435,13 @@ def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
     pt_s = time.perf_counter() - t0
     mid = R // 2
     series = np.array([abs(rm[i][rt[i] == mid][0]) / n for i in range(rt.shape[0])], float)
+    eseries = np.array([-float(rb[i][rt[i] == mid][0]) / n for i in range(rt.shape[0])], float)
     # the larger of the windowed and the blocking estimate, on both sides
     tau_pt_w, tau_pt_b = tau_int(series), tau_blocking(series)
     tau_pt = max(tau_pt_w, tau_pt_b)
     ess_pt = len(series) / (2 * tau_pt) / pt_s
+    tau_pt_e = max(tau_int(eseries), tau_blocking(eseries))
+    ess_pt_e = len(eseries) / (2 * tau_pt_e) / pt_s
     # training data from the plain sampler at T, with Z2 partners
     t1 = time.perf_counter()
     # streaming maximum-likelihood training: every step sees fresh
@@ -470,20 +473,30 @@ def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
     tau_l = max(tau_l_w, tau_l_b)
     ess_l = len(m) / (2 * tau_l) / ch_s
     m_err_l, m_err_pt = jackknife_mean_err(m), jackknife_mean_err(series)
+    e = ch.e_series()[ch.K:]
+    tau_l_e = max(tau_int(e), tau_blocking(e))
+    ess_l_e = len(e) / (2 * tau_l_e) / ch_s
+    e_err_l, e_err_pt = jackknife_mean_err(e), jackknife_mean_err(eseries)
     out = {"case": f"{dim}D L={L} T={T}", "plain_pt": {
         "replicas": R, "T_grid": [temps[0], temps[-1]], "sweeps": pt_sweeps,
         "seconds": pt_s, "sweeps_per_s": pt_sweeps / pt_s, "tau_int_sweeps": tau_pt,
         "tau_windowed": tau_pt_w, "tau_blocking": tau_pt_b,
-        "ess_per_s": ess_pt, "M": float(series.mean()), "M_err": m_err_pt},
+        "ess_per_s": ess_pt, "M": float(series.mean()), "M_err": m_err_pt,
+        "tau_E_sweeps": tau_pt_e, "ess_E_per_s": ess_pt_e, "E": float(eseries.mean()),
+        "E_err": e_err_pt},
         "learned": {"layers": 6, "channels": 32, "train_steps": steps, "train_s": train_s,
                     "nll_per_site": nll, "batch_K": ch.K, "sweeps_per_batch": ch.sweeps,
                     "proposals": len(m), "seconds": ch_s,
                     "acceptance": float(np.mean(ch.batch_accept[1:])),
                     "tau_int_proposals": tau_l, "tau_windowed": tau_l_w, "tau_blocking": tau_l_b,
-                    "ess_per_s": ess_l, "M": float(m.mean()), "M_err": m_err_l},
-        # both chains sample the same distribution: their |M| must agree
+                    "ess_per_s": ess_l, "M": float(m.mean()), "M_err": m_err_l,
+                    "tau_E_proposals": tau_l_e, "ess_E_per_s": ess_l_e, "E": float(e.mean()),
+                    "E_err": e_err_l},
+        # both chains sample the same distribution: their |M| and E must agree
         "M_diff_sigma": float((m.mean() - series.mean()) / np.hypot(m_err_l, m_err_pt)),
-        "ratio_learned_over_plain": ess_l / ess_pt}
+        "E_diff_sigma": float((e.mean() - eseries.mean()) / np.hypot(e_err_l, e_err_pt)),
+        "ratio_learned_over_plain": ess_l / ess_pt,
+        "ratio_E_learned_over_plain": ess_l_e / ess_pt_e}
     ch.close()
     return out
 
@@ -885,7 +898,8 @@ def run_learned(args):
     cases = [(16, 2, 2.269), (32, 2, 2.269), (8, 3, 4.51)]
     for L, dim, T in cases:
         out = learned_case(pkg, L, dim, T, args.train_seconds, args.chain_batches, args.pt_sweeps)
-        print(json.dumps({"metric": "ESS/s of |M| at T (learned vs plain PT)", **out}), flush=True)
+        print(json.dumps({"metric": "ESS/s of |M| and E at T (learned vs plain PT)", **out}),
+              flush=True)
     return 0
 
 

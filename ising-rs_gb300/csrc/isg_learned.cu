@@ -591,6 +591,9 @@ __global__ void __launch_bounds__(128)
             if (ok2) mma_tap(acc[l - 1], o2 + lo, aoff0, aoff1, wr + 2 * kC * 2);
             if (ok3) mma_tap(acc[l - 1], o3 + lo, aoff0, aoff1, wr + 3 * kC * 2);
         }
+        // the spin sampled at p - 1 (warp 0, end of the previous position) is
+        // read by layer 0 below: the other warps did their look-back taps first
+        __syncthreads();
         // layer 0 (mask A, 1 -> 32)
         {
             const float sv0 = ok0 ? (float)sring[ts0 * kMmaRows + r0] : 0.f;
@@ -659,7 +662,8 @@ __global__ void __launch_bounds__(128)
                 }
             }
         }
-        __syncthreads();
+        // no barrier here: the next position's look-back taps read only hidden
+        // layers written before the last hidden-layer barrier, and write nothing
         if (++x == W) {
             x = 0;
             ++y;

@@ -413,7 +413,8 @@ def jackknife_mean_err(x, nb=20):
 
 
 def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
-    """Config 5: ESS/s of |M| of one chain at T, plain checkerboard PT vs the
+    """Learned-proposal workload (2D L=16/32 at T=2.269, 3D L=8 at T=4.51): ESS/s
+    of |M| and E of one chain at T, plain checkerboard PT vs the
     learned independence proposal (+ interleaved sweeps)."""
     import torch
     import importlib
@@ -502,10 +503,10 @@ def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
 
 
 CONT_WORKLOADS = {
-    # config 3: O(3), L=32,64,96 x 24 replicas on [1.40,1.48], 1 Metropolis (cone) + 4 OR
+    # Heisenberg PT: O(3), L=32,64,96 x 24 replicas on [1.40,1.48], 1 Metropolis (cone) + 4 OR
     "heisenberg": dict(nc=3, sizes=[32, 64, 96], R=24, tmin=1.40, tmax=1.48, n_or=4, delta=0.5,
                        bytes_per_update=36),
-    # config 4: O(2), L=32,64,128 x 16 replicas on [2.18,2.22], uniform-angle Metropolis + 2 OR
+    # XY PT: O(2), L=32,64,128 x 16 replicas on [2.18,2.22], uniform-angle Metropolis + 2 OR
     "xy": dict(nc=2, sizes=[32, 64, 128], R=16, tmin=2.18, tmax=2.22, n_or=2, delta=math.pi,
                bytes_per_update=24),
 }
@@ -525,7 +526,7 @@ def run_continuous(args):
     b.set_stream(stream)
     b.set_temperatures(T)
     if args.workload == "heisenberg":
-        # config 3: cone width tuned for about 50% acceptance during warm-up
+        # Heisenberg: cone width tuned for about 50% acceptance during warm-up
         w = dict(w, delta=pkg.tune_delta(b, w["delta"], w["n_or"], 0.5))
     b.sweep(50, w["delta"], w["n_or"])
     b.reset_sampling()
@@ -975,7 +976,8 @@ def main():
                     choices=["ising", "heisenberg", "xy", "anneal", "kz", "coarsening",
                              "jfit", "jfit-heisenberg", "jfit-xy", "reweight"])
     ap.add_argument("--learned", action="store_true",
-                    help="config 5: learned proposal vs plain PT ESS/s (separate JSON lines)")
+                    help="learned proposal vs plain PT ESS/s on 2D L=16/32 and 3D L=8 "
+                         "(separate JSON lines)")
     ap.add_argument("--train-seconds", type=float, default=60.0)
     ap.add_argument("--chain-batches", type=int, default=800)
     ap.add_argument("--pt-sweeps", type=int, default=200000)

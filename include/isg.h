@@ -66,8 +66,10 @@ extern "C" {
  *  EXCH : replica exchange.  c1 = lower temperature index of the pair,
  *         c0 = exchange uid, step = exchange count of that size;
  *         u = ((w0 << 32 | w1) >> 11) * 2^-53.
- *  CINIT/CMETRO: continuous spins, c1 = natural site index (CINIT) or colour
- *         index (CMETRO), one Philox call per site.
+ *  CINIT/CMETRO: continuous spins, c1 = natural site index (CINIT, one call
+ *         per site) or colour index i (CMETRO: O(3) one call per site, words
+ *         0..2; O(2) one call per index pair at c1 = i >> 1, words 0 and 2 for
+ *         even i, 1 and 3 for odd i).
  */
 #define ISG_TAG_INIT   0x01u
 #define ISG_TAG_ISING  0x02u

@@ -345,9 +345,10 @@ __device__ __forceinline__ bool cone_test(const float (&v)[NC], const float (&h)
 }
 
 // Metropolis with the cone proposal on column tasks (continuous_spin_kernel.cu:9-83
-// with the cone proposal of heisenberg/metropolis.rs:54-69): one Philox block per
-// site, counter = colour index; on renormalisation sweeps every site of this
-// colour is written back normalised.
+// with the cone proposal of heisenberg/metropolis.rs:54-69): O(3) one Philox block
+// per site at its colour index i (words x, y, z); O(2) one block per colour-index
+// pair at i >> 1 (words x, z for even i, y, w for odd i); on renormalisation
+// sweeps every site of this colour is written back normalised.
 template <int NC>
 __global__ void __launch_bounds__(kCThreads, 3)
     k_cont_metro_col(const __grid_constant__ ContParams P, int colour, int sweep_off,
@@ -413,7 +414,10 @@ __global__ void __launch_bounds__(kCThreads, 3)
                 v[k] = lv[k];
             }
             if (z + 1 < c.z1) load_step(z + 1);
-            const U4 u = philox10(uid, i, c2, c3, k0, k1);
+            // O(3): one block per site; O(2): one block per colour-index pair,
+            // words (x, z) for the even index, (y, w) for the odd
+            U4 u = philox10(uid, NC == 3 ? i : i >> 1, c2, c3, k0, k1);
+            if (NC == 2 && (i & 1u)) u = U4{u.y, u.x, u.w, u.z};
             const bool accepted = cone_test<NC>(v, h, u, cos_delta, delta, beta, P.J, w);
             n_acc += accepted ? 1u : 0u;
             if (accepted || renorm_now) {
@@ -446,9 +450,10 @@ __global__ void __launch_bounds__(kCThreads, 3)
 }
 
 // Metropolis on column tasks of two adjacent sites (the pair layout of
-// k_cont_or_col2): each site draws from its own Philox counter (its colour
-// index) and goes through cone_test exactly as in k_cont_metro_col; a site
-// neither accepted nor renormalised is written back unchanged.
+// k_cont_or_col2): each site draws the Philox words k_cont_metro_col gives it
+// (O(3): its own block; O(2): the pair's one block) and goes through cone_test
+// exactly as there; a site neither accepted nor renormalised is written back
+// unchanged.
 template <int NC>
 __global__ void __launch_bounds__(kCThreads, 2)
     k_cont_metro_col2(const __grid_constant__ ContParams P, int colour, int sweep_off,
@@ -518,8 +523,16 @@ __global__ void __launch_bounds__(kCThreads, 2)
                 vb[k] = lv[k].y;
             }
             if (z + 1 < c.z1) load_step(z + 1);
-            const U4 u0 = philox10(uid, i, c2, c3, k0, k1);
-            const U4 u1 = philox10(uid, i + 1, c2, c3, k0, k1);
+            // O(3): one block per site; O(2): the pair's one block (i is even),
+            // words (x, z) for site k, (y, w) for site k+1
+            U4 u0, u1;
+            if constexpr (NC == 3) {
+                u0 = philox10(uid, i, c2, c3, k0, k1);
+                u1 = philox10(uid, i + 1, c2, c3, k0, k1);
+            } else {
+                u0 = philox10(uid, i >> 1, c2, c3, k0, k1);
+                u1 = U4{u0.y, u0.x, u0.w, u0.z};
+            }
             const bool acc_a = cone_test<NC>(va, ha, u0, cos_delta, delta, beta, P.J, wa);
             const bool acc_b = cone_test<NC>(vb, hb, u1, cos_delta, delta, beta, P.J, wb);
             n_acc += (acc_a ? 1u : 0u) + (acc_b ? 1u : 0u);

@@ -13,7 +13,8 @@
  *    cos(theta) = 1 - u0 (1 - cos delta), phi = 2 pi u1, and the same
  *    perpendicular frame; O(2) rotates by delta (2 u0 - 1); accept if dE <= 0
  *    or u2 < exp(-beta dE) (src/heisenberg/metropolis.rs:26-35), with u0..u2
- *    the 24-bit uniforms of the ISG_TAG_CMETRO Philox words;
+ *    the 24-bit uniforms of the ISG_TAG_CMETRO Philox words (O(2): the block of
+ *    colour index c >> 1, words 0 and 2 for even c, 1 and 3 for odd c);
  *  - measure: E = -J sum_bonds S.S' and M (src/heisenberg/mod.rs:59-74,
  *    src/xy/mod.rs:50-64) plus the helicity bond sums.
  * The GPU computes in FP32, so agreement is within FP32 rounding, and an
@@ -106,7 +107,14 @@ void or_cont_metropolis(int L, int nc, double* s, int colour, uint64_t seed, uin
                 field(L, nc, s, x, y, z, h);
                 double* v = s + i * nc;
                 uint32_t w[4];
-                words(seed, uid, (uint32_t)(i >> 1), sweep, TAG_CMETRO, (uint32_t)colour, w);
+                const uint32_t ci = (uint32_t)(i >> 1);  /* colour index */
+                /* O(3): one block per site; O(2): one block per pair of colour
+                   indices (2j, 2j+1), words 0 and 2 for the even, 1 and 3 for the odd */
+                words(seed, uid, nc == 3 ? ci : ci >> 1, sweep, TAG_CMETRO, (uint32_t)colour, w);
+                if (nc == 2 && (ci & 1u)) {
+                    w[0] = w[1];
+                    w[2] = w[3];
+                }
                 double nv[3];
                 if (nc == 3) {
                     double ct = 1.0 - u24(w[0]) * (1.0 - cd);

@@ -455,7 +455,7 @@ __global__ void __launch_bounds__(kCThreads, 3)
 // exactly as there; a site neither accepted nor renormalised is written back
 // unchanged.
 template <int NC>
-__global__ void __launch_bounds__(kCThreads, 2)
+__global__ void __launch_bounds__(kCThreads, NC == 2 ? 3 : 2)
     k_cont_metro_col2(const __grid_constant__ ContParams P, int colour, int sweep_off,
                       float cos_delta, float delta) {
     const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;

@@ -439,54 +439,6 @@ void or_ref_run(int L, int dim, double T, double J, double h, uint64_t seed, int
     free(nb);
 }
 
-/* Timed CPU baseline: `threads` independent replicas (one per thread), each
- * running `sweeps` random-site sweeps of an L^dim lattice at temperature T.
- * Returns wall seconds; *flips = total attempted site updates. */
-typedef struct {
-    int L, dim;
-    double beta, J, h;
-    uint64_t seed;
-    int64_t sweeps;
-    const int32_t* nb;
-    int64_t checksum;
-} bench_arg;
-
-static void* bench_worker(void* vp) {
-    bench_arg* a = (bench_arg*)vp;
-    int64_t n = nsites(a->L, a->dim);
-    int8_t* spins = (int8_t*)malloc((size_t)n);
-    xo256 g;
-    or_xo_seed(&g, a->seed);
-    or_ref_randomise(spins, n, &g);
-    for (int64_t s = 0; s < a->sweeps; ++s)
-        or_ref_metropolis_sweep(spins, n, a->nb, 2 * a->dim, a->beta, a->J, a->h, &g);
-    int64_t b, m;
-    or_ising_measure(a->L, a->dim, spins, &b, &m);
-    a->checksum = b;
-    free(spins);
-    return NULL;
-}
-
-double or_ref_bench(int L, int dim, double T, int64_t sweeps, int threads, uint64_t seed,
-                    double* flips) {
-    int32_t* nb = or_ref_neighbours(L, dim);
-    bench_arg* args = (bench_arg*)calloc((size_t)threads, sizeof(bench_arg));
-    pthread_t* tid = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
-    struct timespec t0, t1;
-    clock_gettime(CLOCK_MONOTONIC, &t0);
-    for (int i = 0; i < threads; ++i) {
-        args[i].L = L; args[i].dim = dim; args[i].beta = 1.0 / T; args[i].J = 1.0; args[i].h = 0.0;
-        args[i].seed = seed + (uint64_t)i * 1000 + (uint64_t)L;
-        args[i].sweeps = sweeps; args[i].nb = nb;
-        pthread_create(&tid[i], NULL, bench_worker, &args[i]);
-    }
-    for (int i = 0; i < threads; ++i) pthread_join(tid[i], NULL);
-    clock_gettime(CLOCK_MONOTONIC, &t1);
-    *flips = (double)nsites(L, dim) * (double)sweeps * (double)threads;
-    free(args); free(tid); free(nb);
-    return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
-}
-
 /* Timed checkerboard replay (same stream as the GPU), `threads` replicas. */
 typedef struct {
     int L, dim;

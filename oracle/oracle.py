@@ -53,9 +53,6 @@ def lib():
         L.or_ising_pt.restype = C.c_int64
         L.or_ref_run.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64,
                                  C.c_int64, C.c_int64, f64p, f64p]
-        L.or_ref_bench.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int64, C.c_int, C.c_uint64,
-                                   C.POINTER(C.c_double)]
-        L.or_ref_bench.restype = C.c_double
         L.or_replay_bench.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int64, C.c_int, C.c_uint64,
                                       C.POINTER(C.c_double)]
         L.or_replay_bench.restype = C.c_double
@@ -456,12 +453,6 @@ def ref_run(L: int, dim: int, T: float, seed: int, warmup: int, samples: int, J=
     m = np.zeros(samples, np.float64)
     lib().or_ref_run(L, dim, T, J, h, seed, warmup, samples, e, m)
     return e, m
-
-
-def ref_bench(L: int, dim: int, T: float, sweeps: int, threads: int, seed: int = 42):
-    flips = C.c_double()
-    sec = lib().or_ref_bench(L, dim, T, sweeps, threads, seed, C.byref(flips))
-    return sec, flips.value
 
 
 def replay_bench(L: int, dim: int, T: float, sweeps: int, threads: int, seed: int = 42):

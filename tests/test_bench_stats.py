@@ -1,5 +1,6 @@
-"""The autocorrelation estimators bench.py uses for ESS/s: the windowed tau_int
-and the blocking estimate that catches rare long excursions."""
+"""Host-side parts of bench.py: the autocorrelation estimators it uses for ESS/s
+(the windowed tau_int and the blocking estimate that catches rare long
+excursions) and the JSON line of its reference arm."""
 from __future__ import annotations
 
 import numpy as np
@@ -45,3 +46,30 @@ def test_jackknife_error_of_white_noise():
     x = rng.standard_normal(200_000)
     err = b.jackknife_mean_err(x)
     assert abs(err - 1 / np.sqrt(len(x))) < 0.4 / np.sqrt(len(x))
+
+
+def test_reference_arm_line_keeps_the_contract():
+    """`bench.py --impl reference` (host CPU, no GPU): one JSON line with the
+    headline's metric, unit and workload, a cpu_baseline describing the run and
+    an e2e entry with no host-device bytes."""
+    import json
+    import subprocess
+    import sys
+
+    from conftest import ROOT
+
+    b = _bench()
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                          "--steps", "2", "--warmup", "3", "--ref-seconds", "2"],
+                         capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == b.METRIC and d["unit"] == "flips/ns"
+    assert d["config"]["workload"] == b.WORKLOAD and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 2 and d["warmup"] == 3
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
+    e = d["e2e"]
+    assert e["value"] == d["value"] and e["h2d_bytes_per_step"] == 0 == e["d2h_bytes_per_step"]

@@ -73,3 +73,16 @@ def test_reference_arm_line_keeps_the_contract():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     e = d["e2e"]
     assert e["value"] == d["value"] and e["h2d_bytes_per_step"] == 0 == e["d2h_bytes_per_step"]
+
+
+def test_tau_int_matches_the_reference_estimator():
+    """bench.tau_int (FFT autocorrelation) against the reference's own
+    `integrated_autocorrelation_time(autocorrelation(x))` of
+    analysis/scripts/reproduce_validation.py, evaluated on seeded series by
+    tests/golden/make_tau_golden.py."""
+    from conftest import ROOT
+
+    b = _bench()
+    g = np.load(ROOT / "tests" / "golden" / "tau_golden.npz")
+    for x, t in zip(g["series"], g["tau"]):
+        assert abs(b.tau_int(x) - t) <= 1e-9 * max(1.0, t), (b.tau_int(x), t)

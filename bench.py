@@ -76,9 +76,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per half-sweep launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "ising_halfsweep_L8-128x32.txt"
+HEADLINE_PROFILE = "ising_halfsweep_L8-128x32.txt"
+HBM_PROFILE = "ising_halfsweep_L128x128.txt"
+HBM_REPLICAS = 128
+ESS_SWEEPS = 40000
+
+
+def ncu_traffic(name: str):
+    """DRAM bytes per half-sweep launch from a committed ncu summary, if any."""
+    p = ROOT / "profiles" / name
     if p.exists():
         m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", p.read_text())
         if m:
@@ -263,6 +269,143 @@ def run_reference(args):
     return 0
 
 
+def _timed_pt_steps(b, stream, flush, steps):
+    """Per-step device ms of `steps` PT steps (one exchange period each, one CUDA
+    graph replay), L2 flushed before every step, events on the library's stream."""
+    import torch
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for i in range(steps):
+            flush.fill_(i & 0xFF)
+            starts[i].record(stream)
+            # 10 sweeps, 2 fused measures, 1 exchange; records stay in the
+            # device ring (read after the timed region)
+            b.pt_launch(SWEEPS_PER_STEP, EXCHANGE_EVERY, MEASURE_EVERY)
+            ends[i].record(stream)
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)]
+
+
+def _roofline(b, launch_ms, peak, peak_kind, traffic, kernel, residency):
+    sites_launch = b.sites_per_halfsweep()
+    alg_bytes = sites_launch * BYTES_PER_UPDATE
+    achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
+            "bytes_per_launch": alg_bytes, "launch_ms": launch_ms, "residency": residency,
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, copy bandwidth)"}
+
+
+def hbm_case(pkg, stream, flush, steps, peak, peak_kind):
+    """3D Ising L = 128 alone, 128 replicas on the same T grid width (268 MB of
+    spins, twice the L2): the spec roofline configuration.  Same step and
+    timing as the headline; the half-sweep is timed inside a graph of 20 launches
+    with L2 flushed before each replay."""
+    R = HBM_REPLICAS
+    T = [TMIN + (TMAX - TMIN) * i / (R - 1) for i in range(R)]
+    b = pkg.IsingBatch([128], R, seed=SEED + 7)
+    b.set_stream(stream)
+    b.set_temperatures(T)
+    b.step(20)
+    b.reset_sampling()
+    for _ in range(3):
+        b.pt_launch(SWEEPS_PER_STEP, EXCHANGE_EVERY, MEASURE_EVERY)
+    step_ms = _timed_pt_steps(b, stream, flush, steps)
+    dev_ms = float(sum(step_ms))
+    sites = R * 128 ** 3
+    value = sites * SWEEPS_PER_STEP * steps / (dev_ms * 1e6)
+    launch_ms = b.time_halfsweep_graph(2 * SWEEPS_PER_STEP, 256 << 20, 5)
+    roof = _roofline(b, launch_ms, peak, peak_kind, ncu_traffic(HBM_PROFILE),
+                     "k_ising_words<3,0,1> (one half-sweep of 128 L=128 lattices)",
+                     f"HBM: {R * 128 ** 3 / 2 ** 20:.0f} MiB of spins, twice the L2; "
+                     f"graph of {2 * SWEEPS_PER_STEP} half-sweeps, L2 flushed before each replay")
+    b.close()
+    return {"workload": f"3D Ising PT L=128 x {R} replicas, T in [{TMIN},{TMAX}], exchange 10, "
+                        f"measure 5", "value": value, "unit": "flips/ns",
+            "ms_per_step": dev_ms / steps, "steps": steps,
+            "sweeps_per_s": SWEEPS_PER_STEP * steps / (dev_ms * 1e-3), "roofline": roof}
+
+
+def ess_case(pkg, stream, sweeps_per_s):
+    """ESS/s of |M| on the headline batch from a run of its own: 5000 warm-up
+    sweeps, then ESS_SWEEPS sweeps with a record every 5 (at L = 128 near Tc,
+    tau_int is several hundred sweeps, so the run covers >= 50 tau).  tau is the
+    larger of the windowed estimate (reproduce_validation.py:157-163) and the
+    20-block estimate, per size at the slot nearest Tc.  ESS/s follows the
+    spec definition: sweeps/s of the timed batch / tau_int(|M|) in sweeps,
+    with tau_int = 1/2 + sum of the autocorrelation (1/2 for independent samples;
+    N / (2 tau_int) is the other common convention and is half of it)."""
+    T = temps()
+    b = pkg.IsingBatch(SIZES, REPLICAS, seed=SEED + 11)
+    b.set_stream(stream)
+    b.set_temperatures(T)
+    b.step(5000)
+    b.reset_sampling()
+    rt, rb, rm = b.pt_run(ESS_SWEEPS, EXCHANGE_EVERY, MEASURE_EVERY)
+    b.close()
+    slot = int(np.argmin([abs(t - TC_3D) for t in T]))
+    per = {}
+    for s, L in enumerate(SIZES):
+        sl = slice(s * REPLICAS, (s + 1) * REPLICAS)
+        mask = rt[:, sl] == slot
+        series = np.abs(rm[:, sl][mask].astype(float)) / L ** 3
+        tw, tb = tau_int(series), tau_blocking(series)
+        tau_s = max(tw, tb) * MEASURE_EVERY
+        per[str(L)] = {"tau_int_sweeps": tau_s, "tau_windowed_sweeps": tw * MEASURE_EVERY,
+                       "tau_blocking_sweeps": tb * MEASURE_EVERY, "records": int(len(series)),
+                       "records_per_tau": len(series) * MEASURE_EVERY / tau_s,
+                       "ess_per_s": sweeps_per_s / tau_s}
+    h = per["128"]
+    return {"value": h["ess_per_s"], "unit": "ESS/s", "observable": "|M|", "L": 128,
+            "T": T[slot], "tau_int_sweeps": h["tau_int_sweeps"], "records": h["records"],
+            "sweeps": ESS_SWEEPS, "warmup_sweeps": 5000,
+            "convention": "sweeps/s / tau_int(|M|) in sweeps, tau_int = 1/2 + sum rho(t) "
+                          "(max of windowed and 20-block estimates); N/(2 tau) is half of it",
+            "per_size": per}
+
+
+def config1_case(pkg):
+    """3D cubic Ising L = 16, single T = 4.5115, seed 42, 1000 warm-up + 1000
+    measured sweeps with E and |M| every sweep (the reference's plain sweep
+    binary).  One synchronous C-ABI call (isg_ising_run_schedule) runs all 2000
+    sweeps in one launch of the cluster-resident kernel; timed end to end
+    (host record arrays included).  Beside it, the reference CPU path (random-site
+    Metropolis, src/metropolis.rs:8-27, restated in C) on one host thread."""
+    L, T, n = 16, TC_3D, 16 ** 3
+    b = pkg.IsingBatch([L], 1, seed=SEED)
+    b.set_temperatures([T])
+    b.run_schedule(None, 2000, 1)        # warm the code path (module load, first launch)
+    times, recs = [], None
+    for rep in range(5):
+        c = pkg.IsingBatch([L], 1, seed=SEED)
+        c.set_temperatures([T])
+        t0 = time.perf_counter()
+        bond, mag = c.run_schedule(None, 2000, 1)
+        times.append(time.perf_counter() - t0)
+        recs = (bond, mag)
+        c.close()
+    b.close()
+    wall = statistics.median(times)
+    m = np.abs(recs[1][1000:, 0].astype(float)) / n
+    e = -recs[0][1000:, 0].astype(float) / n
+    tau = max(tau_int(m), tau_blocking(m))
+    oracle = _load("isg_oracle", ROOT / "oracle" / "oracle.py")
+    t0 = time.perf_counter()
+    oracle.ref_run(L, 3, T, SEED, 1000, 1000)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "3D Ising L=16, T=4.5115, 1000 warm-up + 1000 measured sweeps, E and |M| "
+                        "every sweep (one lattice)",
+            "value": 2000 * n / (wall * 1e9), "unit": "flips/ns", "wall_ms": wall * 1e3,
+            "sweeps_per_s": 2000 / wall, "E": float(e.mean()), "M": float(m.mean()),
+            "tau_int_sweeps": tau, "ess_per_s": 1000 / tau / wall,
+            "path": "isg_ising_run_schedule (C ABI), one resident-kernel launch, host records",
+            "cpu_baseline": {"value": 2000 * n / (cpu_s * 1e9), "unit": "flips/ns", "cores": 1,
+                             "kind": "port", "wall_ms": cpu_s * 1e3,
+                             "sample": "the same 2000 sweeps on one host thread (reference CPU "
+                                       "path restated in C)"}}
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = dist_info()
@@ -284,35 +427,22 @@ def run_gpu(args):
     b.reset_sampling()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     nsweep_sites = sites_per_sweep()
-    # warmup steps
     for _ in range(args.warmup):
         b.pt_run(SWEEPS_PER_STEP, EXCHANGE_EVERY, MEASURE_EVERY)
     b.reset_sampling()
-    # timed region: per-step CUDA events on the library's stream, L2 flushed
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     with clocks:
         wall0 = time.perf_counter()
-        with torch.cuda.stream(stream):
-            for i in range(args.steps):
-                flush.fill_(i & 0xFF)
-                starts[i].record(stream)
-                # one CUDA-graph replay: 10 sweeps, 2 fused measures, 1 exchange;
-                # records stay in the device ring (read after the timed region)
-                b.pt_launch(SWEEPS_PER_STEP, EXCHANGE_EVERY, MEASURE_EVERY)
-                ends[i].record(stream)
-        torch.cuda.synchronize()
+        step_ms = _timed_pt_steps(b, stream, flush, args.steps)
         wall = time.perf_counter() - wall0
-    rec_t, rec_b, rec_m = b.read_records(args.steps * SWEEPS_PER_STEP // MEASURE_EVERY)
     if ws > 1:
         torch.distributed.barrier()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     dev_ms = max_over_ranks(float(sum(step_ms)), dev)
     value = job_flips_per_ns(nsweep_sites, SWEEPS_PER_STEP * args.steps, ws, dev_ms)
+    sweeps_per_s = SWEEPS_PER_STEP * args.steps / (dev_ms * 1e-3)
 
     # e2e: the C-ABI call with host record buffers, records copied back each step
     b2 = pkg.IsingBatch(SIZES, REPLICAS, seed=SEED + 1000 + rank)
@@ -332,32 +462,23 @@ def run_gpu(args):
     e2e_value = nsweep_sites * SWEEPS_PER_STEP * e2e_steps * ws / (e2e_s * 1e9)
     b2.close()
 
-    # roofline of the half-sweep kernel (CUDA events on the library's stream)
-    launch_ms = b.time_halfsweep(40)
-    sites_launch = b.sites_per_halfsweep()
-    alg_bytes = sites_launch * BYTES_PER_UPDATE
-    achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
+    # roofline of the half-sweep kernel as it runs in the timed step: a graph of
+    # the step's 20 half-sweeps, L2 flushed before each replay
     peak, peak_kind = measured_peaks()
-    traffic = ncu_traffic()
-
-    # ESS/s of |M| at the slot nearest Tc for L = 128 (records of the timed run)
-    n_rec = rec_t.shape[0]
-    s128 = SIZES.index(128)
-    slot = int(np.argmin([abs(t - TC_3D) for t in T]))
-    series = []
-    for row in range(n_rec):
-        for rr in range(REPLICAS):
-            if rec_t[row, s128 * REPLICAS + rr] == slot:
-                series.append(abs(float(rec_m[row, s128 * REPLICAS + rr])) / 128 ** 3)
-    tau_rec = tau_int(series) if len(series) > 8 else float("nan")
-    tau_sweeps = tau_rec * MEASURE_EVERY
-    sweeps_per_s = SWEEPS_PER_STEP * args.steps / (dev_ms * 1e-3)
-    # ESS = N / (2 tau_int) with the windowed estimator (tau_int = 1/2 for
-    # independent samples)
-    ess = sweeps_per_s / (2.0 * tau_sweeps) if tau_sweeps > 0 else None
+    launch_ms = b.time_halfsweep_graph(2 * SWEEPS_PER_STEP, 256 << 20, 5)
+    roof = _roofline(b, launch_ms, peak, peak_kind, ncu_traffic(HEADLINE_PROFILE),
+                     "k_ising_words<3,0,2> (one half-sweep, all 160 lattices)",
+                     "L2: the 73 MiB batch fits in L2, which is flushed once per 20 "
+                     "half-sweeps (before every step), so most launches read L2; the HBM "
+                     "figure is roofline_hbm")
+    roof["share_of_step"] = 2 * SWEEPS_PER_STEP * launch_ms / (dev_ms / args.steps)
+    b.close()
 
     if rank != 0:
         return 0
+    hbm = hbm_case(pkg, stream, flush, max(3, min(args.steps, 100)), peak, peak_kind)
+    ess = ess_case(pkg, stream, sweeps_per_s)
+    cfg1 = config1_case(pkg)
     threads = host_threads()
     cpu_v, cpu_s, cpu_f = cpu_sample(threads, sweeps=args.cpu_sweeps)
     launches_per_step = 2 * SWEEPS_PER_STEP + (SWEEPS_PER_STEP // MEASURE_EVERY)
@@ -370,21 +491,18 @@ def run_gpu(args):
                                                  "(one CUDA graph)",
                    "sites_per_sweep": nsweep_sites, "l2": "flushed (256 MiB write) before "
                                                           "every timed step",
-                   "launch": "persistent word kernel, grid = SMs x occupancy; rolling loads two planes ahead (2 blocks/SM) because the batch fits in L2"},
+                   "launch": "persistent word kernel, grid = SMs x occupancy"},
         "sweeps_per_s": sweeps_per_s,
         "hbm_gbs_algorithmic": value * BYTES_PER_UPDATE,
-        "ess_per_s": {"value": ess, "observable": "|M|", "L": 128, "T": T[slot],
-                      "tau_int_sweeps": tau_sweeps, "records": len(series)},
+        "ess_per_s": ess,
         "e2e": {"value": e2e_value, "unit": "flips/ns", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": d2h // e2e_steps,
                 "path": "isg_ising_pt_run (C ABI) per step, (slot,E,M) records copied to host "
                         "arrays in the timed region; a PT step consumes no host input "
                         "(lattices and temperature tables stay resident in HBM)"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "k_ising_words<3,0> (one half-sweep, all 160 lattices)",
-                     "bytes_per_launch": alg_bytes, "launch_ms": launch_ms,
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "roofline": roof,
+        "roofline_hbm": hbm,
+        "config1": cfg1,
         "cpu_baseline": {"value": cpu_v, "unit": "flips/ns", "cores": threads, "kind": "port",
                          "sample": f"{threads} threads x {args.cpu_sweeps:g} random-site sweeps "
                                    f"of L=8..128 each ({cpu_f:.3g} flips, {cpu_s:.1f} s); "
@@ -912,19 +1030,14 @@ def ncu_case_graph(kind: str):
     batch (4096 rounded up to whole waves of the sampler) of the untrained 2D
     L=32 network (sampling, then the flipped scores)."""
     pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
-    if kind in ("learned", "learned-train"):
+    if kind == "learned":
         import importlib
         import torch
         torch.cuda.set_device(0)
         lrn = importlib.import_module(pkg.__name__ + ".learned")
         q = lrn.LearnedProposal(32, 32, layers=6, seed=SEED)
-        if kind == "learned-train":
-            data = lrn.collect_training_set(32, 2, 2.269, chains=16, rounds=8, gap=10,
-                                            warmup=200)
-            q.train(data, batch=128, steps=3, lr=1e-3)
-        else:
-            qn = q.batch_quantum()
-            q.sample(-(-4096 // qn) * qn, 1)
+        qn = q.batch_quantum()
+        q.sample(-(-4096 // qn) * qn, 1)
         q.sync()
         print("ncu case done")
         return 0
@@ -983,18 +1096,17 @@ def main():
     ap.add_argument("--pt-sweeps", type=int, default=200000)
     ap.add_argument("--ncu-case", nargs="?", const="words",
                     choices=["words", "resident", "graph", "cgraph3", "cgraph2", "reweight",
-                             "learned", "learned-train"],
+                             "learned"],
                     help="no timing: 'words' = a few half-sweeps of L=128 x 96 replicas (201 MB, "
                          "larger than L2) for an ncu capture of the half-sweep kernel; "
                          "'resident' = one 2000-sweep schedule of an L=30 lattice; "
                          "'graph'/'cgraph3'/'cgraph2' = one 100-sweep launch of the graph "
                          "kernels (BCC 8^3, 20 replicas); 'reweight' = one WHAM analysis; "
-                         "'learned' = 4096 proposals of the L=32 network (sample + score); "
-                         "'learned-train' = three training steps of that network")
+                         "'learned' = 4096 proposals of the L=32 network (sample + score)")
     args = ap.parse_args()
     if args.ncu_case == "resident":
         return ncu_case_resident()
-    if args.ncu_case in ("graph", "cgraph3", "cgraph2", "reweight", "learned", "learned-train"):
+    if args.ncu_case in ("graph", "cgraph3", "cgraph2", "reweight", "learned"):
         return ncu_case_graph(args.ncu_case)
     if args.ncu_case:
         return ncu_case()

@@ -230,6 +230,14 @@ int isg_ising_autotune(isg_ising* h, int* best);
 /* Mean device time (ms, CUDA events on the handle's stream) of one half-sweep
  * launch over n_launches launches of the current batch (colours alternate). */
 int isg_ising_time_halfsweep(isg_ising* h, int n_launches, float* avg_ms);
+/* Mean device time (ms) of one half-sweep launch as it runs inside a PT cycle:
+ * n_launches launches (1..4096, colours alternating) captured as one CUDA
+ * graph, each of `replays` replays preceded by a write of flush_bytes of
+ * scratch memory (0 = no flush), events around the graph alone.  Spins and
+ * sweep counter are restored.  Measurement utility (no reference counterpart;
+ * it backs the roofline figures of the bench). */
+int isg_ising_time_halfsweep_graph(isg_ising* h, int n_launches, int64_t flush_bytes,
+                                   int replays, float* avg_ms);
 
 /* Sites updated by one half-sweep launch (all sizes and replicas). */
 int isg_ising_sites_per_halfsweep(isg_ising* h, int64_t* sites);
@@ -312,6 +320,9 @@ int isg_cont_sites_per_sweep(isg_cont* h, int64_t* sites);
  * must not exceed 16384, i.e. at most 16,777,216 sites per call; larger
  * requests return ISG_ERR_ARG).  The first call on each device looks up that
  * array's device address, so make it before capturing a stream into a graph.
+ * That address is kept for the life of the process: after cudaDeviceReset (or
+ * anything else that tears down the device's primary context and reloads the
+ * module) it is stale, so do not use this entry point again in that process.
  * All calls share the array: calls that overlap on the GPU (different
  * streams, no ordering) race and must be serialised by the caller. */
 int isg_cont_observables_static(const float* d_spins, int L, int n_comp, int replicas, double J,

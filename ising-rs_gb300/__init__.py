@@ -106,6 +106,7 @@ def _declare(L):
         "isg_ising_autotune": [vp, vp],
         "isg_ising_set_prefetch": [vp, i32],
         "isg_ising_time_halfsweep": [vp, i32, vp],
+        "isg_ising_time_halfsweep_graph": [vp, i32, i64, i32, vp],
         "isg_ising_sites_per_halfsweep": [vp, vp],
         "isg_jackknife": [vp, vp, i64, dbl, dbl, i32, vp],
         "isg_fss_anneal": [vp, i32, i32, dbl, dbl, i32, dbl, dbl, i64, i64, u64, vp],
@@ -547,6 +548,15 @@ class IsingBatch:
     def time_halfsweep(self, n_launches: int = 20) -> float:
         v = C.c_float()
         _check(lib().isg_ising_time_halfsweep(self._h, n_launches, C.byref(v)))
+        return v.value
+
+    def time_halfsweep_graph(self, n_launches: int = 20, flush_bytes: int = 256 << 20,
+                             replays: int = 5) -> float:
+        """Mean ms of one half-sweep inside a captured graph of n_launches
+        half-sweeps, L2 flushed before each replay (as in a timed PT step)."""
+        v = C.c_float()
+        _check(lib().isg_ising_time_halfsweep_graph(self._h, n_launches, int(flush_bytes),
+                                                    replays, C.byref(v)))
         return v.value
 
     def sites_per_halfsweep(self) -> int:

@@ -2009,6 +2009,71 @@ int isg_ising_time_halfsweep(isg_ising* H, int n_launches, float* avg_ms) {
     return timed_halfsweeps(H, n_launches, avg_ms);
 }
 
+// The half-sweeps as they run inside a PT cycle: n_launches launches (colours
+// alternating, as n_launches/2 sweeps) captured as one CUDA graph, each replay
+// preceded by a write of flush_bytes (so the first launch of a replay starts
+// from a cold L2, like the first launch of a timed PT step), timed with events
+// on the handle's stream around the graph alone.  Spins and sweep counter are
+// restored afterwards.
+int isg_ising_time_halfsweep_graph(isg_ising* H, int n_launches, int64_t flush_bytes,
+                                   int replays, float* avg_ms) {
+    if (!H || !avg_ms || n_launches < 1 || n_launches > 4096 || flush_bytes < 0 || replays < 1)
+        return fail(ISG_ERR_ARG, "isg_ising_time_halfsweep_graph: bad argument");
+    if (!H->temps_set)
+        return fail(ISG_ERR_STATE, "isg_ising_time_halfsweep_graph: temperatures not set");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    uint8_t* backup = nullptr;
+    uint8_t* flush = nullptr;
+    ISG_CK(cudaMalloc((void**)&backup, (size_t)H->spin_bytes));
+    cudaError_t e = cudaSuccess;
+    if (flush_bytes > 0) e = cudaMalloc((void**)&flush, (size_t)flush_bytes);
+    unsigned long long ctrl0 = 0;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(backup, H->d_spins, (size_t)H->spin_bytes, cudaMemcpyDeviceToDevice,
+                            H->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&ctrl0, H->d_ctrl, sizeof(ctrl0), cudaMemcpyDeviceToHost, H->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(H->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        for (int i = 0; i < n_launches; ++i) launch_half(H, i & 1, i >> 1, 0);
+        e = cudaStreamEndCapture(H->stream, &g);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    float total = 0.f;
+    for (int rep = 0; rep <= replays && e == cudaSuccess; ++rep) {  // replay 0 warms up
+        if (flush) e = cudaMemsetAsync(flush, rep & 0xFF, (size_t)flush_bytes, H->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(a, H->stream);
+        if (e == cudaSuccess) e = cudaGraphLaunch(ge, H->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(b, H->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+        if (rep > 0) total += ms;
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(H->d_spins, backup, (size_t)H->spin_bytes, cudaMemcpyDeviceToDevice,
+                            H->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(H->d_ctrl, &ctrl0, sizeof(ctrl0), cudaMemcpyHostToDevice, H->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    if (ge) cudaGraphExecDestroy(ge);
+    if (g) cudaGraphDestroy(g);
+    cudaFree(backup);
+    if (flush) cudaFree(flush);
+    if (e != cudaSuccess) return cuda_fail(e, "isg_ising_time_halfsweep_graph");
+    *avg_ms = total / (float)((int64_t)replays * n_launches);
+    return ISG_OK;
+}
+
 int isg_ising_set_prefetch(isg_ising* H, int depth) {
     if (!H) return fail(ISG_ERR_ARG, "isg_ising_set_prefetch: NULL handle");
     if (depth < 0 || depth > 2) return fail(ISG_ERR_ARG, "isg_ising_set_prefetch: depth must be 0..2");

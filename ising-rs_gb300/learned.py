@@ -10,9 +10,14 @@ The chain at temperature T on a periodic L^dim lattice alternates:
   * one batch of K proposals y ~ q_sym, each tested in order by the
     independence Metropolis-Hastings rule (accept iff log u < A(y) - A(x),
     A = -beta E - log q_sym).
-Both moves leave exp(-beta E) invariant.  When the acceptance of a batch falls
-below `min_accept` the next batch is preceded by `fallback_sweeps` sweeps
-(the plain sampler takes over); otherwise by `sweeps`.
+Both moves leave exp(-beta E) invariant.  The plain sampler is the fallback:
+during the first `burn_in` batches, a batch whose acceptance falls below
+`min_accept` is followed by `fallback_sweeps` sweeps instead of `sweeps`.
+After burn-in the number of sweeps per batch is frozen (`fallback_sweeps` if
+the mean burn-in acceptance is below `min_accept`, else `sweeps`): a rule that
+kept reading the chain's own acceptance would choose the next kernel from the
+current state, and the composite chain would no longer leave exp(-beta E)
+invariant.  Samples taken after burn-in are exact.
 """
 from __future__ import annotations
 
@@ -156,7 +161,7 @@ class LearnedChain:
 
     def __init__(self, proposal: LearnedProposal, L: int, dim: int, T: float, J: float = 1.0,
                  K: int | None = 4096, sweeps: int = 1, fallback_sweeps: int = 20,
-                 min_accept: float = 0.002, seed: int = 11):
+                 min_accept: float = 0.002, seed: int = 11, burn_in: int = 4):
         import torch
         self.q, self.L, self.dim, self.T, self.J = proposal, int(L), int(dim), float(T), float(J)
         if K is None:
@@ -165,6 +170,7 @@ class LearnedChain:
             K = -(-4096 // qn) * qn
         self.K, self.sweeps, self.fallback, self.min_accept = int(K), int(sweeps), \
             int(fallback_sweeps), float(min_accept)
+        self.burn_in = int(burn_in)
         self.n = self.L ** self.dim
         if self.n != proposal.H * proposal.W:
             raise IsingError(-1, "lattice size does not match the proposal raster")
@@ -250,7 +256,12 @@ class LearnedChain:
         rate = (acc - self._acc_prev) / self.K
         self._acc_prev = acc
         self.batch_accept.append(rate)
-        self.next_sweeps = self.fallback if rate < self.min_accept else self.sweeps
+        if self.step_no < self.burn_in:
+            self.next_sweeps = self.fallback if rate < self.min_accept else self.sweeps
+        elif self.step_no == self.burn_in:
+            # frozen from here on: independent of the chain's later states
+            mean = float(np.mean(self.batch_accept[:self.burn_in])) if self.burn_in else 1.0
+            self.next_sweeps = self.fallback if mean < self.min_accept else self.sweeps
         return rate
 
     def m_series(self) -> np.ndarray:

@@ -1,7 +1,6 @@
 """Copies the reference's committed result tables into tests/golden/.
 
-Run in a container where faulknco/ising-rs is checked out (default
-/root/reference).  Sources:
+Usage: python make_golden.py <path of a faulknco/ising-rs checkout>.  Sources:
   analysis/data/gpu_windows_pipeline/publication/gpu_fss_{ising,heisenberg,xy}_N*_summary.csv
       PT summaries from the reference's own GPU path (scripts/run_gpu_publication.sh:22-50)
   results/published/classical_validation_full_v1/analysis/data/derived/validation/*.csv
@@ -12,7 +11,9 @@ import shutil
 import sys
 from pathlib import Path
 
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit(f"usage: python {Path(__file__).name} <reference checkout>")
+REF = Path(sys.argv[1])
 OUT = Path(__file__).resolve().parent
 
 pub = REF / "analysis/data/gpu_windows_pipeline/publication"

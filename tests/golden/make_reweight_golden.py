@@ -1,7 +1,7 @@
 """Golden vectors of the reference's reweighting functions.
 
-Imports analysis/scripts/reweighting.py from a checkout of faulknco/ising-rs
-(default /root/reference; it needs numpy only) and evaluates single_histogram,
+Usage: python make_reweight_golden.py <path of a faulknco/ising-rs checkout>.
+Imports analysis/scripts/reweighting.py from that checkout (numpy only) and evaluates single_histogram,
 wham_reweight and reweight_binder on seeded synthetic PT-like samples: four
 simulations at beta = 0.20..0.23 with overlapping Gaussian total energies and
 |m| values.  Writes tests/golden/reweight_golden.npz (inputs and outputs);
@@ -13,7 +13,9 @@ from pathlib import Path
 
 import numpy as np
 
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit(f"usage: python {Path(__file__).name} <reference checkout>")
+REF = Path(sys.argv[1])
 OUT = Path(__file__).resolve().parent / "reweight_golden.npz"
 
 spec = importlib.util.spec_from_file_location(

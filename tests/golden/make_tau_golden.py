@@ -1,7 +1,7 @@
 """Golden vectors of the reference's integrated-autocorrelation-time estimator.
 
-analysis/scripts/reproduce_validation.py of a faulknco/ising-rs checkout (default
-/root/reference) defines `autocorrelation` and `integrated_autocorrelation_time`
+Usage: python make_tau_golden.py <path of a faulknco/ising-rs checkout>.
+analysis/scripts/reproduce_validation.py of that checkout defines `autocorrelation` and `integrated_autocorrelation_time`
 (the windowed estimator with the self-consistent 6 tau window) but imports
 matplotlib and pandas at module level, which are not installed here.  So this
 script parses the file and executes only those two function definitions (numpy
@@ -15,7 +15,9 @@ from pathlib import Path
 
 import numpy as np
 
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit(f"usage: python {Path(__file__).name} <reference checkout>")
+REF = Path(sys.argv[1])
 OUT = Path(__file__).resolve().parent / "tau_golden.npz"
 WANT = {"autocorrelation", "integrated_autocorrelation_time"}
 

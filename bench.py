@@ -1067,9 +1067,12 @@ def ncu_case_graph(kind: str):
 
 
 def ncu_case():
+    """No timing: a few half-sweeps of the L=128 roofline case (128 replicas,
+    268 MB of spins) for ncu captures of the half-sweep kernel."""
     pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
-    b = pkg.IsingBatch([128], 96, seed=SEED)
-    b.set_temperatures([TMIN + (TMAX - TMIN) * i / 95 for i in range(96)])
+    R = HBM_REPLICAS
+    b = pkg.IsingBatch([128], R, seed=SEED + 7)
+    b.set_temperatures([TMIN + (TMAX - TMIN) * i / (R - 1) for i in range(R)])
     b.step(3)
     b.sync()
     print("ncu case done")
@@ -1097,7 +1100,7 @@ def main():
     ap.add_argument("--ncu-case", nargs="?", const="words",
                     choices=["words", "resident", "graph", "cgraph3", "cgraph2", "reweight",
                              "learned"],
-                    help="no timing: 'words' = a few half-sweeps of L=128 x 96 replicas (201 MB, "
+                    help="no timing: 'words' = a few half-sweeps of L=128 x 128 replicas (268 MB, "
                          "larger than L2) for an ncu capture of the half-sweep kernel; "
                          "'resident' = one 2000-sweep schedule of an L=30 lattice; "
                          "'graph'/'cgraph3'/'cgraph2' = one 100-sweep launch of the graph "

@@ -222,6 +222,15 @@ int isg_ising_set_launch(isg_ising* h, int threads, int blocks_per_sm);
  * 0 = automatic (2 when all spin planes fit in 96 MiB, else 1).  Results never
  * depend on it. */
 int isg_ising_set_prefetch(isg_ising* h, int depth);
+/* Rolling half-sweep (3D, L = 64..256): lanes of each warp also prefetch the
+ * lines of the task's own and other-colour words (and halo rows) `planes`
+ * z-planes ahead of the plane being updated into L1 (level 1) or L2 (level 2);
+ * planes = 0 turns it off (at most 16).  Results never depend on it. */
+int isg_ising_set_cache_prefetch(isg_ising* h, int level, int planes);
+/* Words of 4 sites each lane of the rolling half-sweep updates per plane for
+ * L >= 128: 4 (default; 128-bit loads and stores, 2 blocks per SM) or 2 (as
+ * for L = 64).  Results never depend on it. */
+int isg_ising_set_words_per_lane(isg_ising* h, int words);
 /* Time every supported launch shape (prefetch depth x site-kernel threads x
  * blocks per SM) on a scratch copy of the lattices and keep the fastest.
  * best[0..2] (may be NULL) receives threads, blocks/SM, prefetch depth. */

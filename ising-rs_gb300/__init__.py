@@ -105,6 +105,8 @@ def _declare(L):
         "isg_ising_set_launch": [vp, i32, i32],
         "isg_ising_autotune": [vp, vp],
         "isg_ising_set_prefetch": [vp, i32],
+        "isg_ising_set_cache_prefetch": [vp, i32, i32],
+        "isg_ising_set_words_per_lane": [vp, i32],
         "isg_ising_time_halfsweep": [vp, i32, vp],
         "isg_ising_time_halfsweep_graph": [vp, i32, i64, i32, vp],
         "isg_ising_sites_per_halfsweep": [vp, vp],
@@ -538,6 +540,15 @@ class IsingBatch:
     def set_prefetch(self, depth: int = 0) -> None:
         """Rolling prefetch depth 1 or 2 (0 = automatic); results never depend on it."""
         _check(lib().isg_ising_set_prefetch(self._h, int(depth)))
+
+    def set_cache_prefetch(self, level: int = 2, planes: int = 0) -> None:
+        """Rolling half-sweep: prefetch `planes` z-planes ahead into L1 (level 1)
+        or L2 (level 2); 0 planes = off."""
+        _check(lib().isg_ising_set_cache_prefetch(self._h, int(level), int(planes)))
+
+    def set_words_per_lane(self, words: int = 4) -> None:
+        """Rolling half-sweep, L >= 128: 4 or 2 words per lane (same results)."""
+        _check(lib().isg_ising_set_words_per_lane(self._h, int(words)))
 
     def autotune(self) -> tuple[int, int, int]:
         """Fastest (site threads, blocks per SM, prefetch depth), kept for the batch."""

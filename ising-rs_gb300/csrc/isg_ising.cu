@@ -62,10 +62,10 @@ constexpr int kMaxReplicas = 1024;
 
 // Task kinds of a lattice size (words of 4 same-colour sites of one colour
 // plane of one replica):
-//   kRolling (dim 3, L = 64, 128, 256): a warp task is the nr = 64/(L/8) rows
-//     of one y-block at one z, two adjacent words per lane; consecutive tasks
-//     of a size walk z, so a warp keeps the z-1, z, z+1 words of the other
-//     colour in registers.
+//   kRolling (dim 3, L = 64, 128, 256): a warp task is the rows of one y-block
+//     at one z, 2 adjacent words per lane (64 words, L = 64) or 4 (128 words,
+//     L >= 128); consecutive tasks of a size walk z, so a warp keeps the z-1,
+//     z, z+1 words of the other colour in registers.
 //   kFlat    (other power-of-two L with L/8 dividing 32): 32 consecutive words,
 //     one per lane.
 //   kSite    (any other even L): one thread per site (site kernel).
@@ -84,9 +84,12 @@ struct IsingClass {
     int64_t spin_off;         // byte offset of replica 0 colour 0
     int64_t task_base;        // word kinds: first warp task
     int64_t task_end;
-    int64_t ctask_base;       // word kinds: first CTA task (8 warp tasks)
-    int64_t ctask_end;
+    int64_t ctask_base;       // word kinds: first CTA task (8 warp tasks); rolling
+    int64_t ctask_end;        //   kinds count in work units (see log2_unit)
     int log2_groups;          // rolling: log2(column groups of 8 per replica)
+    int log2_wpl;             // rolling: log2(words per lane), 1 or 2
+    int log2_unit;            // rolling: a CTA task is 1 << log2_unit work units of 512 words
+    int log2_rpc;             // rolling: replicas per CTA task (plane of fewer than 8 y-blocks)
     int64_t site_base;        // site kind: first site (over colour planes)
     int64_t site_end;
 };
@@ -94,6 +97,7 @@ struct IsingClass {
 struct IsingParams {
     uint8_t* spins;                 // down bits: 1 for s = -1, 0 for s = +1
     const uint32_t* thr;            // [slots][16]
+    const uint32_t* thr8;           // [slots][4]: the thresholds as coarse bytes
     const int32_t* r2t;             // [replicas]
     unsigned long long* acc;        // [replicas][2] bond, mag
     const unsigned long long* ctrl; // ctrl[0] = global sweep base
@@ -101,9 +105,11 @@ struct IsingParams {
     int n_classes;
     int dim;
     int64_t total_tasks;
-    int64_t total_ctasks;     // rolling CTA tasks (contiguous ranges per block)
+    int64_t total_ctasks;     // rolling work units (contiguous ranges per block)
     int64_t flat_ctasks;      // flat CTA tasks (round-robin over blocks)
     int64_t total_sites;
+    int l2_ahead;             // rolling: planes ahead of z prefetched (0: off)
+    int pf_level;             // 1: into L1, 2: into L2
     uint32_t rk0[10], rk1[10];      // Philox round keys (constant-bank operands)
     IsingClass cls[kMaxClasses];
 };
@@ -179,6 +185,14 @@ __device__ __forceinline__ uint32_t pin(uint32_t x) {
     return x;
 }
 
+// Prefetch of the 128-byte line holding p into L1 or L2 (no register result).
+__device__ __forceinline__ void prefetch_line(const void* p, bool l1) {
+    if (l1)
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+    else
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ uint32_t lds_u8(uint32_t saddr) {
     uint32_t v;
     asm volatile("ld.shared.u8 %0, [%1];" : "=r"(v) : "r"(saddr) : "memory");
@@ -200,48 +214,70 @@ __device__ __forceinline__ uint2 lds_v2(uint32_t saddr) {
     return v;
 }
 
-// Per-warp threshold table in shared memory: entry own_down*8 + n_down is 8
-// bytes {thr & 0xFFFF0000, thr}.
+// Per-warp threshold table in shared memory: the 16 uint32 thresholds of the
+// warp's current replica, entry own_down*8 + n_down (read by fine decisions).
 __device__ __forceinline__ void load_table(uint32_t* tab, const IsingParams& P, int slot,
                                            int lane) {
     __syncwarp();
-    if (lane < 16) {
-        const uint32_t t = P.thr[slot * 16 + lane];
-        tab[2 * lane] = t & 0xFFFF0000u;
-        tab[2 * lane + 1] = t;
-    }
+    if (lane < 16) tab[lane] = P.thr[slot * 16 + lane];
     __syncwarp();
 }
 
-// New word of 4 same-colour sites: own down bits ow, down-neighbour counts nd
-// (per byte), table at shared address tbase (256-byte aligned), and the sites'
-// coarse 16-bit randoms in bits 16..31 of U0..U3 (bits 0..15 are ignored).
-// A site flips iff u = coarse << 16 | fine <= thr.  The coarse half decides
-// unless it equals thr's upper half; then (probability 2^-16 per site) the
-// fine halves of the word come from Philox counter 0x80000000 | wfine.
-__device__ __forceinline__ uint32_t metropolis_word(uint32_t ow, uint32_t nd, uint32_t tbase,
-                                                    uint32_t U0, uint32_t U1, uint32_t U2,
-                                                    uint32_t U3, const PhiloxPre& pre,
-                                                    const IsingParams& P, uint32_t wfine) {
-    // byte offsets 8*(n_down + 8*own_down) <= 120; the mask keeps every shared
-    // load aligned and inside the warp's 256-byte table whatever the bytes hold
-    const uint32_t idx8 = ((nd << 3) + (ow << 6)) & 0x78787878u;
-    const uint2 e0 = lds_v2(__byte_perm(idx8, tbase, 0x7650));
-    const uint2 e1 = lds_v2(__byte_perm(idx8, tbase, 0x7651));
-    const uint2 e2 = lds_v2(__byte_perm(idx8, tbase, 0x7652));
-    const uint2 e3 = lds_v2(__byte_perm(idx8, tbase, 0x7653));
-    uint32_t f = (U0 < e0.x ? 0x00000001u : 0u) | (U1 < e1.x ? 0x00000100u : 0u) |
-                 (U2 < e2.x ? 0x00010000u : 0u) | (U3 < e3.x ? 0x01000000u : 0u);
-    // tie: equal upper halves, i.e. U - T < 2^16 (T's lower half is zero)
-    const bool tie = min(min(U0 - e0.x, U1 - e1.x), min(U2 - e2.x, U3 - e3.x)) < 0x10000u;
-    if (tie) {
-        const U4 fn = philox_w(pre, P, 0x80000000u | wfine);
-        f = ((((U0 & 0xFFFF0000u) | (fn.x >> 16)) <= e0.y) ? 0x00000001u : 0u) |
-            ((((U1 & 0xFFFF0000u) | (fn.y >> 16)) <= e1.y) ? 0x00000100u : 0u) |
-            ((((U2 & 0xFFFF0000u) | (fn.z >> 16)) <= e2.y) ? 0x00010000u : 0u) |
-            ((((U3 & 0xFFFF0000u) | (fn.w >> 16)) <= e3.y) ? 0x01000000u : 0u);
-    }
-    return ow ^ f;
+// The same thresholds as bytes for the coarse decision, byte own_down*8 +
+// n_down of {t0,t1,t2,t3}: 0x80 for threshold 0xFFFFFFFF (always accept), else
+// threshold >> 25.
+struct Thr8 {
+    uint32_t t0, t1, t2, t3;
+};
+__device__ __forceinline__ Thr8 load_thr8(const IsingParams& P, int slot) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(P.thr8) + slot);
+    return Thr8{v.x, v.y, v.z, v.w};
+}
+
+// Coarse Metropolis decision of a word of 4 same-colour sites, byte-parallel.
+// ow: own down bits (bytes 0/1); nd: down-neighbour counts (bytes 0..6);
+// U: the word's Philox word, byte j holding site j's coarse random in its low
+// 7 bits (bit 7 ignored).  Per byte, with T the threshold byte of (own, nd),
+// D = T + (0x7F - c): bit 7 is set iff c < T (the coarse random decides
+// acceptance), and D == 0x7F iff c == T (a tie, decided by the fine bits).
+// No byte carries into the next (T <= 0x80, c <= 0x7F).  Returns the flip mask
+// (0x01 per accepted byte) and D.
+__device__ __forceinline__ uint32_t coarse_flips(uint32_t ow, uint32_t nd, uint32_t U,
+                                                 const Thr8& T, uint32_t& D) {
+    const uint32_t sel = __byte_perm(nd | (nd >> 4), 0u, 0x0020u);  // nibbles n_down
+    const uint32_t lo = __byte_perm(T.t0, T.t1, sel);                // own up
+    const uint32_t hi = __byte_perm(T.t2, T.t3, sel);                // own down
+    const uint32_t m = ow * 0xFFu;
+    D = ((lo & ~m) | (hi & m)) + (~U & 0x7F7F7F7Fu);
+    return (D >> 7) & 0x01010101u;
+}
+// Any tie in the word (some byte of D equal to 0x7F).
+__device__ __forceinline__ bool any_tie(uint32_t D) {
+    const uint32_t x = D ^ 0x7F7F7F7Fu;
+    return ((x - 0x01010101u) & ~x & 0x80808080u) != 0u;
+}
+// Exactly the tied bytes: 0x80 in each byte of D equal to 0x7F.
+__device__ __forceinline__ uint32_t tie_bytes(uint32_t D) {
+    const uint32_t x = D ^ 0x7F7F7F7Fu;
+    return ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x | 0x7F7F7F7Fu);
+}
+// Fine decision of the tied sites (0x80 per byte of tmask) of word w: idx
+// holds own_down*8 + n_down per byte, tab the replica's thresholds.  A tied
+// site flips iff the top 25 bits of word j of the fine block 0x80000000 | w are
+// <= the low 25 bits of its threshold (the top 7 are the coarse random).
+__device__ __forceinline__ uint32_t fine_flips(uint32_t tmask, uint32_t idx, const uint32_t* tab,
+                                               const PhiloxPre& pre, const IsingParams& P,
+                                               uint32_t w) {
+    const U4 f = philox_w(pre, P, 0x80000000u | w);
+    const uint32_t fw[4] = {f.x, f.y, f.z, f.w};
+    uint32_t flip = 0u;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (tmask & (0x80u << (8 * j))) {
+            const uint32_t t = tab[(idx >> (8 * j)) & 15u];
+            if ((fw[j] >> 7) <= (t & 0x1FFFFFFu)) flip |= 1u << (8 * j);
+        }
+    return flip;
 }
 
 __device__ __forceinline__ void flush_acc(unsigned long long* acc, int rep, long long b,
@@ -285,26 +321,93 @@ __device__ __forceinline__ uint2 ldg_u2(const uint32_t* p) {
     asm volatile("ld.global.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
     return v;
 }
+__device__ __forceinline__ uint4 ldg_nc4(const uint32_t* p) {
+    uint4 v;
+    asm volatile("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint4 ldg_u4(const uint32_t* p) {
+    uint4 v;
+    asm volatile("ld.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p));
+    return v;
+}
+
+// Ties of the rolling half-sweep are resolved later in the same launch, 32 at
+// a time: a tied site keeps its spin provisionally and its word joins the
+// warp's queue {word index, per byte: own_down*8 + n_down | 0x10 if tied}.
+// The fine decision only depends on the site's own spin, its neighbours of the
+// other colour (unchanged during the half-sweep) and its own random bits, so
+// deferring it leaves every result bit as the immediate decision would.
+constexpr uint32_t kTieQ = 256;  // entries per warp (at most 31 + 128 pending)
+
+struct TieQueue {
+    uint32_t head, tail;  // warp-uniform
+};
+
+// Resolve `count` (1..32) queued entries from head: lane l takes entry
+// head + l, draws its fine block, flips the accepted sites of the word in
+// place (atomic XOR: the word was stored by another lane of the warp) and
+// corrects the measurement sums of the provisional state.
+template <int MODE>
+__device__ __forceinline__ void resolve_ties(const uint2* q, uint32_t head, uint32_t count,
+                                             int lane, const uint32_t* tab, const PhiloxPre& pre,
+                                             const IsingParams& P, uint32_t* own, MeasAcc& macc) {
+    __syncwarp();
+    if ((uint32_t)lane < count) {
+        const uint2 e = q[(head + (uint32_t)lane) & (kTieQ - 1)];
+        const uint32_t idx = e.y & 0x0F0F0F0Fu;
+        const uint32_t flip = fine_flips((e.y & 0x10101010u) << 3, idx, tab, pre, P, e.x);
+        if (flip) {
+            atomicXor(own + e.x, flip);
+            if (MODE == 1) {
+                // flipped sites leave their provisional state: down bit o -> o^1
+                const uint32_t od = (idx >> 3) & flip, ou = flip & ~od;
+                const uint32_t nd = idx & 0x07070707u;
+                macc.so += (int)__dp4a(ou, 0x01010101u, 0u) - (int)__dp4a(od, 0x01010101u, 0u);
+                macc.sond += (int)__dp4a(ou, nd, 0u) - (int)__dp4a(od, nd, 0u);
+            }
+        }
+    }
+    __syncwarp();
+}
+
+template <int MODE>
+__device__ __forceinline__ void drain_ties(const uint2* q, TieQueue& tq, int lane,
+                                           const uint32_t* tab, const PhiloxPre& pre,
+                                           const IsingParams& P, uint32_t* own, MeasAcc& macc) {
+    while (tq.tail != tq.head) {
+        const uint32_t c = min(tq.tail - tq.head, 32u);
+        resolve_ties<MODE>(q, tq.head, c, lane, tab, pre, P, own, macc);
+        tq.head += c;
+    }
+}
 
 // One z-step of a rolling column at plane offset `o` (words).  A lane owns two
 // adjacent words (x, y) of a row: their new own words from the other colour's
 // word pairs at z-1, z, z+1 (zm, za, zp) and the halo pair h0 (row y-1 on the
 // first row of the task, y+1 on the last), with the loads of plane z+PF (own,
 // halo) and z+PF+1 (other colour) issued first; PF = 2 keeps one more pair of
-// each in flight (q*).  HI selects the upper halves of the z pair's random
-// words (odd z).  x neighbours: with px = (y + z + colour) & 1 the other
-// colour's bytes at x - 1 + px are bytes {1,2,3} of a word + byte 0 of the
-// next word (px = 1), or byte 3 of the previous word + bytes {0,1,2} (px = 0);
-// one of the two is the lane's own other word, the other comes by one shuffle
-// from the neighbour lane of the row (src_x, whose px is the same).
-template <int MODE, bool HI, int PF>
+// each in flight (q*).  Ua / Ub: the Philox words (word z & 3 of the z quad's
+// blocks) of the two words.  x neighbours: with px = (y + z + colour) & 1 the
+// other colour's bytes at x - 1 + px are bytes {1,2,3} of a word + byte 0 of
+// the next word (px = 1), or byte 3 of the previous word + bytes {0,1,2}
+// (px = 0); one of the two is the lane's own other word, the other comes by
+// one shuffle from the neighbour lane of the row (src_x, whose px is the same).
+template <int MODE, int PF>
 __device__ __forceinline__ void rolling_pair_step(
-    const IsingParams& P, const PhiloxPre& pre, uint32_t tbase, const U4& ua, const U4& ub,
+    const IsingParams& P, const PhiloxPre& pre, const Thr8& T8, uint32_t Ua, uint32_t Ub,
     const uint32_t* oc, const uint32_t* oa, uint32_t* mc, uint32_t col, uint32_t pz,
     uint32_t pwm, bool first, bool last, int src_up, int src_dn, int src_x, bool px,
     uint32_t sel_x, uint32_t& o, uint2& zm, uint2& za, uint2& zp, uint2& qzp, uint2& h0,
-    uint2& qh0, uint2& ow, uint2& qow, MeasAcc& macc) {
+    uint2& qh0, uint2& ow, uint2& qow, MeasAcc& macc, const uint32_t* pfb, uint32_t pfo,
+    bool pf_lane, uint2* q, TieQueue& tq, int lane, const uint32_t* tab, uint32_t* own) {
     const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm;
+    // lanes 0..5 pull the lines of plane z + l2_ahead the warp will load
+    if (pf_lane) prefetch_line(pfb + ((o + pfo) & pwm), P.pf_level == 1);
     uint2 n_zp, n_h0, n_ow;
     if constexpr (PF == 1) {
         n_zp = ldg_nc2(oc + o2);
@@ -327,20 +430,136 @@ __device__ __forceinline__ void rolling_pair_step(
     const uint32_t nd1 = (wx1 + za.y + (last ? h0.y : upy)) + ((first ? h0.y : dny) + zp.y + zm.y);
     uint2 nw = ow;
     if (MODE != 2) {
-        if (HI) {
-            nw.x = metropolis_word(ow.x, nd0, tbase, ua.x, ua.y, ua.z, ua.w, pre, P, o + col);
-            nw.y = metropolis_word(ow.y, nd1, tbase, ub.x, ub.y, ub.z, ub.w, pre, P, o + col + 1);
-        } else {
-            nw.x = metropolis_word(ow.x, nd0, tbase, ua.x << 16, ua.y << 16, ua.z << 16,
-                                   ua.w << 16, pre, P, o + col);
-            nw.y = metropolis_word(ow.y, nd1, tbase, ub.x << 16, ub.y << 16, ub.z << 16,
-                                   ub.w << 16, pre, P, o + col + 1);
-        }
+        uint32_t d0, d1;
+        nw.x = ow.x ^ coarse_flips(ow.x, nd0, Ua, T8, d0);
+        nw.y = ow.y ^ coarse_flips(ow.y, nd1, Ub, T8, d1);
         *reinterpret_cast<uint2*>(mc + o) = nw;
+        const bool t0 = any_tie(d0), t1 = any_tie(d1);
+        if (__any_sync(ISG_FULL_MASK, t0 || t1)) {
+            const uint32_t b0 = __ballot_sync(ISG_FULL_MASK, t0);
+            const uint32_t b1 = __ballot_sync(ISG_FULL_MASK, t1);
+            const uint32_t lt = (1u << lane) - 1u;
+            if (t0)
+                q[(tq.tail + __popc(b0 & lt)) & (kTieQ - 1)] =
+                    make_uint2(o + col, (nd0 + (ow.x << 3)) | (tie_bytes(d0) >> 3));
+            tq.tail += __popc(b0);
+            if (t1)
+                q[(tq.tail + __popc(b1 & lt)) & (kTieQ - 1)] =
+                    make_uint2(o + col + 1, (nd1 + (ow.y << 3)) | (tie_bytes(d1) >> 3));
+            tq.tail += __popc(b1);
+            while (tq.tail - tq.head >= 32u) {
+                resolve_ties<MODE>(q, tq.head, 32u, lane, tab, pre, P, own, macc);
+                tq.head += 32u;
+            }
+        }
     }
     if (MODE != 0) {
         meas_add(macc, nw.x, nd0, za.x);
         meas_add(macc, nw.y, nd1, za.y);
+    }
+    zm = za;
+    za = zp;
+    if constexpr (PF == 1) {
+        zp = n_zp;
+        h0 = n_h0;
+        ow = n_ow;
+    } else {
+        zp = qzp;
+        qzp = n_zp;
+        h0 = qh0;
+        qh0 = n_h0;
+        ow = qow;
+        qow = n_ow;
+    }
+    o = o1;
+}
+
+// Queue the tied sites of one word (lane-varying t; warp-uniform call).
+__device__ __forceinline__ void queue_word(uint2* q, TieQueue& tq, bool t, uint32_t lt,
+                                           uint32_t w, uint32_t own_w, uint32_t nd,
+                                           uint32_t d) {
+    const uint32_t b = __ballot_sync(ISG_FULL_MASK, t);
+    if (t)
+        q[(tq.tail + __popc(b & lt)) & (kTieQ - 1)] =
+            make_uint2(w, (nd + (own_w << 3)) | (tie_bytes(d) >> 3));
+    tq.tail += __popc(b);
+}
+
+// One z-step of a rolling column with four adjacent words per lane (L >=
+// 128): as rolling_pair_step, with 128-bit loads and stores.  U0..U3: the
+// Philox words of the four word columns for this plane.  x neighbours: the
+// lane's words k-1 / k+1 and, at the row edge of the lane, word 0 of the next
+// lane (px = 1) or word 3 of the previous lane (px = 0) by one shuffle.
+template <int MODE, int PF>
+__device__ __forceinline__ void rolling_quad_step(
+    const IsingParams& P, const PhiloxPre& pre, const Thr8& T8, uint32_t U0, uint32_t U1,
+    uint32_t U2, uint32_t U3, const uint32_t* oc, const uint32_t* oa, uint32_t* mc, uint32_t col,
+    uint32_t pz, uint32_t pwm, bool first, bool last, int src_up, int src_dn, int src_x, bool px,
+    uint32_t sel_x, uint32_t& o, uint4& zm, uint4& za, uint4& zp, uint4& qzp, uint4& h0,
+    uint4& qh0, uint4& ow, uint4& qow, MeasAcc& macc, const uint32_t* pfb, uint32_t pfo,
+    bool pf_lane, uint2* q, TieQueue& tq, int lane, const uint32_t* tab, uint32_t* own) {
+    const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm;
+    if (pf_lane) prefetch_line(pfb + ((o + pfo) & pwm), P.pf_level == 1);
+    uint4 n_zp, n_h0, n_ow;
+    if constexpr (PF == 1) {
+        n_zp = ldg_nc4(oc + o2);
+        n_h0 = ldg_nc4(oa + o1);
+        n_ow = ldg_u4(mc + o1);
+    } else {
+        const uint32_t o3 = (o + 3 * pz) & pwm;
+        n_zp = ldg_nc4(oc + o3);
+        n_h0 = ldg_nc4(oa + o2);
+        n_ow = ldg_u4(mc + o2);
+    }
+    // y neighbours: rows y+1 (up) and y-1 (down) of the task by shuffle, the
+    // halo row for the last (up) and first (down) row
+    uint4 yu, yd;
+    yu.x = __shfl_sync(ISG_FULL_MASK, za.x, src_up);
+    yu.y = __shfl_sync(ISG_FULL_MASK, za.y, src_up);
+    yu.z = __shfl_sync(ISG_FULL_MASK, za.z, src_up);
+    yu.w = __shfl_sync(ISG_FULL_MASK, za.w, src_up);
+    yd.x = __shfl_sync(ISG_FULL_MASK, za.x, src_dn);
+    yd.y = __shfl_sync(ISG_FULL_MASK, za.y, src_dn);
+    yd.z = __shfl_sync(ISG_FULL_MASK, za.z, src_dn);
+    yd.w = __shfl_sync(ISG_FULL_MASK, za.w, src_dn);
+    const uint32_t nb = __shfl_sync(ISG_FULL_MASK, px ? za.x : za.w, src_x);
+    // px = 1: bytes {1,2,3} of word k + byte 0 of word k+1; px = 0: byte 3 of
+    // word k-1 + bytes {0,1,2} of word k (selects, px differs between rows)
+    uint4 wx;
+    wx.x = __byte_perm(za.x, px ? za.y : nb, sel_x);
+    wx.y = __byte_perm(za.y, px ? za.z : za.x, sel_x);
+    wx.z = __byte_perm(za.z, px ? za.w : za.y, sel_x);
+    wx.w = __byte_perm(za.w, px ? nb : za.z, sel_x);
+    const uint32_t nd0 = (wx.x + za.x + (last ? h0.x : yu.x)) + ((first ? h0.x : yd.x) + zp.x + zm.x);
+    const uint32_t nd1 = (wx.y + za.y + (last ? h0.y : yu.y)) + ((first ? h0.y : yd.y) + zp.y + zm.y);
+    const uint32_t nd2 = (wx.z + za.z + (last ? h0.z : yu.z)) + ((first ? h0.z : yd.z) + zp.z + zm.z);
+    const uint32_t nd3 = (wx.w + za.w + (last ? h0.w : yu.w)) + ((first ? h0.w : yd.w) + zp.w + zm.w);
+    uint4 nw = ow;
+    if (MODE != 2) {
+        uint32_t d0, d1, d2, d3;
+        nw.x = ow.x ^ coarse_flips(ow.x, nd0, U0, T8, d0);
+        nw.y = ow.y ^ coarse_flips(ow.y, nd1, U1, T8, d1);
+        nw.z = ow.z ^ coarse_flips(ow.z, nd2, U2, T8, d2);
+        nw.w = ow.w ^ coarse_flips(ow.w, nd3, U3, T8, d3);
+        *reinterpret_cast<uint4*>(mc + o) = nw;
+        const bool t0 = any_tie(d0), t1 = any_tie(d1), t2 = any_tie(d2), t3 = any_tie(d3);
+        if (__any_sync(ISG_FULL_MASK, t0 || t1 || t2 || t3)) {
+            const uint32_t lt = (1u << lane) - 1u;
+            queue_word(q, tq, t0, lt, o + col, ow.x, nd0, d0);
+            queue_word(q, tq, t1, lt, o + col + 1, ow.y, nd1, d1);
+            queue_word(q, tq, t2, lt, o + col + 2, ow.z, nd2, d2);
+            queue_word(q, tq, t3, lt, o + col + 3, ow.w, nd3, d3);
+            while (tq.tail - tq.head >= 32u) {
+                resolve_ties<MODE>(q, tq.head, 32u, lane, tab, pre, P, own, macc);
+                tq.head += 32u;
+            }
+        }
+    }
+    if (MODE != 0) {
+        meas_add(macc, nw.x, nd0, za.x);
+        meas_add(macc, nw.y, nd1, za.y);
+        meas_add(macc, nw.z, nd2, za.z);
+        meas_add(macc, nw.w, nd3, za.w);
     }
     zm = za;
     za = zp;
@@ -371,31 +590,40 @@ __device__ __forceinline__ void rolling_pair_step(
 // PF: rolling loads issued PF planes ahead (1: 3 blocks per SM, 2: 2 blocks
 // per SM with more loads in flight per warp); chosen per batch (configure_launch,
 // isg_ising_autotune).
-template <int DIM, int MODE, int PF>
-__global__ void __launch_bounds__(256, PF == 1 ? 3 : 2)
+// WMAX: 4 if some size runs four words per lane (that path needs more
+// registers: 2 blocks per SM), else 2.
+template <int DIM, int MODE, int PF, int WMAX>
+__global__ void __launch_bounds__(256, (PF == 1 && WMAX == 2) ? 3 : 2)
     k_ising_words(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
-    __shared__ __align__(256) uint32_t s_thr[8][64];
+    __shared__ uint32_t s_thr[8][16];
+    __shared__ uint2 s_q[8][kTieQ];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    // rolling ranges start and end on even CTA tasks, i.e. on even z (L and
-    // every size's task count are even), so each range is whole z pairs
+    // rolling ranges (in work units of 512 words: one CTA task of two words
+    // per lane, half of one of four) start and end on multiples of 8 units,
+    // i.e. on z = 0 mod 4 (every size's unit count is a multiple of 8), so
+    // each range is whole z quads
     const int64_t G = P.total_ctasks;
-    int64_t ct = ((int64_t)blockIdx.x * G / gridDim.x) & ~(int64_t)1;
+    int64_t ct = ((int64_t)blockIdx.x * G / gridDim.x) & ~(int64_t)7;
     const int64_t ct_end = blockIdx.x + 1 == gridDim.x
                                ? G
-                               : (((int64_t)(blockIdx.x + 1) * G / gridDim.x) & ~(int64_t)1);
+                               : (((int64_t)(blockIdx.x + 1) * G / gridDim.x) & ~(int64_t)7);
     int64_t ft = blockIdx.x;  // flat CTA tasks: blockIdx.x, + gridDim.x, ...
 
     const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
     const uint32_t c2 = (uint32_t)sweep;
     const uint32_t c3 = counter_word3(ISG_TAG_ISING, (uint32_t)colour, sweep);
-    const uint32_t tbase = pin((uint32_t)__cvta_generic_to_shared(&s_thr[wib][0]));
+    const uint32_t* tab = s_thr[wib];
+    uint2* q = s_q[wib];
     constexpr int Z = 2 * DIM;
 
     int ci = 0;
     int cur_rep = -1;
+    uint32_t* cur_own = nullptr;  // own plane of cur_rep (queued ties refer to it)
     MeasAcc macc{0, 0, 0, 0, 0};
     PhiloxPre pre{};
+    Thr8 T8{0u, 0u, 0u, 0u};
+    TieQueue tq{0u, 0u};
 
     while (ct < ct_end || ft < P.flat_ctasks) {
         // flat tasks first (short, latency-bound), spread over all blocks
@@ -406,110 +634,157 @@ __global__ void __launch_bounds__(256, PF == 1 ? 3 : 2)
                (P.cls[ci].kind != (flat_now ? kFlat : kRolling) || P.cls[ci].ctask_end <= key))
             ++ci;
         const IsingClass& C = P.cls[ci];
-        const int64_t lct = key - C.ctask_base;
+        const int64_t lct = flat_now ? key - C.ctask_base : (key - C.ctask_base) >> C.log2_unit;
         const uint32_t L = (uint32_t)C.L, Lm = L - 1;
         const int lrw = C.log2_rw;
         const uint32_t rw = 1u << lrw, rwm = rw - 1;
         const uint32_t k4 = (uint32_t)lane & rwm;
         const int src_prev = lane - (int)k4 + (int)((k4 - 1) & rwm);
         const int src_next = lane - (int)k4 + (int)((k4 + 1) & rwm);
+        int r;
+        uint32_t z0 = 0, z1 = 0, yb = 0;
+        int64_t wt = 0;
+        if (DIM == 3 && !flat_now) {
+            // CTA task -> (replica group, column group g, z), z fastest; warp
+            // wib takes y-block (g << lc) + (wib mod 2^lc) of replica
+            // group * rpc + (wib >> lc), lc = log2(y-blocks per CTA task)
+            const int lg = C.log2_groups + C.log2L;
+            const int lc = 3 - C.log2_rpc;
+            r = (int)(lct >> lg) * (1 << C.log2_rpc) + (wib >> lc);
+            const uint32_t rem = (uint32_t)(lct & (((int64_t)1 << lg) - 1));
+            z0 = rem & Lm;
+            yb = ((rem >> C.log2L) << lc) + ((uint32_t)wib & ((1u << lc) - 1));
+            const int64_t zlim = (int64_t)z0 + ((ct_end - ct) >> C.log2_unit);
+            z1 = (uint32_t)(zlim < (int64_t)L ? zlim : (int64_t)L);
+            ct += (int64_t)(z1 - z0) << C.log2_unit;
+            if (r >= C.R) continue;  // the last replica group may be short
+        } else {
+            // flat: warp task 8*lct + wib of this size
+            wt = (lct << 3) + wib;
+            ft += gridDim.x;
+            if (wt >= C.task_end - C.task_base) continue;
+            r = (int)(wt >> C.log2_tpp);
+        }
+        const int rg = C.rep_base + r;
+        uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
+        uint32_t* own = reinterpret_cast<uint32_t*>(base + (int64_t)colour * C.plane_sites);
+        const uint32_t* oth =
+            reinterpret_cast<const uint32_t*>(base + (int64_t)(colour ^ 1) * C.plane_sites);
+        if (rg != cur_rep) {
+            if (MODE != 2) drain_ties<MODE>(q, tq, lane, tab, pre, P, cur_own, macc);
+            if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
+            cur_rep = rg;
+            cur_own = own;
+            if (MODE != 2) {
+                const int slot = C.rep_base + P.r2t[rg];
+                load_table(s_thr[wib], P, slot, lane);
+                T8 = load_thr8(P, slot);
+                pre = philox_pre(replica_uid(C.L, r), c2, c3, P.rk0[0], P.rk1[0]);
+            }
+        }
 
         if (DIM == 3 && !flat_now) {
-            // CTA task -> (replica r, column group g, z), z fastest
-            const int lg = C.log2_groups + C.log2L;
-            const int r = (int)(lct >> lg);
-            const uint32_t rem = (uint32_t)(lct & (((int64_t)1 << lg) - 1));
-            const uint32_t z0 = rem & Lm;
-            const uint32_t g = rem >> C.log2L;
-            const int64_t zlim = (int64_t)z0 + (ct_end - ct);
-            const uint32_t z1 = (uint32_t)(zlim < (int64_t)L ? zlim : (int64_t)L);
-            ct += z1 - z0;
-            const int rg = C.rep_base + r;
-            if (rg != cur_rep) {
-                if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
-                cur_rep = rg;
-                if (MODE != 2) {
-                    load_table(s_thr[wib], P, C.rep_base + P.r2t[rg], lane);
-                    pre = philox_pre(replica_uid(C.L, r), c2, c3, P.rk0[0], P.rk1[0]);
-                }
-            }
-            uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
-            uint32_t* own = reinterpret_cast<uint32_t*>(base + (int64_t)colour * C.plane_sites);
-            const uint32_t* oth =
-                reinterpret_cast<const uint32_t*>(base + (int64_t)(colour ^ 1) * C.plane_sites);
-            // a warp task: 64 words (nr rows of rw words), two adjacent words
-            // per lane; rw >= 8 (L >= 64), so every row has >= 4 lanes and a
-            // task >= 2 rows (L <= 256)
-            const uint32_t yb = (g << 3) + (uint32_t)wib;
+            // a warp task: 32 * wpl words (nr rows of rw words), wpl = 2 or 4
+            // adjacent words per lane; every row has >= 4 lanes and a task
+            // >= 2 rows (L = 64..256)
+            const int lw = C.log2_wpl;
             const uint32_t pz = L << lrw;          // words per z-plane
             const uint32_t pwm = (pz << C.log2L) - 1;  // plane words - 1 (power of two)
-            const int lh = lrw - 1;                // log2(lanes per row)
+            const int lh = lrw - lw;               // log2(lanes per row)
             const uint32_t k2 = (uint32_t)lane & ((1u << lh) - 1);
-            const uint32_t col = (yb << 6) + 2 * (uint32_t)lane;  // the lane's first word
+            const uint32_t col = (yb << (5 + lw)) + ((uint32_t)lane << lw);  // the lane's first word
             const uint32_t rb = (uint32_t)lane >> lh, nr = 32u >> lh;
             const uint32_t y = yb * nr + rb;
             const bool first = rb == 0, last = rb == nr - 1;
-            const uint32_t ha = (((first ? y - 1 : y + 1) & Lm) << lrw) | (2 * k2);
+            const uint32_t ha = (((first ? y - 1 : y + 1) & Lm) << lrw) | (k2 << lw);
             const int src_up = (lane + (1 << lh)) & 31, src_dn = (lane - (1 << lh)) & 31;
             const uint32_t km = (1u << lh) - 1;
-            const int src_prev = lane - (int)k2 + (int)((k2 - 1) & km);
-            const int src_next = lane - (int)k2 + (int)((k2 + 1) & km);
+            const int src_prev2 = lane - (int)k2 + (int)((k2 - 1) & km);
+            const int src_next2 = lane - (int)k2 + (int)((k2 + 1) & km);
             const uint32_t* oc = oth + col;   // column base pointers
             const uint32_t* oa = oth + ha;
             uint32_t* mc = own + col;
+            // cache prefetch: lanes [0, n) the n = 2^lw 128-byte lines of the
+            // task's own words, [n, 2n) those of the other colour, 2n and
+            // 2n + 1 the lines of the other colour's halo rows
+            const int nlines = 1 << lw;
+            const bool pf_lane = P.l2_ahead > 0 && lane < 2 * nlines + 2;
+            const uint32_t y0 = yb * nr;
+            const uint32_t* pfb =
+                lane < 2 * nlines
+                    ? (lane < nlines ? (const uint32_t*)own : oth) + (yb << (5 + lw)) +
+                          32u * (uint32_t)(lane & (nlines - 1))
+                    : oth + ((((lane == 2 * nlines ? y0 - 1 : y0 + nr) & Lm) << lrw) & ~31u);
+            const uint32_t pfo = (uint32_t)P.l2_ahead * pz;
             // x-neighbour parity at even z (z0 is even) and at odd z
             const bool pe = ((y + (uint32_t)colour) & 1u) != 0;
-            const int src_lo = pe ? src_next : src_prev, src_hi = pe ? src_prev : src_next;
+            const int src_lo = pe ? src_next2 : src_prev2, src_hi = pe ? src_prev2 : src_next2;
             const uint32_t sel_lo = pe ? 0x4321u : 0x2107u, sel_hi = pe ? 0x2107u : 0x4321u;
             uint32_t o = z0 * pz;                        // offset of plane z
-            uint2 zm = ldg_nc2(oc + ((o - pz) & pwm));
-            uint2 za = ldg_nc2(oc + o);
-            uint2 zp = ldg_nc2(oc + ((o + pz) & pwm));
-            uint2 h0 = ldg_nc2(oa + o);
-            uint2 ow = ldg_u2(mc + o);
-            uint2 qzp{0u, 0u}, qh0{0u, 0u}, qow{0u, 0u};
-            if constexpr (PF == 2) {
-                qzp = ldg_nc2(oc + ((o + 2 * pz) & pwm));
-                qh0 = ldg_nc2(oa + ((o + pz) & pwm));
-                qow = ldg_u2(mc + ((o + pz) & pwm));
-            }
-            // z pairs (2k, 2k+1) share one Philox block per word: counter
-            // (z>>1)*pz + word, lower 16-bit halves for even z, upper for odd z
-            for (uint32_t z = z0; z < z1; z += 2) {
-                U4 ua{}, ub{};
-                if (MODE != 2) {
-                    ua = philox_w(pre, P, (o >> 1) + col);
-                    ub = philox_w(pre, P, (o >> 1) + col + 1);
+            if (WMAX == 4 && lw == 2) {
+                uint4 zm = ldg_nc4(oc + ((o - pz) & pwm));
+                uint4 za = ldg_nc4(oc + o);
+                uint4 zp = ldg_nc4(oc + ((o + pz) & pwm));
+                uint4 h0 = ldg_nc4(oa + o);
+                uint4 ow = ldg_u4(mc + o);
+                uint4 qzp{0u, 0u, 0u, 0u}, qh0{0u, 0u, 0u, 0u}, qow{0u, 0u, 0u, 0u};
+                if constexpr (PF == 2) {
+                    qzp = ldg_nc4(oc + ((o + 2 * pz) & pwm));
+                    qh0 = ldg_nc4(oa + ((o + pz) & pwm));
+                    qow = ldg_u4(mc + ((o + pz) & pwm));
                 }
-                rolling_pair_step<MODE, false, PF>(P, pre, tbase, ua, ub, oc, oa, mc, col, pz,
-                                                   pwm, first, last, src_up, src_dn, src_lo, pe,
-                                                   sel_lo, o, zm, za, zp, qzp, h0, qh0, ow, qow,
-                                                   macc);
-                rolling_pair_step<MODE, true, PF>(P, pre, tbase, ua, ub, oc, oa, mc, col, pz,
-                                                  pwm, first, last, src_up, src_dn, src_hi, !pe,
-                                                  sel_hi, o, zm, za, zp, qzp, h0, qh0, ow, qow,
-                                                  macc);
+                // z quads (4k .. 4k+3) share one Philox block per word column:
+                // counter (z>>2)*pz + word, Philox word z & 3 for plane z
+                for (uint32_t z = z0; z < z1; z += 4) {
+                    U4 u0{}, u1{}, u2{}, u3{};
+                    if (MODE != 2) {
+                        u0 = philox_w(pre, P, (o >> 2) + col);
+                        u1 = philox_w(pre, P, (o >> 2) + col + 1);
+                        u2 = philox_w(pre, P, (o >> 2) + col + 2);
+                        u3 = philox_w(pre, P, (o >> 2) + col + 3);
+                    }
+#define ISG_ROLL4(W, SRC, PX, SEL)                                                            \
+    rolling_quad_step<MODE, PF>(P, pre, T8, u0.W, u1.W, u2.W, u3.W, oc, oa, mc, col, pz, pwm,  \
+                                first, last, src_up, src_dn, SRC, PX, SEL, o, zm, za, zp, qzp, \
+                                h0, qh0, ow, qow, macc, pfb, pfo, pf_lane, q, tq, lane, tab,   \
+                                own)
+                    ISG_ROLL4(x, src_lo, pe, sel_lo);
+                    ISG_ROLL4(y, src_hi, !pe, sel_hi);
+                    ISG_ROLL4(z, src_lo, pe, sel_lo);
+                    ISG_ROLL4(w, src_hi, !pe, sel_hi);
+#undef ISG_ROLL4
+                }
+            } else {
+                uint2 zm = ldg_nc2(oc + ((o - pz) & pwm));
+                uint2 za = ldg_nc2(oc + o);
+                uint2 zp = ldg_nc2(oc + ((o + pz) & pwm));
+                uint2 h0 = ldg_nc2(oa + o);
+                uint2 ow = ldg_u2(mc + o);
+                uint2 qzp{0u, 0u}, qh0{0u, 0u}, qow{0u, 0u};
+                if constexpr (PF == 2) {
+                    qzp = ldg_nc2(oc + ((o + 2 * pz) & pwm));
+                    qh0 = ldg_nc2(oa + ((o + pz) & pwm));
+                    qow = ldg_u2(mc + ((o + pz) & pwm));
+                }
+                for (uint32_t z = z0; z < z1; z += 4) {
+                    U4 ua{}, ub{};
+                    if (MODE != 2) {
+                        ua = philox_w(pre, P, (o >> 2) + col);
+                        ub = philox_w(pre, P, (o >> 2) + col + 1);
+                    }
+#define ISG_ROLL_STEP(UA, UB, SRC, PX, SEL)                                                    \
+    rolling_pair_step<MODE, PF>(P, pre, T8, UA, UB, oc, oa, mc, col, pz, pwm, first, last,   \
+                                src_up, src_dn, SRC, PX, SEL, o, zm, za, zp, qzp, h0, qh0, ow, \
+                                qow, macc, pfb, pfo, pf_lane, q, tq, lane, tab, own)
+                    ISG_ROLL_STEP(ua.x, ub.x, src_lo, pe, sel_lo);
+                    ISG_ROLL_STEP(ua.y, ub.y, src_hi, !pe, sel_hi);
+                    ISG_ROLL_STEP(ua.z, ub.z, src_lo, pe, sel_lo);
+                    ISG_ROLL_STEP(ua.w, ub.w, src_hi, !pe, sel_hi);
+#undef ISG_ROLL_STEP
+                }
             }
         } else {
-            // flat: warp task 8*lct + wib of this size
-            const int64_t wt = (lct << 3) + wib;
-            ft += gridDim.x;
-            if (wt >= C.task_end - C.task_base) continue;
-            const int r = (int)(wt >> C.log2_tpp);
             const uint32_t tl = (uint32_t)(wt & (int64_t)(C.tasks_per_plane - 1));
-            const int rg = C.rep_base + r;
-            if (rg != cur_rep) {
-                if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
-                cur_rep = rg;
-                if (MODE != 2) {
-                    load_table(s_thr[wib], P, C.rep_base + P.r2t[rg], lane);
-                    pre = philox_pre(replica_uid(C.L, r), c2, c3, P.rk0[0], P.rk1[0]);
-                }
-            }
-            uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
-            uint32_t* own = reinterpret_cast<uint32_t*>(base + (int64_t)colour * C.plane_sites);
-            const uint32_t* oth =
-                reinterpret_cast<const uint32_t*>(base + (int64_t)(colour ^ 1) * C.plane_sites);
             const uint32_t w = (tl << 5) + (uint32_t)lane;
             const uint32_t row = w >> lrw;
             uint32_t y, z;
@@ -543,18 +818,20 @@ __global__ void __launch_bounds__(256, PF == 1 ? 3 : 2)
             const uint32_t ow = own[w];
             uint32_t nw = ow;
             if (MODE != 2) {
-                // z (3D) or y (2D) pair of this word: one Philox block, halves by parity
+                // z (3D) or y (2D) quad of this word: one Philox block, word t & 3
                 const uint32_t t = DIM == 3 ? z : y;
                 const uint32_t slab = DIM == 3 ? (L << lrw) : rw;
-                const U4 u = philox_w(pre, P, w - ((t + 1) >> 1) * slab);
-                const uint32_t sh = (t & 1u) ? 0u : 16u;
-                nw = metropolis_word(ow, nd, tbase, u.x << sh, u.y << sh, u.z << sh, u.w << sh,
-                                     pre, P, w);
+                const U4 u = philox_w(pre, P, w - (t - (t >> 2)) * slab);
+                const uint32_t U = (t & 2u) ? ((t & 1u) ? u.w : u.z) : ((t & 1u) ? u.y : u.x);
+                uint32_t d;
+                nw = ow ^ coarse_flips(ow, nd, U, T8, d);
+                if (any_tie(d)) nw ^= fine_flips(tie_bytes(d), nd + (ow << 3), tab, pre, P, w);
                 own[w] = nw;
             }
             if (MODE != 0) meas_add(macc, nw, nd, wa);
         }
     }
+    if (MODE != 2) drain_ties<MODE>(q, tq, lane, tab, pre, P, cur_own, macc);
     if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
 }
 
@@ -604,21 +881,22 @@ __device__ __forceinline__ int site_update(uint8_t* own, const uint8_t* oth, uin
     int d = own[i];
     if (update) {
         const uint32_t th = tab[d * 8 + nd];
-        // slab S = sites of this colour per z-plane (3D) or row (2D); the
-        // slab pair (t, t+1) shares Philox blocks: v = (t>>1)*S + (i mod S)
+        // slab S = sites of this colour per z-plane (3D) or row (2D); slab quad
+        // t>>2 shares Philox blocks: v = (t>>2)*S + (i mod S), block v >> 2,
+        // word t & 3, coarse = low 7 bits of byte v & 3
         const uint32_t S = plane / L;
         const uint32_t t = DIM == 3 ? z : y;
-        const uint32_t v = (t >> 1) * S + (i - t * S);
+        const uint32_t v = (t >> 2) * S + (i - t * S);
         const U4 u = philox10(uid, v >> 2, c2, c3, k0, k1);
-        const uint32_t jv = v & 3u;
-        const uint32_t uw = jv == 0 ? u.x : jv == 1 ? u.y : jv == 2 ? u.z : u.w;
-        const uint32_t a16 = (t & 1u) ? (uw >> 16) : (uw & 0xFFFFu);
-        bool acc = a16 < (th >> 16);
-        if (a16 == (th >> 16)) {
+        const uint32_t tw = t & 3u;
+        const uint32_t uw = tw == 0 ? u.x : tw == 1 ? u.y : tw == 2 ? u.z : u.w;
+        const uint32_t c7 = (uw >> (8u * (v & 3u))) & 0x7Fu;
+        bool acc = c7 < (th >> 25);
+        if (c7 == (th >> 25)) {
             const U4 f = philox10(uid, 0x80000000u | (i >> 2), c2, c3, k0, k1);
             const uint32_t ji = i & 3u;
             const uint32_t fw = ji == 0 ? f.x : ji == 1 ? f.y : ji == 2 ? f.z : f.w;
-            acc = ((a16 << 16) | (fw >> 16)) <= th;
+            acc = ((c7 << 25) | (fw >> 7)) <= th;
         }
         if (acc) {
             d ^= 1;
@@ -742,9 +1020,9 @@ __device__ __forceinline__ void resident_geom(uint32_t i, uint32_t L, uint32_t h
         nb[4] = nb[5] = 0;
     }
     const uint32_t t = DIM == 3 ? z : y;
-    const uint32_t v = (t >> 1) * S + (i - t * S);
+    const uint32_t v = (t >> 2) * S + (i - t * S);
     c1 = v >> 2;
-    sel = (v & 3u) | ((t & 1u) << 2);
+    sel = (v & 3u) | ((t & 3u) << 2);
 }
 
 __device__ __forceinline__ uint32_t dsm_map(uint32_t local, uint32_t rank) {
@@ -758,21 +1036,21 @@ __device__ __forceinline__ int dsm_ld(uint32_t remote) {
     return (int)v;
 }
 
-// Flip decision from the site's coarse block u (word/half selector sel) and, on
-// a tie with the threshold's upper half, the fine block of counter
-// 0x80000000 | (i >> 2) drawn with the same hoisted rounds.
+// Flip decision from the site's coarse block u (selector sel: byte sel & 3 of
+// word sel >> 2) and, on a tie with the threshold's top 7 bits, the fine block
+// of counter 0x80000000 | (i >> 2) drawn with the same hoisted rounds.
 __device__ __forceinline__ bool resident_accept(const U4& u, uint32_t sel, uint32_t th,
                                                 uint32_t i, const PhiloxPre& pre,
                                                 const IsingParams& P) {
-    const uint32_t jv = sel & 3u;
-    const uint32_t uw = jv == 0 ? u.x : jv == 1 ? u.y : jv == 2 ? u.z : u.w;
-    const uint32_t a16 = (sel & 4u) ? (uw >> 16) : (uw & 0xFFFFu);
-    bool acc = a16 < (th >> 16);
-    if (a16 == (th >> 16)) {
+    const uint32_t jw = sel >> 2;
+    const uint32_t uw = jw == 0 ? u.x : jw == 1 ? u.y : jw == 2 ? u.z : u.w;
+    const uint32_t c7 = (uw >> (8u * (sel & 3u))) & 0x7Fu;
+    bool acc = c7 < (th >> 25);
+    if (c7 == (th >> 25)) {
         const U4 f = philox_w(pre, P, 0x80000000u | (i >> 2));
         const uint32_t ji = i & 3u;
         const uint32_t fw = ji == 0 ? f.x : ji == 1 ? f.y : ji == 2 ? f.z : f.w;
-        acc = ((a16 << 16) | (fw >> 16)) <= th;
+        acc = ((c7 << 25) | (fw >> 7)) <= th;
     }
     return acc;
 }
@@ -1153,6 +1431,7 @@ struct isg_ising {
     uint8_t* d_spins = nullptr;
     int64_t spin_bytes = 0;
     uint32_t* d_thr = nullptr;
+    uint32_t* d_thr8 = nullptr;
     int32_t* d_r2t = nullptr;
     int32_t* d_t2r = nullptr;
     double* d_betas = nullptr;
@@ -1169,6 +1448,9 @@ struct isg_ising {
     int threads = 256;
     int blocks_per_sm = 0;
     int prefetch = 0;          // rolling prefetch depth as set (0: automatic)
+    int wpl_max = 4;           // rolling words per lane for L >= 128 (2 or 4)
+    int wmax = 2;              // word kernel variant: 4 if some size runs 4 words per lane
+    bool cache_pf_set = false; // cache prefetch set by the caller (else automatic)
     int pf = 1;                // depth in use
     int word_grid = 0, site_grid = 0;
     int word_grids[3] = {1, 1, 1};
@@ -1198,21 +1480,65 @@ struct isg_ising {
 
 namespace isg {
 
-static void (*word_kernel(int dim, int mode, int pf))(IsingParams, int, int) {
+// CTA tasks of the rolling sizes: warp tasks of 32 * wpl words (wpl = 2 for
+// L = 64, else wpl_max) are the rows of one y-block at one z; 8 y-blocks of
+// a plane form a column group, and a CTA task is one (replica, group, z), z
+// fastest, so consecutive CTA tasks walk z.
+static void layout_rolling(isg_ising* H) {
+    IsingParams& P = H->P;
+    int64_t ctask = 0;
+    H->wmax = 2;
+    for (int s = 0; s < H->n_classes; ++s) {
+        IsingClass& C = P.cls[s];
+        if (C.kind != kRolling) continue;
+        const int L = C.L, rw = L / 8;
+        C.log2_wpl = H->wpl_max == 4 ? 2 : 1;
+        const int tw = 32 << C.log2_wpl;          // words per warp task
+        const int cols = L * rw / tw;             // y-blocks per plane
+        // a CTA task is 8 y-blocks of one plane, or, when a plane has fewer
+        // (L = 64 with four words per lane: 4), the plane of 8 / cols replicas
+        const int groups = cols >= 8 ? cols / 8 : 1;
+        const int rpc = cols >= 8 ? 1 : 8 / cols;
+        C.log2_groups = 0;
+        while ((1 << C.log2_groups) < groups) ++C.log2_groups;
+        C.log2_rpc = 0;
+        while ((1 << C.log2_rpc) < rpc) ++C.log2_rpc;
+        // blocks split the rolling work by words, not by CTA tasks: a CTA
+        // task of four words per lane counts twice
+        C.log2_unit = C.log2_wpl - 1;
+        C.ctask_base = ctask;
+        ctask += ((int64_t)((C.R + rpc - 1) / rpc) * groups * L) << C.log2_unit;
+        C.ctask_end = ctask;
+        if (C.log2_wpl == 2) H->wmax = 4;
+    }
+    P.total_ctasks = ctask;
+}
+
+static void (*word_kernel(int dim, int mode, int pf, int wmax))(IsingParams, int, int) {
     if (dim == 3) {
-        if (pf == 2) {
-            if (mode == 0) return k_ising_words<3, 0, 2>;
-            if (mode == 1) return k_ising_words<3, 1, 2>;
-            return k_ising_words<3, 2, 2>;
+        if (wmax == 4) {
+            if (pf == 2) {
+                if (mode == 0) return k_ising_words<3, 0, 2, 4>;
+                if (mode == 1) return k_ising_words<3, 1, 2, 4>;
+                return k_ising_words<3, 2, 2, 4>;
+            }
+            if (mode == 0) return k_ising_words<3, 0, 1, 4>;
+            if (mode == 1) return k_ising_words<3, 1, 1, 4>;
+            return k_ising_words<3, 2, 1, 4>;
         }
-        if (mode == 0) return k_ising_words<3, 0, 1>;
-        if (mode == 1) return k_ising_words<3, 1, 1>;
-        return k_ising_words<3, 2, 1>;
+        if (pf == 2) {
+            if (mode == 0) return k_ising_words<3, 0, 2, 2>;
+            if (mode == 1) return k_ising_words<3, 1, 2, 2>;
+            return k_ising_words<3, 2, 2, 2>;
+        }
+        if (mode == 0) return k_ising_words<3, 0, 1, 2>;
+        if (mode == 1) return k_ising_words<3, 1, 1, 2>;
+        return k_ising_words<3, 2, 1, 2>;
     }
     // no rolling tasks in 2D: one prefetch form
-    if (mode == 0) return k_ising_words<2, 0, 1>;
-    if (mode == 1) return k_ising_words<2, 1, 1>;
-    return k_ising_words<2, 2, 1>;
+    if (mode == 0) return k_ising_words<2, 0, 1, 2>;
+    if (mode == 1) return k_ising_words<2, 1, 1, 2>;
+    return k_ising_words<2, 2, 1, 2>;
 }
 static void (*site_kernel(int dim, int mode))(IsingParams, int, int) {
     if (dim == 3) {
@@ -1234,12 +1560,20 @@ static void (*site_kernel(int dim, int mode))(IsingParams, int, int) {
 static int configure_launch(isg_ising* H) {
     const int thr = H->threads;
     const int64_t need = std::max<int64_t>(H->P.total_ctasks, H->P.flat_ctasks);
-    H->pf = H->prefetch > 0 ? H->prefetch : (H->spin_bytes <= ((int64_t)96 << 20) ? 2 : 1);
+    const bool in_l2 = H->spin_bytes <= ((int64_t)96 << 20);
+    // two words per lane: loads two planes ahead help L2-resident batches;
+    // four words per lane (2 blocks per SM either way): one plane ahead
+    H->pf = H->prefetch > 0 ? H->prefetch : (in_l2 && H->wmax == 2 ? 2 : 1);
     if (H->dim != 3) H->pf = 1;
+    // batches larger than L2: lines 3 planes ahead prefetched into L2
+    if (!H->cache_pf_set) {
+        H->P.l2_ahead = in_l2 ? 0 : 3;
+        H->P.pf_level = 2;
+    }
     for (int mode = 0; mode < 3; ++mode) {
         int occ = 0;
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ, (const void*)word_kernel(H->dim, mode, H->pf), 256, 0);
+            &occ, (const void*)word_kernel(H->dim, mode, H->pf, H->wmax), 256, 0);
         if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
         if (occ < 1) occ = 1;
         const int bps = H->blocks_per_sm > 0 ? std::min(H->blocks_per_sm, occ) : occ;
@@ -1254,7 +1588,7 @@ static int configure_launch(isg_ising* H) {
 
 static void launch_half(isg_ising* H, int colour, int sweep_off, int mode) {
     if (H->P.total_tasks > 0)
-        word_kernel(H->dim, mode, H->pf)<<<H->word_grids[mode], 256, 0, H->stream>>>(H->P, colour,
+        word_kernel(H->dim, mode, H->pf, H->wmax)<<<H->word_grids[mode], 256, 0, H->stream>>>(H->P, colour,
                                                                              sweep_off);
     if (H->P.total_sites > 0)
         site_kernel(H->dim, mode)<<<H->site_grid, H->threads, 0, H->stream>>>(H->P, colour,
@@ -1415,15 +1749,9 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         if (C.kind != kSite) task += (int64_t)C.tasks_per_plane * replicas;
         C.task_end = task;
         C.log2_groups = 0;
+        C.log2_wpl = 1;
         if (C.kind == kRolling) {
-            // warp tasks of 64 words = 64/(L/8) rows: L*L/512 per z-plane, in
-            // groups of 8
-            const int cols = (L / (64 / rw));
-            int groups = cols / 8;
-            while ((1 << C.log2_groups) < groups) ++C.log2_groups;
-            C.ctask_base = ctask;
-            ctask += (int64_t)replicas * groups * L;
-            C.ctask_end = ctask;
+            // CTA tasks are laid out by layout_rolling
         } else if (C.kind == kFlat) {
             C.ctask_base = fctask;
             fctask += ((int64_t)C.tasks_per_plane * replicas + 7) / 8;
@@ -1446,8 +1774,9 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
     P.n_classes = n_sizes;
     P.dim = dim;
     P.total_tasks = task;
-    P.total_ctasks = ctask;
     P.flat_ctasks = fctask;
+    (void)ctask;
+    layout_rolling(H);
     P.total_sites = site;
     P.seed = seed;
     for (int r = 0; r < 10; ++r) {
@@ -1468,6 +1797,7 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMalloc"));
     ALLOC(H->d_spins, (size_t)off);
     ALLOC(H->d_thr, sizeof(uint32_t) * 16 * RT);
+    ALLOC(H->d_thr8, sizeof(uint32_t) * 4 * RT);
     ALLOC(H->d_r2t, sizeof(int32_t) * RT);
     ALLOC(H->d_t2r, sizeof(int32_t) * RT);
     ALLOC(H->d_betas, sizeof(double) * RT);
@@ -1483,6 +1813,7 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
 
     P.spins = H->d_spins;
     P.thr = H->d_thr;
+    P.thr8 = H->d_thr8;
     P.r2t = H->d_r2t;
     P.acc = H->d_acc;
     P.ctrl = H->d_ctrl;
@@ -1510,6 +1841,7 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
     if (e != cudaSuccess) return cleanup(cuda_fail(e, #call));
     CKC(cudaMemsetAsync(H->d_spins, 0, (size_t)off, H->stream));
     CKC(cudaMemsetAsync(H->d_thr, 0, sizeof(uint32_t) * 16 * RT, H->stream));
+    CKC(cudaMemsetAsync(H->d_thr8, 0, sizeof(uint32_t) * 4 * RT, H->stream));
     CKC(cudaMemsetAsync(H->d_acc, 0, sizeof(unsigned long long) * 2 * RT, H->stream));
     CKC(cudaMemsetAsync(H->d_ctrl, 0, sizeof(unsigned long long) * (1 + 3 * kMaxClasses),
                         H->stream));
@@ -1539,6 +1871,7 @@ int isg_ising_destroy(isg_ising* H) {
     destroy_graph(H);
     cudaFree(H->d_spins);
     cudaFree(H->d_thr);
+    cudaFree(H->d_thr8);
     cudaFree(H->d_r2t);
     cudaFree(H->d_t2r);
     cudaFree(H->d_betas);
@@ -1589,6 +1922,25 @@ static void threshold_table(int dim, double T, double J, double hfield, uint32_t
         }
     }
 }
+
+// Uploads the per-slot thresholds ([slots][16]) and their coarse bytes for the
+// word kernels ([slots][4]: byte own_down*8 + n_down = 0x80 for 0xFFFFFFFF,
+// else threshold >> 25).
+static int upload_thresholds(isg_ising* H, const std::vector<uint32_t>& thr) {
+    const size_t n = thr.size() / 16;
+    std::vector<uint32_t> t8(4 * n, 0u);
+    for (size_t i = 0; i < n; ++i)
+        for (int e = 0; e < 16; ++e) {
+            const uint32_t t = thr[i * 16 + (size_t)e];
+            const uint32_t b = t == 0xFFFFFFFFu ? 0x80u : t >> 25;
+            t8[4 * i + (size_t)(e >> 2)] |= b << (8 * (e & 3));
+        }
+    ISG_CK(cudaMemcpyAsync(H->d_thr, thr.data(), thr.size() * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, H->stream));
+    ISG_CK(cudaMemcpyAsync(H->d_thr8, t8.data(), t8.size() * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, H->stream));
+    return ISG_OK;
+}
 }  // namespace isg
 
 extern "C" {
@@ -1607,8 +1959,10 @@ int isg_ising_set_temperatures(isg_ising* H, const double* temps, double J, doub
     }
     std::vector<int32_t> ident(RT);
     for (int i = 0; i < RT; ++i) ident[i] = i % H->R;
-    ISG_CK(cudaMemcpyAsync(H->d_thr, thr.data(), thr.size() * sizeof(uint32_t),
-                           cudaMemcpyHostToDevice, H->stream));
+    {
+        const int rc = upload_thresholds(H, thr);
+        if (rc) return rc;
+    }
     ISG_CK(cudaMemcpyAsync(H->d_betas, betas.data(), betas.size() * sizeof(double),
                            cudaMemcpyHostToDevice, H->stream));
     ISG_CK(cudaMemcpyAsync(H->d_r2t, ident.data(), sizeof(int32_t) * RT, cudaMemcpyHostToDevice,
@@ -2074,6 +2428,31 @@ int isg_ising_time_halfsweep_graph(isg_ising* H, int n_launches, int64_t flush_b
     return ISG_OK;
 }
 
+int isg_ising_set_cache_prefetch(isg_ising* H, int level, int planes) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_set_cache_prefetch: NULL handle");
+    if (planes < 0 || planes > 16 || (level != 1 && level != 2))
+        return fail(ISG_ERR_ARG, "isg_ising_set_cache_prefetch: level must be 1 or 2, planes 0..16");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    H->P.l2_ahead = planes;
+    H->P.pf_level = level;
+    H->cache_pf_set = true;
+    destroy_graph(H);
+    return ISG_OK;
+}
+
+int isg_ising_set_words_per_lane(isg_ising* H, int words) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_set_words_per_lane: NULL handle");
+    if (words != 2 && words != 4)
+        return fail(ISG_ERR_ARG, "isg_ising_set_words_per_lane: words must be 2 or 4");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    H->wpl_max = words;
+    layout_rolling(H);
+    destroy_graph(H);
+    return configure_launch(H);
+}
+
 int isg_ising_set_prefetch(isg_ising* H, int depth) {
     if (!H) return fail(ISG_ERR_ARG, "isg_ising_set_prefetch: NULL handle");
     if (depth < 0 || depth > 2) return fail(ISG_ERR_ARG, "isg_ising_set_prefetch: depth must be 0..2");
@@ -2159,8 +2538,10 @@ static int all_slots_to(isg_ising* H, double T) {
     threshold_table(H->dim, T, H->J, H->h, thr.data());
     for (int i = 1; i < RT; ++i) std::copy(thr.begin(), thr.begin() + 16, thr.begin() + 16 * i);
     std::vector<double> betas(RT, 1.0 / T);
-    ISG_CK(cudaMemcpyAsync(H->d_thr, thr.data(), thr.size() * sizeof(uint32_t),
-                           cudaMemcpyHostToDevice, H->stream));
+    {
+        const int rc = upload_thresholds(H, thr);
+        if (rc) return rc;
+    }
     ISG_CK(cudaMemcpyAsync(H->d_betas, betas.data(), betas.size() * sizeof(double),
                            cudaMemcpyHostToDevice, H->stream));
     return ISG_OK;

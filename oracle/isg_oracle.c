@@ -141,11 +141,12 @@ static inline int64_t site_index(int L, int dim, int x, int y, int z) {
  * assembled from two Philox blocks of the ISING stream (the GPU kernels'
  * definition, include/isg.h):
  *   S = L^(dim-1)/2 sites of one colour per z-plane (3D) or row (2D),
- *   t = ci / S, j = ci % S, v = (t >> 1) * S + j;
- *   coarse = bits 16*(t & 1) .. +15 of word (v & 3) of block c1 = v >> 2;
- *   fine   = bits 16..31 of word (ci & 3) of block c1 = 0x80000000 | (ci >> 2);
- *   u = coarse << 16 | fine, and the site flips iff u <= thr.
- * The fine block is only drawn when coarse equals thr's upper half (otherwise
+ *   t = ci / S, j = ci % S, v = (t >> 2) * S + j;
+ *   coarse = the low 7 bits of byte (v & 3) of word (t & 3) of block
+ *            c1 = v >> 2 (one block serves the 16 sites of 4 slabs);
+ *   fine   = bits 7..31 of word (ci & 3) of block c1 = 0x80000000 | (ci >> 2);
+ *   u = coarse << 25 | fine, and the site flips iff u <= thr.
+ * The fine block is only drawn when coarse equals thr's top 7 bits (otherwise
  * the comparison is already decided). */
 void or_ising_halfsweep(int L, int dim, int8_t* spins, int colour, uint64_t seed, uint32_t uid,
                         uint64_t sweep, const uint32_t thr[16]) {
@@ -173,20 +174,20 @@ void or_ising_halfsweep(int L, int dim, int8_t* spins, int colour, uint64_t seed
                 }
                 int od = spins[idx] < 0;
                 const uint32_t th = thr[od * 8 + nd];
-                const int64_t t = ci / S, v = (t >> 1) * S + (ci - t * S);
+                const int64_t t = ci / S, v = (t >> 2) * S + (ci - t * S);
                 if ((v >> 2) != cached_block) {
                     cached_block = v >> 2;
                     stream_words(seed, (uint32_t)cached_block, uid, sweep, TAG_ISING,
                                  (uint32_t)colour, w);
                 }
-                const uint32_t coarse = (t & 1) ? (w[v & 3] >> 16) : (w[v & 3] & 0xFFFFu);
+                const uint32_t coarse = (w[t & 3] >> (8 * (v & 3))) & 0x7Fu;
                 int flip;
-                if (coarse != (th >> 16)) {
-                    flip = coarse < (th >> 16);
+                if (coarse != (th >> 25)) {
+                    flip = coarse < (th >> 25);
                 } else {
                     stream_words(seed, 0x80000000u | (uint32_t)(ci >> 2), uid, sweep, TAG_ISING,
                                  (uint32_t)colour, fw);
-                    flip = ((coarse << 16) | (fw[ci & 3] >> 16)) <= th;
+                    flip = ((coarse << 25) | (fw[ci & 3] >> 7)) <= th;
                 }
                 if (flip) spins[idx] = (int8_t)(-spins[idx]);
             }

@@ -218,6 +218,47 @@ def test_prefetch_depth_keeps_results(gpu):
         assert np.array_equal(x, y)
 
 
+def test_words_per_lane_keep_results(gpu, oracle):
+    """L >= 64 rolls with four words per lane by default (L = 64: two replicas
+    per CTA task, so R = 3 leaves the last task half empty), or with two: the
+    same bits, through sweeps with fused measurements and exchanges, with the
+    cache prefetch on or off; an L = 128 sweep also against the oracle."""
+    sizes, R = [64, 128, 256], 3
+    out = []
+    for words, pf in ((4, 0), (2, 0), (4, 3)):
+        b = gpu.IsingBatch(sizes, R, seed=17)
+        b.set_words_per_lane(words)
+        b.set_cache_prefetch(2, pf)
+        b.set_temperatures(grid(4.4, 4.6, R))
+        b.step(3)
+        _, bb, mm = b.pt_run(6, 3, 2)
+        out.append((bb, mm, [b.get_spins(s, r) for s in range(3) for r in range(R)]))
+        b.close()
+    d64 = gpu.IsingBatch([64], 3, seed=29)
+    d64.set_temperatures([4.45, 4.5, 4.55])
+    sp64 = [d64.get_spins(0, r) for r in range(3)]
+    d64.step(1)
+    for r in range(3):
+        thr64 = oracle.thresholds(3, 1 / [4.45, 4.5, 4.55][r])
+        for c in (0, 1):
+            oracle.halfsweep(sp64[r], 64, 3, c, 29, r, 0, thr64)
+        assert np.array_equal(d64.get_spins(0, r), sp64[r]), r
+    d64.close()
+    for o in out[1:]:
+        assert np.array_equal(out[0][0], o[0]) and np.array_equal(out[0][1], o[1])
+        for x, y in zip(out[0][2], o[2]):
+            assert np.array_equal(x, y)
+    d = gpu.IsingBatch([128], 1, seed=23)
+    d.set_temperatures([4.5])
+    sp = d.get_spins(0, 0)
+    d.step(1)
+    thr = oracle.thresholds(3, 1 / 4.5)
+    for c in (0, 1):
+        oracle.halfsweep(sp, 128, 3, c, 23, 0, 0, thr)
+    assert np.array_equal(d.get_spins(0, 0), sp)
+    d.close()
+
+
 def test_autotune_keeps_results(gpu):
     sizes, R = [8, 32, 64], 16
     a = gpu.IsingBatch(sizes, R, seed=1)

@@ -51,18 +51,18 @@ extern "C" {
  *         spin = -1 if the word's top bit is set, else +1.
  *  ISING: Metropolis half-sweep, step = global sweep number, colour = 0
  *         (x+y+z even) or 1.  A site of colour index i = (z*L*L + y*L + x) >> 1
- *         (2D: (y*L + x) >> 1) flips iff the 32-bit u = coarse << 16 | fine
+ *         (2D: (y*L + x) >> 1) flips iff the 32-bit u = coarse << 25 | fine
  *         satisfies u <= threshold[own_down*8 + n_down_neighbours], with
  *         threshold = 0xFFFFFFFF for dE <= 0, else
  *         max(floor(exp(-beta*dE) * 2^32), 1) - 1  (FP64 on the host).
  *         With S = L^(dim-1)/2 sites of one colour per z-plane (3D) or row
- *         (2D), t = i / S, v = (t >> 1)*S + i % S:
- *           coarse = 16-bit half (t & 1) (0: bits 0..15, 1: bits 16..31) of
- *                    word (v & 3) of the block c1 = v >> 2, so one block
- *                    serves 8 sites, 4 at z (or y) = 2k and 4 at 2k+1;
- *           fine   = bits 16..31 of word (i & 3) of the block
+ *         (2D), t = i / S, v = (t >> 2)*S + i % S:
+ *           coarse = the low 7 bits of byte (v & 3) of word (t & 3) of the
+ *                    block c1 = v >> 2, so one block serves 16 sites: 4 at
+ *                    each of z (or y) = 4k .. 4k+3;
+ *           fine   = bits 7..31 of word (i & 3) of the block
  *                    c1 = 0x80000000 | (i >> 2); it only matters when
- *                    coarse equals the threshold's upper 16 bits.
+ *                    coarse equals the threshold's top 7 bits.
  *  EXCH : replica exchange.  c1 = lower temperature index of the pair,
  *         c0 = exchange uid, step = exchange count of that size;
  *         u = ((w0 << 32 | w1) >> 11) * 2^-53.
@@ -231,6 +231,11 @@ int isg_ising_set_cache_prefetch(isg_ising* h, int level, int planes);
  * L >= 128: 4 (default; 128-bit loads and stores, 2 blocks per SM) or 2 (as
  * for L = 64).  Results never depend on it. */
 int isg_ising_set_words_per_lane(isg_ising* h, int words);
+/* Launch the half-sweep word kernels as programmatic dependent launches
+ * (enable = 1, default): their blocks are scheduled while the previous kernel
+ * of the stream drains and wait for it before reading any device state; 0 =
+ * ordinary launches.  Results never depend on it. */
+int isg_ising_set_dependent_launch(isg_ising* h, int enable);
 /* Time every supported launch shape (prefetch depth x site-kernel threads x
  * blocks per SM) on a scratch copy of the lattices and keep the fastest.
  * best[0..2] (may be NULL) receives threads, blocks/SM, prefetch depth. */

@@ -107,6 +107,7 @@ def _declare(L):
         "isg_ising_set_prefetch": [vp, i32],
         "isg_ising_set_cache_prefetch": [vp, i32, i32],
         "isg_ising_set_words_per_lane": [vp, i32],
+        "isg_ising_set_dependent_launch": [vp, i32],
         "isg_ising_time_halfsweep": [vp, i32, vp],
         "isg_ising_time_halfsweep_graph": [vp, i32, i64, i32, vp],
         "isg_ising_sites_per_halfsweep": [vp, vp],
@@ -549,6 +550,10 @@ class IsingBatch:
     def set_words_per_lane(self, words: int = 4) -> None:
         """Rolling half-sweep, L >= 128: 4 or 2 words per lane (same results)."""
         _check(lib().isg_ising_set_words_per_lane(self._h, int(words)))
+
+    def set_dependent_launch(self, enable: bool = True) -> None:
+        """Half-sweep word kernels as programmatic dependent launches (same results)."""
+        _check(lib().isg_ising_set_dependent_launch(self._h, int(bool(enable))))
 
     def autotune(self) -> tuple[int, int, int]:
         """Fastest (site threads, blocks per SM, prefetch depth), kept for the batch."""

@@ -62,10 +62,10 @@ constexpr int kMaxReplicas = 1024;
 
 // Task kinds of a lattice size (words of 4 same-colour sites of one colour
 // plane of one replica):
-//   kRolling (dim 3, L = 64, 128, 256): a warp task is the rows of one y-block
-//     at one z, 2 adjacent words per lane (64 words, L = 64) or 4 (128 words,
-//     L >= 128); consecutive tasks of a size walk z, so a warp keeps the z-1,
-//     z, z+1 words of the other colour in registers.
+//   kRolling (dim 3, L = 32..256): a warp task is the rows of one y-block at
+//     one z, 4 adjacent words per lane (128 words; 2 and 64 if so set);
+//     consecutive tasks of a size walk z, so a warp keeps the z-1, z, z+1
+//     words of the other colour in registers.
 //   kFlat    (other power-of-two L with L/8 dividing 32): 32 consecutive words,
 //     one per lane.
 //   kSite    (any other even L): one thread per site (site kernel).
@@ -486,7 +486,7 @@ __device__ __forceinline__ void queue_word(uint2* q, TieQueue& tq, bool t, uint3
 }
 
 // One z-step of a rolling column with four adjacent words per lane (L >=
-// 128): as rolling_pair_step, with 128-bit loads and stores.  U0..U3: the
+// 32): as rolling_pair_step, with 128-bit loads and stores.  U0..U3: the
 // Philox words of the four word columns for this plane.  x neighbours: the
 // lane's words k-1 / k+1 and, at the row edge of the lane, word 0 of the next
 // lane (px = 1) or word 3 of the previous lane (px = 0) by one shuffle.
@@ -591,9 +591,10 @@ __device__ __forceinline__ void rolling_quad_step(
 // per SM with more loads in flight per warp); chosen per batch (configure_launch,
 // isg_ising_autotune).
 // WMAX: 4 if some size runs four words per lane (that path needs more
-// registers: 2 blocks per SM), else 2.
-template <int DIM, int MODE, int PF, int WMAX>
-__global__ void __launch_bounds__(256, (PF == 1 && WMAX == 2) ? 3 : 2)
+// registers: 2 blocks per SM), else 2.  MINB: blocks per SM the registers
+// are budgeted for.
+template <int DIM, int MODE, int PF, int WMAX, int MINB>
+__global__ void __launch_bounds__(256, MINB)
     k_ising_words(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
     __shared__ uint32_t s_thr[8][16];
     __shared__ uint2 s_q[8][kTieQ];
@@ -609,6 +610,14 @@ __global__ void __launch_bounds__(256, (PF == 1 && WMAX == 2) ? 3 : 2)
                                ? G
                                : (((int64_t)(blockIdx.x + 1) * G / gridDim.x) & ~(int64_t)7);
     int64_t ft = blockIdx.x;  // flat CTA tasks: blockIdx.x, + gridDim.x, ...
+
+    // Launched as a programmatic dependent of the previous kernel of the
+    // stream (when enabled): everything above depends on parameters only;
+    // wait here for the previous grid (and its memory) before the first read
+    // of device state, then let the next kernel's blocks be scheduled as ours
+    // retire.  Both are no-ops for an ordinary launch.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
     const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
     const uint32_t c2 = (uint32_t)sweep;
@@ -685,8 +694,9 @@ __global__ void __launch_bounds__(256, (PF == 1 && WMAX == 2) ? 3 : 2)
 
         if (DIM == 3 && !flat_now) {
             // a warp task: 32 * wpl words (nr rows of rw words), wpl = 2 or 4
-            // adjacent words per lane; every row has >= 4 lanes and a task
-            // >= 2 rows (L = 64..256)
+            // adjacent words per lane; a row has 1 (L = 32) to 16 lanes and a
+            // task 2 to 32 rows; when the task is the whole plane (L = 32),
+            // the y shuffles wrap around it and the halo rows are its own
             const int lw = C.log2_wpl;
             const uint32_t pz = L << lrw;          // words per z-plane
             const uint32_t pwm = (pz << C.log2L) - 1;  // plane words - 1 (power of two)
@@ -734,7 +744,8 @@ __global__ void __launch_bounds__(256, (PF == 1 && WMAX == 2) ? 3 : 2)
                     qow = ldg_u4(mc + ((o + pz) & pwm));
                 }
                 // z quads (4k .. 4k+3) share one Philox block per word column:
-                // counter (z>>2)*pz + word, Philox word z & 3 for plane z
+                // counter (z>>2)*pz + word, Philox word z & 3 for plane z; the
+                // four blocks of a quad are drawn together (independent chains)
                 for (uint32_t z = z0; z < z1; z += 4) {
                     U4 u0{}, u1{}, u2{}, u3{};
                     if (MODE != 2) {
@@ -1022,7 +1033,7 @@ __device__ __forceinline__ void resident_geom(uint32_t i, uint32_t L, uint32_t h
     const uint32_t t = DIM == 3 ? z : y;
     const uint32_t v = (t >> 2) * S + (i - t * S);
     c1 = v >> 2;
-    sel = (v & 3u) | ((t & 3u) << 2);
+    sel = (v & 3u) | ((t & 3u) << 2);  // byte v & 3 of word t & 3
 }
 
 __device__ __forceinline__ uint32_t dsm_map(uint32_t local, uint32_t rank) {
@@ -1451,6 +1462,7 @@ struct isg_ising {
     int wpl_max = 4;           // rolling words per lane for L >= 128 (2 or 4)
     int wmax = 2;              // word kernel variant: 4 if some size runs 4 words per lane
     bool cache_pf_set = false; // cache prefetch set by the caller (else automatic)
+    bool pdl = true;           // word kernels as programmatic dependent launches
     int pf = 1;                // depth in use
     int word_grid = 0, site_grid = 0;
     int word_grids[3] = {1, 1, 1};
@@ -1496,7 +1508,8 @@ static void layout_rolling(isg_ising* H) {
         const int tw = 32 << C.log2_wpl;          // words per warp task
         const int cols = L * rw / tw;             // y-blocks per plane
         // a CTA task is 8 y-blocks of one plane, or, when a plane has fewer
-        // (L = 64 with four words per lane: 4), the plane of 8 / cols replicas
+        // (four words per lane: 4 at L = 64, 1 at L = 32), the plane of
+        // 8 / cols replicas
         const int groups = cols >= 8 ? cols / 8 : 1;
         const int rpc = cols >= 8 ? 1 : 8 / cols;
         C.log2_groups = 0;
@@ -1514,31 +1527,28 @@ static void layout_rolling(isg_ising* H) {
     P.total_ctasks = ctask;
 }
 
+template <int DIM, int PF, int WMAX, int MINB>
+static void (*word_kernel_m(int mode))(IsingParams, int, int) {
+    if (mode == 0) return k_ising_words<DIM, 0, PF, WMAX, MINB>;
+    if (mode == 1) return k_ising_words<DIM, 1, PF, WMAX, MINB>;
+    return k_ising_words<DIM, 2, PF, WMAX, MINB>;
+}
+
+// Variants: two words per lane at 3 blocks per SM (one plane ahead) or 2
+// (two planes ahead); four words per lane at 2 blocks per SM (one or two
+// planes ahead; at 3 blocks per SM its registers spill and it ran 10-19%
+// slower).
 static void (*word_kernel(int dim, int mode, int pf, int wmax))(IsingParams, int, int) {
     if (dim == 3) {
         if (wmax == 4) {
-            if (pf == 2) {
-                if (mode == 0) return k_ising_words<3, 0, 2, 4>;
-                if (mode == 1) return k_ising_words<3, 1, 2, 4>;
-                return k_ising_words<3, 2, 2, 4>;
-            }
-            if (mode == 0) return k_ising_words<3, 0, 1, 4>;
-            if (mode == 1) return k_ising_words<3, 1, 1, 4>;
-            return k_ising_words<3, 2, 1, 4>;
+            if (pf == 2) return word_kernel_m<3, 2, 4, 2>(mode);
+            return word_kernel_m<3, 1, 4, 2>(mode);
         }
-        if (pf == 2) {
-            if (mode == 0) return k_ising_words<3, 0, 2, 2>;
-            if (mode == 1) return k_ising_words<3, 1, 2, 2>;
-            return k_ising_words<3, 2, 2, 2>;
-        }
-        if (mode == 0) return k_ising_words<3, 0, 1, 2>;
-        if (mode == 1) return k_ising_words<3, 1, 1, 2>;
-        return k_ising_words<3, 2, 1, 2>;
+        if (pf == 2) return word_kernel_m<3, 2, 2, 2>(mode);
+        return word_kernel_m<3, 1, 2, 3>(mode);
     }
-    // no rolling tasks in 2D: one prefetch form
-    if (mode == 0) return k_ising_words<2, 0, 1, 2>;
-    if (mode == 1) return k_ising_words<2, 1, 1, 2>;
-    return k_ising_words<2, 2, 1, 2>;
+    // no rolling tasks in 2D: one form
+    return word_kernel_m<2, 1, 2, 3>(mode);
 }
 static void (*site_kernel(int dim, int mode))(IsingParams, int, int) {
     if (dim == 3) {
@@ -1587,9 +1597,22 @@ static int configure_launch(isg_ising* H) {
 }
 
 static void launch_half(isg_ising* H, int colour, int sweep_off, int mode) {
-    if (H->P.total_tasks > 0)
-        word_kernel(H->dim, mode, H->pf, H->wmax)<<<H->word_grids[mode], 256, 0, H->stream>>>(H->P, colour,
-                                                                             sweep_off);
+    if (H->P.total_tasks > 0) {
+        // programmatic dependent launch: the word kernel's blocks may be
+        // scheduled while the previous kernel drains (they wait on it first)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)H->word_grids[mode]);
+        cfg.blockDim = dim3(256);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = H->stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = H->pdl ? 1 : 0;
+        cudaLaunchKernelEx(&cfg, word_kernel(H->dim, mode, H->pf, H->wmax), H->P, colour,
+                           sweep_off);
+    }
     if (H->P.total_sites > 0)
         site_kernel(H->dim, mode)<<<H->site_grid, H->threads, 0, H->stream>>>(H->P, colour,
                                                                              sweep_off);
@@ -1733,7 +1756,7 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         const int rw = L / 8;
         const bool words = pow2 && L >= 8 && L <= 256 && (32 % rw) == 0 &&
                            (C.plane_sites / 4) % 32 == 0;
-        C.kind = !words ? kSite : (dim == 3 && L >= 64) ? kRolling : kFlat;
+        C.kind = !words ? kSite : (dim == 3 && L >= 32) ? kRolling : kFlat;
         C.log2L = 0;
         while ((1 << C.log2L) < L) ++C.log2L;
         C.log2_rw = 0;
@@ -2437,6 +2460,15 @@ int isg_ising_set_cache_prefetch(isg_ising* H, int level, int planes) {
     H->P.l2_ahead = planes;
     H->P.pf_level = level;
     H->cache_pf_set = true;
+    destroy_graph(H);
+    return ISG_OK;
+}
+
+int isg_ising_set_dependent_launch(isg_ising* H, int enable) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_set_dependent_launch: NULL handle");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    H->pdl = enable != 0;
     destroy_graph(H);
     return ISG_OK;
 }

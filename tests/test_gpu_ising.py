@@ -219,20 +219,23 @@ def test_prefetch_depth_keeps_results(gpu):
 
 
 def test_words_per_lane_keep_results(gpu, oracle):
-    """L >= 64 rolls with four words per lane by default (L = 64: two replicas
-    per CTA task, so R = 3 leaves the last task half empty), or with two: the
+    """3D L >= 32 rolls with four words per lane by default (L = 64: two
+    replicas per CTA task, L = 32: eight, so R = 3 leaves tasks part empty;
+    at L = 32 a warp task is a whole plane), or with two: the
     same bits, through sweeps with fused measurements and exchanges, with the
-    cache prefetch on or off; an L = 128 sweep also against the oracle."""
-    sizes, R = [64, 128, 256], 3
+    cache prefetch on or off and with dependent or ordinary launches; L = 64
+    and L = 128 sweeps also against the oracle."""
+    sizes, R = [32, 64, 128, 256], 3
     out = []
-    for words, pf in ((4, 0), (2, 0), (4, 3)):
+    for words, pf, dep in ((4, 0, True), (2, 0, True), (4, 3, True), (4, 0, False)):
         b = gpu.IsingBatch(sizes, R, seed=17)
         b.set_words_per_lane(words)
         b.set_cache_prefetch(2, pf)
+        b.set_dependent_launch(dep)
         b.set_temperatures(grid(4.4, 4.6, R))
         b.step(3)
         _, bb, mm = b.pt_run(6, 3, 2)
-        out.append((bb, mm, [b.get_spins(s, r) for s in range(3) for r in range(R)]))
+        out.append((bb, mm, [b.get_spins(s, r) for s in range(4) for r in range(R)]))
         b.close()
     d64 = gpu.IsingBatch([64], 3, seed=29)
     d64.set_temperatures([4.45, 4.5, 4.55])

@@ -79,7 +79,8 @@ def measured_peaks():
 HEADLINE_PROFILE = "ising_halfsweep_L8-128x32.txt"
 HBM_PROFILE = "ising_halfsweep_L128x128.txt"
 HBM_REPLICAS = 128
-ESS_SWEEPS = 40000
+ESS_SWEEPS = 100000
+ESS_WARMUP = 10000
 
 
 def ncu_traffic(name: str):
@@ -328,9 +329,9 @@ def hbm_case(pkg, stream, flush, steps, peak, peak_kind):
 
 
 def ess_case(pkg, stream, sweeps_per_s):
-    """ESS/s of |M| on the headline batch from a run of its own: 5000 warm-up
-    sweeps, then ESS_SWEEPS sweeps with a record every 5 (at L = 128 near Tc,
-    tau_int is several hundred sweeps, so the run covers >= 50 tau).  tau is the
+    """ESS/s of |M| on the headline batch from a run of its own: ESS_WARMUP
+    warm-up sweeps, then ESS_SWEEPS sweeps with a record every 5 (at L = 128
+    near Tc, tau_int is about 1400 sweeps, so the run covers >= 50 tau).  tau is the
     larger of the windowed estimate (reproduce_validation.py:157-163) and the
     20-block estimate, per size at the slot nearest Tc.  ESS/s follows the
     spec definition: sweeps/s of the timed batch / tau_int(|M|) in sweeps,
@@ -340,7 +341,7 @@ def ess_case(pkg, stream, sweeps_per_s):
     b = pkg.IsingBatch(SIZES, REPLICAS, seed=SEED + 11)
     b.set_stream(stream)
     b.set_temperatures(T)
-    b.step(5000)
+    b.step(ESS_WARMUP)
     b.reset_sampling()
     rt, rb, rm = b.pt_run(ESS_SWEEPS, EXCHANGE_EVERY, MEASURE_EVERY)
     b.close()
@@ -359,7 +360,7 @@ def ess_case(pkg, stream, sweeps_per_s):
     h = per["128"]
     return {"value": h["ess_per_s"], "unit": "ESS/s", "observable": "|M|", "L": 128,
             "T": T[slot], "tau_int_sweeps": h["tau_int_sweeps"], "records": h["records"],
-            "sweeps": ESS_SWEEPS, "warmup_sweeps": 5000,
+            "sweeps": ESS_SWEEPS, "warmup_sweeps": ESS_WARMUP,
             "convention": "sweeps/s / tau_int(|M|) in sweeps, tau_int = 1/2 + sum rho(t) "
                           "(max of windowed and 20-block estimates); N/(2 tau) is half of it",
             "per_size": per}
@@ -1066,6 +1067,26 @@ def ncu_case_graph(kind: str):
     return 0
 
 
+def ncu_case_pt():
+    """No timing: the headline PT workload (L = 8..128 x 32 replicas) for ncu:
+    100 plain sweeps, then 10 PT steps (10 sweeps, 2 fused measurements, 1
+    exchange each), L2 flushed (256 MiB write) before every step as in the
+    timed region."""
+    import torch
+    torch.cuda.set_device(0)
+    pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
+    stream = torch.cuda.Stream()
+    b = pkg.IsingBatch(SIZES, REPLICAS, seed=SEED)
+    b.set_stream(stream)
+    b.set_temperatures(temps())
+    b.step(100)
+    b.reset_sampling()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    _timed_pt_steps(b, stream, flush, 10)
+    print("ncu case done")
+    return 0
+
+
 def ncu_case():
     """No timing: a few half-sweeps of the L=128 roofline case (128 replicas,
     268 MB of spins) for ncu captures of the half-sweep kernel."""
@@ -1098,10 +1119,11 @@ def main():
     ap.add_argument("--chain-batches", type=int, default=800)
     ap.add_argument("--pt-sweeps", type=int, default=200000)
     ap.add_argument("--ncu-case", nargs="?", const="words",
-                    choices=["words", "resident", "graph", "cgraph3", "cgraph2", "reweight",
-                             "learned"],
+                    choices=["words", "pt", "resident", "graph", "cgraph3", "cgraph2",
+                             "reweight", "learned"],
                     help="no timing: 'words' = a few half-sweeps of L=128 x 128 replicas (268 MB, "
                          "larger than L2) for an ncu capture of the half-sweep kernel; "
+                         "'pt' = 10 steps of the headline PT workload (launch list, traffic); "
                          "'resident' = one 2000-sweep schedule of an L=30 lattice; "
                          "'graph'/'cgraph3'/'cgraph2' = one 100-sweep launch of the graph "
                          "kernels (BCC 8^3, 20 replicas); 'reweight' = one WHAM analysis; "
@@ -1109,6 +1131,8 @@ def main():
     args = ap.parse_args()
     if args.ncu_case == "resident":
         return ncu_case_resident()
+    if args.ncu_case == "pt":
+        return ncu_case_pt()
     if args.ncu_case in ("graph", "cgraph3", "cgraph2", "reweight", "learned"):
         return ncu_case_graph(args.ncu_case)
     if args.ncu_case:

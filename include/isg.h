@@ -314,9 +314,16 @@ int isg_cont_set_spins(isg_cont* h, int size_index, int replica, const float* in
 int isg_cont_get_accepted(isg_cont* h, int64_t* accepted);
 int isg_cont_get_metro_accepted(isg_cont* h, int64_t* accepted);
 int isg_cont_sync(isg_cont* h);
-/* Mean device ms of one overrelaxation half-sweep, one Metropolis half-sweep
- * and one measurement (out[3]); the lattices are restored afterwards. */
+/* Mean device ms of one overrelaxation half-sweep, one Metropolis half-sweep,
+ * one measurement and one colour-1 Metropolis half-sweep with the measurement
+ * fused in (0 when the batch runs the one-site kernels) (out[4]); the
+ * lattices are restored afterwards. */
 int isg_cont_time_kernels(isg_cont* h, int n, float* out_ms);
+/* Measured sweeps of isg_cont_pt_run: 1 (default) fuses the measurement into
+ * the colour-1 Metropolis half-sweep when every size is a multiple of 4 (one
+ * pass over the lattices less); 0 measures in a separate pass.  Results are
+ * the same bit for bit. */
+int isg_cont_set_fused_measure(isg_cont* h, int enable);
 /* Site updates of one full sweep of one kind (all sizes and replicas). */
 int isg_cont_sites_per_sweep(isg_cont* h, int64_t* sites);
 

@@ -170,6 +170,7 @@ def _declare(L):
         "isg_cont_get_metro_accepted": [vp, vp],
         "isg_cont_sync": [vp],
         "isg_cont_time_kernels": [vp, i32, vp],
+        "isg_cont_set_fused_measure": [vp, i32],
         "isg_cont_sites_per_sweep": [vp, vp],
     }
     for name, args in sig.items():
@@ -1296,8 +1297,14 @@ class ContinuousBatch:
     def sync(self) -> None:
         _check(lib().isg_cont_sync(self._h))
 
+    def set_fused_measure(self, enable: bool = True) -> None:
+        """Measured PT sweeps: measurement fused into the last half-sweep (same bits)."""
+        _check(lib().isg_cont_set_fused_measure(self._h, int(bool(enable))))
+
     def time_kernels(self, n: int = 10) -> np.ndarray:
-        out = np.zeros(3, np.float32)
+        """Mean ms of an overrelaxation half-sweep, a Metropolis half-sweep, a
+        measurement and a fused Metropolis + measurement half-sweep."""
+        out = np.zeros(4, np.float32)
         _check(lib().isg_cont_time_kernels(self._h, int(n), _ptr(out)))
         return out
 

@@ -449,129 +449,6 @@ __global__ void __launch_bounds__(kCThreads, 3)
     }
 }
 
-// Metropolis on column tasks of two adjacent sites (the pair layout of
-// k_cont_or_col2): each site draws the Philox words k_cont_metro_col gives it
-// (O(3): its own block; O(2): the pair's one block) and goes through cone_test
-// exactly as there; a site neither accepted nor renormalised is written back
-// unchanged.
-template <int NC>
-__global__ void __launch_bounds__(kCThreads, NC == 2 ? 3 : 2)
-    k_cont_metro_col2(const __grid_constant__ ContParams P, int colour, int sweep_off,
-                      float cos_delta, float delta) {
-    const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
-    const bool renorm_now = P.renorm > 0 && ((sweep + 1) % (uint64_t)P.renorm) == 0;
-    const uint32_t c2 = (uint32_t)sweep;
-    const uint32_t c3 = counter_word3(ISG_TAG_CMETRO, (uint32_t)colour, sweep);
-    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
-    const int lane = threadIdx.x & 31;
-    ColRef c;
-    const bool live = col_locate(P, 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x), c);
-    unsigned n_acc = 0;
-    int rg = -1;
-    if (live) {
-        const ContClass& C = P.cls[c.ci];
-        rg = c.rg;
-        const uint32_t L = (uint32_t)C.L, half = L >> 1, plane = C.plane_sites;
-        float* own = P.spins + plane_off<NC>(C, c.r, colour, 0);
-        const float* oth = P.spins + plane_off<NC>(C, c.r, colour ^ 1, 0);
-        const uint32_t row = c.y * half;
-        const uint32_t xo1 = row + (c.k + 2 == half ? 0 : c.k + 2);  // x+ of site k+1 (p = 1)
-        const uint32_t xo0 = row + (c.k == 0 ? half - 1 : c.k - 1);  // x- of site k (p = 0)
-        const uint32_t colp = (c.y + 1 == L ? 0 : c.y + 1) * half + c.k;
-        const uint32_t colm = (c.y == 0 ? L - 1 : c.y - 1) * half + c.k;
-        const uint32_t uid = replica_uid(C.L, c.r);
-        const float beta = P.betaf[C.rep_base + P.r2t[c.rg]];
-        float2 zm[NC], zc[NC];
-        const uint32_t zmb = (c.z0 == 0 ? L - 1 : c.z0 - 1) * c.Pz;
-        float lx[NC];
-        float2 lyp[NC], lym[NC], lzp[NC], lv[NC];
-        auto ld2 = [](const float* q) { return __ldg(reinterpret_cast<const float2*>(q)); };
-        auto load_step = [&](uint32_t z) {
-            const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
-            const uint32_t zb = z * c.Pz, zpb = (z + 1 == L ? 0 : z + 1) * c.Pz;
-            const uint32_t xo = p ? xo1 : xo0;
-#pragma unroll
-            for (int k = 0; k < NC; ++k) {
-                const float* o = oth + (size_t)k * plane;
-                lx[k] = __ldg(o + zb + xo);
-                lyp[k] = ld2(o + zb + colp);
-                lym[k] = ld2(o + zb + colm);
-                lzp[k] = ld2(o + zpb + c.col);
-                lv[k] = *reinterpret_cast<const float2*>(own + (size_t)k * plane + zb + c.col);
-            }
-        };
-#pragma unroll
-        for (int k = 0; k < NC; ++k) {
-            zm[k] = ld2(oth + (size_t)k * plane + zmb + c.col);
-            zc[k] = ld2(oth + (size_t)k * plane + c.z0 * c.Pz + c.col);
-        }
-        load_step(c.z0);
-        for (uint32_t z = c.z0; z < c.z1; ++z) {
-            const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
-            const uint32_t i = z * c.Pz + c.col;  // site k; site k+1 is i + 1
-            float ha[NC], hb[NC], va[NC], vb[NC], wa[NC], wb[NC];
-            float2 zp[NC];
-#pragma unroll
-            for (int k = 0; k < NC; ++k) {
-                const float xn = lx[k];
-                const float xpa = p ? zc[k].y : zc[k].x, xma = p ? zc[k].x : xn;
-                const float xpb = p ? xn : zc[k].y, xmb = p ? zc[k].y : zc[k].x;
-                zp[k] = lzp[k];
-                ha[k] = ((xpa + xma) + (lyp[k].x + lym[k].x)) + (zp[k].x + zm[k].x);
-                hb[k] = ((xpb + xmb) + (lyp[k].y + lym[k].y)) + (zp[k].y + zm[k].y);
-                va[k] = lv[k].x;
-                vb[k] = lv[k].y;
-            }
-            if (z + 1 < c.z1) load_step(z + 1);
-            // O(3): one block per site; O(2): the pair's one block (i is even),
-            // words (x, z) for site k, (y, w) for site k+1
-            U4 u0, u1;
-            if constexpr (NC == 3) {
-                u0 = philox10(uid, i, c2, c3, k0, k1);
-                u1 = philox10(uid, i + 1, c2, c3, k0, k1);
-            } else {
-                u0 = philox10(uid, i >> 1, c2, c3, k0, k1);
-                u1 = U4{u0.y, u0.x, u0.w, u0.z};
-            }
-            const bool acc_a = cone_test<NC>(va, ha, u0, cos_delta, delta, beta, P.J, wa);
-            const bool acc_b = cone_test<NC>(vb, hb, u1, cos_delta, delta, beta, P.J, wb);
-            n_acc += (acc_a ? 1u : 0u) + (acc_b ? 1u : 0u);
-            const bool wr_a = acc_a || renorm_now, wr_b = acc_b || renorm_now;
-            if (wr_a || wr_b) {
-                float n2a = 0.f, n2b = 0.f;
-#pragma unroll
-                for (int k = 0; k < NC; ++k) {
-                    if (acc_a) va[k] = wa[k];
-                    if (acc_b) vb[k] = wb[k];
-                    n2a = fmaf(va[k], va[k], n2a);
-                    n2b = fmaf(vb[k], vb[k], n2b);
-                }
-                const float sca = renorm_now ? rsqrtf(n2a) : 1.0f;
-                const float scb = renorm_now ? rsqrtf(n2b) : 1.0f;
-#pragma unroll
-                for (int k = 0; k < NC; ++k) {
-                    float2 o2;
-                    o2.x = wr_a ? va[k] * sca : va[k];
-                    o2.y = wr_b ? vb[k] * scb : vb[k];
-                    *reinterpret_cast<float2*>(own + (size_t)k * plane + i) = o2;
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < NC; ++k) {
-                zm[k] = zc[k];
-                zc[k] = zp[k];
-            }
-        }
-    }
-    const int rg0 = __shfl_sync(ISG_FULL_MASK, rg, 0);
-    const unsigned cnt = __reduce_add_sync(ISG_FULL_MASK, n_acc);
-    if (__all_sync(ISG_FULL_MASK, rg == rg0 || rg < 0)) {
-        if (lane == 0 && rg0 >= 0 && cnt) atomicAdd(&P.metro_acc[rg0], (unsigned long long)cnt);
-    } else if (rg >= 0 && n_acc) {
-        atomicAdd(&P.metro_acc[rg], (unsigned long long)n_acc);
-    }
-}
-
 // Compensated FP32 pair (sum, error) with TwoSum addition.
 struct CF {
     float s, c;
@@ -610,6 +487,223 @@ __device__ __forceinline__ void meas_bonds(CF (&acc)[kNQ], const float (&s)[NC],
         acc[7 + a] = cf_add(acc[7 + a], sf + sb);
     }
     acc[0] = cf_add(acc[0], -J * e);
+}
+
+__device__ __forceinline__ void meas_block_store(const ContParams& P, CF (&acc)[kNQ], int chunk);
+
+// Metropolis on column tasks of two adjacent sites (the pair layout of
+// k_cont_or_col2): each site draws the Philox words k_cont_metro_col gives it
+// (O(3): its own block; O(2): the pair's one block) and goes through cone_test
+// exactly as there; a site neither accepted nor renormalised is written back
+// unchanged.  With MEAS (the last half-sweep of a measured sweep, colour 1),
+// each pair's final spins and their six neighbours of colour 0 (final too)
+// also go into the compensated sums, in the order and with the thread layout
+// of k_cont_measure2, so the fused sums equal a separate measurement bit for
+// bit.
+template <int NC, bool MEAS>
+__device__ __forceinline__ void metro2_column(const ContParams& P, const ColRef& c, int colour,
+                                              uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                                              float cos_delta, float delta, bool renorm_now,
+                                              unsigned& n_acc, CF (&acc)[kNQ]) {
+    const ContClass& C = P.cls[c.ci];
+    const uint32_t L = (uint32_t)C.L, half = L >> 1, plane = C.plane_sites;
+    float* own = P.spins + plane_off<NC>(C, c.r, colour, 0);
+    const float* oth = P.spins + plane_off<NC>(C, c.r, colour ^ 1, 0);
+    const uint32_t row = c.y * half;
+    const uint32_t xo1 = row + (c.k + 2 == half ? 0 : c.k + 2);  // x+ of site k+1 (p = 1)
+    const uint32_t xo0 = row + (c.k == 0 ? half - 1 : c.k - 1);  // x- of site k (p = 0)
+    const uint32_t colp = (c.y + 1 == L ? 0 : c.y + 1) * half + c.k;
+    const uint32_t colm = (c.y == 0 ? L - 1 : c.y - 1) * half + c.k;
+    const uint32_t uid = replica_uid(C.L, c.r);
+    const float beta = P.betaf[C.rep_base + P.r2t[c.rg]];
+    float2 zm[NC], zc[NC];
+    const uint32_t zmb = (c.z0 == 0 ? L - 1 : c.z0 - 1) * c.Pz;
+    float lx[NC];
+    float2 lyp[NC], lym[NC], lzp[NC], lv[NC];
+    auto ld2 = [](const float* q) { return __ldg(reinterpret_cast<const float2*>(q)); };
+    auto load_step = [&](uint32_t z) {
+        const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
+        const uint32_t zb = z * c.Pz, zpb = (z + 1 == L ? 0 : z + 1) * c.Pz;
+        const uint32_t xo = p ? xo1 : xo0;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            const float* o = oth + (size_t)k * plane;
+            lx[k] = __ldg(o + zb + xo);
+            lyp[k] = ld2(o + zb + colp);
+            lym[k] = ld2(o + zb + colm);
+            lzp[k] = ld2(o + zpb + c.col);
+            lv[k] = *reinterpret_cast<const float2*>(own + (size_t)k * plane + zb + c.col);
+        }
+    };
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        zm[k] = ld2(oth + (size_t)k * plane + zmb + c.col);
+        zc[k] = ld2(oth + (size_t)k * plane + c.z0 * c.Pz + c.col);
+    }
+    load_step(c.z0);
+    for (uint32_t z = c.z0; z < c.z1; ++z) {
+        const uint32_t p = (c.y + z + (uint32_t)colour) & 1u;
+        const uint32_t i = z * c.Pz + c.col;  // site k; site k+1 is i + 1
+        float ha[NC], hb[NC], va[NC], vb[NC], wa[NC], wb[NC];
+        float na[6][NC], nb[6][NC];
+        float2 zp[NC];
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            const float xn = lx[k];
+            const float xpa = p ? zc[k].y : zc[k].x, xma = p ? zc[k].x : xn;
+            const float xpb = p ? xn : zc[k].y, xmb = p ? zc[k].y : zc[k].x;
+            zp[k] = lzp[k];
+            ha[k] = ((xpa + xma) + (lyp[k].x + lym[k].x)) + (zp[k].x + zm[k].x);
+            hb[k] = ((xpb + xmb) + (lyp[k].y + lym[k].y)) + (zp[k].y + zm[k].y);
+            va[k] = lv[k].x;
+            vb[k] = lv[k].y;
+            if (MEAS) {
+                na[0][k] = xpa;
+                na[1][k] = xma;
+                na[2][k] = lyp[k].x;
+                na[3][k] = lym[k].x;
+                na[4][k] = zp[k].x;
+                na[5][k] = zm[k].x;
+                nb[0][k] = xpb;
+                nb[1][k] = xmb;
+                nb[2][k] = lyp[k].y;
+                nb[3][k] = lym[k].y;
+                nb[4][k] = zp[k].y;
+                nb[5][k] = zm[k].y;
+            }
+        }
+        if (z + 1 < c.z1) load_step(z + 1);
+        // O(3): one block per site; O(2): the pair's one block (i is even),
+        // words (x, z) for site k, (y, w) for site k+1
+        U4 u0, u1;
+        if constexpr (NC == 3) {
+            u0 = philox10(uid, i, c2, c3, k0, k1);
+            u1 = philox10(uid, i + 1, c2, c3, k0, k1);
+        } else {
+            u0 = philox10(uid, i >> 1, c2, c3, k0, k1);
+            u1 = U4{u0.y, u0.x, u0.w, u0.z};
+        }
+        const bool acc_a = cone_test<NC>(va, ha, u0, cos_delta, delta, beta, P.J, wa);
+        const bool acc_b = cone_test<NC>(vb, hb, u1, cos_delta, delta, beta, P.J, wb);
+        n_acc += (acc_a ? 1u : 0u) + (acc_b ? 1u : 0u);
+        const bool wr_a = acc_a || renorm_now, wr_b = acc_b || renorm_now;
+        if (MEAS || wr_a || wr_b) {
+            float n2a = 0.f, n2b = 0.f;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                if (acc_a) va[k] = wa[k];
+                if (acc_b) vb[k] = wb[k];
+                n2a = fmaf(va[k], va[k], n2a);
+                n2b = fmaf(vb[k], vb[k], n2b);
+            }
+            const float sca = renorm_now ? rsqrtf(n2a) : 1.0f;
+            const float scb = renorm_now ? rsqrtf(n2b) : 1.0f;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                va[k] = wr_a ? va[k] * sca : va[k];
+                vb[k] = wr_b ? vb[k] * scb : vb[k];
+            }
+            if (wr_a || wr_b) {
+#pragma unroll
+                for (int k = 0; k < NC; ++k)
+                    *reinterpret_cast<float2*>(own + (size_t)k * plane + i) = make_float2(va[k], vb[k]);
+            }
+        }
+        if (MEAS) {
+#pragma unroll
+            for (int k = 0; k < NC; ++k) acc[1 + k] = cf_add(acc[1 + k], va[k] + zc[k].x);
+            meas_bonds<NC>(acc, va, na, P.J);
+#pragma unroll
+            for (int k = 0; k < NC; ++k) acc[1 + k] = cf_add(acc[1 + k], vb[k] + zc[k].y);
+            meas_bonds<NC>(acc, vb, nb, P.J);
+        }
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            zm[k] = zc[k];
+            zc[k] = zp[k];
+        }
+    }
+}
+
+__device__ __forceinline__ void count_accepted(const ContParams& P, int rg, unsigned n_acc) {
+    // per-replica acceptance count: one atomic per warp when the warp's
+    // tasks are of one replica
+    const int lane = threadIdx.x & 31;
+    const int rg0 = __shfl_sync(ISG_FULL_MASK, rg, 0);
+    const unsigned cnt = __reduce_add_sync(ISG_FULL_MASK, n_acc);
+    if (__all_sync(ISG_FULL_MASK, rg == rg0 || rg < 0)) {
+        if (lane == 0 && rg0 >= 0 && cnt) atomicAdd(&P.metro_acc[rg0], (unsigned long long)cnt);
+    } else if (rg >= 0 && n_acc) {
+        atomicAdd(&P.metro_acc[rg], (unsigned long long)n_acc);
+    }
+}
+
+template <int NC>
+__global__ void __launch_bounds__(kCThreads, NC == 2 ? 3 : 2)
+    k_cont_metro_col2(const __grid_constant__ ContParams P, int colour, int sweep_off,
+                      float cos_delta, float delta) {
+    const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
+    const bool renorm_now = P.renorm > 0 && ((sweep + 1) % (uint64_t)P.renorm) == 0;
+    const uint32_t c2 = (uint32_t)sweep;
+    const uint32_t c3 = counter_word3(ISG_TAG_CMETRO, (uint32_t)colour, sweep);
+    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    ColRef c;
+    const bool live = col_locate(P, 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x), c);
+    unsigned n_acc = 0;
+    CF none[kNQ];
+    if (live)
+        metro2_column<NC, false>(P, c, colour, c2, c3, k0, k1, cos_delta, delta, renorm_now,
+                                 n_acc, none);
+    count_accepted(P, live ? c.rg : -1, n_acc);
+}
+
+// The colour-1 Metropolis half-sweep of a measured sweep with the measurement
+// fused in: blocks are the measurement chunks of k_cont_measure2 (kCThreads
+// two-site column tasks of one replica), and each block stores its partials
+// for k_cont_combine.  The spins are updated exactly as by k_cont_metro_col2
+// (the random stream is defined per site), and the 10 sums equal
+// k_cont_measure2's on the updated spins, so this replaces the pair
+// "Metropolis colour 1, then measure" and saves the measurement's pass over
+// both colour planes.
+template <int NC>
+__global__ void __launch_bounds__(kCThreads, 2)
+    k_cont_metro_meas2(const __grid_constant__ ContParams P, int sweep_off, float cos_delta,
+                       float delta) {
+    const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
+    const bool renorm_now = P.renorm > 0 && ((sweep + 1) % (uint64_t)P.renorm) == 0;
+    const uint32_t c2 = (uint32_t)sweep;
+    const uint32_t c3 = counter_word3(ISG_TAG_CMETRO, 1u, sweep);
+    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+    const int chunk = blockIdx.x;
+    int ci = 0;
+    while (ci + 1 < P.n_classes && P.cls[ci + 1].chunk_base <= chunk) ++ci;
+    const ContClass& C = P.cls[ci];
+    const int lc = chunk - C.chunk_base;
+    const int r = lc / C.chunks_per_rep;
+    const uint32_t L = (uint32_t)C.L, half = L >> 1, Pz = L * half;
+    const uint32_t u = (uint32_t)(lc - r * C.chunks_per_rep) * kCThreads + threadIdx.x;
+    CF acc[kNQ];
+#pragma unroll
+    for (int q = 0; q < kNQ; ++q) acc[q] = CF{0.f, 0.f};
+    unsigned n_acc = 0;
+    const bool live = u < (uint32_t)C.nseg * (Pz / 2);
+    if (live) {
+        ColRef c;
+        const uint32_t zseg = u / (Pz / 2);
+        c.ci = ci;
+        c.r = r;
+        c.rg = C.rep_base + r;
+        c.Pz = Pz;
+        c.col = 2 * (u - zseg * (Pz / 2));
+        c.y = fdiv(c.col, C.div_half);
+        c.k = c.col - c.y * half;
+        c.z0 = zseg * kColZ;
+        c.z1 = min(L, c.z0 + (uint32_t)kColZ);
+        metro2_column<NC, true>(P, c, 1, c2, c3, k0, k1, cos_delta, delta, renorm_now, n_acc,
+                                acc);
+    }
+    count_accepted(P, live ? C.rep_base + r : -1, n_acc);
+    meas_block_store(P, acc, chunk);
 }
 
 // Block reduction of the compensated sums into one FP64 partial per quantity.
@@ -963,6 +1057,7 @@ struct isg_cont {
     int sms = 1;
     int grid = 1;
     bool pairs = false;  // every size a multiple of 4: two-site column kernels
+    bool fuse_measure = true;  // measured sweeps: measurement fused into the last half-sweep
     uint64_t ksample = 0, records_made = 0, records_done = 0;
     cudaGraphExec_t graph = nullptr;
     int g_ee = 0, g_me = 0, g_period = 0, g_nor = -1, g_renorm = -1;
@@ -1048,12 +1143,35 @@ static void issue_cont_sweep(isg_cont* H, int sweep_off, double delta, int n_or)
     launch_metro(H, 1, sweep_off, delta);
 }
 
+// The colour-1 Metropolis half-sweep with the measurement fused in (two-site
+// column batches), then the FP64 combine of the block partials.
+static void launch_metro_measure(isg_cont* H, int sweep_off, double delta) {
+    const float cd = (float)std::cos(std::min(delta, M_PI));
+    if (H->nc == 3)
+        k_cont_metro_meas2<3><<<H->P.total_chunks, kCThreads, 0, H->stream>>>(H->P, sweep_off, cd,
+                                                                              (float)delta);
+    else
+        k_cont_metro_meas2<2><<<H->P.total_chunks, kCThreads, 0, H->stream>>>(H->P, sweep_off, cd,
+                                                                              (float)delta);
+    k_cont_combine<<<(H->RT + 127) / 128, 128, 0, H->stream>>>(H->P, H->d_obs);
+}
+
 static void issue_cont_sample(isg_cont* H, uint64_t k, int sweep_off, int ee, int me,
                               double delta, int n_or, int advance) {
     const bool do_m = ((k + 1) % (uint64_t)me) == 0;
     const bool do_x = ((k + 1) % (uint64_t)ee) == 0;
-    issue_cont_sweep(H, sweep_off, delta, n_or);
-    if (do_m || do_x) launch_measure(H);
+    if ((do_m || do_x) && H->pairs && H->fuse_measure) {
+        // measured sweep: the measurement rides on the last half-sweep
+        for (int j = 0; j < n_or; ++j) {
+            launch_or(H, 0);
+            launch_or(H, 1);
+        }
+        launch_metro(H, 0, sweep_off, delta);
+        launch_metro_measure(H, sweep_off, delta);
+    } else {
+        issue_cont_sweep(H, sweep_off, delta, n_or);
+        if (do_m || do_x) launch_measure(H);
+    }
     if (do_m || do_x || advance) launch_cpost(H, do_m ? 1 : 0, do_x ? 1 : 0, -1, advance);
 }
 
@@ -1588,6 +1706,15 @@ int isg_cont_sync(isg_cont* H) {
 
 // Mean device times (ms) of one overrelaxation half-sweep, one Metropolis
 // half-sweep and one measurement, on a copy that is restored afterwards.
+int isg_cont_set_fused_measure(isg_cont* H, int enable) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_cont_set_fused_measure: NULL handle");
+    cudaSetDevice(H->device);
+    ISG_CK(cudaStreamSynchronize(H->stream));
+    H->fuse_measure = enable != 0;
+    cont_destroy_graph(H);
+    return ISG_OK;
+}
+
 int isg_cont_time_kernels(isg_cont* H, int n, float* out_ms) {
     if (!H || !out_ms || n < 1) return fail(ISG_ERR_ARG, "isg_cont_time_kernels: bad argument");
     if (!H->temps_set) return fail(ISG_ERR_STATE, "isg_cont_time_kernels: temperatures not set");
@@ -1606,13 +1733,18 @@ int isg_cont_time_kernels(isg_cont* H, int n, float* out_ms) {
         e = cudaMemcpyAsync(macc.data(), H->d_macc, 8 * H->RT, cudaMemcpyDeviceToHost, H->stream);
     if (e == cudaSuccess) e = cudaEventCreate(&a);
     if (e == cudaSuccess) e = cudaEventCreate(&b);
-    for (int which = 0; which < 3 && e == cudaSuccess; ++which) {
+    for (int which = 0; which < 4 && e == cudaSuccess; ++which) {
         float total = 0.f;
+        if (which == 3 && !H->pairs) {
+            out_ms[3] = 0.f;
+            break;
+        }
         for (int i = 0; i < n && e == cudaSuccess; ++i) {
             e = cudaEventRecord(a, H->stream);
             if (which == 0) launch_or(H, i & 1);
             else if (which == 1) launch_metro(H, i & 1, i >> 1, 0.5);
-            else launch_measure(H);
+            else if (which == 2) launch_measure(H);
+            else launch_metro_measure(H, i, 0.5);
             if (e == cudaSuccess) e = cudaEventRecord(b, H->stream);
             if (e == cudaSuccess) e = cudaEventSynchronize(b);
             float ms = 0.f;

@@ -94,6 +94,32 @@ def test_two_site_kernels_match_one_site(gpu, nc):
 
 
 @pytest.mark.parametrize("nc", [3, 2])
+def test_fused_measurement_matches_separate_pass(gpu, nc):
+    """Measured PT sweeps fuse the measurement into the colour-1 Metropolis
+    half-sweep (sizes multiples of 4): records (slots, E, M, bond sums) and
+    spins equal those of the separate measurement pass bit for bit, through
+    exchanges and a renormalisation sweep."""
+    sizes, R = [8, 12, 16], 3
+    temps = [1.3, 1.45, 1.6] if nc == 3 else [1.9, 2.2, 2.5]
+    out = []
+    for fused in (True, False):
+        b = gpu.ContinuousBatch(sizes, R, nc, seed=61)
+        b.set_fused_measure(fused)
+        b.set_temperatures(temps)
+        b.sweep(4, 0.6, 2)
+        b.reset_sampling()
+        rec = b.pt_run(40, 4, 2, delta=0.6, n_overrelax=2, renorm_every=10)
+        out.append((rec, [b.get_spins(s_, r) for s_ in range(3) for r in range(R)],
+                    b.metropolis_accepted()))
+        b.close()
+    for x, y in zip(out[0][0], out[1][0]):
+        assert np.array_equal(x, y)
+    for x, y in zip(out[0][1], out[1][1]):
+        assert np.array_equal(x, y)
+    assert np.array_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("nc", [3, 2])
 def test_overrelaxation_conserves_energy(gpu, nc):
     """overrelax.rs:74-86 (1e-8 in FP64); FP32 device: relative 1e-5."""
     b = gpu.ContinuousBatch([16, 32], 3, nc, seed=9)

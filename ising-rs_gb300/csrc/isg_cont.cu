@@ -1,7 +1,8 @@
 // isg_cont.cu — continuous-spin O(n) models (n = 3 Heisenberg, n = 2 XY) on
 // periodic cubic lattices: checkerboard Metropolis with a cone proposal,
-// microcanonical overrelaxation, deterministic compensated-FP32 observables
-// with an FP64 combine, device replica exchange and the PT cycle as a graph.
+// microcanonical overrelaxation, deterministic observables summed exactly in
+// fixed point (2^-24) and converted to FP64 at the combine, device replica
+// exchange and the PT cycle as a graph.
 //
 // Reference path being replaced (faulknco/ising-rs):
 //   src/cuda/continuous_spin_kernel.cu:9-142  Metropolis + overrelaxation
@@ -67,9 +68,10 @@ struct ContParams {
     const int32_t* r2t;
     unsigned long long* ctrl;  // [0] sweep base
     unsigned long long* metro_acc;
-    double* partials;          // [chunks][kNQ]
+    long long* partials;       // [chunks][kNQ] fixed-point block sums (2^-24 units)
     uint64_t seed;
     float J;
+    double Jd;
     int n_classes;
     int renorm;
     int64_t total_sites;
@@ -449,29 +451,22 @@ __global__ void __launch_bounds__(kCThreads, 3)
     }
 }
 
-// Compensated FP32 pair (sum, error) with TwoSum addition.
-struct CF {
-    float s, c;
-};
-__device__ __forceinline__ CF cf_add(CF a, float b) {
-    const float t = a.s + b;
-    const float bb = t - a.s;
-    const float err = (a.s - (t - bb)) + (b - bb);
-    return CF{t, a.c + err};
-}
-__device__ __forceinline__ CF cf_merge(CF a, CF b) {
-    CF r = cf_add(a, b.s);
-    r.c += b.c;
-    return r;
-}
+// Fixed-point sums of the measurement: every term (a spin component, a bond
+// product S.S' or (S x S')_z, all of magnitude <= 1 up to FP32 drift) is
+// rounded once to a multiple of 2^-24 and summed exactly in integers: int32
+// per thread (at most 32 terms of 2^24: < 2^30), int64 across threads and
+// blocks.  Exact integer sums do not depend on the order of summation; the
+// only rounding is the one per term, below the FP32 rounding of the products.
+constexpr float kFix = 16777216.0f;  // 2^24
+__device__ __forceinline__ int fx(float x) { return __float2int_rn(x * kFix); }
 
 // The six bonds of one colour-1 site s with neighbours n (x+, x-, y+, y-,
-// z+, z-) into the compensated sums: per axis a the forward bond (i, i+a) and
-// the backward bond (i-a, i), C_a += S.S, S_a += (S x S')_z, E += -J S.S.
+// z+, z-) into the sums: per axis a the forward bond (i, i+a) and the
+// backward bond (i-a, i), C_a += S.S, S_a += (S x S')_z.  E = -J (C_x + C_y +
+// C_z) is formed at the combine.
 template <int NC>
-__device__ __forceinline__ void meas_bonds(CF (&acc)[kNQ], const float (&s)[NC],
-                                           const float (&n)[6][NC], float J) {
-    float e = 0.f;
+__device__ __forceinline__ void meas_bonds(int (&acc)[kNQ], const float (&s)[NC],
+                                           const float (&n)[6][NC]) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         float cf = 0.f, cb = 0.f;
@@ -482,14 +477,12 @@ __device__ __forceinline__ void meas_bonds(CF (&acc)[kNQ], const float (&s)[NC],
         }
         const float sf = s[0] * n[2 * a][1] - s[1] * n[2 * a][0];
         const float sb = n[2 * a + 1][0] * s[1] - n[2 * a + 1][1] * s[0];
-        e += cf + cb;
-        acc[4 + a] = cf_add(acc[4 + a], cf + cb);
-        acc[7 + a] = cf_add(acc[7 + a], sf + sb);
+        acc[4 + a] += fx(cf) + fx(cb);
+        acc[7 + a] += fx(sf) + fx(sb);
     }
-    acc[0] = cf_add(acc[0], -J * e);
 }
 
-__device__ __forceinline__ void meas_block_store(const ContParams& P, CF (&acc)[kNQ], int chunk);
+__device__ __forceinline__ void meas_block_store(const ContParams& P, int (&acc)[kNQ], int chunk);
 
 // Metropolis on column tasks of two adjacent sites (the pair layout of
 // k_cont_or_col2): each site draws the Philox words k_cont_metro_col gives it
@@ -497,14 +490,14 @@ __device__ __forceinline__ void meas_block_store(const ContParams& P, CF (&acc)[
 // exactly as there; a site neither accepted nor renormalised is written back
 // unchanged.  With MEAS (the last half-sweep of a measured sweep, colour 1),
 // each pair's final spins and their six neighbours of colour 0 (final too)
-// also go into the compensated sums, in the order and with the thread layout
+// also go into the fixed-point sums, in the order and with the thread layout
 // of k_cont_measure2, so the fused sums equal a separate measurement bit for
 // bit.
 template <int NC, bool MEAS>
 __device__ __forceinline__ void metro2_column(const ContParams& P, const ColRef& c, int colour,
                                               uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
                                               float cos_delta, float delta, bool renorm_now,
-                                              unsigned& n_acc, CF (&acc)[kNQ]) {
+                                              unsigned& n_acc, int (&acc)[kNQ]) {
     const ContClass& C = P.cls[c.ci];
     const uint32_t L = (uint32_t)C.L, half = L >> 1, plane = C.plane_sites;
     float* own = P.spins + plane_off<NC>(C, c.r, colour, 0);
@@ -611,11 +604,11 @@ __device__ __forceinline__ void metro2_column(const ContParams& P, const ColRef&
         }
         if (MEAS) {
 #pragma unroll
-            for (int k = 0; k < NC; ++k) acc[1 + k] = cf_add(acc[1 + k], va[k] + zc[k].x);
-            meas_bonds<NC>(acc, va, na, P.J);
+            for (int k = 0; k < NC; ++k) acc[1 + k] += fx(va[k]) + fx(zc[k].x);
+            meas_bonds<NC>(acc, va, na);
 #pragma unroll
-            for (int k = 0; k < NC; ++k) acc[1 + k] = cf_add(acc[1 + k], vb[k] + zc[k].y);
-            meas_bonds<NC>(acc, vb, nb, P.J);
+            for (int k = 0; k < NC; ++k) acc[1 + k] += fx(vb[k]) + fx(zc[k].y);
+            meas_bonds<NC>(acc, vb, nb);
         }
 #pragma unroll
         for (int k = 0; k < NC; ++k) {
@@ -650,7 +643,7 @@ __global__ void __launch_bounds__(kCThreads, NC == 2 ? 3 : 2)
     ColRef c;
     const bool live = col_locate(P, 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x), c);
     unsigned n_acc = 0;
-    CF none[kNQ];
+    int none[kNQ];
     if (live)
         metro2_column<NC, false>(P, c, colour, c2, c3, k0, k1, cos_delta, delta, renorm_now,
                                  n_acc, none);
@@ -682,9 +675,9 @@ __global__ void __launch_bounds__(kCThreads, 2)
     const int r = lc / C.chunks_per_rep;
     const uint32_t L = (uint32_t)C.L, half = L >> 1, Pz = L * half;
     const uint32_t u = (uint32_t)(lc - r * C.chunks_per_rep) * kCThreads + threadIdx.x;
-    CF acc[kNQ];
+    int acc[kNQ];
 #pragma unroll
-    for (int q = 0; q < kNQ; ++q) acc[q] = CF{0.f, 0.f};
+    for (int q = 0; q < kNQ; ++q) acc[q] = 0;
     unsigned n_acc = 0;
     const bool live = u < (uint32_t)C.nseg * (Pz / 2);
     if (live) {
@@ -706,24 +699,25 @@ __global__ void __launch_bounds__(kCThreads, 2)
     meas_block_store(P, acc, chunk);
 }
 
-// Block reduction of the compensated sums into one FP64 partial per quantity.
-__device__ __forceinline__ void meas_block_store(const ContParams& P, CF (&acc)[kNQ], int chunk) {
-    __shared__ CF red[kCThreads / 32][kNQ];
+// Block reduction of the fixed-point sums into one int64 partial per quantity
+// (slot 0, the energy, is formed at the combine).  A thread's sums are below
+// 2^30, so a warp sums their upper parts (>> 8) and low bytes separately in
+// int32 and joins them in int64.
+__device__ __forceinline__ void meas_block_store(const ContParams& P, int (&acc)[kNQ], int chunk) {
+    __shared__ long long red[kCThreads / 32][kNQ];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-    for (int q = 0; q < kNQ; ++q) {
-        CF v = acc[q];
-        for (int o = 16; o > 0; o >>= 1) {
-            CF w{__shfl_down_sync(ISG_FULL_MASK, v.s, o), __shfl_down_sync(ISG_FULL_MASK, v.c, o)};
-            v = cf_merge(v, w);
-        }
-        if (lane == 0) red[wid][q] = v;
+    for (int q = 1; q < kNQ; ++q) {
+        const int hi = __reduce_add_sync(ISG_FULL_MASK, acc[q] >> 8);
+        const unsigned lo = __reduce_add_sync(ISG_FULL_MASK, (unsigned)(acc[q] & 0xFF));
+        if (lane == 0) red[wid][q] = (long long)hi * 256 + (long long)lo;
     }
     __syncthreads();
     if (threadIdx.x < kNQ) {
-        CF v = red[0][threadIdx.x];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = cf_merge(v, red[w][threadIdx.x]);
-        P.partials[(int64_t)chunk * kNQ + threadIdx.x] = (double)v.s + (double)v.c;
+        long long v = 0;
+        if (threadIdx.x > 0)
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
+        P.partials[(int64_t)chunk * kNQ + threadIdx.x] = v;
     }
 }
 
@@ -743,9 +737,9 @@ __global__ void __launch_bounds__(kCThreads) k_cont_measure(const __grid_constan
     const int r = lc / C.chunks_per_rep;
     const uint32_t L = (uint32_t)C.L, half = L >> 1, Pz = L * half, plane = C.plane_sites;
     const uint32_t u = (uint32_t)(lc - r * C.chunks_per_rep) * kCThreads + threadIdx.x;
-    CF acc[kNQ];
+    int acc[kNQ];
 #pragma unroll
-    for (int q = 0; q < kNQ; ++q) acc[q] = CF{0.f, 0.f};
+    for (int q = 0; q < kNQ; ++q) acc[q] = 0;
     if (u < (uint32_t)C.nseg * Pz) {
         const uint32_t zseg = u / Pz, col = u - zseg * Pz;
         const uint32_t y = fdiv(col, C.div_half), k = col - y * half;
@@ -781,9 +775,9 @@ __global__ void __launch_bounds__(kCThreads) k_cont_measure(const __grid_constan
                 n[1][c] = p ? zc[c] : xn;
                 n[4][c] = zp[c];
                 n[5][c] = zm[c];
-                acc[1 + c] = cf_add(acc[1 + c], s[c] + zc[c]);
+                acc[1 + c] += fx(s[c]) + fx(zc[c]);
             }
-            meas_bonds<NC>(acc, s, n, P.J);
+            meas_bonds<NC>(acc, s, n);
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
                 zm[c] = zc[c];
@@ -808,9 +802,9 @@ __global__ void __launch_bounds__(kCThreads, 3) k_cont_measure2(const __grid_con
     const int r = lc / C.chunks_per_rep;
     const uint32_t L = (uint32_t)C.L, half = L >> 1, Pz = L * half, plane = C.plane_sites;
     const uint32_t u = (uint32_t)(lc - r * C.chunks_per_rep) * kCThreads + threadIdx.x;
-    CF acc[kNQ];
+    int acc[kNQ];
 #pragma unroll
-    for (int q = 0; q < kNQ; ++q) acc[q] = CF{0.f, 0.f};
+    for (int q = 0; q < kNQ; ++q) acc[q] = 0;
     if (u < (uint32_t)C.nseg * (Pz / 2)) {
         const uint32_t zseg = u / (Pz / 2), col = 2 * (u - zseg * (Pz / 2));
         const uint32_t y = fdiv(col, C.div_half), k = col - y * half;
@@ -859,11 +853,11 @@ __global__ void __launch_bounds__(kCThreads, 3) k_cont_measure2(const __grid_con
                 nb[5][c] = zm[c].y;
             }
 #pragma unroll
-            for (int c = 0; c < NC; ++c) acc[1 + c] = cf_add(acc[1 + c], sa[c] + zc[c].x);
-            meas_bonds<NC>(acc, sa, na, P.J);
+            for (int c = 0; c < NC; ++c) acc[1 + c] += fx(sa[c]) + fx(zc[c].x);
+            meas_bonds<NC>(acc, sa, na);
 #pragma unroll
-            for (int c = 0; c < NC; ++c) acc[1 + c] = cf_add(acc[1 + c], sb[c] + zc[c].y);
-            meas_bonds<NC>(acc, sb, nb, P.J);
+            for (int c = 0; c < NC; ++c) acc[1 + c] += fx(sb[c]) + fx(zc[c].y);
+            meas_bonds<NC>(acc, sb, nb);
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
                 zm[c] = zc[c];
@@ -874,7 +868,8 @@ __global__ void __launch_bounds__(kCThreads, 3) k_cont_measure2(const __grid_con
     meas_block_store(P, acc, chunk);
 }
 
-// FP64 combine of the block partials of each replica, in chunk order.
+// Combine of the block partials of each replica: exact int64 sums, then
+// one conversion to FP64 (units of 2^-24); E = -J (C_x + C_y + C_z).
 __global__ void k_cont_combine(const __grid_constant__ ContParams P, double* out) {
     const int rg = blockIdx.x * blockDim.x + threadIdx.x;
     int ci = 0;
@@ -882,12 +877,14 @@ __global__ void k_cont_combine(const __grid_constant__ ContParams P, double* out
     const ContClass& C = P.cls[ci];
     if (rg >= C.rep_base + C.R) return;
     const int r = rg - C.rep_base;
-    double q[kNQ];
-    for (int k = 0; k < kNQ; ++k) q[k] = 0.0;
+    long long q[kNQ];
+    for (int k = 0; k < kNQ; ++k) q[k] = 0;
     const int c0 = C.chunk_base + r * C.chunks_per_rep;
     for (int c = 0; c < C.chunks_per_rep; ++c)
-        for (int k = 0; k < kNQ; ++k) q[k] += P.partials[(int64_t)(c0 + c) * kNQ + k];
-    for (int k = 0; k < kNQ; ++k) out[(int64_t)rg * kNQ + k] = q[k];
+        for (int k = 1; k < kNQ; ++k) q[k] += P.partials[(int64_t)(c0 + c) * kNQ + k];
+    const double unit = 1.0 / 16777216.0;
+    out[(int64_t)rg * kNQ] = __dmul_rn(-P.Jd, (double)(q[4] + q[5] + q[6]) * unit);
+    for (int k = 1; k < kNQ; ++k) out[(int64_t)rg * kNQ + k] = (double)q[k] * unit;
 }
 
 __global__ void k_cont_init(const __grid_constant__ ContParams P, int nc) {
@@ -1043,7 +1040,7 @@ struct isg_cont {
     int32_t* d_t2r = nullptr;
     unsigned long long* d_ctrl = nullptr;
     unsigned long long* d_macc = nullptr;
-    double* d_partials = nullptr;
+    long long* d_partials = nullptr;
     double* d_obs = nullptr;
     int64_t ring_cap = 0;
     int32_t* d_rec_t = nullptr;
@@ -1289,6 +1286,7 @@ int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas,
     P.total_chunks = chunk;
     P.seed = seed;
     P.J = 1.0f;
+    P.Jd = 1.0;
     P.renorm = 0;
     H->n_floats = off;
     const int RT = H->RT;
@@ -1310,7 +1308,7 @@ int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas,
     ALLOC(H->d_t2r, sizeof(int32_t) * RT);
     ALLOC(H->d_ctrl, sizeof(unsigned long long) * (1 + 3 * kCMaxClasses));
     ALLOC(H->d_macc, sizeof(unsigned long long) * RT);
-    ALLOC(H->d_partials, sizeof(double) * (size_t)chunk * kNQ);
+    ALLOC(H->d_partials, sizeof(long long) * (size_t)chunk * kNQ);
     ALLOC(H->d_obs, sizeof(double) * (size_t)RT * kNQ);
     ALLOC(H->d_rec_t, sizeof(int32_t) * (size_t)H->ring_cap * RT);
     ALLOC(H->d_rec_e, sizeof(double) * (size_t)H->ring_cap * RT);
@@ -1425,6 +1423,7 @@ int isg_cont_set_temperatures(isg_cont* H, const double* temps, double J) {
     ISG_CK(cudaStreamSynchronize(H->stream));
     H->J = J;
     H->P.J = (float)J;
+    H->P.Jd = J;
     H->temps_set = true;
     cont_destroy_graph(H);
     return ISG_OK;

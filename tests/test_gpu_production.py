@@ -130,8 +130,9 @@ def _ref_scheme(g: np.ndarray, L: int, nc: int):
 
 @pytest.mark.parametrize("nc,sizes,temps,delta,n_or", PROD, ids=["O3", "O2"])
 def test_observable_error_vs_fp64(gpu, oracle, nc, sizes, temps, delta, n_or):
-    """Each observable of a device measurement against the FP64 sum over the
-    same spins, and the same for the reference's scheme; the derived chi, Cv,
+    """Each observable of a device measurement (fixed-point sums, FP64 at the
+    combine) against the FP64 sum over the same spins, and the same for the
+    reference's scheme; the derived chi, Cv,
     U4 (and, for O(2), the helicity modulus) are formed from 12 measurements
     both ways.  Writes the table to $ISG_REPORT_DIR/fp64_error_O<n>.json when
     that variable is set."""
@@ -198,7 +199,7 @@ def test_observable_error_vs_fp64(gpu, oracle, nc, sizes, temps, delta, n_or):
             rep[key] = {"device": float(max(dd)),
                         "reference_scheme": float(max(dr)) if dr else None}
         report[str(L)] = rep
-        # the device's compensated reduction is bounded as the tolerance states
+        # the device's reduction is bounded as the tolerance states
         assert rep["E"]["device"] < 2e-6 * 3
         assert rep["M"]["device"] < 2e-6
         assert rep["bond_sums"]["device"] < 2e-6 * 3

@@ -3,9 +3,10 @@
 It serves callers that cannot call cudaMalloc, such as code whose device memory
 all comes from its own pool, so it keeps its block partials in a fixed device
 array. This test calls it through the C ABI on lattices that the test owns, and
-checks it against the allocating path (isg_cont_measure). Both reduce in
-compensated FP32 with an FP64 combine, in different orders, so the tolerance is
-2e-6 per bond, as in tests/test_gpu_continuous.py. It makes two calls in a row
+checks it against the allocating path (isg_cont_measure). The allocating path
+sums in exact fixed point and this one in compensated FP32 with an FP64 combine,
+so the two differ by rounding and the tolerance is 2e-6 per bond, as in
+tests/test_gpu_continuous.py. It makes two calls in a row
 on different lattices, because the second call reuses the partials the first one
 left behind. The file is named to run last, and the test also passes on its own
 in a fresh process."""

@@ -214,8 +214,10 @@ int isg_ising_get_sweep(isg_ising* h, uint64_t* sweep);
 
 int isg_ising_sync(isg_ising* h);
 
-/* Launch shape of the half-sweep kernel: threads per block and blocks per SM
- * (0 = occupancy maximum).  Results never depend on it. */
+/* Launch shape of the half-sweep kernel: blocks per SM (0 = occupancy
+ * maximum).  Every size, one-site tasks included, runs in the one 256-thread
+ * half-sweep kernel, so `threads` (64, 128, 256 or 512) is validated and
+ * kept but no longer changes the launch.  Results never depend on either. */
 int isg_ising_set_launch(isg_ising* h, int threads, int blocks_per_sm);
 /* Prefetch depth of the rolling half-sweep (3D, L = 64..256): 1 = loads one
  * plane ahead, 3 blocks per SM; 2 = two planes ahead, 2 blocks per SM;

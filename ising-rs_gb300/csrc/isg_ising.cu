@@ -15,19 +15,16 @@
 // (z*L*L + y*L + x) >> 1, so one 32-bit word carries 4 consecutive same-colour
 // sites of a row.  Planes of one size are contiguous ([R][2][L^dim/2] bytes).
 //
-// Half-sweep kernels (one launch covers every size and replica):
-//  * word kernel — for L in {8..256}, a power of two whose row (L/8 words)
-//    divides a warp.  One lane updates one word (4 sites) per warp task of 32
-//    words; the x-neighbour word shifted by one byte comes from the row's
-//    other lanes through __shfl_sync + funnel shift; neighbour counts are
-//    byte-SIMD sums of (word & 0x02020202); the acceptance threshold comes
-//    from a 16-entry table of the replica's temperature in shared memory.
-//    Warps own contiguous task ranges (persistent grid) so a warp changes
-//    replica rarely and flushes its integer E/M partials with one 64-bit
-//    atomic per replica change.
-//  * site kernel — any other even L: one thread per site, same stream and
-//    update rule.
-// Both produce identical bits for the same state (the random stream is
+// Half-sweep kernel (one launch covers every size and replica):
+//  * rolling tasks — 3D L = 32..256, a power of two: a warp walks z down a
+//    column of 128 words (4 sites each), four adjacent words per lane; byte-
+//    parallel Metropolis decisions against thresholds held as bytes.
+//  * flat tasks — 3D L = 8, 16 and 2D: one word per lane, 32 per warp task;
+//    the x-neighbour word shifted by one byte comes from the row's other
+//    lanes through __shfl_sync + funnel shift.
+//  * site tasks — any other even L: one site per thread, strided over the
+//    whole launch.
+// All produce identical bits for the same state (the random stream is
 // defined per site, not per thread).
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -68,7 +65,8 @@ constexpr int kMaxReplicas = 1024;
 //     words of the other colour in registers.
 //   kFlat    (other power-of-two L with L/8 dividing 32): 32 consecutive words,
 //     one per lane.
-//   kSite    (any other even L): one thread per site (site kernel).
+//   kSite    (any other even L): one thread per site (site tasks of the same
+//     launch).
 enum { kSite = 0, kFlat = 1, kRolling = 2 };
 
 struct IsingClass {
@@ -90,6 +88,9 @@ struct IsingClass {
     int log2_wpl;             // rolling: log2(words per lane), 1 or 2
     int log2_unit;            // rolling: a CTA task is 1 << log2_unit work units of 512 words
     int log2_rpc;             // rolling: replicas per CTA task (plane of fewer than 8 y-blocks)
+    FastDiv div_half, div_L;  // site kind: divisions by L/2 and L
+    FastDiv div_plane;        // site kind: division by plane_sites (when R * plane_sites < 2^31)
+    int plane_fast;
     int64_t site_base;        // site kind: first site (over colour planes)
     int64_t site_end;
 };
@@ -578,6 +579,82 @@ __device__ __forceinline__ void rolling_quad_step(
     o = o1;
 }
 
+
+// One site of a one-site task (any even L), split in two so that a thread
+// can issue the loads of several sites before it decides any: site_gather
+// reads the site's down bit, its down-neighbour count and the other colour's
+// byte at the same index (for the magnetisation), and locates its coarse
+// random (block, Philox word, byte); site_decide draws the blocks and flips.
+// The rule is the word kernels' per-site definition (coarse 7 bits of byte
+// v & 3 of word t & 3 of block v >> 2, fine 25 bits on a tie).
+struct SiteWork {
+    uint8_t* own;
+    const uint32_t* tab;
+    uint32_t i, uid, blk, sel;  // sel: byte v & 3 | (word t & 3) << 2
+    int d, nd, oth_i, rg;
+};
+
+template <int DIM>
+__device__ __forceinline__ void site_gather(SiteWork& w, uint8_t* own, const uint8_t* oth,
+                                            uint32_t i, uint32_t L, const FastDiv& dh,
+                                            const FastDiv& dL, uint32_t colour) {
+    const uint32_t half = L >> 1;
+    const uint32_t row = fdiv(i, dh);
+    const uint32_t k = i - row * half;
+    uint32_t y, z, p;
+    if (DIM == 3) {
+        z = fdiv(row, dL);
+        y = row - z * L;
+        p = (y + z + colour) & 1u;
+    } else {
+        y = row;
+        z = 0;
+        p = (y + colour) & 1u;
+    }
+    const uint32_t x = 2 * k + p;
+    const uint32_t xp = x + 1 == L ? 0 : x + 1, xm = x == 0 ? L - 1 : x - 1;
+    const uint32_t yp = y + 1 == L ? 0 : y + 1, ym = y == 0 ? L - 1 : y - 1;
+    const uint32_t rowL = (z * L + y) * L;
+    int nd = (int)__ldg(oth + ((rowL + xp) >> 1)) + (int)__ldg(oth + ((rowL + xm) >> 1)) +
+             (int)__ldg(oth + (((z * L + yp) * L + x) >> 1)) +
+             (int)__ldg(oth + (((z * L + ym) * L + x) >> 1));
+    if (DIM == 3) {
+        const uint32_t zp = z + 1 == L ? 0 : z + 1, zm = z == 0 ? L - 1 : z - 1;
+        nd += (int)__ldg(oth + (((zp * L + y) * L + x) >> 1)) +
+              (int)__ldg(oth + (((zm * L + y) * L + x) >> 1));
+    }
+    w.own = own;
+    w.i = i;
+    w.nd = nd;
+    w.d = own[i];
+    w.oth_i = (int)__ldg(oth + i);
+    const uint32_t S = DIM == 3 ? half * L : half;  // sites of the colour per slab
+    const uint32_t t = DIM == 3 ? z : y;
+    const uint32_t v = (t >> 2) * S + (i - t * S);
+    w.blk = v >> 2;
+    w.sel = (v & 3u) | ((t & 3u) << 2);
+}
+
+__device__ __forceinline__ void site_decide(SiteWork& w, uint32_t c2, uint32_t c3, uint32_t k0,
+                                            uint32_t k1) {
+    const uint32_t th = w.tab[w.d * 8 + w.nd];
+    const U4 u = philox10(w.uid, w.blk, c2, c3, k0, k1);
+    const uint32_t tw = w.sel >> 2;
+    const uint32_t uw = tw == 0 ? u.x : tw == 1 ? u.y : tw == 2 ? u.z : u.w;
+    const uint32_t c7 = (uw >> (8u * (w.sel & 3u))) & 0x7Fu;
+    bool acc = c7 < (th >> 25);
+    if (c7 == (th >> 25)) {
+        const U4 f = philox10(w.uid, 0x80000000u | (w.i >> 2), c2, c3, k0, k1);
+        const uint32_t ji = w.i & 3u;
+        const uint32_t fw = ji == 0 ? f.x : ji == 1 ? f.y : ji == 2 ? f.z : f.w;
+        acc = ((c7 << 25) | (fw >> 7)) <= th;
+    }
+    if (acc) {
+        w.d ^= 1;
+        w.own[w.i] = (uint8_t)w.d;
+    }
+}
+
 // MODE 0: update; 1: update then accumulate bond/mag of the new state;
 // 2: accumulate only (no update).
 //
@@ -844,110 +921,51 @@ __global__ void __launch_bounds__(256, MINB)
     }
     if (MODE != 2) drain_ties<MODE>(q, tq, lane, tab, pre, P, cur_own, macc);
     if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
-}
 
-template <bool CG>
-__device__ __forceinline__ int ld_spin(const uint8_t* p) {
-    if (CG) return (int)__ldcg(p);
-    return (int)*p;
-}
-
-// Metropolis update of the site at colour index i of one colour plane (any
-// even L): own / oth are the lattice's planes of this colour and the other,
-// tab its 16-entry threshold table.  Returns the site's down bit after the
-// update (before it when !update) and its down-neighbour count in nd_out.
-// CG loads the other colour through L2 only (planes written by other CTAs of
-// a cluster).
-template <int DIM, bool CG>
-__device__ __forceinline__ int site_update(uint8_t* own, const uint8_t* oth, uint32_t i, uint32_t L,
-                                           uint32_t plane, uint32_t colour, const uint32_t* tab,
-                                           uint32_t uid, uint32_t c2, uint32_t c3, uint32_t k0,
-                                           uint32_t k1, bool update, int& nd_out) {
-    const uint32_t half = L >> 1;
-    const uint32_t row = i / half;
-    const uint32_t k = i - row * half;
-    uint32_t y, z, p;
-    if (DIM == 3) {
-        y = row % L;
-        z = row / L;
-        p = (y + z + colour) & 1u;
-    } else {
-        y = row;
-        z = 0;
-        p = (y + colour) & 1u;
-    }
-    const uint32_t x = 2 * k + p;
-    const uint32_t xp = (x + 1) % L, xm = (x + L - 1) % L;
-    const uint32_t yp = (y + 1) % L, ym = (y + L - 1) % L;
-    const uint64_t rowL = (uint64_t)(z * L + y) * L;
-    int nd = ld_spin<CG>(oth + ((rowL + xp) >> 1)) + ld_spin<CG>(oth + ((rowL + xm) >> 1)) +
-             ld_spin<CG>(oth + (((uint64_t)(z * L + yp) * L + x) >> 1)) +
-             ld_spin<CG>(oth + (((uint64_t)(z * L + ym) * L + x) >> 1));
-    if (DIM == 3) {
-        const uint32_t zp = (z + 1) % L, zm = (z + L - 1) % L;
-        nd += ld_spin<CG>(oth + (((uint64_t)(zp * L + y) * L + x) >> 1)) +
-              ld_spin<CG>(oth + (((uint64_t)(zm * L + y) * L + x) >> 1));
-    }
-    nd_out = nd;
-    int d = own[i];
-    if (update) {
-        const uint32_t th = tab[d * 8 + nd];
-        // slab S = sites of this colour per z-plane (3D) or row (2D); slab quad
-        // t>>2 shares Philox blocks: v = (t>>2)*S + (i mod S), block v >> 2,
-        // word t & 3, coarse = low 7 bits of byte v & 3
-        const uint32_t S = plane / L;
-        const uint32_t t = DIM == 3 ? z : y;
-        const uint32_t v = (t >> 2) * S + (i - t * S);
-        const U4 u = philox10(uid, v >> 2, c2, c3, k0, k1);
-        const uint32_t tw = t & 3u;
-        const uint32_t uw = tw == 0 ? u.x : tw == 1 ? u.y : tw == 2 ? u.z : u.w;
-        const uint32_t c7 = (uw >> (8u * (v & 3u))) & 0x7Fu;
-        bool acc = c7 < (th >> 25);
-        if (c7 == (th >> 25)) {
-            const U4 f = philox10(uid, 0x80000000u | (i >> 2), c2, c3, k0, k1);
-            const uint32_t ji = i & 3u;
-            const uint32_t fw = ji == 0 ? f.x : ji == 1 ? f.y : ji == 2 ? f.z : f.w;
-            acc = ((c7 << 25) | (fw >> 7)) <= th;
-        }
-        if (acc) {
-            d ^= 1;
-            own[i] = (uint8_t)d;
-        }
-    }
-    return d;
-}
-
-template <int DIM, int MODE>
-__global__ void __launch_bounds__(kMaxThreads)
-    k_ising_sites(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
-    const uint64_t sweep = P.ctrl[0] + (uint64_t)sweep_off;
-    const uint32_t c2 = (uint32_t)sweep;
-    const uint32_t c3 = counter_word3(ISG_TAG_ISING, (uint32_t)colour, sweep);
-    const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < P.total_sites;
-         g += stride) {
-        int ci = 0;
-        while (P.cls[ci].site_end <= g) ++ci;
-        const IsingClass& C = P.cls[ci];
-        const int64_t lg = g - C.site_base;
-        const int r = (int)(lg / C.plane_sites);
-        const uint32_t i = (uint32_t)(lg - (int64_t)r * C.plane_sites);
-        uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
-        uint8_t* own = base + (int64_t)colour * C.plane_sites;
-        const uint8_t* oth = base + (int64_t)(colour ^ 1) * C.plane_sites;
-        const int rg = C.rep_base + r;
-        const uint32_t* tab = P.thr + (int64_t)(C.rep_base + (MODE != 2 ? P.r2t[rg] : 0)) * 16;
-        int nd;
-        const int d = site_update<DIM, false>(own, oth, i, (uint32_t)C.L, C.plane_sites,
-                                              (uint32_t)colour, tab, replica_uid(C.L, r), c2, c3,
-                                              k0, k1, MODE != 2, nd);
-        if (MODE != 0) {
-            const int s = 1 - 2 * d;
-            const long long b = (long long)(s * (2 * DIM - 2 * nd));
-            const long long m = (long long)(s + 1 - 2 * oth[i]);
-            atomicAdd(&P.acc[2 * rg], (unsigned long long)b);
-            atomicAdd(&P.acc[2 * rg + 1], (unsigned long long)m);
+    // site tasks (even L that are not word sizes): one site per thread,
+    // strided over every thread of the launch, by the per-site rule of
+    // site_gather / site_decide (the same bits as the word paths and the oracle)
+    if (P.total_sites > 0) {
+        const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
+        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+        // four independent sites per iteration: all their loads are issued
+        // before any decision (one site at a time waits on each load chain)
+        for (int64_t g0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g0 < P.total_sites;
+             g0 += 4 * stride) {
+            SiteWork sw[4];
+            bool live[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t g = g0 + u * stride;
+                live[u] = g < P.total_sites;
+                if (!live[u]) continue;
+                int sc = 0;
+                while (P.cls[sc].site_end <= g) ++sc;
+                const IsingClass& C = P.cls[sc];
+                const int64_t lg = g - C.site_base;
+                const int r = C.plane_fast ? (int)fdiv((uint32_t)lg, C.div_plane)
+                                           : (int)(lg / C.plane_sites);
+                const uint32_t i = (uint32_t)(lg - (int64_t)r * C.plane_sites);
+                uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
+                site_gather<DIM>(sw[u], base + (int64_t)colour * C.plane_sites,
+                                 base + (int64_t)(colour ^ 1) * C.plane_sites, i, (uint32_t)C.L,
+                                 C.div_half, C.div_L, (uint32_t)colour);
+                sw[u].rg = C.rep_base + r;
+                sw[u].uid = replica_uid(C.L, r);
+                sw[u].tab = P.thr + (int64_t)(C.rep_base + (MODE != 2 ? P.r2t[sw[u].rg] : 0)) * 16;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (!live[u]) continue;
+                if (MODE != 2) site_decide(sw[u], c2, c3, k0, k1);
+                if (MODE != 0) {
+                    const int sp = 1 - 2 * sw[u].d;
+                    const long long bnd = (long long)(sp * (2 * DIM - 2 * sw[u].nd));
+                    const long long m = (long long)(sp + 1 - 2 * sw[u].oth_i);
+                    atomicAdd(&P.acc[2 * sw[u].rg], (unsigned long long)bnd);
+                    atomicAdd(&P.acc[2 * sw[u].rg + 1], (unsigned long long)m);
+                }
+            }
         }
     }
 }
@@ -959,7 +977,7 @@ __global__ void __launch_bounds__(kMaxThreads)
 // distributed shared memory (mapa + ld.shared::cluster), and hardware cluster
 // barriers (release / acquire at cluster scope) separate the half-sweeps.
 // Spins are loaded from HBM at the start and written back at the end.  Same
-// per-site update rule and random stream as the site kernel (site_update), so
+// per-site update rule and random stream as the site tasks (site_decide), so
 // any launch shape gives the same bits.
 constexpr int kResidentThreads = 1024;
 
@@ -999,7 +1017,7 @@ __device__ __forceinline__ int dsm_spin(uint32_t sbase, uint32_t pl, uint32_t j,
 }
 
 // Neighbour colour indices, Philox block and word/half selector of the site at
-// colour index i (see site_update).
+// colour index i (see site_gather).
 template <int DIM>
 __device__ __forceinline__ void resident_geom(uint32_t i, uint32_t L, uint32_t half, uint32_t S,
                                               const FastDiv& dh, const FastDiv& dL,
@@ -1464,7 +1482,7 @@ struct isg_ising {
     bool cache_pf_set = false; // cache prefetch set by the caller (else automatic)
     bool pdl = true;           // word kernels as programmatic dependent launches
     int pf = 1;                // depth in use
-    int word_grid = 0, site_grid = 0;
+    int word_grid = 0;
     int word_grids[3] = {1, 1, 1};
     int sms = 1;
     // sampling-phase mirror of the device counters
@@ -1550,16 +1568,6 @@ static void (*word_kernel(int dim, int mode, int pf, int wmax))(IsingParams, int
     // no rolling tasks in 2D: one form
     return word_kernel_m<2, 1, 2, 3>(mode);
 }
-static void (*site_kernel(int dim, int mode))(IsingParams, int, int) {
-    if (dim == 3) {
-        if (mode == 0) return k_ising_sites<3, 0>;
-        if (mode == 1) return k_ising_sites<3, 1>;
-        return k_ising_sites<3, 2>;
-    }
-    if (mode == 0) return k_ising_sites<2, 0>;
-    if (mode == 1) return k_ising_sites<2, 1>;
-    return k_ising_sites<2, 2>;
-}
 
 // Word kernels run 256-thread blocks (one CTA task = 8 warp tasks); the
 // grid is SMs x blocks per SM (occupancy maximum unless set), at most one
@@ -1569,7 +1577,10 @@ static void (*site_kernel(int dim, int mode))(IsingParams, int, int) {
 // keep more DRAM requests in flight) — measured on both kinds of workload.
 static int configure_launch(isg_ising* H) {
     const int thr = H->threads;
-    const int64_t need = std::max<int64_t>(H->P.total_ctasks, H->P.flat_ctasks);
+    // one launch per half-sweep covers every size: rolling ranges, flat
+    // tasks and one-site tasks (256 per block)
+    const int64_t need = std::max<int64_t>(std::max<int64_t>(H->P.total_ctasks, H->P.flat_ctasks),
+                                           (H->P.total_sites + 255) / 256);
     const bool in_l2 = H->spin_bytes <= ((int64_t)96 << 20);
     // two words per lane: loads two planes ahead help L2-resident batches;
     // four words per lane (2 blocks per SM either way): one plane ahead
@@ -1591,13 +1602,12 @@ static int configure_launch(isg_ising* H) {
         H->word_grids[mode] = (int)std::max<int64_t>(1, std::min(max_blocks, need));
     }
     H->word_grid = H->word_grids[0];
-    int64_t sneed = (H->P.total_sites + thr - 1) / thr;
-    H->site_grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)H->sms * 8, sneed));
+    (void)thr;
     return ISG_OK;
 }
 
 static void launch_half(isg_ising* H, int colour, int sweep_off, int mode) {
-    if (H->P.total_tasks > 0) {
+    if (H->P.total_tasks > 0 || H->P.total_sites > 0) {
         // programmatic dependent launch: the word kernel's blocks may be
         // scheduled while the previous kernel drains (they wait on it first)
         cudaLaunchConfig_t cfg = {};
@@ -1613,9 +1623,6 @@ static void launch_half(isg_ising* H, int colour, int sweep_off, int mode) {
         cudaLaunchKernelEx(&cfg, word_kernel(H->dim, mode, H->pf, H->wmax), H->P, colour,
                            sweep_off);
     }
-    if (H->P.total_sites > 0)
-        site_kernel(H->dim, mode)<<<H->site_grid, H->threads, 0, H->stream>>>(H->P, colour,
-                                                                             sweep_off);
 }
 
 static void launch_post(isg_ising* H, int do_record, int do_exchange, int parity, int zero_acc,
@@ -1782,6 +1789,10 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         } else {
             C.ctask_base = C.ctask_end = 0;
         }
+        C.div_half = make_div((uint32_t)(L / 2));
+        C.div_L = make_div((uint32_t)L);
+        C.div_plane = make_div(C.plane_sites);
+        C.plane_fast = (int64_t)C.plane_sites * replicas < ((int64_t)1 << 31) ? 1 : 0;
         C.site_base = site;
         if (C.kind == kSite) site += (int64_t)C.plane_sites * replicas;
         C.site_end = site;

@@ -53,9 +53,12 @@ def test_hot_start_bit_exact(gpu, oracle, dim, sizes):
 
 
 @pytest.mark.parametrize("dim,sizes,h", [(3, [2, 4, 6, 8, 10, 16, 32], 0.0),
+                                         (3, [8, 12, 24, 32, 48, 64], 0.0),
                                          (3, [4, 8, 16], 0.35),
                                          (2, [4, 6, 8, 16, 32, 64], 0.0)])
 def test_sweeps_bit_exact(gpu, oracle, dim, sizes, h):
+    """Every size of a batch advances in the one half-sweep launch (rolling,
+    flat and one-site tasks side by side) and matches the oracle bit for bit."""
     R, seed, J = 3, 42, 1.0
     temps = [2.0, 4.5, 7.0] if dim == 3 else [1.5, 2.269, 3.5]
     b = gpu.IsingBatch(sizes, R, seed=seed, dim=dim)

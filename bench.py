@@ -480,6 +480,7 @@ def run_gpu(args):
     hbm = hbm_case(pkg, stream, flush, max(3, min(args.steps, 100)), peak, peak_kind)
     ess = ess_case(pkg, stream, sweeps_per_s)
     cfg1 = config1_case(pkg)
+    learned = learned_summary(pkg, args) if args.learned_seconds > 0 else None
     threads = host_threads()
     cpu_v, cpu_s, cpu_f = cpu_sample(threads, sweeps=args.cpu_sweeps)
     launches_per_step = 2 * SWEEPS_PER_STEP + (SWEEPS_PER_STEP // MEASURE_EVERY)
@@ -504,6 +505,7 @@ def run_gpu(args):
         "roofline": roof,
         "roofline_hbm": hbm,
         "config1": cfg1,
+        "learned": learned,
         "cpu_baseline": {"value": cpu_v, "unit": "flips/ns", "cores": threads, "kind": "port",
                          "sample": f"{threads} threads x {args.cpu_sweeps:g} random-site sweeps "
                                    f"of L=8..128 each ({cpu_f:.3g} flips, {cpu_s:.1f} s); "
@@ -1020,6 +1022,25 @@ def ncu_case_resident():
     return 0
 
 
+def learned_summary(pkg, args):
+    """The learned proposal against plain checkerboard PT, bounded for the
+    default run: 2D L = 16 and L = 32 at T = 2.269, args.learned_seconds of
+    streaming training each, 150 chain batches, 50,000 plain PT sweeps; ESS/s
+    of |M| and E on both sides with the same estimator (learned_case).
+    The full comparison is `bench.py --learned` (60 s of training, 800 batches)."""
+    out = {"target": "learned / plain ESS/s of |M| >= 3 at 2D L=32, T=2.269", "cases": []}
+    for L in (16, 32):
+        c = learned_case(pkg, L, 2, 2.269, args.learned_seconds, 150, 50000)
+        out["cases"].append({
+            "case": c["case"], "ratio_M": c["ratio_learned_over_plain"],
+            "ratio_E": c["ratio_E_learned_over_plain"],
+            "plain_ess_M_per_s": c["plain_pt"]["ess_per_s"],
+            "learned_ess_M_per_s": c["learned"]["ess_per_s"],
+            "acceptance": c["learned"]["acceptance"], "train_s": c["learned"]["train_s"],
+            "nll_per_site": c["learned"]["nll_per_site"], "M_diff_sigma": c["M_diff_sigma"]})
+    return out
+
+
 def run_learned(args):
     import torch
     torch.cuda.set_device(0)
@@ -1125,6 +1146,9 @@ def main():
                     help="learned proposal vs plain PT ESS/s on 2D L=16/32 and 3D L=8 "
                          "(separate JSON lines)")
     ap.add_argument("--train-seconds", type=float, default=60.0)
+    ap.add_argument("--learned-seconds", type=float, default=20.0,
+                    help="training seconds per case of the learned comparison carried by the "
+                         "default line (0: leave it out)")
     ap.add_argument("--chain-batches", type=int, default=800)
     ap.add_argument("--pt-sweeps", type=int, default=200000)
     ap.add_argument("--ncu-case", nargs="?", const="words",

@@ -69,6 +69,7 @@ struct ContParams {
     unsigned long long* ctrl;  // [0] sweep base
     unsigned long long* metro_acc;
     long long* partials;       // [chunks][kNQ] fixed-point block sums (2^-24 units)
+    uint32_t rk0[10], rk1[10]; // Philox round keys of the seed
     uint64_t seed;
     float J;
     double Jd;
@@ -313,8 +314,12 @@ __device__ __forceinline__ bool cone_test(const float (&v)[NC], const float (&h)
     if constexpr (NC == 3) {
         const float ct = 1.0f - uniform24(u.x) * (1.0f - cos_delta);
         const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+        // azimuth 2 pi u1: sin and cos of 2 pi u1 - pi (inside [-pi, pi),
+        // where the fast intrinsics are accurate to a few 1e-7), negated
         float sp, cp;
-        sincospif(2.0f * uniform24(u.y), &sp, &cp);
+        __sincosf(6.28318530717958648f * uniform24(u.y) - 3.14159265358979324f, &sp, &cp);
+        sp = -sp;
+        cp = -cp;
         const float tx = fabsf(v[0]) < 0.9f ? 1.0f : 0.0f;
         const float ty = 1.0f - tx;
         const float ts = tx * v[0] + ty * v[1];
@@ -334,8 +339,8 @@ __device__ __forceinline__ bool cone_test(const float (&v)[NC], const float (&h)
 #pragma unroll
         for (int k = 0; k < 3; ++k) w[k] *= wn;
     } else {
-        float sd, cd;
-        sincospif(delta * 0.318309886183790672f * (2.0f * uniform24(u.x) - 1.0f), &sd, &cd);
+        float sd, cd;  // angle in [-delta, delta], delta <= pi
+        __sincosf(delta * (2.0f * uniform24(u.x) - 1.0f), &sd, &cd);
         w[0] = v[0] * cd - v[1] * sd;
         w[1] = v[1] * cd + v[0] * sd;
     }
@@ -343,7 +348,7 @@ __device__ __forceinline__ bool cone_test(const float (&v)[NC], const float (&h)
 #pragma unroll
     for (int k = 0; k < NC; ++k) dot = fmaf(w[k] - v[k], h[k], dot);
     const float dE = -J * dot;
-    return dE <= 0.0f || uniform24(u.z) < expf(-beta * dE);
+    return dE <= 0.0f || uniform24(u.z) < __expf(-beta * dE);
 }
 
 // Metropolis with the cone proposal on column tasks (continuous_spin_kernel.cu:9-83
@@ -377,6 +382,8 @@ __global__ void __launch_bounds__(kCThreads, 3)
         const uint32_t colp = (c.y + 1 == L ? 0 : c.y + 1) * half + c.k;
         const uint32_t colm = (c.y == 0 ? L - 1 : c.y - 1) * half + c.k;
         const uint32_t uid = replica_uid(C.L, c.r);
+        // the warp-uniform part of the Philox rounds (counter {uid, i, c2, c3})
+        const PhiloxPre pre = philox_pre(uid, c2, c3, k0, k1);
         const float beta = P.betaf[C.rep_base + P.r2t[c.rg]];
         float zm[NC], zc[NC];
         const uint32_t zmb = (c.z0 == 0 ? L - 1 : c.z0 - 1) * c.Pz;
@@ -418,7 +425,7 @@ __global__ void __launch_bounds__(kCThreads, 3)
             if (z + 1 < c.z1) load_step(z + 1);
             // O(3): one block per site; O(2): one block per colour-index pair,
             // words (x, z) for the even index, (y, w) for the odd
-            U4 u = philox10(uid, NC == 3 ? i : i >> 1, c2, c3, k0, k1);
+            U4 u = philox_w(pre, P, NC == 3 ? i : i >> 1);
             if (NC == 2 && (i & 1u)) u = U4{u.y, u.x, u.w, u.z};
             const bool accepted = cone_test<NC>(v, h, u, cos_delta, delta, beta, P.J, w);
             n_acc += accepted ? 1u : 0u;
@@ -508,6 +515,8 @@ __device__ __forceinline__ void metro2_column(const ContParams& P, const ColRef&
     const uint32_t colp = (c.y + 1 == L ? 0 : c.y + 1) * half + c.k;
     const uint32_t colm = (c.y == 0 ? L - 1 : c.y - 1) * half + c.k;
     const uint32_t uid = replica_uid(C.L, c.r);
+    // the warp-uniform part of the Philox rounds (counter {uid, i, c2, c3})
+    const PhiloxPre pre = philox_pre(uid, c2, c3, k0, k1);
     const float beta = P.betaf[C.rep_base + P.r2t[c.rg]];
     float2 zm[NC], zc[NC];
     const uint32_t zmb = (c.z0 == 0 ? L - 1 : c.z0 - 1) * c.Pz;
@@ -570,10 +579,10 @@ __device__ __forceinline__ void metro2_column(const ContParams& P, const ColRef&
         // words (x, z) for site k, (y, w) for site k+1
         U4 u0, u1;
         if constexpr (NC == 3) {
-            u0 = philox10(uid, i, c2, c3, k0, k1);
-            u1 = philox10(uid, i + 1, c2, c3, k0, k1);
+            u0 = philox_w(pre, P, i);
+            u1 = philox_w(pre, P, i + 1);
         } else {
-            u0 = philox10(uid, i >> 1, c2, c3, k0, k1);
+            u0 = philox_w(pre, P, i >> 1);
             u1 = U4{u0.y, u0.x, u0.w, u0.z};
         }
         const bool acc_a = cone_test<NC>(va, ha, u0, cos_delta, delta, beta, P.J, wa);
@@ -1285,6 +1294,10 @@ int isg_cont_create(isg_cont** out, const int* sizes, int n_sizes, int replicas,
     P.total_sites = site;
     P.total_chunks = chunk;
     P.seed = seed;
+    for (int r = 0; r < 10; ++r) {
+        P.rk0[r] = (uint32_t)seed + (uint32_t)r * kPhiloxW0;
+        P.rk1[r] = (uint32_t)(seed >> 32) + (uint32_t)r * kPhiloxW1;
+    }
     P.J = 1.0f;
     P.Jd = 1.0;
     P.renorm = 0;

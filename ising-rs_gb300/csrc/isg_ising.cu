@@ -117,58 +117,6 @@ struct IsingParams {
 
 // ---------------------------------------------------------------- kernels
 
-// Philox4x32-10 of counter {uid, w, c2, c3} with the warp-uniform part of the
-// first three rounds (everything that does not depend on w) computed once per
-// replica.  Products are formed as 64-bit values (one wide multiply each).
-struct PhiloxPre {
-    uint32_t x0, x2, x3, hi02, lo02;
-};
-
-__device__ __forceinline__ uint64_t mulw(uint32_t a, uint32_t b) { return (uint64_t)a * b; }
-
-__device__ __forceinline__ PhiloxPre philox_pre(uint32_t uid, uint32_t c2, uint32_t c3,
-                                                uint32_t k0, uint32_t k1) {
-    PhiloxPre p;
-    // round 0: M0*uid and M1*c2 are uniform
-    const uint64_t p0 = mulw(kPhiloxM0, uid), p1 = mulw(kPhiloxM1, c2);
-    p.x0 = (uint32_t)(p1 >> 32) ^ k0;  // a0 = x0 ^ w
-    const uint32_t a1 = (uint32_t)p1;
-    const uint32_t a2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
-    const uint32_t a3 = (uint32_t)p0;
-    // round 1 (keys + W): M1*a2 uniform
-    const uint64_t q1 = mulw(kPhiloxM1, a2);
-    const uint32_t b0 = (uint32_t)(q1 >> 32) ^ a1 ^ (k0 + kPhiloxW0);
-    const uint32_t b1 = (uint32_t)q1;
-    p.x2 = a3 ^ (k1 + kPhiloxW1);  // b2 = hi(M0*a0) ^ x2, b3 = lo(M0*a0)
-    // round 2 (keys + 2W): M0*b0 uniform
-    const uint64_t q0 = mulw(kPhiloxM0, b0);
-    p.hi02 = (uint32_t)(q0 >> 32) ^ (k1 + 2u * kPhiloxW1);  // c2 = b3 ^ hi02
-    p.lo02 = (uint32_t)q0;                                  // c3
-    p.x3 = b1 ^ (k0 + 2u * kPhiloxW0);                      // c0 = hi(M1*b2) ^ x3
-    return p;
-}
-
-__device__ __forceinline__ U4 philox_w(const PhiloxPre& p, const IsingParams& P, uint32_t w) {
-    const uint32_t a0 = p.x0 ^ w;
-    const uint64_t r1 = mulw(kPhiloxM0, a0);
-    const uint32_t b2 = (uint32_t)(r1 >> 32) ^ p.x2;
-    const uint32_t b3 = (uint32_t)r1;
-    const uint64_t r2 = mulw(kPhiloxM1, b2);
-    uint32_t c0 = (uint32_t)(r2 >> 32) ^ p.x3;
-    uint32_t c1 = (uint32_t)r2;
-    uint32_t c2 = b3 ^ p.hi02;
-    uint32_t c3 = p.lo02;
-#pragma unroll
-    for (int r = 3; r < 10; ++r) {
-        const uint64_t m0 = mulw(kPhiloxM0, c0), m1 = mulw(kPhiloxM1, c2);
-        c0 = (uint32_t)(m1 >> 32) ^ c1 ^ P.rk0[r];
-        c1 = (uint32_t)m1;
-        c2 = (uint32_t)(m0 >> 32) ^ c3 ^ P.rk1[r];
-        c3 = (uint32_t)m0;
-    }
-    return U4{c0, c1, c2, c3};
-}
-
 // Loads issued where they are written (volatile asm keeps the compiler from
 // sinking a prefetch next to its use).
 __device__ __forceinline__ uint32_t ldg_nc(const uint32_t* p) {

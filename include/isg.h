@@ -238,6 +238,14 @@ int isg_ising_set_words_per_lane(isg_ising* h, int words);
  * of the stream drains and wait for it before reading any device state; 0 =
  * ordinary launches.  Results never depend on it. */
 int isg_ising_set_dependent_launch(isg_ising* h, int enable);
+/* isg_ising_pt_run with host record arrays on a batch of small lattices (at
+ * most 16 x 1024 sites per colour plane, all resident at once, no energy
+ * histograms): enable = 1 (default) runs the whole PT cycle — sweeps, fused
+ * measurements, records and exchanges at a bounded grid barrier — in one
+ * cooperative launch of the cluster-resident kernel per 65,536 sweeps; 0 =
+ * the CUDA-graph cycle of separate launches.  Results are the same bit for
+ * bit; a barrier wait that gives up returns ISG_ERR_TIMEOUT. */
+int isg_ising_set_resident_pt(isg_ising* h, int enable);
 /* Time every supported launch shape (prefetch depth x site-kernel threads x
  * blocks per SM) on a scratch copy of the lattices and keep the fastest.
  * best[0..2] (may be NULL) receives threads, blocks/SM, prefetch depth. */

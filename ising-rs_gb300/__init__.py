@@ -108,6 +108,7 @@ def _declare(L):
         "isg_ising_set_cache_prefetch": [vp, i32, i32],
         "isg_ising_set_words_per_lane": [vp, i32],
         "isg_ising_set_dependent_launch": [vp, i32],
+        "isg_ising_set_resident_pt": [vp, i32],
         "isg_ising_time_halfsweep": [vp, i32, vp],
         "isg_ising_time_halfsweep_graph": [vp, i32, i64, i32, vp],
         "isg_ising_sites_per_halfsweep": [vp, vp],
@@ -551,6 +552,10 @@ class IsingBatch:
     def set_words_per_lane(self, words: int = 4) -> None:
         """Rolling half-sweep, L >= 128: 4 or 2 words per lane (same results)."""
         _check(lib().isg_ising_set_words_per_lane(self._h, int(words)))
+
+    def set_resident_pt(self, enable: bool = True) -> None:
+        """pt_run of small lattices in one cooperative resident launch (same bits)."""
+        _check(lib().isg_ising_set_resident_pt(self._h, int(bool(enable))))
 
     def set_dependent_launch(self, enable: bool = True) -> None:
         """Half-sweep word kernels as programmatic dependent launches (same results)."""

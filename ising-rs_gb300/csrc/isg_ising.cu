@@ -942,6 +942,26 @@ struct ResidentParams {
     int log2_chunk;           // colour indices per CTA and plane: 1 << log2_chunk
     FastDiv div_half[kMaxClasses];  // L/2
     FastDiv div_L[kMaxClasses];
+    // parallel tempering (pt != 0; one site per thread): the PT cycle of
+    // k_ising_post inside the launch.  Sampling sweep ks0 + k is measured when
+    // (ks0 + k + 1) % me == 0 and exchanges when (ks0 + k + 1) % ee == 0; at
+    // an exchange every lattice publishes its energy, all blocks meet at a
+    // bounded grid barrier, and every CTA computes its size's exchange pass on
+    // its own copy of the ladder (the same FP64 arithmetic as k_ising_post).
+    int pt, ee, me;
+    uint64_t ks0;
+    int32_t* rec_t;               // [rows][lattices] slot of each record
+    unsigned long long* eacc;     // [lattices][2] bond, mag of the current measurement (zeroed)
+    double* ebuf;                 // [2][lattices] energies at exchange points
+    int32_t* r2t;
+    int32_t* t2r;
+    const double* betas;          // per slot
+    unsigned long long* ctrl;     // PostParams layout: [1+NC+s] exchanges, [1+2NC+s] accepted
+    unsigned int* bar;            // grid barrier [arrivals, generation] (zeroed)
+    int* err;                     // set when a barrier wait gives up
+    double J, h;
+    uint64_t seed;
+    int n_classes;
 };
 
 __device__ __forceinline__ void cluster_sync_all() {
@@ -1067,6 +1087,136 @@ __device__ __forceinline__ int resident_nd(uint32_t sbase, uint32_t pl, int lc,
     return nd;
 }
 
+// The PT form of the resident kernel's one-site-per-thread loop (Q.pt).
+template <int DIM>
+__device__ __forceinline__ void resident_pt_loop(
+    const IsingParams& P, const ResidentParams& Q, uint32_t* tab, int lid, int crank, int s, int r,
+    int rg, uint32_t uid, bool has, uint32_t i, const uint32_t (&na0)[6],
+    const uint32_t (&na1)[6], uint32_t a0, uint32_t a1, uint32_t c10, uint32_t c11,
+    uint32_t sel0, uint32_t sel1) {
+    __shared__ int s_t2r[kMaxReplicas], s_r2t[kMaxReplicas];
+    __shared__ double s_e[kMaxReplicas];
+    __shared__ int s_acc, s_ok;
+    const int R = P.cls[0].R;
+    const int base = s * R;
+    const int lane = threadIdx.x & 31;
+    const uint32_t bd = blockDim.x;
+    const int NC = Q.n_classes;
+    for (int j = threadIdx.x; j < R; j += bd) {
+        s_t2r[j] = Q.t2r[base + j];
+        s_r2t[j] = Q.r2t[base + j];
+    }
+    if (threadIdx.x == 0) {
+        s_acc = 0;
+        s_ok = 1;
+    }
+    unsigned long long xc = Q.ctrl[1 + NC + s];
+    __syncthreads();
+    const uint64_t ks0 = Q.ks0;
+    const int64_t row0 = (int64_t)(ks0 / (uint64_t)Q.me);
+    for (int64_t k = 0; k < Q.n_sweeps; ++k) {
+        const uint64_t ks = ks0 + (uint64_t)k;
+        const bool do_m = ((ks + 1) % (uint64_t)Q.me) == 0;
+        const bool do_x = ((ks + 1) % (uint64_t)Q.ee) == 0;
+        const bool meas = do_m || do_x;
+        const uint64_t sweep = Q.sweep0 + (uint64_t)k;
+        int bsum = 0, msum = 0;
+        resident_fast_half<DIM, 0>(P, tab, uid, sweep, has, i, na0, a0, a1, c10, sel0, meas, bsum,
+                                   msum);
+        cluster_sync_all();
+        resident_fast_half<DIM, 1>(P, tab, uid, sweep, has, i, na1, a1, a0, c11, sel1, meas, bsum,
+                                   msum);
+        if (meas) {
+            bsum = __reduce_add_sync(ISG_FULL_MASK, bsum);
+            msum = __reduce_add_sync(ISG_FULL_MASK, msum);
+            // before the cluster barrier, so CTA 0 sees every warp's sums
+            if (lane == 0 && (bsum != 0 || msum != 0)) {
+                atomicAdd(&Q.eacc[2 * lid], (unsigned long long)(long long)bsum);
+                atomicAdd(&Q.eacc[2 * lid + 1], (unsigned long long)(long long)msum);
+            }
+        }
+        cluster_sync_all();
+        if (!meas) continue;
+        if (crank == 0 && threadIdx.x == 0) {
+            const long long b = (long long)atomicExch(&Q.eacc[2 * lid], 0ull);
+            const long long m = (long long)atomicExch(&Q.eacc[2 * lid + 1], 0ull);
+            if (do_m) {
+                const int64_t row = (int64_t)((ks + 1) / (uint64_t)Q.me) - 1 - row0;
+                Q.rec[(row * Q.lattices + lid) * 2] = (unsigned long long)b;
+                Q.rec[(row * Q.lattices + lid) * 2 + 1] = (unsigned long long)m;
+                Q.rec_t[row * Q.lattices + lid] = s_r2t[r];
+            }
+            if (do_x) {
+                const double t1 = __dmul_rn(Q.J, (double)b);
+                const double t2 = __dmul_rn(Q.h, (double)m);
+                Q.ebuf[(xc & 1ull) * Q.lattices + lid] = __dsub_rn(-t1, t2);
+            }
+        }
+        if (!do_x) continue;
+        // every lattice's energy of this exchange point, then the pass
+        const bool ok = grid_barrier(Q.bar, Q.err, gridDim.x);
+        // the cluster follows its CTA 0's outcome, so that all its CTAs leave
+        // (or go on) at the same point; a wait that gave up set Q.err, which
+        // every block sees at the next barrier at the latest
+        if (threadIdx.x == 0) s_ok = ok ? 1 : 0;
+        cluster_sync_all();
+        uint32_t ok0 = 1;
+        {
+            const uint32_t local = (uint32_t)__cvta_generic_to_shared(&s_ok);
+            asm volatile("ld.shared::cluster.u32 %0, [%1];"
+                         : "=r"(ok0)
+                         : "r"(dsm_map(local, 0u))
+                         : "memory");
+        }
+        cluster_sync_all();
+        if (!ok0) {
+            if (threadIdx.x == 0) s_ok = 0;
+            __syncthreads();
+            break;
+        }
+        for (int j = threadIdx.x; j < R; j += bd)
+            s_e[j] = __ldcg(Q.ebuf + (xc & 1ull) * Q.lattices + base + j);
+        __syncthreads();
+        const int par = (int)(xc & 1ull);
+        const uint32_t k0 = (uint32_t)Q.seed, k1 = (uint32_t)(Q.seed >> 32);
+        const uint32_t c3 = counter_word3(ISG_TAG_EXCH, 0, xc);
+        for (int j = par + 2 * (int)threadIdx.x; j + 1 < R; j += 2 * (int)bd) {
+            const int ri = s_t2r[j], rj = s_t2r[j + 1];
+            const double d = __dmul_rn(__dsub_rn(Q.betas[base + j], Q.betas[base + j + 1]),
+                                       __dsub_rn(s_e[rj], s_e[ri]));
+            bool acc = d < 0.0;
+            if (!acc) {
+                const U4 u = philox10(exchange_uid(P.cls[s].L), (uint32_t)j, (uint32_t)xc, c3, k0, k1);
+                acc = uniform53(u.x, u.y) < exp(-d);
+            }
+            if (acc) {
+                s_t2r[j] = rj;
+                s_t2r[j + 1] = ri;
+                s_r2t[ri] = j + 1;
+                s_r2t[rj] = j;
+                atomicAdd(&s_acc, 1);
+            }
+        }
+        ++xc;
+        __syncthreads();
+        // the table of this lattice's (possibly new) slot
+        if (threadIdx.x < 16) tab[threadIdx.x] = Q.tables[(int64_t)(base + s_r2t[r]) * 16 + threadIdx.x];
+        __syncthreads();
+    }
+    // the ladder, exchange count and acceptances back to the handle's state
+    if (crank == 0) {
+        if (threadIdx.x == 0) Q.r2t[rg] = s_r2t[r];
+        if (r == 0) {
+            for (int j = threadIdx.x; j < R; j += bd) Q.t2r[base + j] = s_t2r[j];
+            if (threadIdx.x == 0 && s_ok) {
+                Q.ctrl[1 + NC + s] = xc;
+                Q.ctrl[1 + 2 * NC + s] += (unsigned long long)s_acc;
+            }
+        }
+    }
+    cluster_sync_all();
+}
+
 template <int DIM>
 __global__ void __launch_bounds__(kResidentThreads, 1)
     k_ising_resident(const __grid_constant__ IsingParams P, const __grid_constant__ ResidentParams Q) {
@@ -1120,6 +1270,10 @@ __global__ void __launch_bounds__(kResidentThreads, 1)
                 na1[j] = dsm_map(sbase + (nb[j] & (chunk - 1u)), nb[j] >> lc);
         }
         const uint32_t a0 = sbase + (i - i0), a1 = sbase + chunk + (i - i0);
+        if (Q.pt) {
+            resident_pt_loop<DIM>(P, Q, s_tab[0], lid, crank, s, r, rg, uid, has, i, na0, na1, a0,
+                                  a1, c10, c11, sel0, sel1);
+        } else
         for (int64_t k = 0; k < Q.n_sweeps; ++k) {
             const uint32_t* tab = s_tab[k & 1];
             uint32_t tnext = 0;
@@ -1450,6 +1604,12 @@ struct isg_ising {
     int64_t sched_cap = 0;
     unsigned long long* d_srec = nullptr;
     int64_t srec_cap = 0;
+    // resident PT (small lattices): record slots and exchange scratch
+    bool resident_pt = true;
+    int32_t* d_srec_t = nullptr;
+    int64_t srec_t_cap = 0;
+    unsigned long long* d_pt_scratch = nullptr;  // eacc [RT][2], ebuf [2][RT], bar, err
+    int64_t pt_scratch_cap = 0;
     // energy histograms (isg_ising_hist_*)
     unsigned long long* d_hist = nullptr;
     int32_t* d_hist_rng = nullptr;
@@ -1865,6 +2025,8 @@ int isg_ising_destroy(isg_ising* H) {
     cudaFree(H->d_sched_tab);
     cudaFree(H->d_sched);
     cudaFree(H->d_srec);
+    cudaFree(H->d_srec_t);
+    cudaFree(H->d_pt_scratch);
     cudaFree(H->d_hist);
     cudaFree(H->d_hist_rng);
     if (H->own_stream) cudaStreamDestroy(H->own_stream);
@@ -1923,6 +2085,11 @@ static int upload_thresholds(isg_ising* H, const std::vector<uint32_t>& thr) {
                            cudaMemcpyHostToDevice, H->stream));
     return ISG_OK;
 }
+}  // namespace isg
+
+namespace isg {
+static int pt_resident(isg_ising* H, int64_t n_sweeps, int ee, int me, int32_t* tslot,
+                       int64_t* bond, int64_t* mag, int64_t max_records, int64_t* n_records);
 }  // namespace isg
 
 extern "C" {
@@ -2188,6 +2355,11 @@ int isg_ising_pt_run(isg_ising* H, int64_t n_sweeps, int ee, int me, int32_t* ts
                                      std::to_string(max_records) + " rows, " +
                                      std::to_string(need) + " needed");
     if (n_records) *n_records = 0;
+    if (!keep && n_sweeps > 0) {
+        // small lattices: the whole run in the resident kernel (1: not eligible)
+        const int rc = pt_resident(H, n_sweeps, ee, me, tslot, bond, mag, max_records, n_records);
+        if (rc != 1) return rc;
+    }
     const int64_t g = gcd64(ee, me);
     const int64_t lcm = (int64_t)ee / g * me;
     const int period = lcm <= 1000 ? (int)lcm : 0;
@@ -2423,6 +2595,12 @@ int isg_ising_set_cache_prefetch(isg_ising* H, int level, int planes) {
     return ISG_OK;
 }
 
+int isg_ising_set_resident_pt(isg_ising* H, int enable) {
+    if (!H) return fail(ISG_ERR_ARG, "isg_ising_set_resident_pt: NULL handle");
+    H->resident_pt = enable != 0;
+    return ISG_OK;
+}
+
 int isg_ising_set_dependent_launch(isg_ising* H, int enable) {
     if (!H) return fail(ISG_ERR_ARG, "isg_ising_set_dependent_launch: NULL handle");
     cudaSetDevice(H->device);
@@ -2559,6 +2737,53 @@ static int copy_records(isg_ising* H, const unsigned long long* d_rec, int64_t r
     return ISG_OK;
 }
 
+// Launch shape of the resident kernel: the largest cluster that fits a GPC
+// (16, 8, 4, 2 or 1 CTAs of kResidentThreads), each CTA holding a power-of-two
+// chunk (>= 256 sites where the cluster has several CTAs) of both colour
+// planes.  Sets cfg (grid, block, shared memory, cluster attribute in attr[0]),
+// Q.cs and Q.log2_chunk; *active = clusters that can be resident at once.
+static bool resident_config(isg_ising* H, cudaLaunchConfig_t& cfg, cudaLaunchAttribute* attr,
+                            ResidentParams& Q, const void* kfun, uint32_t max_plane, int* active) {
+    const int RT = H->replicas_total;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    cfg.blockDim = dim3(kResidentThreads, 1, 1);
+    cfg.stream = H->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    *active = 0;
+    for (int target = 16; target >= 1; target /= 2) {
+        int lc = 0;
+        while ((1u << lc) * (uint32_t)target < max_plane) ++lc;
+        if (lc < 8 && target > 1) continue;  // fewer than 256 sites per CTA: smaller cluster
+        const int cs = (int)((max_plane + (1u << lc) - 1) >> lc);
+        const size_t smem = (size_t)2 << lc;
+        if (smem > 200 * 1024) break;
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(kfun, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        Q.cs = cs;
+        Q.log2_chunk = lc;
+        cfg.gridDim = dim3((unsigned)(RT * cs), 1, 1);
+        cfg.dynamicSmemBytes = smem;
+        attr[0].val.clusterDim.x = (unsigned)cs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        int a = 0;
+        if (cudaOccupancyMaxActiveClusters(&a, kfun, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        if (a > 0) {
+            *active = a;
+            return true;
+        }
+    }
+    return false;
+}
+
 static int schedule_resident(isg_ising* H, const double* temps, int64_t n_sweeps, int every,
                              int phase, int64_t* bond, int64_t* mag) {
     const int RT = H->replicas_total;
@@ -2618,7 +2843,7 @@ static int schedule_resident(isg_ising* H, const double* temps, int64_t n_sweeps
         if (rows > 0)
             ISG_CK(cudaMemsetAsync(H->d_srec, 0, rows * RT * 2 * sizeof(unsigned long long),
                                    H->stream));
-        ResidentParams Q;
+        ResidentParams Q{};
         Q.tables = temps ? H->d_sched_tab : H->d_thr;
         Q.sched = temps ? H->d_sched + k0 : nullptr;
         Q.rec = H->d_srec;
@@ -2633,43 +2858,9 @@ static int schedule_resident(isg_ising* H, const double* temps, int64_t n_sweeps
             Q.div_L[c] = make_div((uint32_t)L);
         }
         cudaLaunchConfig_t cfg = {};
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        cfg.blockDim = dim3(kResidentThreads, 1, 1);
-        cfg.stream = H->stream;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        // largest cluster that fits a GPC: target 16, 8, 4, 2, 1 CTAs
-        bool placed = false;
-        for (int target = 16; target >= 1 && !placed; target /= 2) {
-            int lc = 0;
-            while ((1u << lc) * (uint32_t)target < max_plane) ++lc;
-            if (lc < 8 && target > 1) continue;  // fewer than 256 sites per CTA: smaller cluster
-            const int cs = (int)((max_plane + (1u << lc) - 1) >> lc);
-            const size_t smem = (size_t)2 << lc;
-            if (smem > 200 * 1024) break;
-            if (smem > 48 * 1024 &&
-                cudaFuncSetAttribute(kfun, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem) != cudaSuccess) {
-                cudaGetLastError();
-                continue;
-            }
-            Q.cs = cs;
-            Q.log2_chunk = lc;
-            cfg.gridDim = dim3((unsigned)(RT * cs), 1, 1);
-            cfg.dynamicSmemBytes = smem;
-            attr[0].val.clusterDim.x = (unsigned)cs;
-            attr[0].val.clusterDim.y = 1;
-            attr[0].val.clusterDim.z = 1;
-            int active = 0;
-            cudaError_t oe = cudaOccupancyMaxActiveClusters(&active, kfun, &cfg);
-            if (oe != cudaSuccess) {
-                cudaGetLastError();
-                continue;
-            }
-            placed = active > 0;
-        }
-        if (!placed)
+        cudaLaunchAttribute attr[2];
+        int active = 0;
+        if (!resident_config(H, cfg, attr, Q, kfun, max_plane, &active) || active < 1)
             return fail(ISG_ERR_UNSUPPORTED, "isg_ising_run_schedule: no cluster shape fits");
         cudaError_t e = H->dim == 3 ? cudaLaunchKernelEx(&cfg, k_ising_resident<3>, H->P, Q)
                                     : cudaLaunchKernelEx(&cfg, k_ising_resident<2>, H->P, Q);
@@ -2689,6 +2880,124 @@ static int schedule_resident(isg_ising* H, const double* temps, int64_t n_sweeps
 
 // Larger lattices: half-sweep kernels sweep by sweep, the measurement fused
 // into the second half-sweep of a recorded sweep.
+// PT sampling of small lattices (at most 16 CTAs of one site per thread per
+// colour plane) in one cooperative launch of the resident kernel per span of
+// sweeps (ResidentParams::pt): the sweeps, fused measurements, exchanges and
+// records of k_ising_post's cycle without a kernel boundary.  Records go to
+// the caller's arrays; the device ring is not used.  Returns 1 (and touches
+// nothing) when the batch does not qualify, so the caller takes the graph path.
+static int pt_resident(isg_ising* H, int64_t n_sweeps, int ee, int me, int32_t* tslot,
+                       int64_t* bond, int64_t* mag, int64_t max_records, int64_t* n_records) {
+    const int RT = H->replicas_total;
+    if (!H->resident_pt || H->d_hist || H->records_made != H->records_done) return 1;
+    uint32_t max_plane = 0;
+    for (int s = 0; s < H->n_classes; ++s) max_plane = std::max(max_plane, H->P.cls[s].plane_sites);
+    if (max_plane > 16u * kResidentThreads) return 1;
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, H->device);
+    if (!coop) return 1;
+    const void* kfun = H->dim == 3 ? (const void*)k_ising_resident<3>
+                                   : (const void*)k_ising_resident<2>;
+    if (cudaFuncSetAttribute(kfun, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+        cudaSuccess)
+        cudaGetLastError();
+    ResidentParams Q{};
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[2];
+    int active = 0;
+    if (!resident_config(H, cfg, attr, Q, kfun, max_plane, &active) || active < RT ||
+        (1u << Q.log2_chunk) > (uint32_t)kResidentThreads)
+        return 1;
+    attr[1].id = cudaLaunchAttributeCooperative;
+    attr[1].val.cooperative = 1;
+    cfg.numAttrs = 2;
+    const uint64_t k0 = H->ksample;
+    const int64_t need = (int64_t)((k0 + (uint64_t)n_sweeps) / (uint64_t)me - k0 / (uint64_t)me);
+    if (need > 0 && (!tslot || !bond || !mag || max_records < need))
+        return fail(ISG_ERR_ARG, "isg_ising_pt_run: record arrays hold " +
+                                     std::to_string(max_records) + " rows, " +
+                                     std::to_string(need) + " needed");
+    const int64_t span_max = (int64_t)1 << 16;
+    const int64_t rows_max = span_max / me + 1;
+    int rc = grow((void**)&H->d_srec, &H->srec_cap,
+                  rows_max * RT * 2 * (int64_t)sizeof(unsigned long long));
+    if (rc) return rc;
+    rc = grow((void**)&H->d_srec_t, &H->srec_t_cap, rows_max * RT * (int64_t)sizeof(int32_t));
+    if (rc) return rc;
+    const int64_t scratch = (2 * (int64_t)RT + 2 * (int64_t)RT + 2) * 8;
+    rc = grow((void**)&H->d_pt_scratch, &H->pt_scratch_cap, scratch);
+    if (rc) return rc;
+    unsigned long long* eacc = H->d_pt_scratch;
+    double* ebuf = reinterpret_cast<double*>(H->d_pt_scratch + 2 * RT);
+    unsigned int* bar = reinterpret_cast<unsigned int*>(H->d_pt_scratch + 4 * RT);
+    int* err = reinterpret_cast<int*>(H->d_pt_scratch + 4 * RT + 1);
+    Q.tables = H->d_thr;
+    Q.sched = nullptr;
+    Q.rec = H->d_srec;
+    Q.measure_every = 0;
+    Q.measure_phase = 0;
+    Q.lattices = RT;
+    for (int c = 0; c < kMaxClasses; ++c) {
+        const int L = H->P.cls[c < H->n_classes ? c : 0].L;
+        Q.div_half[c] = make_div((uint32_t)(L / 2));
+        Q.div_L[c] = make_div((uint32_t)L);
+    }
+    Q.pt = 1;
+    Q.ee = ee;
+    Q.me = me;
+    Q.rec_t = H->d_srec_t;
+    Q.eacc = eacc;
+    Q.ebuf = ebuf;
+    Q.r2t = H->d_r2t;
+    Q.t2r = H->d_t2r;
+    Q.betas = H->d_betas;
+    Q.ctrl = H->d_ctrl;
+    Q.bar = bar;
+    Q.err = err;
+    Q.J = H->J;
+    Q.h = H->h;
+    Q.seed = H->seed;
+    Q.n_classes = H->n_classes;
+    int64_t done = 0, row = 0;
+    std::vector<int32_t> tbuf;
+    while (done < n_sweeps) {
+        const int64_t n = std::min(span_max, n_sweeps - done);
+        const uint64_t ks = H->ksample;
+        const int64_t rows = (int64_t)((ks + (uint64_t)n) / (uint64_t)me - ks / (uint64_t)me);
+        ISG_CK(cudaMemsetAsync(H->d_pt_scratch, 0, (size_t)scratch, H->stream));
+        Q.sweep0 = H->gsweep;
+        Q.ks0 = ks;
+        Q.n_sweeps = n;
+        cudaError_t e = H->dim == 3 ? cudaLaunchKernelEx(&cfg, k_ising_resident<3>, H->P, Q)
+                                    : cudaLaunchKernelEx(&cfg, k_ising_resident<2>, H->P, Q);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            if (done == 0) return 1;  // this launch form is not available: graph path
+            return cuda_fail(e, "cudaLaunchKernelEx(k_ising_resident, PT)");
+        }
+        launch_post(H, 0, 0, 0, 0, (int)n);  // device sweep counter
+        H->gsweep += (uint64_t)n;
+        H->ksample += (uint64_t)n;
+        rc = check_launch("isg_ising_pt_run");
+        if (rc) return rc;
+        int herr = 0;
+        ISG_CK(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, H->stream));
+        ISG_CK(cudaStreamSynchronize(H->stream));
+        if (herr)
+            return fail(ISG_ERR_TIMEOUT, "isg_ising_pt_run: an exchange barrier wait gave up");
+        if (rows > 0) {
+            rc = copy_records(H, H->d_srec, rows, row, bond, mag);
+            if (rc) return rc;
+            ISG_CK(cudaMemcpy(tslot + (size_t)row * RT, H->d_srec_t,
+                              (size_t)rows * RT * sizeof(int32_t), cudaMemcpyDeviceToHost));
+            row += rows;
+        }
+        done += n;
+    }
+    if (n_records) *n_records = row;
+    return ISG_OK;
+}
+
 static int schedule_sweeps(isg_ising* H, const double* temps, int64_t n_sweeps, int every,
                            int phase, int64_t* bond, int64_t* mag) {
     const int RT = H->replicas_total;

@@ -77,6 +77,34 @@ def test_sweeps_bit_exact(gpu, oracle, dim, sizes, h):
         assert bond[s * R + r] == ob and mag[s * R + r] == om
 
 
+@pytest.mark.parametrize("dim,sizes,R", [(3, [8, 12, 16, 32], 5), (2, [16, 32, 64], 17)])
+def test_resident_pt_matches_graph_cycle(gpu, dim, sizes, R):
+    """Small lattices run pt_run in one cooperative resident launch (sweeps,
+    measurements, exchanges at a grid barrier); the CUDA-graph cycle of
+    separate launches gives the same records, ladder, acceptances and spins
+    bit for bit, also across calls that split the exchange period."""
+    temps = grid(4.3, 4.7, R) if dim == 3 else grid(2.1, 2.5, R)
+    out = []
+    for resident in (True, False):
+        b = gpu.IsingBatch(sizes, R, seed=77, dim=dim)
+        b.set_resident_pt(resident)
+        b.set_temperatures(temps)
+        b.step(7)
+        b.reset_sampling()
+        parts = [b.pt_run(n, 10, 3) for n in (37, 100, 13)]
+        rec = [np.concatenate([p_[i] for p_ in parts]) for i in range(3)]
+        out.append((rec, b.r2t(), b.accepted(), b.sweep_counter(),
+                    [b.get_spins(s_, r) for s_ in range(len(sizes)) for r in range(R)]))
+        b.close()
+    (ra, ta, aa, sa, pa), (rb, tb, ab, sb, pb) = out
+    for x, y in zip(ra, rb):
+        assert np.array_equal(x, y)
+    assert np.array_equal(ta, tb) and np.array_equal(aa, ab) and sa == sb
+    assert aa.sum() > 0
+    for x, y in zip(pa, pb):
+        assert np.array_equal(x, y)
+
+
 def test_set_spins_roundtrip_and_ordered_limits(gpu, oracle):
     """Ground state: E = -3 (3D) / -2 (2D) per site, |m| = 1 at T = 0.1
     (known_limits_summary.csv, observables.rs:189-216)."""

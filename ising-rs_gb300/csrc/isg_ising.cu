@@ -491,13 +491,23 @@ __device__ __forceinline__ void rolling_quad_step(
         nw.z = ow.z ^ coarse_flips(ow.z, nd2, U2, T8, d2);
         nw.w = ow.w ^ coarse_flips(ow.w, nd3, U3, T8, d3);
         *reinterpret_cast<uint4*>(mc + o) = nw;
-        const bool t0 = any_tie(d0), t1 = any_tie(d1), t2 = any_tie(d2), t3 = any_tie(d3);
-        if (__any_sync(ISG_FULL_MASK, t0 || t1 || t2 || t3)) {
+        uint32_t tm = (any_tie(d0) ? 1u : 0u) | (any_tie(d1) ? 2u : 0u) |
+                      (any_tie(d2) ? 4u : 0u) | (any_tie(d3) ? 8u : 0u);
+        if (__any_sync(ISG_FULL_MASK, tm != 0u)) {
             const uint32_t lt = (1u << lane) - 1u;
-            queue_word(q, tq, t0, lt, o + col, ow.x, nd0, d0);
-            queue_word(q, tq, t1, lt, o + col + 1, ow.y, nd1, d1);
-            queue_word(q, tq, t2, lt, o + col + 2, ow.z, nd2, d2);
-            queue_word(q, tq, t3, lt, o + col + 3, ow.w, nd3, d3);
+            // one entry per lane and pass, the lane's first tied word: a pass
+            // costs one queue append for the warp, and a lane with several
+            // tied words (a few per cent of the warp-steps) takes more passes
+            do {
+                const bool has = tm != 0u;
+                const uint32_t k = has ? (uint32_t)(__ffs(tm) - 1) : 0u;
+                const bool k1 = (k & 1u) != 0, k2 = (k & 2u) != 0;
+                const uint32_t dk = k2 ? (k1 ? d3 : d2) : (k1 ? d1 : d0);
+                const uint32_t ndk = k2 ? (k1 ? nd3 : nd2) : (k1 ? nd1 : nd0);
+                const uint32_t owk = k2 ? (k1 ? ow.w : ow.z) : (k1 ? ow.y : ow.x);
+                queue_word(q, tq, has, lt, o + col + k, owk, ndk, dk);
+                tm &= tm - 1u;
+            } while (__any_sync(ISG_FULL_MASK, tm != 0u));
             while (tq.tail - tq.head >= 32u) {
                 resolve_ties<MODE>(q, tq.head, 32u, lane, tab, pre, P, own, macc);
                 tq.head += 32u;

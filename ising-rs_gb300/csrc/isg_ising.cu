@@ -446,7 +446,8 @@ __device__ __forceinline__ void rolling_quad_step(
     uint32_t pz, uint32_t pwm, bool first, bool last, int src_up, int src_dn, int src_x, bool px,
     uint32_t sel_x, uint32_t& o, uint4& zm, uint4& za, uint4& zp, uint4& qzp, uint4& h0,
     uint4& qh0, uint4& ow, uint4& qow, MeasAcc& macc, const uint32_t* pfb, uint32_t pfo,
-    bool pf_lane, uint2* q, TieQueue& tq, int lane, const uint32_t* tab, uint32_t* own) {
+    bool pf_lane, uint2* q, TieQueue& tq, int lane, const uint32_t* tab, uint32_t* own,
+    uint4* yb, uint32_t y_own, uint32_t y_halo, uint32_t y_halo_step, bool has_halo) {
     const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm;
     if (pf_lane) prefetch_line(pfb + ((o + pfo) & pwm), P.pf_level == 1);
     uint4 n_zp, n_h0, n_ow;
@@ -460,17 +461,15 @@ __device__ __forceinline__ void rolling_quad_step(
         n_h0 = ldg_nc4(oa + o2);
         n_ow = ldg_u4(mc + o2);
     }
-    // y neighbours: rows y+1 (up) and y-1 (down) of the task by shuffle, the
-    // halo row for the last (up) and first (down) row
-    uint4 yu, yd;
-    yu.x = __shfl_sync(ISG_FULL_MASK, za.x, src_up);
-    yu.y = __shfl_sync(ISG_FULL_MASK, za.y, src_up);
-    yu.z = __shfl_sync(ISG_FULL_MASK, za.z, src_up);
-    yu.w = __shfl_sync(ISG_FULL_MASK, za.w, src_up);
-    yd.x = __shfl_sync(ISG_FULL_MASK, za.x, src_dn);
-    yd.y = __shfl_sync(ISG_FULL_MASK, za.y, src_dn);
-    yd.z = __shfl_sync(ISG_FULL_MASK, za.z, src_dn);
-    yd.w = __shfl_sync(ISG_FULL_MASK, za.w, src_dn);
+    // y neighbours through the warp's row buffer in shared memory: rows
+    // 1..nr hold the task's rows of the other colour, row 0 the halo row
+    // below the first (written by the first row's lanes), row nr + 1 the one
+    // above the last; a lane reads the rows above and below its own
+    __syncwarp();
+    yb[y_own] = za;
+    if (has_halo) yb[y_halo] = h0;
+    __syncwarp();
+    const uint4 yu = yb[y_own + y_halo_step], yd = yb[y_own - y_halo_step];
     const uint32_t nb = __shfl_sync(ISG_FULL_MASK, px ? za.x : za.w, src_x);
     // px = 1: bytes {1,2,3} of word k + byte 0 of word k+1; px = 0: byte 3 of
     // word k-1 + bytes {0,1,2} of word k (selects, px differs between rows)
@@ -479,10 +478,10 @@ __device__ __forceinline__ void rolling_quad_step(
     wx.y = __byte_perm(za.y, px ? za.z : za.x, sel_x);
     wx.z = __byte_perm(za.z, px ? za.w : za.y, sel_x);
     wx.w = __byte_perm(za.w, px ? nb : za.z, sel_x);
-    const uint32_t nd0 = (wx.x + za.x + (last ? h0.x : yu.x)) + ((first ? h0.x : yd.x) + zp.x + zm.x);
-    const uint32_t nd1 = (wx.y + za.y + (last ? h0.y : yu.y)) + ((first ? h0.y : yd.y) + zp.y + zm.y);
-    const uint32_t nd2 = (wx.z + za.z + (last ? h0.z : yu.z)) + ((first ? h0.z : yd.z) + zp.z + zm.z);
-    const uint32_t nd3 = (wx.w + za.w + (last ? h0.w : yu.w)) + ((first ? h0.w : yd.w) + zp.w + zm.w);
+    const uint32_t nd0 = (wx.x + za.x + yu.x) + (yd.x + zp.x + zm.x);
+    const uint32_t nd1 = (wx.y + za.y + yu.y) + (yd.y + zp.y + zm.y);
+    const uint32_t nd2 = (wx.z + za.z + yu.z) + (yd.z + zp.z + zm.z);
+    const uint32_t nd3 = (wx.w + za.w + yu.w) + (yd.w + zp.w + zm.w);
     uint4 nw = ow;
     if (MODE != 2) {
         uint32_t d0, d1, d2, d3;
@@ -633,6 +632,9 @@ __global__ void __launch_bounds__(256, MINB)
     k_ising_words(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
     __shared__ uint32_t s_thr[8][16];
     __shared__ uint2 s_q[8][kTieQ];
+    // four words per lane: per warp the rows of its task plus two halo rows
+    // (at most (8 + 2) rows of 4 lanes, or (4 + 2) of 8, (16 + 2) of 2, (32 + 2) of 1)
+    __shared__ uint4 s_y[WMAX == 4 ? 8 : 1][WMAX == 4 ? 80 : 1];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     // rolling ranges (in work units of 512 words: one CTA task of two words
@@ -767,6 +769,11 @@ __global__ void __launch_bounds__(256, MINB)
             const uint32_t sel_lo = pe ? 0x4321u : 0x2107u, sel_hi = pe ? 0x2107u : 0x4321u;
             uint32_t o = z0 * pz;                        // offset of plane z
             if (WMAX == 4 && lw == 2) {
+                // row buffer slots: own row rb + 1; halo row 0 (first row) or
+                // nr + 1 (last row); a row is lpr lanes
+                const uint32_t lpr = 1u << lh;
+                const uint32_t y_own = (rb + 1) * lpr + k2;
+                const uint32_t y_halo = (first ? 0u : (nr + 1) * lpr) + k2;
                 uint4 zm = ldg_nc4(oc + ((o - pz) & pwm));
                 uint4 za = ldg_nc4(oc + o);
                 uint4 zp = ldg_nc4(oc + ((o + pz) & pwm));
@@ -793,7 +800,7 @@ __global__ void __launch_bounds__(256, MINB)
     rolling_quad_step<MODE, PF>(P, pre, T8, u0.W, u1.W, u2.W, u3.W, oc, oa, mc, col, pz, pwm,  \
                                 first, last, src_up, src_dn, SRC, PX, SEL, o, zm, za, zp, qzp, \
                                 h0, qh0, ow, qow, macc, pfb, pfo, pf_lane, q, tq, lane, tab,   \
-                                own)
+                                own, s_y[wib], y_own, y_halo, lpr, first || last)
                     ISG_ROLL4(x, src_lo, pe, sel_lo);
                     ISG_ROLL4(y, src_hi, !pe, sel_hi);
                     ISG_ROLL4(z, src_lo, pe, sel_lo);

@@ -298,8 +298,9 @@ int isg_cont_normalize(isg_cont* h);
 /* Observables of every replica, synchronous: energy[r] = -J sum_bonds S.S',
  * mag[r*3 + k] = sum S_k (k = 2 is 0 for XY), bonds[r*6 + a] (may be NULL) =
  * sum_i S_i.S_{i+a} for a = x, y, z, then sum_i (S_i x S_{i+a})_z: the
- * helicity-modulus sums.  Compensated FP32 per block, FP64 combine in a fixed
- * order (deterministic).  Replaces ContinuousGpuLattice::measure_gpu
+ * helicity-modulus sums.  Exact fixed-point sums (each term rounded once to a
+ * multiple of 2^-24, int64 across threads and blocks, one FP64 conversion):
+ * the result does not depend on the order of summation.  Replaces ContinuousGpuLattice::measure_gpu
  * (gpu_lattice_continuous.rs:177-240; reduce_kernel.cu:70-151). */
 int isg_cont_measure(isg_cont* h, double* energy, double* mag, double* bonds);
 /* Exchange pass on the energies of the last measurement (as

@@ -8,11 +8,12 @@
 // isg_cont_observables_static serves them: the caller passes the lattices and
 // the output buffer (both device memory it owns), and the block partials that
 // the reduction needs live in a fixed file-scope __device__ array instead of
-// memory the library would allocate.  It is the same reduction as the measure
-// step of the O(n) path (compensated FP32 per block, FP64 combine in a fixed
-// order), applied to lattices in the natural interleaved layout the
-// reference uses for continuous spins (n_comp floats per site, site index
-// z*L*L + y*L + x).
+// memory the library would allocate.  It computes the observables of the
+// measure step of the O(n) path, summed in compensated FP32 per block with an
+// FP64 combine in a fixed order (deterministic; it agrees with the exact
+// fixed-point sums of isg_cont_measure to FP32 rounding), on lattices in the
+// natural interleaved layout the reference uses for continuous spins (n_comp
+// floats per site, site index z*L*L + y*L + x).
 #include <cuda_runtime.h>
 #include <stdint.h>
 

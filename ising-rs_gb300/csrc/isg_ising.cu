@@ -423,15 +423,72 @@ __device__ __forceinline__ void rolling_pair_step(
     o = o1;
 }
 
-// Queue the tied sites of one word (lane-varying t; warp-uniform call).
-__device__ __forceinline__ void queue_word(uint2* q, TieQueue& tq, bool t, uint32_t lt,
-                                           uint32_t w, uint32_t own_w, uint32_t nd,
-                                           uint32_t d) {
-    const uint32_t b = __ballot_sync(ISG_FULL_MASK, t);
-    if (t)
-        q[(tq.tail + __popc(b & lt)) & (kTieQ - 1)] =
-            make_uint2(w, (nd + (own_w << 3)) | (tie_bytes(d) >> 3));
-    tq.tail += __popc(b);
+// Tie queue of the four-words-per-lane path: one entry per lane-step with a
+// tie in any of its four words, holding the raw per-word values the fine
+// decision needs, so that appending costs no per-word selection: the first
+// word index, per word own_down*8 + n_down per byte, and the coarse values D
+// (tied bytes are those equal to 0x7F).  A step appends at most 32 entries
+// and 32 are resolved whenever that many are pending, so at most 63 wait.
+constexpr uint32_t kQuadQ = 64;
+struct QuadTies {
+    uint32_t w[kQuadQ];
+    uint4 idx[kQuadQ];
+    uint4 d[kQuadQ];
+};
+
+// Byte-wise zero test of D ^ 0x7F7F7F7F without the final mask: OR the
+// values of several words, then (acc & 0x80808080) != 0 iff some byte of
+// some word is a tie (exact for this any-test).
+__device__ __forceinline__ uint32_t tie_acc(uint32_t D) {
+    const uint32_t x = D ^ 0x7F7F7F7Fu;
+    return (x - 0x01010101u) & ~x;
+}
+
+// Resolve `count` (1..32) queued lane-step entries from head: lane l takes
+// entry head + l and decides each of its tied words in turn (one fine block
+// per tied word; lanes with more tied words take more turns).
+template <int MODE>
+__device__ __forceinline__ void resolve_quad(const QuadTies& Q, uint32_t head, uint32_t count,
+                                             int lane, const uint32_t* tab, const PhiloxPre& pre,
+                                             const IsingParams& P, uint32_t* own, MeasAcc& macc) {
+    __syncwarp();
+    if ((uint32_t)lane < count) {
+        const uint32_t s = (head + (uint32_t)lane) & (kQuadQ - 1);
+        const uint32_t w0 = Q.w[s];
+        const uint4 I = Q.idx[s], D = Q.d[s];
+        const uint32_t t0 = tie_bytes(D.x), t1 = tie_bytes(D.y), t2 = tie_bytes(D.z),
+                       t3 = tie_bytes(D.w);
+        uint32_t tm = (t0 ? 1u : 0u) | (t1 ? 2u : 0u) | (t2 ? 4u : 0u) | (t3 ? 8u : 0u);
+        while (tm) {
+            const uint32_t k = (uint32_t)(__ffs(tm) - 1);
+            tm &= tm - 1u;
+            const bool k1 = (k & 1u) != 0, k2 = (k & 2u) != 0;
+            const uint32_t tb = k2 ? (k1 ? t3 : t2) : (k1 ? t1 : t0);
+            const uint32_t idx = k2 ? (k1 ? I.w : I.z) : (k1 ? I.y : I.x);
+            const uint32_t flip = fine_flips(tb, idx, tab, pre, P, w0 + k);
+            if (flip) {
+                atomicXor(own + w0 + k, flip);
+                if (MODE == 1) {
+                    const uint32_t od = (idx >> 3) & flip, ou = flip & ~od;
+                    const uint32_t nd = idx & 0x07070707u;
+                    macc.so += (int)__dp4a(ou, 0x01010101u, 0u) - (int)__dp4a(od, 0x01010101u, 0u);
+                    macc.sond += (int)__dp4a(ou, nd, 0u) - (int)__dp4a(od, nd, 0u);
+                }
+            }
+        }
+    }
+    __syncwarp();
+}
+
+template <int MODE>
+__device__ __forceinline__ void drain_quad(const QuadTies& Q, TieQueue& tq, int lane,
+                                           const uint32_t* tab, const PhiloxPre& pre,
+                                           const IsingParams& P, uint32_t* own, MeasAcc& macc) {
+    while (tq.tail != tq.head) {
+        const uint32_t c = min(tq.tail - tq.head, 32u);
+        resolve_quad<MODE>(Q, tq.head, c, lane, tab, pre, P, own, macc);
+        tq.head += c;
+    }
 }
 
 // One z-step of a rolling column with four adjacent words per lane (L >=
@@ -446,7 +503,7 @@ __device__ __forceinline__ void rolling_quad_step(
     uint32_t pz, uint32_t pwm, bool first, bool last, int src_up, int src_dn, int src_x, bool px,
     uint32_t sel_x, uint32_t& o, uint4& zm, uint4& za, uint4& zp, uint4& qzp, uint4& h0,
     uint4& qh0, uint4& ow, uint4& qow, MeasAcc& macc, const uint32_t* pfb, uint32_t pfo,
-    bool pf_lane, uint2* q, TieQueue& tq, int lane, const uint32_t* tab, uint32_t* own,
+    bool pf_lane, QuadTies& Q, TieQueue& tq, int lane, const uint32_t* tab, uint32_t* own,
     uint4* yb, uint32_t y_own, uint32_t y_halo, uint32_t y_halo_step, bool has_halo) {
     const uint32_t o1 = (o + pz) & pwm, o2 = (o + 2 * pz) & pwm;
     if (pf_lane) prefetch_line(pfb + ((o + pfo) & pwm), P.pf_level == 1);
@@ -490,25 +547,23 @@ __device__ __forceinline__ void rolling_quad_step(
         nw.z = ow.z ^ coarse_flips(ow.z, nd2, U2, T8, d2);
         nw.w = ow.w ^ coarse_flips(ow.w, nd3, U3, T8, d3);
         *reinterpret_cast<uint4*>(mc + o) = nw;
-        uint32_t tm = (any_tie(d0) ? 1u : 0u) | (any_tie(d1) ? 2u : 0u) |
-                      (any_tie(d2) ? 4u : 0u) | (any_tie(d3) ? 8u : 0u);
-        if (__any_sync(ISG_FULL_MASK, tm != 0u)) {
-            const uint32_t lt = (1u << lane) - 1u;
-            // one entry per lane and pass, the lane's first tied word: a pass
-            // costs one queue append for the warp, and a lane with several
-            // tied words (a few per cent of the warp-steps) takes more passes
-            do {
-                const bool has = tm != 0u;
-                const uint32_t k = has ? (uint32_t)(__ffs(tm) - 1) : 0u;
-                const bool k1 = (k & 1u) != 0, k2 = (k & 2u) != 0;
-                const uint32_t dk = k2 ? (k1 ? d3 : d2) : (k1 ? d1 : d0);
-                const uint32_t ndk = k2 ? (k1 ? nd3 : nd2) : (k1 ? nd1 : nd0);
-                const uint32_t owk = k2 ? (k1 ? ow.w : ow.z) : (k1 ? ow.y : ow.x);
-                queue_word(q, tq, has, lt, o + col + k, owk, ndk, dk);
-                tm &= tm - 1u;
-            } while (__any_sync(ISG_FULL_MASK, tm != 0u));
-            while (tq.tail - tq.head >= 32u) {
-                resolve_ties<MODE>(q, tq.head, 32u, lane, tab, pre, P, own, macc);
+        const bool has =
+            ((tie_acc(d0) | tie_acc(d1) | tie_acc(d2) | tie_acc(d3)) & 0x80808080u) != 0u;
+        const uint32_t b = __ballot_sync(ISG_FULL_MASK, has);
+        if (b != 0u) {
+            // one entry per lane-step with a tie, at its rank among this
+            // step's entries
+            if (has) {
+                const uint32_t s =
+                    (tq.tail + __popc(b & ((1u << lane) - 1u))) & (kQuadQ - 1);
+                Q.w[s] = o + col;
+                Q.idx[s] = make_uint4(nd0 + (ow.x << 3), nd1 + (ow.y << 3), nd2 + (ow.z << 3),
+                                      nd3 + (ow.w << 3));
+                Q.d[s] = make_uint4(d0, d1, d2, d3);
+            }
+            tq.tail += __popc(b);
+            if (tq.tail - tq.head >= 32u) {
+                resolve_quad<MODE>(Q, tq.head, 32u, lane, tab, pre, P, own, macc);
                 tq.head += 32u;
             }
         }
@@ -631,7 +686,14 @@ template <int DIM, int MODE, int PF, int WMAX, int MINB>
 __global__ void __launch_bounds__(256, MINB)
     k_ising_words(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
     __shared__ uint32_t s_thr[8][16];
-    __shared__ uint2 s_q[8][kTieQ];
+    // per warp: the tie queue of the two-words-per-lane path or that of the
+    // four-words path (a kernel runs one of the two: every rolling size of a
+    // batch has the same words per lane)
+    union TieStore {
+        uint2 pair[kTieQ];
+        QuadTies quad;
+    };
+    __shared__ TieStore s_ties[8];
     // four words per lane: per warp the rows of its task plus two halo rows
     // (at most (8 + 2) rows of 4 lanes, or (4 + 2) of 8, (16 + 2) of 2, (32 + 2) of 1)
     __shared__ uint4 s_y[WMAX == 4 ? 8 : 1][WMAX == 4 ? 80 : 1];
@@ -660,7 +722,8 @@ __global__ void __launch_bounds__(256, MINB)
     const uint32_t c2 = (uint32_t)sweep;
     const uint32_t c3 = counter_word3(ISG_TAG_ISING, (uint32_t)colour, sweep);
     const uint32_t* tab = s_thr[wib];
-    uint2* q = s_q[wib];
+    uint2* q = s_ties[wib].pair;
+    QuadTies& qq = s_ties[wib].quad;
     constexpr int Z = 2 * DIM;
 
     int ci = 0;
@@ -717,7 +780,12 @@ __global__ void __launch_bounds__(256, MINB)
         const uint32_t* oth =
             reinterpret_cast<const uint32_t*>(base + (int64_t)(colour ^ 1) * C.plane_sites);
         if (rg != cur_rep) {
-            if (MODE != 2) drain_ties<MODE>(q, tq, lane, tab, pre, P, cur_own, macc);
+            if (MODE != 2) {
+                if (WMAX == 4)
+                    drain_quad<MODE>(qq, tq, lane, tab, pre, P, cur_own, macc);
+                else
+                    drain_ties<MODE>(q, tq, lane, tab, pre, P, cur_own, macc);
+            }
             if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
             cur_rep = rg;
             cur_own = own;
@@ -768,7 +836,9 @@ __global__ void __launch_bounds__(256, MINB)
             const int src_lo = pe ? src_next2 : src_prev2, src_hi = pe ? src_prev2 : src_next2;
             const uint32_t sel_lo = pe ? 0x4321u : 0x2107u, sel_hi = pe ? 0x2107u : 0x4321u;
             uint32_t o = z0 * pz;                        // offset of plane z
-            if (WMAX == 4 && lw == 2) {
+            if constexpr (WMAX == 4) {
+                // (a kernel with WMAX = 4 runs every rolling size at four
+                // words per lane: lw == 2)
                 // row buffer slots: own row rb + 1; halo row 0 (first row) or
                 // nr + 1 (last row); a row is lpr lanes
                 const uint32_t lpr = 1u << lh;
@@ -799,7 +869,7 @@ __global__ void __launch_bounds__(256, MINB)
 #define ISG_ROLL4(W, SRC, PX, SEL)                                                            \
     rolling_quad_step<MODE, PF>(P, pre, T8, u0.W, u1.W, u2.W, u3.W, oc, oa, mc, col, pz, pwm,  \
                                 first, last, src_up, src_dn, SRC, PX, SEL, o, zm, za, zp, qzp, \
-                                h0, qh0, ow, qow, macc, pfb, pfo, pf_lane, q, tq, lane, tab,   \
+                                h0, qh0, ow, qow, macc, pfb, pfo, pf_lane, qq, tq, lane, tab,  \
                                 own, s_y[wib], y_own, y_halo, lpr, first || last)
                     ISG_ROLL4(x, src_lo, pe, sel_lo);
                     ISG_ROLL4(y, src_hi, !pe, sel_hi);
@@ -884,7 +954,12 @@ __global__ void __launch_bounds__(256, MINB)
             if (MODE != 0) meas_add(macc, nw, nd, wa);
         }
     }
-    if (MODE != 2) drain_ties<MODE>(q, tq, lane, tab, pre, P, cur_own, macc);
+    if (MODE != 2) {
+        if (WMAX == 4)
+            drain_quad<MODE>(qq, tq, lane, tab, pre, P, cur_own, macc);
+        else
+            drain_ties<MODE>(q, tq, lane, tab, pre, P, cur_own, macc);
+    }
     if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
 
     // site tasks (even L that are not word sizes): one site per thread,

@@ -219,10 +219,12 @@ int isg_ising_sync(isg_ising* h);
  * half-sweep kernel, so `threads` (64, 128, 256 or 512) is validated and
  * kept but no longer changes the launch.  Results never depend on either. */
 int isg_ising_set_launch(isg_ising* h, int threads, int blocks_per_sm);
-/* Prefetch depth of the rolling half-sweep (3D, L = 64..256): 1 = loads one
- * plane ahead, 3 blocks per SM; 2 = two planes ahead, 2 blocks per SM;
- * 0 = automatic (2 when all spin planes fit in 96 MiB, else 1).  Results never
- * depend on it. */
+/* Prefetch form of the rolling half-sweep (3D, L = 32..256): 1 = loads one
+ * plane ahead into registers; 2 = two planes ahead; 3 = (four words per lane)
+ * copies into a per-warp ring in shared memory, own words two planes and the
+ * other colour three planes ahead; 0 = automatic (3 with four words per
+ * lane, else 2 when all spin planes fit in 96 MiB, else 1; 3 falls back to
+ * that choice with two words per lane).  Results never depend on it. */
 int isg_ising_set_prefetch(isg_ising* h, int depth);
 /* Rolling half-sweep (3D, L = 64..256): lanes of each warp also prefetch the
  * lines of the task's own and other-colour words (and halo rows) `planes`

@@ -592,6 +592,128 @@ __device__ __forceinline__ void rolling_quad_step(
 }
 
 
+// Four words per lane fed through a per-warp ring in shared memory (PF = 3):
+// each step copies, with cp.async (straight into shared memory, no
+// registers held while the copy is in flight), the lane's own words two
+// planes ahead and its other-colour words (plus the halo rows) three planes
+// ahead.  A ring stage of the other colour holds the task's rows at one
+// plane with the halo rows below and above (row r at slots (r + 1) * lpr +
+// k2), so the y neighbours are read from the stage directly.  Both rings
+// have 4 stages, so with z quads aligned to z = 0 mod 4 a step's stage
+// indices are compile-time constants.  Copies of a step form one group
+// (empty past the end of the task): at the top of step z one group may be
+// outstanding, so the one of step z - 2 (own plane z, other plane z + 1)
+// is complete.
+constexpr uint32_t kRingSO = 48;  // other-colour slots per stage ((nr + 2) lpr <= 48 for L <= 256)
+constexpr uint32_t kRingWarpBytes = 4u * (kRingSO + 32u) * 16u;
+constexpr uint32_t kRingBytes = 8u * kRingWarpBytes;  // per 256-thread block
+
+__device__ __forceinline__ void cp_async16(uint32_t saddr, const void* g) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ uint4 lds_v4(uint32_t saddr) {
+    uint4 v;
+    asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "r"(saddr)
+                 : "memory");
+    return v;
+}
+
+// Ring addresses of one warp: oth = stage 0 of the other colour, own = stage
+// 0 of the own colour; y_own / y_halo: the lane's slot and its halo slot.
+struct Ring {
+    uint32_t oth, own, y_own, y_halo, lpr;
+    bool has_halo;
+};
+
+// Copies of plane j's own words (stage j & 3) and plane j + 1's other-colour
+// words (stage (j + 1) & 3) at plane offsets oj / oj1, then the group commit.
+template <int SJ>
+__device__ __forceinline__ void ring_issue(const Ring& G, const uint32_t* oc, const uint32_t* oa,
+                                           const uint32_t* mc, uint32_t oj, uint32_t oj1,
+                                           bool copy, int lane) {
+    if (copy) {
+        cp_async16(G.own + ((uint32_t)(SJ & 3) * 32u + (uint32_t)lane) * 16u, mc + oj);
+        const uint32_t st = G.oth + (uint32_t)((SJ + 1) & 3) * kRingSO * 16u;
+        cp_async16(st + G.y_own * 16u, oc + oj1);
+        if (G.has_halo) cp_async16(st + G.y_halo * 16u, oa + oj1);
+    }
+    cp_async_commit();
+}
+
+template <int MODE, int S>
+__device__ __forceinline__ void ring_quad_step(
+    const IsingParams& P, const PhiloxPre& pre, const Thr8& T8, uint32_t U0, uint32_t U1,
+    uint32_t U2, uint32_t U3, const Ring& G, const uint32_t* oc, const uint32_t* oa, uint32_t* mc,
+    uint32_t col, uint32_t pz, uint32_t pwm, uint32_t z, uint32_t z1, int src_x, bool px,
+    uint32_t sel_x, uint32_t& o, uint4& zm, uint4& za, MeasAcc& macc, const uint32_t* pfb,
+    uint32_t pfo, bool pf_lane, QuadTies& Q, TieQueue& tq, int lane, const uint32_t* tab,
+    uint32_t* own) {
+    cp_async_wait<1>();
+    __syncwarp();  // the group of step z - 2 is visible to the warp; step z - 1's reads are done
+    ring_issue<S + 2>(G, oc, oa, mc, (o + 2 * pz) & pwm, (o + 3 * pz) & pwm, z + 2 < z1, lane);
+    if (pf_lane) prefetch_line(pfb + ((o + pfo) & pwm), P.pf_level == 1);
+    const uint32_t st = G.oth + (uint32_t)S * kRingSO * 16u;
+    const uint4 zp = lds_v4(G.oth + ((uint32_t)((S + 1) & 3) * kRingSO + G.y_own) * 16u);
+    const uint4 yu = lds_v4(st + (G.y_own + G.lpr) * 16u);
+    const uint4 yd = lds_v4(st + (G.y_own - G.lpr) * 16u);
+    const uint4 ow = lds_v4(G.own + ((uint32_t)S * 32u + (uint32_t)lane) * 16u);
+    const uint32_t nb = __shfl_sync(ISG_FULL_MASK, px ? za.x : za.w, src_x);
+    uint4 wx;
+    wx.x = __byte_perm(za.x, px ? za.y : nb, sel_x);
+    wx.y = __byte_perm(za.y, px ? za.z : za.x, sel_x);
+    wx.z = __byte_perm(za.z, px ? za.w : za.y, sel_x);
+    wx.w = __byte_perm(za.w, px ? nb : za.z, sel_x);
+    const uint32_t nd0 = (wx.x + za.x + yu.x) + (yd.x + zp.x + zm.x);
+    const uint32_t nd1 = (wx.y + za.y + yu.y) + (yd.y + zp.y + zm.y);
+    const uint32_t nd2 = (wx.z + za.z + yu.z) + (yd.z + zp.z + zm.z);
+    const uint32_t nd3 = (wx.w + za.w + yu.w) + (yd.w + zp.w + zm.w);
+    uint4 nw = ow;
+    if (MODE != 2) {
+        uint32_t d0, d1, d2, d3;
+        nw.x = ow.x ^ coarse_flips(ow.x, nd0, U0, T8, d0);
+        nw.y = ow.y ^ coarse_flips(ow.y, nd1, U1, T8, d1);
+        nw.z = ow.z ^ coarse_flips(ow.z, nd2, U2, T8, d2);
+        nw.w = ow.w ^ coarse_flips(ow.w, nd3, U3, T8, d3);
+        *reinterpret_cast<uint4*>(mc + o) = nw;
+        const bool has =
+            ((tie_acc(d0) | tie_acc(d1) | tie_acc(d2) | tie_acc(d3)) & 0x80808080u) != 0u;
+        const uint32_t b = __ballot_sync(ISG_FULL_MASK, has);
+        if (b != 0u) {
+            if (has) {
+                const uint32_t s =
+                    (tq.tail + __popc(b & ((1u << lane) - 1u))) & (kQuadQ - 1);
+                Q.w[s] = o + col;
+                Q.idx[s] = make_uint4(nd0 + (ow.x << 3), nd1 + (ow.y << 3), nd2 + (ow.z << 3),
+                                      nd3 + (ow.w << 3));
+                Q.d[s] = make_uint4(d0, d1, d2, d3);
+            }
+            tq.tail += __popc(b);
+            if (tq.tail - tq.head >= 32u) {
+                resolve_quad<MODE>(Q, tq.head, 32u, lane, tab, pre, P, own, macc);
+                tq.head += 32u;
+            }
+        }
+    }
+    if (MODE != 0) {
+        meas_add(macc, nw.x, nd0, za.x);
+        meas_add(macc, nw.y, nd1, za.y);
+        meas_add(macc, nw.z, nd2, za.z);
+        meas_add(macc, nw.w, nd3, za.w);
+    }
+    zm = za;
+    za = zp;
+    o = (o + pz) & pwm;
+}
+
 // One site of a one-site task (any even L), split in two so that a thread
 // can issue the loads of several sites before it decides any: site_gather
 // reads the site's down bit, its down-neighbour count and the other colour's
@@ -676,9 +798,10 @@ __device__ __forceinline__ void site_decide(SiteWork& w, uint32_t c2, uint32_t c
 // neighbours load at the same time (L1 hits); consecutive CTA tasks walk z, so
 // the z-1/z/z+1 words of the other colour stay in registers (64 words per warp
 // task).  Flat sizes give each warp one 32-word task per CTA task.
-// PF: rolling loads issued PF planes ahead (1: 3 blocks per SM, 2: 2 blocks
-// per SM with more loads in flight per warp); chosen per batch (configure_launch,
-// isg_ising_autotune).
+// PF: rolling loads issued PF planes ahead into registers (1: 3 blocks per
+// SM, 2: 2 blocks per SM with more loads in flight per warp), or 3: four
+// words per lane fed through the shared-memory ring (ring_quad_step); chosen
+// per batch (configure_launch, isg_ising_autotune).
 // WMAX: 4 if some size runs four words per lane (that path needs more
 // registers: 2 blocks per SM), else 2.  MINB: blocks per SM the registers
 // are budgeted for.
@@ -696,7 +819,9 @@ __global__ void __launch_bounds__(256, MINB)
     __shared__ TieStore s_ties[8];
     // four words per lane: per warp the rows of its task plus two halo rows
     // (at most (8 + 2) rows of 4 lanes, or (4 + 2) of 8, (16 + 2) of 2, (32 + 2) of 1)
-    __shared__ uint4 s_y[WMAX == 4 ? 8 : 1][WMAX == 4 ? 80 : 1];
+    __shared__ uint4 s_y[WMAX == 4 && PF != 3 ? 8 : 1][WMAX == 4 && PF != 3 ? 80 : 1];
+    // PF = 3: the per-warp rings (kRingBytes of dynamic shared memory)
+    extern __shared__ uint4 s_ring[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     // rolling ranges (in work units of 512 words: one CTA task of two words
@@ -836,9 +961,47 @@ __global__ void __launch_bounds__(256, MINB)
             const int src_lo = pe ? src_next2 : src_prev2, src_hi = pe ? src_prev2 : src_next2;
             const uint32_t sel_lo = pe ? 0x4321u : 0x2107u, sel_hi = pe ? 0x2107u : 0x4321u;
             uint32_t o = z0 * pz;                        // offset of plane z
-            if constexpr (WMAX == 4) {
+            if constexpr (WMAX == 4 && PF == 3) {
                 // (a kernel with WMAX = 4 runs every rolling size at four
-                // words per lane: lw == 2)
+                // words per lane: lw == 2) ring slots: own row rb + 1; halo
+                // row 0 (first row) or nr + 1 (last row); a row is lpr lanes
+                const uint32_t lpr = 1u << lh;
+                Ring G;
+                G.oth = (uint32_t)__cvta_generic_to_shared(s_ring) + (uint32_t)wib * kRingWarpBytes;
+                G.own = G.oth + 4u * kRingSO * 16u;
+                G.y_own = (rb + 1) * lpr + k2;
+                G.y_halo = (first ? 0u : (nr + 1) * lpr) + k2;
+                G.lpr = lpr;
+                G.has_halo = first || last;
+                __syncwarp();  // the warp's reads of the ring in its previous task are done
+                // prologue (z0 = 0 mod 4): the task's rows of the other colour
+                // at z0 join the group of (own z0, other z0 + 1); then the
+                // group of (own z0 + 1, other z0 + 2)
+                cp_async16(G.oth + G.y_own * 16u, oc + o);
+                if (G.has_halo) cp_async16(G.oth + G.y_halo * 16u, oa + o);
+                ring_issue<0>(G, oc, oa, mc, o, (o + pz) & pwm, true, lane);
+                ring_issue<1>(G, oc, oa, mc, (o + pz) & pwm, (o + 2 * pz) & pwm, true, lane);
+                uint4 zm = ldg_nc4(oc + ((o - pz) & pwm));
+                uint4 za = ldg_nc4(oc + o);
+                for (uint32_t z = z0; z < z1; z += 4) {
+                    U4 u0{}, u1{}, u2{}, u3{};
+                    if (MODE != 2) {
+                        u0 = philox_w(pre, P, (o >> 2) + col);
+                        u1 = philox_w(pre, P, (o >> 2) + col + 1);
+                        u2 = philox_w(pre, P, (o >> 2) + col + 2);
+                        u3 = philox_w(pre, P, (o >> 2) + col + 3);
+                    }
+#define ISG_RING4(S, W, SRC, PX, SEL)                                                           \
+    ring_quad_step<MODE, S>(P, pre, T8, u0.W, u1.W, u2.W, u3.W, G, oc, oa, mc, col, pz, pwm,     \
+                            z + S, z1, SRC, PX, SEL, o, zm, za, macc, pfb, pfo, pf_lane, qq, tq, \
+                            lane, tab, own)
+                    ISG_RING4(0, x, src_lo, pe, sel_lo);
+                    ISG_RING4(1, y, src_hi, !pe, sel_hi);
+                    ISG_RING4(2, z, src_lo, pe, sel_lo);
+                    ISG_RING4(3, w, src_hi, !pe, sel_hi);
+#undef ISG_RING4
+                }
+            } else if constexpr (WMAX == 4) {
                 // row buffer slots: own row rb + 1; halo row 0 (first row) or
                 // nr + 1 (last row); a row is lpr lanes
                 const uint32_t lpr = 1u << lh;
@@ -1759,6 +1922,7 @@ static void (*word_kernel_m(int mode))(IsingParams, int, int) {
 static void (*word_kernel(int dim, int mode, int pf, int wmax))(IsingParams, int, int) {
     if (dim == 3) {
         if (wmax == 4) {
+            if (pf == 3) return word_kernel_m<3, 3, 4, 2>(mode);
             if (pf == 2) return word_kernel_m<3, 2, 4, 2>(mode);
             return word_kernel_m<3, 1, 4, 2>(mode);
         }
@@ -1769,12 +1933,20 @@ static void (*word_kernel(int dim, int mode, int pf, int wmax))(IsingParams, int
     return word_kernel_m<2, 1, 2, 3>(mode);
 }
 
+// Dynamic shared memory of the word kernel: the per-warp rings of PF = 3.
+static size_t word_smem(const isg_ising* H) {
+    return H->dim == 3 && H->wmax == 4 && H->pf == 3 ? (size_t)kRingBytes : 0;
+}
+
 // Word kernels run 256-thread blocks (one CTA task = 8 warp tasks); the
 // grid is SMs x blocks per SM (occupancy maximum unless set), at most one
-// block per CTA task.  `threads` applies to the site kernel.  Prefetch depth:
-// as set, else 2 when the batch's spins fit in L2 (latency of L2 hits is
-// hidden better by loads further ahead) and 1 otherwise (three blocks per SM
-// keep more DRAM requests in flight) — measured on both kinds of workload.
+// block per CTA task.  `threads` applies to the site kernel.  Prefetch form:
+// as set, else the shared-memory ring with four words per lane (5% faster at
+// L = 128 x 128 than loads one plane ahead in registers, 7% on the mixed PT
+// batch), and with two words per lane 2 when the batch's spins fit in L2
+// (latency of L2 hits is hidden better by loads further ahead) and 1
+// otherwise (three blocks per SM keep more DRAM requests in flight) —
+// measured on both kinds of workload.
 static int configure_launch(isg_ising* H) {
     const int thr = H->threads;
     // one launch per half-sweep covers every size: rolling ranges, flat
@@ -1784,17 +1956,24 @@ static int configure_launch(isg_ising* H) {
     const bool in_l2 = H->spin_bytes <= ((int64_t)96 << 20);
     // two words per lane: loads two planes ahead help L2-resident batches;
     // four words per lane (2 blocks per SM either way): one plane ahead
-    H->pf = H->prefetch > 0 ? H->prefetch : (in_l2 && H->wmax == 2 ? 2 : 1);
-    if (H->dim != 3) H->pf = 1;
-    // batches larger than L2: lines 3 planes ahead prefetched into L2
+    H->pf = H->prefetch > 0 ? H->prefetch : (H->wmax == 4 ? 3 : in_l2 ? 2 : 1);
+    if (H->dim != 3 || (H->pf == 3 && H->wmax != 4)) H->pf = H->dim == 3 && in_l2 ? 2 : 1;
+    // batches larger than L2 on the register paths: lines 3 planes ahead
+    // prefetched into L2 (the ring's copies run far enough ahead without)
     if (!H->cache_pf_set) {
-        H->P.l2_ahead = in_l2 ? 0 : 3;
+        H->P.l2_ahead = in_l2 || H->pf == 3 ? 0 : 3;
         H->P.pf_level = 2;
     }
+    const size_t dyn = word_smem(H);
     for (int mode = 0; mode < 3; ++mode) {
         int occ = 0;
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ, (const void*)word_kernel(H->dim, mode, H->pf, H->wmax), 256, 0);
+        const void* fn = (const void*)word_kernel(H->dim, mode, H->pf, H->wmax);
+        if (dyn > 0) {
+            cudaError_t a =
+                cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+            if (a != cudaSuccess) return cuda_fail(a, "cudaFuncSetAttribute");
+        }
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 256, dyn);
         if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
         if (occ < 1) occ = 1;
         const int bps = H->blocks_per_sm > 0 ? std::min(H->blocks_per_sm, occ) : occ;
@@ -1813,7 +1992,7 @@ static void launch_half(isg_ising* H, int colour, int sweep_off, int mode) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)H->word_grids[mode]);
         cfg.blockDim = dim3(256);
-        cfg.dynamicSmemBytes = 0;
+        cfg.dynamicSmemBytes = word_smem(H);
         cfg.stream = H->stream;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -2716,7 +2895,7 @@ int isg_ising_set_words_per_lane(isg_ising* H, int words) {
 
 int isg_ising_set_prefetch(isg_ising* H, int depth) {
     if (!H) return fail(ISG_ERR_ARG, "isg_ising_set_prefetch: NULL handle");
-    if (depth < 0 || depth > 2) return fail(ISG_ERR_ARG, "isg_ising_set_prefetch: depth must be 0..2");
+    if (depth < 0 || depth > 3) return fail(ISG_ERR_ARG, "isg_ising_set_prefetch: depth must be 0..3");
     cudaSetDevice(H->device);
     ISG_CK(cudaStreamSynchronize(H->stream));
     H->prefetch = depth;
@@ -2732,7 +2911,9 @@ int isg_ising_autotune(isg_ising* H, int* best) {
     const int bps_opts[] = {1, 2, 4, 8, 16, 0};
     float best_ms = 1e30f;
     int bt = H->threads, bb = H->blocks_per_sm, bp = H->prefetch;
-    const int npf = H->dim == 3 ? 2 : 1;
+    // prefetch forms: registers one or two planes ahead; with four words per
+    // lane also the shared-memory ring
+    const int npf = H->dim == 3 ? (H->wmax == 4 ? 3 : 2) : 1;
     for (int pf = 1; pf <= npf; ++pf)
         for (int t : thr_opts)
             for (int b : bps_opts) {

@@ -214,12 +214,13 @@ def test_production_size_properties(gpu, oracle):
         assert np.array_equal(d.get_spins(0, r), sp)
 
 
-@pytest.mark.parametrize("depth", [1, 2])
+@pytest.mark.parametrize("depth", [1, 2, 3])
 def test_rolling_sizes_match_replay(gpu, oracle, depth):
-    """Every rolling size (L = 64: 8-row tasks; L = 256: 2-row tasks, the
-    first/last halo rows of every lane pair) against the replay, bit for bit,
-    at both prefetch depths."""
-    for L in (64, 256):
+    """Every rolling size (L = 32: a warp task is the whole plane; L = 64:
+    16-row tasks; L = 256: 4-row tasks, the first/last halo rows of every
+    lane group) against the replay, bit for bit, with loads one or two planes
+    ahead in registers or through the shared-memory ring (depth 3)."""
+    for L in (32, 64, 256):
         d = gpu.IsingBatch([L], 1, seed=5)
         d.set_prefetch(depth)
         d.set_temperatures([4.51])
@@ -234,19 +235,21 @@ def test_rolling_sizes_match_replay(gpu, oracle, depth):
 
 
 def test_prefetch_depth_keeps_results(gpu):
-    """Both rolling prefetch depths give the same bits (L = 64 and 128 are rolling)."""
+    """Every rolling prefetch form gives the same bits (L = 64 and 128 are
+    rolling), through sweeps with fused measurements and exchanges."""
     sizes, R = [64, 128], 2
     out = []
-    for depth in (1, 2):
+    for depth in (1, 2, 3):
         b = gpu.IsingBatch(sizes, R, seed=13)
         b.set_prefetch(depth)
         b.set_temperatures(grid(4.4, 4.6, R))
         b.step(4)
         _, bb, mm = b.pt_run(6, 3, 2)
         out.append((bb, mm, [b.get_spins(s, r) for s in range(2) for r in range(R)]))
-    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
-    for x, y in zip(out[0][2], out[1][2]):
-        assert np.array_equal(x, y)
+    for o in out[1:]:
+        assert np.array_equal(out[0][0], o[0]) and np.array_equal(out[0][1], o[1])
+        for x, y in zip(out[0][2], o[2]):
+            assert np.array_equal(x, y)
 
 
 def test_words_per_lane_keep_results(gpu, oracle):
@@ -300,7 +303,7 @@ def test_autotune_keeps_results(gpu):
     a.step(5)
     ref = [a.get_spins(2, r) for r in range(R)]
     best = a.autotune()
-    assert best[0] in (128, 256, 512) and best[2] in (1, 2)
+    assert best[0] in (128, 256, 512) and best[2] in (1, 2, 3)
     for r in range(R):
         assert np.array_equal(a.get_spins(2, r), ref[r])
     assert a.sweep_counter() == 5

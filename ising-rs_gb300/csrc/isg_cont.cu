@@ -22,6 +22,7 @@
 // no trigonometry per neighbour.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include <algorithm>
 #include <cmath>
@@ -1052,6 +1053,7 @@ struct isg_cont {
     long long* d_partials = nullptr;
     double* d_obs = nullptr;
     int64_t ring_cap = 0;
+    unsigned char* h_stage = nullptr;  // pinned staging of drained records
     int32_t* d_rec_t = nullptr;
     double* d_rec_e = nullptr;
     double* d_rec_m = nullptr;
@@ -1187,26 +1189,56 @@ static int cont_check(const char* what) {
     return ISG_OK;
 }
 
+// Records leave the device ring through a pinned staging buffer of at most
+// 4 MiB: each batch's copies (at most two ring chunks per array) are queued
+// on the stream behind the sweeps that made them, the host waits once, then
+// copies the rows into the caller's arrays.
 static int cont_drain(isg_cont* H, int32_t* t, double* e, double* m, double* hb, int64_t row0) {
-    ISG_CK(cudaStreamSynchronize(H->stream));
     const int RT = H->RT;
     uint64_t n = H->records_made - H->records_done;
+    if (n == 0) {
+        ISG_CK(cudaStreamSynchronize(H->stream));
+        return ISG_OK;
+    }
+    constexpr size_t kRowBytes = 4 + 8 + 3 * 8 + 6 * 8;  // per replica: slot, E, M[3], bonds[6]
+    const uint64_t srows =
+        std::max<uint64_t>(1, std::min<uint64_t>(256, ((size_t)4 << 20) / (kRowBytes * RT)));
+    const size_t sn = (size_t)srows * RT;
+    if (!H->h_stage) ISG_CK(cudaMallocHost((void**)&H->h_stage, sn * kRowBytes));
+    double* st_e = reinterpret_cast<double*>(H->h_stage);
+    double* st_m = st_e + sn;
+    double* st_h = st_m + 3 * sn;
+    int32_t* st_t = reinterpret_cast<int32_t*>(st_h + 6 * sn);
     int64_t row = row0;
     while (n > 0) {
-        const uint64_t slot = H->records_done % (uint64_t)H->ring_cap;
-        const uint64_t chunk = std::min<uint64_t>(n, (uint64_t)H->ring_cap - slot);
-        const size_t cnt = (size_t)chunk * RT, off = (size_t)slot * RT;
-        ISG_CK(cudaMemcpy(t + (size_t)row * RT, H->d_rec_t + off, cnt * sizeof(int32_t),
-                          cudaMemcpyDeviceToHost));
-        ISG_CK(cudaMemcpy(e + (size_t)row * RT, H->d_rec_e + off, cnt * sizeof(double),
-                          cudaMemcpyDeviceToHost));
-        ISG_CK(cudaMemcpy(m + (size_t)row * RT * 3, H->d_rec_m + off * 3, cnt * 3 * sizeof(double),
-                          cudaMemcpyDeviceToHost));
-        ISG_CK(cudaMemcpy(hb + (size_t)row * RT * 6, H->d_rec_h + off * 6,
-                          cnt * 6 * sizeof(double), cudaMemcpyDeviceToHost));
-        H->records_done += chunk;
-        row += (int64_t)chunk;
-        n -= chunk;
+        const uint64_t batch = std::min<uint64_t>(n, srows);
+        uint64_t done = H->records_done, left = batch;
+        size_t srow = 0;
+        while (left > 0) {
+            const uint64_t slot = done % (uint64_t)H->ring_cap;
+            const uint64_t chunk = std::min<uint64_t>(left, (uint64_t)H->ring_cap - slot);
+            const size_t cnt = (size_t)chunk * RT, off = (size_t)slot * RT, so = srow * RT;
+            ISG_CK(cudaMemcpyAsync(st_t + so, H->d_rec_t + off, cnt * sizeof(int32_t),
+                                   cudaMemcpyDeviceToHost, H->stream));
+            ISG_CK(cudaMemcpyAsync(st_e + so, H->d_rec_e + off, cnt * sizeof(double),
+                                   cudaMemcpyDeviceToHost, H->stream));
+            ISG_CK(cudaMemcpyAsync(st_m + so * 3, H->d_rec_m + off * 3, cnt * 3 * sizeof(double),
+                                   cudaMemcpyDeviceToHost, H->stream));
+            ISG_CK(cudaMemcpyAsync(st_h + so * 6, H->d_rec_h + off * 6, cnt * 6 * sizeof(double),
+                                   cudaMemcpyDeviceToHost, H->stream));
+            srow += chunk;
+            done += chunk;
+            left -= chunk;
+        }
+        ISG_CK(cudaStreamSynchronize(H->stream));
+        const size_t cnt = (size_t)batch * RT;
+        memcpy(t + (size_t)row * RT, st_t, cnt * sizeof(int32_t));
+        memcpy(e + (size_t)row * RT, st_e, cnt * sizeof(double));
+        memcpy(m + (size_t)row * RT * 3, st_m, cnt * 3 * sizeof(double));
+        memcpy(hb + (size_t)row * RT * 6, st_h, cnt * 6 * sizeof(double));
+        H->records_done += batch;
+        row += (int64_t)batch;
+        n -= batch;
     }
     return ISG_OK;
 }
@@ -1395,6 +1427,7 @@ int isg_cont_destroy(isg_cont* H) {
     cudaFree(H->d_partials);
     cudaFree(H->d_obs);
     cudaFree(H->d_rec_t);
+    if (H->h_stage) cudaFreeHost(H->h_stage);
     cudaFree(H->d_rec_e);
     cudaFree(H->d_rec_m);
     cudaFree(H->d_rec_h);

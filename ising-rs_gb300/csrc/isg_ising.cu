@@ -1824,6 +1824,7 @@ struct isg_ising {
     unsigned long long* d_acc = nullptr;
     unsigned long long* d_ctrl = nullptr;
     int64_t ring_cap = 0;
+    unsigned char* h_stage = nullptr;  // pinned staging of drained records (kStageRows rows)
     int32_t* d_rec_t = nullptr;
     long long* d_rec_b = nullptr;
     long long* d_rec_m = nullptr;
@@ -2061,26 +2062,53 @@ static int build_graph(isg_ising* H, int ee, int me, int period) {
     return ISG_OK;
 }
 
+// Records leave the device ring through a pinned staging buffer: the copies
+// of up to kStageRows rows (at most two ring chunks per array) are queued on
+// the stream behind the sweeps that made them, the host waits once, then
+// copies the rows into the caller's arrays.  (Direct copies into pageable
+// caller memory cost one synchronous transfer per array and chunk.)
+constexpr int64_t kStageRows = 256;
+
 static int drain_records(isg_ising* H, int32_t* tslot, int64_t* bond, int64_t* mag,
                          int64_t row0) {
-    ISG_CK(cudaStreamSynchronize(H->stream));
     const int RT = H->replicas_total;
     uint64_t n = H->records_made - H->records_done;
+    if (n == 0) {
+        ISG_CK(cudaStreamSynchronize(H->stream));
+        return ISG_OK;
+    }
+    const size_t srows = (size_t)kStageRows * RT;
+    if (!H->h_stage) ISG_CK(cudaMallocHost((void**)&H->h_stage, srows * 20));
+    int64_t* st_b = reinterpret_cast<int64_t*>(H->h_stage);
+    int64_t* st_m = st_b + srows;
+    int32_t* st_t = reinterpret_cast<int32_t*>(st_m + srows);
     int64_t row = row0;
     while (n > 0) {
-        uint64_t slot = H->records_done % (uint64_t)H->ring_cap;
-        uint64_t chunk = std::min<uint64_t>(n, (uint64_t)H->ring_cap - slot);
-        size_t cnt = (size_t)chunk * RT;
-        size_t off = (size_t)slot * RT;
-        ISG_CK(cudaMemcpy(tslot + (size_t)row * RT, H->d_rec_t + off, cnt * sizeof(int32_t),
-                          cudaMemcpyDeviceToHost));
-        ISG_CK(cudaMemcpy(bond + (size_t)row * RT, H->d_rec_b + off, cnt * sizeof(int64_t),
-                          cudaMemcpyDeviceToHost));
-        ISG_CK(cudaMemcpy(mag + (size_t)row * RT, H->d_rec_m + off, cnt * sizeof(int64_t),
-                          cudaMemcpyDeviceToHost));
-        H->records_done += chunk;
-        row += (int64_t)chunk;
-        n -= chunk;
+        const uint64_t batch = std::min<uint64_t>(n, (uint64_t)kStageRows);
+        uint64_t done = H->records_done, left = batch;
+        size_t srow = 0;
+        while (left > 0) {
+            const uint64_t slot = done % (uint64_t)H->ring_cap;
+            const uint64_t chunk = std::min<uint64_t>(left, (uint64_t)H->ring_cap - slot);
+            const size_t cnt = (size_t)chunk * RT, off = (size_t)slot * RT, so = srow * RT;
+            ISG_CK(cudaMemcpyAsync(st_t + so, H->d_rec_t + off, cnt * sizeof(int32_t),
+                                   cudaMemcpyDeviceToHost, H->stream));
+            ISG_CK(cudaMemcpyAsync(st_b + so, H->d_rec_b + off, cnt * sizeof(int64_t),
+                                   cudaMemcpyDeviceToHost, H->stream));
+            ISG_CK(cudaMemcpyAsync(st_m + so, H->d_rec_m + off, cnt * sizeof(int64_t),
+                                   cudaMemcpyDeviceToHost, H->stream));
+            srow += chunk;
+            done += chunk;
+            left -= chunk;
+        }
+        ISG_CK(cudaStreamSynchronize(H->stream));
+        const size_t cnt = (size_t)batch * RT;
+        memcpy(tslot + (size_t)row * RT, st_t, cnt * sizeof(int32_t));
+        memcpy(bond + (size_t)row * RT, st_b, cnt * sizeof(int64_t));
+        memcpy(mag + (size_t)row * RT, st_m, cnt * sizeof(int64_t));
+        H->records_done += batch;
+        row += (int64_t)batch;
+        n -= batch;
     }
     return ISG_OK;
 }
@@ -2292,6 +2320,7 @@ int isg_ising_destroy(isg_ising* H) {
     cudaFree(H->d_ctrl);
     cudaFree(H->d_rec_t);
     cudaFree(H->d_rec_b);
+    if (H->h_stage) cudaFreeHost(H->h_stage);
     cudaFree(H->d_rec_m);
     cudaFree(H->d_sched_tab);
     cudaFree(H->d_sched);

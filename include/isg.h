@@ -215,7 +215,7 @@ int isg_ising_get_sweep(isg_ising* h, uint64_t* sweep);
 int isg_ising_sync(isg_ising* h);
 
 /* Launch shape of the half-sweep kernel: blocks per SM (0 = occupancy
- * maximum).  Every size, one-site tasks included, runs in the one 256-thread
+ * maximum).  Every size, site-block tasks included, runs in the one 256-thread
  * half-sweep kernel, so `threads` (64, 128, 256 or 512) is validated and
  * kept but no longer changes the launch.  Results never depend on either. */
 int isg_ising_set_launch(isg_ising* h, int threads, int blocks_per_sm);

@@ -17,13 +17,14 @@
 //
 // Half-sweep kernel (one launch covers every size and replica):
 //  * rolling tasks — 3D L = 32..256, a power of two: a warp walks z down a
-//    column of 128 words (4 sites each), four adjacent words per lane; byte-
-//    parallel Metropolis decisions against thresholds held as bytes.
+//    column of 128 words (4 sites each), four adjacent words per lane fed
+//    through a per-warp cp.async ring in shared memory; byte-parallel
+//    Metropolis decisions against thresholds held as bytes.
 //  * flat tasks — 3D L = 8, 16 and 2D: one word per lane, 32 per warp task;
 //    the x-neighbour word shifted by one byte comes from the row's other
 //    lanes through __shfl_sync + funnel shift.
-//  * site tasks — any other even L: one site per thread, strided over the
-//    whole launch.
+//  * site-block tasks — any other even L: the 16 sites of one Philox block
+//    per thread, strided over the whole launch.
 // All produce identical bits for the same state (the random stream is
 // defined per site, not per thread).
 #include <cuda_runtime.h>
@@ -65,8 +66,8 @@ constexpr int kMaxReplicas = 1024;
 //     words of the other colour in registers.
 //   kFlat    (other power-of-two L with L/8 dividing 32): 32 consecutive words,
 //     one per lane.
-//   kSite    (any other even L): one thread per site (site tasks of the same
-//     launch).
+//   kSite    (any other even L): one thread per Philox block of 16 sites
+//     (site-block tasks of the same launch).
 enum { kSite = 0, kFlat = 1, kRolling = 2 };
 
 struct IsingClass {
@@ -93,6 +94,13 @@ struct IsingClass {
     int plane_fast;
     int64_t site_base;        // site kind: first site (over colour planes)
     int64_t site_end;
+    // site kind, site-block tasks (site_block): S = sites of a colour per slab,
+    // s_nv = v range ((L + 3) / 4 quads of S), s_nb = blocks per colour plane
+    uint32_t s_nv, s_nb;
+    FastDiv div_slab, div_nb;
+    int sblk_fast;            // R * s_nb < 2^31: replica by multiply-high
+    int64_t sblk_base;        // first site block of the class over all classes
+    int64_t sblk_end;
 };
 
 struct IsingParams {
@@ -109,6 +117,7 @@ struct IsingParams {
     int64_t total_ctasks;     // rolling work units (contiguous ranges per block)
     int64_t flat_ctasks;      // flat CTA tasks (round-robin over blocks)
     int64_t total_sites;
+    int64_t total_sblocks;    // site-block tasks of all site kinds
     int l2_ahead;             // rolling: planes ahead of z prefetched (0: off)
     int pf_level;             // 1: into L1, 2: into L2
     uint32_t rk0[10], rk1[10];      // Philox round keys (constant-bank operands)
@@ -714,78 +723,97 @@ __device__ __forceinline__ void ring_quad_step(
     o = (o + pz) & pwm;
 }
 
-// One site of a one-site task (any even L), split in two so that a thread
-// can issue the loads of several sites before it decides any: site_gather
-// reads the site's down bit, its down-neighbour count and the other colour's
-// byte at the same index (for the magnetisation), and locates its coarse
-// random (block, Philox word, byte); site_decide draws the blocks and flips.
-// The rule is the word kernels' per-site definition (coarse 7 bits of byte
-// v & 3 of word t & 3 of block v >> 2, fine 25 bits on a tie).
-struct SiteWork {
-    uint8_t* own;
-    const uint32_t* tab;
-    uint32_t i, uid, blk, sel;  // sel: byte v & 3 | (word t & 3) << 2
-    int d, nd, oth_i, rg;
-};
-
-template <int DIM>
-__device__ __forceinline__ void site_gather(SiteWork& w, uint8_t* own, const uint8_t* oth,
-                                            uint32_t i, uint32_t L, const FastDiv& dh,
-                                            const FastDiv& dL, uint32_t colour) {
-    const uint32_t half = L >> 1;
-    const uint32_t row = fdiv(i, dh);
-    const uint32_t k = i - row * half;
-    uint32_t y, z, p;
-    if (DIM == 3) {
-        z = fdiv(row, dL);
-        y = row - z * L;
-        p = (y + z + colour) & 1u;
-    } else {
-        y = row;
-        z = 0;
-        p = (y + colour) & 1u;
+// Site-block tasks (any even L that is not a word size): a thread takes the
+// 16 sites that share one Philox block, draws the block once and decides
+// them.  The rule is the word kernels' per-site definition: with S the sites
+// of a colour per slab (z-plane in 3D, row in 2D), t the slab and p the
+// position in it, v = (t >> 2) S + p, the coarse random of the site is the
+// low 7 bits of byte v & 3 of word t & 3 of block v >> 2, and a tie (coarse
+// random equal to the threshold's top 7 bits) is decided by the top 25 bits
+// of word i & 3 of the fine block 0x80000000 | (i >> 2), i = t S + p.  So
+// block b holds the sites v = 4b .. 4b + 3 at the (up to) four slabs
+// t = 4 (v / S) + w, w = 0..3.  Neighbours are read as bytes of the other
+// colour at index z S + y L/2 + (x >> 1).
+template <int DIM, int MODE>
+__device__ __forceinline__ void site_block(const IsingParams& P, const IsingClass& C, int r,
+                                           uint32_t b, int colour, uint32_t c2, uint32_t c3,
+                                           uint32_t k0, uint32_t k1) {
+    const uint32_t L = (uint32_t)C.L, half = L >> 1;
+    const uint32_t S = DIM == 3 ? half * L : half;
+    uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
+    uint8_t* own = base + (int64_t)colour * C.plane_sites;
+    const uint8_t* oth = base + (int64_t)(colour ^ 1) * C.plane_sites;
+    const int rg = C.rep_base + r;
+    const uint32_t uid = replica_uid(C.L, r);
+    const uint32_t* tab = P.thr + (int64_t)(C.rep_base + (MODE != 2 ? P.r2t[rg] : 0)) * 16;
+    U4 u{0u, 0u, 0u, 0u};
+    if (MODE != 2) u = philox10(uid, b, c2, c3, k0, k1);
+    const uint32_t W[4] = {u.x, u.y, u.z, u.w};
+    int sb = 0, sm = 0;  // measurement sums of the block's sites
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t v = 4 * b + (uint32_t)j;
+        if (v >= C.s_nv) break;
+        const uint32_t q = fdiv(v, C.div_slab);
+        const uint32_t pp = v - q * S;
+        uint32_t y0 = 0, k = pp;
+        if (DIM == 3) {
+            y0 = fdiv(pp, C.div_half);
+            k = pp - y0 * half;
+        }
+        // gather the (up to) four slabs' sites before deciding any
+        uint32_t idx[4];
+        int d[4], nd[4], oi[4];
+        bool live[4];
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            const uint32_t t = 4 * q + (uint32_t)w;
+            live[w] = t < L;
+            if (!live[w]) continue;
+            const uint32_t z = DIM == 3 ? t : 0u, y = DIM == 3 ? y0 : t;
+            const uint32_t x = 2 * k + ((y + z + (uint32_t)colour) & 1u);
+            const uint32_t xp = x + 1 == L ? 0 : x + 1, xm = x == 0 ? L - 1 : x - 1;
+            const uint32_t yp = y + 1 == L ? 0 : y + 1, ym = y == 0 ? L - 1 : y - 1;
+            const uint32_t zs = z * S, row = zs + y * half;
+            int n = (int)__ldg(oth + row + (xp >> 1)) + (int)__ldg(oth + row + (xm >> 1)) +
+                    (int)__ldg(oth + zs + yp * half + k) + (int)__ldg(oth + zs + ym * half + k);
+            if (DIM == 3) {
+                const uint32_t zp = z + 1 == L ? 0 : z + 1, zm = z == 0 ? L - 1 : z - 1;
+                n += (int)__ldg(oth + zp * S + y * half + k) + (int)__ldg(oth + zm * S + y * half + k);
+            }
+            idx[w] = row + k;
+            nd[w] = n;
+            d[w] = own[row + k];
+            oi[w] = MODE != 0 ? (int)__ldg(oth + row + k) : 0;
+        }
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            if (!live[w]) continue;
+            if (MODE != 2) {
+                const uint32_t th = tab[d[w] * 8 + nd[w]];
+                const uint32_t c7 = (W[w] >> (8 * j)) & 0x7Fu;
+                bool acc = c7 < (th >> 25);
+                if (c7 == (th >> 25)) {
+                    const U4 f = philox10(uid, 0x80000000u | (idx[w] >> 2), c2, c3, k0, k1);
+                    const uint32_t ji = idx[w] & 3u;
+                    const uint32_t fw = ji == 0 ? f.x : ji == 1 ? f.y : ji == 2 ? f.z : f.w;
+                    acc = ((c7 << 25) | (fw >> 7)) <= th;
+                }
+                if (acc) {
+                    d[w] ^= 1;
+                    own[idx[w]] = (uint8_t)d[w];
+                }
+            }
+            if (MODE != 0) {
+                const int sp = 1 - 2 * d[w];
+                sb += sp * (2 * DIM - 2 * nd[w]);
+                sm += sp + 1 - 2 * oi[w];
+            }
+        }
     }
-    const uint32_t x = 2 * k + p;
-    const uint32_t xp = x + 1 == L ? 0 : x + 1, xm = x == 0 ? L - 1 : x - 1;
-    const uint32_t yp = y + 1 == L ? 0 : y + 1, ym = y == 0 ? L - 1 : y - 1;
-    const uint32_t rowL = (z * L + y) * L;
-    int nd = (int)__ldg(oth + ((rowL + xp) >> 1)) + (int)__ldg(oth + ((rowL + xm) >> 1)) +
-             (int)__ldg(oth + (((z * L + yp) * L + x) >> 1)) +
-             (int)__ldg(oth + (((z * L + ym) * L + x) >> 1));
-    if (DIM == 3) {
-        const uint32_t zp = z + 1 == L ? 0 : z + 1, zm = z == 0 ? L - 1 : z - 1;
-        nd += (int)__ldg(oth + (((zp * L + y) * L + x) >> 1)) +
-              (int)__ldg(oth + (((zm * L + y) * L + x) >> 1));
-    }
-    w.own = own;
-    w.i = i;
-    w.nd = nd;
-    w.d = own[i];
-    w.oth_i = (int)__ldg(oth + i);
-    const uint32_t S = DIM == 3 ? half * L : half;  // sites of the colour per slab
-    const uint32_t t = DIM == 3 ? z : y;
-    const uint32_t v = (t >> 2) * S + (i - t * S);
-    w.blk = v >> 2;
-    w.sel = (v & 3u) | ((t & 3u) << 2);
-}
-
-__device__ __forceinline__ void site_decide(SiteWork& w, uint32_t c2, uint32_t c3, uint32_t k0,
-                                            uint32_t k1) {
-    const uint32_t th = w.tab[w.d * 8 + w.nd];
-    const U4 u = philox10(w.uid, w.blk, c2, c3, k0, k1);
-    const uint32_t tw = w.sel >> 2;
-    const uint32_t uw = tw == 0 ? u.x : tw == 1 ? u.y : tw == 2 ? u.z : u.w;
-    const uint32_t c7 = (uw >> (8u * (w.sel & 3u))) & 0x7Fu;
-    bool acc = c7 < (th >> 25);
-    if (c7 == (th >> 25)) {
-        const U4 f = philox10(w.uid, 0x80000000u | (w.i >> 2), c2, c3, k0, k1);
-        const uint32_t ji = w.i & 3u;
-        const uint32_t fw = ji == 0 ? f.x : ji == 1 ? f.y : ji == 2 ? f.z : f.w;
-        acc = ((c7 << 25) | (fw >> 7)) <= th;
-    }
-    if (acc) {
-        w.d ^= 1;
-        w.own[w.i] = (uint8_t)w.d;
+    if (MODE != 0) {
+        atomicAdd(&P.acc[2 * rg], (unsigned long long)(long long)sb);
+        atomicAdd(&P.acc[2 * rg + 1], (unsigned long long)(long long)sm);
     }
 }
 
@@ -1125,50 +1153,20 @@ __global__ void __launch_bounds__(256, MINB)
     }
     if (MODE != 0 && cur_rep >= 0) meas_flush(P.acc, cur_rep, macc, Z, lane);
 
-    // site tasks (even L that are not word sizes): one site per thread,
-    // strided over every thread of the launch, by the per-site rule of
-    // site_gather / site_decide (the same bits as the word paths and the oracle)
-    if (P.total_sites > 0) {
+    // site-block tasks (even L that are not word sizes): one Philox block's
+    // 16 sites per thread, strided over every thread of the launch
+    if (P.total_sblocks > 0) {
         const uint32_t k0 = (uint32_t)P.seed, k1 = (uint32_t)(P.seed >> 32);
         const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-        // four independent sites per iteration: all their loads are issued
-        // before any decision (one site at a time waits on each load chain)
-        for (int64_t g0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g0 < P.total_sites;
-             g0 += 4 * stride) {
-            SiteWork sw[4];
-            bool live[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int64_t g = g0 + u * stride;
-                live[u] = g < P.total_sites;
-                if (!live[u]) continue;
-                int sc = 0;
-                while (P.cls[sc].site_end <= g) ++sc;
-                const IsingClass& C = P.cls[sc];
-                const int64_t lg = g - C.site_base;
-                const int r = C.plane_fast ? (int)fdiv((uint32_t)lg, C.div_plane)
-                                           : (int)(lg / C.plane_sites);
-                const uint32_t i = (uint32_t)(lg - (int64_t)r * C.plane_sites);
-                uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
-                site_gather<DIM>(sw[u], base + (int64_t)colour * C.plane_sites,
-                                 base + (int64_t)(colour ^ 1) * C.plane_sites, i, (uint32_t)C.L,
-                                 C.div_half, C.div_L, (uint32_t)colour);
-                sw[u].rg = C.rep_base + r;
-                sw[u].uid = replica_uid(C.L, r);
-                sw[u].tab = P.thr + (int64_t)(C.rep_base + (MODE != 2 ? P.r2t[sw[u].rg] : 0)) * 16;
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (!live[u]) continue;
-                if (MODE != 2) site_decide(sw[u], c2, c3, k0, k1);
-                if (MODE != 0) {
-                    const int sp = 1 - 2 * sw[u].d;
-                    const long long bnd = (long long)(sp * (2 * DIM - 2 * sw[u].nd));
-                    const long long m = (long long)(sp + 1 - 2 * sw[u].oth_i);
-                    atomicAdd(&P.acc[2 * sw[u].rg], (unsigned long long)bnd);
-                    atomicAdd(&P.acc[2 * sw[u].rg + 1], (unsigned long long)m);
-                }
-            }
+        for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < P.total_sblocks;
+             g += stride) {
+            int sc = 0;
+            while (P.cls[sc].sblk_end <= g) ++sc;
+            const IsingClass& C = P.cls[sc];
+            const int64_t lg = g - C.sblk_base;
+            const int r = C.sblk_fast ? (int)fdiv((uint32_t)lg, C.div_nb) : (int)(lg / C.s_nb);
+            const uint32_t b = (uint32_t)(lg - (int64_t)r * C.s_nb);
+            site_block<DIM, MODE>(P, C, r, b, colour, c2, c3, k0, k1);
         }
     }
 }
@@ -1180,8 +1178,8 @@ __global__ void __launch_bounds__(256, MINB)
 // distributed shared memory (mapa + ld.shared::cluster), and hardware cluster
 // barriers (release / acquire at cluster scope) separate the half-sweeps.
 // Spins are loaded from HBM at the start and written back at the end.  Same
-// per-site update rule and random stream as the site tasks (site_decide), so
-// any launch shape gives the same bits.
+// per-site update rule and random stream as the site-block tasks
+// (site_block), so any launch shape gives the same bits.
 constexpr int kResidentThreads = 1024;
 
 struct ResidentParams {
@@ -1953,7 +1951,7 @@ static int configure_launch(isg_ising* H) {
     // one launch per half-sweep covers every size: rolling ranges, flat
     // tasks and one-site tasks (256 per block)
     const int64_t need = std::max<int64_t>(std::max<int64_t>(H->P.total_ctasks, H->P.flat_ctasks),
-                                           (H->P.total_sites + 255) / 256);
+                                           (H->P.total_sblocks + 255) / 256);
     const bool in_l2 = H->spin_bytes <= ((int64_t)96 << 20);
     // two words per lane: loads two planes ahead help L2-resident batches;
     // four words per lane (2 blocks per SM either way): one plane ahead
@@ -2158,7 +2156,7 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
     H->sizes.assign(sizes, sizes + n_sizes);
 
     IsingParams& P = H->P;
-    int64_t off = 0, task = 0, site = 0, ctask = 0, fctask = 0;
+    int64_t off = 0, task = 0, site = 0, sblk = 0, ctask = 0, fctask = 0;
     for (int s = 0; s < n_sizes; ++s) {
         IsingClass& C = P.cls[s];
         const int L = sizes[s];
@@ -2203,6 +2201,17 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         C.site_base = site;
         if (C.kind == kSite) site += (int64_t)C.plane_sites * replicas;
         C.site_end = site;
+        {
+            const uint32_t S = dim == 3 ? (uint32_t)(L / 2) * (uint32_t)L : (uint32_t)(L / 2);
+            C.s_nv = (uint32_t)((L + 3) / 4) * S;
+            C.s_nb = (C.s_nv + 3) / 4;
+            C.div_slab = make_div(S);
+            C.div_nb = make_div(C.s_nb);
+            C.sblk_fast = (int64_t)C.s_nb * replicas < ((int64_t)1 << 31) ? 1 : 0;
+            C.sblk_base = sblk;
+            if (C.kind == kSite) sblk += (int64_t)C.s_nb * replicas;
+            C.sblk_end = sblk;
+        }
     }
     // sentinel classes so the device class search always terminates
     for (int s = n_sizes; s < kMaxClasses; ++s) {
@@ -2211,6 +2220,7 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         P.cls[s].ctask_base = P.cls[s].ctask_end = INT64_MAX;
         P.cls[s].kind = -1;
         P.cls[s].site_base = P.cls[s].site_end = INT64_MAX;
+        P.cls[s].sblk_base = P.cls[s].sblk_end = INT64_MAX;
     }
     P.n_classes = n_sizes;
     P.dim = dim;
@@ -2219,6 +2229,7 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
     (void)ctask;
     layout_rolling(H);
     P.total_sites = site;
+    P.total_sblocks = sblk;
     P.seed = seed;
     for (int r = 0; r < 10; ++r) {
         P.rk0[r] = (uint32_t)seed + (uint32_t)r * kPhiloxW0;

@@ -155,6 +155,35 @@ def test_pt_run_bit_exact(gpu, oracle, ee, me):
     assert np.all(acc > 0)
 
 
+def test_site_block_pt_matches_oracle(gpu, oracle):
+    """Sizes that are not word sizes run as site-block tasks (one Philox block's
+    16 sites per thread), here in the graph cycle (the lattices are above the
+    resident kernel's limit or it is switched off): records with the fused
+    E/M sums, exchanges and final spins equal the oracle's PT replay."""
+    sizes, R, dim, seed = [12, 24, 48], 2, 3, 31
+    temps = grid(4.4, 4.6, R)
+    b = gpu.IsingBatch(sizes, R, seed=seed, dim=dim)
+    b.set_resident_pt(False)
+    b.set_temperatures(temps)
+    b.step(3)
+    b.reset_sampling()
+    rt, rb, rm = b.pt_run(20, 5, 2)
+    r2t = b.r2t()
+    for s, L in enumerate(sizes):
+        pt = oracle.IsingPT(L, dim, R, temps, seed)
+        pt.warmup(3)
+        pt.reset_sampling()
+        ot, ob, om = pt.sample(20, 5, 2)
+        sl = slice(s * R, (s + 1) * R)
+        assert np.array_equal(rt[:, sl], ot), L
+        assert np.array_equal(rb[:, sl], ob), L
+        assert np.array_equal(rm[:, sl], om), L
+        assert np.array_equal(r2t[sl], pt.r2t), L
+        for r in range(R):
+            assert np.array_equal(b.get_spins(s, r), pt.replica_spins(r)), (L, r)
+    b.close()
+
+
 def test_exchange_api_matches_oracle(gpu, oracle):
     sizes, R, seed = [8, 16], 6, 7
     temps = grid(4.0, 5.0, R)

@@ -20,9 +20,10 @@
 //    column of 128 words (4 sites each), four adjacent words per lane fed
 //    through a per-warp cp.async ring in shared memory; byte-parallel
 //    Metropolis decisions against thresholds held as bytes.
-//  * flat tasks — 3D L = 8, 16 and 2D: one word per lane, 32 per warp task;
-//    the x-neighbour word shifted by one byte comes from the row's other
-//    lanes through __shfl_sync + funnel shift.
+//  * flat tasks — 3D L = 8, 16, other multiples of 8 (24, 48, 96, ...) and
+//    2D: one word per lane, 32 per warp task; the x-neighbour word shifted by
+//    one byte comes from the row's other lanes through __shfl_sync (or a
+//    load, for rows that are not a power of two words) + funnel shift.
 //  * site-block tasks — any other even L: the 16 sites of one Philox block
 //    per thread, strided over the whole launch.
 // All produce identical bits for the same state (the random stream is
@@ -64,8 +65,11 @@ constexpr int kMaxReplicas = 1024;
 //     one z, 4 adjacent words per lane (128 words; 2 and 64 if so set);
 //     consecutive tasks of a size walk z, so a warp keeps the z-1, z, z+1
 //     words of the other colour in registers.
-//   kFlat    (other power-of-two L with L/8 dividing 32): 32 consecutive words,
-//     one per lane.
+//   kFlat    (other power-of-two L with L/8 dividing 32, and any other L that
+//     is a multiple of 8 with whole 32-word tasks per plane, e.g. 3D L = 24,
+//     48, 96, 512): 32 consecutive words, one per lane; the x-neighbour word
+//     comes by shuffle from the row's lanes, or (rows that are not a power of
+//     two words long) by a load.
 //   kSite    (any other even L): one thread per Philox block of 16 sites
 //     (site-block tasks of the same launch).
 enum { kSite = 0, kFlat = 1, kRolling = 2 };
@@ -99,6 +103,15 @@ struct IsingClass {
     uint32_t s_nv, s_nb;
     FastDiv div_slab, div_nb;
     int sblk_fast;            // R * s_nb < 2^31: replica by multiply-high
+    // flat kind with word rows that are not a power of two (L % 8 == 0):
+    // indices by multiply-high, the x-neighbour word loaded, not shuffled
+    int flat_gen;
+    FastDiv div_rw;
+    // flat kinds: a warp takes a group of up to FG consecutive tasks of a plane
+    // (FG: the kernel's group size, layout_flat)
+    uint32_t gpp;             // groups per plane: ceil(tasks_per_plane / 4)
+    int gpp_fast;             // R * gpp < 2^31: replica by multiply-high
+    FastDiv div_gpp;
     int64_t sblk_base;        // first site block of the class over all classes
     int64_t sblk_end;
 };
@@ -833,7 +846,7 @@ __device__ __forceinline__ void site_block(const IsingParams& P, const IsingClas
 // WMAX: 4 if some size runs four words per lane (that path needs more
 // registers: 2 blocks per SM), else 2.  MINB: blocks per SM the registers
 // are budgeted for.
-template <int DIM, int MODE, int PF, int WMAX, int MINB>
+template <int DIM, int MODE, int PF, int WMAX, int MINB, int FG>
 __global__ void __launch_bounds__(256, MINB)
     k_ising_words(const __grid_constant__ IsingParams P, int colour, int sweep_off) {
     __shared__ uint32_t s_thr[8][16];
@@ -921,11 +934,17 @@ __global__ void __launch_bounds__(256, MINB)
             ct += (int64_t)(z1 - z0) << C.log2_unit;
             if (r >= C.R) continue;  // the last replica group may be short
         } else {
-            // flat: warp task 8*lct + wib of this size
+            // flat: warp task (FG = 1) or group of up to FG tasks 8*lct + wib
+            // of this size
             wt = (lct << 3) + wib;
             ft += gridDim.x;
-            if (wt >= C.task_end - C.task_base) continue;
-            r = (int)(wt >> C.log2_tpp);
+            if constexpr (FG == 1) {
+                if (wt >= C.task_end - C.task_base) continue;
+                r = (int)(wt >> C.log2_tpp);
+            } else {
+                if (wt >= (int64_t)C.gpp * C.R) continue;
+                r = C.gpp_fast ? (int)fdiv((uint32_t)wt, C.div_gpp) : (int)(wt / (int64_t)C.gpp);
+            }
         }
         const int rg = C.rep_base + r;
         uint8_t* base = P.spins + C.spin_off + (int64_t)r * 2 * C.plane_sites;
@@ -1098,51 +1117,146 @@ __global__ void __launch_bounds__(256, MINB)
                 }
             }
         } else {
-            const uint32_t tl = (uint32_t)(wt & (int64_t)(C.tasks_per_plane - 1));
-            const uint32_t w = (tl << 5) + (uint32_t)lane;
-            const uint32_t row = w >> lrw;
-            uint32_t y, z;
-            if (DIM == 3) {
-                y = row & Lm;
-                z = row >> C.log2L;
+            if constexpr (FG == 1) {
+                const uint32_t tl = (uint32_t)(wt & (int64_t)(C.tasks_per_plane - 1));
+                const uint32_t w = (tl << 5) + (uint32_t)lane;
+                const uint32_t row = w >> lrw;
+                uint32_t y, z;
+                if (DIM == 3) {
+                    y = row & Lm;
+                    z = row >> C.log2L;
+                } else {
+                    y = row;
+                    z = 0;
+                }
+                const uint32_t yp = (y + 1) & Lm, ym = (y - 1) & Lm;
+                uint32_t wa, wyp, wym, wzp = 0, wzm = 0;
+                if (DIM == 3) {
+                    const uint32_t zb = z << C.log2L;
+                    wa = __ldg(oth + (((zb + y) << lrw) + k4));
+                    wyp = __ldg(oth + (((zb + yp) << lrw) + k4));
+                    wym = __ldg(oth + (((zb + ym) << lrw) + k4));
+                    wzp = __ldg(oth + (((((z + 1) & Lm) << C.log2L) + y) << lrw) + k4);
+                    wzm = __ldg(oth + (((((z - 1) & Lm) << C.log2L) + y) << lrw) + k4);
+                } else {
+                    wa = __ldg(oth + ((y << lrw) + k4));
+                    wyp = __ldg(oth + ((yp << lrw) + k4));
+                    wym = __ldg(oth + ((ym << lrw) + k4));
+                }
+                const uint32_t p = (y + z + (uint32_t)colour) & 1u;
+                const uint32_t prev = __shfl_sync(ISG_FULL_MASK, wa, src_prev);
+                const uint32_t next = __shfl_sync(ISG_FULL_MASK, wa, src_next);
+                const uint32_t wx = p ? __funnelshift_r(wa, next, 8) : __funnelshift_l(prev, wa, 8);
+                uint32_t nd = wx + wa + wyp + wym;
+                if (DIM == 3) nd += wzp + wzm;
+                const uint32_t ow = own[w];
+                uint32_t nw = ow;
+                if (MODE != 2) {
+                    // z (3D) or y (2D) quad of this word: one Philox block, word t & 3
+                    const uint32_t t = DIM == 3 ? z : y;
+                    const uint32_t slab = DIM == 3 ? (L << lrw) : rw;
+                    const U4 u = philox_w(pre, P, w - (t - (t >> 2)) * slab);
+                    const uint32_t U = (t & 2u) ? ((t & 1u) ? u.w : u.z) : ((t & 1u) ? u.y : u.x);
+                    uint32_t d;
+                    nw = ow ^ coarse_flips(ow, nd, U, T8, d);
+                    if (any_tie(d)) nw ^= fine_flips(tie_bytes(d), nd + (ow << 3), tab, pre, P, w);
+                    own[w] = nw;
+                }
+                if (MODE != 0) meas_add(macc, nw, nd, wa);
             } else {
-                y = row;
-                z = 0;
+                // a flat group: up to (uint32_t)FG consecutive 32-word tasks of one plane,
+                // one word per lane each; all loads of the group are issued
+                // before any decision (one task at a time waits on each load)
+                const uint32_t grp = (uint32_t)(wt - (int64_t)r * C.gpp);
+                uint32_t fw[FG], fa[FG], fn[FG], fyp[FG], fym[FG], fzp[FG], fzm[FG], fo[FG], fy[FG], fz[FG];
+    #pragma unroll
+                for (int g = 0; g < FG; ++g) {
+                    const uint32_t tl = grp * (uint32_t)FG + (uint32_t)g;
+                    if (tl >= C.tasks_per_plane) break;  // warp-uniform
+                    const uint32_t w = (tl << 5) + (uint32_t)lane;
+                    uint32_t y, z;
+                    fzp[g] = fzm[g] = fn[g] = 0u;
+                    if (C.flat_gen) {
+                        // rows of rwg = L / 8 words, not a power of two: the
+                        // row's x-neighbour word (wrapping) is loaded
+                        const uint32_t rwg = L >> 3;
+                        const uint32_t row = fdiv(w, C.div_rw);
+                        const uint32_t kk = w - row * rwg;
+                        if (DIM == 3) {
+                            z = fdiv(row, C.div_L);
+                            y = row - z * L;
+                        } else {
+                            y = row;
+                            z = 0;
+                        }
+                        const uint32_t yp = y + 1 == L ? 0 : y + 1, ym = y == 0 ? L - 1 : y - 1;
+                        const uint32_t p = (y + z + (uint32_t)colour) & 1u;
+                        const uint32_t kx =
+                            p ? (kk + 1 == rwg ? 0 : kk + 1) : (kk == 0 ? rwg - 1 : kk - 1);
+                        const uint32_t zb = z * L;
+                        fa[g] = __ldg(oth + (zb + y) * rwg + kk);
+                        fn[g] = __ldg(oth + (zb + y) * rwg + kx);
+                        fyp[g] = __ldg(oth + (zb + yp) * rwg + kk);
+                        fym[g] = __ldg(oth + (zb + ym) * rwg + kk);
+                        if (DIM == 3) {
+                            const uint32_t zp = z + 1 == L ? 0 : z + 1, zm = z == 0 ? L - 1 : z - 1;
+                            fzp[g] = __ldg(oth + (zp * L + y) * rwg + kk);
+                            fzm[g] = __ldg(oth + (zm * L + y) * rwg + kk);
+                        }
+                    } else {
+                        const uint32_t row = w >> lrw;
+                        if (DIM == 3) {
+                            y = row & Lm;
+                            z = row >> C.log2L;
+                        } else {
+                            y = row;
+                            z = 0;
+                        }
+                        const uint32_t yp = (y + 1) & Lm, ym = (y - 1) & Lm;
+                        const uint32_t zb = DIM == 3 ? z << C.log2L : 0u;
+                        fa[g] = __ldg(oth + (((zb + y) << lrw) + k4));
+                        fyp[g] = __ldg(oth + (((zb + yp) << lrw) + k4));
+                        fym[g] = __ldg(oth + (((zb + ym) << lrw) + k4));
+                        if (DIM == 3) {
+                            fzp[g] = __ldg(oth + (((((z + 1) & Lm) << C.log2L) + y) << lrw) + k4);
+                            fzm[g] = __ldg(oth + (((((z - 1) & Lm) << C.log2L) + y) << lrw) + k4);
+                        }
+                    }
+                    fw[g] = w;
+                    fy[g] = y;
+                    fz[g] = z;
+                    fo[g] = own[w];
+                }
+    #pragma unroll
+                for (int g = 0; g < FG; ++g) {
+                    if (grp * (uint32_t)FG + (uint32_t)g >= C.tasks_per_plane) break;
+                    const uint32_t w = fw[g], wa = fa[g], y = fy[g], z = fz[g], ow = fo[g];
+                    const uint32_t p = (y + z + (uint32_t)colour) & 1u;
+                    uint32_t wx;
+                    if (C.flat_gen) {
+                        wx = p ? __funnelshift_r(wa, fn[g], 8) : __funnelshift_l(fn[g], wa, 8);
+                    } else {
+                        const uint32_t prev = __shfl_sync(ISG_FULL_MASK, wa, src_prev);
+                        const uint32_t next = __shfl_sync(ISG_FULL_MASK, wa, src_next);
+                        wx = p ? __funnelshift_r(wa, next, 8) : __funnelshift_l(prev, wa, 8);
+                    }
+                    uint32_t nd = wx + wa + fyp[g] + fym[g];
+                    if (DIM == 3) nd += fzp[g] + fzm[g];
+                    uint32_t nw = ow;
+                    if (MODE != 2) {
+                        // z (3D) or y (2D) quad of this word: one Philox block, word t & 3
+                        const uint32_t t = DIM == 3 ? z : y;
+                        const uint32_t slab = DIM == 3 ? L * (L >> 3) : L >> 3;  // words per slab
+                        const U4 u = philox_w(pre, P, w - (t - (t >> 2)) * slab);
+                        const uint32_t U = (t & 2u) ? ((t & 1u) ? u.w : u.z) : ((t & 1u) ? u.y : u.x);
+                        uint32_t d;
+                        nw = ow ^ coarse_flips(ow, nd, U, T8, d);
+                        if (any_tie(d)) nw ^= fine_flips(tie_bytes(d), nd + (ow << 3), tab, pre, P, w);
+                        own[w] = nw;
+                    }
+                    if (MODE != 0) meas_add(macc, nw, nd, wa);
+                }
             }
-            const uint32_t yp = (y + 1) & Lm, ym = (y - 1) & Lm;
-            uint32_t wa, wyp, wym, wzp = 0, wzm = 0;
-            if (DIM == 3) {
-                const uint32_t zb = z << C.log2L;
-                wa = __ldg(oth + (((zb + y) << lrw) + k4));
-                wyp = __ldg(oth + (((zb + yp) << lrw) + k4));
-                wym = __ldg(oth + (((zb + ym) << lrw) + k4));
-                wzp = __ldg(oth + (((((z + 1) & Lm) << C.log2L) + y) << lrw) + k4);
-                wzm = __ldg(oth + (((((z - 1) & Lm) << C.log2L) + y) << lrw) + k4);
-            } else {
-                wa = __ldg(oth + ((y << lrw) + k4));
-                wyp = __ldg(oth + ((yp << lrw) + k4));
-                wym = __ldg(oth + ((ym << lrw) + k4));
-            }
-            const uint32_t p = (y + z + (uint32_t)colour) & 1u;
-            const uint32_t prev = __shfl_sync(ISG_FULL_MASK, wa, src_prev);
-            const uint32_t next = __shfl_sync(ISG_FULL_MASK, wa, src_next);
-            const uint32_t wx = p ? __funnelshift_r(wa, next, 8) : __funnelshift_l(prev, wa, 8);
-            uint32_t nd = wx + wa + wyp + wym;
-            if (DIM == 3) nd += wzp + wzm;
-            const uint32_t ow = own[w];
-            uint32_t nw = ow;
-            if (MODE != 2) {
-                // z (3D) or y (2D) quad of this word: one Philox block, word t & 3
-                const uint32_t t = DIM == 3 ? z : y;
-                const uint32_t slab = DIM == 3 ? (L << lrw) : rw;
-                const U4 u = philox_w(pre, P, w - (t - (t >> 2)) * slab);
-                const uint32_t U = (t & 2u) ? ((t & 1u) ? u.w : u.z) : ((t & 1u) ? u.y : u.x);
-                uint32_t d;
-                nw = ow ^ coarse_flips(ow, nd, U, T8, d);
-                if (any_tie(d)) nw ^= fine_flips(tie_bytes(d), nd + (ow << 3), tab, pre, P, w);
-                own[w] = nw;
-            }
-            if (MODE != 0) meas_add(macc, nw, nd, wa);
         }
     }
     if (MODE != 2) {
@@ -1835,6 +1949,7 @@ struct isg_ising {
     int prefetch = 0;          // rolling prefetch depth as set (0: automatic)
     int wpl_max = 4;           // rolling words per lane for L >= 128 (2 or 4)
     int wmax = 2;              // word kernel variant: 4 if some size runs 4 words per lane
+    int flatg = 1;             // flat tasks per warp group (layout_flat)
     bool cache_pf_set = false; // cache prefetch set by the caller (else automatic)
     bool pdl = true;           // word kernels as programmatic dependent launches
     int pf = 1;                // depth in use
@@ -1907,29 +2022,64 @@ static void layout_rolling(isg_ising* H) {
     P.total_ctasks = ctask;
 }
 
-template <int DIM, int PF, int WMAX, int MINB>
+// CTA tasks of the flat sizes: groups of FG consecutive warp tasks of one
+// plane per warp, 8 groups per CTA task.  FG = 1 (the original one-task form)
+// unless some size has rows that are not a power of two words long (its
+// tasks read the x-neighbour word from memory, so several in flight per warp
+// hide the latency): then 4, or 2 next to four-words-per-lane rolling sizes
+// (the groups' registers would cost that kernel more).
+static void layout_flat(isg_ising* H) {
+    IsingParams& P = H->P;
+    bool gen = false;
+    for (int s = 0; s < H->n_classes; ++s) gen = gen || (P.cls[s].kind == kFlat && P.cls[s].flat_gen);
+    H->flatg = !gen ? 1 : H->wmax == 4 ? 2 : 4;
+    int64_t fctask = 0;
+    for (int s = 0; s < H->n_classes; ++s) {
+        IsingClass& C = P.cls[s];
+        if (C.kind != kFlat) continue;
+        C.gpp = (C.tasks_per_plane + (uint32_t)H->flatg - 1) / (uint32_t)H->flatg;
+        C.div_gpp = make_div(std::max<uint32_t>(1u, C.gpp));
+        C.gpp_fast = (int64_t)C.gpp * C.R < ((int64_t)1 << 31) ? 1 : 0;
+        C.ctask_base = fctask;
+        fctask += ((int64_t)C.gpp * C.R + 7) / 8;
+        C.ctask_end = fctask;
+    }
+    P.flat_ctasks = fctask;
+}
+
+template <int DIM, int PF, int WMAX, int MINB, int FG>
 static void (*word_kernel_m(int mode))(IsingParams, int, int) {
-    if (mode == 0) return k_ising_words<DIM, 0, PF, WMAX, MINB>;
-    if (mode == 1) return k_ising_words<DIM, 1, PF, WMAX, MINB>;
-    return k_ising_words<DIM, 2, PF, WMAX, MINB>;
+    if (mode == 0) return k_ising_words<DIM, 0, PF, WMAX, MINB, FG>;
+    if (mode == 1) return k_ising_words<DIM, 1, PF, WMAX, MINB, FG>;
+    return k_ising_words<DIM, 2, PF, WMAX, MINB, FG>;
 }
 
 // Variants: two words per lane at 3 blocks per SM (one plane ahead) or 2
 // (two planes ahead); four words per lane at 2 blocks per SM (one or two
 // planes ahead; at 3 blocks per SM its registers spill and it ran 10-19%
 // slower).
-static void (*word_kernel(int dim, int mode, int pf, int wmax))(IsingParams, int, int) {
+static void (*word_kernel(int dim, int mode, int pf, int wmax, int fg))(IsingParams, int, int) {
     if (dim == 3) {
         if (wmax == 4) {
-            if (pf == 3) return word_kernel_m<3, 3, 4, 2>(mode);
-            if (pf == 2) return word_kernel_m<3, 2, 4, 2>(mode);
-            return word_kernel_m<3, 1, 4, 2>(mode);
+            if (fg > 1) {
+                if (pf == 3) return word_kernel_m<3, 3, 4, 2, 2>(mode);
+                if (pf == 2) return word_kernel_m<3, 2, 4, 2, 2>(mode);
+                return word_kernel_m<3, 1, 4, 2, 2>(mode);
+            }
+            if (pf == 3) return word_kernel_m<3, 3, 4, 2, 1>(mode);
+            if (pf == 2) return word_kernel_m<3, 2, 4, 2, 1>(mode);
+            return word_kernel_m<3, 1, 4, 2, 1>(mode);
         }
-        if (pf == 2) return word_kernel_m<3, 2, 2, 2>(mode);
-        return word_kernel_m<3, 1, 2, 3>(mode);
+        if (fg > 1) {  // (the flat groups' registers: 2 blocks per SM)
+            if (pf == 2) return word_kernel_m<3, 2, 2, 2, 4>(mode);
+            return word_kernel_m<3, 1, 2, 2, 4>(mode);
+        }
+        if (pf == 2) return word_kernel_m<3, 2, 2, 2, 1>(mode);
+        return word_kernel_m<3, 1, 2, 3, 1>(mode);
     }
-    // no rolling tasks in 2D: one form
-    return word_kernel_m<2, 1, 2, 3>(mode);
+    // no rolling tasks in 2D: one form per flat group size
+    if (fg > 1) return word_kernel_m<2, 1, 2, 3, 4>(mode);
+    return word_kernel_m<2, 1, 2, 3, 1>(mode);
 }
 
 // Dynamic shared memory of the word kernel: the per-warp rings of PF = 3.
@@ -1966,7 +2116,7 @@ static int configure_launch(isg_ising* H) {
     const size_t dyn = word_smem(H);
     for (int mode = 0; mode < 3; ++mode) {
         int occ = 0;
-        const void* fn = (const void*)word_kernel(H->dim, mode, H->pf, H->wmax);
+        const void* fn = (const void*)word_kernel(H->dim, mode, H->pf, H->wmax, H->flatg);
         if (dyn > 0) {
             cudaError_t a =
                 cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
@@ -1998,7 +2148,7 @@ static void launch_half(isg_ising* H, int colour, int sweep_off, int mode) {
         attr[0].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = attr;
         cfg.numAttrs = H->pdl ? 1 : 0;
-        cudaLaunchKernelEx(&cfg, word_kernel(H->dim, mode, H->pf, H->wmax), H->P, colour,
+        cudaLaunchKernelEx(&cfg, word_kernel(H->dim, mode, H->pf, H->wmax, H->flatg), H->P, colour,
                            sweep_off);
     }
 }
@@ -2156,7 +2306,7 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
     H->sizes.assign(sizes, sizes + n_sizes);
 
     IsingParams& P = H->P;
-    int64_t off = 0, task = 0, site = 0, sblk = 0, ctask = 0, fctask = 0;
+    int64_t off = 0, task = 0, site = 0, sblk = 0, ctask = 0;
     for (int s = 0; s < n_sizes; ++s) {
         IsingClass& C = P.cls[s];
         const int L = sizes[s];
@@ -2168,13 +2318,17 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         const int rw = L / 8;
         const bool words = pow2 && L >= 8 && L <= 256 && (32 % rw) == 0 &&
                            (C.plane_sites / 4) % 32 == 0;
-        C.kind = !words ? kSite : (dim == 3 && L >= 32) ? kRolling : kFlat;
+        // other sizes with whole words per row and whole warp tasks per plane
+        const bool gwords = !words && L % 8 == 0 && (C.plane_sites / 4) % 32 == 0;
+        C.kind = words ? ((dim == 3 && L >= 32) ? kRolling : kFlat) : gwords ? kFlat : kSite;
+        C.flat_gen = gwords ? 1 : 0;
         C.log2L = 0;
         while ((1 << C.log2L) < L) ++C.log2L;
         C.log2_rw = 0;
         if (words)
             while ((1 << C.log2_rw) < rw) ++C.log2_rw;
-        C.tasks_per_plane = words ? C.plane_sites / 128 : 0;
+        C.tasks_per_plane = words || gwords ? C.plane_sites / 128 : 0;
+        C.div_rw = make_div((uint32_t)std::max(1, rw));
         C.log2_tpp = 0;
         while (words && (1u << C.log2_tpp) < C.tasks_per_plane) ++C.log2_tpp;
         C.rep_base = s * replicas;
@@ -2185,15 +2339,8 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
         C.task_end = task;
         C.log2_groups = 0;
         C.log2_wpl = 1;
-        if (C.kind == kRolling) {
-            // CTA tasks are laid out by layout_rolling
-        } else if (C.kind == kFlat) {
-            C.ctask_base = fctask;
-            fctask += ((int64_t)C.tasks_per_plane * replicas + 7) / 8;
-            C.ctask_end = fctask;
-        } else {
-            C.ctask_base = C.ctask_end = 0;
-        }
+        // CTA tasks of the word kinds are laid out by layout_rolling / layout_flat
+        C.ctask_base = C.ctask_end = 0;
         C.div_half = make_div((uint32_t)(L / 2));
         C.div_L = make_div((uint32_t)L);
         C.div_plane = make_div(C.plane_sites);
@@ -2225,9 +2372,9 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
     P.n_classes = n_sizes;
     P.dim = dim;
     P.total_tasks = task;
-    P.flat_ctasks = fctask;
     (void)ctask;
     layout_rolling(H);
+    layout_flat(H);
     P.total_sites = site;
     P.total_sblocks = sblk;
     P.seed = seed;
@@ -2929,6 +3076,7 @@ int isg_ising_set_words_per_lane(isg_ising* H, int words) {
     ISG_CK(cudaStreamSynchronize(H->stream));
     H->wpl_max = words;
     layout_rolling(H);
+    layout_flat(H);
     destroy_graph(H);
     return configure_launch(H);
 }

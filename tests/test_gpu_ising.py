@@ -53,12 +53,14 @@ def test_hot_start_bit_exact(gpu, oracle, dim, sizes):
 
 
 @pytest.mark.parametrize("dim,sizes,h", [(3, [2, 4, 6, 8, 10, 16, 32], 0.0),
-                                         (3, [8, 12, 24, 32, 48, 64], 0.0),
-                                         (3, [4, 8, 16], 0.35),
-                                         (2, [4, 6, 8, 16, 32, 64], 0.0)])
+                                         (3, [8, 12, 24, 32, 40, 48, 64], 0.0),
+                                         (3, [4, 8, 16, 24], 0.35),
+                                         (2, [4, 6, 8, 16, 32, 48, 64, 80], 0.0)])
 def test_sweeps_bit_exact(gpu, oracle, dim, sizes, h):
     """Every size of a batch advances in the one half-sweep launch (rolling,
-    flat and one-site tasks side by side) and matches the oracle bit for bit."""
+    flat and site-block tasks side by side; 3D L = 24, 40, 48 and 2D L = 48,
+    80 are flat tasks with rows of a non-power-of-two number of words) and
+    matches the oracle bit for bit."""
     R, seed, J = 3, 42, 1.0
     temps = [2.0, 4.5, 7.0] if dim == 3 else [1.5, 2.269, 3.5]
     b = gpu.IsingBatch(sizes, R, seed=seed, dim=dim)
@@ -155,12 +157,13 @@ def test_pt_run_bit_exact(gpu, oracle, ee, me):
     assert np.all(acc > 0)
 
 
-def test_site_block_pt_matches_oracle(gpu, oracle):
-    """Sizes that are not word sizes run as site-block tasks (one Philox block's
-    16 sites per thread), here in the graph cycle (the lattices are above the
-    resident kernel's limit or it is switched off): records with the fused
-    E/M sums, exchanges and final spins equal the oracle's PT replay."""
-    sizes, R, dim, seed = [12, 24, 48], 2, 3, 31
+def test_uneven_sizes_pt_matches_oracle(gpu, oracle):
+    """Sizes that are not powers of two run as flat word tasks (L = 24, 48:
+    multiples of 8) or site-block tasks (L = 12, 20: one Philox block's 16
+    sites per thread), here in the graph cycle (the resident kernel is
+    switched off): records with the fused E/M sums, exchanges and final spins
+    equal the oracle's PT replay."""
+    sizes, R, dim, seed = [12, 24, 48, 20], 2, 3, 31
     temps = grid(4.4, 4.6, R)
     b = gpu.IsingBatch(sizes, R, seed=seed, dim=dim)
     b.set_resident_pt(False)

@@ -328,6 +328,36 @@ def hbm_case(pkg, stream, flush, steps, peak, peak_kind):
             "sweeps_per_s": SWEEPS_PER_STEP * steps / (dev_ms * 1e-3), "roofline": roof}
 
 
+UNEVEN_SIZES = [8, 12, 16, 24, 32, 48, 64, 96, 128]
+
+
+def uneven_case(pkg, stream, flush, steps):
+    """Sizes from 8 to 128 that are not all powers of two, 32 replicas each, in
+    one launch per half-sweep: rolling tasks (32, 64, 128), flat word tasks
+    (8, 16, and 24, 48, 96 with rows that are not a power of two words long)
+    and site-block tasks (12).  The same PT step and timing as the headline."""
+    R = REPLICAS
+    T = [TMIN + (TMAX - TMIN) * i / (R - 1) for i in range(R)]
+    b = pkg.IsingBatch(UNEVEN_SIZES, R, seed=SEED + 5)
+    b.set_stream(stream)
+    b.set_temperatures(T)
+    b.step(10)
+    b.reset_sampling()
+    for _ in range(3):
+        b.pt_launch(SWEEPS_PER_STEP, EXCHANGE_EVERY, MEASURE_EVERY)
+    step_ms = _timed_pt_steps(b, stream, flush, steps)
+    dev_ms = float(sum(step_ms))
+    sites = R * sum(L ** 3 for L in UNEVEN_SIZES)
+    launch_ms = b.time_halfsweep_graph(2 * SWEEPS_PER_STEP, 256 << 20, 5)
+    b.close()
+    return {"workload": f"3D Ising PT L={','.join(map(str, UNEVEN_SIZES))} x {R} replicas, "
+                        f"T in [{TMIN},{TMAX}], exchange 10, measure 5",
+            "value": sites * SWEEPS_PER_STEP * steps / (dev_ms * 1e6), "unit": "flips/ns",
+            "ms_per_step": dev_ms / steps, "steps": steps,
+            "halfsweep_launches_per_sweep": 2, "halfsweep_ms": launch_ms,
+            "halfsweep_flips_per_ns": sites / 2 / (launch_ms * 1e6)}
+
+
 def ess_case(pkg, stream, sweeps_per_s):
     """ESS/s of |M| on the headline batch from a run of its own: ESS_WARMUP
     warm-up sweeps, then ESS_SWEEPS sweeps with a record every 5 (at L = 128
@@ -480,6 +510,7 @@ def run_gpu(args):
     hbm = hbm_case(pkg, stream, flush, max(3, min(args.steps, 100)), peak, peak_kind)
     ess = ess_case(pkg, stream, sweeps_per_s)
     cfg1 = config1_case(pkg)
+    uneven = uneven_case(pkg, stream, flush, args.steps)
     learned = learned_summary(pkg, args) if args.learned_seconds > 0 else None
     threads = host_threads()
     cpu_v, cpu_s, cpu_f = cpu_sample(threads, sweeps=args.cpu_sweeps)
@@ -505,6 +536,7 @@ def run_gpu(args):
         "roofline": roof,
         "roofline_hbm": hbm,
         "config1": cfg1,
+        "uneven": uneven,
         "learned": learned,
         "cpu_baseline": {"value": cpu_v, "unit": "flips/ns", "cores": threads, "kind": "port",
                          "sample": f"{threads} threads x {args.cpu_sweeps:g} random-site sweeps "

@@ -602,7 +602,7 @@ def learned_case(pkg, L, dim, T, train_seconds, chain_batches, pt_sweeps):
     # configurations of the plain sampler at T (256 chains, a snapshot every 10
     # sweeps, with negations), so the network cannot memorise a fixed set
     stream = lrn.TrainingStream(L, dim, T, chains=256, gap=10, warmup=2000)
-    q = lrn.LearnedProposal(H, W, layers=6, seed=SEED)
+    q = lrn.LearnedProposal(H, W, layers=6, seed=SEED, zrow=L if dim == 3 else 0)
     steps = 0
     tt = time.perf_counter()
     while time.perf_counter() - tt < train_seconds:

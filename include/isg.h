@@ -374,6 +374,11 @@ int isg_cont_observables_static(const float* d_spins, int L, int n_comp, int rep
  * bytes.  All device work runs on the handle's stream (isg_learned_stream). */
 typedef struct isg_learned isg_learned;
 int isg_learned_create(isg_learned** out, int H, int W, int layers, uint64_t seed);
+/* As isg_learned_create, for the raster of a 3D lattice: zrow = rows per
+ * z-plane (L for the L^2 x L raster of an L^3 lattice; 0 = 2D).  Layer 0 then
+ * has a fifth tap, the site one z-plane back (zrow rows up, same x), so the
+ * network sees the z-neighbour that the 3x3 raster taps cannot reach. */
+int isg_learned_create2(isg_learned** out, int H, int W, int zrow, int layers, uint64_t seed);
 int isg_learned_destroy(isg_learned* h);
 int isg_learned_num_params(isg_learned* h, int* n);
 int isg_learned_get_weights(isg_learned* h, float* w);

@@ -40,28 +40,30 @@ namespace {
 constexpr int kC = 32;         // channels
 constexpr int kMaxLayers = 8;
 constexpr int kTaps = 5;       // (-1,-1) (-1,0) (-1,+1) (0,-1) (0,0)
-__host__ __device__ __forceinline__ int tap_dy(int t) { return t < 3 ? -1 : 0; }
 __host__ __device__ __forceinline__ int tap_dx(int t) { return t < 3 ? t - 1 : (t == 3 ? -1 : 0); }
 constexpr uint32_t kTagLearn = 0x06u;
 
-// Weight layout per layer l: w[tap][cin][cout] (taps 0..3 for layer 0, else
-// 0..4), then bias[cout].  cin = 1 for layer 0, cout = 1 for the last layer.
+// Weight layout per layer l: w[tap][cin][cout] (taps 0..3 for layer 0, 0..4
+// for a 3D network's layer 0 and for the other layers), then bias[cout].
+// cin = 1 for layer 0, cout = 1 for the last layer.
 struct NetShape {
     int D;                       // layers
+    int zrow;                    // rows per z-plane of a 3D lattice's raster (0: 2D)
     int cin[kMaxLayers], cout[kMaxLayers], taps[kMaxLayers];
     int woff[kMaxLayers];        // offset of layer weights
     int boff[kMaxLayers];        // offset of layer bias
     int total;
 };
 
-NetShape make_shape(int D) {
+NetShape make_shape(int D, int zrow) {
     NetShape s{};
     s.D = D;
+    s.zrow = zrow;
     int off = 0;
     for (int l = 0; l < D; ++l) {
         s.cin[l] = l == 0 ? 1 : kC;
         s.cout[l] = l == D - 1 ? 1 : kC;
-        s.taps[l] = l == 0 ? 4 : 5;
+        s.taps[l] = l == 0 ? (zrow > 0 ? 5 : 4) : 5;
         s.woff[l] = off;
         off += s.taps[l] * s.cin[l] * s.cout[l];
         s.boff[l] = off;
@@ -69,6 +71,19 @@ NetShape make_shape(int D) {
     }
     s.total = off;
     return s;
+}
+
+// Row offset of tap t of layer l: taps 0..2 look one row back, tap 3 along
+// the row; tap 4 is the centre for layers >= 1 and, for layer 0 of a 3D
+// network (whose raster is the L^2 x L image of its z-y rows), the site one
+// z-plane back: zrow rows up, same x.  In raster order that site precedes the
+// current one, so the mask stays autoregressive.
+__host__ __device__ __forceinline__ int tap_dy(const NetShape& S, int l, int t) {
+    return (l == 0 && t == 4) ? -S.zrow : (t < 3 ? -1 : 0);
+}
+// Rows of layer l's input that its taps reach back, staged by k_tf_wgrad.
+__host__ __device__ __forceinline__ int wg_halo(const NetShape& S, int l, int W) {
+    return (l == 0 && S.zrow > 0 && S.zrow * W > W + 1) ? S.zrow * W : W + 1;
 }
 
 __device__ __forceinline__ float bf(const __nv_bfloat16* w, int i) { return __bfloat162float(w[i]); }
@@ -122,7 +137,7 @@ __global__ void __launch_bounds__(G * kC)
                 const int co = last ? 0 : c;
                 acc = bf(w, S.boff[l] + co);
                 for (int t = 0; t < taps; ++t) {
-                    const int yy = y + tap_dy(t), xx = x + tap_dx(t);
+                    const int yy = y + tap_dy(S, l, t), xx = x + tap_dx(t);
                     if (yy < 0 || xx < 0 || xx >= W) continue;
                     const int q = yy * W + xx;
                     const __nv_bfloat16* wt = w + S.woff[l] + (t * S.cin[l]) * S.cout[l] + co;
@@ -179,7 +194,7 @@ __global__ void k_tf_layer(const __nv_bfloat16* __restrict__ w, NetShape S, int 
         const int y = p / W, x = p - y * W;
         float acc = bf(w, S.boff[l] + co);
         for (int t = 0; t < taps; ++t) {
-            const int yy = y + tap_dy(t), xx = x + tap_dx(t);
+            const int yy = y + tap_dy(S, l, t), xx = x + tap_dx(t);
             if (yy < 0 || xx < 0 || xx >= W) continue;
             const float* src = in + (b * HW + yy * W + xx) * cin;
             const __nv_bfloat16* wt = w + S.woff[l] + (t * cin) * cout + co;
@@ -231,7 +246,7 @@ __global__ void k_tf_dgrad(const __nv_bfloat16* __restrict__ w, NetShape S, int 
         float acc = 0.f;
         for (int t = 0; t < taps; ++t) {
             // output position q with q + off_t = p
-            const int yy = y - tap_dy(t), xx = x - tap_dx(t);
+            const int yy = y - tap_dy(S, l, t), xx = x - tap_dx(t);
             if (yy >= H || xx < 0 || xx >= W) continue;
             const float* g = dz + (b * HW + yy * W + xx) * cout;
             const __nv_bfloat16* wt = w + S.woff[l] + (t * cin + ci) * cout;
@@ -260,7 +275,7 @@ __global__ void k_tf_wgrad(NetShape S, int l, int H, int W, int B, const float* 
     const int64_t n = (int64_t)B * HW;
     const int64_t start = (int64_t)blockIdx.x * chunk;
     const int cnt = (int)(start + chunk < n ? chunk : n - start);
-    const int halo = W + 1;
+    const int halo = wg_halo(S, l, W);
     float* s_dz = wg_sm;                              // [chunk][cout]
     float* s_in = s_dz + (size_t)chunk * cout;        // [halo + chunk][cin]
     unsigned char* s_ok = reinterpret_cast<unsigned char*>(s_in + (size_t)(halo + chunk) * cin);
@@ -274,7 +289,7 @@ __global__ void k_tf_wgrad(NetShape S, int l, int H, int W, int B, const float* 
         const int y = p / W, x = p - y * W;
         unsigned char m = 0;
         for (int t = 0; t < taps; ++t) {
-            const int yy = y + tap_dy(t), xx = x + tap_dx(t);
+            const int yy = y + tap_dy(S, l, t), xx = x + tap_dx(t);
             if (yy >= 0 && xx >= 0 && xx < W) m |= (unsigned char)(1u << t);
         }
         s_ok[q] = m;
@@ -286,7 +301,7 @@ __global__ void k_tf_wgrad(NetShape S, int l, int H, int W, int B, const float* 
             const int co = j % cout;
             const int ci = (j / cout) % cin;
             const int t = j / (cout * cin);
-            const int off = halo + tap_dy(t) * W + tap_dx(t);  // s_in row of q's tap
+            const int off = halo + tap_dy(S, l, t) * W + tap_dx(t);  // s_in row of q's tap
             const unsigned char bit = (unsigned char)(1u << t);
             for (int q = 0; q < cnt; ++q)
                 if (s_ok[q] & bit) acc = fmaf(s_in[(q + off) * cin + ci], s_dz[q * cout + co], acc);
@@ -458,9 +473,11 @@ __device__ __forceinline__ uint32_t ring_off(int row, int chunk) {
 }
 
 struct MmaSmem {
-    size_t rings, bt, btlast, w0, bias, spins, total;
+    size_t rings, bt, btlast, w0, bias, spins, zring, total;
 };
-__host__ __device__ inline MmaSmem mma_layout(int D, int W) {
+// zring (3D networks): the spins of the last zrow * W positions, read by
+// layer 0's z-plane tap
+__host__ __device__ inline MmaSmem mma_layout(int D, int W, int zrow) {
     MmaSmem m{};
     const size_t slot = (size_t)kMmaRows * 64;
     m.rings = 0;
@@ -469,7 +486,8 @@ __host__ __device__ inline MmaSmem mma_layout(int D, int W) {
     m.w0 = m.btlast + (size_t)8 * kBtRow * 2;
     m.bias = m.w0 + sizeof(float) * 4 * kC;
     m.spins = m.bias + sizeof(float) * ((size_t)(D - 1) * kC + 1);
-    m.total = m.spins + (size_t)(W + 2) * kMmaRows;
+    m.zring = m.spins + (size_t)(W + 2) * kMmaRows;
+    m.total = m.zring + (size_t)zrow * W * kMmaRows;
     m.total = (m.total + 15) & ~(size_t)15;
     return m;
 }
@@ -504,8 +522,10 @@ __global__ void __launch_bounds__(128)
              int8_t* __restrict__ spins, float* __restrict__ logq, int n_cfg, uint64_t seed,
              uint64_t step) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const MmaSmem L = mma_layout(D, W);
+    const MmaSmem L = mma_layout(D, W, S.zrow);
     unsigned char* rings = smem + L.rings;
+    int8_t* zring = reinterpret_cast<int8_t*>(smem + L.zring);
+    const int zw = S.zrow * W;  // positions one z-plane back (0: 2D)
     __nv_bfloat16* bt = reinterpret_cast<__nv_bfloat16*>(smem + L.bt);
     __nv_bfloat16* btl = reinterpret_cast<__nv_bfloat16*>(smem + L.btlast);
     int8_t* sring = reinterpret_cast<int8_t*>(smem + L.spins);
@@ -531,12 +551,13 @@ __global__ void __launch_bounds__(128)
     }
     // layer 0: thread = 8 r + j computes channels 4j..4j+3 of configuration r
     const int r0 = tid >> 3, j0 = tid & 7;
-    float w0r[4][4], b0r[4];
+    float w0r[5][4], b0r[4];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
         b0r[e] = bf(w, S.boff[0] + 4 * j0 + e);
 #pragma unroll
-        for (int t = 0; t < 4; ++t) w0r[t][e] = bf(w, S.woff[0] + t * kC + 4 * j0 + e);
+        for (int t = 0; t < 5; ++t)
+            w0r[t][e] = t < S.taps[0] ? bf(w, S.woff[0] + t * kC + 4 * j0 + e) : 0.f;
     }
     const int g = lane >> 2, q4 = lane & 3;
     // epilogue biases of this lane's two columns in every hidden layer
@@ -600,6 +621,9 @@ __global__ void __launch_bounds__(128)
             const float sv1 = ok1 ? (float)sring[ts1 * kMmaRows + r0] : 0.f;
             const float sv2 = ok2 ? (float)sring[ts2 * kMmaRows + r0] : 0.f;
             const float sv3 = ok3 ? (float)sring[ts3 * kMmaRows + r0] : 0.f;
+            // z-plane tap: position p - zw, whose spin zring slot p mod zw
+            // still holds (this position's spin replaces it below)
+            const float sv4 = (zw > 0 && p >= zw) ? (float)zring[(p % zw) * kMmaRows + r0] : 0.f;
             float v[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
@@ -608,6 +632,7 @@ __global__ void __launch_bounds__(128)
                 a = fmaf(w0r[1][e], sv1, a);
                 a = fmaf(w0r[2][e], sv2, a);
                 a = fmaf(w0r[3][e], sv3, a);
+                if (zw > 0) a = fmaf(w0r[4][e], sv4, a);
                 v[e] = fmaxf(a, 0.f);
             }
             __nv_bfloat162 p0 = __floats2bfloat162_rn(v[0], v[1]);
@@ -658,6 +683,7 @@ __global__ void __launch_bounds__(128)
                                 lqb += log_sigmoid((float)sv * z);
                         }
                         sring[slot * kMmaRows + row] = sv;
+                        if (zw > 0) zring[(p % zw) * kMmaRows + row] = sv;
                     }
                 }
             }
@@ -696,7 +722,7 @@ __host__ __device__ inline ScoreSmem score_layout(int D, int HW) {
     m.bt = m.zero + 64;
     m.btlast = m.bt + (size_t)(D - 2) * kC * kBtRow * 2;
     m.w0 = m.btlast + (size_t)8 * kBtRow * 2;
-    m.bias = m.w0 + sizeof(float) * 4 * kC;
+    m.bias = m.w0 + sizeof(float) * 5 * kC;
     m.term = m.bias + sizeof(float) * ((size_t)(D - 1) * kC + 4);
     m.spin = m.term + sizeof(float) * (size_t)HW;
     m.total = (m.spin + (size_t)HW + 15) & ~(size_t)15;
@@ -730,7 +756,7 @@ __global__ void __launch_bounds__(256, 1)
         const int n = i / kBtRow, k = i - n * kBtRow;
         btl[i] = (n == 0 && k < 5 * kC) ? w[S.woff[D - 1] + k] : __float2bfloat16(0.f);
     }
-    for (int i = tid; i < 4 * kC; i += blockDim.x) w0[i] = bf(w, S.woff[0] + i);
+    for (int i = tid; i < S.taps[0] * kC; i += blockDim.x) w0[i] = bf(w, S.woff[0] + i);
     for (int l = 0; l < D - 1; ++l)
         for (int i = tid; i < kC; i += blockDim.x) bias[l * kC + i] = bf(w, S.boff[l] + i);
     if (tid == 0) bias[(D - 1) * kC] = bf(w, S.boff[D - 1]);
@@ -744,6 +770,8 @@ __global__ void __launch_bounds__(256, 1)
     }
     __syncthreads();
     // layer 0 (mask A, 1 -> 32), as the sampler: a = bias; fma over taps 0..3
+    // and, for a 3D network, the z-plane tap
+    const int zw = S.zrow * W;
     for (int i = tid; i < HW * 4; i += blockDim.x) {
         const int p = i >> 2, j2 = i & 3;  // channels 8 j2 .. 8 j2 + 7 (one chunk)
         const int y = p / W, x = p - y * W;
@@ -752,6 +780,7 @@ __global__ void __launch_bounds__(256, 1)
         const float s1 = up ? (float)sp[p - W] : 0.f;
         const float s2 = (up && right) ? (float)sp[p - W + 1] : 0.f;
         const float s3 = left ? (float)sp[p - 1] : 0.f;
+        const float s4 = (zw > 0 && p >= zw) ? (float)sp[p - zw] : 0.f;
         uint32_t packed[4];
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
@@ -764,6 +793,7 @@ __global__ void __launch_bounds__(256, 1)
                 a = fmaf(w0[1 * kC + co], s1, a);
                 a = fmaf(w0[2 * kC + co], s2, a);
                 a = fmaf(w0[3 * kC + co], s3, a);
+                if (zw > 0) a = fmaf(w0[4 * kC + co], s4, a);
                 v[e] = fmaxf(a, 0.f);
             }
             __nv_bfloat162 b2 = __floats2bfloat162_rn(v[0], v[1]);
@@ -904,13 +934,13 @@ static int grid_for(int64_t n, int thr) {
 
 // The tensor-core kernel when its rings and weights fit in shared memory.
 static bool use_mma(const isg_learned* h) {
-    return h->D >= 2 && h->D <= 8 && mma_layout(h->D, h->W).total <= 232448;
+    return h->D >= 2 && h->D <= 8 && mma_layout(h->D, h->W, h->S.zrow).total <= 232448;
 }
 
 template <int D>
 static int launch_mma(isg_learned* h, int mode, int flip, int8_t* spins, float* lq, int K,
                       uint64_t step) {
-    const size_t smem = mma_layout(D, h->W).total;
+    const size_t smem = mma_layout(D, h->W, h->S.zrow).total;
     ISG_CK(cudaFuncSetAttribute(k_ar_mma<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
     k_ar_mma<D><<<(K + kMmaRows - 1) / kMmaRows, 128, smem, h->stream>>>(
@@ -1013,8 +1043,12 @@ static int forward_backward(isg_learned* h, int B, float* mean_lq) {
     float* dn = h->d_dz2;
     const int chunk = 128;
     const int nparts = (int)(((int64_t)B * HW + chunk - 1) / chunk);
-    const size_t wg_smem = sizeof(float) * ((size_t)chunk * kC + (size_t)(h->W + 1 + chunk) * kC) +
-                           (size_t)chunk;
+    size_t wg_smem = 0;
+    for (int l = 0; l < h->D; ++l)
+        wg_smem = std::max(wg_smem, sizeof(float) * ((size_t)chunk * h->S.cout[l] +
+                                                     (size_t)(wg_halo(h->S, l, h->W) + chunk) *
+                                                         h->S.cin[l]) +
+                                        (size_t)chunk);
     for (int l = h->D - 1; l >= 0; --l) {
         const int nw = h->S.taps[l] * h->S.cin[l] * h->S.cout[l] + h->S.cout[l];
         if ((int64_t)nparts * nw > h->part_cap) {
@@ -1053,10 +1087,16 @@ static int forward_backward(isg_learned* h, int B, float* mean_lq) {
 extern "C" {
 
 int isg_learned_create(isg_learned** out, int H, int W, int layers, uint64_t seed) {
+    return isg_learned_create2(out, H, W, 0, layers, seed);
+}
+
+int isg_learned_create2(isg_learned** out, int H, int W, int zrow, int layers, uint64_t seed) {
     if (!out) return fail(ISG_ERR_ARG, "isg_learned_create: out is NULL");
     *out = nullptr;
     if (H < 2 || W < 2 || H * W > 65536 || layers < 2 || layers > kMaxLayers)
         return fail(ISG_ERR_ARG, "isg_learned_create: need 2 <= H, W, H*W <= 65536, 2..8 layers");
+    if (zrow < 0 || zrow >= H)
+        return fail(ISG_ERR_ARG, "isg_learned_create: need 0 <= zrow < H");
     isg_learned* h = new (std::nothrow) isg_learned();
     if (!h) return fail(ISG_ERR_ARG, "isg_learned_create: out of host memory");
     cudaGetDevice(&h->device);
@@ -1064,7 +1104,7 @@ int isg_learned_create(isg_learned** out, int H, int W, int layers, uint64_t see
     h->W = W;
     h->D = layers;
     h->seed = seed;
-    h->S = make_shape(layers);
+    h->S = make_shape(layers, zrow);
     const int n = h->S.total;
     // He-style initial weights from a host generator seeded by `seed`
     std::vector<float> w(n, 0.f);
@@ -1239,7 +1279,7 @@ int isg_learned_batch_quantum(isg_learned* h, int* quantum) {
     ISG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
     int per_sm = 1, rows = kMmaRows;
     if (use_mma(h)) {
-        const size_t smem = mma_layout(h->D, h->W).total;
+        const size_t smem = mma_layout(h->D, h->W, h->S.zrow).total;
         void (*k)(const __nv_bfloat16*, NetShape, int, int, int, int, int8_t*, float*, int,
                   uint64_t, uint64_t) = nullptr;
         switch (h->D) {

@@ -33,6 +33,7 @@ def _declare_learned(L):
     vp, i32, i64, u64, dbl, f32 = C.c_void_p, C.c_int, C.c_int64, C.c_uint64, C.c_double, C.c_float
     sig = {
         "isg_learned_create": [C.POINTER(vp), i32, i32, i32, u64],
+        "isg_learned_create2": [C.POINTER(vp), i32, i32, i32, i32, u64],
         "isg_learned_destroy": [vp],
         "isg_learned_num_params": [vp, vp],
         "isg_learned_get_weights": [vp, vp],
@@ -72,12 +73,16 @@ def _tptr(t) -> C.c_void_p:
 
 
 class LearnedProposal:
-    """Masked-conv autoregressive network over an H x W raster of +-1 spins."""
+    """Masked-conv autoregressive network over an H x W raster of +-1 spins;
+    zrow > 0 (a 3D lattice's L^2 x L raster: zrow = L) adds layer 0's z-plane
+    tap (isg_learned_create2)."""
 
-    def __init__(self, H: int, W: int, layers: int = 6, seed: int = 7):
+    def __init__(self, H: int, W: int, layers: int = 6, seed: int = 7, zrow: int = 0):
         self.H, self.W, self.layers, self.seed = int(H), int(W), int(layers), int(seed)
+        self.zrow = int(zrow)
         h = C.c_void_p()
-        _check(_lib().isg_learned_create(C.byref(h), self.H, self.W, self.layers, self.seed))
+        _check(_lib().isg_learned_create2(C.byref(h), self.H, self.W, self.zrow, self.layers,
+                                          self.seed))
         self._h = h
         n = C.c_int()
         _check(_lib().isg_learned_num_params(self._h, C.byref(n)))

@@ -23,8 +23,9 @@ def learned(pkg):
     return importlib.import_module(pkg.__name__ + ".learned")
 
 
-def torch_logq(w, D, H, W, cfg, bf16_acts=False):
-    """torch FP32 restatement of the network (masks as zeroed 3x3 taps);
+def torch_logq(w, D, H, W, cfg, bf16_acts=False, zrow=0):
+    """torch FP32 restatement of the network (masks as zeroed 3x3 taps; with
+    zrow > 0 layer 0 adds the z-plane tap, the input zrow rows up);
     bf16_acts rounds the hidden activations to BF16 as the tensor-core
     sampling kernel stores them."""
     import torch
@@ -35,18 +36,22 @@ def torch_logq(w, D, H, W, cfg, bf16_acts=False):
     for l in range(D):
         cin = 1 if l == 0 else 32
         cout = 1 if l == D - 1 else 32
-        nt = 4 if l == 0 else 5
+        nt = (5 if zrow else 4) if l == 0 else 5
         n = nt * cin * cout
         wl = w[off:off + n].view(nt, cin, cout)
         off += n
         b = w[off:off + cout]
         off += cout
         grid = [torch.zeros(cout, cin, dtype=w.dtype)] * 9
-        for t in range(nt):
+        for t in range(4 if l == 0 else nt):
             dy, dx = taps[t]
             grid[(1 + dy) * 3 + (1 + dx)] = wl[t].t()
         K = torch.stack(grid, dim=-1).view(cout, cin, 3, 3)
-        x = F.conv2d(x, K, b, padding=1)
+        xin = x
+        x = F.conv2d(xin, K, b, padding=1)
+        if l == 0 and zrow:
+            shifted = F.pad(xin, (0, 0, zrow, 0))[:, :, :H, :]  # input at (y - zrow, x)
+            x = x + torch.einsum("bihw,io->bohw", shifted, wl[4])
         if l < D - 1:
             x = torch.relu(x)
             if bf16_acts:
@@ -55,11 +60,14 @@ def torch_logq(w, D, H, W, cfg, bf16_acts=False):
     return F.logsigmoid(cfg.view(-1, H * W) * logits).sum(1)
 
 
-@pytest.mark.parametrize("H,W,D", [(6, 6, 4), (8, 4, 6)])
-def test_gradient_matches_torch_cpu(gpu, H, W, D):
+@pytest.mark.parametrize("H,W,D,zrow", [(6, 6, 4, 0), (8, 4, 6, 0), (16, 4, 4, 4)])
+def test_gradient_matches_torch_cpu(gpu, H, W, D, zrow):
+    """Gradients of the hand-written training kernels against torch-CPU FP32
+    autograd of the same network (the last case: the 4^3 raster with layer 0's
+    z-plane tap)."""
     import torch
     L = learned(gpu)
-    q = L.LearnedProposal(H, W, layers=D, seed=5)
+    q = L.LearnedProposal(H, W, layers=D, seed=5, zrow=zrow)
     rng = np.random.default_rng(0)
     # perturb biases too so every parameter is exercised
     w0 = q.weights() + rng.normal(0, 0.05, q.n_params).astype(np.float32)
@@ -68,7 +76,7 @@ def test_gradient_matches_torch_cpu(gpu, H, W, D):
     cfg = np.where(rng.random((16, H * W)) < 0.5, 1, -1).astype(np.int8)
     g, nll = q.gradient(cfg)
     wt = torch.tensor(wq, dtype=torch.float32, requires_grad=True)
-    loss = -torch_logq(wt, D, H, W, torch.tensor(cfg, dtype=torch.float32)).mean()
+    loss = -torch_logq(wt, D, H, W, torch.tensor(cfg, dtype=torch.float32), zrow=zrow).mean()
     loss.backward()
     gt = wt.grad.numpy()
     assert abs(nll - loss.item()) < 2e-3 * max(1.0, abs(loss.item()))
@@ -97,25 +105,36 @@ def test_sample_score_identical_and_matches_torch(gpu):
     assert torch.equal(p2, props) and torch.equal(l2, lq) and not torch.equal(p3, props)
 
 
-@pytest.mark.parametrize("H,W,D", [(16, 16, 6), (32, 32, 6), (64, 8, 6), (12, 20, 4)])
-def test_sample_score_identical_at_chain_sizes(gpu, H, W, D):
+@pytest.mark.parametrize("H,W,D,zrow", [(16, 16, 6, 0), (32, 32, 6, 0), (64, 8, 6, 0),
+                                        (12, 20, 4, 0), (64, 8, 6, 8), (144, 12, 5, 12)])
+def test_sample_score_identical_at_chain_sizes(gpu, H, W, D, zrow):
     """The sampler and the whole-lattice scorer give bit-identical log q (and
-    log q of the negation) at the raster sizes the chains use."""
+    log q of the negation) at the raster sizes the chains use, 3D rasters with
+    layer 0's z-plane tap included."""
     import torch
     L = learned(gpu)
-    q = L.LearnedProposal(H, W, layers=D, seed=21)
+    q = L.LearnedProposal(H, W, layers=D, seed=21, zrow=zrow)
     props, lq, lqf = q.sample(300, 5)
     s1 = q.score(props)
     s2 = q.score(props, flip=True)
     q.sync()
     assert torch.equal(lq, s1) and torch.equal(lqf, s2)
+    if zrow:
+        ref = torch_logq(torch.tensor(q.weights()), D, H, W, props.cpu().float(),
+                         bf16_acts=True, zrow=zrow)
+        # FP32 sums of H*W log-sigmoid terms in two different orders: the
+        # difference grows with the number of terms (2e-3 at 512 positions)
+        tol = 2e-3 * max(1.0, H * W / 512)
+        assert torch.max(torch.abs(ref - lq.cpu())) < tol
 
 
-def test_distribution_is_normalised(gpu):
+@pytest.mark.parametrize("H,W,zrow", [(3, 3, 0), (4, 2, 2)])
+def test_distribution_is_normalised(gpu, H, W, zrow):
+    """q sums to 1 over all configurations (the 2^3 lattice's 4 x 2 raster
+    with the z-plane tap too)."""
     import torch
     L = learned(gpu)
-    H = W = 3
-    q = L.LearnedProposal(H, W, layers=3, seed=13)
+    q = L.LearnedProposal(H, W, layers=3, seed=13, zrow=zrow)
     w = q.weights()
     q.set_weights(w * 3.0)  # a sharper, non-trivial distribution
     allc = np.array(list(itertools.product([-1, 1], repeat=H * W)), np.int8)
@@ -145,7 +164,7 @@ def test_chain_is_exact(gpu, oracle, L_, dim, T):
     n = L_ ** dim
     H, W = (L_, L_) if dim == 2 else (L_ * L_, L_)
     data = L.collect_training_set(L_, dim, T, chains=32, rounds=16, gap=5, warmup=200)
-    q = L.LearnedProposal(H, W, layers=4, seed=2)
+    q = L.LearnedProposal(H, W, layers=4, seed=2, zrow=L_ if dim == 3 else 0)
     q.train(data, batch=64, steps=60, lr=3e-3)
     ch = L.LearnedChain(q, L_, dim, T, K=2048, sweeps=1, fallback_sweeps=5, min_accept=0.05)
     request_close = ch.close

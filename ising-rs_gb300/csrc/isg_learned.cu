@@ -313,6 +313,302 @@ __global__ void k_tf_wgrad(NetShape S, int l, int H, int W, int B, const float* 
     }
 }
 
+// -------------------------------------------- training on the tensor cores
+// The convolutions of the layers with 32 input channels (layers 1..D-1) as
+// implicit GEMMs on mma.sync m16n8k8 with TF32 operands and FP32
+// accumulation.  An FP32 operand x is split into hi = tf32(x) and lo =
+// tf32(x - hi), and a product takes the MMAs a_lo b + a_hi b (the BF16
+// weights are exact in TF32), or a_lo b_hi + a_hi b_lo + a_hi b_hi for the
+// weight gradient, so the sums keep FP32 accuracy to about 1e-6 relative.  Rows (16 per warp) are positions m = b HW + p of the
+// flattened batch; a block stages the rows its taps reach (rows padded to
+// 36 words, so a warp's fragment loads hit 32 different banks) and the layer's
+// weights (k = tap * 32 + channel, rows padded to 40 words, likewise).  Layer
+// 0 (one input channel) stays on the CUDA cores.
+constexpr int kTcTile = 128;   // positions per block tile (8 warps x 16)
+constexpr int kTcRow = 36;     // staged words per position row
+constexpr int kTcWRow = 40;    // staged words per weight row
+constexpr int kTcChunk = 512;  // positions per block of the weight gradient
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+// hi / lo TF32 parts of an FP32 value held as its bit pattern
+__device__ __forceinline__ void split_tf32(uint32_t x, uint32_t& hi, uint32_t& lo) {
+    const float f = __uint_as_float(x);
+    hi = to_tf32(f);
+    lo = to_tf32(f - __uint_as_float(hi));
+}
+__device__ __forceinline__ void mma_tf32(float* d, uint32_t a0, uint32_t a1, uint32_t a2,
+                                         uint32_t a3, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+// Tap t of layer l >= 1 at position p: its offset in the flattened batch and
+// whether it lies inside the lattice.
+__device__ __forceinline__ bool tc_tap(const NetShape& S, int l, int t, int p, int W, int& off) {
+    const int dy = tap_dy(S, l, t), dx = tap_dx(t);
+    const int y = p / W, x = p - y * W;
+    off = dy * W + dx;
+    return y + dy >= 0 && x + dx >= 0 && x + dx < W;
+}
+__host__ __device__ inline size_t tc_fwd_smem(int W) {
+    return sizeof(uint32_t) * ((size_t)5 * kC * kTcWRow + (size_t)(W + 1 + kTcTile + 1) * kTcRow);
+}
+__host__ __device__ inline size_t tc_wgrad_smem(int W) {
+    return sizeof(uint32_t) * ((size_t)(W + 1 + kTcChunk) * kTcRow + (size_t)kTcChunk * kTcWRow) +
+           (size_t)kTcChunk;
+}
+
+// Forward of layer l >= 1: z[m][co] = bias[co] + sum_t sum_ci w[t][ci][co]
+// in[m + off_t][ci] (taps outside the lattice add nothing), a = relu(z) for a
+// hidden layer.  cout = 32, or 1 for the last layer.
+__global__ void __launch_bounds__(256) k_tc_fwd(const __nv_bfloat16* __restrict__ w, NetShape S,
+                                                int l, int H, int W, int B,
+                                                const float* __restrict__ in,
+                                                float* __restrict__ z, float* __restrict__ a) {
+    extern __shared__ uint32_t tsm[];
+    const int cout = S.cout[l], nt = cout == 1 ? 1 : 4;
+    const int HW = H * W, halo = W + 1;
+    const int64_t M = (int64_t)B * HW;
+    uint32_t* s_w = tsm;                                  // [160][kTcWRow]
+    uint32_t* s_in = s_w + 5 * kC * kTcWRow;              // [halo + tile + 1][kTcRow]
+    const uint32_t* zrow = s_in + (size_t)(halo + kTcTile) * kTcRow;
+    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5, g = lane >> 2, q = lane & 3;
+    for (int i = tid; i < 5 * kC * kTcWRow; i += blockDim.x) {
+        const int k = i / kTcWRow, n = i - k * kTcWRow;
+        s_w[i] = n < cout ? to_tf32(bf(w, S.woff[l] + k * cout + n)) : 0u;
+    }
+    for (int i = tid; i < kTcRow; i += blockDim.x) s_in[(size_t)(halo + kTcTile) * kTcRow + i] = 0u;
+    for (int64_t m0 = (int64_t)blockIdx.x * kTcTile; m0 < M; m0 += (int64_t)gridDim.x * kTcTile) {
+        __syncthreads();  // the previous tile's reads are done
+        for (int i = tid; i < (halo + kTcTile) * kC; i += blockDim.x) {
+            const int r = i >> 5, c = i & 31;
+            const int64_t mm = m0 - halo + r;
+            s_in[r * kTcRow + c] = (mm >= 0 && mm < M) ? __float_as_uint(in[mm * kC + c]) : 0u;
+        }
+        __syncthreads();
+        const int rA = 16 * wp + g, rB = rA + 8;  // rows of the tile
+        const int64_t mA = m0 + rA, mB = m0 + rB;
+        const int pA = (int)(mA % HW), pB = (int)(mB % HW);
+        float acc[4][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[j][e] = 0.f;
+#pragma unroll
+        for (int t = 0; t < 5; ++t) {
+            int offA, offB;
+            const bool vA = tc_tap(S, l, t, pA, W, offA) && mA < M;
+            const bool vB = tc_tap(S, l, t, pB, W, offB) && mB < M;
+            const uint32_t* ra = vA ? s_in + (size_t)(halo + rA + offA) * kTcRow : zrow;
+            const uint32_t* rb = vB ? s_in + (size_t)(halo + rB + offB) * kTcRow : zrow;
+#pragma unroll
+            for (int cb = 0; cb < 4; ++cb) {
+                uint32_t h0, h1, h2, h3, l0, l1, l2, l3;
+                split_tf32(ra[8 * cb + q], h0, l0);
+                split_tf32(rb[8 * cb + q], h1, l1);
+                split_tf32(ra[8 * cb + q + 4], h2, l2);
+                split_tf32(rb[8 * cb + q + 4], h3, l3);
+                const uint32_t* wk = s_w + (size_t)((t * 4 + cb) * 8 + q) * kTcWRow;
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (j < nt) {
+                        const uint32_t b0 = wk[8 * j + g], b1 = wk[4 * kTcWRow + 8 * j + g];
+                        mma_tf32(acc[j], l0, l1, l2, l3, b0, b1);
+                        mma_tf32(acc[j], h0, h1, h2, h3, b0, b1);
+                    }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (j >= nt) break;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int n = 8 * j + 2 * q + (e & 1);
+                const int64_t m = e < 2 ? mA : mB;
+                if (n < cout && m < M) {
+                    const float v = acc[j][e] + bf(w, S.boff[l] + n);
+                    z[m * cout + n] = v;
+                    if (a) a[m * cout + n] = fmaxf(v, 0.f);
+                }
+            }
+        }
+    }
+}
+
+// Input gradient of a hidden layer l >= 1 (cin = cout = 32):
+// din[m][ci] = relu'(zin[m][ci]) sum_t sum_co w[t][ci][co] dz[m - off_t][co],
+// where the position m - off_t is the one whose tap t reads m.
+__global__ void __launch_bounds__(256) k_tc_dgrad(const __nv_bfloat16* __restrict__ w, NetShape S,
+                                                  int l, int H, int W, int B,
+                                                  const float* __restrict__ dz,
+                                                  const float* __restrict__ zin,
+                                                  float* __restrict__ din) {
+    extern __shared__ uint32_t tsm[];
+    const int HW = H * W, halo = W + 1;
+    const int64_t M = (int64_t)B * HW;
+    uint32_t* s_w = tsm;                      // [k = t*32 + co][n = ci]
+    uint32_t* s_dz = s_w + 5 * kC * kTcWRow;  // rows m0 .. m0 + tile + halo
+    const uint32_t* zrow = s_dz + (size_t)(halo + kTcTile) * kTcRow;
+    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5, g = lane >> 2, q = lane & 3;
+    for (int i = tid; i < 5 * kC * kTcWRow; i += blockDim.x) {
+        const int k = i / kTcWRow, n = i - k * kTcWRow;
+        const int t = k >> 5, co = k & 31;
+        s_w[i] = n < kC ? to_tf32(bf(w, S.woff[l] + (t * kC + n) * kC + co)) : 0u;
+    }
+    for (int i = tid; i < kTcRow; i += blockDim.x) s_dz[(size_t)(halo + kTcTile) * kTcRow + i] = 0u;
+    for (int64_t m0 = (int64_t)blockIdx.x * kTcTile; m0 < M; m0 += (int64_t)gridDim.x * kTcTile) {
+        __syncthreads();
+        for (int i = tid; i < (halo + kTcTile) * kC; i += blockDim.x) {
+            const int r = i >> 5, c = i & 31;
+            const int64_t mm = m0 + r;
+            s_dz[r * kTcRow + c] = mm < M ? __float_as_uint(dz[mm * kC + c]) : 0u;
+        }
+        __syncthreads();
+        const int rA = 16 * wp + g, rB = rA + 8;
+        const int64_t mA = m0 + rA, mB = m0 + rB;
+        const int pA = (int)(mA % HW), pB = (int)(mB % HW);
+        float acc[4][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[j][e] = 0.f;
+#pragma unroll
+        for (int t = 0; t < 5; ++t) {
+            // the position whose tap t reads p: p - off_t, inside the lattice
+            const int dy = tap_dy(S, l, t), dx = tap_dx(t), off = dy * W + dx;
+            const int yA = pA / W, xA = pA - yA * W, yB = pB / W, xB = pB - yB * W;
+            const bool vA = mA < M && yA - dy < H && xA - dx >= 0 && xA - dx < W;
+            const bool vB = mB < M && yB - dy < H && xB - dx >= 0 && xB - dx < W;
+            const uint32_t* ra = vA ? s_dz + (size_t)(rA - off) * kTcRow : zrow;
+            const uint32_t* rb = vB ? s_dz + (size_t)(rB - off) * kTcRow : zrow;
+#pragma unroll
+            for (int cb = 0; cb < 4; ++cb) {
+                uint32_t h0, h1, h2, h3, l0, l1, l2, l3;
+                split_tf32(ra[8 * cb + q], h0, l0);
+                split_tf32(rb[8 * cb + q], h1, l1);
+                split_tf32(ra[8 * cb + q + 4], h2, l2);
+                split_tf32(rb[8 * cb + q + 4], h3, l3);
+                const uint32_t* wk = s_w + (size_t)((t * 4 + cb) * 8 + q) * kTcWRow;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const uint32_t b0 = wk[8 * j + g], b1 = wk[4 * kTcWRow + 8 * j + g];
+                    mma_tf32(acc[j], l0, l1, l2, l3, b0, b1);
+                    mma_tf32(acc[j], h0, h1, h2, h3, b0, b1);
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int n = 8 * j + 2 * q + (e & 1);
+                const int64_t m = e < 2 ? mA : mB;
+                if (m < M) din[m * kC + n] = zin[m * kC + n] > 0.f ? acc[j][e] : 0.f;
+            }
+    }
+}
+
+// Weight and bias gradient partials of layer l >= 1 over one chunk of
+// kTcChunk positions (one block of 10 warps per chunk):
+// part[block][(t*32 + ci)*cout + co] = sum_m [tap t of m inside] in[m + off_t][ci] dz[m][co],
+// then the cout bias sums.  Warp r computes rows (t, ci) = 16 r .. 16 r + 15.
+__global__ void __launch_bounds__(320) k_tc_wgrad(NetShape S, int l, int H, int W, int B,
+                                                  const float* __restrict__ in,
+                                                  const float* __restrict__ dz,
+                                                  float* __restrict__ part) {
+    extern __shared__ uint32_t tsm[];
+    const int cout = S.cout[l], nt = cout == 1 ? 1 : 4;
+    const int HW = H * W, halo = W + 1;
+    const int64_t M = (int64_t)B * HW;
+    const int nw = 5 * kC * cout + cout;
+    const int64_t m0 = (int64_t)blockIdx.x * kTcChunk;
+    uint32_t* s_in = tsm;                                          // [halo + chunk][kTcRow]
+    uint32_t* s_dz = s_in + (size_t)(halo + kTcChunk) * kTcRow;    // [chunk][kTcWRow]
+    unsigned char* s_ok = reinterpret_cast<unsigned char*>(s_dz + (size_t)kTcChunk * kTcWRow);
+    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5, g = lane >> 2, q = lane & 3;
+    for (int i = tid; i < (halo + kTcChunk) * kC; i += blockDim.x) {
+        const int r = i >> 5, c = i & 31;
+        const int64_t mm = m0 - halo + r;
+        s_in[r * kTcRow + c] = (mm >= 0 && mm < M) ? __float_as_uint(in[mm * kC + c]) : 0u;
+    }
+    for (int i = tid; i < kTcChunk * kTcWRow; i += blockDim.x) {
+        const int r = i / kTcWRow, c = i - r * kTcWRow;
+        const int64_t mm = m0 + r;
+        s_dz[i] = (c < cout && mm < M) ? __float_as_uint(dz[mm * cout + c]) : 0u;
+    }
+    for (int r = tid; r < kTcChunk; r += blockDim.x) {
+        const int64_t mm = m0 + r;
+        unsigned char bits = 0;
+        if (mm < M) {
+            const int p = (int)(mm % HW);
+            for (int t = 0; t < 5; ++t) {
+                int off;
+                if (tc_tap(S, l, t, p, W, off)) bits |= (unsigned char)(1u << t);
+            }
+        }
+        s_ok[r] = bits;
+    }
+    __syncthreads();
+    // warp wp: tap t = wp / 2, channels ci0 .. ci0 + 15
+    const int t = wp >> 1, ci0 = (wp & 1) * 16;
+    const int off = tap_dy(S, l, t) * W + tap_dx(t);
+    const unsigned char bit = (unsigned char)(1u << t);
+    float acc[4][4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[j][e] = 0.f;
+    for (int kb = 0; kb < kTcChunk; kb += 8) {
+        // A[row = ci][col = position]: in[m + off][ci] where tap t of m is inside
+        const int c0 = kb + q, c1 = c0 + 4;
+        const bool v0 = (s_ok[c0] & bit) != 0, v1 = (s_ok[c1] & bit) != 0;
+        const uint32_t* r0 = s_in + (size_t)(halo + c0 + off) * kTcRow + ci0;
+        const uint32_t* r1 = s_in + (size_t)(halo + c1 + off) * kTcRow + ci0;
+        uint32_t h0, h1, h2, h3, l0, l1, l2, l3;
+        split_tf32(v0 ? r0[g] : 0u, h0, l0);
+        split_tf32(v0 ? r0[g + 8] : 0u, h1, l1);
+        split_tf32(v1 ? r1[g] : 0u, h2, l2);
+        split_tf32(v1 ? r1[g + 8] : 0u, h3, l3);
+        const uint32_t* bk = s_dz + (size_t)(kb + q) * kTcWRow;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (j < nt) {
+                uint32_t bh0, bl0, bh1, bl1;
+                split_tf32(bk[8 * j + g], bh0, bl0);
+                split_tf32(bk[4 * kTcWRow + 8 * j + g], bh1, bl1);
+                mma_tf32(acc[j], l0, l1, l2, l3, bh0, bh1);
+                mma_tf32(acc[j], h0, h1, h2, h3, bl0, bl1);
+                mma_tf32(acc[j], h0, h1, h2, h3, bh0, bh1);
+            }
+    }
+    float* pb = part + (int64_t)blockIdx.x * nw;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (j >= nt) break;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int ci = ci0 + g + (e < 2 ? 0 : 8);
+            const int co = 8 * j + 2 * q + (e & 1);
+            if (co < cout) pb[(t * kC + ci) * cout + co] = acc[j][e];
+        }
+    }
+    // bias partials: sum of dz over the chunk, in position order
+    for (int co = tid; co < cout; co += blockDim.x) {
+        float sacc = 0.f;
+        for (int r = 0; r < kTcChunk; ++r) {
+            const int64_t mm = m0 + r;
+            if (mm < M) sacc += dz[mm * cout + co];
+        }
+        pb[5 * kC * cout + co] = sacc;
+    }
+}
+
 __global__ void k_sum_parts(const float* __restrict__ part, int nparts, int nw,
                             float* __restrict__ grad) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -916,6 +1212,7 @@ struct isg_learned {
     int64_t adam_t = 0;
     // training buffers (capacity B)
     int cap_B = 0;
+    bool tc_attr = false;     // shared-memory limits of the tensor-core training kernels set
     float* d_act = nullptr;   // [D+1][B][HW][kC]: a_0 = input spins, a_l = layer l-1 output
     float* d_z = nullptr;     // [D][B][HW][kC] pre-activations
     float* d_dz = nullptr;    // [B][HW][kC]
@@ -1029,12 +1326,34 @@ static int forward_backward(isg_learned* h, int B, float* mean_lq) {
     const size_t stride = (size_t)B * HW * kC;
     cudaStream_t st = h->stream;
     k_to_float<<<grid_for((int64_t)B * HW, 256), 256, 0, st>>>(h->d_cfg, h->d_act, (int64_t)B * HW);
+    // layers >= 1 on the tensor cores (rows of up to 256 positions fit the
+    // staged tiles), layer 0 on the CUDA cores
+    const bool tc = h->W <= 256;
+    const int64_t M = (int64_t)B * HW;
+    int sms = 1;
+    ISG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+    const int tc_grid = (int)std::max<int64_t>(1, std::min<int64_t>((M + kTcTile - 1) / kTcTile,
+                                                                   2 * (int64_t)sms));
+    const size_t fsm = tc_fwd_smem(h->W), wsm = tc_wgrad_smem(h->W);
+    if (tc && !h->tc_attr) {
+        ISG_CK(cudaFuncSetAttribute(k_tc_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+        ISG_CK(cudaFuncSetAttribute(k_tc_dgrad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)fsm));
+        ISG_CK(cudaFuncSetAttribute(k_tc_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)wsm));
+        h->tc_attr = true;
+    }
     for (int l = 0; l < h->D; ++l) {
         const bool last = l == h->D - 1;
         const int64_t n = (int64_t)B * HW * h->S.cout[l];
-        k_tf_layer<<<grid_for(n, 256), 256, 0, st>>>(h->d_wbf, h->S, l, h->H, h->W, B,
-                                                      h->d_act + l * stride, h->d_z + l * stride,
-                                                      last ? nullptr : h->d_act + (l + 1) * stride);
+        if (tc && l >= 1)
+            k_tc_fwd<<<tc_grid, 256, fsm, st>>>(h->d_wbf, h->S, l, h->H, h->W, B,
+                                                h->d_act + l * stride, h->d_z + l * stride,
+                                                last ? nullptr : h->d_act + (l + 1) * stride);
+        else
+            k_tf_layer<<<grid_for(n, 256), 256, 0, st>>>(h->d_wbf, h->S, l, h->H, h->W, B,
+                                                          h->d_act + l * stride, h->d_z + l * stride,
+                                                          last ? nullptr : h->d_act + (l + 1) * stride);
     }
     // output gradient (layer D-1 pre-activation = logits)
     k_tf_out_grad<<<B, 256, 0, st>>>(h->d_z + (h->D - 1) * stride, h->d_act, HW, B, h->d_dz,
@@ -1049,24 +1368,36 @@ static int forward_backward(isg_learned* h, int B, float* mean_lq) {
                                                      (size_t)(wg_halo(h->S, l, h->W) + chunk) *
                                                          h->S.cin[l]) +
                                         (size_t)chunk);
+    const int nparts_tc = (int)((M + kTcChunk - 1) / kTcChunk);
     for (int l = h->D - 1; l >= 0; --l) {
         const int nw = h->S.taps[l] * h->S.cin[l] * h->S.cout[l] + h->S.cout[l];
-        if ((int64_t)nparts * nw > h->part_cap) {
+        const bool tcl = tc && l >= 1;
+        const int np = tcl ? nparts_tc : nparts;
+        if ((int64_t)np * nw > h->part_cap) {
             cudaFree(h->d_part);
-            h->part_cap = nparts * nw;
+            h->part_cap = (int64_t)np * nw;
             ISG_CK(cudaMalloc((void**)&h->d_part, sizeof(float) * h->part_cap));
         }
-        if (wg_smem > 48 * 1024)
-            ISG_CK(cudaFuncSetAttribute(k_tf_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)wg_smem));
-        k_tf_wgrad<<<nparts, 256, wg_smem, st>>>(h->S, l, h->H, h->W, B, h->d_act + l * stride, dz,
-                                                 chunk, h->d_part);
-        k_sum_parts<<<(nw + 255) / 256, 256, 0, st>>>(h->d_part, nparts, nw,
+        if (tcl) {
+            k_tc_wgrad<<<np, 320, wsm, st>>>(h->S, l, h->H, h->W, B, h->d_act + l * stride, dz,
+                                             h->d_part);
+        } else {
+            if (wg_smem > 48 * 1024)
+                ISG_CK(cudaFuncSetAttribute(k_tf_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)wg_smem));
+            k_tf_wgrad<<<np, 256, wg_smem, st>>>(h->S, l, h->H, h->W, B, h->d_act + l * stride,
+                                                 dz, chunk, h->d_part);
+        }
+        k_sum_parts<<<(nw + 255) / 256, 256, 0, st>>>(h->d_part, np, nw,
                                                       h->d_grad + h->S.woff[l]);
         if (l > 0) {
             const int64_t n = (int64_t)B * HW * h->S.cin[l];
-            k_tf_dgrad<<<grid_for(n, 256), 256, 0, st>>>(h->d_wbf, h->S, l, h->H, h->W, B, dz,
-                                                          h->d_z + (l - 1) * stride, dn);
+            if (tc && h->S.cout[l] == kC)
+                k_tc_dgrad<<<tc_grid, 256, fsm, st>>>(h->d_wbf, h->S, l, h->H, h->W, B, dz,
+                                                      h->d_z + (l - 1) * stride, dn);
+            else
+                k_tf_dgrad<<<grid_for(n, 256), 256, 0, st>>>(h->d_wbf, h->S, l, h->H, h->W, B, dz,
+                                                              h->d_z + (l - 1) * stride, dn);
             std::swap(dz, dn);
         }
     }

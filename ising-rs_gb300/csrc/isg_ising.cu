@@ -56,7 +56,6 @@ int cuda_fail(cudaError_t e, const char* what) {
 }
 
 constexpr int kMaxClasses = 16;
-constexpr int kMaxThreads = 512;
 constexpr int kMaxReplicas = 1024;
 
 // Task kinds of a lattice size (words of 4 same-colour sites of one colour
@@ -2099,7 +2098,7 @@ static size_t word_smem(const isg_ising* H) {
 static int configure_launch(isg_ising* H) {
     const int thr = H->threads;
     // one launch per half-sweep covers every size: rolling ranges, flat
-    // tasks and one-site tasks (256 per block)
+    // groups and site-block tasks (256 per block)
     const int64_t need = std::max<int64_t>(std::max<int64_t>(H->P.total_ctasks, H->P.flat_ctasks),
                                            (H->P.total_sblocks + 255) / 256);
     const bool in_l2 = H->spin_bytes <= ((int64_t)96 << 20);
@@ -2306,7 +2305,7 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
     H->sizes.assign(sizes, sizes + n_sizes);
 
     IsingParams& P = H->P;
-    int64_t off = 0, task = 0, site = 0, sblk = 0, ctask = 0;
+    int64_t off = 0, task = 0, site = 0, sblk = 0;
     for (int s = 0; s < n_sizes; ++s) {
         IsingClass& C = P.cls[s];
         const int L = sizes[s];
@@ -2372,7 +2371,6 @@ int isg_ising_create(isg_ising** out, const int* sizes, int n_sizes, int replica
     P.n_classes = n_sizes;
     P.dim = dim;
     P.total_tasks = task;
-    (void)ctask;
     layout_rolling(H);
     layout_flat(H);
     P.total_sites = site;

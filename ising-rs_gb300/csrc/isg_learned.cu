@@ -39,7 +39,6 @@ namespace {
 
 constexpr int kC = 32;         // channels
 constexpr int kMaxLayers = 8;
-constexpr int kTaps = 5;       // (-1,-1) (-1,0) (-1,+1) (0,-1) (0,0)
 __host__ __device__ __forceinline__ int tap_dx(int t) { return t < 3 ? t - 1 : (t == 3 ? -1 : 0); }
 constexpr uint32_t kTagLearn = 0x06u;
 

@@ -1091,7 +1091,8 @@ def ncu_case_graph(kind: str):
     of a BCC 8^3 graph (1024 nodes, 20 replicas) with a record every sweep;
     reweight: one WHAM analysis of 20 x 100,000 samples; learned: one chain
     batch (4096 rounded up to whole waves of the sampler) of the untrained 2D
-    L=32 network (sampling, then the flipped scores)."""
+    L=32 network (sampling, then the flipped scores); train: three training
+    steps of that network on 128 seeded configurations."""
     pkg = _load("ising_gb300", ROOT / "ising-rs_gb300" / "__init__.py")
     if kind == "learned":
         import importlib
@@ -1101,6 +1102,20 @@ def ncu_case_graph(kind: str):
         q = lrn.LearnedProposal(32, 32, layers=6, seed=SEED)
         qn = q.batch_quantum()
         q.sample(-(-4096 // qn) * qn, 1)
+        q.sync()
+        print("ncu case done")
+        return 0
+    if kind == "train":
+        # three training steps of the 2D L = 32 network on 128 configurations
+        # (seeded +-1 bytes): the tensor-core forward, input and weight gradients
+        import importlib
+        import torch
+        torch.cuda.set_device(0)
+        lrn = importlib.import_module(pkg.__name__ + ".learned")
+        q = lrn.LearnedProposal(32, 32, layers=6, seed=SEED)
+        g = torch.Generator(device="cuda").manual_seed(SEED)
+        d = (torch.randint(0, 2, (128, 1024), device="cuda", generator=g, dtype=torch.int8) * 2 - 1)
+        q.train(d, batch=128, steps=3, lr=1e-3)
         q.sync()
         print("ncu case done")
         return 0
@@ -1185,20 +1200,21 @@ def main():
     ap.add_argument("--pt-sweeps", type=int, default=200000)
     ap.add_argument("--ncu-case", nargs="?", const="words",
                     choices=["words", "pt", "resident", "graph", "cgraph3", "cgraph2",
-                             "reweight", "learned"],
+                             "reweight", "learned", "train"],
                     help="no timing: 'words' = a few half-sweeps of L=128 x 128 replicas (268 MB, "
                          "larger than L2) for an ncu capture of the half-sweep kernel; "
                          "'pt' = 10 steps of the headline PT workload (launch list, traffic); "
                          "'resident' = one 2000-sweep schedule of an L=30 lattice; "
                          "'graph'/'cgraph3'/'cgraph2' = one 100-sweep launch of the graph "
                          "kernels (BCC 8^3, 20 replicas); 'reweight' = one WHAM analysis; "
-                         "'learned' = 4096 proposals of the L=32 network (sample + score)")
+                         "'learned' = 4096 proposals of the L=32 network (sample + score); "
+                         "'train' = three training steps of that network")
     args = ap.parse_args()
     if args.ncu_case == "resident":
         return ncu_case_resident()
     if args.ncu_case == "pt":
         return ncu_case_pt()
-    if args.ncu_case in ("graph", "cgraph3", "cgraph2", "reweight", "learned"):
+    if args.ncu_case in ("graph", "cgraph3", "cgraph2", "reweight", "learned", "train"):
         return ncu_case_graph(args.ncu_case)
     if args.ncu_case:
         return ncu_case()

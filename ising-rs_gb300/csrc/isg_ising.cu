@@ -2024,14 +2024,22 @@ static void layout_rolling(isg_ising* H) {
 // CTA tasks of the flat sizes: groups of FG consecutive warp tasks of one
 // plane per warp, 8 groups per CTA task.  FG = 1 (the original one-task form)
 // unless some size has rows that are not a power of two words long (its
-// tasks read the x-neighbour word from memory, so several in flight per warp
-// hide the latency): then 4, or 2 next to four-words-per-lane rolling sizes
-// (the groups' registers would cost that kernel more).
+// tasks read the x-neighbour word from memory) or the flat work is large
+// (at least 8192 warp tasks, e.g. 2D L = 256 x 32): several tasks in flight
+// per warp then hide the latency (2D L = 256 x 128: +24%), while a batch of a
+// few small lattices needs every warp it can get (3D L = 8, 16 x 128: -26%
+// with groups).  FG = 4, or 2 next to four-words-per-lane rolling sizes (the
+// groups' registers would cost that kernel more).
 static void layout_flat(isg_ising* H) {
     IsingParams& P = H->P;
     bool gen = false;
-    for (int s = 0; s < H->n_classes; ++s) gen = gen || (P.cls[s].kind == kFlat && P.cls[s].flat_gen);
-    H->flatg = !gen ? 1 : H->wmax == 4 ? 2 : 4;
+    int64_t tasks = 0;
+    for (int s = 0; s < H->n_classes; ++s)
+        if (P.cls[s].kind == kFlat) {
+            gen = gen || P.cls[s].flat_gen;
+            tasks += (int64_t)P.cls[s].tasks_per_plane * P.cls[s].R;
+        }
+    H->flatg = !(gen || tasks >= 8192) ? 1 : H->wmax == 4 ? 2 : 4;
     int64_t fctask = 0;
     for (int s = 0; s < H->n_classes; ++s) {
         IsingClass& C = P.cls[s];

@@ -187,6 +187,29 @@ def test_uneven_sizes_pt_matches_oracle(gpu, oracle):
     b.close()
 
 
+def test_large_flat_batches_group_tasks(gpu, oracle):
+    """A 2D batch of at least 8192 flat warp tasks (L = 256 x 32) runs its flat
+    tasks four per warp (all loads of a group before any decision); replicas
+    across the batch match the oracle bit for bit, and so do the measured
+    bond and magnetisation sums."""
+    L, R, seed = 256, 32, 11
+    temps = grid(2.0, 2.6, R)
+    b = gpu.IsingBatch([L], R, seed=seed, dim=2)
+    b.set_temperatures(temps)
+    b.step(3)
+    bond, mag = b.measure()
+    for r in (0, 17, 31):
+        sp = oracle.hot_start(L, 2, seed, r)
+        thr = oracle.thresholds(2, 1.0 / temps[r])
+        for k in range(3):
+            for c in (0, 1):
+                oracle.halfsweep(sp, L, 2, c, seed, r, k, thr)
+        assert np.array_equal(b.get_spins(0, r), sp), r
+        ob, om = oracle.measure(sp, L, 2)
+        assert bond[r] == ob and mag[r] == om, r
+    b.close()
+
+
 def test_exchange_api_matches_oracle(gpu, oracle):
     sizes, R, seed = [8, 16], 6, 7
     temps = grid(4.0, 5.0, R)

@@ -187,6 +187,28 @@ def test_uneven_sizes_pt_matches_oracle(gpu, oracle):
     b.close()
 
 
+def test_largest_sizes_match_oracle(gpu, oracle):
+    """The largest lattices: 3D L = 512 (134M sites, flat word tasks with rows of
+    64 words) and 2D L = 1024 (rows of 128 words), bit for bit against the
+    oracle through sweeps and the measured sums."""
+    for dim, L, R, n_sw, T in ((3, 512, 1, 1, 4.5), (2, 1024, 2, 2, 2.3)):
+        seed = 5
+        b = gpu.IsingBatch([L], R, seed=seed, dim=dim)
+        b.set_temperatures([T] * R)
+        b.step(n_sw)
+        bond, mag = b.measure()
+        thr = oracle.thresholds(dim, 1.0 / T)
+        for r in range(R):
+            sp = oracle.hot_start(L, dim, seed, r)
+            for k in range(n_sw):
+                for c in (0, 1):
+                    oracle.halfsweep(sp, L, dim, c, seed, r, k, thr)
+            assert np.array_equal(b.get_spins(0, r), sp), (dim, L, r)
+            ob, om = oracle.measure(sp, L, dim)
+            assert bond[r] == ob and mag[r] == om, (dim, L, r)
+        b.close()
+
+
 def test_large_flat_batches_group_tasks(gpu, oracle):
     """A 2D batch of at least 8192 flat warp tasks (L = 256 x 32) runs its flat
     tasks four per warp (all loads of a group before any decision); replicas

@@ -318,7 +318,7 @@ def hbm_case(pkg, stream, flush, steps, peak, peak_kind):
     value = sites * SWEEPS_PER_STEP * steps / (dev_ms * 1e6)
     launch_ms = b.time_halfsweep_graph(2 * SWEEPS_PER_STEP, 256 << 20, 5)
     roof = _roofline(b, launch_ms, peak, peak_kind, ncu_traffic(HBM_PROFILE),
-                     "k_ising_words<3,0,3,4,2> (one half-sweep of 128 L=128 lattices; four words per lane through the shared-memory ring)",
+                     "k_ising_words<3,0,3,4,2,1> (one half-sweep of 128 L=128 lattices; four words per lane through the shared-memory ring)",
                      f"HBM: {R * 128 ** 3 / 2 ** 20:.0f} MiB of spins, twice the L2; "
                      f"graph of {2 * SWEEPS_PER_STEP} half-sweeps, L2 flushed before each replay")
     b.close()
@@ -498,7 +498,7 @@ def run_gpu(args):
     peak, peak_kind = measured_peaks()
     launch_ms = b.time_halfsweep_graph(2 * SWEEPS_PER_STEP, 256 << 20, 5)
     roof = _roofline(b, launch_ms, peak, peak_kind, ncu_traffic(HEADLINE_PROFILE),
-                     "k_ising_words<3,0,3,4,2> (one half-sweep, all 160 lattices)",
+                     "k_ising_words<3,0,3,4,2,1> (one half-sweep, all 160 lattices)",
                      "L2: the 73 MiB batch fits in L2, which is flushed once per 20 "
                      "half-sweeps (before every step), so most launches read L2; the HBM "
                      "figure is roofline_hbm")

@@ -361,7 +361,8 @@ def uneven_case(pkg, stream, flush, steps):
 def ess_case(pkg, stream, sweeps_per_s):
     """ESS/s of |M| on the headline batch from a run of its own: ESS_WARMUP
     warm-up sweeps, then ESS_SWEEPS sweeps with a record every 5 (at L = 128
-    near Tc, tau_int is about 1400 sweeps, so the run covers >= 50 tau).  tau is the
+    near Tc, tau_int has come out between about 800 and 1700 sweeps, so the
+    run covers 60-125 tau).  tau is the
     larger of the windowed estimate (reproduce_validation.py:157-163) and the
     20-block estimate, per size at the slot nearest Tc.  ESS/s follows the
     spec definition: sweeps/s of the timed batch / tau_int(|M|) in sweeps,
